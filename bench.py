@@ -1,0 +1,338 @@
+"""Benchmark of the coupled SPH + wave step on GB300.
+
+Metric: particle + wave-cell updates per second (one update = one particle
+or one wave cell advanced one step).  Workload: the 1,048,576-particle
+dam-break (128^3 lattice, s = 0.0075, h = 2s, 67^3 grid cells) coupled to a
+1024^2 height field, float32 with compensated neighbour sums, synthetic
+seeded inputs.  Each timed step is one full cwa_step (grid sort -> rho_pres
+-> force -> integrate + coupling -> wave) with the state resident in HBM;
+L2 is flushed (256 MiB write on the sim's stream) before every step, outside
+the per-step CUDA events.
+
+`e2e` runs the same steps through the public C ABI with host buffers: each
+step uploads the particle records and both wave fields from pinned host
+memory, steps, and downloads the particle records and u^n.
+
+N > 1 (torchrun): every rank runs an independent replica (the single-scene
+step does not shard); value = all ranks' updates / the slowest rank's time.
+
+`--impl reference` times the reference algorithm on the host cores instead:
+the reference's GLSL cannot run here (no graphics stack), so its CPU
+restatement (oracle/, FP64, OpenMP over all host threads) runs on the same
+workload, a bounded number of steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle+wave-cell updates/s on 1 GB300, batched vs plain, % of HBM roofline"
+UNIT = "updates/s"
+# Algorithmic bytes per unit of work (one particle or grid/wave cell per step).
+BYTES_PER_PARTICLE = {"grid": 20 + 140, "rho_pres": 24, "force": 64, "integrate": 100}
+BYTES_PER_GRID_CELL = {"grid": 28}
+BYTES_PER_WAVE_CELL = {"wave": 20}
+FALLBACK_HBM_GBS = 6800.0
+
+
+def _peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def _profiled_traffic() -> dict:
+    """Per-launch DRAM bytes per pass from the committed ncu summaries."""
+    out = {}
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for m in re.finditer(r"^traffic_per_launch\s+(\w+)\s+(\d+)\s*$", f.read_text(), re.M):
+            out[m.group(1)] = int(m.group(2))
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"cwa_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self) -> dict:
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(k)
+        self.path.unlink(missing_ok=True)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _cpu_leg(workload, max_seconds: float, min_steps: int = 1):
+    """Time the oracle (FP64 CPU restatement) on the workload's first scene."""
+    from oracle import oracle as orc
+    sc = workload.scenes[0]
+    d = sc.desc
+    p16 = orc.to_f64(sc.particles.view(np.float32).reshape(-1, 16))
+    un = sc.wave.astype(np.float64)
+    unm1 = un.copy()
+    orc.step(d, p16, un, unm1, 1)  # warm-up (page-in, thread pool)
+    steps, t0 = 0, time.perf_counter()
+    while steps < min_steps or (time.perf_counter() - t0) < max_seconds * 0.5:
+        orc.step(d, p16, un, unm1, 1)
+        steps += 1
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    dt = time.perf_counter() - t0
+    units = (d.n_particles + d.wave_nx * d.wave_nz) * steps
+    return units / dt, steps, dt, orc.threads()
+
+
+def run_reference(args) -> None:
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    from coupledwateranimation_gb300 import scenes
+    wl = scenes.CONFIGS[args.config]()
+    budget = float(os.environ.get("CWA_REF_SECONDS", "120"))
+    value, steps, secs, cores = _cpu_leg(wl, budget, min_steps=1)
+    d = wl.scenes[0].desc
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded dam-break + Gaussian bumps)",
+        "config": {"workload": wl.name, "particles": d.n_particles, "wave": f"{d.wave_nx}x{d.wave_nz}"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{steps} full steps of the workload ({secs:.1f} s) on the FP64 "
+                                   f"OpenMP restatement of the reference shaders; the GLSL itself "
+                                   f"cannot run (no graphics stack)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args) -> None:
+    import torch
+    import torch.distributed as dist
+
+    import coupledwateranimation_gb300 as cwa
+    from coupledwateranimation_gb300 import PARTICLE_DTYPE, Sim, scenes
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    wl = scenes.CONFIGS[args.config]()
+    sims = []
+    sim = Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local)
+    for k, s in enumerate(wl.scenes):
+        sim.upload_particles(k, s.particles)
+        sim.upload_wave(k, s.wave, s.wave)
+    view = sim.device_view(0)
+    stream = torch.cuda.ExternalStream(view.stream, device=torch.device("cuda", local))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    n_units = wl.n_particles + wl.n_wave_cells
+
+    # warm-up (graph capture happens here)
+    sim.step(args.warmup)
+    sim.synchronize()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = sim.launch_count
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.fill_(k & 0xFF)
+                starts[k].record(stream)
+                sim.step(1)
+                ends[k].record(stream)
+        torch.cuda.synchronize()
+    launches = sim.launch_count - l0
+    sim.synchronize()
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    if ws > 1:
+        t = torch.tensor([ms], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = n_units * ws * args.steps / (ms * 1e-3)
+
+    # per-pass profile (CUDA events on the sim's stream, eager launches)
+    sim.set_profiling(True)
+    acc = {p: 0.0 for p in cwa.PASSES}
+    prof_steps = max(3, min(args.steps, 10))
+    with torch.cuda.stream(stream):
+        for k in range(prof_steps):
+            flush.fill_(k & 0xFF)
+            sim.step(1)
+            for p, v in sim.pass_times().items():
+                acc[p] += v
+    sim.set_profiling(False)
+    pass_ms = {p: v / prof_steps for p, v in acc.items()}
+    top = max(pass_ms, key=pass_ms.get)
+    n_p, n_c, n_w = wl.n_particles, sum(int(np.prod(sim.grid_dims(k))) for k in range(len(wl.scenes))), \
+        wl.n_wave_cells
+    alg = {p: BYTES_PER_PARTICLE.get(p, 0) * n_p + BYTES_PER_GRID_CELL.get(p, 0) * n_c
+           + BYTES_PER_WAVE_CELL.get(p, 0) * n_w for p in cwa.PASSES}
+    peak, peak_kind = _peaks()
+    achieved = alg[top] / (pass_ms[top] * 1e-3) / 1e9
+    traffic = _profiled_traffic().get(top)
+
+    # end-to-end through the C ABI with pinned host buffers
+    e2e_steps = max(3, min(args.steps, 10))
+    pin = []
+    for s in wl.scenes:
+        hp = torch.empty(s.desc.n_particles * 64, dtype=torch.uint8, pin_memory=True)
+        hp.numpy()[:] = s.particles.view(np.uint8)
+        hu = torch.empty((s.desc.wave_nz, s.desc.wave_nx), dtype=torch.float32, pin_memory=True)
+        hu.numpy()[:] = s.wave
+        hu2 = hu.clone().pin_memory()
+        pin.append((hp, hu, hu2))
+    h2d = sum(hp.numel() + hu.numel() * 8 for hp, hu, _ in pin)
+    d2h = sum(hp.numel() + hu.numel() * 4 for hp, hu, _ in pin)
+    lib = cwa.load()
+    import ctypes as C
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for k, (hp, hu, hu2) in enumerate(pin):
+            cwa._abi.check(lib.cwa_upload_particles(sim.handle, k, C.c_void_p(hp.data_ptr()),
+                                                    wl.scenes[k].desc.n_particles), "upload")
+            cwa._abi.check(lib.cwa_upload_wave(sim.handle, k, C.c_void_p(hu.data_ptr()),
+                                               C.c_void_p(hu2.data_ptr()), hu.shape[1], hu.shape[0]),
+                           "upload_wave")
+        sim.step(1)
+        for k, (hp, hu, hu2) in enumerate(pin):
+            cwa._abi.check(lib.cwa_download_particles(sim.handle, k, C.c_void_p(hp.data_ptr()),
+                                                      wl.scenes[k].desc.n_particles), "download")
+            cwa._abi.check(lib.cwa_download_wave(sim.handle, k, C.c_void_p(hu.data_ptr()), None,
+                                                 hu.shape[1], hu.shape[0]), "download_wave")
+    e2e_s = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = n_units * ws * e2e_steps / e2e_s
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        v, steps, secs, cores = _cpu_leg(wl, float(os.environ.get("CWA_CPU_SECONDS", "20")))
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{steps} full step(s) of the same workload ({secs:.1f} s), FP64 OpenMP "
+                         f"restatement of the reference shaders (oracle/)"}
+    sim.close()
+    del sims
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded dam-break + Gaussian bumps)",
+            "config": {"workload": wl.name, "particles": wl.n_particles, "wave_cells": wl.n_wave_cells,
+                       "grid_cells": n_c, "precision": ["fp32", "fp32-compensated", "fp64"][args.precision],
+                       "l2": "flushed before every step (256 MiB write, outside the step events)",
+                       "parallelism": f"replicas x{ws}"},
+            "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": alg[top],
+                         "ms_per_launch": pass_ms[top]},
+            "pass_ms": pass_ms,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": e2e_steps},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2])
+    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

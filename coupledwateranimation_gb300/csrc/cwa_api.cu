@@ -1,0 +1,910 @@
+// cwa_api.cu — the C ABI (include/cwa.h): simulation lifecycle, the pass
+// sequence of one step, CUDA-graph replay, host<->device transfer,
+// checkpoints and the stand-alone scan / grid operators.
+//
+// Pass sequence of a step (CoupledWaterAnimation/Main.cpp:549-560 plus the
+// grid sort): grid -> rho_pres -> force -> integrate -> wave.  All scenes of
+// a sim are concatenated: particles, grid cells and wave cells of scene s
+// occupy [poff, poff+n), [coff, coff+ncells), [woff, woff+nx*nz) of shared
+// arrays, so each pass is one launch over every scene, fed by a table of
+// per-scene tiles.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "cwa_internal.h"
+
+namespace cwa {
+namespace {
+thread_local std::string g_error;
+}
+void set_error(const std::string& msg) { g_error = msg; }
+}  // namespace cwa
+
+using namespace cwa;
+
+struct cwa_sim {
+  int device = 0;
+  cwa_sim_options opt{};
+  cudaStream_t stream = nullptr;
+  std::vector<cwa_scene_desc> desc;
+  std::vector<SceneDev> sd;
+  SceneDev* d_scenes = nullptr;
+  int32_t n_total = 0, c_total = 0, w_total = 0, n_max = 0;
+  bool move_force = false;
+  // particle state, cell-sorted; P/V/ID (and F when the reference torque
+  // needs last step's force) ping-pong through the reorder.
+  float4* P[2] = {nullptr, nullptr};
+  float4* V[2] = {nullptr, nullptr};
+  float4* F[2] = {nullptr, nullptr};
+  float2* RP = nullptr;  // (rho, pressure)
+  float2* EX = nullptr;  // extras.zw, indexed by upload id
+  int32_t* ID[2] = {nullptr, nullptr};
+  int cur = 0;
+  // grid
+  int32_t* key = nullptr;
+  int32_t* slot = nullptr;
+  int32_t* list = nullptr;
+  int32_t* count = nullptr;
+  int32_t* start = nullptr;
+  void* scan_ws = nullptr;
+  ScanWorkspace scan{};
+  // wave: U[wcur] = u^n, U[(wcur+2)%3] = u^(n-1), U[(wcur+1)%3] = next
+  float* U[3] = {nullptr, nullptr, nullptr};
+  int wcur = 0;
+  unsigned long long* D = nullptr;
+  // work tiles
+  Tile* d_ptiles = nullptr;
+  int32_t n_ptiles = 0, ptile = 128;
+  Tile* d_wtiles = nullptr;
+  int32_t n_wtiles = 0, wtile = 256;
+  // staging / status / totals
+  cwa_particle* staging = nullptr;
+  int32_t* d_status = nullptr;
+  int32_t* h_status = nullptr;
+  double* d_totals = nullptr;
+  double* h_totals = nullptr;
+  int64_t steps = 0;
+  int64_t launches = 0;
+  bool grid_fresh = false;
+  bool profiling = false;
+  bool pass_times_valid = false;
+  cudaEvent_t ev[CWA_PASS_COUNT + 1] = {};
+  cudaGraphExec_t graph[6] = {};
+  std::vector<void*> dev_allocs;
+};
+
+namespace {
+
+#define CWA_CUDA(expr)                                                        \
+  do {                                                                        \
+    cudaError_t e_ = (expr);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      set_error(std::string(#expr) + ": " + cudaGetErrorString(e_));          \
+      return e_ == cudaErrorMemoryAllocation ? CWA_ERR_OOM : CWA_ERR_CUDA;    \
+    }                                                                         \
+  } while (0)
+
+#define CWA_TRY(expr)                  \
+  do {                                 \
+    cwa_status s_ = (expr);            \
+    if (s_ != CWA_OK) return s_;       \
+  } while (0)
+
+cwa_status arg_error(const std::string& msg) {
+  set_error(msg);
+  return CWA_ERR_INVALID_ARG;
+}
+
+constexpr int kMaxScenes = 1 << 20;
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kShaderPi = 3.141592741;  // PI #define of the reference shaders
+
+template <class T>
+cwa_status dev_alloc(cwa_sim* s, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    *p = nullptr;
+    return CWA_ERR_OOM;
+  }
+  s->dev_allocs.push_back(*p);
+  e = cudaMemset(*p, 0, count * sizeof(T));
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaMemset: ") + cudaGetErrorString(e));
+    return CWA_ERR_CUDA;
+  }
+  return CWA_OK;
+}
+
+cwa_status validate_scene(const cwa_scene_desc& d, int idx) {
+  auto bad = [&](const char* what) {
+    char buf[160];
+    snprintf(buf, sizeof(buf), "scene %d: %s", idx, what);
+    return arg_error(buf);
+  };
+  if (d.preset != CWA_PRESET_REFERENCE_3D && d.preset != CWA_PRESET_MULLER) return bad("unknown preset");
+  if (d.n_particles < 0) return bad("n_particles < 0");
+  if (d.wave_nx < 1 || d.wave_nz < 1) return bad("wave grid must be at least 1x1");
+  if ((int64_t)d.wave_nx * d.wave_nz > (1ll << 28)) return bad("wave grid above 2^28 cells");
+  if (!(d.smoothing_length > 0.0f) || !(d.cell_size >= d.smoothing_length))
+    return bad("need 0 < smoothing_length <= cell_size");
+  if (!(d.mass > 0.0f) || !(d.rest_rho > 0.0f) || !(d.dt > 0.0f)) return bad("mass, rest_rho, dt must be > 0");
+  for (int a = 0; a < 3; ++a)
+    if (!(d.box_hi[a] > d.box_lo[a])) return bad("box_hi must exceed box_lo");
+  if (d.deposit_shift < 0 || d.deposit_shift > 62) return bad("deposit_shift outside [0, 62]");
+  if (d.flags != 0) return bad("flags must be 0");
+  if (d.preset == CWA_PRESET_REFERENCE_3D && !(d.gas_const * d.particle_radius != 0.0f))
+    return bad("reference preset needs gas_const * particle_radius != 0");
+  return CWA_OK;
+}
+
+SceneDev make_scene_dev(const cwa_scene_desc& d, const int32_t dims[3], int32_t poff, int32_t coff,
+                        int32_t woff) {
+  SceneDev s;
+  memset(&s, 0, sizeof(s));
+  const bool ref = d.preset == CWA_PRESET_REFERENCE_3D;
+  s.poff = poff;
+  s.n = d.n_particles;
+  s.coff = coff;
+  s.ncells = dims[0] * dims[1] * dims[2];
+  for (int a = 0; a < 3; ++a) {
+    s.dims[a] = dims[a];
+    s.lo[a] = d.box_lo[a];
+    s.hi[a] = d.box_hi[a];
+    s.g[a] = d.gravity[a];
+  }
+  s.cell = d.cell_size;
+  s.preset = d.preset;
+  s.h = d.smoothing_length;
+  s.h2 = d.smoothing_length * d.smoothing_length;
+  s.mass = d.mass;
+  s.visc = d.visc;
+  s.rho0 = d.rest_rho;
+  s.k = d.gas_const;
+  s.dt = d.dt;
+  s.e_wall = d.wall_restitution;
+  s.damp = 1.0f - d.velocity_damping * d.dt;
+  s.radius = d.particle_radius;
+  s.crest = d.crest_height;
+  s.foam = d.foam_speed;
+  const double pi = ref ? kShaderPi : kPi;
+  const double h = d.smoothing_length;
+  s.c_poly6_d = (double)d.mass * 315.0 / (64.0 * pi * pow(h, 9));
+  s.k_grad_d = (ref ? 20.0 : 45.0) / (pi * pow(h, 6));
+  s.c_poly6 = (float)s.c_poly6_d;
+  s.k_grad = (float)s.k_grad_d;
+  s.inv_kr = ref ? (float)(1.0 / ((double)d.gas_const * d.particle_radius)) : 0.0f;
+  s.woff = woff;
+  s.nx = d.wave_nx;
+  s.nz = d.wave_nz;
+  s.lam = d.wave_lambda;
+  s.atten = d.wave_atten;
+  s.wa = (float)(2.0 - 4.0 * (double)d.wave_lambda - (double)d.wave_beta);
+  s.wb = (float)(1.0 - (double)d.wave_beta);
+  s.mode = d.wave_mode;
+  s.uvs[0] = d.wave_uv_scale[0];
+  s.uvs[1] = d.wave_uv_scale[1];
+  s.uvo[0] = d.wave_uv_offset[0];
+  s.uvo[1] = d.wave_uv_offset[1];
+  s.y0 = d.surface_y0;
+  s.e_surf = d.surface_restitution;
+  s.gain = d.couple_gain;
+  s.shift = d.deposit_shift;
+  s.qscale = ldexpf(1.0f, d.deposit_shift);
+  s.dq = ldexpf(1.0f, -d.deposit_shift);
+  s.line_source = (d.wave_mode > 0.0f && d.wave_mode < 1.0f) ? 1 : 0;
+  s.coupled = d.preset == CWA_PRESET_MULLER ? 1 : 0;
+  return s;
+}
+
+cwa_status check_sim(cwa_sim* s) {
+  if (!s) return arg_error("null sim");
+  CWA_CUDA(cudaSetDevice(s->device));
+  return CWA_OK;
+}
+
+cwa_status check_scene(cwa_sim* s, int32_t scene) {
+  CWA_TRY(check_sim(s));
+  if (scene < 0 || scene >= (int32_t)s->desc.size()) return arg_error("scene index out of range");
+  return CWA_OK;
+}
+
+float4* cur_force(cwa_sim* s) { return s->move_force ? s->F[s->cur] : s->F[0]; }
+
+// ---- passes (enqueue only) ----
+cwa_status run_grid(cwa_sim* s) {
+  cudaStream_t st = s->stream;
+  const int nxt = s->cur ^ 1;
+  CWA_CUDA(launch_hash_count(s->P[s->cur], s->d_ptiles, s->n_ptiles, s->ptile, s->d_scenes, s->key, s->slot,
+                             s->count, s->d_status, st));
+  s->launches += s->n_ptiles > 0;
+  CWA_CUDA(scan_launch(s->count, s->start, s->c_total, s->c_total + 1, true, s->scan, s->d_status, st,
+                       &s->launches));
+  CWA_CUDA(launch_list_insert(s->key, s->slot, s->start, s->list, s->n_total, st));
+  CWA_CUDA(launch_rank_reorder(s->key, s->slot, s->start, s->list, s->P[s->cur], s->V[s->cur],
+                               s->move_force ? s->F[s->cur] : nullptr, s->ID[s->cur], s->P[nxt], s->V[nxt],
+                               s->move_force ? s->F[nxt] : nullptr, s->ID[nxt], s->n_total, s->d_status, st));
+  s->launches += s->n_total > 0 ? 2 : 0;
+  s->cur = nxt;
+  s->grid_fresh = true;
+  return CWA_OK;
+}
+
+cwa_status run_rho_pres(cwa_sim* s) {
+  CWA_CUDA(launch_rho_pres(s->opt.precision, s->P[s->cur], s->start, s->d_ptiles, s->n_ptiles, s->ptile,
+                           s->d_scenes, s->U[s->wcur], s->RP, s->stream));
+  s->launches += s->n_ptiles > 0;
+  return CWA_OK;
+}
+
+cwa_status run_force(cwa_sim* s) {
+  CWA_CUDA(launch_force(s->opt.precision, s->P[s->cur], s->V[s->cur], s->RP, s->start, s->d_ptiles,
+                        s->n_ptiles, s->ptile, s->d_scenes, s->U[s->wcur], cur_force(s), s->stream));
+  s->launches += s->n_ptiles > 0;
+  return CWA_OK;
+}
+
+cwa_status run_integrate(cwa_sim* s) {
+  CWA_CUDA(launch_integrate(s->P[s->cur], s->V[s->cur], cur_force(s), s->RP, s->d_ptiles, s->n_ptiles,
+                            s->ptile, s->d_scenes, s->U[s->wcur], s->D, s->stream));
+  s->launches += s->n_ptiles > 0;
+  s->grid_fresh = false;
+  return CWA_OK;
+}
+
+cwa_status run_wave(cwa_sim* s) {
+  const int w = s->wcur;
+  CWA_CUDA(launch_wave(s->U[w], s->U[(w + 2) % 3], s->U[(w + 1) % 3], s->D, s->d_wtiles, s->n_wtiles, s->wtile,
+                       s->d_scenes, s->stream));
+  s->launches += 1;
+  s->wcur = (w + 1) % 3;  // StencilImage2DTripleBuffered::PingPong (:33-40)
+  s->steps += 1;
+  return CWA_OK;
+}
+
+cwa_status record(cwa_sim* s, int idx) {
+  if (s->profiling) CWA_CUDA(cudaEventRecord(s->ev[idx], s->stream));
+  return CWA_OK;
+}
+
+cwa_status enqueue_step(cwa_sim* s) {
+  CWA_TRY(record(s, 0));
+  CWA_TRY(run_grid(s));
+  CWA_TRY(record(s, 1));
+  CWA_TRY(run_rho_pres(s));
+  CWA_TRY(record(s, 2));
+  CWA_TRY(run_force(s));
+  CWA_TRY(record(s, 3));
+  CWA_TRY(run_integrate(s));
+  CWA_TRY(record(s, 4));
+  CWA_TRY(run_wave(s));
+  CWA_TRY(record(s, 5));
+  if (s->profiling) s->pass_times_valid = true;
+  return CWA_OK;
+}
+
+// Capture one step for the current (cur, wcur) phase; the host-side state
+// the capture advanced is rolled back, the graph launch advances it again.
+cwa_status graph_step(cwa_sim* s) {
+  const int phase = s->cur * 3 + s->wcur;
+  const int cur0 = s->cur, w0 = s->wcur;
+  const int64_t steps0 = s->steps, launches0 = s->launches;
+  if (!s->graph[phase]) {
+    cudaGraph_t g = nullptr;
+    CWA_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    cwa_status st = enqueue_step(s);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    s->cur = cur0;
+    s->wcur = w0;
+    s->steps = steps0;
+    s->launches = launches0;
+    if (st != CWA_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    CWA_CUDA(e);
+    e = cudaGraphInstantiate(&s->graph[phase], g, 0);
+    cudaGraphDestroy(g);
+    CWA_CUDA(e);
+  }
+  // The launch-count and state bookkeeping of one step, as enqueue_step does.
+  const int64_t before = s->launches;
+  CWA_CUDA(cudaGraphLaunch(s->graph[phase], s->stream));
+  s->launches = before + (s->n_ptiles > 0 ? 6 : 0) + 1 + 1;  // hash,list,reorder,rho,force,integrate + scan + wave
+  s->cur ^= 1;
+  s->wcur = (s->wcur + 1) % 3;
+  s->steps += 1;
+  s->grid_fresh = false;
+  return CWA_OK;
+}
+
+cwa_status read_status(cwa_sim* s) {
+  CWA_CUDA(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  const int32_t v = *s->h_status;
+  if (v == 0) return CWA_OK;
+  CWA_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(int32_t), s->stream));
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  if (v & kStatusTimeout) {
+    set_error("a bounded device wait (scan look-back) timed out");
+    return CWA_ERR_TIMEOUT;
+  }
+  if (v & kStatusNonFinite) {
+    set_error("non-finite particle position");
+    return CWA_ERR_NONFINITE;
+  }
+  set_error("a grid cell held more than 1024 particles; its insert order fell back to arrival order");
+  return CWA_ERR_CAPACITY;
+}
+
+void free_sim(cwa_sim* s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (auto& g : s->graph)
+    if (g) cudaGraphExecDestroy(g);
+  for (auto& e : s->ev)
+    if (e) cudaEventDestroy(e);
+  for (void* p : s->dev_allocs) cudaFree(p);
+  if (s->h_status) cudaFreeHost(s->h_status);
+  if (s->h_totals) cudaFreeHost(s->h_totals);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cwa_status_str(cwa_status s) {
+  switch (s) {
+    case CWA_OK: return "ok";
+    case CWA_ERR_INVALID_ARG: return "invalid argument";
+    case CWA_ERR_OOM: return "out of memory";
+    case CWA_ERR_CUDA: return "CUDA error";
+    case CWA_ERR_TIMEOUT: return "device wait timed out";
+    case CWA_ERR_NONFINITE: return "non-finite value";
+    case CWA_ERR_IO: return "I/O error";
+    case CWA_ERR_NO_DEVICE: return "no CUDA device";
+    case CWA_ERR_CAPACITY: return "capacity exceeded";
+  }
+  return "unknown status";
+}
+
+int32_t cwa_abi_version(void) { return CWA_ABI_VERSION; }
+
+const char* cwa_last_error(void) { return g_error.c_str(); }
+
+cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, int32_t n_scenes,
+                      cwa_sim** out) {
+  if (!out) return arg_error("null output pointer");
+  *out = nullptr;
+  if (!scenes || n_scenes < 1 || n_scenes > kMaxScenes) return arg_error("need 1 <= n_scenes <= 2^20");
+  cwa_sim_options o{};
+  o.precision = CWA_PREC_COMPENSATED;
+  o.use_graph = 1;
+  if (opt) o = *opt;
+  if (o.precision < CWA_PREC_FP32 || o.precision > CWA_PREC_FP64) return arg_error("unknown precision");
+  if (o.nb_threads != 0 && (o.nb_threads < 32 || o.nb_threads > 128 || (o.nb_threads & 31)))
+    return arg_error("nb_threads must be 0 or a multiple of 32 in [32, 128]");
+  std::vector<int32_t> dims(3 * (size_t)n_scenes);
+  int64_t np = 0, nc = 0, nw = 0;
+  int32_t nmax = 0;
+  for (int i = 0; i < n_scenes; ++i) {
+    CWA_TRY(validate_scene(scenes[i], i));
+    cwa_status st = cwa_grid_dims(&scenes[i], &dims[3 * (size_t)i]);
+    if (st != CWA_OK) return st == CWA_ERR_CAPACITY ? st : arg_error("bad grid dimensions");
+    np += scenes[i].n_particles;
+    nc += (int64_t)dims[3 * i] * dims[3 * i + 1] * dims[3 * i + 2];
+    nw += (int64_t)scenes[i].wave_nx * scenes[i].wave_nz;
+    if (scenes[i].n_particles > nmax) nmax = scenes[i].n_particles;
+  }
+  const int64_t lim = (1ll << 31) - (1ll << 20);
+  if (np > lim || nc > lim || nw > lim) {
+    set_error("total particles, grid cells or wave cells above 2^31 - 2^20");
+    return CWA_ERR_CAPACITY;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    set_error("no CUDA device");
+    return CWA_ERR_NO_DEVICE;
+  }
+  if (o.device < 0 || o.device >= ndev) return arg_error("device ordinal out of range");
+
+  cwa_sim* s = new cwa_sim();
+  s->device = o.device;
+  s->opt = o;
+  s->desc.assign(scenes, scenes + n_scenes);
+  s->n_total = (int32_t)np;
+  s->c_total = (int32_t)nc;
+  s->w_total = (int32_t)nw;
+  s->n_max = nmax;
+  s->ptile = o.nb_threads ? o.nb_threads : 128;
+  auto fail = [&](cwa_status st) {
+    free_sim(s);
+    return st;
+  };
+  if (cudaSetDevice(s->device) != cudaSuccess) return fail(CWA_ERR_CUDA);
+
+  std::vector<Tile> ptiles, wtiles;
+  int32_t poff = 0, coff = 0, woff = 0;
+  for (int i = 0; i < n_scenes; ++i) {
+    const cwa_scene_desc& d = scenes[i];
+    s->sd.push_back(make_scene_dev(d, &dims[3 * (size_t)i], poff, coff, woff));
+    if (d.preset == CWA_PRESET_REFERENCE_3D) s->move_force = true;
+    for (int32_t b = 0; b < d.n_particles; b += s->ptile)
+      ptiles.push_back(Tile{i, poff + b, poff + std::min(b + s->ptile, d.n_particles)});
+    const int32_t cells = d.wave_nx * d.wave_nz;
+    for (int32_t b = 0; b < cells; b += s->wtile)
+      wtiles.push_back(Tile{i, woff + b, woff + std::min(b + s->wtile, cells)});
+    poff += d.n_particles;
+    coff += s->sd.back().ncells;
+    woff += cells;
+  }
+  s->n_ptiles = (int32_t)ptiles.size();
+  s->n_wtiles = (int32_t)wtiles.size();
+
+  cwa_status st = CWA_OK;
+  const size_t N = (size_t)s->n_total;
+#define ALLOC(ptr, cnt)                               \
+  do {                                                \
+    st = dev_alloc(s, &(ptr), (cnt));                 \
+    if (st != CWA_OK) return fail(st);                \
+  } while (0)
+  for (int b = 0; b < 2; ++b) {
+    ALLOC(s->P[b], N);
+    ALLOC(s->V[b], N);
+    ALLOC(s->ID[b], N);
+  }
+  ALLOC(s->F[0], N);
+  if (s->move_force) ALLOC(s->F[1], N);
+  ALLOC(s->RP, N);
+  ALLOC(s->EX, N);
+  ALLOC(s->key, N);
+  ALLOC(s->slot, N);
+  ALLOC(s->list, N);
+  ALLOC(s->count, (size_t)s->c_total);
+  ALLOC(s->start, (size_t)s->c_total + 1);
+  {
+    char* ws = nullptr;
+    ALLOC(ws, scan_workspace_bytes(s->c_total + 1));
+    s->scan_ws = ws;
+    scan_bind_workspace(ws, s->c_total + 1, &s->scan);
+  }
+  for (int b = 0; b < 3; ++b) ALLOC(s->U[b], (size_t)s->w_total);
+  ALLOC(s->D, (size_t)s->w_total);
+  ALLOC(s->d_scenes, s->sd.size());
+  ALLOC(s->d_ptiles, ptiles.size());
+  ALLOC(s->d_wtiles, wtiles.size());
+  ALLOC(s->staging, (size_t)s->n_max);
+  ALLOC(s->d_status, 1);
+  ALLOC(s->d_totals, (size_t)(kTotalsBlocks + 1) * CWA_TOTALS_COUNT);
+#undef ALLOC
+  if (cudaMallocHost((void**)&s->h_status, sizeof(int32_t)) != cudaSuccess ||
+      cudaMallocHost((void**)&s->h_totals, CWA_TOTALS_COUNT * sizeof(double)) != cudaSuccess) {
+    set_error("cudaMallocHost failed");
+    return fail(CWA_ERR_OOM);
+  }
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(CWA_ERR_CUDA);
+  for (auto& e : s->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return fail(CWA_ERR_CUDA);
+  std::vector<int32_t> ids(N);
+  for (size_t i = 0; i < s->sd.size(); ++i)
+    for (int32_t k = 0; k < s->sd[i].n; ++k) ids[(size_t)s->sd[i].poff + k] = k;
+  bool ok = cudaMemcpy(s->d_scenes, s->sd.data(), s->sd.size() * sizeof(SceneDev), cudaMemcpyHostToDevice) ==
+                cudaSuccess &&
+            (ptiles.empty() || cudaMemcpy(s->d_ptiles, ptiles.data(), ptiles.size() * sizeof(Tile),
+                                          cudaMemcpyHostToDevice) == cudaSuccess) &&
+            cudaMemcpy(s->d_wtiles, wtiles.data(), wtiles.size() * sizeof(Tile), cudaMemcpyHostToDevice) ==
+                cudaSuccess &&
+            (N == 0 || (cudaMemcpy(s->ID[0], ids.data(), N * sizeof(int32_t), cudaMemcpyHostToDevice) ==
+                            cudaSuccess &&
+                        cudaMemcpy(s->ID[1], ids.data(), N * sizeof(int32_t), cudaMemcpyHostToDevice) ==
+                            cudaSuccess));
+  if (!ok) {
+    set_error("initial upload failed");
+    return fail(CWA_ERR_CUDA);
+  }
+  *out = s;
+  return CWA_OK;
+}
+
+cwa_status cwa_destroy(cwa_sim* sim) {
+  if (!sim) return arg_error("null sim");
+  free_sim(sim);
+  return CWA_OK;
+}
+
+cwa_status cwa_upload_particles(cwa_sim* s, int32_t scene, const cwa_particle* host, int32_t n) {
+  CWA_TRY(check_scene(s, scene));
+  const SceneDev& d = s->sd[scene];
+  if (n != d.n || (!host && n > 0)) return arg_error("upload size must equal the scene's n_particles");
+  if (n == 0) return CWA_OK;
+  CWA_CUDA(cudaMemcpyAsync(s->staging, host, (size_t)n * sizeof(cwa_particle), cudaMemcpyHostToDevice,
+                           s->stream));
+  CWA_CUDA(launch_unpack(s->staging, n, d.poff, s->P[s->cur], s->V[s->cur], cur_force(s), s->RP, s->EX,
+                         s->ID[s->cur], s->stream));
+  s->launches += 1;
+  s->grid_fresh = false;
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  return CWA_OK;
+}
+
+cwa_status cwa_download_particles(cwa_sim* s, int32_t scene, cwa_particle* host, int32_t n) {
+  CWA_TRY(check_scene(s, scene));
+  const SceneDev& d = s->sd[scene];
+  if (n != d.n || (!host && n > 0)) return arg_error("download size must equal the scene's n_particles");
+  if (n == 0) return CWA_OK;
+  CWA_CUDA(launch_pack(s->staging, n, d.poff, s->P[s->cur], s->V[s->cur], cur_force(s), s->RP, s->EX,
+                       s->ID[s->cur], s->stream));
+  s->launches += 1;
+  CWA_CUDA(cudaMemcpyAsync(host, s->staging, (size_t)n * sizeof(cwa_particle), cudaMemcpyDeviceToHost,
+                           s->stream));
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  return CWA_OK;
+}
+
+cwa_status cwa_upload_wave(cwa_sim* s, int32_t scene, const float* u_n, const float* u_nm1, int32_t nx,
+                           int32_t nz) {
+  CWA_TRY(check_scene(s, scene));
+  const SceneDev& d = s->sd[scene];
+  if (nx != d.nx || nz != d.nz || !u_n) return arg_error("wave upload size must equal the scene's grid");
+  const size_t bytes = (size_t)nx * nz * sizeof(float);
+  const int w = s->wcur;
+  CWA_CUDA(cudaMemcpyAsync(s->U[w] + d.woff, u_n, bytes, cudaMemcpyHostToDevice, s->stream));
+  CWA_CUDA(cudaMemcpyAsync(s->U[(w + 2) % 3] + d.woff, u_nm1 ? u_nm1 : u_n, bytes, cudaMemcpyHostToDevice,
+                           s->stream));
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  return CWA_OK;
+}
+
+cwa_status cwa_download_wave(cwa_sim* s, int32_t scene, float* u_n, float* u_nm1, int32_t nx, int32_t nz) {
+  CWA_TRY(check_scene(s, scene));
+  const SceneDev& d = s->sd[scene];
+  if (nx != d.nx || nz != d.nz) return arg_error("wave download size must equal the scene's grid");
+  const size_t bytes = (size_t)nx * nz * sizeof(float);
+  const int w = s->wcur;
+  if (u_n) CWA_CUDA(cudaMemcpyAsync(u_n, s->U[w] + d.woff, bytes, cudaMemcpyDeviceToHost, s->stream));
+  if (u_nm1)
+    CWA_CUDA(cudaMemcpyAsync(u_nm1, s->U[(w + 2) % 3] + d.woff, bytes, cudaMemcpyDeviceToHost, s->stream));
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  return CWA_OK;
+}
+
+cwa_status cwa_wave_reinit(cwa_sim* s, int32_t scene) {
+  CWA_TRY(check_scene(s, scene));
+  const SceneDev& d = s->sd[scene];
+  const int w = s->wcur;
+  CWA_CUDA(launch_wave_init(s->U[w] + d.woff, d.nx, d.nz, d.mode, s->stream));
+  CWA_CUDA(launch_wave_init(s->U[(w + 2) % 3] + d.woff, d.nx, d.nz, d.mode, s->stream));
+  s->launches += 2;
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  return CWA_OK;
+}
+
+cwa_status cwa_step(cwa_sim* s, int32_t n_steps) {
+  CWA_TRY(check_sim(s));
+  if (n_steps < 0) return arg_error("n_steps < 0");
+  for (int32_t k = 0; k < n_steps; ++k) {
+    if (s->opt.use_graph && !s->profiling)
+      CWA_TRY(graph_step(s));
+    else
+      CWA_TRY(enqueue_step(s));
+  }
+  return CWA_OK;
+}
+
+cwa_status cwa_pass_grid(cwa_sim* s) {
+  CWA_TRY(check_sim(s));
+  return run_grid(s);
+}
+
+cwa_status cwa_pass_rho_pres(cwa_sim* s) {
+  CWA_TRY(check_sim(s));
+  if (!s->grid_fresh) return arg_error("cwa_pass_grid must run before rho_pres in each step");
+  return run_rho_pres(s);
+}
+
+cwa_status cwa_pass_force(cwa_sim* s) {
+  CWA_TRY(check_sim(s));
+  if (!s->grid_fresh) return arg_error("cwa_pass_grid must run before force in each step");
+  return run_force(s);
+}
+
+cwa_status cwa_pass_integrate(cwa_sim* s) {
+  CWA_TRY(check_sim(s));
+  return run_integrate(s);
+}
+
+cwa_status cwa_pass_wave(cwa_sim* s) {
+  CWA_TRY(check_sim(s));
+  return run_wave(s);
+}
+
+cwa_status cwa_synchronize(cwa_sim* s) {
+  CWA_TRY(check_sim(s));
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  return read_status(s);
+}
+
+cwa_status cwa_get_step_count(cwa_sim* s, int64_t* steps) {
+  CWA_TRY(check_sim(s));
+  if (!steps) return arg_error("null output");
+  *steps = s->steps;
+  return CWA_OK;
+}
+
+cwa_status cwa_get_device_view(cwa_sim* s, int32_t scene, cwa_device_view* v) {
+  CWA_TRY(check_scene(s, scene));
+  if (!v) return arg_error("null output");
+  const SceneDev& d = s->sd[scene];
+  v->n_particles = d.n;
+  v->n_cells = d.ncells;
+  for (int a = 0; a < 3; ++a) v->grid_dims[a] = d.dims[a];
+  v->wave_nx = d.nx;
+  v->wave_nz = d.nz;
+  v->pos = reinterpret_cast<float*>(s->P[s->cur] + d.poff);
+  v->vel = reinterpret_cast<float*>(s->V[s->cur] + d.poff);
+  v->force = reinterpret_cast<float*>(cur_force(s) + d.poff);
+  v->rho_p = reinterpret_cast<float*>(s->RP + d.poff);
+  v->particle_id = s->ID[s->cur] + d.poff;
+  v->cell_start = s->start + d.coff;
+  v->wave_u_n = s->U[s->wcur] + d.woff;
+  v->wave_u_nm1 = s->U[(s->wcur + 2) % 3] + d.woff;
+  v->stream = (void*)s->stream;
+  return CWA_OK;
+}
+
+cwa_status cwa_download_grid(cwa_sim* s, int32_t scene, int32_t* cell_start, int32_t n_cells_p1,
+                             int32_t* sorted_id, int32_t n) {
+  CWA_TRY(check_scene(s, scene));
+  const SceneDev& d = s->sd[scene];
+  if (cell_start && n_cells_p1 != d.ncells + 1) return arg_error("cell_start needs n_cells + 1 entries");
+  if (sorted_id && n != d.n) return arg_error("sorted_id needs n_particles entries");
+  if (cell_start) {
+    CWA_CUDA(cudaMemcpyAsync(cell_start, s->start + d.coff, (size_t)n_cells_p1 * sizeof(int32_t),
+                             cudaMemcpyDeviceToHost, s->stream));
+  }
+  if (sorted_id && n > 0)
+    CWA_CUDA(cudaMemcpyAsync(sorted_id, s->ID[s->cur] + d.poff, (size_t)n * sizeof(int32_t),
+                             cudaMemcpyDeviceToHost, s->stream));
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  if (cell_start)
+    for (int32_t c = 0; c < n_cells_p1; ++c) cell_start[c] -= d.poff;
+  return CWA_OK;
+}
+
+cwa_status cwa_download_deposits(cwa_sim* s, int32_t scene, int64_t* out, int32_t nx, int32_t nz) {
+  CWA_TRY(check_scene(s, scene));
+  const SceneDev& d = s->sd[scene];
+  if (!out || nx != d.nx || nz != d.nz) return arg_error("deposit download size must equal the wave grid");
+  CWA_CUDA(cudaMemcpyAsync(out, s->D + d.woff, (size_t)nx * nz * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                           s->stream));
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  return CWA_OK;
+}
+
+cwa_status cwa_reduce_totals(cwa_sim* s, int32_t scene, double out[CWA_TOTALS_COUNT]) {
+  CWA_TRY(check_scene(s, scene));
+  if (!out) return arg_error("null output");
+  const SceneDev& d = s->sd[scene];
+  CWA_CUDA(launch_totals(s->P[s->cur], s->V[s->cur], d.poff, d.n, s->U[s->wcur], s->U[(s->wcur + 2) % 3],
+                         d.woff, d.nx * d.nz, s->d_scenes, scene, s->d_totals, s->stream));
+  s->launches += 2;
+  CWA_CUDA(cudaMemcpyAsync(s->h_totals, s->d_totals + (size_t)kTotalsBlocks * CWA_TOTALS_COUNT,
+                           CWA_TOTALS_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  memcpy(out, s->h_totals, CWA_TOTALS_COUNT * sizeof(double));
+  return CWA_OK;
+}
+
+// Checkpoint: "CWAS", version 1, n_scenes, step count, then per scene its
+// descriptor and the sorted internal state (pos, vel, force, rho_p, id,
+// extras.zw) plus u^n and u^(n-1).  Restoring the sorted order keeps the
+// resumed run bit-identical to an uninterrupted one.
+cwa_status cwa_save(cwa_sim* s, const char* path) {
+  CWA_TRY(check_sim(s));
+  if (!path) return arg_error("null path");
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  FILE* f = fopen(path, "wb");
+  if (!f) {
+    set_error(std::string("cannot open ") + path);
+    return CWA_ERR_IO;
+  }
+  bool ok = true;
+  auto put = [&](const void* p, size_t b) { ok = ok && (b == 0 || fwrite(p, 1, b, f) == b); };
+  const uint32_t magic = 0x53415743u, version = 1;  // "CWAS"
+  const int32_t ns = (int32_t)s->desc.size();
+  put(&magic, 4);
+  put(&version, 4);
+  put(&ns, 4);
+  put(&s->steps, 8);
+  std::vector<char> buf;
+  for (int32_t i = 0; i < ns && ok; ++i) {
+    const SceneDev& d = s->sd[i];
+    put(&s->desc[i], sizeof(cwa_scene_desc));
+    struct Item {
+      const void* dev;
+      size_t bytes;
+    } items[] = {
+        {s->P[s->cur] + d.poff, (size_t)d.n * 16}, {s->V[s->cur] + d.poff, (size_t)d.n * 16},
+        {cur_force(s) + d.poff, (size_t)d.n * 16}, {s->RP + d.poff, (size_t)d.n * 8},
+        {s->ID[s->cur] + d.poff, (size_t)d.n * 4}, {s->EX + d.poff, (size_t)d.n * 8},
+        {s->U[s->wcur] + d.woff, (size_t)d.nx * d.nz * 4},
+        {s->U[(s->wcur + 2) % 3] + d.woff, (size_t)d.nx * d.nz * 4},
+    };
+    for (const Item& it : items) {
+      buf.resize(it.bytes);
+      if (it.bytes && cudaMemcpy(buf.data(), it.dev, it.bytes, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        fclose(f);
+        set_error("checkpoint readback failed");
+        return CWA_ERR_CUDA;
+      }
+      put(buf.data(), it.bytes);
+    }
+  }
+  if (fclose(f) != 0) ok = false;
+  if (!ok) {
+    set_error(std::string("write failed: ") + path);
+    return CWA_ERR_IO;
+  }
+  return CWA_OK;
+}
+
+cwa_status cwa_load(cwa_sim* s, const char* path) {
+  CWA_TRY(check_sim(s));
+  if (!path) return arg_error("null path");
+  FILE* f = fopen(path, "rb");
+  if (!f) {
+    set_error(std::string("cannot open ") + path);
+    return CWA_ERR_IO;
+  }
+  bool ok = true;
+  auto get = [&](void* p, size_t b) { ok = ok && (b == 0 || fread(p, 1, b, f) == b); };
+  uint32_t magic = 0, version = 0;
+  int32_t ns = 0;
+  int64_t steps = 0;
+  get(&magic, 4);
+  get(&version, 4);
+  get(&ns, 4);
+  get(&steps, 8);
+  if (!ok || magic != 0x53415743u || version != 1 || ns != (int32_t)s->desc.size()) {
+    fclose(f);
+    set_error("checkpoint header does not match this sim");
+    return ok ? CWA_ERR_INVALID_ARG : CWA_ERR_IO;
+  }
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  std::vector<char> buf;
+  for (int32_t i = 0; i < ns && ok; ++i) {
+    const SceneDev& d = s->sd[i];
+    cwa_scene_desc desc;
+    get(&desc, sizeof(desc));
+    if (!ok || memcmp(&desc, &s->desc[i], sizeof(desc)) != 0) {
+      fclose(f);
+      set_error("checkpoint scene descriptor does not match this sim");
+      return ok ? CWA_ERR_INVALID_ARG : CWA_ERR_IO;
+    }
+    struct Item {
+      void* dev;
+      size_t bytes;
+    } items[] = {
+        {s->P[s->cur] + d.poff, (size_t)d.n * 16}, {s->V[s->cur] + d.poff, (size_t)d.n * 16},
+        {cur_force(s) + d.poff, (size_t)d.n * 16}, {s->RP + d.poff, (size_t)d.n * 8},
+        {s->ID[s->cur] + d.poff, (size_t)d.n * 4}, {s->EX + d.poff, (size_t)d.n * 8},
+        {s->U[s->wcur] + d.woff, (size_t)d.nx * d.nz * 4},
+        {s->U[(s->wcur + 2) % 3] + d.woff, (size_t)d.nx * d.nz * 4},
+    };
+    for (const Item& it : items) {
+      buf.resize(it.bytes);
+      get(buf.data(), it.bytes);
+      if (!ok) break;
+      if (it.bytes && cudaMemcpy(it.dev, buf.data(), it.bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+        fclose(f);
+        set_error("checkpoint upload failed");
+        return CWA_ERR_CUDA;
+      }
+    }
+  }
+  fclose(f);
+  if (!ok) {
+    set_error(std::string("truncated checkpoint: ") + path);
+    return CWA_ERR_IO;
+  }
+  s->steps = steps;
+  s->grid_fresh = false;
+  return CWA_OK;
+}
+
+cwa_status cwa_set_profiling(cwa_sim* s, int32_t enable) {
+  CWA_TRY(check_sim(s));
+  s->profiling = enable != 0;
+  s->pass_times_valid = false;
+  return CWA_OK;
+}
+
+cwa_status cwa_get_pass_times(cwa_sim* s, float* ms, int32_t n) {
+  CWA_TRY(check_sim(s));
+  if (!ms || n < CWA_PASS_COUNT) return arg_error("need CWA_PASS_COUNT outputs");
+  if (!s->pass_times_valid) return arg_error("no profiled step yet (cwa_set_profiling, then cwa_step)");
+  CWA_CUDA(cudaEventSynchronize(s->ev[CWA_PASS_COUNT]));
+  for (int k = 0; k < CWA_PASS_COUNT; ++k) CWA_CUDA(cudaEventElapsedTime(ms + k, s->ev[k], s->ev[k + 1]));
+  return CWA_OK;
+}
+
+cwa_status cwa_get_launch_count(cwa_sim* s, int64_t* launches) {
+  CWA_TRY(check_sim(s));
+  if (!launches) return arg_error("null output");
+  *launches = s->launches;
+  return CWA_OK;
+}
+
+// ---- stand-alone operators ----
+size_t cwa_scan_workspace_bytes(int32_t n) { return scan_workspace_bytes(n < 0 ? 0 : n) + 256; }
+
+cwa_status cwa_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int32_t n, void* d_workspace,
+                                  size_t workspace_bytes, void* stream) {
+  if (n < 0) return arg_error("n < 0");
+  if (n == 0) return CWA_OK;
+  if (!d_in || !d_out || !d_workspace) return arg_error("null device pointer");
+  if (workspace_bytes < cwa_scan_workspace_bytes(n)) return arg_error("workspace too small");
+  ScanWorkspace ws;
+  scan_bind_workspace(d_workspace, n, &ws);
+  // A status word follows the tile states; a look-back time-out sets it.
+  int32_t* status = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(d_workspace) + scan_workspace_bytes(n));
+  cudaStream_t st = (cudaStream_t)stream;
+  CWA_CUDA(cudaMemsetAsync(status, 0, sizeof(int32_t), st));
+  CWA_CUDA(scan_launch(d_in, d_out, n, n, false, ws, status, st, nullptr));
+  return CWA_OK;
+}
+
+size_t cwa_grid_workspace_bytes(int32_t n, int32_t n_cells) {
+  if (n < 0 || n_cells < 1) return 0;
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  return up(scan_workspace_bytes(n_cells + 1)) + up((size_t)n_cells * 4) + 3 * up((size_t)n * 4 + 4) + 256;
+}
+
+cwa_status cwa_grid_build(const float* d_pos4, int32_t n, const float lo[3], float cell_size,
+                          const int32_t dims[3], int32_t* d_cell_start, int32_t* d_sorted_index,
+                          int32_t* d_cell_of, void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (n < 0 || !lo || !dims || !d_cell_start) return arg_error("bad arguments");
+  if (!(cell_size > 0.0f) || dims[0] < 1 || dims[1] < 1 || dims[2] < 1) return arg_error("bad grid");
+  const int64_t nc64 = (int64_t)dims[0] * dims[1] * dims[2];
+  if (nc64 > (1ll << 31) - (1ll << 20)) return arg_error("too many cells");
+  const int32_t nc = (int32_t)nc64;
+  if (!d_workspace || workspace_bytes < cwa_grid_workspace_bytes(n, nc)) return arg_error("workspace too small");
+  if (n > 0 && (!d_pos4 || !d_sorted_index)) return arg_error("null device pointer");
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  char* w = reinterpret_cast<char*>(d_workspace);
+  ScanWorkspace ws;
+  scan_bind_workspace(w, nc + 1, &ws);
+  w += up(scan_workspace_bytes(nc + 1));
+  int32_t* count = reinterpret_cast<int32_t*>(w);
+  w += up((size_t)nc * 4);
+  int32_t* key = reinterpret_cast<int32_t*>(w);
+  w += up((size_t)n * 4 + 4);
+  int32_t* slot = reinterpret_cast<int32_t*>(w);
+  w += up((size_t)n * 4 + 4);
+  int32_t* list = reinterpret_cast<int32_t*>(w);
+  w += up((size_t)n * 4 + 4);
+  int32_t* status = reinterpret_cast<int32_t*>(w);
+  if (d_cell_of) key = d_cell_of;
+  cudaStream_t st = (cudaStream_t)stream;
+  CWA_CUDA(cudaMemsetAsync(count, 0, (size_t)nc * 4, st));
+  CWA_CUDA(cudaMemsetAsync(status, 0, 4, st));
+  CWA_CUDA(launch_point_hash(reinterpret_cast<const float4*>(d_pos4), n, lo[0], lo[1], lo[2], cell_size, dims[0],
+                             dims[1], dims[2], key, slot, count, status, st));
+  CWA_CUDA(scan_launch(count, d_cell_start, nc, nc + 1, false, ws, status, st, nullptr));
+  CWA_CUDA(launch_list_insert(key, slot, d_cell_start, list, n, st));
+  CWA_CUDA(launch_point_rank(key, slot, d_cell_start, list, n, d_sorted_index, status, st));
+  return CWA_OK;
+}
+
+}  // extern "C"

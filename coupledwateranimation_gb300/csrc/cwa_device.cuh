@@ -1,0 +1,74 @@
+// cwa_device.cuh — device helpers shared by the kernels: the float32 cell
+// hash and the bilinear height-field sample, both written one rounding per
+// operation (__f*_rn) so results do not depend on FMA contraction.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "cwa_internal.h"
+
+namespace cwa {
+
+// clamp(floor((p - lo) / cell), 0, n - 1)  (UniformGrid2D/ugrid_particles_cs.glsl:97-103)
+__device__ __forceinline__ int cell_axis(float p, float lo, float cell, int n) {
+  float t = __fdiv_rn(__fsub_rn(p, lo), cell);
+  float f = floorf(t);
+  f = fminf(fmaxf(f, 0.0f), (float)(n - 1));
+  return (int)f;
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// texture(wave_tex, uv) with GL_LINEAR / GL_CLAMP_TO_EDGE on an R32F image
+// (StencilImage2DTripleBuffered.cpp:21-26): texel centres at (i + 0.5) / W.
+struct Bilinear {
+  float v00, v10, v01, v11, ax, ay;
+};
+
+__device__ __forceinline__ Bilinear bilinear_patch(const float* __restrict__ u, int w, int h, float s,
+                                                   float t) {
+  float tx = __fsub_rn(__fmul_rn(s, (float)w), 0.5f);
+  float ty = __fsub_rn(__fmul_rn(t, (float)h), 0.5f);
+  tx = fminf(fmaxf(tx, -1.0f), (float)w);
+  ty = fminf(fmaxf(ty, -1.0f), (float)h);
+  float fx = floorf(tx), fy = floorf(ty);
+  Bilinear b;
+  b.ax = __fsub_rn(tx, fx);
+  b.ay = __fsub_rn(ty, fy);
+  int x0 = (int)fx, y0 = (int)fy;
+  int x1 = clampi(x0 + 1, 0, w - 1), y1 = clampi(y0 + 1, 0, h - 1);
+  x0 = clampi(x0, 0, w - 1);
+  y0 = clampi(y0, 0, h - 1);
+  b.v00 = __ldg(u + (size_t)y0 * w + x0);
+  b.v10 = __ldg(u + (size_t)y0 * w + x1);
+  b.v01 = __ldg(u + (size_t)y1 * w + x0);
+  b.v11 = __ldg(u + (size_t)y1 * w + x1);
+  return b;
+}
+
+__device__ __forceinline__ float bilinear_value(const Bilinear& b, float* top_out = nullptr,
+                                                float* bot_out = nullptr) {
+  float bx = __fsub_rn(1.0f, b.ax);
+  float top = __fadd_rn(__fmul_rn(bx, b.v00), __fmul_rn(b.ax, b.v10));
+  float bot = __fadd_rn(__fmul_rn(bx, b.v01), __fmul_rn(b.ax, b.v11));
+  if (top_out) *top_out = top;
+  if (bot_out) *bot_out = bot;
+  return __fadd_rn(__fmul_rn(__fsub_rn(1.0f, b.ay), top), __fmul_rn(b.ay, bot));
+}
+
+__device__ __forceinline__ float sample_height(const float* __restrict__ u, int w, int h, float s, float t) {
+  return bilinear_value(bilinear_patch(u, w, h, s, t));
+}
+
+// Value and derivatives along the texel axes of the same bilinear patch.
+__device__ __forceinline__ void sample_height_grad(const float* __restrict__ u, int w, int h, float s,
+                                                   float t, float* val, float* dtx, float* dty) {
+  Bilinear b = bilinear_patch(u, w, h, s, t);
+  float top, bot;
+  float by = __fsub_rn(1.0f, b.ay);
+  *val = bilinear_value(b, &top, &bot);
+  *dtx = __fadd_rn(__fmul_rn(by, __fsub_rn(b.v10, b.v00)), __fmul_rn(b.ay, __fsub_rn(b.v11, b.v01)));
+  *dty = __fsub_rn(bot, top);
+}
+
+}  // namespace cwa

@@ -1,0 +1,313 @@
+// cwa_grid.cu — uniform-grid counting sort: cell hash + count, single-pass
+// exclusive scan (decoupled look-back), stable insert, reorder.
+//
+// Replaces the reference's COMPUTE_COUNTS / ParallelScan / INSERT sequence
+// (SphWave2D/UniformGridGpu2D.cpp:220-265, SphWave2D/uniform_grid_sph_cs.glsl:112-165,
+// UniformGrid2D/ugrid_particles_cs.glsl:90-117, SphWave2D/ParallelScan.cpp:43-95,
+// SphWave2D/prefix_sum_cs.glsl:18-43).  Differences by design:
+//   * the insert is stable (input order within a cell) instead of atomic
+//     arrival order, so the sorted order is deterministic;
+//   * the scan is one launch for any n instead of 2*log2(n) dispatches over
+//     a power-of-two array;
+//   * particle state is moved into sorted order so the neighbour passes read
+//     contiguous cell ranges.
+#include <cuda_runtime.h>
+
+#include "cwa_device.cuh"
+#include "cwa_internal.h"
+
+namespace cwa {
+namespace {
+
+constexpr int kScanBlock = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanBlock * kScanItems;
+constexpr unsigned long long kFlagAgg = 1ull << 32;
+constexpr unsigned long long kFlagInc = 2ull << 32;
+constexpr long kSpinLimit = 1l << 22;
+
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_relaxed(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ int warp_sum(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// One tile of kScanTile items per CTA; tiles are ticketed in start order so a
+// CTA only ever waits on CTAs that are already running.
+template <bool kZero>
+__global__ void __launch_bounds__(kScanBlock)
+    k_scan(int32_t* in, int32_t* out, int32_t n_in, int32_t n_out, unsigned int* counter,
+           unsigned long long* state, int32_t* status) {
+  __shared__ int s_tile, s_prefix;
+  __shared__ int s_warp[kScanBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
+  __syncthreads();
+  const int tile = s_tile;
+  const long base = (long)tile * kScanTile + (long)threadIdx.x * kScanItems;
+
+  int v[kScanItems];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    long idx = base + k;
+    v[k] = idx < n_in ? in[idx] : 0;
+  }
+  if (kZero) {
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k)
+      if (base + k < n_in) in[base + k] = 0;
+  }
+  int tsum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int x = v[k];
+    v[k] = tsum;
+    tsum += x;
+  }
+  int incl = tsum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  int warp_excl = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < kScanBlock / 32; ++w) {
+    int s = s_warp[w];
+    if (w < warp) warp_excl += s;
+    total += s;
+  }
+  const int thread_excl = warp_excl + incl - tsum;
+
+  if (warp == 0) {
+    if (tile == 0) {
+      if (lane == 0) {
+        st_relaxed(state, kFlagInc | (unsigned int)total);
+        s_prefix = 0;
+      }
+    } else {
+      if (lane == 0) st_relaxed(state + tile, kFlagAgg | (unsigned int)total);
+      int pred = tile - 1;
+      int excl = 0;
+      long spins = 0;
+      while (true) {
+        int idx = pred - lane;
+        unsigned long long s = idx >= 0 ? ld_relaxed(state + idx) : kFlagInc;
+        unsigned int flag = (unsigned int)(s >> 32);
+        if (__any_sync(0xffffffffu, flag == 0)) {
+          if (++spins > kSpinLimit) {
+            if (lane == 0) atomicOr(status, kStatusTimeout);
+            break;
+          }
+          __nanosleep(32);
+          continue;
+        }
+        int val = (int)(unsigned int)s;
+        unsigned int inc = __ballot_sync(0xffffffffu, flag == 2u);
+        if (inc) {
+          int first = __ffs(inc) - 1;
+          excl += warp_sum(lane <= first ? val : 0);
+          break;
+        }
+        excl += warp_sum(val);
+        pred -= 32;
+      }
+      if (lane == 0) {
+        st_relaxed(state + tile, kFlagInc | (unsigned int)(excl + total));
+        s_prefix = excl;
+      }
+    }
+  }
+  __syncthreads();
+  const int prefix = s_prefix + thread_excl;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    long idx = base + k;
+    if (idx < n_out) out[idx] = prefix + v[k];
+  }
+}
+
+__device__ __forceinline__ bool finite3(float4 p) {
+  return isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
+}
+
+// Warp-aggregated count: lanes with the same key share one atomicAdd; each
+// lane's slot is its arrival rank within the cell.
+__device__ __forceinline__ int count_slot(int32_t* count, int key) {
+  const unsigned int active = __activemask();
+  const unsigned int peers = __match_any_sync(active, key);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  const int rank = __popc(peers & ((1u << lane) - 1u));
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count + key, __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return base + rank;
+}
+
+__global__ void __launch_bounds__(256)
+    k_hash_count(const float4* __restrict__ pos, const Tile* __restrict__ tiles,
+                 const SceneDev* __restrict__ scenes, int32_t* __restrict__ key,
+                 int32_t* __restrict__ slot, int32_t* __restrict__ count, int32_t* status) {
+  const Tile t = tiles[blockIdx.x];
+  const SceneDev* S = scenes + t.scene;
+  const float lx = S->lo[0], ly = S->lo[1], lz = S->lo[2], cs = S->cell;
+  const int nx = S->dims[0], ny = S->dims[1], nz = S->dims[2], coff = S->coff;
+  for (int i = t.begin + threadIdx.x; i < t.end; i += blockDim.x) {
+    float4 p = pos[i];
+    if (!finite3(p)) atomicOr(status, kStatusNonFinite);
+    int cx = cell_axis(p.x, lx, cs, nx);
+    int cy = cell_axis(p.y, ly, cs, ny);
+    int cz = cell_axis(p.z, lz, cs, nz);
+    int k = coff + (cx * ny + cy) * nz + cz;
+    key[i] = k;
+    slot[i] = count_slot(count, k);
+  }
+}
+
+__global__ void k_point_hash(const float4* __restrict__ pos, int32_t n, float lx, float ly, float lz,
+                             float cs, int32_t nx, int32_t ny, int32_t nz, int32_t* __restrict__ key,
+                             int32_t* __restrict__ slot, int32_t* __restrict__ count, int32_t* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p = pos[i];
+  if (!finite3(p)) atomicOr(status, kStatusNonFinite);
+  int k = (cell_axis(p.x, lx, cs, nx) * ny + cell_axis(p.y, ly, cs, ny)) * nz + cell_axis(p.z, lz, cs, nz);
+  key[i] = k;
+  slot[i] = count_slot(count, k);
+}
+
+__global__ void k_list_insert(const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
+                              const int32_t* __restrict__ start, int32_t* __restrict__ list, int32_t n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  list[start[key[i]] + slot[i]] = i;
+}
+
+// Stable rank of particle i in its cell = members with a smaller index.
+__device__ __forceinline__ int stable_rank(const int32_t* __restrict__ list, int b, int e, int i,
+                                           int slot, int32_t* status) {
+  if (e - b > kMaxStableCell) {
+    if (slot == 0) atomicOr(status, kStatusBigCell);
+    return slot;
+  }
+  int r = 0;
+  for (int m = b; m < e; ++m) r += list[m] < i;
+  return r;
+}
+
+__global__ void __launch_bounds__(256)
+    k_rank_reorder(const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
+                   const int32_t* __restrict__ start, const int32_t* __restrict__ list,
+                   const float4* __restrict__ pin, const float4* __restrict__ vin,
+                   const float4* __restrict__ fin, const int32_t* __restrict__ idin,
+                   float4* __restrict__ pout, float4* __restrict__ vout, float4* __restrict__ fout,
+                   int32_t* __restrict__ idout, int32_t n, int32_t* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int k = key[i];
+  int b = start[k], e = start[k + 1];
+  int dst = b + stable_rank(list, b, e, i, slot[i], status);
+  pout[dst] = pin[i];
+  vout[dst] = vin[i];
+  if (fout) fout[dst] = fin[i];
+  idout[dst] = idin[i];
+}
+
+__global__ void k_point_rank(const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
+                             const int32_t* __restrict__ start, const int32_t* __restrict__ list,
+                             int32_t n, int32_t* __restrict__ sorted_index, int32_t* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int k = key[i];
+  int b = start[k], e = start[k + 1];
+  sorted_index[b + stable_rank(list, b, e, i, slot[i], status)] = i;
+}
+
+inline int blocks_for(long n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+int scan_tile_items() { return kScanTile; }
+
+size_t scan_workspace_bytes(int32_t n_out) {
+  long tiles = blocks_for(n_out > 0 ? n_out : 1, kScanTile);
+  return 256 + (size_t)tiles * sizeof(unsigned long long);
+}
+
+void scan_bind_workspace(void* ws, int32_t n_out, ScanWorkspace* out) {
+  out->counter = reinterpret_cast<unsigned int*>(ws);
+  out->state = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(ws) + 256);
+  out->n_tiles = blocks_for(n_out > 0 ? n_out : 1, kScanTile);
+}
+
+cudaError_t scan_launch(const int32_t* in, int32_t* out, int32_t n_in, int32_t n_out, bool zero_input,
+                        const ScanWorkspace& ws, int32_t* status, cudaStream_t stream, int64_t* launches) {
+  if (n_out <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(ws.counter, 0, 256 + (size_t)ws.n_tiles * 8, stream);
+  if (e != cudaSuccess) return e;
+  int32_t* inw = const_cast<int32_t*>(in);
+  if (zero_input)
+    k_scan<true><<<ws.n_tiles, kScanBlock, 0, stream>>>(inw, out, n_in, n_out, ws.counter, ws.state, status);
+  else
+    k_scan<false><<<ws.n_tiles, kScanBlock, 0, stream>>>(inw, out, n_in, n_out, ws.counter, ws.state, status);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hash_count(const float4* pos, const Tile* tiles, int32_t n_tiles, int32_t tile_size,
+                              const SceneDev* scenes, int32_t* key, int32_t* slot, int32_t* count,
+                              int32_t* status, cudaStream_t stream) {
+  if (n_tiles <= 0) return cudaSuccess;
+  k_hash_count<<<n_tiles, tile_size, 0, stream>>>(pos, tiles, scenes, key, slot, count, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_list_insert(const int32_t* key, const int32_t* slot, const int32_t* start, int32_t* list,
+                               int32_t n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  k_list_insert<<<blocks_for(n, 256), 256, 0, stream>>>(key, slot, start, list, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rank_reorder(const int32_t* key, const int32_t* slot, const int32_t* start,
+                                const int32_t* list, const float4* pin, const float4* vin,
+                                const float4* fin, const int32_t* idin, float4* pout, float4* vout,
+                                float4* fout, int32_t* idout, int32_t n, int32_t* status,
+                                cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  k_rank_reorder<<<blocks_for(n, 256), 256, 0, stream>>>(key, slot, start, list, pin, vin, fin, idin, pout,
+                                                         vout, fout, idout, n, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_point_hash(const float4* pos, int32_t n, float lx, float ly, float lz, float cell,
+                              int32_t dx, int32_t dy, int32_t dz, int32_t* key, int32_t* slot,
+                              int32_t* count, int32_t* status, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  k_point_hash<<<blocks_for(n, 256), 256, 0, stream>>>(pos, n, lx, ly, lz, cell, dx, dy, dz, key, slot,
+                                                       count, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_point_rank(const int32_t* key, const int32_t* slot, const int32_t* start,
+                              const int32_t* list, int32_t n, int32_t* sorted_index, int32_t* status,
+                              cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  k_point_rank<<<blocks_for(n, 256), 256, 0, stream>>>(key, slot, start, list, n, sorted_index, status);
+  return cudaGetLastError();
+}
+
+}  // namespace cwa

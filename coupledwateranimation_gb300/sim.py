@@ -1,0 +1,198 @@
+"""Host-side mirror of the reference's step interface over the C ABI.
+
+The reference drives its step from idle() (CoupledWaterAnimation/Main.cpp:530-562):
+three particle dispatches (rho_pres, force, integrate) and Module::sComputeAll(),
+which runs StencilImage2DTripleBuffered::Compute (the wave evolve + PingPong).
+`Sim` exposes the same passes one by one (`rho_pres`, `force`, `integrate`,
+`wave`, plus the grid sort that precedes them) and the whole step (`step`).
+`WaveModule` mirrors the Module hooks Init / Reinit / Compute of
+StencilImage2DTripleBuffered (StencilImage2DTripleBuffered.h:8-41).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import (PARTICLE_DTYPE, PASSES, PREC_COMPENSATED, TOTALS, DeviceView, SceneDesc,
+                   SimOptions, check, ptr)
+
+
+@dataclass
+class GridArrays:
+    cell_start: np.ndarray  # n_cells + 1, scene-local offsets
+    sorted_id: np.ndarray   # upload index of each sorted particle
+
+
+class Sim:
+    """One or more independent scenes stepped together on one GPU."""
+
+    def __init__(self, scenes, precision: int = PREC_COMPENSATED, use_graph: bool = True,
+                 device: int = 0, nb_threads: int = 0):
+        self._lib = _abi.load()
+        if isinstance(scenes, SceneDesc):
+            scenes = [scenes]
+        self.scenes = [s.copy() for s in scenes]
+        arr = (SceneDesc * len(self.scenes))(*self.scenes)
+        opt = SimOptions(device=device, precision=precision, use_graph=int(use_graph),
+                         nb_threads=nb_threads)
+        h = C.c_void_p()
+        check(self._lib.cwa_create(C.byref(opt), arr, len(self.scenes), C.byref(h)), "cwa_create")
+        self._h = h
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            check(self._lib.cwa_destroy(self._h), "cwa_destroy")
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    # -- data in / out -----------------------------------------------------
+    def upload_particles(self, scene: int, particles: np.ndarray) -> None:
+        p = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE)
+        check(self._lib.cwa_upload_particles(self._h, scene, ptr(p), len(p)), "cwa_upload_particles")
+
+    def download_particles(self, scene: int = 0) -> np.ndarray:
+        n = self.scenes[scene].n_particles
+        out = np.zeros(n, dtype=PARTICLE_DTYPE)
+        check(self._lib.cwa_download_particles(self._h, scene, ptr(out), n), "cwa_download_particles")
+        return out
+
+    def upload_wave(self, scene: int, u_n: np.ndarray, u_nm1: np.ndarray | None = None) -> None:
+        d = self.scenes[scene]
+        a = np.ascontiguousarray(u_n, dtype=np.float32).reshape(d.wave_nz, d.wave_nx)
+        b = None if u_nm1 is None else np.ascontiguousarray(u_nm1, dtype=np.float32).reshape(a.shape)
+        check(self._lib.cwa_upload_wave(self._h, scene, ptr(a), ptr(b), d.wave_nx, d.wave_nz),
+              "cwa_upload_wave")
+
+    def download_wave(self, scene: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        d = self.scenes[scene]
+        a = np.zeros((d.wave_nz, d.wave_nx), np.float32)
+        b = np.zeros_like(a)
+        check(self._lib.cwa_download_wave(self._h, scene, ptr(a), ptr(b), d.wave_nx, d.wave_nz),
+              "cwa_download_wave")
+        return a, b
+
+    def wave_reinit(self, scene: int = 0) -> None:
+        check(self._lib.cwa_wave_reinit(self._h, scene), "cwa_wave_reinit")
+
+    # -- the step ------------------------------------------------------------
+    def step(self, n: int = 1) -> None:
+        check(self._lib.cwa_step(self._h, n), "cwa_step")
+
+    def grid(self) -> None:
+        check(self._lib.cwa_pass_grid(self._h), "cwa_pass_grid")
+
+    def rho_pres(self) -> None:
+        check(self._lib.cwa_pass_rho_pres(self._h), "cwa_pass_rho_pres")
+
+    def force(self) -> None:
+        check(self._lib.cwa_pass_force(self._h), "cwa_pass_force")
+
+    def integrate(self) -> None:
+        check(self._lib.cwa_pass_integrate(self._h), "cwa_pass_integrate")
+
+    def wave(self) -> None:
+        check(self._lib.cwa_pass_wave(self._h), "cwa_pass_wave")
+
+    def synchronize(self) -> None:
+        check(self._lib.cwa_synchronize(self._h), "cwa_synchronize")
+
+    # -- inspection ----------------------------------------------------------
+    @property
+    def step_count(self) -> int:
+        v = C.c_int64()
+        check(self._lib.cwa_get_step_count(self._h, C.byref(v)), "cwa_get_step_count")
+        return v.value
+
+    @property
+    def launch_count(self) -> int:
+        v = C.c_int64()
+        check(self._lib.cwa_get_launch_count(self._h, C.byref(v)), "cwa_get_launch_count")
+        return v.value
+
+    def grid_dims(self, scene: int = 0) -> tuple[int, int, int]:
+        dims = (C.c_int32 * 3)()
+        check(self._lib.cwa_grid_dims(C.byref(self.scenes[scene]), dims), "cwa_grid_dims")
+        return tuple(dims)
+
+    def download_grid(self, scene: int = 0) -> GridArrays:
+        d = self.scenes[scene]
+        nc = int(np.prod(self.grid_dims(scene)))
+        start = np.zeros(nc + 1, np.int32)
+        sid = np.zeros(d.n_particles, np.int32)
+        check(self._lib.cwa_download_grid(self._h, scene, ptr(start), nc + 1, ptr(sid), d.n_particles),
+              "cwa_download_grid")
+        return GridArrays(start, sid)
+
+    def download_deposits(self, scene: int = 0) -> np.ndarray:
+        d = self.scenes[scene]
+        out = np.zeros((d.wave_nz, d.wave_nx), np.int64)
+        check(self._lib.cwa_download_deposits(self._h, scene, ptr(out), d.wave_nx, d.wave_nz),
+              "cwa_download_deposits")
+        return out
+
+    def totals(self, scene: int = 0) -> dict[str, float]:
+        out = np.zeros(len(TOTALS), np.float64)
+        check(self._lib.cwa_reduce_totals(self._h, scene, ptr(out)), "cwa_reduce_totals")
+        return dict(zip(TOTALS, out.tolist()))
+
+    def device_view(self, scene: int = 0) -> DeviceView:
+        v = DeviceView()
+        check(self._lib.cwa_get_device_view(self._h, scene, C.byref(v)), "cwa_get_device_view")
+        return v
+
+    def save(self, path: str) -> None:
+        check(self._lib.cwa_save(self._h, str(path).encode()), "cwa_save")
+
+    def load(self, path: str) -> None:
+        check(self._lib.cwa_load(self._h, str(path).encode()), "cwa_load")
+
+    def set_profiling(self, on: bool) -> None:
+        check(self._lib.cwa_set_profiling(self._h, int(on)), "cwa_set_profiling")
+
+    def pass_times(self) -> dict[str, float]:
+        out = np.zeros(len(PASSES), np.float32)
+        check(self._lib.cwa_get_pass_times(self._h, ptr(out), len(PASSES)), "cwa_get_pass_times")
+        return dict(zip(PASSES, out.tolist()))
+
+
+class WaveModule:
+    """StencilImage2DTripleBuffered's Module hooks over one scene of a Sim.
+
+    Init / Reinit run the MODE_INIT dispatch into both history buffers
+    (StencilImage2DTripleBuffered.cpp:10-59); Compute runs one EvolveWave +
+    PingPong (:79-95).  GetReadImage(0/1) return u^n and u^(n-1).
+    """
+
+    def __init__(self, sim: Sim, scene: int = 0):
+        self.sim, self.scene = sim, scene
+
+    def Init(self) -> None:  # noqa: N802 (reference method names)
+        self.Reinit()
+
+    def Reinit(self) -> None:  # noqa: N802
+        self.sim.wave_reinit(self.scene)
+
+    def Compute(self) -> None:  # noqa: N802
+        self.sim.wave()
+
+    def GetReadImage(self, i: int) -> np.ndarray:  # noqa: N802
+        return self.sim.download_wave(self.scene)[i]

@@ -1,0 +1,261 @@
+/*
+ * cwa.h — C ABI of the GB300 coupled SPH + wave-heightfield simulation step.
+ *
+ * The reference (VarunRamakri7/CoupledWaterAnimation) has no library ABI: its
+ * step is a sequence of GLSL compute dispatches issued from idle()
+ * (CoupledWaterAnimation/Main.cpp:530-562) over an SSBO of 64-byte particles
+ * and a triple-buffered RGBA32F wave image.  Every entry point below replaces
+ * one piece of that GL binding contract; the comment on each names the
+ * reference code it stands in for.  All functions return a cwa_status and
+ * never throw across the ABI.  Plain pointers and sizes only.
+ *
+ * Ownership: the library owns all device memory of a cwa_sim.  Host arrays
+ * passed in are caller-owned and copied.  Device views are borrowed and stay
+ * valid until the next cwa_step / pass call or cwa_destroy.
+ *
+ * Threading: one cwa_sim per host thread (no internal locking).  All work of a
+ * sim runs on one CUDA stream owned by the sim; cwa_step and the pass calls
+ * are asynchronous, downloads / reductions / cwa_synchronize block.
+ */
+#ifndef CWA_H
+#define CWA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CWA_ABI_VERSION 1
+
+typedef enum cwa_status {
+  CWA_OK = 0,
+  CWA_ERR_INVALID_ARG = 1, /* bad pointer, size, index or parameter          */
+  CWA_ERR_OOM = 2,         /* device or pinned allocation failed             */
+  CWA_ERR_CUDA = 3,        /* a CUDA runtime call failed                     */
+  CWA_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up             */
+  CWA_ERR_NONFINITE = 5,   /* a NaN/Inf particle position was met            */
+  CWA_ERR_IO = 6,          /* checkpoint file could not be read or written   */
+  CWA_ERR_NO_DEVICE = 7,   /* no CUDA device / driver                        */
+  CWA_ERR_CAPACITY = 8     /* size beyond a stated maximum                   */
+} cwa_status;
+
+/* Physics presets.
+ * REFERENCE_3D: the shaders' own constants and rules
+ *   (rho_pres_comp.glsl:49-81, force_comp.glsl:160-237,
+ *    integrate_comp.glsl:56-178, wave_comp.glsl:348-383).
+ * MULLER: the 3D Mueller-2003 SPH of the benchmark configurations (poly6
+ *   density, spiky pressure gradient -45/(pi h^6), viscosity Laplacian,
+ *   p = k(rho - rho0), reflective walls) with two-way particle<->heightfield
+ *   coupling through fixed-point deposits. */
+enum { CWA_PRESET_REFERENCE_3D = 0, CWA_PRESET_MULLER = 1 };
+
+/* Accumulation precision of the density / force neighbour sums. */
+enum { CWA_PREC_FP32 = 0, CWA_PREC_COMPENSATED = 1, CWA_PREC_FP64 = 2 };
+
+/* std430 `struct Particle {vec4 pos, vel, force, extras;}`
+ * (CoupledWaterAnimation/Main.cpp:167-173, rho_pres_comp.glsl:14-20).
+ * extras = (rho, pressure, foam threshold, density coefficient). 64 bytes. */
+typedef struct cwa_particle {
+  float pos[4];
+  float vel[4];
+  float force[4];
+  float extras[4];
+} cwa_particle;
+
+/* One independent scene.  Fields mirror the reference's uniform blocks:
+ * ConstantsUniform (Main.cpp:184-190), BoundaryUniform (Main.cpp:192-198),
+ * WaveUniforms (Main.cpp:200-204) and the shader #defines / consts. */
+typedef struct cwa_scene_desc {
+  int32_t preset;          /* CWA_PRESET_*                                    */
+  int32_t n_particles;     /* NUM_PARTICLES                                   */
+  int32_t wave_nx;         /* wave image width  (texture s axis = world x)    */
+  int32_t wave_nz;         /* wave image height (texture t axis = world z)    */
+  float box_lo[3];         /* BoundaryUniform.lower.xyz                       */
+  float box_hi[3];         /* BoundaryUniform.upper.xyz                       */
+  float cell_size;         /* uniform-grid cell edge; must be >= h            */
+  float mass;              /* ConstantsUniform.mass                           */
+  float smoothing_length;  /* h = smoothing_coeff * PARTICLE_RADIUS           */
+  float visc;              /* ConstantsUniform.visc                           */
+  float rest_rho;          /* ConstantsUniform.resting_rho                    */
+  float gas_const;         /* GAS_CONST (reference 4000; Mueller k)           */
+  float dt;                /* SPH time step                                   */
+  float gravity[3];        /* G                                               */
+  float wall_restitution;  /* reference DAMPING 0.3; Mueller restitution     */
+  float velocity_damping;  /* v *= 1 - velocity_damping*dt (reference 0.3)    */
+  float particle_radius;   /* PARTICLE_RADIUS                                 */
+  float crest_height;      /* CREST_THRESHOLD (reference only)                */
+  float foam_speed;        /* |v| above which a particle turns to foam        */
+  float wave_lambda;       /* WaveUniforms.attributes[0]                      */
+  float wave_atten;        /* WaveUniforms.attributes[1]                      */
+  float wave_beta;         /* WaveUniforms.attributes[2]                      */
+  float wave_mode;         /* WaveUniforms.attributes[3]                      */
+  float wave_uv_scale[2];  /* texture uv = pos.xz * scale + offset            */
+  float wave_uv_offset[2];
+  float surface_y0;        /* heightfield rest level (Mueller coupling)       */
+  float surface_restitution; /* normal-push restitution (Mueller coupling)    */
+  float couple_gain;       /* height change per unit deposited momentum       */
+  int32_t deposit_shift;   /* deposit quantum = 2^-deposit_shift momentum     */
+  int32_t flags;           /* reserved, must be 0                             */
+} cwa_scene_desc;
+
+typedef struct cwa_sim_options {
+  int32_t device;          /* CUDA device ordinal                             */
+  int32_t precision;       /* CWA_PREC_*                                      */
+  int32_t use_graph;       /* capture cwa_step into CUDA graphs               */
+  int32_t nb_threads;      /* threads per CTA of the neighbour passes; 0=auto */
+  int32_t reserved[8];
+} cwa_sim_options;
+
+/* Borrowed device pointers of one scene, all in the current sorted order.
+ * pos/vel/force are float4 arrays; rho_p is float2 (rho, pressure);
+ * particle_id[i] is the upload index of sorted particle i. */
+typedef struct cwa_device_view {
+  int32_t n_particles;
+  int32_t n_cells;
+  int32_t grid_dims[3];
+  int32_t wave_nx, wave_nz;
+  float* pos;
+  float* vel;
+  float* force;
+  float* rho_p;
+  int32_t* particle_id;
+  int32_t* cell_start;     /* n_cells + 1 entries, scene-local offsets        */
+  float* wave_u_n;         /* current height field u^n                        */
+  float* wave_u_nm1;       /* previous height field u^(n-1)                   */
+  void* stream;            /* cudaStream_t of the sim                         */
+} cwa_device_view;
+
+typedef struct cwa_sim cwa_sim;
+
+/* Indices into the cwa_reduce_totals output. */
+enum {
+  CWA_TOTAL_MASS = 0,
+  CWA_TOTAL_MOMENTUM_X = 1,
+  CWA_TOTAL_MOMENTUM_Y = 2,
+  CWA_TOTAL_MOMENTUM_Z = 3,
+  CWA_TOTAL_KINETIC = 4,
+  CWA_TOTAL_POTENTIAL = 5,
+  CWA_TOTAL_WAVE_VOLUME = 6,
+  CWA_TOTAL_WAVE_ENERGY = 7,
+  CWA_TOTALS_COUNT = 8
+};
+
+/* Passes of one step, in launch order (for cwa_get_pass_times). */
+enum {
+  CWA_PASS_GRID = 0,      /* hash + count + scan + stable insert + reorder */
+  CWA_PASS_RHO_PRES = 1,
+  CWA_PASS_FORCE = 2,
+  CWA_PASS_INTEGRATE = 3,
+  CWA_PASS_WAVE = 4,
+  CWA_PASS_COUNT = 5
+};
+
+/* ---- misc --------------------------------------------------------------- */
+const char* cwa_status_str(cwa_status s);
+int32_t cwa_abi_version(void);
+/* Last error text of this thread (CUDA error string or argument check). */
+const char* cwa_last_error(void);
+
+/* Fill a scene with a preset's constants.  REFERENCE_3D gives the values of
+ * Main.cpp:28-35,184-204 and the shader consts; MULLER gives the benchmark
+ * physics for lattice spacing `spacing` (h = 2s, m = rho0 s^3). */
+cwa_status cwa_scene_defaults(int32_t preset, float spacing, cwa_scene_desc* out);
+/* Set the wave grid size; for MULLER also re-derive lambda, beta, the uv
+ * mapping over the box, the coupling gain and the deposit quantum. */
+cwa_status cwa_scene_set_wave_grid(cwa_scene_desc* scene, int32_t nx, int32_t nz);
+/* Uniform-grid dimensions ceil((hi-lo)/cell_size) per axis, in float32. */
+cwa_status cwa_grid_dims(const cwa_scene_desc* scene, int32_t dims[3]);
+
+/* ---- scene generators (host) ---------------------------------------------
+ * make_cube: the reference's 64x5x64 lattice (Main.cpp:735-794).
+ * dam_break: lattice dims[0..2] at `spacing` from box_lo + spacing/2, x
+ *   fastest, jittered by U(-jitter*s, +jitter*s) per axis (seeded
+ *   splitmix64 -> xoshiro256**), zero velocity.
+ * bumps: sum of n_bumps Gaussians A~U(0.01,0.05), sigma~U(0.02,0.1),
+ *   centre~U(0,1)^2 in texture uv, evaluated at texel centres. */
+cwa_status cwa_make_reference_cube(const cwa_scene_desc* scene, cwa_particle* out, int32_t n);
+cwa_status cwa_make_dam_break(const cwa_scene_desc* scene, const int32_t dims[3], float spacing,
+                              float jitter, uint64_t seed, cwa_particle* out, int32_t n);
+cwa_status cwa_make_bumps(const cwa_scene_desc* scene, int32_t n_bumps, uint64_t seed,
+                          float* out_u, int32_t nx, int32_t nz);
+
+/* ---- simulation lifecycle ------------------------------------------------
+ * Replaces init_particles()/glBufferData (Main.cpp:764-794) and
+ * StencilImage2DTripleBuffered::Init (StencilImage2DTripleBuffered.cpp:10-31). */
+cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, int32_t n_scenes,
+                      cwa_sim** out);
+cwa_status cwa_destroy(cwa_sim* sim);
+cwa_status cwa_upload_particles(cwa_sim* sim, int32_t scene, const cwa_particle* host, int32_t n);
+cwa_status cwa_download_particles(cwa_sim* sim, int32_t scene, cwa_particle* host, int32_t n);
+cwa_status cwa_upload_wave(cwa_sim* sim, int32_t scene, const float* u_n, const float* u_nm1,
+                           int32_t nx, int32_t nz);
+cwa_status cwa_download_wave(cwa_sim* sim, int32_t scene, float* u_n, float* u_nm1, int32_t nx,
+                             int32_t nz);
+/* StencilImage2DTripleBuffered::Reinit (StencilImage2DTripleBuffered.cpp:42-59):
+ * wave_comp.glsl InitWave (MODE_INIT, :259-317) into both history buffers. */
+cwa_status cwa_wave_reinit(cwa_sim* sim, int32_t scene);
+
+/* One full step per iteration: grid -> rho_pres -> force -> integrate -> wave
+ * (idle(), Main.cpp:549-560, plus the uniform-grid sort).  Asynchronous. */
+cwa_status cwa_step(cwa_sim* sim, int32_t n_steps);
+/* The same passes one at a time (one glDispatchCompute each).  cwa_pass_grid
+ * must precede rho_pres in every step; the wave pass ends the step. */
+cwa_status cwa_pass_grid(cwa_sim* sim);
+cwa_status cwa_pass_rho_pres(cwa_sim* sim);
+cwa_status cwa_pass_force(cwa_sim* sim);
+cwa_status cwa_pass_integrate(cwa_sim* sim);
+cwa_status cwa_pass_wave(cwa_sim* sim);
+/* Wait for the sim's stream; report a device-side status (timeout, NaN). */
+cwa_status cwa_synchronize(cwa_sim* sim);
+cwa_status cwa_get_step_count(cwa_sim* sim, int64_t* steps);
+cwa_status cwa_get_device_view(cwa_sim* sim, int32_t scene, cwa_device_view* out);
+
+/* Grid of the last cwa_pass_grid: cell_start (n_cells+1, scene-local) and
+ * sorted_id (upload index of each sorted particle). */
+cwa_status cwa_download_grid(cwa_sim* sim, int32_t scene, int32_t* cell_start, int32_t n_cells_p1,
+                             int32_t* sorted_id, int32_t n);
+/* Fixed-point deposits made by the last cwa_pass_integrate (before the wave
+ * pass consumes and clears them): nx*nz int64 per scene. */
+cwa_status cwa_download_deposits(cwa_sim* sim, int32_t scene, int64_t* out, int32_t nx, int32_t nz);
+
+/* FP64 on-device totals of one scene (CWA_TOTAL_* order). */
+cwa_status cwa_reduce_totals(cwa_sim* sim, int32_t scene, double out[CWA_TOTALS_COUNT]);
+
+/* Versioned little-endian checkpoint of every scene's state + step count. */
+cwa_status cwa_save(cwa_sim* sim, const char* path);
+cwa_status cwa_load(cwa_sim* sim, const char* path);
+
+/* Per-pass CUDA-event timing of the most recent step (ms), when enabled. */
+cwa_status cwa_set_profiling(cwa_sim* sim, int32_t enable);
+cwa_status cwa_get_pass_times(cwa_sim* sim, float* ms, int32_t n);
+/* Number of kernels launched by the library on this sim since creation. */
+cwa_status cwa_get_launch_count(cwa_sim* sim, int64_t* launches);
+
+/* ---- stand-alone operators on caller-owned device buffers ----------------
+ * Exclusive prefix sum of int32 (replaces ParallelScan::Compute,
+ * SphWave2D/ParallelScan.cpp:43-95 and prefix_sum_cs.glsl:18-43).  Any n >= 0
+ * (the reference requires a power of two).  d_out may equal d_in.  The
+ * workspace must hold cwa_scan_workspace_bytes(n) bytes of device memory. */
+size_t cwa_scan_workspace_bytes(int32_t n);
+cwa_status cwa_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int32_t n, void* d_workspace,
+                                  size_t workspace_bytes, void* stream);
+
+/* Uniform-grid build of n points (float4 xyz, stride 16 B): cell =
+ * clamp(floor((p-lo)/cell), 0, dims-1), cell id (k*dims[1]+j)*dims[0]+i,
+ * stable counting sort.  Replaces the COMPUTE_COUNTS / scan / INSERT
+ * sequence of UniformGridSph2D::CollisionQuery (SphWave2D/UniformGridGpu2D.cpp:220-265)
+ * and UniformGrid2D/ugrid_particles_cs.glsl:90-117, with a deterministic
+ * (input-order) insert.  Outputs: d_cell_start (ncells+1), d_sorted_index (n),
+ * optional d_cell_of (n, cell id of each input point, may be NULL). */
+size_t cwa_grid_workspace_bytes(int32_t n, int32_t n_cells);
+cwa_status cwa_grid_build(const float* d_pos4, int32_t n, const float lo[3], float cell_size,
+                          const int32_t dims[3], int32_t* d_cell_start, int32_t* d_sorted_index,
+                          int32_t* d_cell_of, void* d_workspace, size_t workspace_bytes,
+                          void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CWA_H */

@@ -1,0 +1,93 @@
+/*
+ * cwa_oracle.h — CPU oracle of the coupled SPH + wave step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the correctness checker and the timed
+ * CPU baseline; the product (libcwa) never links, loads or calls it.  Only
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+ * legs may use it.
+ *
+ * It restates the reference's GLSL compute shaders in plain C++:
+ *   - FP64 versions of every pass (rho_pres, force, integrate, wave) used for
+ *     the tolerance checks and the CPU baseline;
+ *   - FP32-exact versions of the integer / element-wise parts (cell hash,
+ *     stable counting sort, exclusive scan, integrate + fixed-point deposits,
+ *     wave stencil, wave init) that the GPU must reproduce bit for bit.
+ * Build flags: -O3 -fopenmp -ffp-contract=off (no FMA contraction, so the
+ * FP32-exact routines round every operation separately).
+ *
+ * Parity pinning: the reference's only known-answer test is the exclusive
+ * scan (SphWave2D/ParallelScan.cpp:124-155); the scan restatement is pinned
+ * to it.  The reference's shaders cannot be executed (GLSL through OpenGL, no
+ * graphics stack), so the SPH, integrate, coupling and wave restatements are
+ * parity unpinned: they follow the shader source line by line (cited per
+ * function) but no reference output exists to check them against.
+ *
+ * Particle arrays are the 64-byte reference struct widened to double:
+ * 16 doubles per particle = pos[4], vel[4], force[4], extras[4].
+ */
+#ifndef CWA_ORACLE_H
+#define CWA_ORACLE_H
+
+#include <stdint.h>
+
+#include "../include/cwa.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int orc_num_threads(void);
+void orc_set_num_threads(int n);
+
+/* ---- FP32-exact integer parts ------------------------------------------ */
+/* Exclusive scan, the CPU truth of SphWave2D/ParallelScan.cpp:130-137. */
+void orc_exclusive_scan_i32(const int32_t* in, int32_t* out, int32_t n);
+/* Cell of a float32 point, UniformGrid2D/ugrid_particles_cs.glsl:97-103. */
+int32_t orc_cell_id_f32(const float p[3], const float lo[3], float cell, const int32_t dims[3]);
+/* Stable counting sort (UniformGrid2D/UniformGrid2D.cpp:33-92 with one cell
+ * per point): cell_start[ncells+1], sorted_index[n], cell_of[n] (nullable). */
+void orc_grid_build_f32(const float* pos4, int32_t n, const float lo[3], float cell,
+                        const int32_t dims[3], int32_t* cell_start, int32_t* sorted_index,
+                        int32_t* cell_of);
+void orc_grid_dims(const cwa_scene_desc* sc, int32_t dims[3]);
+
+/* ---- scene generators (independent restatement of the library's) -------- */
+void orc_scene_defaults(int32_t preset, float spacing, cwa_scene_desc* out);
+void orc_scene_set_wave_grid(cwa_scene_desc* sc, int32_t nx, int32_t nz);
+void orc_make_reference_cube(const cwa_scene_desc* sc, float* p16f, int32_t n);
+void orc_make_dam_break(const cwa_scene_desc* sc, const int32_t dims[3], float spacing,
+                        float jitter, uint64_t seed, float* p16f, int32_t n);
+void orc_make_bumps(const cwa_scene_desc* sc, int32_t n_bumps, uint64_t seed, float* u,
+                    int32_t nx, int32_t nz);
+
+/* ---- FP64 passes (particles in any order; p16 = n x 16 doubles) -------- */
+/* brute != 0: all-pairs O(N^2) loop as the shaders do; else uniform grid. */
+void orc_rho_pres(const cwa_scene_desc* sc, int32_t n, double* p16, const double* u_n,
+                  int32_t brute);
+void orc_force(const cwa_scene_desc* sc, int32_t n, double* p16, const double* u_n,
+               int32_t brute);
+/* deposits: nx*nz int64 accumulated (not cleared), may be NULL. */
+void orc_integrate(const cwa_scene_desc* sc, int32_t n, double* p16, const double* u_n,
+                   int64_t* deposits);
+/* u_out = evolve(u_n, u_nm1) + deposits (deposits may be NULL). */
+void orc_wave(const cwa_scene_desc* sc, const double* u_n, const double* u_nm1, double* u_out,
+              const int64_t* deposits);
+/* Full steps in place; wave buffers rotate: after a step u_n holds u^(n+1). */
+void orc_step(const cwa_scene_desc* sc, int32_t n, double* p16, double* u_n, double* u_nm1,
+              int32_t n_steps, int32_t brute);
+/* FP64 totals in CWA_TOTAL_* order. */
+void orc_totals(const cwa_scene_desc* sc, int32_t n, const double* p16, const double* u_n,
+                const double* u_nm1, double out[CWA_TOTALS_COUNT]);
+
+/* ---- FP32-exact element-wise passes (p16f = n x 16 floats) ------------- */
+void orc_integrate_f32(const cwa_scene_desc* sc, int32_t n, float* p16f, const float* u_n,
+                       int64_t* deposits);
+void orc_wave_f32(const cwa_scene_desc* sc, const float* u_n, const float* u_nm1, float* u_out,
+                  const int64_t* deposits);
+void orc_wave_init_f32(const cwa_scene_desc* sc, float* u);
+float orc_sample_f32(const float* u, int32_t w, int32_t h, float s, float t);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,218 @@
+"""ctypes binding of the CPU oracle (oracle/cwa_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline / reference legs.  The product never imports it.
+Particles cross this boundary as (n, 16) float64 arrays (pos, vel, force,
+extras) for the FP64 passes and as the 64-byte record for the float32 ones.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libcwa_oracle.so"
+
+_P = C.c_void_p
+_I = C.c_int32
+_lib = None
+
+
+def build() -> Path:
+    r = subprocess.run(["make", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        lib = C.CDLL(str(LIB))
+        protos = {
+            "orc_num_threads": (C.c_int, []),
+            "orc_set_num_threads": (None, [C.c_int]),
+            "orc_exclusive_scan_i32": (None, [_P, _P, _I]),
+            "orc_cell_id_f32": (_I, [_P, _P, C.c_float, _P]),
+            "orc_grid_build_f32": (None, [_P, _I, _P, C.c_float, _P, _P, _P, _P]),
+            "orc_grid_dims": (None, [_P, _P]),
+            "orc_scene_defaults": (None, [_I, C.c_float, _P]),
+            "orc_scene_set_wave_grid": (None, [_P, _I, _I]),
+            "orc_make_reference_cube": (None, [_P, _P, _I]),
+            "orc_make_dam_break": (None, [_P, _P, C.c_float, C.c_float, C.c_uint64, _P, _I]),
+            "orc_make_bumps": (None, [_P, _I, C.c_uint64, _P, _I, _I]),
+            "orc_rho_pres": (None, [_P, _I, _P, _P, _I]),
+            "orc_force": (None, [_P, _I, _P, _P, _I]),
+            "orc_integrate": (None, [_P, _I, _P, _P, _P]),
+            "orc_wave": (None, [_P, _P, _P, _P, _P]),
+            "orc_step": (None, [_P, _I, _P, _P, _P, _I, _I]),
+            "orc_totals": (None, [_P, _I, _P, _P, _P, _P]),
+            "orc_integrate_f32": (None, [_P, _I, _P, _P, _P]),
+            "orc_wave_f32": (None, [_P, _P, _P, _P, _P]),
+            "orc_wave_init_f32": (None, [_P, _P]),
+            "orc_sample_f32": (C.c_float, [_P, _I, _I, C.c_float, C.c_float]),
+        }
+        for name, (res, args) in protos.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _d(desc):
+    return C.cast(C.byref(desc), C.c_void_p)
+
+
+def threads() -> int:
+    return load().orc_num_threads()
+
+
+def set_threads(n: int) -> None:
+    load().orc_set_num_threads(n)
+
+
+# ---------------------------------------------------------------- helpers --
+def to_f64(particles: np.ndarray) -> np.ndarray:
+    """64-byte particle records -> (n, 16) float64."""
+    return np.ascontiguousarray(particles.view(np.float32).reshape(-1, 16), dtype=np.float64)
+
+
+def to_f32_records(p16: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(p16, dtype=np.float32).reshape(-1, 16)
+
+
+# ------------------------------------------------------------ integer parts --
+def exclusive_scan(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.int32)
+    out = np.zeros_like(x)
+    load().orc_exclusive_scan_i32(_p(x), _p(out), len(x))
+    return out
+
+
+def grid_dims(desc) -> tuple[int, int, int]:
+    dims = np.zeros(3, np.int32)
+    load().orc_grid_dims(_d(desc), _p(dims))
+    return tuple(int(v) for v in dims)
+
+
+def grid_build(pos4: np.ndarray, lo, cell: float, dims):
+    pos4 = np.ascontiguousarray(pos4, np.float32).reshape(-1, 4)
+    lo = np.ascontiguousarray(lo, np.float32)
+    dims = np.ascontiguousarray(dims, np.int32)
+    n = len(pos4)
+    nc = int(np.prod(dims))
+    start = np.zeros(nc + 1, np.int32)
+    order = np.zeros(n, np.int32)
+    cell_of = np.zeros(n, np.int32)
+    load().orc_grid_build_f32(_p(pos4), n, _p(lo), cell, _p(dims), _p(start), _p(order), _p(cell_of))
+    return start, order, cell_of
+
+
+# ---------------------------------------------------------------- scenes --
+def scene_defaults(preset: int, spacing: float, desc_type):
+    d = desc_type()
+    load().orc_scene_defaults(preset, spacing, _d(d))
+    return d
+
+
+def scene_set_wave_grid(desc, nx: int, nz: int) -> None:
+    load().orc_scene_set_wave_grid(_d(desc), nx, nz)
+
+
+def make_reference_cube(desc, n: int) -> np.ndarray:
+    out = np.zeros((n, 16), np.float32)
+    load().orc_make_reference_cube(_d(desc), _p(out), n)
+    return out
+
+
+def make_dam_break(desc, dims, spacing, jitter, seed, n) -> np.ndarray:
+    out = np.zeros((n, 16), np.float32)
+    d = np.ascontiguousarray(dims, np.int32)
+    load().orc_make_dam_break(_d(desc), _p(d), spacing, jitter, seed, _p(out), n)
+    return out
+
+
+def make_bumps(desc, n_bumps, seed, nx, nz) -> np.ndarray:
+    out = np.zeros((nz, nx), np.float32)
+    load().orc_make_bumps(_d(desc), n_bumps, seed, _p(out), nx, nz)
+    return out
+
+
+# ------------------------------------------------------------ FP64 passes --
+def rho_pres(desc, p16: np.ndarray, u_n: np.ndarray, brute=False) -> None:
+    load().orc_rho_pres(_d(desc), len(p16), _p(p16), _p(np.ascontiguousarray(u_n, np.float64)), int(brute))
+
+
+def force(desc, p16: np.ndarray, u_n: np.ndarray, brute=False) -> None:
+    load().orc_force(_d(desc), len(p16), _p(p16), _p(np.ascontiguousarray(u_n, np.float64)), int(brute))
+
+
+def integrate(desc, p16: np.ndarray, u_n: np.ndarray, deposits: np.ndarray | None = None) -> None:
+    load().orc_integrate(_d(desc), len(p16), _p(p16), _p(np.ascontiguousarray(u_n, np.float64)),
+                         _p(deposits))
+
+
+def wave(desc, u_n, u_nm1, deposits=None) -> np.ndarray:
+    a = np.ascontiguousarray(u_n, np.float64)
+    b = np.ascontiguousarray(u_nm1, np.float64)
+    out = np.zeros_like(a)
+    load().orc_wave(_d(desc), _p(a), _p(b), _p(out), _p(deposits))
+    return out
+
+
+def step(desc, p16: np.ndarray, u_n: np.ndarray, u_nm1: np.ndarray, n_steps: int, brute=False) -> None:
+    """In place: p16 (n,16) f64, u_n / u_nm1 f64 (rotated each step)."""
+    for a in (p16, u_n, u_nm1):
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    load().orc_step(_d(desc), len(p16), _p(p16), _p(u_n), _p(u_nm1), n_steps, int(brute))
+
+
+def totals(desc, p16, u_n, u_nm1) -> np.ndarray:
+    out = np.zeros(8, np.float64)
+    load().orc_totals(_d(desc), len(p16), _p(p16), _p(np.ascontiguousarray(u_n, np.float64)),
+                      _p(np.ascontiguousarray(u_nm1, np.float64)), _p(out))
+    return out
+
+
+# ------------------------------------------------------- FP32-exact passes --
+def integrate_f32(desc, p16f: np.ndarray, u_n: np.ndarray, with_deposits=True):
+    p16f = np.ascontiguousarray(p16f, np.float32).copy()
+    dep = np.zeros((desc.wave_nz, desc.wave_nx), np.int64) if with_deposits else None
+    load().orc_integrate_f32(_d(desc), len(p16f), _p(p16f), _p(np.ascontiguousarray(u_n, np.float32)),
+                             _p(dep))
+    return p16f, dep
+
+
+def wave_f32(desc, u_n, u_nm1, deposits=None) -> np.ndarray:
+    a = np.ascontiguousarray(u_n, np.float32)
+    b = np.ascontiguousarray(u_nm1, np.float32)
+    out = np.zeros_like(a)
+    dep = None if deposits is None else np.ascontiguousarray(deposits, np.int64)
+    load().orc_wave_f32(_d(desc), _p(a), _p(b), _p(out), _p(dep))
+    return out
+
+
+def wave_init_f32(desc) -> np.ndarray:
+    out = np.zeros((desc.wave_nz, desc.wave_nx), np.float32)
+    load().orc_wave_init_f32(_d(desc), _p(out))
+    return out
+
+
+def sample_f32(u, s, t) -> float:
+    u = np.ascontiguousarray(u, np.float32)
+    return float(load().orc_sample_f32(_p(u), u.shape[1], u.shape[0], s, t))
+
+
+def omp_threads_env() -> int:
+    return int(os.environ.get("OMP_NUM_THREADS", "0") or 0)

@@ -1,0 +1,137 @@
+"""CPU tests of the C ABI: the library loads, exports every function that
+include/cwa.h declares, and its host-only entry points behave (argument
+checks, presets, generators).  No kernel runs here."""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+
+import numpy as np
+import pytest
+
+from coupledwateranimation_gb300 import _abi, scenes
+
+
+def test_exports_every_declared_symbol(lib):
+    names = _abi.declared_functions()
+    assert len(names) >= 35
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert missing == []
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_abi.LIB_PATH)], capture_output=True,
+                         text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert set(names) <= exported
+    # every binding in the Python mirror names a declared function
+    assert set(_abi._PROTOS) <= set(names)
+
+
+def test_abi_version_and_status_strings(lib):
+    assert lib.cwa_abi_version() == 1
+    for s in range(9):
+        assert _abi.status_str(s) != "unknown status"
+    assert _abi.status_str(99) == "unknown status"
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """ctypes mirrors of the ABI structs have the C compiler's size and offsets."""
+    structs = {"cwa_scene_desc": _abi.SceneDesc, "cwa_sim_options": _abi.SimOptions,
+               "cwa_device_view": _abi.DeviceView}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{_abi.LIB_PATH.parent.parent}/include/cwa.h"',
+             "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append('printf("cwa_particle size %zu\\n", sizeof(cwa_particle));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-o", str(exe), str(src)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py)
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+    assert got[("cwa_particle", "size")] == _abi.PARTICLE_DTYPE.itemsize == 64
+
+
+def test_reference_preset_constants():
+    d = scenes.defaults(_abi.PRESET_REFERENCE_3D)
+    # CoupledWaterAnimation/Main.cpp:31-32,184-204 and shader consts
+    assert d.n_particles == 20480
+    assert d.mass == pytest.approx(0.02)
+    assert d.smoothing_length == pytest.approx(0.01)
+    assert d.visc == 3000 and d.rest_rho == 1000 and d.gas_const == 4000
+    assert d.dt == pytest.approx(5e-5)
+    assert d.gravity[1] == pytest.approx(-9806.65)
+    assert list(d.box_lo) == pytest.approx([0.0, -0.02, 0.0])
+    assert list(d.box_hi) == pytest.approx([0.48, 1.0, 0.48])
+    assert (d.wave_lambda, d.wave_atten, d.wave_beta, d.wave_mode) == pytest.approx((0.01, 0.985, 0.001, 1.0))
+    assert (d.wave_nx, d.wave_nz) == (64, 64)
+
+
+def test_muller_preset_constants():
+    d = scenes.defaults(_abi.PRESET_MULLER, 0.02)
+    assert d.smoothing_length == pytest.approx(0.04)
+    assert d.mass == pytest.approx(1000 * 0.02 ** 3)
+    assert (d.gas_const, d.visc, d.dt, d.wall_restitution) == pytest.approx((50, 0.1, 1e-4, 0.5))
+    assert d.gravity[1] == pytest.approx(-9.81)
+    scenes.set_wave_grid(d, 256, 256)
+    assert d.wave_lambda == pytest.approx(0.25)  # (c dt_w / dx)^2 with dt_w = dx / 2
+    assert d.wave_beta == pytest.approx(0.01 * 0.5 / 256)
+
+
+def test_invalid_arguments_rejected(lib):
+    d = scenes.defaults(_abi.PRESET_MULLER, 0.02)
+    assert lib.cwa_scene_defaults(7, 0.02, C.byref(d)) == _abi.CWA_ERR_INVALID_ARG
+    assert lib.cwa_scene_defaults(_abi.PRESET_MULLER, 0.0, C.byref(d)) == _abi.CWA_ERR_INVALID_ARG
+    assert lib.cwa_scene_set_wave_grid(C.byref(d), 0, 5) == _abi.CWA_ERR_INVALID_ARG
+    bad = d.copy()
+    bad.cell_size = 0.0
+    dims = (C.c_int32 * 3)()
+    assert lib.cwa_grid_dims(C.byref(bad), dims) == _abi.CWA_ERR_INVALID_ARG
+    assert lib.cwa_make_reference_cube(C.byref(d), None, 10) == _abi.CWA_ERR_INVALID_ARG
+    assert lib.cwa_destroy(None) == _abi.CWA_ERR_INVALID_ARG
+    assert lib.cwa_step(None, 1) == _abi.CWA_ERR_INVALID_ARG
+    h = C.c_void_p()
+    assert lib.cwa_create(None, None, 0, C.byref(h)) == _abi.CWA_ERR_INVALID_ARG
+    assert lib.cwa_exclusive_scan_i32(None, None, -1, None, 0, None) == _abi.CWA_ERR_INVALID_ARG
+    assert lib.cwa_exclusive_scan_i32(None, None, 0, None, 0, None) == _abi.CWA_OK
+    assert lib.cwa_scan_workspace_bytes(1 << 20) > lib.cwa_scan_workspace_bytes(16)
+
+
+def test_create_without_gpu_reports_no_device(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    d = scenes.dam_break((4, 4, 4), 0.05, (16, 16)).desc
+    h = C.c_void_p()
+    assert lib.cwa_create(None, C.byref(d), 1, C.byref(h)) == _abi.CWA_ERR_NO_DEVICE
+    assert h.value is None
+
+
+def test_scene_validation_messages(lib):
+    # Descriptors are validated before the device query: an invalid one is
+    # rejected with a message on any machine.
+    d = scenes.dam_break((4, 4, 4), 0.05, (16, 16)).desc
+    d.cell_size = d.smoothing_length * 0.5
+    h = C.c_void_p()
+    assert lib.cwa_create(None, C.byref(d), 1, C.byref(h)) == _abi.CWA_ERR_INVALID_ARG
+    assert "cell_size" in _abi.last_error()
+
+
+def test_generated_scenes_shapes():
+    s = scenes.dam_break((8, 9, 10), 0.02, (32, 16))
+    assert s.particles.shape == (720,)
+    assert s.wave.shape == (16, 32)
+    p = s.particles["pos"]
+    assert np.all(p[:, 0] > 0) and np.all(p[:, 0] < 8 * 0.02 + 0.02)
+    assert np.all(s.particles["extras"][:, 0] == 1000)
+    w = scenes.config3(n_scenes=12)
+    assert len(w.scenes) == 12
+    for sc in w.scenes:
+        assert 1000 <= sc.desc.n_particles <= 80000
+        assert sc.desc.wave_nx in (64, 128, 256, 512)
+        assert sc.desc.cell_size >= sc.desc.smoothing_length
