@@ -51,6 +51,8 @@ struct cwa_sim {
   int32_t* list = nullptr;
   int32_t* count = nullptr;
   int32_t* start = nullptr;
+  int32_t* nbr = nullptr;      // neighbour lists, kMaxNbr x n_total
+  int32_t* nbr_cnt = nullptr;
   void* scan_ws = nullptr;
   ScanWorkspace scan{};
   // wave: U[wcur] = u^n, U[(wcur+2)%3] = u^(n-1), U[(wcur+1)%3] = next
@@ -61,7 +63,7 @@ struct cwa_sim {
   Tile* d_ptiles = nullptr;
   int32_t n_ptiles = 0, ptile = 128;
   Tile* d_wtiles = nullptr;
-  int32_t n_wtiles = 0, wtile = 256;
+  int32_t n_wtiles = 0, wtile = 1024;
   // staging / status / totals
   cwa_particle* staging = nullptr;
   int32_t* d_status = nullptr;
@@ -239,14 +241,15 @@ cwa_status run_grid(cwa_sim* s) {
 
 cwa_status run_rho_pres(cwa_sim* s) {
   CWA_CUDA(launch_rho_pres(s->opt.precision, s->P[s->cur], s->start, s->d_ptiles, s->n_ptiles, s->ptile,
-                           s->d_scenes, s->U[s->wcur], s->RP, s->stream));
+                           s->d_scenes, s->U[s->wcur], s->RP, s->nbr, s->nbr_cnt, s->n_total, s->stream));
   s->launches += s->n_ptiles > 0;
   return CWA_OK;
 }
 
 cwa_status run_force(cwa_sim* s) {
   CWA_CUDA(launch_force(s->opt.precision, s->P[s->cur], s->V[s->cur], s->RP, s->start, s->d_ptiles,
-                        s->n_ptiles, s->ptile, s->d_scenes, s->U[s->wcur], cur_force(s), s->stream));
+                        s->n_ptiles, s->ptile, s->d_scenes, s->U[s->wcur], cur_force(s), s->nbr, s->nbr_cnt,
+                        s->n_total, s->stream));
   s->launches += s->n_ptiles > 0;
   return CWA_OK;
 }
@@ -403,7 +406,7 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
     if (st != CWA_OK) return st == CWA_ERR_CAPACITY ? st : arg_error("bad grid dimensions");
     np += scenes[i].n_particles;
     nc += (int64_t)dims[3 * i] * dims[3 * i + 1] * dims[3 * i + 2];
-    nw += (int64_t)scenes[i].wave_nx * scenes[i].wave_nz;
+    nw += ((int64_t)scenes[i].wave_nx * scenes[i].wave_nz + 31) / 32 * 32;  // 128-byte aligned regions
     if (scenes[i].n_particles > nmax) nmax = scenes[i].n_particles;
   }
   const int64_t lim = (1ll << 31) - (1ll << 20);
@@ -447,7 +450,7 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
       wtiles.push_back(Tile{i, woff + b, woff + std::min(b + s->wtile, cells)});
     poff += d.n_particles;
     coff += s->sd.back().ncells;
-    woff += cells;
+    woff += (cells + 31) / 32 * 32;
   }
   s->n_ptiles = (int32_t)ptiles.size();
   s->n_wtiles = (int32_t)wtiles.size();
@@ -471,6 +474,8 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   ALLOC(s->key, N);
   ALLOC(s->slot, N);
   ALLOC(s->list, N);
+  ALLOC(s->nbr, N * kMaxNbr);
+  ALLOC(s->nbr_cnt, N);
   ALLOC(s->count, (size_t)s->c_total);
   ALLOC(s->start, (size_t)s->c_total + 1);
   {

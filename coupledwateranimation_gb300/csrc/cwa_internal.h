@@ -94,13 +94,17 @@ cudaError_t launch_point_rank(const int32_t* key, const int32_t* slot, const int
                               cudaStream_t stream);
 
 // ---- SPH kernels (cwa_sph.cu) ----
+// Neighbour list: nbr[k * n_total + i] (k < kMaxNbr) and nbr_cnt[i], written
+// by rho_pres, read by force.
+constexpr int kMaxNbr = 64;
 cudaError_t launch_rho_pres(int precision, const float4* pos, const int32_t* start, const Tile* tiles,
                             int32_t n_tiles, int32_t tile_size, const SceneDev* scenes,
-                            const float* wave_u, float2* rho_p, cudaStream_t stream);
+                            const float* wave_u, float2* rho_p, int32_t* nbr, int32_t* nbr_cnt,
+                            int32_t n_total, cudaStream_t stream);
 cudaError_t launch_force(int precision, const float4* pos, const float4* vel, const float2* rho_p,
                          const int32_t* start, const Tile* tiles, int32_t n_tiles, int32_t tile_size,
-                         const SceneDev* scenes, const float* wave_u, float4* force,
-                         cudaStream_t stream);
+                         const SceneDev* scenes, const float* wave_u, float4* force, const int32_t* nbr,
+                         const int32_t* nbr_cnt, int32_t n_total, cudaStream_t stream);
 
 // ---- integrate / wave / packing kernels (cwa_step.cu) ----
 cudaError_t launch_integrate(float4* pos, float4* vel, float4* force, float2* rho_p, const Tile* tiles,

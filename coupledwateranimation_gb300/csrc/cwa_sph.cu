@@ -12,6 +12,8 @@
 // loop visits exactly those rows.  Every pair with r < h lies inside them,
 // so the neighbour sets equal the shaders'.  Lanes of a warp that sit in the
 // same cell walk the same rows in lock step, so their loads broadcast.
+// rho_pres does the candidate tests once and leaves each particle's hits as
+// a neighbour list; force then runs its pair terms over that list only.
 //
 // Sums are accumulated in one of three precisions (template P):
 //   CWA_PREC_FP32 plain float, CWA_PREC_COMPENSATED float with a two-sum
@@ -72,21 +74,23 @@ __device__ __forceinline__ CellCoord cell_of(const SceneDev* S, float4 p) {
   return c;
 }
 
-// Calls body(j) for every sorted index j of the 27 cells around c, row by
-// row (x outer, y inner, contiguous z range).
-template <class Body>
-__device__ __forceinline__ void for_block27(const SceneDev* S, const int32_t* __restrict__ start,
-                                            CellCoord c, Body body) {
+// Sorted-index ranges [b, e) of the 9 z-rows that hold the 27 cells around
+// c (x outer, y inner); rows outside the grid are empty.  All 18 loads are
+// independent, so they overlap.
+__device__ __forceinline__ void row_ranges(const SceneDev* S, const int32_t* __restrict__ start, CellCoord c,
+                                           int b[9], int e[9]) {
   const int nx = S->dims[0], ny = S->dims[1], nz = S->dims[2];
   const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, nz - 1);
-  const int x0 = max(c.x - 1, 0), x1 = min(c.x + 1, nx - 1);
-  const int y0 = max(c.y - 1, 0), y1 = min(c.y + 1, ny - 1);
-  for (int x = x0; x <= x1; ++x) {
-    for (int y = y0; y <= y1; ++y) {
+#pragma unroll
+  for (int dx = -1; dx <= 1; ++dx) {
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int r = (dx + 1) * 3 + (dy + 1);
+      const int x = c.x + dx, y = c.y + dy;
+      const bool ok = x >= 0 && x < nx && y >= 0 && y < ny;
       const int row = S->coff + (x * ny + y) * nz;
-      const int b = __ldg(start + row + z0);
-      const int e = __ldg(start + row + z1 + 1);
-      for (int j = b; j < e; ++j) body(j);
+      b[r] = ok ? __ldg(start + row + z0) : 0;
+      e[r] = ok ? __ldg(start + row + z1 + 1) : 0;
     }
   }
 }
@@ -94,11 +98,21 @@ __device__ __forceinline__ void for_block27(const SceneDev* S, const int32_t* __
 __device__ __forceinline__ float uv_s(const SceneDev* S, float x) { return x * S->uvs[0] + S->uvo[0]; }
 __device__ __forceinline__ float uv_t(const SceneDev* S, float z) { return z * S->uvs[1] + S->uvo[1]; }
 
+// Neighbour-list capacity per particle.  ~33 neighbours at rest density with
+// h = 2 s; a particle with more falls back to the candidate scan in force.
+constexpr int kNbThreads = 128;
+
+// rho_pres: tests every candidate of the 27-cell block once, accumulates
+// the poly6 sum branch-free per row (q = max(h^2 - r^2, 0), sum of q^3 in
+// float within a row, rows combined by the precision mode's accumulator),
+// and writes the hits (r < h, j != i) as the particle's neighbour list
+// nbr[k * n_total + i], k < kMaxNbr, which the force pass consumes.
 template <int P>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kNbThreads)
     k_rho_pres(const float4* __restrict__ pos, const int32_t* __restrict__ start,
                const Tile* __restrict__ tiles, const SceneDev* __restrict__ scenes,
-               const float* __restrict__ wave, float2* __restrict__ rho_p) {
+               const float* __restrict__ wave, float2* __restrict__ rho_p, int32_t* __restrict__ nbr,
+               int32_t* __restrict__ nbr_cnt, int32_t n_total) {
   using T = Real<P>;
   const Tile tl = tiles[blockIdx.x];
   const int i = tl.begin + threadIdx.x;
@@ -108,16 +122,28 @@ __global__ void __launch_bounds__(128)
   const T hh = (T)S->h;
   const T h2 = hh * hh;
   const T px = pi.x, py = pi.y, pz = pi.z;
+  int b[9], e[9];
+  row_ranges(S, start, cell_of(S, pi), b, e);
   Sum<P> acc;
-  for_block27(S, start, cell_of(S, pi), [&](int j) {
-    const float4 pj = __ldg(pos + j);
-    const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
-    const T r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 < h2) {
-      const T q = h2 - r2;
-      acc.add(q * q * q);
+  int cnt = 0;
+#pragma unroll
+  for (int r = 0; r < 9; ++r) {
+    T part = (T)0;
+#pragma unroll 4
+    for (int j = b[r]; j < e[r]; ++j) {
+      const float4 pj = __ldg(pos + j);
+      const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
+      const T q = h2 - (dx * dx + dy * dy + dz * dz);
+      const T qp = q > (T)0 ? q : (T)0;
+      part += qp * qp * qp;
+      if (q > (T)0 && j != i) {
+        if (cnt < kMaxNbr) nbr[(size_t)cnt * n_total + i] = j;
+        ++cnt;
+      }
     }
-  });
+    acc.add(part);
+  }
+  nbr_cnt[i] = cnt;
   const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
   float rho = (float)rho_t;
   float p = S->k * (rho - S->rho0);
@@ -133,12 +159,48 @@ __global__ void __launch_bounds__(128)
   rho_p[i] = make_float2(rho, p);
 }
 
+// Three-component sum in the precision mode: COMPENSATED adds pair terms
+// in float into a partial that is folded into a two-sum accumulator every
+// 8 terms (cascaded summation); FP32 is plain; FP64 is double.
 template <int P>
-__global__ void __launch_bounds__(128)
+struct Acc3 {
+  Sum<P> x, y, z;
+  Real<P> px = 0, py = 0, pz = 0;
+  int n = 0;
+  __device__ __forceinline__ void add(Real<P> a, Real<P> b, Real<P> c) {
+    if (P == CWA_PREC_COMPENSATED) {
+      px += a;
+      py += b;
+      pz += c;
+      if (++n == 8) flush();
+    } else {
+      x.add(a);
+      y.add(b);
+      z.add(c);
+    }
+  }
+  __device__ __forceinline__ void flush() {
+    if (P == CWA_PREC_COMPENSATED) {
+      x.add(px);
+      y.add(py);
+      z.add(pz);
+      px = py = pz = 0;
+      n = 0;
+    }
+  }
+};
+
+// force: spiky pressure gradient + viscosity Laplacian over the neighbour
+// list written by rho_pres (same pairs, same order as the candidate scan),
+// then the preset's extra terms.  A particle whose list overflowed rescans
+// its 27-cell block.
+template <int P>
+__global__ void __launch_bounds__(kNbThreads)
     k_force(const float4* __restrict__ pos, const float4* __restrict__ vel,
             const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
             const Tile* __restrict__ tiles, const SceneDev* __restrict__ scenes,
-            const float* __restrict__ wave, float4* __restrict__ force) {
+            const float* __restrict__ wave, float4* __restrict__ force, const int32_t* __restrict__ nbr,
+            const int32_t* __restrict__ nbr_cnt, int32_t n_total) {
   using T = Real<P>;
   const Tile tl = tiles[blockIdx.x];
   const int i = tl.begin + threadIdx.x;
@@ -151,32 +213,46 @@ __global__ void __launch_bounds__(128)
   const T h2 = hh * hh;
   const T px = pi.x, py = pi.y, pz = pi.z;
   const T vx = vi.x, vy = vi.y, vz = vi.z, pres_i = rpi.y;
-  Sum<P> fpx, fpy, fpz, fvx, fvy, fvz;
-  for_block27(S, start, cell_of(S, pi), [&](int j) {
+  Acc3<P> fp, fv;
+  auto pair = [&](int j) {
     const float4 pj = __ldg(pos + j);
+    const float4 vj = __ldg(vel + j);
+    const float2 rpj = __ldg(rho_p + j);
     const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
     const T r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 < h2 && j != i) {
-      const float4 vj = __ldg(vel + j);
-      const float2 rpj = __ldg(rho_p + j);
-      const T inv_r = r2 > (T)0 ? inv_sqrt(r2) : (T)0;  // normalize(0) := 0
-      const T r = r2 * inv_r;
-      const T hr = hh - r;
-      const T irho = recip((T)rpj.x);
-      const T sp = (pres_i + (T)rpj.y) * irho * hr * hr * inv_r;
-      fpx.add(sp * dx);
-      fpy.add(sp * dy);
-      fpz.add(sp * dz);
-      const T sv = irho * hr;
-      fvx.add(sv * ((T)vj.x - vx));
-      fvy.add(sv * ((T)vj.y - vy));
-      fvz.add(sv * ((T)vj.z - vz));
+    const T inv_r = r2 > (T)0 ? inv_sqrt(r2) : (T)0;  // normalize(0) := 0
+    const T r = r2 * inv_r;
+    const T hr = hh - r;
+    const T irho = recip((T)rpj.x);
+    const T sp = (pres_i + (T)rpj.y) * irho * hr * hr * inv_r;
+    fp.add(sp * dx, sp * dy, sp * dz);
+    const T sv = irho * hr;
+    fv.add(sv * ((T)vj.x - vx), sv * ((T)vj.y - vy), sv * ((T)vj.z - vz));
+  };
+  const int cnt = __ldg(nbr_cnt + i);
+  if (cnt <= kMaxNbr) {
+    int jn = cnt > 0 ? __ldg(nbr + i) : 0;
+    for (int k = 0; k < cnt; ++k) {
+      const int j = jn;
+      if (k + 1 < cnt) jn = __ldg(nbr + (size_t)(k + 1) * n_total + i);
+      pair(j);
     }
-  });
+  } else {
+    int b[9], e[9];
+    row_ranges(S, start, cell_of(S, pi), b, e);
+    for (int r = 0; r < 9; ++r)
+      for (int j = b[r]; j < e[r]; ++j) {
+        const float4 pj = __ldg(pos + j);
+        const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
+        if (h2 - (dx * dx + dy * dy + dz * dz) > (T)0 && j != i) pair(j);
+      }
+  }
+  fp.flush();
+  fv.flush();
   const T cg = P == CWA_PREC_FP64 ? (T)S->k_grad_d * (T)S->mass : (T)(S->k_grad * S->mass);
   const T cp = (T)0.5 * cg;
-  float fp[3] = {(float)(cp * fpx.get()), (float)(cp * fpy.get()), (float)(cp * fpz.get())};
-  float fv[3] = {(float)(cg * fvx.get()), (float)(cg * fvy.get()), (float)(cg * fvz.get())};
+  float fpr[3] = {(float)(cp * fp.x.get()), (float)(cp * fp.y.get()), (float)(cp * fp.z.get())};
+  float fvr[3] = {(float)(cg * fv.x.get()), (float)(cg * fv.y.get()), (float)(cg * fv.z.get())};
   const float rho = rpi.x;
   float4 out;
   if (S->preset == CWA_PRESET_REFERENCE_3D) {
@@ -209,12 +285,12 @@ __global__ void __launch_bounds__(128)
     for (int c = 0; c < 3; ++c) {
       const float drag = -0.25f * (vv[c] - wv[c]);
       const float wf = -H * nrm[c] * 0.5f;
-      f[c] = fp[c] + fv[c] * vs + rho * S->g[c] + tq[c] + drag + wf;
+      f[c] = fpr[c] + fvr[c] * vs + rho * S->g[c] + tq[c] + drag + wf;
     }
     out = make_float4(f[0], f[1], f[2], fprev.w);
   } else {
-    out = make_float4(fp[0] + fv[0] * S->visc + rho * S->g[0], fp[1] + fv[1] * S->visc + rho * S->g[1],
-                      fp[2] + fv[2] * S->visc + rho * S->g[2], 0.0f);
+    out = make_float4(fpr[0] + fvr[0] * S->visc + rho * S->g[0], fpr[1] + fvr[1] * S->visc + rho * S->g[1],
+                      fpr[2] + fvr[2] * S->visc + rho * S->g[2], 0.0f);
   }
   force[i] = out;
 }
@@ -223,39 +299,42 @@ __global__ void __launch_bounds__(128)
 
 cudaError_t launch_rho_pres(int precision, const float4* pos, const int32_t* start, const Tile* tiles,
                             int32_t n_tiles, int32_t tile_size, const SceneDev* scenes,
-                            const float* wave_u, float2* rho_p, cudaStream_t stream) {
+                            const float* wave_u, float2* rho_p, int32_t* nbr, int32_t* nbr_cnt,
+                            int32_t n_total, cudaStream_t stream) {
   if (n_tiles <= 0) return cudaSuccess;
   switch (precision) {
     case CWA_PREC_FP32:
-      k_rho_pres<CWA_PREC_FP32><<<n_tiles, tile_size, 0, stream>>>(pos, start, tiles, scenes, wave_u, rho_p);
+      k_rho_pres<CWA_PREC_FP32><<<n_tiles, tile_size, 0, stream>>>(pos, start, tiles, scenes, wave_u, rho_p, nbr,
+                                                                   nbr_cnt, n_total);
       break;
     case CWA_PREC_FP64:
-      k_rho_pres<CWA_PREC_FP64><<<n_tiles, tile_size, 0, stream>>>(pos, start, tiles, scenes, wave_u, rho_p);
+      k_rho_pres<CWA_PREC_FP64><<<n_tiles, tile_size, 0, stream>>>(pos, start, tiles, scenes, wave_u, rho_p, nbr,
+                                                                   nbr_cnt, n_total);
       break;
     default:
       k_rho_pres<CWA_PREC_COMPENSATED><<<n_tiles, tile_size, 0, stream>>>(pos, start, tiles, scenes, wave_u,
-                                                                          rho_p);
+                                                                          rho_p, nbr, nbr_cnt, n_total);
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_force(int precision, const float4* pos, const float4* vel, const float2* rho_p,
                          const int32_t* start, const Tile* tiles, int32_t n_tiles, int32_t tile_size,
-                         const SceneDev* scenes, const float* wave_u, float4* force,
-                         cudaStream_t stream) {
+                         const SceneDev* scenes, const float* wave_u, float4* force, const int32_t* nbr,
+                         const int32_t* nbr_cnt, int32_t n_total, cudaStream_t stream) {
   if (n_tiles <= 0) return cudaSuccess;
   switch (precision) {
     case CWA_PREC_FP32:
       k_force<CWA_PREC_FP32><<<n_tiles, tile_size, 0, stream>>>(pos, vel, rho_p, start, tiles, scenes, wave_u,
-                                                                force);
+                                                                force, nbr, nbr_cnt, n_total);
       break;
     case CWA_PREC_FP64:
       k_force<CWA_PREC_FP64><<<n_tiles, tile_size, 0, stream>>>(pos, vel, rho_p, start, tiles, scenes, wave_u,
-                                                                force);
+                                                                force, nbr, nbr_cnt, n_total);
       break;
     default:
       k_force<CWA_PREC_COMPENSATED><<<n_tiles, tile_size, 0, stream>>>(pos, vel, rho_p, start, tiles, scenes,
-                                                                       wave_u, force);
+                                                                       wave_u, force, nbr, nbr_cnt, n_total);
   }
   return cudaGetLastError();
 }

@@ -122,36 +122,81 @@ __global__ void __launch_bounds__(128)
   vel[i] = make_float4(v[0], v[1], v[2], v0.w);
 }
 
-// EvolveWave (wave_comp.glsl:348-383) with get_clamp borders, plus the
-// particle deposits, which it reads and clears for the next step.
+// One cell of EvolveWave (wave_comp.glsl:348-383) with get_clamp borders,
+// plus the particle deposit d: one rounding per operation, in the order the
+// float32 restatement uses.
+__device__ __forceinline__ float evolve_cell(const SceneDev* S, float c0, float c1, float nn, float ss, float ee,
+                                             float ww, int i, long long d) {
+  const float nb = fadd(fadd(nn, ss), fadd(ee, ww));
+  float w = fadd(fmul(S->wa, c0), fmul(S->lam, nb));
+  w = fsub(w, fmul(S->wb, c1));
+  w = fmul(S->atten, w);
+  if (S->line_source && w > 0.0001f && i == S->nx / 2) w = fadd(w, 0.001f);
+  if (S->coupled) w = fadd(w, fmul(S->gain, fmul(__ll2float_rn(d), S->dq)));
+  return w;
+}
+
+// The wave pass over every scene: a tile is kWaveCellsPerThread x blockDim
+// cells of one scene.  Rows whose width is a multiple of 4 take the float4
+// path (4 cells per thread: three float4 rows, two edge scalars, the
+// previous field and two 16-byte deposit loads, all independent); other
+// widths take the scalar path.  Deposits are read and cleared here.
+constexpr int kWaveCellsPerThread = 4;
+
 __global__ void __launch_bounds__(256)
     k_wave(const float* __restrict__ un, const float* __restrict__ unm1, float* __restrict__ uout,
            unsigned long long* __restrict__ deposits, const Tile* __restrict__ tiles,
            const SceneDev* __restrict__ scenes) {
   const Tile tl = tiles[blockIdx.x];
-  const int c = tl.begin + threadIdx.x;
-  if (c >= tl.end) return;
   const SceneDev* S = scenes + tl.scene;
-  const int W = S->nx, H = S->nz;
-  const int local = c - S->woff;
-  const int j = local / W, i = local - j * W;
-  const float* u = un + S->woff;
-  const float c0 = u[local], c1 = unm1[c];
-  const float nn = u[min(j + 1, H - 1) * W + i];
-  const float ss = u[max(j - 1, 0) * W + i];
-  const float ee = u[j * W + min(i + 1, W - 1)];
-  const float ww = u[j * W + max(i - 1, 0)];
-  const float nb = fadd(fadd(nn, ss), fadd(ee, ww));
-  float w = fadd(fmul(S->wa, c0), fmul(S->lam, nb));
-  w = fsub(w, fmul(S->wb, c1));
-  w = fmul(S->atten, w);
-  if (S->line_source && w > 0.0001f && i == W / 2) w = fadd(w, 0.001f);
-  if (S->coupled) {
-    const long long d = (long long)deposits[c];
-    deposits[c] = 0ull;
-    w = fadd(w, fmul(S->gain, fmul(__ll2float_rn(d), S->dq)));
+  const int W = S->nx, H = S->nz, woff = S->woff;
+  const int local0 = tl.begin - woff + threadIdx.x * kWaveCellsPerThread;
+  if (local0 + woff >= tl.end) return;
+  const float* u = un + woff;
+  const float* um = unm1 + woff;
+  float* uo = uout + woff;
+  unsigned long long* dep = deposits + woff;
+  if ((W & 3) == 0) {
+    const int j = local0 / W, i = local0 - j * W;
+    const float4 C = __ldg(reinterpret_cast<const float4*>(u + local0));
+    const float4 N = j + 1 < H ? __ldg(reinterpret_cast<const float4*>(u + local0 + W)) : C;
+    const float4 Sd = j > 0 ? __ldg(reinterpret_cast<const float4*>(u + local0 - W)) : C;
+    const float west = i > 0 ? __ldg(u + local0 - 1) : C.x;
+    const float east = i + 4 < W ? __ldg(u + local0 + 4) : C.w;
+    const float4 P = __ldg(reinterpret_cast<const float4*>(um + local0));
+    long long d[4] = {0, 0, 0, 0};
+    if (S->coupled) {
+      const longlong2 a = *reinterpret_cast<const longlong2*>(dep + local0);
+      const longlong2 b = *reinterpret_cast<const longlong2*>(dep + local0 + 2);
+      d[0] = a.x;
+      d[1] = a.y;
+      d[2] = b.x;
+      d[3] = b.y;
+      *reinterpret_cast<longlong2*>(dep + local0) = make_longlong2(0, 0);
+      *reinterpret_cast<longlong2*>(dep + local0 + 2) = make_longlong2(0, 0);
+    }
+    float4 o;
+    o.x = evolve_cell(S, C.x, P.x, N.x, Sd.x, C.y, west, i, d[0]);
+    o.y = evolve_cell(S, C.y, P.y, N.y, Sd.y, C.z, C.x, i + 1, d[1]);
+    o.z = evolve_cell(S, C.z, P.z, N.z, Sd.z, C.w, C.y, i + 2, d[2]);
+    o.w = evolve_cell(S, C.w, P.w, N.w, Sd.w, east, C.z, i + 3, d[3]);
+    *reinterpret_cast<float4*>(uo + local0) = o;
+  } else {
+    const int ncell = W * H;
+#pragma unroll
+    for (int k = 0; k < kWaveCellsPerThread; ++k) {
+      const int local = local0 + k;
+      if (local >= ncell) break;
+      const int j = local / W, i = local - j * W;
+      long long d = 0;
+      if (S->coupled) {
+        d = (long long)dep[local];
+        dep[local] = 0ull;
+      }
+      uo[local] = evolve_cell(S, u[local], um[local], u[min(j + 1, H - 1) * W + i], u[max(j - 1, 0) * W + i],
+                              u[j * W + min(i + 1, W - 1)], u[j * W + max(i - 1, 0)], i, d);
+    }
   }
-  uout[c] = w;
 }
 
 // InitWave (wave_comp.glsl:259-317): peak * smoothstep(5, 0, d) around two
@@ -300,7 +345,7 @@ cudaError_t launch_wave(const float* u_n, const float* u_nm1, float* u_out, unsi
                         const Tile* wtiles, int32_t n_wtiles, int32_t wtile_size, const SceneDev* scenes,
                         cudaStream_t stream) {
   if (n_wtiles <= 0) return cudaSuccess;
-  k_wave<<<n_wtiles, wtile_size, 0, stream>>>(u_n, u_nm1, u_out, deposits, wtiles, scenes);
+  k_wave<<<n_wtiles, wtile_size / kWaveCellsPerThread, 0, stream>>>(u_n, u_nm1, u_out, deposits, wtiles, scenes);
   return cudaGetLastError();
 }
 

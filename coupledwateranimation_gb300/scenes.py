@@ -93,8 +93,12 @@ def config0(seed=BASE_SEED) -> Workload:
 
 
 def config1(seed=BASE_SEED) -> Workload:
-    return Workload("c1: 128^3 particles s=0.0075, 1024^2 wave",
-                    [dam_break((128, 128, 128), 0.0075, (1024, 1024), seed=seed)], 500)
+    # The workload is stated as 1,048,576 particles on a "128^3" lattice, which
+    # disagree (128^3 = 2,097,152); the particle count is kept: 128 x 64 x 128
+    # (x, y, z), a 0.96 x 0.48 x 0.96 block.
+    return Workload("c1: 1,048,576 particles (128x64x128, s=0.0075), 1024^2 wave",
+                    [dam_break((128, 64, 128), 0.0075, (1024, 1024), seed=seed)], 500,
+                    notes="128x64x128 lattice keeps the stated 1,048,576 particles")
 
 
 def config2(seed=BASE_SEED) -> Workload:

@@ -177,6 +177,24 @@ def test_integrate_and_deposits_bit_exact(lib, orc, preset):
         assert np.count_nonzero(sim.download_deposits(0)) == 0  # the wave pass clears them
 
 
+@pytest.mark.parametrize("wave", [(37, 29), (64, 20), (4, 3)])
+def test_wave_pass_bit_exact_any_width(lib, orc, wave):
+    # widths that are not a multiple of 4 take the scalar path of the wave kernel
+    sc = small_muller((10, 10, 10), 0.03, wave)
+    with Sim(sc.desc) as sim:
+        load_scene(sim, 0, sc)
+        sim.step(2)
+        sim.grid()
+        sim.rho_pres()
+        sim.force()
+        sim.integrate()
+        dep = sim.download_deposits(0)
+        u_n, u_nm1 = sim.download_wave(0)
+        sim.wave()
+        got, _ = sim.download_wave(0)
+    assert np.array_equal(bits(got), bits(orc.wave_f32(sc.desc, u_n, u_nm1, dep)))
+
+
 @pytest.mark.parametrize("mode", [1.0, 0.0, 0.5])
 def test_wave_init_bit_exact(lib, orc, mode):
     sc = small_reference(64)
@@ -310,7 +328,8 @@ def _run(scene_list, steps, **kw):
 def test_batched_equals_single(lib):
     scs = [small_muller((10, 12, 14), 0.02, (64, 32), seed=1),
            small_muller((20, 8, 8), 0.03, (48, 48), seed=2),
-           scenes.dam_break((9, 9, 9), 0.025, (40, 72), box_hi=(1.5, 1.0, 1.0), seed=3)]
+           scenes.dam_break((9, 9, 9), 0.025, (40, 72), box_hi=(1.5, 1.0, 1.0), seed=3),
+           small_muller((7, 9, 11), 0.03, (37, 21), seed=4)]
     together = _run(scs, 12)
     for k, s in enumerate(scs):
         alone = _run([s], 12)[0]
