@@ -97,6 +97,13 @@ class ClockSampler:
                 self.proc.kill()
             self.fh.close()
 
+    def lines(self) -> int:
+        try:
+            self.fh.flush()
+            return len(self.path.read_text().splitlines())
+        except Exception:
+            return 99
+
     def summary(self) -> dict:
         if not self.proc or not self.path.exists():
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
@@ -195,9 +202,14 @@ def run_gpu(args) -> None:
     n_units = wl.n_particles + wl.n_wave_cells
 
     clk = ClockSampler(local).__enter__()  # samples across warm-up, timed steps, profile and e2e
-    # warm-up (graph capture happens here)
+    # warm-up (graph capture happens here); keep the GPU loaded until the
+    # clock sampler is logging, at most ~5 s
     sim.step(args.warmup)
     sim.synchronize()
+    t_w = time.perf_counter()
+    while clk.lines() < 3 and time.perf_counter() - t_w < 5.0:
+        sim.step(20)
+        sim.synchronize()
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]

@@ -58,7 +58,7 @@ class SceneDesc(C.Structure):
 
 class SimOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("use_graph", C.c_int32),
-                ("nb_threads", C.c_int32), ("reserved", C.c_int32 * 8)]
+                ("nb_threads", C.c_int32), ("nb_stage", C.c_int32), ("reserved", C.c_int32 * 7)]
 
 
 class DeviceView(C.Structure):

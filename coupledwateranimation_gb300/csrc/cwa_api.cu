@@ -51,7 +51,7 @@ struct cwa_sim {
   int32_t* list = nullptr;
   int32_t* count = nullptr;
   int32_t* start = nullptr;
-  int32_t* nbr = nullptr;      // neighbour lists, kMaxNbr x n_total
+  uint16_t* nbr = nullptr;     // neighbour lists, kMaxNbr x n_total codes
   int32_t* nbr_cnt = nullptr;
   void* scan_ws = nullptr;
   ScanWorkspace scan{};
@@ -241,7 +241,8 @@ cwa_status run_grid(cwa_sim* s) {
 
 cwa_status run_rho_pres(cwa_sim* s) {
   CWA_CUDA(launch_rho_pres(s->opt.precision, s->P[s->cur], s->start, s->d_ptiles, s->n_ptiles, s->ptile,
-                           s->d_scenes, s->U[s->wcur], s->RP, s->nbr, s->nbr_cnt, s->n_total, s->stream));
+                           s->d_scenes, s->U[s->wcur], s->RP, s->nbr, s->nbr_cnt, s->n_total, s->d_status,
+                           s->opt.nb_stage >= 0 ? 1 : 0, s->stream));
   s->launches += s->n_ptiles > 0;
   return CWA_OK;
 }
@@ -395,6 +396,7 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   o.use_graph = 1;
   if (opt) o = *opt;
   if (o.precision < CWA_PREC_FP32 || o.precision > CWA_PREC_FP64) return arg_error("unknown precision");
+  if (o.nb_stage < -1 || o.nb_stage > 1) return arg_error("nb_stage must be -1, 0 or 1");
   if (o.nb_threads != 0 && (o.nb_threads < 32 || o.nb_threads > 128 || (o.nb_threads & 31)))
     return arg_error("nb_threads must be 0 or a multiple of 32 in [32, 128]");
   std::vector<int32_t> dims(3 * (size_t)n_scenes);

@@ -94,16 +94,19 @@ cudaError_t launch_point_rank(const int32_t* key, const int32_t* slot, const int
                               cudaStream_t stream);
 
 // ---- SPH kernels (cwa_sph.cu) ----
-// Neighbour list: nbr[k * n_total + i] (k < kMaxNbr) and nbr_cnt[i], written
-// by rho_pres, read by force.
+// Neighbour list: nbr[k * n_total + i] (k < kMaxNbr) holds 16-bit hit codes
+// (row << 12 | offset in the row's sorted range; the particle itself is one
+// of them) and nbr_cnt[i] their count (kMaxNbr + 1 = overflow, force
+// rescans); written by rho_pres, read by force.  stage != 0 lets rho_pres
+// stage candidate rows in shared memory.
 constexpr int kMaxNbr = 64;
 cudaError_t launch_rho_pres(int precision, const float4* pos, const int32_t* start, const Tile* tiles,
                             int32_t n_tiles, int32_t tile_size, const SceneDev* scenes,
-                            const float* wave_u, float2* rho_p, int32_t* nbr, int32_t* nbr_cnt,
-                            int32_t n_total, cudaStream_t stream);
+                            const float* wave_u, float2* rho_p, uint16_t* nbr, int32_t* nbr_cnt,
+                            int32_t n_total, int32_t* status, int32_t stage, cudaStream_t stream);
 cudaError_t launch_force(int precision, const float4* pos, const float4* vel, const float2* rho_p,
                          const int32_t* start, const Tile* tiles, int32_t n_tiles, int32_t tile_size,
-                         const SceneDev* scenes, const float* wave_u, float4* force, const int32_t* nbr,
+                         const SceneDev* scenes, const float* wave_u, float4* force, const uint16_t* nbr,
                          const int32_t* nbr_cnt, int32_t n_total, cudaStream_t stream);
 
 // ---- integrate / wave / packing kernels (cwa_step.cu) ----

@@ -10,15 +10,24 @@
 // particles are sorted by uniform-grid cell (cell edge >= h), so the 27-cell
 // block around a particle is 9 contiguous z-rows of the sorted arrays; the
 // loop visits exactly those rows.  Every pair with r < h lies inside them,
-// so the neighbour sets equal the shaders'.  Lanes of a warp that sit in the
-// same cell walk the same rows in lock step, so their loads broadcast.
-// rho_pres does the candidate tests once and leaves each particle's hits as
-// a neighbour list; force then runs its pair terms over that list only.
+// so the neighbour sets equal the shaders'.
+//
+// rho_pres does the candidate tests once.  A CTA owns up to 128 consecutive
+// sorted particles, which lie in one or two grid columns; it copies the
+// candidate rows of those columns into shared memory with bulk TMA copies
+// (cp.async.bulk, completion on an mbarrier) and tests every candidate from
+// shared memory.  Each particle's hits are kept as a neighbour list of 16-bit
+// codes (row << 12 | offset in the row's sorted range), which force decodes
+// with the same 9 row starts and runs its pair terms over.  CTAs whose
+// particles span more columns, or whose rows exceed the staging capacity,
+// read candidates straight from global memory (same order, same results).
 //
 // Sums are accumulated in one of three precisions (template P):
-//   CWA_PREC_FP32 plain float, CWA_PREC_COMPENSATED float with a two-sum
-//   error term (Knuth), CWA_PREC_FP64 double pair math and sums.
+//   CWA_PREC_FP32 plain float; CWA_PREC_COMPENSATED float partial sums
+//   (per row for density, per 8 pairs for force) folded into a Knuth two-sum
+//   accumulator; CWA_PREC_FP64 double pair math and sums.
 #include <cuda_runtime.h>
+#include <stdint.h>
 
 #include <type_traits>
 
@@ -75,7 +84,7 @@ __device__ __forceinline__ CellCoord cell_of(const SceneDev* S, float4 p) {
 }
 
 // Sorted-index ranges [b, e) of the 9 z-rows that hold the 27 cells around
-// c (x outer, y inner); rows outside the grid are empty.  All 18 loads are
+// c (x outer, y inner); rows outside the grid are empty.  The 18 loads are
 // independent, so they overlap.
 __device__ __forceinline__ void row_ranges(const SceneDev* S, const int32_t* __restrict__ start, CellCoord c,
                                            int b[9], int e[9]) {
@@ -98,52 +107,200 @@ __device__ __forceinline__ void row_ranges(const SceneDev* S, const int32_t* __r
 __device__ __forceinline__ float uv_s(const SceneDev* S, float x) { return x * S->uvs[0] + S->uvo[0]; }
 __device__ __forceinline__ float uv_t(const SceneDev* S, float z) { return z * S->uvs[1] + S->uvo[1]; }
 
-// Neighbour-list capacity per particle.  ~33 neighbours at rest density with
-// h = 2 s; a particle with more falls back to the candidate scan in force.
+// ---- shared-memory staging with bulk TMA copies --------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// Global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on phase 0 of the staging barrier.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar) {
+  for (int k = 0; k < (1 << 20); ++k)
+    if (mbar_try_wait(bar, 0)) return true;
+  return false;
+}
+
 constexpr int kNbThreads = 128;
+constexpr int kStageCap = 1536;   // staged candidates per CTA (24 KB)
+constexpr int kRowCodeBits = 12;  // a hit is (row << 12) | offset in the row
+constexpr int kRowCodeMax = 1 << kRowCodeBits;
+constexpr int kMaxSegs = 18;      // 2 columns x 9 rows
+
+struct StagePlan {
+  int32_t seg_b[kMaxSegs];        // global sorted index of each staged segment
+  int32_t seg_off[kMaxSegs + 1];  // staged offset (prefix of lengths)
+  int32_t col0;                   // first column (x*ny + y) of the CTA
+  int32_t ncols;                  // 1 or 2; 0 = read from global memory
+};
+
+// Warp 0 plans the CTA's staging: the columns its particles occupy and, per
+// column, the candidate rows over the z-range its particles need (+-1 cell).
+__device__ __forceinline__ void plan_stage(const SceneDev* S, const int32_t* __restrict__ start,
+                                           const float4* __restrict__ pos, const Tile& tl, StagePlan& sp) {
+  const int lane = threadIdx.x & 31;
+  const CellCoord a = cell_of(S, __ldg(pos + tl.begin));
+  const CellCoord b = cell_of(S, __ldg(pos + tl.end - 1));
+  const int nx = S->dims[0], ny = S->dims[1], nz = S->dims[2];
+  const int colA = a.x * ny + a.y, colB = b.x * ny + b.y;
+  const int ncols = colB - colA + 1;
+  int len = 0, gb = 0;
+  if (ncols <= 2 && lane < 9 * ncols) {
+    const int g = lane / 9, r = lane % 9;
+    const int col = colA + g;
+    const int cx = col / ny, cy = col - cx * ny;
+    const int zlo = g == 0 ? max(a.z - 1, 0) : 0;
+    const int zhi = (g == ncols - 1) ? min(b.z + 1, nz - 1) : nz - 1;
+    const int x = cx + r / 3 - 1, y = cy + r % 3 - 1;
+    if (x >= 0 && x < nx && y >= 0 && y < ny) {
+      const int row = S->coff + (x * ny + y) * nz;
+      gb = __ldg(start + row + zlo);
+      len = __ldg(start + row + zhi + 1) - gb;
+    }
+  }
+  int incl = len;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  if (lane < kMaxSegs) {
+    sp.seg_b[lane] = gb;
+    sp.seg_off[lane] = incl - len;
+  }
+  if (lane == 0) {
+    sp.seg_off[kMaxSegs] = total;
+    sp.col0 = colA;
+    sp.ncols = (ncols <= 2 && total <= kStageCap) ? ncols : 0;
+  }
+}
+
+// Candidate test of one row: poly6 partial sum; every hit (r < h, the
+// particle itself included) is appended to the lane's code list.  The list
+// pointer advances by one slot per hit and is clamped at the overflow slot,
+// so the loop has no branch; a list that reached the overflow slot is
+// marked overflowed by the caller.
+template <class T, class Load>
+__device__ __forceinline__ T scan_row(Load load, int len, uint32_t row_code, T px, T py, T pz, T h2,
+                                      uint16_t*& hp, uint16_t* hp_end) {
+  T part = (T)0;
+#pragma unroll 4
+  for (int o = 0; o < len; ++o) {
+    const float4 pj = load(o);
+    const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
+    T q = fma(-dx, dx, h2);
+    q = fma(-dy, dy, q);
+    q = fma(-dz, dz, q);
+    const T qp = q > (T)0 ? q : (T)0;
+    part = fma(qp * qp, qp, part);
+    if (q > (T)0) {
+      *hp = (uint16_t)(row_code + (uint32_t)o);
+      hp += kNbThreads;
+    }
+    hp = hp < hp_end ? hp : hp_end;
+  }
+  return part;
+}
 
 // rho_pres: tests every candidate of the 27-cell block once, accumulates
 // the poly6 sum branch-free per row (q = max(h^2 - r^2, 0), sum of q^3 in
-// float within a row, rows combined by the precision mode's accumulator),
-// and writes the hits (r < h, j != i) as the particle's neighbour list
-// nbr[k * n_total + i], k < kMaxNbr, which the force pass consumes.
+// the row, rows folded by the precision mode's accumulator) and keeps the
+// hits (r < h, j != i) as the particle's neighbour list.
 template <int P>
 __global__ void __launch_bounds__(kNbThreads)
     k_rho_pres(const float4* __restrict__ pos, const int32_t* __restrict__ start,
                const Tile* __restrict__ tiles, const SceneDev* __restrict__ scenes,
-               const float* __restrict__ wave, float2* __restrict__ rho_p, int32_t* __restrict__ nbr,
-               int32_t* __restrict__ nbr_cnt, int32_t n_total) {
+               const float* __restrict__ wave, float2* __restrict__ rho_p, uint16_t* __restrict__ nbr,
+               int32_t* __restrict__ nbr_cnt, int32_t n_total, int32_t* status, int32_t allow_stage) {
   using T = Real<P>;
+  __shared__ __align__(128) float4 s_cand[kStageCap];
+  __shared__ uint16_t s_hit[kMaxNbr + 1][kNbThreads];  // + the overflow slot
+  __shared__ StagePlan sp;
+  __shared__ __align__(8) uint64_t s_bar;
   const Tile tl = tiles[blockIdx.x];
-  const int i = tl.begin + threadIdx.x;
-  if (i >= tl.end) return;
   const SceneDev* S = scenes + tl.scene;
+  if (threadIdx.x < 32) plan_stage(S, start, pos, tl, sp);
+  if (threadIdx.x == 0) mbar_init(&s_bar, 1);
+  __syncthreads();
+  const bool staged = allow_stage && sp.ncols > 0;
+  if (staged && threadIdx.x == 0) {
+    mbar_expect_tx(&s_bar, (uint32_t)sp.seg_off[kMaxSegs] * 16u);
+    for (int s = 0; s < 9 * sp.ncols; ++s) {
+      const int len = sp.seg_off[s + 1] - sp.seg_off[s];
+      if (len > 0) bulk_g2s(&s_cand[sp.seg_off[s]], pos + sp.seg_b[s], (uint32_t)len * 16u, &s_bar);
+    }
+  }
+  bool ready = true;
+  if (staged && !mbar_wait_bounded(&s_bar)) {
+    ready = false;
+    if (threadIdx.x == 0) atomicOr(status, kStatusTimeout);
+    mbar_wait_bounded(&s_bar);  // let copies in flight land before the CTA exits
+  }
+  const int i = tl.begin + threadIdx.x;
+  if (i >= tl.end || !ready) return;
+
   const float4 pi = __ldg(pos + i);
   const T hh = (T)S->h;
   const T h2 = hh * hh;
   const T px = pi.x, py = pi.y, pz = pi.z;
+  const CellCoord c = cell_of(S, pi);
   int b[9], e[9];
-  row_ranges(S, start, cell_of(S, pi), b, e);
+  row_ranges(S, start, c, b, e);
+  const int g = staged ? c.x * S->dims[1] + c.y - sp.col0 : 0;
+  uint16_t* const hit_col = &s_hit[0][threadIdx.x];
+  uint16_t* const hp_end = hit_col + kMaxNbr * kNbThreads;  // the overflow slot
+  uint16_t* hp = hit_col;
   Sum<P> acc;
-  int cnt = 0;
+  bool overflow = false;
 #pragma unroll
   for (int r = 0; r < 9; ++r) {
-    T part = (T)0;
-#pragma unroll 4
-    for (int j = b[r]; j < e[r]; ++j) {
-      const float4 pj = __ldg(pos + j);
-      const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
-      const T q = h2 - (dx * dx + dy * dy + dz * dz);
-      const T qp = q > (T)0 ? q : (T)0;
-      part += qp * qp * qp;
-      if (q > (T)0 && j != i) {
-        if (cnt < kMaxNbr) nbr[(size_t)cnt * n_total + i] = j;
-        ++cnt;
-      }
+    const int len = e[r] - b[r];
+    overflow |= len >= kRowCodeMax;
+    const uint32_t row_code = (uint32_t)r << kRowCodeBits;
+    T part;
+    if (staged) {
+      const float4* cand = s_cand + (sp.seg_off[g * 9 + r] + (b[r] - sp.seg_b[g * 9 + r]));
+      part = scan_row<T>([&](int o) { return cand[o]; }, len, row_code, px, py, pz, h2, hp, hp_end);
+    } else {
+      const float4* cand = pos + b[r];
+      part = scan_row<T>([&](int o) { return __ldg(cand + o); }, len, row_code, px, py, pz, h2, hp, hp_end);
     }
     acc.add(part);
   }
-  nbr_cnt[i] = cnt;
+  // Coalesced list write: entry k of every lane is one 64-byte store per warp.
+  const int cnt = (int)(hp - hit_col) / kNbThreads;
+  overflow |= cnt >= kMaxNbr;
+  for (int k = 0; k < cnt; ++k) nbr[(size_t)k * n_total + i] = hit_col[k * kNbThreads];
+  nbr_cnt[i] = overflow ? kMaxNbr + 1 : cnt;
+
   const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
   float rho = (float)rho_t;
   float p = S->k * (rho - S->rho0);
@@ -160,19 +317,18 @@ __global__ void __launch_bounds__(kNbThreads)
 }
 
 // Three-component sum in the precision mode: COMPENSATED adds pair terms
-// in float into a partial that is folded into a two-sum accumulator every
-// 8 terms (cascaded summation); FP32 is plain; FP64 is double.
+// in float into a partial that the caller folds into a two-sum accumulator
+// after every group of 8 pairs (cascaded summation); FP32 is plain; FP64 is
+// double.
 template <int P>
 struct Acc3 {
   Sum<P> x, y, z;
   Real<P> px = 0, py = 0, pz = 0;
-  int n = 0;
   __device__ __forceinline__ void add(Real<P> a, Real<P> b, Real<P> c) {
     if (P == CWA_PREC_COMPENSATED) {
       px += a;
       py += b;
       pz += c;
-      if (++n == 8) flush();
     } else {
       x.add(a);
       y.add(b);
@@ -185,7 +341,6 @@ struct Acc3 {
       y.add(py);
       z.add(pz);
       px = py = pz = 0;
-      n = 0;
     }
   }
 };
@@ -195,13 +350,14 @@ struct Acc3 {
 // then the preset's extra terms.  A particle whose list overflowed rescans
 // its 27-cell block.
 template <int P>
-__global__ void __launch_bounds__(kNbThreads)
+__global__ void __launch_bounds__(kNbThreads, 8)
     k_force(const float4* __restrict__ pos, const float4* __restrict__ vel,
             const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
             const Tile* __restrict__ tiles, const SceneDev* __restrict__ scenes,
-            const float* __restrict__ wave, float4* __restrict__ force, const int32_t* __restrict__ nbr,
+            const float* __restrict__ wave, float4* __restrict__ force, const uint16_t* __restrict__ nbr,
             const int32_t* __restrict__ nbr_cnt, int32_t n_total) {
   using T = Real<P>;
+  __shared__ int32_t s_rb[9][kNbThreads];
   const Tile tl = tiles[blockIdx.x];
   const int i = tl.begin + threadIdx.x;
   if (i >= tl.end) return;
@@ -230,22 +386,39 @@ __global__ void __launch_bounds__(kNbThreads)
     fv.add(sv * ((T)vj.x - vx), sv * ((T)vj.y - vy), sv * ((T)vj.z - vz));
   };
   const int cnt = __ldg(nbr_cnt + i);
+  int b[9], e[9];
+  row_ranges(S, start, cell_of(S, pi), b, e);
   if (cnt <= kMaxNbr) {
-    int jn = cnt > 0 ? __ldg(nbr + i) : 0;
-    for (int k = 0; k < cnt; ++k) {
-      const int j = jn;
-      if (k + 1 < cnt) jn = __ldg(nbr + (size_t)(k + 1) * n_total + i);
-      pair(j);
+#pragma unroll
+    for (int r = 0; r < 9; ++r) s_rb[r][threadIdx.x] = b[r];
+    // Groups of 8 hits: the 8 codes are loaded first so the gathers overlap.
+    // The list holds the particle itself (r = 0), which is skipped.
+    for (int k0 = 0; k0 < cnt; k0 += 8) {
+      uint32_t code[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        code[u] = k0 + u < cnt ? __ldg(nbr + (size_t)(k0 + u) * n_total + i) : 0u;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = s_rb[code[u] >> kRowCodeBits][threadIdx.x] + (int)(code[u] & (kRowCodeMax - 1));
+        if (k0 + u < cnt && j != i) pair(j);
+      }
+      fp.flush();
+      fv.flush();
     }
   } else {
-    int b[9], e[9];
-    row_ranges(S, start, cell_of(S, pi), b, e);
-    for (int r = 0; r < 9; ++r)
+    for (int r = 0; r < 9; ++r) {
       for (int j = b[r]; j < e[r]; ++j) {
         const float4 pj = __ldg(pos + j);
         const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
-        if (h2 - (dx * dx + dy * dy + dz * dz) > (T)0 && j != i) pair(j);
+        T q = fma(-dx, dx, h2);
+        q = fma(-dy, dy, q);
+        q = fma(-dz, dz, q);
+        if (q > (T)0 && j != i) pair(j);
       }
+      fp.flush();
+      fv.flush();
+    }
   }
   fp.flush();
   fv.flush();
@@ -299,28 +472,28 @@ __global__ void __launch_bounds__(kNbThreads)
 
 cudaError_t launch_rho_pres(int precision, const float4* pos, const int32_t* start, const Tile* tiles,
                             int32_t n_tiles, int32_t tile_size, const SceneDev* scenes,
-                            const float* wave_u, float2* rho_p, int32_t* nbr, int32_t* nbr_cnt,
-                            int32_t n_total, cudaStream_t stream) {
+                            const float* wave_u, float2* rho_p, uint16_t* nbr, int32_t* nbr_cnt,
+                            int32_t n_total, int32_t* status, int32_t stage, cudaStream_t stream) {
   if (n_tiles <= 0) return cudaSuccess;
   switch (precision) {
     case CWA_PREC_FP32:
       k_rho_pres<CWA_PREC_FP32><<<n_tiles, tile_size, 0, stream>>>(pos, start, tiles, scenes, wave_u, rho_p, nbr,
-                                                                   nbr_cnt, n_total);
+                                                                   nbr_cnt, n_total, status, stage);
       break;
     case CWA_PREC_FP64:
       k_rho_pres<CWA_PREC_FP64><<<n_tiles, tile_size, 0, stream>>>(pos, start, tiles, scenes, wave_u, rho_p, nbr,
-                                                                   nbr_cnt, n_total);
+                                                                   nbr_cnt, n_total, status, stage);
       break;
     default:
       k_rho_pres<CWA_PREC_COMPENSATED><<<n_tiles, tile_size, 0, stream>>>(pos, start, tiles, scenes, wave_u,
-                                                                          rho_p, nbr, nbr_cnt, n_total);
+                                                                          rho_p, nbr, nbr_cnt, n_total, status, stage);
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_force(int precision, const float4* pos, const float4* vel, const float2* rho_p,
                          const int32_t* start, const Tile* tiles, int32_t n_tiles, int32_t tile_size,
-                         const SceneDev* scenes, const float* wave_u, float4* force, const int32_t* nbr,
+                         const SceneDev* scenes, const float* wave_u, float4* force, const uint16_t* nbr,
                          const int32_t* nbr_cnt, int32_t n_total, cudaStream_t stream) {
   if (n_tiles <= 0) return cudaSuccess;
   switch (precision) {

@@ -30,14 +30,14 @@ class Sim:
     """One or more independent scenes stepped together on one GPU."""
 
     def __init__(self, scenes, precision: int = PREC_COMPENSATED, use_graph: bool = True,
-                 device: int = 0, nb_threads: int = 0):
+                 device: int = 0, nb_threads: int = 0, nb_stage: int = 0):
         self._lib = _abi.load()
         if isinstance(scenes, SceneDesc):
             scenes = [scenes]
         self.scenes = [s.copy() for s in scenes]
         arr = (SceneDesc * len(self.scenes))(*self.scenes)
         opt = SimOptions(device=device, precision=precision, use_graph=int(use_graph),
-                         nb_threads=nb_threads)
+                         nb_threads=nb_threads, nb_stage=nb_stage)
         h = C.c_void_p()
         check(self._lib.cwa_create(C.byref(opt), arr, len(self.scenes), C.byref(h)), "cwa_create")
         self._h = h

@@ -105,7 +105,9 @@ typedef struct cwa_sim_options {
   int32_t precision;       /* CWA_PREC_*                                      */
   int32_t use_graph;       /* capture cwa_step into CUDA graphs               */
   int32_t nb_threads;      /* threads per CTA of the neighbour passes; 0=auto */
-  int32_t reserved[8];
+  int32_t nb_stage;        /* density pass stages candidate rows in shared
+                              memory: 0/1 = on (default), -1 = off         */
+  int32_t reserved[7];
 } cwa_sim_options;
 
 /* Borrowed device pointers of one scene, all in the current sorted order.
