@@ -244,6 +244,20 @@ size_t cwa_scan_workspace_bytes(int32_t n);
 cwa_status cwa_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int32_t n, void* d_workspace,
                                   size_t workspace_bytes, void* stream);
 
+/* Exclusive scan that allocates nothing.  No counterpart in the reference:
+ * it exists for callers that cannot lend the workspace the scan above needs
+ * and must not call cudaMalloc themselves (code inside a host application
+ * that owns the whole device-memory budget, or real-time loops that cannot
+ * risk the device synchronisation an allocation may cause).  The scan's
+ * scratch is a fixed 66,048-byte array declared by the library, held on
+ * every GPU that loads it until the process exits.  n above
+ * CWA_NOALLOC_SCAN_MAX_N is rejected with CWA_ERR_CAPACITY.  The first call
+ * on a device looks up the array's device address; make it before any
+ * stream capture.  All calls on a device share the array: calls whose
+ * kernels overlap on the GPU race, so order them (e.g. one stream). */
+#define CWA_NOALLOC_SCAN_MAX_N 16777216
+cwa_status cwa_exclusive_scan_i32_noalloc(const int32_t* d_in, int32_t* d_out, int32_t n, void* stream);
+
 /* Uniform-grid build of n points (float4 xyz, stride 16 B): cell =
  * clamp(floor((p-lo)/cell), 0, dims-1), cell id (k*dims[1]+j)*dims[0]+i,
  * stable counting sort.  Replaces the COMPUTE_COUNTS / scan / INSERT
