@@ -39,7 +39,7 @@ class SceneDesc(C.Structure):
     _fields_ = [
         ("preset", C.c_int32), ("n_particles", C.c_int32), ("wave_nx", C.c_int32),
         ("wave_nz", C.c_int32), ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3),
-        ("cell_size", C.c_float), ("mass", C.c_float), ("smoothing_length", C.c_float),
+        ("cell_size", C.c_float), ("cell_size_z", C.c_float), ("mass", C.c_float), ("smoothing_length", C.c_float),
         ("visc", C.c_float), ("rest_rho", C.c_float), ("gas_const", C.c_float), ("dt", C.c_float),
         ("gravity", C.c_float * 3), ("wall_restitution", C.c_float),
         ("velocity_damping", C.c_float), ("particle_radius", C.c_float),

@@ -137,6 +137,8 @@ cwa_status validate_scene(const cwa_scene_desc& d, int idx) {
   if ((int64_t)d.wave_nx * d.wave_nz > (1ll << 28)) return bad("wave grid above 2^28 cells");
   if (!(d.smoothing_length > 0.0f) || !(d.cell_size >= d.smoothing_length))
     return bad("need 0 < smoothing_length <= cell_size");
+  if (d.cell_size_z > 0.0f && !(d.cell_size_z * 64.0f >= d.smoothing_length))
+    return bad("cell_size_z below smoothing_length / 64");
   if (!(d.mass > 0.0f) || !(d.rest_rho > 0.0f) || !(d.dt > 0.0f)) return bad("mass, rest_rho, dt must be > 0");
   for (int a = 0; a < 3; ++a)
     if (!(d.box_hi[a] > d.box_lo[a])) return bad("box_hi must exceed box_lo");
@@ -163,6 +165,11 @@ SceneDev make_scene_dev(const cwa_scene_desc& d, const int32_t dims[3], int32_t 
     s.g[a] = d.gravity[a];
   }
   s.cell = d.cell_size;
+  s.cellz = d.cell_size_z > 0.0f ? d.cell_size_z : d.cell_size;
+  s.inv_cell = 1.0f / s.cell;
+  s.inv_cellz = 1.0f / s.cellz;
+  s.hs = (float)((double)d.smoothing_length * (1.0 + 1.0 / 1024.0));
+  s.hs2 = s.hs * s.hs;
   s.preset = d.preset;
   s.h = d.smoothing_length;
   s.h2 = d.smoothing_length * d.smoothing_length;

@@ -163,14 +163,14 @@ __global__ void __launch_bounds__(256)
                  int32_t* __restrict__ slot, int32_t* __restrict__ count, int32_t* status) {
   const Tile t = tiles[blockIdx.x];
   const SceneDev* S = scenes + t.scene;
-  const float lx = S->lo[0], ly = S->lo[1], lz = S->lo[2], cs = S->cell;
+  const float lx = S->lo[0], ly = S->lo[1], lz = S->lo[2], cs = S->cell, csz = S->cellz;
   const int nx = S->dims[0], ny = S->dims[1], nz = S->dims[2], coff = S->coff;
   for (int i = t.begin + threadIdx.x; i < t.end; i += blockDim.x) {
     float4 p = pos[i];
     if (!finite3(p)) atomicOr(status, kStatusNonFinite);
     int cx = cell_axis(p.x, lx, cs, nx);
     int cy = cell_axis(p.y, ly, cs, ny);
-    int cz = cell_axis(p.z, lz, cs, nz);
+    int cz = cell_axis(p.z, lz, csz, nz);
     int k = coff + (cx * ny + cy) * nz + cz;
     key[i] = k;
     slot[i] = count_slot(count, k);

@@ -30,7 +30,8 @@ struct SceneDev {
   int32_t coff, ncells;
   int32_t dims[3];
   float lo[3], hi[3];
-  float cell;
+  float cell, cellz, inv_cell, inv_cellz;  // x/y and z cell edges
+  float hs, hs2;  // search radius: h * (1 + 2^-10), so float rounding never drops a pair
   // physics
   int32_t preset;
   float h, h2, mass, visc, rho0, k, dt;

@@ -93,6 +93,7 @@ cwa_status cwa_scene_defaults(int32_t preset, float spacing, cwa_scene_desc* o) 
     o->particle_radius = 0.005f;
     o->smoothing_length = 2.0f * 0.005f;  // smoothing_coeff * PARTICLE_RADIUS
     o->cell_size = o->smoothing_length;
+    o->cell_size_z = o->cell_size;
     o->mass = 0.02f;
     o->visc = 3000.0f;
     o->rest_rho = 1000.0f;
@@ -117,6 +118,7 @@ cwa_status cwa_scene_defaults(int32_t preset, float spacing, cwa_scene_desc* o) 
     o->particle_radius = (float)(0.5 * s);
     o->smoothing_length = (float)(2.0 * s);
     o->cell_size = o->smoothing_length;
+    o->cell_size_z = o->cell_size;
     o->rest_rho = 1000.0f;
     o->mass = (float)(1000.0 * s * s * s);
     o->visc = 0.1f;
@@ -142,10 +144,11 @@ cwa_status cwa_scene_set_wave_grid(cwa_scene_desc* o, int32_t nx, int32_t nz) {
 cwa_status cwa_grid_dims(const cwa_scene_desc* sc, int32_t dims[3]) {
   if (!sc || !dims) return CWA_ERR_INVALID_ARG;
   if (!(sc->cell_size > 0.0f)) return CWA_ERR_INVALID_ARG;
+  const float csz = sc->cell_size_z > 0.0f ? sc->cell_size_z : sc->cell_size;
   for (int a = 0; a < 3; ++a) {
     const float ext = sc->box_hi[a] - sc->box_lo[a];
     if (!(ext > 0.0f)) return CWA_ERR_INVALID_ARG;
-    const float q = ext / sc->cell_size;
+    const float q = ext / (a == 2 ? csz : sc->cell_size);
     if (!(q < 1.0e7f)) return CWA_ERR_CAPACITY;
     const int d = (int)ceilf(q);
     dims[a] = d < 1 ? 1 : d;

@@ -79,24 +79,37 @@ __device__ __forceinline__ CellCoord cell_of(const SceneDev* S, float4 p) {
   CellCoord c;
   c.x = cell_axis(p.x, S->lo[0], S->cell, S->dims[0]);
   c.y = cell_axis(p.y, S->lo[1], S->cell, S->dims[1]);
-  c.z = cell_axis(p.z, S->lo[2], S->cell, S->dims[2]);
+  c.z = cell_axis(p.z, S->lo[2], S->cellz, S->dims[2]);
   return c;
 }
 
-// Sorted-index ranges [b, e) of the 9 z-rows that hold the 27 cells around
-// c (x outer, y inner); rows outside the grid are empty.  The 18 loads are
-// independent, so they overlap.
-__device__ __forceinline__ void row_ranges(const SceneDev* S, const int32_t* __restrict__ start, CellCoord c,
-                                           int b[9], int e[9]) {
+// Sorted-index ranges [b, e) of the 9 rows (columns x-1..x+1, y-1..y+1)
+// that can hold a neighbour within h of p.  A row whose column is farther
+// than h from p in (x, y) is empty; the others cover only the z cells of the
+// window |z - pz| < sqrt(h^2 - d^2), d = the column's (x, y) distance.  The
+// search radius is h (1 + 2^-10), so float rounding never drops a pair.
+// The 18 start loads are independent, so they overlap.
+__device__ __forceinline__ void row_ranges(const SceneDev* S, const int32_t* __restrict__ start, float4 p,
+                                           CellCoord c, int b[9], int e[9]) {
   const int nx = S->dims[0], ny = S->dims[1], nz = S->dims[2];
-  const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, nz - 1);
+  const float x0f = S->lo[0] + (float)c.x * S->cell;
+  const float y0f = S->lo[1] + (float)c.y * S->cell;
+  const float dxm = fmaxf(p.x - x0f, 0.0f), dxp = fmaxf(x0f + S->cell - p.x, 0.0f);
+  const float dym = fmaxf(p.y - y0f, 0.0f), dyp = fmaxf(y0f + S->cell - p.y, 0.0f);
+  const float hs2 = S->hs2, zl = p.z - S->lo[2], izc = S->inv_cellz, zmax = (float)(nz - 1);
 #pragma unroll
   for (int dx = -1; dx <= 1; ++dx) {
 #pragma unroll
     for (int dy = -1; dy <= 1; ++dy) {
       const int r = (dx + 1) * 3 + (dy + 1);
       const int x = c.x + dx, y = c.y + dy;
-      const bool ok = x >= 0 && x < nx && y >= 0 && y < ny;
+      const float ddx = dx < 0 ? dxm : (dx > 0 ? dxp : 0.0f);
+      const float ddy = dy < 0 ? dym : (dy > 0 ? dyp : 0.0f);
+      const float d2 = ddx * ddx + ddy * ddy;
+      const bool ok = x >= 0 && x < nx && y >= 0 && y < ny && d2 < hs2;
+      const float w = sqrtf(fmaxf(hs2 - d2, 0.0f));
+      const int z0 = (int)fminf(fmaxf(floorf((zl - w) * izc), 0.0f), zmax);
+      const int z1 = (int)fminf(fmaxf(floorf((zl + w) * izc), 0.0f), zmax);
       const int row = S->coff + (x * ny + y) * nz;
       b[r] = ok ? __ldg(start + row + z0) : 0;
       e[r] = ok ? __ldg(start + row + z1 + 1) : 0;
@@ -162,7 +175,8 @@ struct StagePlan {
 };
 
 // Warp 0 plans the CTA's staging: the columns its particles occupy and, per
-// column, the candidate rows over the z-range its particles need (+-1 cell).
+// column, the candidate rows over the z cells its particles' windows can
+// reach (R = ceil(h_search / cell_z) + 1 cells beyond the particles' own).
 __device__ __forceinline__ void plan_stage(const SceneDev* S, const int32_t* __restrict__ start,
                                            const float4* __restrict__ pos, const Tile& tl, StagePlan& sp) {
   const int lane = threadIdx.x & 31;
@@ -171,13 +185,14 @@ __device__ __forceinline__ void plan_stage(const SceneDev* S, const int32_t* __r
   const int nx = S->dims[0], ny = S->dims[1], nz = S->dims[2];
   const int colA = a.x * ny + a.y, colB = b.x * ny + b.y;
   const int ncols = colB - colA + 1;
+  const int R = (int)ceilf(S->hs * S->inv_cellz) + 1;
   int len = 0, gb = 0;
   if (ncols <= 2 && lane < 9 * ncols) {
     const int g = lane / 9, r = lane % 9;
     const int col = colA + g;
     const int cx = col / ny, cy = col - cx * ny;
-    const int zlo = g == 0 ? max(a.z - 1, 0) : 0;
-    const int zhi = (g == ncols - 1) ? min(b.z + 1, nz - 1) : nz - 1;
+    const int zlo = g == 0 ? max(a.z - R, 0) : 0;
+    const int zhi = (g == ncols - 1) ? min(b.z + R, nz - 1) : nz - 1;
     const int x = cx + r / 3 - 1, y = cy + r % 3 - 1;
     if (x >= 0 && x < nx && y >= 0 && y < ny) {
       const int row = S->coff + (x * ny + y) * nz;
@@ -273,7 +288,7 @@ __global__ void __launch_bounds__(kNbThreads)
   const T px = pi.x, py = pi.y, pz = pi.z;
   const CellCoord c = cell_of(S, pi);
   int b[9], e[9];
-  row_ranges(S, start, c, b, e);
+  row_ranges(S, start, pi, c, b, e);
   const int g = staged ? c.x * S->dims[1] + c.y - sp.col0 : 0;
   uint16_t* const hit_col = &s_hit[0][threadIdx.x];
   uint16_t* const hp_end = hit_col + kMaxNbr * kNbThreads;  // the overflow slot
@@ -286,7 +301,9 @@ __global__ void __launch_bounds__(kNbThreads)
     overflow |= len >= kRowCodeMax;
     const uint32_t row_code = (uint32_t)r << kRowCodeBits;
     T part;
-    if (staged) {
+    if (len <= 0) {
+      part = (T)0;
+    } else if (staged) {
       const float4* cand = s_cand + (sp.seg_off[g * 9 + r] + (b[r] - sp.seg_b[g * 9 + r]));
       part = scan_row<T>([&](int o) { return cand[o]; }, len, row_code, px, py, pz, h2, hp, hp_end);
     } else {
@@ -387,7 +404,7 @@ __global__ void __launch_bounds__(kNbThreads, 8)
   };
   const int cnt = __ldg(nbr_cnt + i);
   int b[9], e[9];
-  row_ranges(S, start, cell_of(S, pi), b, e);
+  row_ranges(S, start, pi, cell_of(S, pi), b, e);
   if (cnt <= kMaxNbr) {
 #pragma unroll
     for (int r = 0; r < 9; ++r) s_rb[r][threadIdx.x] = b[r];

@@ -69,9 +69,11 @@ def reference() -> Scene:
 
 
 def dam_break(lattice=(32, 32, 32), spacing=0.02, wave=(256, 256), box_hi=(1.0, 1.0, 1.0),
-              seed=BASE_SEED, n_bumps=8, jitter=0.05) -> Scene:
+              seed=BASE_SEED, n_bumps=8, jitter=0.05, zsub=1) -> Scene:
+    """zsub > 1 sorts by z cells of edge h / zsub (x and y cells stay h)."""
     lib = _abi.load()
     d = defaults(PRESET_MULLER, spacing)
+    d.cell_size_z = d.cell_size / zsub
     for a in range(3):
         d.box_hi[a] = box_hi[a]
     set_wave_grid(d, wave[0], wave[1])
@@ -138,3 +140,10 @@ def config4(seed=BASE_SEED, n_scenes=64) -> Workload:
 
 
 CONFIGS = {0: config0, 1: config1, 2: config2, 3: config3, 4: config4}
+
+
+def with_zsub(wl: Workload, zsub: int) -> Workload:
+    """The same workload with the sort grid's z cells split zsub times."""
+    for s in wl.scenes:
+        s.desc.cell_size_z = s.desc.cell_size / zsub
+    return wl

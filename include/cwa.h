@@ -74,7 +74,10 @@ typedef struct cwa_scene_desc {
   int32_t wave_nz;         /* wave image height (texture t axis = world z)    */
   float box_lo[3];         /* BoundaryUniform.lower.xyz                       */
   float box_hi[3];         /* BoundaryUniform.upper.xyz                       */
-  float cell_size;         /* uniform-grid cell edge; must be >= h            */
+  float cell_size;         /* uniform-grid cell edge in x and y; must be >= h */
+  float cell_size_z;       /* cell edge in z; <= 0 means cell_size.  A finer
+                              z edge (e.g. h/4) lets each particle scan only
+                              the z-window its neighbours can occupy        */
   float mass;              /* ConstantsUniform.mass                           */
   float smoothing_length;  /* h = smoothing_coeff * PARTICLE_RADIUS           */
   float visc;              /* ConstantsUniform.visc                           */

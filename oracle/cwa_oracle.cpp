@@ -110,9 +110,20 @@ struct Grid64 {
   std::vector<int> cell;    // cell of each particle
 };
 
+double cell_edge(const cwa_scene_desc* sc, int a) {
+  return (a == 2 && sc->cell_size_z > 0.0f) ? sc->cell_size_z : sc->cell_size;
+}
+
+int cell_axis64(const cwa_scene_desc* sc, const int dims[3], int a, double x) {
+  double t = floor((x - sc->box_lo[a]) / cell_edge(sc, a));
+  if (!(t >= 0.0)) t = 0.0;
+  if (t > dims[a] - 1) t = dims[a] - 1;
+  return (int)t;
+}
+
 void cell_coords64(const cwa_scene_desc* sc, const int dims[3], const double* p, int c[3]) {
   for (int a = 0; a < 3; ++a) {
-    double t = floor((p[a] - sc->box_lo[a]) / sc->cell_size);
+    double t = floor((p[a] - sc->box_lo[a]) / cell_edge(sc, a));
     if (!(t >= 0.0)) t = 0.0;
     if (t > dims[a] - 1) t = dims[a] - 1;
     c[a] = (int)t;
@@ -159,7 +170,9 @@ inline void for_neighbours(const cwa_scene_desc* sc, const Grid64& g, const doub
     for (int dy = -1; dy <= 1; ++dy) {
       int y = c[1] + dy;
       if (y < 0 || y >= g.dims[1]) continue;
-      int z0 = std::max(c[2] - 1, 0), z1 = std::min(c[2] + 1, g.dims[2] - 1);
+      // every z cell a neighbour within h can occupy
+      int z0 = cell_axis64(sc, g.dims, 2, p[2] - sc->smoothing_length);
+      int z1 = cell_axis64(sc, g.dims, 2, p[2] + sc->smoothing_length);
       int b = g.start[cell_index(g.dims, x, y, z0)];
       int e = g.start[cell_index(g.dims, x, y, z1) + 1];
       for (int k = b; k < e; ++k) fn(g.order[k]);
@@ -245,16 +258,16 @@ void orc_exclusive_scan_i32(const int32_t* in, int32_t* out, int32_t n) {
 
 // UniformGrid2D/ugrid_particles_cs.glsl:97-108, in float32:
 // cell = clamp(floor((p - lo) / cell_size), 0, n - 1), id = (x*ny + y)*nz + z.
-int32_t orc_cell_id_f32(const float p[3], const float lo[3], float cell, const int32_t dims[3]) {
-  int cx = cell_axis_f32(p[0], lo[0], cell, dims[0]);
-  int cy = cell_axis_f32(p[1], lo[1], cell, dims[1]);
-  int cz = cell_axis_f32(p[2], lo[2], cell, dims[2]);
+int32_t orc_cell_id_f32(const float p[3], const float lo[3], const float cell[3], const int32_t dims[3]) {
+  int cx = cell_axis_f32(p[0], lo[0], cell[0], dims[0]);
+  int cy = cell_axis_f32(p[1], lo[1], cell[1], dims[1]);
+  int cz = cell_axis_f32(p[2], lo[2], cell[2], dims[2]);
   return (cx * dims[1] + cy) * dims[2] + cz;
 }
 
 // UniformGrid2D/UniformGrid2D.cpp:33-92 with one cell per point: count,
 // exclusive offsets, insert in input order (stable).
-void orc_grid_build_f32(const float* pos4, int32_t n, const float lo[3], float cell,
+void orc_grid_build_f32(const float* pos4, int32_t n, const float lo[3], const float cell[3],
                         const int32_t dims[3], int32_t* cell_start, int32_t* sorted_index,
                         int32_t* cell_of) {
   size_t nc = (size_t)dims[0] * dims[1] * dims[2];
@@ -271,9 +284,10 @@ void orc_grid_build_f32(const float* pos4, int32_t n, const float lo[3], float c
 }
 
 void orc_grid_dims(const cwa_scene_desc* sc, int32_t dims[3]) {
+  const float csz = sc->cell_size_z > 0.0f ? sc->cell_size_z : sc->cell_size;
   for (int a = 0; a < 3; ++a) {
     float ext = sc->box_hi[a] - sc->box_lo[a];
-    float q = ext / sc->cell_size;
+    float q = ext / (a == 2 ? csz : sc->cell_size);
     int d = (int)ceilf(q);
     dims[a] = d < 1 ? 1 : d;
   }
@@ -293,6 +307,7 @@ void orc_scene_defaults(int32_t preset, float spacing, cwa_scene_desc* o) {
     o->particle_radius = 0.005f;
     o->smoothing_length = 2.0f * 0.005f;
     o->cell_size = o->smoothing_length;
+    o->cell_size_z = o->cell_size;
     o->mass = 0.02f;
     o->visc = 3000.0f;
     o->rest_rho = 1000.0f;
@@ -318,6 +333,7 @@ void orc_scene_defaults(int32_t preset, float spacing, cwa_scene_desc* o) {
     o->particle_radius = (float)(0.5 * s);
     o->smoothing_length = (float)(2.0 * s);
     o->cell_size = o->smoothing_length;
+    o->cell_size_z = o->cell_size;
     o->rest_rho = 1000.0f;
     o->mass = (float)(1000.0 * s * s * s);
     o->visc = 0.1f;

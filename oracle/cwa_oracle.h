@@ -42,11 +42,12 @@ void orc_set_num_threads(int n);
 /* ---- FP32-exact integer parts ------------------------------------------ */
 /* Exclusive scan, the CPU truth of SphWave2D/ParallelScan.cpp:130-137. */
 void orc_exclusive_scan_i32(const int32_t* in, int32_t* out, int32_t n);
-/* Cell of a float32 point, UniformGrid2D/ugrid_particles_cs.glsl:97-103. */
-int32_t orc_cell_id_f32(const float p[3], const float lo[3], float cell, const int32_t dims[3]);
+/* Cell of a float32 point, UniformGrid2D/ugrid_particles_cs.glsl:97-103,
+ * with a cell edge per axis. */
+int32_t orc_cell_id_f32(const float p[3], const float lo[3], const float cell[3], const int32_t dims[3]);
 /* Stable counting sort (UniformGrid2D/UniformGrid2D.cpp:33-92 with one cell
  * per point): cell_start[ncells+1], sorted_index[n], cell_of[n] (nullable). */
-void orc_grid_build_f32(const float* pos4, int32_t n, const float lo[3], float cell,
+void orc_grid_build_f32(const float* pos4, int32_t n, const float lo[3], const float cell[3],
                         const int32_t dims[3], int32_t* cell_start, int32_t* sorted_index,
                         int32_t* cell_of);
 void orc_grid_dims(const cwa_scene_desc* sc, int32_t dims[3]);

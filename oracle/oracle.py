@@ -39,8 +39,8 @@ def load() -> C.CDLL:
             "orc_num_threads": (C.c_int, []),
             "orc_set_num_threads": (None, [C.c_int]),
             "orc_exclusive_scan_i32": (None, [_P, _P, _I]),
-            "orc_cell_id_f32": (_I, [_P, _P, C.c_float, _P]),
-            "orc_grid_build_f32": (None, [_P, _I, _P, C.c_float, _P, _P, _P, _P]),
+            "orc_cell_id_f32": (_I, [_P, _P, _P, _P]),
+            "orc_grid_build_f32": (None, [_P, _I, _P, _P, _P, _P, _P, _P]),
             "orc_grid_dims": (None, [_P, _P]),
             "orc_scene_defaults": (None, [_I, C.c_float, _P]),
             "orc_scene_set_wave_grid": (None, [_P, _I, _I]),
@@ -100,22 +100,29 @@ def exclusive_scan(x: np.ndarray) -> np.ndarray:
     return out
 
 
+def cell_edges(desc) -> tuple[float, float, float]:
+    z = desc.cell_size_z if desc.cell_size_z > 0 else desc.cell_size
+    return (desc.cell_size, desc.cell_size, z)
+
+
 def grid_dims(desc) -> tuple[int, int, int]:
     dims = np.zeros(3, np.int32)
     load().orc_grid_dims(_d(desc), _p(dims))
     return tuple(int(v) for v in dims)
 
 
-def grid_build(pos4: np.ndarray, lo, cell: float, dims):
+def grid_build(pos4: np.ndarray, lo, cell, dims):
+    """cell: one edge for all axes, or (x, y, z) edges."""
     pos4 = np.ascontiguousarray(pos4, np.float32).reshape(-1, 4)
     lo = np.ascontiguousarray(lo, np.float32)
+    cell = np.ascontiguousarray(np.broadcast_to(np.asarray(cell, np.float32), (3,)), np.float32)
     dims = np.ascontiguousarray(dims, np.int32)
     n = len(pos4)
     nc = int(np.prod(dims))
     start = np.zeros(nc + 1, np.int32)
     order = np.zeros(n, np.int32)
     cell_of = np.zeros(n, np.int32)
-    load().orc_grid_build_f32(_p(pos4), n, _p(lo), cell, _p(dims), _p(start), _p(order), _p(cell_of))
+    load().orc_grid_build_f32(_p(pos4), n, _p(lo), _p(cell), _p(dims), _p(start), _p(order), _p(cell_of))
     return start, order, cell_of
 
 

@@ -65,7 +65,7 @@ def make_oracle_regression() -> None:
     d = orc.scene_defaults(abi.PRESET_REFERENCE_3D, 0.0, abi.SceneDesc)
     cube = orc.make_reference_cube(d, d.n_particles)
     dims = orc.grid_dims(d)
-    start, order, cell_of = orc.grid_build(cube[:, 0:4], list(d.box_lo), d.cell_size, dims)
+    start, order, cell_of = orc.grid_build(cube[:, 0:4], list(d.box_lo), orc.cell_edges(d), dims)
     out["reference_cube"] = {"dims": dims, "cell_start_sha256": _h(start), "order_sha256": _h(order),
                              "cube_sha256": _h(cube)}
     u0 = orc.wave_init_f32(d)

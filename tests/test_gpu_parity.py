@@ -93,11 +93,12 @@ def test_grid_build_operator(lib, orc):
 
 
 def _oracle_grid_of(orc, sc_desc, pos_current):
-    return orc.grid_build(pos_current, list(sc_desc.box_lo), sc_desc.cell_size, orc.grid_dims(sc_desc))
+    return orc.grid_build(pos_current, list(sc_desc.box_lo), orc.cell_edges(sc_desc), orc.grid_dims(sc_desc))
 
 
-def test_sim_grid_bit_exact_across_steps(lib, orc):
-    sc = small_muller((20, 20, 20), 0.02, (64, 64))
+@pytest.mark.parametrize("zsub", [1, 4])
+def test_sim_grid_bit_exact_across_steps(lib, orc, zsub):
+    sc = small_muller((20, 20, 20), 0.02, (64, 64), zsub=zsub)
     with Sim(sc.desc) as sim:
         load_scene(sim, 0, sc)
         order_ids = np.arange(sc.desc.n_particles, dtype=np.int32)  # current order = upload order
@@ -124,9 +125,11 @@ def _oracle_state(orc, parts_records):
 
 @pytest.mark.parametrize("preset", ["reference", "muller"])
 @pytest.mark.parametrize("prec", [PREC_FP32, PREC_COMPENSATED, PREC_FP64])
-def test_rho_pres_force_parity(lib, orc, preset, prec):
+@pytest.mark.parametrize("zsub,stage", [(1, 0), (4, 0), (4, -1)])
+def test_rho_pres_force_parity(lib, orc, preset, prec, zsub, stage):
     sc = small_reference() if preset == "reference" else small_muller()
-    with Sim(sc.desc, precision=prec) as sim:
+    sc.desc.cell_size_z = sc.desc.cell_size / zsub
+    with Sim(sc.desc, precision=prec, nb_stage=stage) as sim:
         load_scene(sim, 0, sc)
         u_n, _ = sim.download_wave(0)
         p0 = records_f32(sim.download_particles(0))
@@ -239,8 +242,9 @@ def test_reference_line_source_mode(lib, orc):
 
 
 # ---------------------------------------------------- whole steps -----------
-def test_full_step_matches_oracle_one_step(lib, orc):
-    sc = small_muller((20, 20, 20), 0.02, (128, 128))
+@pytest.mark.parametrize("zsub", [1, 4])
+def test_full_step_matches_oracle_one_step(lib, orc, zsub):
+    sc = small_muller((20, 20, 20), 0.02, (128, 128), zsub=zsub)
     with Sim(sc.desc) as sim:
         load_scene(sim, 0, sc)
         sim.step(1)
@@ -325,11 +329,14 @@ def _run(scene_list, steps, **kw):
         return [(records_f32(sim.download_particles(k)), sim.download_wave(k)[0]) for k in range(len(scene_list))]
 
 
-def test_batched_equals_single(lib):
+@pytest.mark.parametrize("zsub", [1, 4])
+def test_batched_equals_single(lib, zsub):
     scs = [small_muller((10, 12, 14), 0.02, (64, 32), seed=1),
            small_muller((20, 8, 8), 0.03, (48, 48), seed=2),
            scenes.dam_break((9, 9, 9), 0.025, (40, 72), box_hi=(1.5, 1.0, 1.0), seed=3),
            small_muller((7, 9, 11), 0.03, (37, 21), seed=4)]
+    for s in scs:
+        s.desc.cell_size_z = s.desc.cell_size / zsub
     together = _run(scs, 12)
     for k, s in enumerate(scs):
         alone = _run([s], 12)[0]

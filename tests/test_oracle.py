@@ -77,7 +77,7 @@ def test_golden_oracle_regression(orc):
     cube = orc.make_reference_cube(d, d.n_particles)
     h = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()  # noqa: E731
     assert h(cube) == g["reference_cube"]["cube_sha256"]
-    start, order, _ = orc.grid_build(cube[:, :4], list(d.box_lo), d.cell_size, orc.grid_dims(d))
+    start, order, _ = orc.grid_build(cube[:, :4], list(d.box_lo), orc.cell_edges(d), orc.grid_dims(d))
     assert h(start) == g["reference_cube"]["cell_start_sha256"]
     assert h(order) == g["reference_cube"]["order_sha256"]
     assert h(orc.wave_init_f32(d)) == g["reference_wave_init"]["sha256"]
@@ -228,3 +228,21 @@ def test_generators_match_library(orc, lib):
     cube = orc.make_reference_cube(dr, dr.n_particles)
     assert np.array_equal(cube.view(np.uint32), r.particles.view(np.float32).reshape(-1, 16).view(np.uint32))
     del C
+
+
+def test_z_subcells_keep_the_neighbour_set(orc):
+    # Sorting by finer z cells changes only the search structure.
+    d, p, u = _small_muller(orc)
+    a = orc.to_f64(p.copy())
+    b = a.copy()
+    uu = u.astype(np.float64)
+    orc.rho_pres(d, a, uu, brute=True)
+    d4 = type(d).from_buffer_copy(d)
+    d4.cell_size_z = d.cell_size / 4
+    orc.rho_pres(d4, b, uu, brute=False)
+    np.testing.assert_allclose(a[:, 12:14], b[:, 12:14], rtol=1e-12, atol=1e-9)
+    orc.force(d, a, uu, brute=True)
+    orc.force(d4, b, uu, brute=False)
+    assert np.abs(a[:, 8:11] - b[:, 8:11]).max() <= 1e-11 * np.abs(a[:, 8:11]).max()
+    dims = orc.grid_dims(d4)
+    assert dims[2] == 4 * orc.grid_dims(d)[2]
