@@ -179,6 +179,51 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def batched_vs_plain(args, torch) -> dict:
+    """The 256-scene workload stepped as one batched sim (one launch per pass
+    over all scenes, CUDA graph) and as 256 single-scene sims run one at a
+    time (each its own graph).  Host wall-clock around the GPU work, with a
+    synchronise at the end of every scene's steps in the plain leg."""
+    from coupledwateranimation_gb300 import Sim, scenes
+    wl = scenes.with_zsub(scenes.config3(), args.zsub)
+    steps = max(3, min(args.steps, 10))
+    n_units = wl.n_particles + wl.n_wave_cells
+    with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True) as sim:
+        for k, s in enumerate(wl.scenes):
+            sim.upload_particles(k, s.particles)
+            sim.upload_wave(k, s.wave, s.wave)
+        sim.step(3)
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.step(steps)
+        sim.synchronize()
+        t_batched = time.perf_counter() - t0
+        launches = sim.launch_count
+    plain = []
+    try:
+        for s in wl.scenes:
+            p = Sim(s.desc, precision=args.precision, use_graph=True)
+            p.upload_particles(0, s.particles)
+            p.upload_wave(0, s.wave, s.wave)
+            p.step(3)
+            p.synchronize()
+            plain.append(p)
+        t0 = time.perf_counter()
+        for p in plain:
+            p.step(steps)
+            p.synchronize()
+        t_plain = time.perf_counter() - t0
+    finally:
+        for p in plain:
+            p.close()
+    return {"workload": wl.name, "scenes": len(wl.scenes), "particles": wl.n_particles,
+            "wave_cells": wl.n_wave_cells, "steps": steps,
+            "batched_updates_per_s": n_units * steps / t_batched,
+            "plain_updates_per_s": n_units * steps / t_plain,
+            "speedup": t_plain / t_batched,
+            "batched_ms_per_step": t_batched / steps * 1e3, "plain_ms_per_step": t_plain / steps * 1e3}
+
+
 def run_gpu(args) -> None:
     import torch
     import torch.distributed as dist
@@ -190,7 +235,7 @@ def run_gpu(args) -> None:
     torch.cuda.set_device(local)
     if ws > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    wl = scenes.CONFIGS[args.config]()
+    wl = scenes.with_zsub(scenes.CONFIGS[args.config](), args.zsub)
     sims = []
     sim = Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local)
     for k, s in enumerate(wl.scenes):
@@ -294,6 +339,9 @@ def run_gpu(args) -> None:
     e2e_value = n_units * ws * e2e_steps / e2e_s
     clk.__exit__(None, None, None)
 
+    batched = None
+    if rank == 0 and ws == 1 and not args.no_batched:
+        batched = batched_vs_plain(args, torch)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         v, steps, secs, cores = _cpu_leg(wl, float(os.environ.get("CWA_CPU_SECONDS", "20")))
@@ -310,6 +358,7 @@ def run_gpu(args) -> None:
             "data": "synthetic (seeded dam-break + Gaussian bumps)",
             "config": {"workload": wl.name, "particles": wl.n_particles, "wave_cells": wl.n_wave_cells,
                        "grid_cells": n_c, "precision": ["fp32", "fp32-compensated", "fp64"][args.precision],
+                       "grid_cell": f"h x h x h/{args.zsub}",
                        "l2": "flushed before every step (256 MiB write, outside the step events)",
                        "parallelism": f"replicas x{ws}"},
             "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
@@ -324,9 +373,27 @@ def run_gpu(args) -> None:
         }
         if cpu:
             line["cpu_baseline"] = cpu
+        if batched:
+            line["batched_vs_plain"] = batched
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+def run_profile(args) -> None:
+    """Plain eager steps of the workload for ncu captures: no timing, no L2
+    flush, each kernel a separate launch (the launch order of one step is
+    hash, scan, list insert, reorder, rho_pres, force, integrate, wave)."""
+    from coupledwateranimation_gb300 import Sim, scenes
+    wl = scenes.with_zsub(scenes.CONFIGS[args.config](), args.zsub)
+    with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=False) as sim:
+        for k, s in enumerate(wl.scenes):
+            sim.upload_particles(k, s.particles)
+            sim.upload_wave(k, s.wave, s.wave)
+        sim.step(args.warmup + args.steps)
+        sim.synchronize()
+        print(json.dumps({"mode": "profile", "workload": wl.name, "steps": args.warmup + args.steps,
+                          "launches": sim.launch_count}))
 
 
 def main() -> None:
@@ -335,14 +402,19 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
     ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2])
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--zsub", type=int, default=2, help="z sub-cells per h of the sort grid")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.mode == "profile":
+        run_profile(args)
     else:
         run_gpu(args)
 
