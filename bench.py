@@ -192,6 +192,8 @@ def batched_vs_plain(args, torch) -> dict:
         for k, s in enumerate(wl.scenes):
             sim.upload_particles(k, s.particles)
             sim.upload_wave(k, s.wave, s.wave)
+        if not args.no_tune:
+            sim.autotune(trial_steps=2)
         sim.step(3)
         sim.synchronize()
         t0 = time.perf_counter()
@@ -246,6 +248,9 @@ def run_gpu(args) -> None:
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     n_units = wl.n_particles + wl.n_wave_cells
 
+    tune = None
+    if not args.no_tune:  # pick the kernel variants on this workload (state restored)
+        tune = sim.autotune(trial_steps=3)
     clk = ClockSampler(local).__enter__()  # samples across warm-up, timed steps, profile and e2e
     # warm-up (graph capture happens here); keep the GPU loaded until the
     # clock sampler is logging, at most ~5 s
@@ -369,6 +374,8 @@ def run_gpu(args) -> None:
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps},
             "gpu_launches": launches,
+            "autotune": None if tune is None else {"best": tune["best"], "best_ms": tune["best_ms"],
+                                                  "entry_ms": tune["entry_ms"], "tried": len(tune["tried"])},
             "clocks": clk.summary(),
         }
         if cpu:
@@ -407,6 +414,7 @@ def main() -> None:
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--zsub", type=int, default=2, help="z sub-cells per h of the sort grid")
     args = ap.parse_args()
     if args.warmup < 3:

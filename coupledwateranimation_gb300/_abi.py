@@ -58,7 +58,13 @@ class SceneDesc(C.Structure):
 
 class SimOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("use_graph", C.c_int32),
-                ("nb_threads", C.c_int32), ("nb_stage", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("nb_threads", C.c_int32), ("nb_stage", C.c_int32), ("verlet_skin", C.c_float),
+                ("nb_scan_minb", C.c_int32), ("nb_force_minb", C.c_int32), ("reserved", C.c_int32 * 4)]
+
+
+class TuneReport(C.Structure):
+    _fields_ = [("best", SimOptions), ("best_ms", C.c_float), ("entry_ms", C.c_float),
+                ("n_tried", C.c_int32), ("tried", SimOptions * 32), ("tried_ms", C.c_float * 32)]
 
 
 class DeviceView(C.Structure):
@@ -99,6 +105,7 @@ _PROTOS = {
     "cwa_pass_wave": (C.c_int, [_P]),
     "cwa_synchronize": (C.c_int, [_P]),
     "cwa_get_step_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "cwa_get_rebuild_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "cwa_get_device_view": (C.c_int, [_P, _I32, C.POINTER(DeviceView)]),
     "cwa_download_grid": (C.c_int, [_P, _I32, _P, _I32, _P, _I32]),
     "cwa_download_deposits": (C.c_int, [_P, _I32, _P, _I32, _I32]),
@@ -108,6 +115,8 @@ _PROTOS = {
     "cwa_set_profiling": (C.c_int, [_P, _I32]),
     "cwa_get_pass_times": (C.c_int, [_P, _P, _I32]),
     "cwa_get_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "cwa_autotune": (C.c_int, [_P, _I32, C.POINTER(TuneReport)]),
+    "cwa_get_options": (C.c_int, [_P, C.POINTER(SimOptions)]),
     "cwa_scan_workspace_bytes": (C.c_size_t, [_I32]),
     "cwa_exclusive_scan_i32": (C.c_int, [_P, _P, _I32, _P, C.c_size_t, _P]),
     "cwa_exclusive_scan_i32_noalloc": (C.c_int, [_P, _P, _I32, _P]),

@@ -13,6 +13,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -51,8 +52,16 @@ struct cwa_sim {
   int32_t* list = nullptr;
   int32_t* count = nullptr;
   int32_t* start = nullptr;
-  uint16_t* nbr = nullptr;     // neighbour lists, kMaxNbr x n_total codes
+  uint16_t* nbr = nullptr;     // this step's hit lists, kMaxNbr x n_total codes
   int32_t* nbr_cnt = nullptr;
+  int32_t* KS = nullptr;       // sorted cell key of each particle (last grid build)
+  // Verlet mode
+  bool verlet = false;
+  uint16_t* vlist = nullptr;   // kMaxVerlet x n_total codes
+  int32_t* vcnt = nullptr;
+  float4* XR = nullptr;        // positions at the last rebuild
+  int32_t* d_flag = nullptr;   // rebuild flag, raised by integrate / uploads
+  unsigned long long* d_rebuilds = nullptr;
   void* scan_ws = nullptr;
   ScanWorkspace scan{};
   // wave: U[wcur] = u^n, U[(wcur+2)%3] = u^(n-1), U[(wcur+1)%3] = next
@@ -77,6 +86,7 @@ struct cwa_sim {
   bool pass_times_valid = false;
   cudaEvent_t ev[CWA_PASS_COUNT + 1] = {};
   cudaGraphExec_t graph[6] = {};
+  int64_t graph_launches[6] = {};
   std::vector<void*> dev_allocs;
 };
 
@@ -150,7 +160,7 @@ cwa_status validate_scene(const cwa_scene_desc& d, int idx) {
 }
 
 SceneDev make_scene_dev(const cwa_scene_desc& d, const int32_t dims[3], int32_t poff, int32_t coff,
-                        int32_t woff) {
+                        int32_t woff, float skin) {
   SceneDev s;
   memset(&s, 0, sizeof(s));
   const bool ref = d.preset == CWA_PRESET_REFERENCE_3D;
@@ -170,6 +180,14 @@ SceneDev make_scene_dev(const cwa_scene_desc& d, const int32_t dims[3], int32_t 
   s.inv_cellz = 1.0f / s.cellz;
   s.hs = (float)((double)d.smoothing_length * (1.0 + 1.0 / 1024.0));
   s.hs2 = s.hs * s.hs;
+  s.hl = skin > 0.0f ? (float)((double)d.smoothing_length * (1.0 + skin) * (1.0 + 1.0 / 1024.0)) : s.hs;
+  s.hl2 = s.hl * s.hl;
+  s.rz = (int32_t)ceilf(s.hl * s.inv_cellz) + 1;
+  // The rebuild threshold uses the skin the x/y cells really hold, so every
+  // pair that can come within h before the next rebuild is in the list.
+  const double skin_eff = std::min((double)skin, (double)d.cell_size / (double)d.smoothing_length - 1.0);
+  s.disp2 = skin > 0.0f ? (float)(0.25 * skin_eff * skin_eff * (double)d.smoothing_length * d.smoothing_length)
+                        : 0.0f;
   s.preset = d.preset;
   s.h = d.smoothing_length;
   s.h2 = d.smoothing_length * d.smoothing_length;
@@ -227,46 +245,130 @@ cwa_status check_scene(cwa_sim* s, int32_t scene) {
 
 float4* cur_force(cwa_sim* s) { return s->move_force ? s->F[s->cur] : s->F[0]; }
 
+// Particle work tiles of `size` particles, never straddling two scenes.
+std::vector<Tile> particle_tiles(const cwa_sim* s, int32_t size) {
+  std::vector<Tile> t;
+  for (size_t i = 0; i < s->sd.size(); ++i) {
+    const SceneDev& d = s->sd[i];
+    for (int32_t b = 0; b < d.n; b += size)
+      t.push_back(Tile{(int32_t)i, d.poff + b, d.poff + std::min(b + size, d.n)});
+  }
+  return t;
+}
+
+cwa_status set_particle_tiles(cwa_sim* s, int32_t size) {
+  std::vector<Tile> t = particle_tiles(s, size);
+  Tile* d = nullptr;
+  CWA_CUDA(cudaMalloc((void**)&d, std::max<size_t>(t.size(), 1) * sizeof(Tile)));
+  if (!t.empty()) {
+    cudaError_t e = cudaMemcpy(d, t.data(), t.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(d);
+      CWA_CUDA(e);
+    }
+  }
+  for (auto& p : s->dev_allocs)
+    if (p == s->d_ptiles) {
+      cudaFree(p);
+      p = d;
+    }
+  s->d_ptiles = d;
+  s->n_ptiles = (int32_t)t.size();
+  s->ptile = size;
+  return CWA_OK;
+}
+
+void drop_graphs(cwa_sim* s) {
+  for (auto& g : s->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
 // ---- passes (enqueue only) ----
+NbArgs nb_args(cwa_sim* s) {
+  NbArgs a;
+  a.pos = s->P[s->cur];
+  a.vel = s->V[s->cur];
+  a.force = cur_force(s);
+  a.rho_p = s->RP;
+  a.start = s->start;
+  a.keys = s->KS;
+  a.tiles = s->d_ptiles;
+  a.n_tiles = s->n_ptiles;
+  a.tile_size = s->ptile;
+  a.scenes = s->d_scenes;
+  a.wave = s->U[s->wcur];
+  a.nbr = s->nbr;
+  a.nbr_cnt = s->nbr_cnt;
+  a.vlist = s->vlist;
+  a.vcnt = s->vcnt;
+  a.xref = s->XR;
+  a.n_total = s->n_total;
+  a.status = s->d_status;
+  a.flag = s->verlet ? s->d_flag : nullptr;
+  a.stage = s->opt.nb_stage >= 0 ? 1 : 0;
+  a.scan_minb = s->opt.nb_scan_minb ? s->opt.nb_scan_minb : 4;
+  a.force_minb = s->opt.nb_force_minb ? s->opt.nb_force_minb : 8;
+  return a;
+}
+
+// Grid pass: hash + count, scan, stable insert, reorder.  Per-step mode
+// flips the live buffers every step.  Verlet mode runs the same kernels
+// only when the device rebuild flag is up (each kernel checks it), copies
+// the reordered state back into the live buffers and rebuilds the Verlet
+// list, so the host-side buffer roles never change.
 cwa_status run_grid(cwa_sim* s) {
   cudaStream_t st = s->stream;
-  const int nxt = s->cur ^ 1;
-  CWA_CUDA(launch_hash_count(s->P[s->cur], s->d_ptiles, s->n_ptiles, s->ptile, s->d_scenes, s->key, s->slot,
-                             s->count, s->d_status, st));
+  const int cur = s->cur, nxt = cur ^ 1;
+  const int32_t* flag = s->verlet ? s->d_flag : nullptr;
+  CWA_CUDA(launch_hash_count(s->P[cur], s->d_ptiles, s->n_ptiles, s->ptile, s->d_scenes, s->key, s->slot,
+                             s->count, s->d_status, flag, st));
   s->launches += s->n_ptiles > 0;
   CWA_CUDA(scan_launch(s->count, s->start, s->c_total, s->c_total + 1, true, s->scan, s->d_status, st,
-                       &s->launches));
-  CWA_CUDA(launch_list_insert(s->key, s->slot, s->start, s->list, s->n_total, st));
-  CWA_CUDA(launch_rank_reorder(s->key, s->slot, s->start, s->list, s->P[s->cur], s->V[s->cur],
-                               s->move_force ? s->F[s->cur] : nullptr, s->ID[s->cur], s->P[nxt], s->V[nxt],
-                               s->move_force ? s->F[nxt] : nullptr, s->ID[nxt], s->n_total, s->d_status, st));
+                       &s->launches, flag));
+  CWA_CUDA(launch_list_insert(s->key, s->slot, s->start, s->list, s->n_total, flag, st));
+  CWA_CUDA(launch_rank_reorder(s->key, s->slot, s->start, s->list, s->P[cur], s->V[cur],
+                               s->move_force ? s->F[cur] : nullptr, s->ID[cur], s->P[nxt], s->V[nxt],
+                               s->move_force ? s->F[nxt] : nullptr, s->ID[nxt], s->KS, s->n_total, s->d_status,
+                               flag, st));
   s->launches += s->n_total > 0 ? 2 : 0;
-  s->cur = nxt;
+  if (s->verlet) {
+    CWA_CUDA(launch_copy_back(s->P[nxt], s->V[nxt], s->move_force ? s->F[nxt] : nullptr, s->ID[nxt], s->P[cur],
+                              s->V[cur], s->move_force ? s->F[cur] : nullptr, s->ID[cur], s->n_total, s->d_flag,
+                              s->d_rebuilds, st));
+    CWA_CUDA(launch_scan_cands(s->opt.precision, true, nb_args(s), st));
+    s->launches += s->n_total > 0 ? 2 : 0;
+  } else {
+    s->cur = nxt;
+  }
   s->grid_fresh = true;
   return CWA_OK;
 }
 
 cwa_status run_rho_pres(cwa_sim* s) {
-  CWA_CUDA(launch_rho_pres(s->opt.precision, s->P[s->cur], s->start, s->d_ptiles, s->n_ptiles, s->ptile,
-                           s->d_scenes, s->U[s->wcur], s->RP, s->nbr, s->nbr_cnt, s->n_total, s->d_status,
-                           s->opt.nb_stage >= 0 ? 1 : 0, s->stream));
+  if (s->verlet)
+    CWA_CUDA(launch_rho_list(s->opt.precision, nb_args(s), s->stream));
+  else
+    CWA_CUDA(launch_scan_cands(s->opt.precision, false, nb_args(s), s->stream));
   s->launches += s->n_ptiles > 0;
   return CWA_OK;
 }
 
 cwa_status run_force(cwa_sim* s) {
-  CWA_CUDA(launch_force(s->opt.precision, s->P[s->cur], s->V[s->cur], s->RP, s->start, s->d_ptiles,
-                        s->n_ptiles, s->ptile, s->d_scenes, s->U[s->wcur], cur_force(s), s->nbr, s->nbr_cnt,
-                        s->n_total, s->stream));
+  CWA_CUDA(launch_force(s->opt.precision, nb_args(s), s->stream));
   s->launches += s->n_ptiles > 0;
   return CWA_OK;
 }
 
 cwa_status run_integrate(cwa_sim* s) {
+  if (s->verlet) CWA_CUDA(cudaMemsetAsync(s->d_flag, 0, sizeof(int32_t), s->stream));
   CWA_CUDA(launch_integrate(s->P[s->cur], s->V[s->cur], cur_force(s), s->RP, s->d_ptiles, s->n_ptiles,
-                            s->ptile, s->d_scenes, s->U[s->wcur], s->D, s->stream));
+                            s->ptile, s->d_scenes, s->U[s->wcur], s->D, s->verlet ? s->XR : nullptr,
+                            s->verlet ? s->d_flag : nullptr, s->stream));
   s->launches += s->n_ptiles > 0;
-  s->grid_fresh = false;
+  if (!s->verlet) s->grid_fresh = false;  // a Verlet list stays usable
   return CWA_OK;
 }
 
@@ -312,6 +414,7 @@ cwa_status graph_step(cwa_sim* s) {
     CWA_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     cwa_status st = enqueue_step(s);
     cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    s->graph_launches[phase] = s->launches - launches0;
     s->cur = cur0;
     s->wcur = w0;
     s->steps = steps0;
@@ -326,13 +429,16 @@ cwa_status graph_step(cwa_sim* s) {
     CWA_CUDA(e);
   }
   // The launch-count and state bookkeeping of one step, as enqueue_step does.
-  const int64_t before = s->launches;
   CWA_CUDA(cudaGraphLaunch(s->graph[phase], s->stream));
-  s->launches = before + (s->n_ptiles > 0 ? 6 : 0) + 1 + 1;  // hash,list,reorder,rho,force,integrate + scan + wave
-  s->cur ^= 1;
+  s->launches += s->graph_launches[phase];
+  if (!s->verlet) {
+    s->cur ^= 1;
+    s->grid_fresh = false;
+  } else {
+    s->grid_fresh = true;
+  }
   s->wcur = (s->wcur + 1) % 3;
   s->steps += 1;
-  s->grid_fresh = false;
   return CWA_OK;
 }
 
@@ -404,6 +510,9 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   if (opt) o = *opt;
   if (o.precision < CWA_PREC_FP32 || o.precision > CWA_PREC_FP64) return arg_error("unknown precision");
   if (o.nb_stage < -1 || o.nb_stage > 1) return arg_error("nb_stage must be -1, 0 or 1");
+  if (!(o.verlet_skin >= 0.0f && o.verlet_skin <= 1.0f)) return arg_error("verlet_skin must be in [0, 1]");
+  if (o.nb_scan_minb < 0 || o.nb_scan_minb > 8 || o.nb_force_minb < 0 || o.nb_force_minb > 8)
+    return arg_error("nb_scan_minb and nb_force_minb must be 0..8");
   if (o.nb_threads != 0 && (o.nb_threads < 32 || o.nb_threads > 128 || (o.nb_threads & 31)))
     return arg_error("nb_threads must be 0 or a multiple of 32 in [32, 128]");
   std::vector<int32_t> dims(3 * (size_t)n_scenes);
@@ -411,6 +520,12 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   int32_t nmax = 0;
   for (int i = 0; i < n_scenes; ++i) {
     CWA_TRY(validate_scene(scenes[i], i));
+    if (o.verlet_skin > 0.0f && !((double)scenes[i].cell_size >=
+                                  (double)scenes[i].smoothing_length * (1.0 + o.verlet_skin) * (1.0 - 1e-5))) {
+      char buf[160];
+      snprintf(buf, sizeof(buf), "scene %d: Verlet mode needs cell_size >= h (1 + verlet_skin)", i);
+      return arg_error(buf);
+    }
     cwa_status st = cwa_grid_dims(&scenes[i], &dims[3 * (size_t)i]);
     if (st != CWA_OK) return st == CWA_ERR_CAPACITY ? st : arg_error("bad grid dimensions");
     np += scenes[i].n_particles;
@@ -440,6 +555,7 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   s->w_total = (int32_t)nw;
   s->n_max = nmax;
   s->ptile = o.nb_threads ? o.nb_threads : 128;
+  s->verlet = o.verlet_skin > 0.0f;
   auto fail = [&](cwa_status st) {
     free_sim(s);
     return st;
@@ -450,7 +566,7 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   int32_t poff = 0, coff = 0, woff = 0;
   for (int i = 0; i < n_scenes; ++i) {
     const cwa_scene_desc& d = scenes[i];
-    s->sd.push_back(make_scene_dev(d, &dims[3 * (size_t)i], poff, coff, woff));
+    s->sd.push_back(make_scene_dev(d, &dims[3 * (size_t)i], poff, coff, woff, o.verlet_skin));
     if (d.preset == CWA_PRESET_REFERENCE_3D) s->move_force = true;
     for (int32_t b = 0; b < d.n_particles; b += s->ptile)
       ptiles.push_back(Tile{i, poff + b, poff + std::min(b + s->ptile, d.n_particles)});
@@ -485,6 +601,14 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   ALLOC(s->list, N);
   ALLOC(s->nbr, N * kMaxNbr);
   ALLOC(s->nbr_cnt, N);
+  ALLOC(s->KS, N);
+  ALLOC(s->d_flag, 1);
+  ALLOC(s->d_rebuilds, 1);
+  if (s->verlet) {
+    ALLOC(s->vlist, N * kMaxVerlet);
+    ALLOC(s->vcnt, N);
+    ALLOC(s->XR, N);
+  }
   ALLOC(s->count, (size_t)s->c_total);
   ALLOC(s->start, (size_t)s->c_total + 1);
   {
@@ -510,6 +634,10 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(CWA_ERR_CUDA);
   for (auto& e : s->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return fail(CWA_ERR_CUDA);
+  if (s->verlet) {  // the first step builds the grid and the Verlet list
+    const int32_t one = 1;
+    if (cudaMemcpy(s->d_flag, &one, sizeof(one), cudaMemcpyHostToDevice) != cudaSuccess) return fail(CWA_ERR_CUDA);
+  }
   std::vector<int32_t> ids(N);
   for (size_t i = 0; i < s->sd.size(); ++i)
     for (int32_t k = 0; k < s->sd[i].n; ++k) ids[(size_t)s->sd[i].poff + k] = k;
@@ -548,6 +676,10 @@ cwa_status cwa_upload_particles(cwa_sim* s, int32_t scene, const cwa_particle* h
                          s->ID[s->cur], s->stream));
   s->launches += 1;
   s->grid_fresh = false;
+  if (s->verlet) {  // the new particles need a fresh grid and Verlet list
+    const int32_t one = 1;
+    CWA_CUDA(cudaMemcpyAsync(s->d_flag, &one, sizeof(one), cudaMemcpyHostToDevice, s->stream));
+  }
   CWA_CUDA(cudaStreamSynchronize(s->stream));
   return CWA_OK;
 }
@@ -618,7 +750,22 @@ cwa_status cwa_step(cwa_sim* s, int32_t n_steps) {
 
 cwa_status cwa_pass_grid(cwa_sim* s) {
   CWA_TRY(check_sim(s));
+  if (s->verlet) {  // an explicit grid pass always rebuilds
+    const int32_t one = 1;
+    CWA_CUDA(cudaMemcpyAsync(s->d_flag, &one, sizeof(one), cudaMemcpyHostToDevice, s->stream));
+    CWA_CUDA(cudaStreamSynchronize(s->stream));
+  }
   return run_grid(s);
+}
+
+cwa_status cwa_get_rebuild_count(cwa_sim* s, int64_t* rebuilds) {
+  CWA_TRY(check_sim(s));
+  if (!rebuilds) return arg_error("null output");
+  unsigned long long v = 0;
+  CWA_CUDA(cudaMemcpyAsync(&v, s->d_rebuilds, sizeof(v), cudaMemcpyDeviceToHost, s->stream));
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  *rebuilds = (int64_t)v;
+  return CWA_OK;
 }
 
 cwa_status cwa_pass_rho_pres(cwa_sim* s) {
@@ -720,10 +867,34 @@ cwa_status cwa_reduce_totals(cwa_sim* s, int32_t scene, double out[CWA_TOTALS_CO
   return CWA_OK;
 }
 
-// Checkpoint: "CWAS", version 1, n_scenes, step count, then per scene its
-// descriptor and the sorted internal state (pos, vel, force, rho_p, id,
-// extras.zw) plus u^n and u^(n-1).  Restoring the sorted order keeps the
-// resumed run bit-identical to an uninterrupted one.
+// Checkpoint: "CWAS", version 2, n_scenes, step count, every scene's
+// descriptor, then the sim's device state in a fixed order: the sorted
+// particle arrays (pos, vel, force, rho_p, id), extras.zw, the sorted keys
+// and cell starts of the last grid build, u^n and u^(n-1), and in Verlet
+// mode the Verlet list, its counts, the rebuild positions and the rebuild
+// flag.  Restoring the sorted order and the grid keeps a resumed run
+// bit-identical to an uninterrupted one.
+struct StateItem {
+  void* dev;
+  size_t bytes;
+};
+
+std::vector<StateItem> state_items(cwa_sim* s) {
+  const size_t N = (size_t)s->n_total, W = (size_t)s->w_total;
+  std::vector<StateItem> it = {
+      {s->P[s->cur], N * 16}, {s->V[s->cur], N * 16}, {cur_force(s), N * 16}, {s->RP, N * 8},
+      {s->ID[s->cur], N * 4}, {s->EX, N * 8},          {s->KS, N * 4},        {s->start, ((size_t)s->c_total + 1) * 4},
+      {s->U[s->wcur], W * 4}, {s->U[(s->wcur + 2) % 3], W * 4},
+  };
+  if (s->verlet) {
+    it.push_back({s->vlist, N * kMaxVerlet * 2});
+    it.push_back({s->vcnt, N * 4});
+    it.push_back({s->XR, N * 16});
+    it.push_back({s->d_flag, 4});
+  }
+  return it;
+}
+
 cwa_status cwa_save(cwa_sim* s, const char* path) {
   CWA_TRY(check_sim(s));
   if (!path) return arg_error("null path");
@@ -735,35 +906,24 @@ cwa_status cwa_save(cwa_sim* s, const char* path) {
   }
   bool ok = true;
   auto put = [&](const void* p, size_t b) { ok = ok && (b == 0 || fwrite(p, 1, b, f) == b); };
-  const uint32_t magic = 0x53415743u, version = 1;  // "CWAS"
-  const int32_t ns = (int32_t)s->desc.size();
+  const uint32_t magic = 0x53415743u, version = 2;  // "CWAS"
+  const int32_t ns = (int32_t)s->desc.size(), verlet = s->verlet ? 1 : 0;
   put(&magic, 4);
   put(&version, 4);
   put(&ns, 4);
+  put(&verlet, 4);
   put(&s->steps, 8);
+  put(s->desc.data(), s->desc.size() * sizeof(cwa_scene_desc));
   std::vector<char> buf;
-  for (int32_t i = 0; i < ns && ok; ++i) {
-    const SceneDev& d = s->sd[i];
-    put(&s->desc[i], sizeof(cwa_scene_desc));
-    struct Item {
-      const void* dev;
-      size_t bytes;
-    } items[] = {
-        {s->P[s->cur] + d.poff, (size_t)d.n * 16}, {s->V[s->cur] + d.poff, (size_t)d.n * 16},
-        {cur_force(s) + d.poff, (size_t)d.n * 16}, {s->RP + d.poff, (size_t)d.n * 8},
-        {s->ID[s->cur] + d.poff, (size_t)d.n * 4}, {s->EX + d.poff, (size_t)d.n * 8},
-        {s->U[s->wcur] + d.woff, (size_t)d.nx * d.nz * 4},
-        {s->U[(s->wcur + 2) % 3] + d.woff, (size_t)d.nx * d.nz * 4},
-    };
-    for (const Item& it : items) {
-      buf.resize(it.bytes);
-      if (it.bytes && cudaMemcpy(buf.data(), it.dev, it.bytes, cudaMemcpyDeviceToHost) != cudaSuccess) {
-        fclose(f);
-        set_error("checkpoint readback failed");
-        return CWA_ERR_CUDA;
-      }
-      put(buf.data(), it.bytes);
+  for (const StateItem& it : state_items(s)) {
+    if (!ok) break;
+    buf.resize(it.bytes);
+    if (it.bytes && cudaMemcpy(buf.data(), it.dev, it.bytes, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      fclose(f);
+      set_error("checkpoint readback failed");
+      return CWA_ERR_CUDA;
     }
+    put(buf.data(), it.bytes);
   }
   if (fclose(f) != 0) ok = false;
   if (!ok) {
@@ -784,47 +944,32 @@ cwa_status cwa_load(cwa_sim* s, const char* path) {
   bool ok = true;
   auto get = [&](void* p, size_t b) { ok = ok && (b == 0 || fread(p, 1, b, f) == b); };
   uint32_t magic = 0, version = 0;
-  int32_t ns = 0;
+  int32_t ns = 0, verlet = 0;
   int64_t steps = 0;
   get(&magic, 4);
   get(&version, 4);
   get(&ns, 4);
+  get(&verlet, 4);
   get(&steps, 8);
-  if (!ok || magic != 0x53415743u || version != 1 || ns != (int32_t)s->desc.size()) {
+  std::vector<cwa_scene_desc> desc(ns > 0 && ns == (int32_t)s->desc.size() ? ns : 0);
+  if (ok) get(desc.data(), desc.size() * sizeof(cwa_scene_desc));
+  if (!ok || magic != 0x53415743u || version != 2 || ns != (int32_t)s->desc.size() ||
+      verlet != (s->verlet ? 1 : 0) ||
+      memcmp(desc.data(), s->desc.data(), desc.size() * sizeof(cwa_scene_desc)) != 0) {
     fclose(f);
-    set_error("checkpoint header does not match this sim");
+    set_error("checkpoint does not match this sim (scenes, mode or version)");
     return ok ? CWA_ERR_INVALID_ARG : CWA_ERR_IO;
   }
   CWA_CUDA(cudaStreamSynchronize(s->stream));
   std::vector<char> buf;
-  for (int32_t i = 0; i < ns && ok; ++i) {
-    const SceneDev& d = s->sd[i];
-    cwa_scene_desc desc;
-    get(&desc, sizeof(desc));
-    if (!ok || memcmp(&desc, &s->desc[i], sizeof(desc)) != 0) {
+  for (const StateItem& it : state_items(s)) {
+    buf.resize(it.bytes);
+    get(buf.data(), it.bytes);
+    if (!ok) break;
+    if (it.bytes && cudaMemcpy(it.dev, buf.data(), it.bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
       fclose(f);
-      set_error("checkpoint scene descriptor does not match this sim");
-      return ok ? CWA_ERR_INVALID_ARG : CWA_ERR_IO;
-    }
-    struct Item {
-      void* dev;
-      size_t bytes;
-    } items[] = {
-        {s->P[s->cur] + d.poff, (size_t)d.n * 16}, {s->V[s->cur] + d.poff, (size_t)d.n * 16},
-        {cur_force(s) + d.poff, (size_t)d.n * 16}, {s->RP + d.poff, (size_t)d.n * 8},
-        {s->ID[s->cur] + d.poff, (size_t)d.n * 4}, {s->EX + d.poff, (size_t)d.n * 8},
-        {s->U[s->wcur] + d.woff, (size_t)d.nx * d.nz * 4},
-        {s->U[(s->wcur + 2) % 3] + d.woff, (size_t)d.nx * d.nz * 4},
-    };
-    for (const Item& it : items) {
-      buf.resize(it.bytes);
-      get(buf.data(), it.bytes);
-      if (!ok) break;
-      if (it.bytes && cudaMemcpy(it.dev, buf.data(), it.bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
-        fclose(f);
-        set_error("checkpoint upload failed");
-        return CWA_ERR_CUDA;
-      }
+      set_error("checkpoint upload failed");
+      return CWA_ERR_CUDA;
     }
   }
   fclose(f);
@@ -833,7 +978,7 @@ cwa_status cwa_load(cwa_sim* s, const char* path) {
     return CWA_ERR_IO;
   }
   s->steps = steps;
-  s->grid_fresh = false;
+  s->grid_fresh = s->verlet;  // per-step mode rebuilds its grid every step anyway
   return CWA_OK;
 }
 
@@ -857,6 +1002,122 @@ cwa_status cwa_get_launch_count(cwa_sim* s, int64_t* launches) {
   CWA_TRY(check_sim(s));
   if (!launches) return arg_error("null output");
   *launches = s->launches;
+  return CWA_OK;
+}
+
+// ---- autotuner ----
+// Tries the kernel variants on the sim's own state: candidate staging on /
+// off, the density-scan and force launch-bound variants and 128- or
+// 64-particle CTAs.  Every trial starts from a device-side snapshot of the
+// state and runs one warm-up step and `trial_steps` timed steps (CUDA
+// events, eager launches); the fastest is kept and the state restored.
+cwa_status cwa_autotune(cwa_sim* s, int32_t trial_steps, cwa_tune_report* out) {
+  CWA_TRY(check_sim(s));
+  if (trial_steps < 1 || trial_steps > 1000) return arg_error("trial_steps must be in [1, 1000]");
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  std::vector<StateItem> items = state_items(s);
+  size_t total = 0;
+  for (const StateItem& it : items) total += (it.bytes + 255) & ~(size_t)255;
+  char* snap = nullptr;
+  CWA_CUDA(cudaMalloc((void**)&snap, std::max<size_t>(total, 1)));
+  auto copy_state = [&](bool save) -> cudaError_t {
+    size_t off = 0;
+    for (const StateItem& it : items) {
+      cudaError_t e = save ? cudaMemcpyAsync(snap + off, it.dev, it.bytes, cudaMemcpyDeviceToDevice, s->stream)
+                           : cudaMemcpyAsync(it.dev, snap + off, it.bytes, cudaMemcpyDeviceToDevice, s->stream);
+      if (e != cudaSuccess) return e;
+      off += (it.bytes + 255) & ~(size_t)255;
+    }
+    return cudaSuccess;
+  };
+  const cwa_sim_options entry = s->opt;
+  const int32_t entry_ptile = s->ptile;
+  const int64_t steps0 = s->steps, launches0 = s->launches;
+  const int cur0 = s->cur, w0 = s->wcur;
+  const bool prof0 = s->profiling;
+  s->profiling = false;
+  cwa_tune_report rep;
+  memset(&rep, 0, sizeof(rep));
+  rep.best_ms = 1e30f;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t err = copy_state(true);
+  if (err == cudaSuccess) err = cudaEventCreate(&e0);
+  if (err == cudaSuccess) err = cudaEventCreate(&e1);
+  const int stages[2] = {0, -1}, scans[3] = {4, 6, 8}, forces[2] = {6, 8}, ctas[2] = {128, 64};
+  for (int a = 0; a < 2 && err == cudaSuccess; ++a)
+    for (int b = 0; b < 3 && err == cudaSuccess; ++b)
+      for (int c = 0; c < 2 && err == cudaSuccess; ++c)
+        for (int d = 0; d < 2 && err == cudaSuccess; ++d) {
+          cwa_sim_options o = entry;
+          o.nb_stage = stages[a];
+          o.nb_scan_minb = scans[b];
+          o.nb_force_minb = forces[c];
+          o.nb_threads = ctas[d];
+          s->opt = o;
+          if (s->ptile != ctas[d]) {
+            cwa_status st = set_particle_tiles(s, ctas[d]);
+            if (st != CWA_OK) {
+              err = cudaErrorMemoryAllocation;
+              break;
+            }
+          }
+          err = copy_state(false);
+          s->cur = cur0;
+          s->wcur = w0;
+          if (err != cudaSuccess) break;
+          cwa_status st = enqueue_step(s);  // warm-up
+          if (st == CWA_OK) err = cudaEventRecord(e0, s->stream);
+          for (int k = 0; k < trial_steps && st == CWA_OK && err == cudaSuccess; ++k) st = enqueue_step(s);
+          if (st != CWA_OK) {
+            err = cudaErrorLaunchFailure;
+            break;
+          }
+          if (err == cudaSuccess) err = cudaEventRecord(e1, s->stream);
+          if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+          float ms = 0.0f;
+          if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+          ms /= (float)trial_steps;
+          if (rep.n_tried < CWA_TUNE_MAX_TRIED) {
+            rep.tried[rep.n_tried] = o;
+            rep.tried_ms[rep.n_tried] = ms;
+          }
+          rep.n_tried++;
+          // the entry options, with 0 read as each knob's default
+          if ((o.nb_stage < 0) == (entry.nb_stage < 0) &&
+              o.nb_scan_minb == (entry.nb_scan_minb ? entry.nb_scan_minb : 4) &&
+              o.nb_force_minb == (entry.nb_force_minb ? entry.nb_force_minb : 8) &&
+              o.nb_threads == (entry.nb_threads ? entry.nb_threads : 128))
+            rep.entry_ms = ms;
+          if (ms < rep.best_ms) {
+            rep.best_ms = ms;
+            rep.best = o;
+          }
+        }
+  // keep the winner (or the entry options on failure) and restore the state
+  s->opt = err == cudaSuccess ? rep.best : entry;
+  const int32_t want_ptile = s->opt.nb_threads ? s->opt.nb_threads : entry_ptile;
+  if (s->ptile != want_ptile) set_particle_tiles(s, want_ptile);
+  cudaError_t e2 = copy_state(false);
+  if (err == cudaSuccess) err = e2;
+  cudaStreamSynchronize(s->stream);
+  s->cur = cur0;
+  s->wcur = w0;
+  s->steps = steps0;
+  s->launches = launches0;
+  s->profiling = prof0;
+  drop_graphs(s);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(snap);
+  if (out) *out = rep;
+  CWA_CUDA(err);
+  return CWA_OK;
+}
+
+cwa_status cwa_get_options(cwa_sim* s, cwa_sim_options* out) {
+  CWA_TRY(check_sim(s));
+  if (!out) return arg_error("null output");
+  *out = s->opt;
   return CWA_OK;
 }
 
@@ -916,7 +1177,7 @@ cwa_status cwa_grid_build(const float* d_pos4, int32_t n, const float lo[3], flo
   CWA_CUDA(launch_point_hash(reinterpret_cast<const float4*>(d_pos4), n, lo[0], lo[1], lo[2], cell_size, dims[0],
                              dims[1], dims[2], key, slot, count, status, st));
   CWA_CUDA(scan_launch(count, d_cell_start, nc, nc + 1, false, ws, status, st, nullptr));
-  CWA_CUDA(launch_list_insert(key, slot, d_cell_start, list, n, st));
+  CWA_CUDA(launch_list_insert(key, slot, d_cell_start, list, n, nullptr, st));
   CWA_CUDA(launch_point_rank(key, slot, d_cell_start, list, n, d_sorted_index, status, st));
   return CWA_OK;
 }

@@ -47,8 +47,9 @@ __device__ __forceinline__ int warp_sum(int v) {
 template <bool kZero>
 __global__ void __launch_bounds__(kScanBlock)
     k_scan(int32_t* in, int32_t* out, int32_t n_in, int32_t n_out, unsigned int* counter,
-           unsigned long long* state, int32_t* status) {
+           unsigned long long* state, int32_t* status, const int32_t* flag) {
   __shared__ int s_tile, s_prefix;
+  if (flag && __ldg(flag) == 0) return;  // grid kept this step (Verlet mode)
   __shared__ int s_warp[kScanBlock / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
@@ -160,7 +161,9 @@ __device__ __forceinline__ int count_slot(int32_t* count, int key) {
 __global__ void __launch_bounds__(256)
     k_hash_count(const float4* __restrict__ pos, const Tile* __restrict__ tiles,
                  const SceneDev* __restrict__ scenes, int32_t* __restrict__ key,
-                 int32_t* __restrict__ slot, int32_t* __restrict__ count, int32_t* status) {
+                 int32_t* __restrict__ slot, int32_t* __restrict__ count, int32_t* status,
+                 const int32_t* flag) {
+  if (flag && __ldg(flag) == 0) return;
   const Tile t = tiles[blockIdx.x];
   const SceneDev* S = scenes + t.scene;
   const float lx = S->lo[0], ly = S->lo[1], lz = S->lo[2], cs = S->cell, csz = S->cellz;
@@ -190,7 +193,9 @@ __global__ void k_point_hash(const float4* __restrict__ pos, int32_t n, float lx
 }
 
 __global__ void k_list_insert(const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
-                              const int32_t* __restrict__ start, int32_t* __restrict__ list, int32_t n) {
+                              const int32_t* __restrict__ start, int32_t* __restrict__ list, int32_t n,
+                              const int32_t* flag) {
+  if (flag && __ldg(flag) == 0) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   list[start[key[i]] + slot[i]] = i;
@@ -214,7 +219,9 @@ __global__ void __launch_bounds__(256)
                    const float4* __restrict__ pin, const float4* __restrict__ vin,
                    const float4* __restrict__ fin, const int32_t* __restrict__ idin,
                    float4* __restrict__ pout, float4* __restrict__ vout, float4* __restrict__ fout,
-                   int32_t* __restrict__ idout, int32_t n, int32_t* status) {
+                   int32_t* __restrict__ idout, int32_t* __restrict__ kout, int32_t n, int32_t* status,
+                   const int32_t* flag) {
+  if (flag && __ldg(flag) == 0) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int k = key[i];
@@ -224,6 +231,22 @@ __global__ void __launch_bounds__(256)
   vout[dst] = vin[i];
   if (fout) fout[dst] = fin[i];
   idout[dst] = idin[i];
+  kout[dst] = k;
+}
+
+__global__ void __launch_bounds__(256)
+    k_copy_back(const float4* __restrict__ p2, const float4* __restrict__ v2, const float4* __restrict__ f2,
+                const int32_t* __restrict__ id2, float4* __restrict__ p, float4* __restrict__ v,
+                float4* __restrict__ f, int32_t* __restrict__ id, int32_t n, const int32_t* flag,
+                unsigned long long* rebuilds) {
+  if (__ldg(flag) == 0) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rebuilds, 1ull);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    p[i] = p2[i];
+    v[i] = v2[i];
+    if (f) f[i] = f2[i];
+    id[i] = id2[i];
+  }
 }
 
 __global__ void k_point_rank(const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
@@ -254,42 +277,54 @@ void scan_bind_workspace(void* ws, int32_t n_out, ScanWorkspace* out) {
 }
 
 cudaError_t scan_launch(const int32_t* in, int32_t* out, int32_t n_in, int32_t n_out, bool zero_input,
-                        const ScanWorkspace& ws, int32_t* status, cudaStream_t stream, int64_t* launches) {
+                        const ScanWorkspace& ws, int32_t* status, cudaStream_t stream, int64_t* launches,
+                        const int32_t* flag) {
   if (n_out <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(ws.counter, 0, 256 + (size_t)ws.n_tiles * 8, stream);
   if (e != cudaSuccess) return e;
   int32_t* inw = const_cast<int32_t*>(in);
   if (zero_input)
-    k_scan<true><<<ws.n_tiles, kScanBlock, 0, stream>>>(inw, out, n_in, n_out, ws.counter, ws.state, status);
+    k_scan<true><<<ws.n_tiles, kScanBlock, 0, stream>>>(inw, out, n_in, n_out, ws.counter, ws.state, status,
+                                                         flag);
   else
-    k_scan<false><<<ws.n_tiles, kScanBlock, 0, stream>>>(inw, out, n_in, n_out, ws.counter, ws.state, status);
+    k_scan<false><<<ws.n_tiles, kScanBlock, 0, stream>>>(inw, out, n_in, n_out, ws.counter, ws.state, status,
+                                                          flag);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }
 
 cudaError_t launch_hash_count(const float4* pos, const Tile* tiles, int32_t n_tiles, int32_t tile_size,
                               const SceneDev* scenes, int32_t* key, int32_t* slot, int32_t* count,
-                              int32_t* status, cudaStream_t stream) {
+                              int32_t* status, const int32_t* flag, cudaStream_t stream) {
   if (n_tiles <= 0) return cudaSuccess;
-  k_hash_count<<<n_tiles, tile_size, 0, stream>>>(pos, tiles, scenes, key, slot, count, status);
+  k_hash_count<<<n_tiles, tile_size, 0, stream>>>(pos, tiles, scenes, key, slot, count, status, flag);
   return cudaGetLastError();
 }
 
 cudaError_t launch_list_insert(const int32_t* key, const int32_t* slot, const int32_t* start, int32_t* list,
-                               int32_t n, cudaStream_t stream) {
+                               int32_t n, const int32_t* flag, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  k_list_insert<<<blocks_for(n, 256), 256, 0, stream>>>(key, slot, start, list, n);
+  k_list_insert<<<blocks_for(n, 256), 256, 0, stream>>>(key, slot, start, list, n, flag);
   return cudaGetLastError();
 }
 
 cudaError_t launch_rank_reorder(const int32_t* key, const int32_t* slot, const int32_t* start,
                                 const int32_t* list, const float4* pin, const float4* vin,
                                 const float4* fin, const int32_t* idin, float4* pout, float4* vout,
-                                float4* fout, int32_t* idout, int32_t n, int32_t* status,
-                                cudaStream_t stream) {
+                                float4* fout, int32_t* idout, int32_t* kout, int32_t n, int32_t* status,
+                                const int32_t* flag, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   k_rank_reorder<<<blocks_for(n, 256), 256, 0, stream>>>(key, slot, start, list, pin, vin, fin, idin, pout,
-                                                         vout, fout, idout, n, status);
+                                                         vout, fout, idout, kout, n, status, flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_back(const float4* p2, const float4* v2, const float4* f2, const int32_t* id2,
+                             float4* p, float4* v, float4* f, int32_t* id, int32_t n, const int32_t* flag,
+                             unsigned long long* rebuilds, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  k_copy_back<<<min(blocks_for(n, 256), 1216), 256, 0, stream>>>(p2, v2, f2, id2, p, v, f, id, n, flag,
+                                                                 rebuilds);
   return cudaGetLastError();
 }
 

@@ -31,7 +31,10 @@ struct SceneDev {
   int32_t dims[3];
   float lo[3], hi[3];
   float cell, cellz, inv_cell, inv_cellz;  // x/y and z cell edges
-  float hs, hs2;  // search radius: h * (1 + 2^-10), so float rounding never drops a pair
+  float hs, hs2;  // h * (1 + 2^-10): float rounding never drops a pair
+  float hl, hl2;  // candidate-scan radius: hs, or h (1 + skin)(1 + 2^-10) in Verlet mode
+  int32_t rz;     // z cells below a particle's cell that cover its scan window
+  float disp2;    // Verlet rebuild threshold (skin h / 2)^2; 0 = per-step mode
   // physics
   int32_t preset;
   float h, h2, mass, visc, rho0, k, dt;
@@ -74,18 +77,27 @@ void scan_bind_workspace(void* ws, int32_t n_out, ScanWorkspace* out);
 // zero_input clears `in` as it is read.  Workspace must be zeroed first
 // (scan_launch does it with a memset on `stream`).
 cudaError_t scan_launch(const int32_t* in, int32_t* out, int32_t n_in, int32_t n_out, bool zero_input,
-                        const ScanWorkspace& ws, int32_t* status, cudaStream_t stream, int64_t* launches);
+                        const ScanWorkspace& ws, int32_t* status, cudaStream_t stream, int64_t* launches,
+                        const int32_t* flag = nullptr);
 
+// The grid-build kernels take the Verlet rebuild flag (null = always run).
 cudaError_t launch_hash_count(const float4* pos, const Tile* tiles, int32_t n_tiles, int32_t tile_size,
                               const SceneDev* scenes, int32_t* key, int32_t* slot, int32_t* count,
-                              int32_t* status, cudaStream_t stream);
+                              int32_t* status, const int32_t* flag, cudaStream_t stream);
 cudaError_t launch_list_insert(const int32_t* key, const int32_t* slot, const int32_t* start, int32_t* list,
-                               int32_t n, cudaStream_t stream);
+                               int32_t n, const int32_t* flag, cudaStream_t stream);
+// Moves the particle state into sorted order and writes each particle's cell
+// key (kout) in that order.
 cudaError_t launch_rank_reorder(const int32_t* key, const int32_t* slot, const int32_t* start,
                                 const int32_t* list, const float4* pin, const float4* vin,
                                 const float4* fin, const int32_t* idin, float4* pout, float4* vout,
-                                float4* fout, int32_t* idout, int32_t n, int32_t* status,
-                                cudaStream_t stream);
+                                float4* fout, int32_t* idout, int32_t* kout, int32_t n, int32_t* status,
+                                const int32_t* flag, cudaStream_t stream);
+// Verlet mode: copies the reordered state back into the live buffers (when
+// the flag is set) and counts rebuilds.
+cudaError_t launch_copy_back(const float4* p2, const float4* v2, const float4* f2, const int32_t* id2,
+                             float4* p, float4* v, float4* f, int32_t* id, int32_t n, const int32_t* flag,
+                             unsigned long long* rebuilds, cudaStream_t stream);
 // Plain point grid for cwa_grid_build (one scene, no reorder).
 cudaError_t launch_point_hash(const float4* pos, int32_t n, float lx, float ly, float lz, float cell,
                               int32_t dx, int32_t dy, int32_t dz, int32_t* key, int32_t* slot,
@@ -95,25 +107,51 @@ cudaError_t launch_point_rank(const int32_t* key, const int32_t* slot, const int
                               cudaStream_t stream);
 
 // ---- SPH kernels (cwa_sph.cu) ----
-// Neighbour list: nbr[k * n_total + i] (k < kMaxNbr) holds 16-bit hit codes
-// (row << 12 | offset in the row's sorted range; the particle itself is one
-// of them) and nbr_cnt[i] their count (kMaxNbr + 1 = overflow, force
-// rescans); written by rho_pres, read by force.  stage != 0 lets rho_pres
-// stage candidate rows in shared memory.
+// Neighbour lists hold 16-bit codes (row << 12 | offset from the row's
+// cell-based start), entry k of particle i at list[k * n_total + i].
+// nbr / nbr_cnt: this step's hits (r < h, the particle itself included),
+// written by the density pass and read by force.  vlist / vcnt: the Verlet
+// list (pairs within h (1 + skin) at the last rebuild).  A count of cap + 1
+// marks an overflowed list; its reader rescans the particle's rows.
 constexpr int kMaxNbr = 64;
-cudaError_t launch_rho_pres(int precision, const float4* pos, const int32_t* start, const Tile* tiles,
-                            int32_t n_tiles, int32_t tile_size, const SceneDev* scenes,
-                            const float* wave_u, float2* rho_p, uint16_t* nbr, int32_t* nbr_cnt,
-                            int32_t n_total, int32_t* status, int32_t stage, cudaStream_t stream);
-cudaError_t launch_force(int precision, const float4* pos, const float4* vel, const float2* rho_p,
-                         const int32_t* start, const Tile* tiles, int32_t n_tiles, int32_t tile_size,
-                         const SceneDev* scenes, const float* wave_u, float4* force, const uint16_t* nbr,
-                         const int32_t* nbr_cnt, int32_t n_total, cudaStream_t stream);
+constexpr int kMaxVerlet = 128;
+struct NbArgs {
+  const float4* pos;
+  const float4* vel;
+  float4* force;
+  float2* rho_p;
+  const int32_t* start;
+  const int32_t* keys;  // sorted cell key of each particle (at the last grid build)
+  const Tile* tiles;
+  int32_t n_tiles, tile_size;
+  const SceneDev* scenes;
+  const float* wave;
+  uint16_t* nbr;
+  int32_t* nbr_cnt;
+  uint16_t* vlist;
+  int32_t* vcnt;
+  float4* xref;         // positions at the last rebuild (Verlet mode)
+  int32_t n_total;
+  int32_t* status;
+  const int32_t* flag;  // rebuild flag (Verlet mode), else null
+  int32_t stage;        // candidate scan may stage rows in shared memory
+  int32_t scan_minb;    // launch-bound variant of the candidate scan (4, 6, 8)
+  int32_t force_minb;   // launch-bound variant of force (6, 8, 10)
+};
+// Candidate scan: the per-step density + hit list, or (list_mode) the
+// Verlet list, run only when *flag is set.
+cudaError_t launch_scan_cands(int precision, bool list_mode, const NbArgs& a, cudaStream_t stream);
+// Verlet-mode density over the Verlet list; writes the step's hit list.
+cudaError_t launch_rho_list(int precision, const NbArgs& a, cudaStream_t stream);
+cudaError_t launch_force(int precision, const NbArgs& a, cudaStream_t stream);
 
 // ---- integrate / wave / packing kernels (cwa_step.cu) ----
+// xref/flag (Verlet mode): raises *flag when a particle has moved more than
+// skin h / 2 from its rebuild position; null otherwise.
 cudaError_t launch_integrate(float4* pos, float4* vel, float4* force, float2* rho_p, const Tile* tiles,
                              int32_t n_tiles, int32_t tile_size, const SceneDev* scenes,
-                             const float* wave_u, unsigned long long* deposits, cudaStream_t stream);
+                             const float* wave_u, unsigned long long* deposits, const float4* xref,
+                             int32_t* flag, cudaStream_t stream);
 cudaError_t launch_wave(const float* u_n, const float* u_nm1, float* u_out, unsigned long long* deposits,
                         const Tile* wtiles, int32_t n_wtiles, int32_t wtile_size, const SceneDev* scenes,
                         cudaStream_t stream);

@@ -7,25 +7,31 @@
 //             (force_comp.glsl:160-237) or gravity only (MULLER).
 //
 // The reference loops over all N particles per particle (O(N^2)).  Here the
-// particles are sorted by uniform-grid cell (cell edge >= h), so the 27-cell
-// block around a particle is 9 contiguous z-rows of the sorted arrays; the
-// loop visits exactly those rows.  Every pair with r < h lies inside them,
-// so the neighbour sets equal the shaders'.
+// particles are sorted by uniform-grid cell (x/y cell edge >= the search
+// radius), so the candidates of a particle lie in 9 rows (columns x-1..x+1,
+// y-1..y+1) of the sorted arrays, each a contiguous z range.  Every pair with
+// r < h lies inside them, so the neighbour sets equal the shaders'.
 //
-// rho_pres does the candidate tests once.  A CTA owns up to 128 consecutive
-// sorted particles, which lie in one or two grid columns; it copies the
-// candidate rows of those columns into shared memory with bulk TMA copies
-// (cp.async.bulk, completion on an mbarrier) and tests every candidate from
-// shared memory.  Each particle's hits are kept as a neighbour list of 16-bit
-// codes (row << 12 | offset in the row's sorted range), which force decodes
-// with the same 9 row starts and runs its pair terms over.  CTAs whose
-// particles span more columns, or whose rows exceed the staging capacity,
-// read candidates straight from global memory (same order, same results).
+// Two modes (cwa_sim_options.verlet_skin):
+//  * per-step (skin 0): k_scan_cands tests every candidate of the particle's
+//    rows once, accumulates the density and keeps the hits as this step's
+//    neighbour list;
+//  * Verlet (skin > 0): the grid and a list of every pair within
+//    h (1 + skin) are rebuilt only when some particle has moved more than
+//    skin h / 2 since the last rebuild (integrate raises a device flag);
+//    k_rho_list walks that list each step, tests r < h and keeps the hits.
+// Either way force runs its pair terms over the step's hit list only.
+//
+// Neighbour lists hold 16-bit codes (row << 12 | offset from the row's
+// cell-based start = start[row + max(cz - rz, 0)]), decodable from the
+// particle's sorted cell key alone, so a Verlet list stays valid while the
+// particles move.  The candidate scan can stage the CTA's rows in shared
+// memory with bulk TMA copies (cp.async.bulk, completion on an mbarrier).
 //
 // Sums are accumulated in one of three precisions (template P):
-//   CWA_PREC_FP32 plain float; CWA_PREC_COMPENSATED float partial sums
-//   (per row for density, per 8 pairs for force) folded into a Knuth two-sum
-//   accumulator; CWA_PREC_FP64 double pair math and sums.
+//   CWA_PREC_FP32 plain float; CWA_PREC_COMPENSATED float partial sums (per
+//   row or per 8 pairs) folded into a Knuth two-sum accumulator;
+//   CWA_PREC_FP64 double pair math and sums.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -83,42 +89,80 @@ __device__ __forceinline__ CellCoord cell_of(const SceneDev* S, float4 p) {
   return c;
 }
 
-// Sorted-index ranges [b, e) of the 9 rows (columns x-1..x+1, y-1..y+1)
-// that can hold a neighbour within h of p.  A row whose column is farther
-// than h from p in (x, y) is empty; the others cover only the z cells of the
-// window |z - pz| < sqrt(h^2 - d^2), d = the column's (x, y) distance.  The
-// search radius is h (1 + 2^-10), so float rounding never drops a pair.
-// The 18 start loads are independent, so they overlap.
+// Cell coordinates of a global cell id.
+__device__ __forceinline__ CellCoord cell_of_key(const SceneDev* S, int key) {
+  const int local = key - S->coff, nz = S->dims[2], ny = S->dims[1];
+  const int xy = local / nz;
+  CellCoord c;
+  c.z = local - xy * nz;
+  c.x = xy / ny;
+  c.y = xy - c.x * ny;
+  return c;
+}
+
+__device__ __forceinline__ bool row_valid(const SceneDev* S, CellCoord c, int r) {
+  const int x = c.x + r / 3 - 1, y = c.y + r % 3 - 1;
+  return x >= 0 && x < S->dims[0] && y >= 0 && y < S->dims[1];
+}
+
+__device__ __forceinline__ int row_id(const SceneDev* S, CellCoord c, int r) {
+  return S->coff + ((c.x + r / 3 - 1) * S->dims[1] + (c.y + r % 3 - 1)) * S->dims[2];
+}
+
+// Cell-based start of each row: the base that neighbour codes are relative
+// to.  rz z cells below the particle's cell cover every window.
+__device__ __forceinline__ void row_bases(const SceneDev* S, const int32_t* __restrict__ start, CellCoord c,
+                                          int base[9]) {
+  const int z0 = max(c.z - S->rz, 0);
+#pragma unroll
+  for (int r = 0; r < 9; ++r) base[r] = row_valid(S, c, r) ? __ldg(start + row_id(S, c, r) + z0) : 0;
+}
+
+// Sorted-index ranges [b, e) of the candidates within radius sqrt(rad2) of
+// p, row by row.  A row whose column is farther than the radius in (x, y)
+// is empty; the others cover the z cells of the window
+// |z - pz| < sqrt(rad2 - d^2), d = the column's (x, y) distance.  The
+// radius carries a 2^-10 margin, so float rounding never drops a pair.
 __device__ __forceinline__ void row_ranges(const SceneDev* S, const int32_t* __restrict__ start, float4 p,
-                                           CellCoord c, int b[9], int e[9]) {
-  const int nx = S->dims[0], ny = S->dims[1], nz = S->dims[2];
+                                           CellCoord c, float rad2, int b[9], int e[9]) {
+  const int nz = S->dims[2];
   const float x0f = S->lo[0] + (float)c.x * S->cell;
   const float y0f = S->lo[1] + (float)c.y * S->cell;
   const float dxm = fmaxf(p.x - x0f, 0.0f), dxp = fmaxf(x0f + S->cell - p.x, 0.0f);
   const float dym = fmaxf(p.y - y0f, 0.0f), dyp = fmaxf(y0f + S->cell - p.y, 0.0f);
-  const float hs2 = S->hs2, zl = p.z - S->lo[2], izc = S->inv_cellz, zmax = (float)(nz - 1);
+  const float zl = p.z - S->lo[2], izc = S->inv_cellz, zmax = (float)(nz - 1);
 #pragma unroll
-  for (int dx = -1; dx <= 1; ++dx) {
-#pragma unroll
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int r = (dx + 1) * 3 + (dy + 1);
-      const int x = c.x + dx, y = c.y + dy;
-      const float ddx = dx < 0 ? dxm : (dx > 0 ? dxp : 0.0f);
-      const float ddy = dy < 0 ? dym : (dy > 0 ? dyp : 0.0f);
-      const float d2 = ddx * ddx + ddy * ddy;
-      const bool ok = x >= 0 && x < nx && y >= 0 && y < ny && d2 < hs2;
-      const float w = sqrtf(fmaxf(hs2 - d2, 0.0f));
-      const int z0 = (int)fminf(fmaxf(floorf((zl - w) * izc), 0.0f), zmax);
-      const int z1 = (int)fminf(fmaxf(floorf((zl + w) * izc), 0.0f), zmax);
-      const int row = S->coff + (x * ny + y) * nz;
-      b[r] = ok ? __ldg(start + row + z0) : 0;
-      e[r] = ok ? __ldg(start + row + z1 + 1) : 0;
-    }
+  for (int r = 0; r < 9; ++r) {
+    const int dx = r / 3 - 1, dy = r % 3 - 1;
+    const float ddx = dx < 0 ? dxm : (dx > 0 ? dxp : 0.0f);
+    const float ddy = dy < 0 ? dym : (dy > 0 ? dyp : 0.0f);
+    const float d2 = ddx * ddx + ddy * ddy;
+    const bool ok = row_valid(S, c, r) && d2 < rad2;
+    const float w = sqrtf(fmaxf(rad2 - d2, 0.0f));
+    const int z0 = (int)fminf(fmaxf(floorf((zl - w) * izc), 0.0f), zmax);
+    const int z1 = (int)fminf(fmaxf(floorf((zl + w) * izc), 0.0f), zmax);
+    const int row = row_id(S, c, r);
+    b[r] = ok ? __ldg(start + row + z0) : 0;
+    e[r] = ok ? __ldg(start + row + z1 + 1) : 0;
   }
 }
 
 __device__ __forceinline__ float uv_s(const SceneDev* S, float x) { return x * S->uvs[0] + S->uvo[0]; }
 __device__ __forceinline__ float uv_t(const SceneDev* S, float z) { return z * S->uvs[1] + S->uvo[1]; }
+
+// rho, p and the reference's wave terms (rho_pres_comp.glsl:70-80).
+__device__ __forceinline__ float2 eos(const SceneDev* S, float rho, float4 pi, const float* __restrict__ wave) {
+  float p = S->k * (rho - S->rho0);
+  if (S->preset == CWA_PRESET_REFERENCE_3D) {
+    p = fmaxf(p, 0.0f);
+    const float H = sample_height(wave + S->woff, S->nx, S->nz, uv_s(S, pi.x), uv_t(S, pi.z));
+    const float wf = H * rho;
+    p += wf;
+    rho += wf * S->inv_kr;
+    rho = fmaxf(S->rho0, rho);
+  }
+  return make_float2(rho, p);
+}
 
 // ---- shared-memory staging with bulk TMA copies --------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -163,7 +207,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar) {
 
 constexpr int kNbThreads = 128;
 constexpr int kStageCap = 1536;   // staged candidates per CTA (24 KB)
-constexpr int kRowCodeBits = 12;  // a hit is (row << 12) | offset in the row
+constexpr int kRowCodeBits = 12;  // a hit is (row << 12) | offset from the row's cell-based start
 constexpr int kRowCodeMax = 1 << kRowCodeBits;
 constexpr int kMaxSegs = 18;      // 2 columns x 9 rows
 
@@ -176,16 +220,16 @@ struct StagePlan {
 
 // Warp 0 plans the CTA's staging: the columns its particles occupy and, per
 // column, the candidate rows over the z cells its particles' windows can
-// reach (R = ceil(h_search / cell_z) + 1 cells beyond the particles' own).
+// reach (rz cells beyond the particles' own).
 __device__ __forceinline__ void plan_stage(const SceneDev* S, const int32_t* __restrict__ start,
-                                           const float4* __restrict__ pos, const Tile& tl, StagePlan& sp) {
+                                           const int32_t* __restrict__ keys, const Tile& tl, StagePlan& sp) {
   const int lane = threadIdx.x & 31;
-  const CellCoord a = cell_of(S, __ldg(pos + tl.begin));
-  const CellCoord b = cell_of(S, __ldg(pos + tl.end - 1));
+  const CellCoord a = cell_of_key(S, __ldg(keys + tl.begin));
+  const CellCoord b = cell_of_key(S, __ldg(keys + tl.end - 1));
   const int nx = S->dims[0], ny = S->dims[1], nz = S->dims[2];
   const int colA = a.x * ny + a.y, colB = b.x * ny + b.y;
   const int ncols = colB - colA + 1;
-  const int R = (int)ceilf(S->hs * S->inv_cellz) + 1;
+  const int R = S->rz;
   int len = 0, gb = 0;
   if (ncols <= 2 && lane < 9 * ncols) {
     const int g = lane / 9, r = lane % 9;
@@ -218,26 +262,27 @@ __device__ __forceinline__ void plan_stage(const SceneDev* S, const int32_t* __r
   }
 }
 
-// Candidate test of one row: poly6 partial sum; every hit (r < h, the
-// particle itself included) is appended to the lane's code list.  The list
-// pointer advances by one slot per hit and is clamped at the overflow slot,
-// so the loop has no branch; a list that reached the overflow slot is
-// marked overflowed by the caller.
-template <class T, class Load>
-__device__ __forceinline__ T scan_row(Load load, int len, uint32_t row_code, T px, T py, T pz, T h2,
+// Candidate test of one row.  DENSITY: q = max(h^2 - r^2, 0) and the sum of
+// q^3.  A hit (q > 0 for the radius hit2) is appended to the lane's code
+// list, the particle itself included; the list pointer advances one slot
+// per hit and is clamped at the overflow slot, so the loop has no branch.
+template <bool DENSITY, class T, class Load>
+__device__ __forceinline__ T scan_row(Load load, int len, uint32_t code0, T px, T py, T pz, T hit2,
                                       uint16_t*& hp, uint16_t* hp_end) {
   T part = (T)0;
 #pragma unroll 4
   for (int o = 0; o < len; ++o) {
     const float4 pj = load(o);
     const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
-    T q = fma(-dx, dx, h2);
+    T q = fma(-dx, dx, hit2);
     q = fma(-dy, dy, q);
     q = fma(-dz, dz, q);
-    const T qp = q > (T)0 ? q : (T)0;
-    part = fma(qp * qp, qp, part);
+    if (DENSITY) {
+      const T qp = q > (T)0 ? q : (T)0;
+      part = fma(qp * qp, qp, part);
+    }
     if (q > (T)0) {
-      *hp = (uint16_t)(row_code + (uint32_t)o);
+      *hp = (uint16_t)(code0 + (uint32_t)o);
       hp += kNbThreads;
     }
     hp = hp < hp_end ? hp : hp_end;
@@ -245,27 +290,36 @@ __device__ __forceinline__ T scan_row(Load load, int len, uint32_t row_code, T p
   return part;
 }
 
-// rho_pres: tests every candidate of the 27-cell block once, accumulates
-// the poly6 sum branch-free per row (q = max(h^2 - r^2, 0), sum of q^3 in
-// the row, rows folded by the precision mode's accumulator) and keeps the
-// hits (r < h, j != i) as the particle's neighbour list.
-template <int P>
-__global__ void __launch_bounds__(kNbThreads)
-    k_rho_pres(const float4* __restrict__ pos, const int32_t* __restrict__ start,
-               const Tile* __restrict__ tiles, const SceneDev* __restrict__ scenes,
-               const float* __restrict__ wave, float2* __restrict__ rho_p, uint16_t* __restrict__ nbr,
-               int32_t* __restrict__ nbr_cnt, int32_t n_total, int32_t* status, int32_t allow_stage) {
+// Candidate scan.  MODE_DENSITY (per-step mode): radius h, density + this
+// step's hit list.  MODE_LIST (Verlet mode, only when the rebuild flag is
+// up): radius h (1 + skin), the Verlet list and the rebuild positions.
+constexpr int MODE_DENSITY = 0;
+constexpr int MODE_LIST = 1;
+
+template <int P, int MODE, int MINB>
+__global__ void __launch_bounds__(kNbThreads, MINB)
+    k_scan_cands(const float4* __restrict__ pos, const int32_t* __restrict__ start,
+                 const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
+                 const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
+                 float2* __restrict__ rho_p, uint16_t* __restrict__ list, int32_t* __restrict__ list_cnt,
+                 float4* __restrict__ xref, int32_t n_total, int32_t* status, const int32_t* __restrict__ flag,
+                 int32_t allow_stage) {
   using T = Real<P>;
-  __shared__ __align__(128) float4 s_cand[kStageCap];
-  __shared__ uint16_t s_hit[kMaxNbr + 1][kNbThreads];  // + the overflow slot
+  constexpr int kCap = MODE == MODE_LIST ? kMaxVerlet : kMaxNbr;
+  // The list build (rare: Verlet rebuilds only) reads candidates from global
+  // memory, which keeps its static shared memory under 48 KB.
+  constexpr bool kCanStage = MODE == MODE_DENSITY;
+  __shared__ __align__(128) float4 s_cand[kCanStage ? kStageCap : 1];
+  __shared__ uint16_t s_hit[kCap + 1][kNbThreads];  // + the overflow slot
   __shared__ StagePlan sp;
   __shared__ __align__(8) uint64_t s_bar;
+  if (MODE == MODE_LIST && flag && __ldg(flag) == 0) return;  // no rebuild this step
   const Tile tl = tiles[blockIdx.x];
   const SceneDev* S = scenes + tl.scene;
-  if (threadIdx.x < 32) plan_stage(S, start, pos, tl, sp);
+  if (threadIdx.x < 32) plan_stage(S, start, keys, tl, sp);
   if (threadIdx.x == 0) mbar_init(&s_bar, 1);
   __syncthreads();
-  const bool staged = allow_stage && sp.ncols > 0;
+  const bool staged = kCanStage && allow_stage && sp.ncols > 0;
   if (staged && threadIdx.x == 0) {
     mbar_expect_tx(&s_bar, (uint32_t)sp.seg_off[kMaxSegs] * 16u);
     for (int s = 0; s < 9 * sp.ncols; ++s) {
@@ -284,53 +338,127 @@ __global__ void __launch_bounds__(kNbThreads)
 
   const float4 pi = __ldg(pos + i);
   const T hh = (T)S->h;
-  const T h2 = hh * hh;
+  const T hit2 = MODE == MODE_DENSITY ? hh * hh : (T)S->hl2;
   const T px = pi.x, py = pi.y, pz = pi.z;
-  const CellCoord c = cell_of(S, pi);
-  int b[9], e[9];
-  row_ranges(S, start, pi, c, b, e);
+  const CellCoord c = cell_of_key(S, __ldg(keys + i));
+  int b[9], e[9], base[9];
+  row_ranges(S, start, pi, c, S->hl2, b, e);
+  row_bases(S, start, c, base);
   const int g = staged ? c.x * S->dims[1] + c.y - sp.col0 : 0;
   uint16_t* const hit_col = &s_hit[0][threadIdx.x];
-  uint16_t* const hp_end = hit_col + kMaxNbr * kNbThreads;  // the overflow slot
+  uint16_t* const hp_end = hit_col + kCap * kNbThreads;  // the overflow slot
   uint16_t* hp = hit_col;
   Sum<P> acc;
   bool overflow = false;
 #pragma unroll
   for (int r = 0; r < 9; ++r) {
     const int len = e[r] - b[r];
-    overflow |= len >= kRowCodeMax;
-    const uint32_t row_code = (uint32_t)r << kRowCodeBits;
-    T part;
-    if (len <= 0) {
-      part = (T)0;
-    } else if (staged) {
-      const float4* cand = s_cand + (sp.seg_off[g * 9 + r] + (b[r] - sp.seg_b[g * 9 + r]));
-      part = scan_row<T>([&](int o) { return cand[o]; }, len, row_code, px, py, pz, h2, hp, hp_end);
-    } else {
-      const float4* cand = pos + b[r];
-      part = scan_row<T>([&](int o) { return __ldg(cand + o); }, len, row_code, px, py, pz, h2, hp, hp_end);
+    const int off0 = b[r] - base[r];
+    overflow |= off0 + len > kRowCodeMax;
+    const uint32_t code0 = ((uint32_t)r << kRowCodeBits) + (uint32_t)off0;
+    T part = (T)0;
+    if (len > 0) {
+      if (staged) {
+        const float4* cand = s_cand + (sp.seg_off[g * 9 + r] + (b[r] - sp.seg_b[g * 9 + r]));
+        part = scan_row<MODE == MODE_DENSITY, T>([&](int o) { return cand[o]; }, len, code0, px, py, pz, hit2,
+                                                 hp, hp_end);
+      } else {
+        const float4* cand = pos + b[r];
+        part = scan_row<MODE == MODE_DENSITY, T>([&](int o) { return __ldg(cand + o); }, len, code0, px, py,
+                                                 pz, hit2, hp, hp_end);
+      }
     }
-    acc.add(part);
+    if (MODE == MODE_DENSITY) acc.add(part);
   }
   // Coalesced list write: entry k of every lane is one 64-byte store per warp.
   const int cnt = (int)(hp - hit_col) / kNbThreads;
-  overflow |= cnt >= kMaxNbr;
-  for (int k = 0; k < cnt; ++k) nbr[(size_t)k * n_total + i] = hit_col[k * kNbThreads];
-  nbr_cnt[i] = overflow ? kMaxNbr + 1 : cnt;
-
-  const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
-  float rho = (float)rho_t;
-  float p = S->k * (rho - S->rho0);
-  if (S->preset == CWA_PRESET_REFERENCE_3D) {
-    // rho_pres_comp.glsl:70-80
-    p = fmaxf(p, 0.0f);
-    const float H = sample_height(wave + S->woff, S->nx, S->nz, uv_s(S, pi.x), uv_t(S, pi.z));
-    const float wf = H * rho;
-    p += wf;
-    rho += wf * S->inv_kr;
-    rho = fmaxf(S->rho0, rho);
+  overflow |= cnt >= kCap;
+  for (int k = 0; k < cnt; ++k) list[(size_t)k * n_total + i] = hit_col[k * kNbThreads];
+  list_cnt[i] = overflow ? kCap + 1 : cnt;
+  if (MODE == MODE_LIST) {
+    xref[i] = pi;
+  } else {
+    const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
+    rho_p[i] = eos(S, (float)rho_t, pi, wave);
   }
-  rho_p[i] = make_float2(rho, p);
+}
+
+// Verlet density: walks the particle's list (pairs within h (1 + skin) at
+// the last rebuild), accumulates the poly6 sum over r < h in groups of 8
+// (partials folded into the precision mode's accumulator), and writes this
+// step's hit list for force.  A particle whose Verlet list overflowed rescans
+// the rows of its rebuild cell.
+template <int P>
+__global__ void __launch_bounds__(kNbThreads)
+    k_rho_list(const float4* __restrict__ pos, const int32_t* __restrict__ start,
+               const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
+               const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
+               float2* __restrict__ rho_p, const uint16_t* __restrict__ vlist,
+               const int32_t* __restrict__ vcnt, uint16_t* __restrict__ nbr, int32_t* __restrict__ nbr_cnt,
+               int32_t n_total) {
+  using T = Real<P>;
+  __shared__ int32_t s_rb[9][kNbThreads];
+  const Tile tl = tiles[blockIdx.x];
+  const int i = tl.begin + threadIdx.x;
+  if (i >= tl.end) return;
+  const SceneDev* S = scenes + tl.scene;
+  const float4 pi = __ldg(pos + i);
+  const T hh = (T)S->h;
+  const T h2 = hh * hh;
+  const T px = pi.x, py = pi.y, pz = pi.z;
+  const CellCoord c = cell_of_key(S, __ldg(keys + i));
+  int base[9];
+  row_bases(S, start, c, base);
+  Sum<P> acc;
+  int cnt = 0;
+  const int vn = __ldg(vcnt + i);
+  auto test = [&](int j, uint32_t code) {
+    const float4 pj = __ldg(pos + j);
+    const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
+    T q = fma(-dx, dx, h2);
+    q = fma(-dy, dy, q);
+    q = fma(-dz, dz, q);
+    const T qp = q > (T)0 ? q : (T)0;
+    if (q > (T)0) {
+      if (cnt < kMaxNbr) nbr[(size_t)cnt * n_total + i] = (uint16_t)code;
+      ++cnt;
+    }
+    return qp * qp * qp;
+  };
+  bool overflow = false;
+  if (vn <= kMaxVerlet) {
+#pragma unroll
+    for (int r = 0; r < 9; ++r) s_rb[r][threadIdx.x] = base[r];
+    for (int k0 = 0; k0 < vn; k0 += 8) {
+      uint32_t code[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) code[u] = k0 + u < vn ? __ldg(vlist + (size_t)(k0 + u) * n_total + i) : 0u;
+      T part = (T)0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = s_rb[code[u] >> kRowCodeBits][threadIdx.x] + (int)(code[u] & (kRowCodeMax - 1));
+        if (k0 + u < vn) part += test(j, code[u]);
+      }
+      acc.add(part);
+    }
+  } else {
+    // the rows of the rebuild cell over every z cell a pair within
+    // h (1 + skin) could occupy; hits are coded against the same bases
+    const int z1 = min(c.z + S->rz, S->dims[2] - 1);
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+      if (!row_valid(S, c, r)) continue;
+      const int e = __ldg(start + row_id(S, c, r) + z1 + 1);
+      overflow |= e - base[r] > kRowCodeMax;
+      T part = (T)0;
+      for (int j = base[r]; j < e; ++j)
+        part += test(j, ((uint32_t)r << kRowCodeBits) + (uint32_t)(j - base[r]));
+      acc.add(part);
+    }
+  }
+  nbr_cnt[i] = (overflow || cnt > kMaxNbr) ? kMaxNbr + 1 : cnt;
+  const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
+  rho_p[i] = eos(S, (float)rho_t, pi, wave);
 }
 
 // Three-component sum in the precision mode: COMPENSATED adds pair terms
@@ -362,17 +490,16 @@ struct Acc3 {
   }
 };
 
-// force: spiky pressure gradient + viscosity Laplacian over the neighbour
-// list written by rho_pres (same pairs, same order as the candidate scan),
-// then the preset's extra terms.  A particle whose list overflowed rescans
-// its 27-cell block.
-template <int P>
-__global__ void __launch_bounds__(kNbThreads, 8)
+// force: spiky pressure gradient + viscosity Laplacian over the step's hit
+// list, then the preset's extra terms.  A particle whose list overflowed
+// rescans the rows of its cell over every z cell a neighbour can occupy.
+template <int P, int MINB>
+__global__ void __launch_bounds__(kNbThreads, MINB)
     k_force(const float4* __restrict__ pos, const float4* __restrict__ vel,
             const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
-            const Tile* __restrict__ tiles, const SceneDev* __restrict__ scenes,
-            const float* __restrict__ wave, float4* __restrict__ force, const uint16_t* __restrict__ nbr,
-            const int32_t* __restrict__ nbr_cnt, int32_t n_total) {
+            const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
+            const SceneDev* __restrict__ scenes, const float* __restrict__ wave, float4* __restrict__ force,
+            const uint16_t* __restrict__ nbr, const int32_t* __restrict__ nbr_cnt, int32_t n_total) {
   using T = Real<P>;
   __shared__ int32_t s_rb[9][kNbThreads];
   const Tile tl = tiles[blockIdx.x];
@@ -403,11 +530,12 @@ __global__ void __launch_bounds__(kNbThreads, 8)
     fv.add(sv * ((T)vj.x - vx), sv * ((T)vj.y - vy), sv * ((T)vj.z - vz));
   };
   const int cnt = __ldg(nbr_cnt + i);
-  int b[9], e[9];
-  row_ranges(S, start, pi, cell_of(S, pi), b, e);
+  const CellCoord c = cell_of_key(S, __ldg(keys + i));
+  int base[9];
+  row_bases(S, start, c, base);
   if (cnt <= kMaxNbr) {
 #pragma unroll
-    for (int r = 0; r < 9; ++r) s_rb[r][threadIdx.x] = b[r];
+    for (int r = 0; r < 9; ++r) s_rb[r][threadIdx.x] = base[r];
     // Groups of 8 hits: the 8 codes are loaded first so the gathers overlap.
     // The list holds the particle itself (r = 0), which is skipped.
     for (int k0 = 0; k0 < cnt; k0 += 8) {
@@ -424,8 +552,12 @@ __global__ void __launch_bounds__(kNbThreads, 8)
       fv.flush();
     }
   } else {
+    const int z1 = min(c.z + S->rz, S->dims[2] - 1);
+#pragma unroll
     for (int r = 0; r < 9; ++r) {
-      for (int j = b[r]; j < e[r]; ++j) {
+      if (!row_valid(S, c, r)) continue;
+      const int e = __ldg(start + row_id(S, c, r) + z1 + 1);
+      for (int j = base[r]; j < e; ++j) {
         const float4 pj = __ldg(pos + j);
         const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
         T q = fma(-dx, dx, h2);
@@ -472,10 +604,10 @@ __global__ void __launch_bounds__(kNbThreads, 8)
     const float vv[3] = {vi.x, vi.y, vi.z};
     float f[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const float drag = -0.25f * (vv[c] - wv[c]);
-      const float wf = -H * nrm[c] * 0.5f;
-      f[c] = fpr[c] + fvr[c] * vs + rho * S->g[c] + tq[c] + drag + wf;
+    for (int c2 = 0; c2 < 3; ++c2) {
+      const float drag = -0.25f * (vv[c2] - wv[c2]);
+      const float wf = -H * nrm[c2] * 0.5f;
+      f[c2] = fpr[c2] + fvr[c2] * vs + rho * S->g[c2] + tq[c2] + drag + wf;
     }
     out = make_float4(f[0], f[1], f[2], fprev.w);
   } else {
@@ -485,46 +617,76 @@ __global__ void __launch_bounds__(kNbThreads, 8)
   force[i] = out;
 }
 
+// Launch-bound variants (min CTAs per SM): the register budget trades
+// occupancy against loads in flight per warp; the autotuner picks one.
+template <int P, int MODE>
+void scan_variant(int minb, const NbArgs& a, uint16_t* list, int32_t* cnt, float4* xref, const int32_t* flag,
+                  cudaStream_t st) {
+#define CWA_SCAN(MB)                                                                                          \
+  k_scan_cands<P, MODE, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.start, a.keys, a.tiles, a.scenes,    \
+                                                               a.wave, a.rho_p, list, cnt, xref, a.n_total,   \
+                                                               a.status, flag, a.stage)
+  if (minb >= 8)
+    CWA_SCAN(8);
+  else if (minb >= 6)
+    CWA_SCAN(6);
+  else
+    CWA_SCAN(4);
+#undef CWA_SCAN
+}
+
+template <int P>
+void dispatch_scan(bool list_mode, const NbArgs& a, cudaStream_t st) {
+  if (list_mode)
+    scan_variant<P, MODE_LIST>(a.scan_minb, a, a.vlist, a.vcnt, a.xref, a.flag, st);
+  else
+    scan_variant<P, MODE_DENSITY>(a.scan_minb, a, a.nbr, a.nbr_cnt, nullptr, nullptr, st);
+}
+
+template <int P>
+void dispatch_force(const NbArgs& a, cudaStream_t st) {
+#define CWA_FORCE(MB)                                                                                         \
+  k_force<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles, a.scenes, \
+                                                    a.wave, a.force, a.nbr, a.nbr_cnt, a.n_total)
+  if (a.force_minb >= 8)
+    CWA_FORCE(8);
+  else
+    CWA_FORCE(6);
+#undef CWA_FORCE
+}
+
 }  // namespace
 
-cudaError_t launch_rho_pres(int precision, const float4* pos, const int32_t* start, const Tile* tiles,
-                            int32_t n_tiles, int32_t tile_size, const SceneDev* scenes,
-                            const float* wave_u, float2* rho_p, uint16_t* nbr, int32_t* nbr_cnt,
-                            int32_t n_total, int32_t* status, int32_t stage, cudaStream_t stream) {
-  if (n_tiles <= 0) return cudaSuccess;
+cudaError_t launch_scan_cands(int precision, bool list_mode, const NbArgs& a, cudaStream_t stream) {
+  if (a.n_tiles <= 0) return cudaSuccess;
   switch (precision) {
-    case CWA_PREC_FP32:
-      k_rho_pres<CWA_PREC_FP32><<<n_tiles, tile_size, 0, stream>>>(pos, start, tiles, scenes, wave_u, rho_p, nbr,
-                                                                   nbr_cnt, n_total, status, stage);
-      break;
-    case CWA_PREC_FP64:
-      k_rho_pres<CWA_PREC_FP64><<<n_tiles, tile_size, 0, stream>>>(pos, start, tiles, scenes, wave_u, rho_p, nbr,
-                                                                   nbr_cnt, n_total, status, stage);
-      break;
-    default:
-      k_rho_pres<CWA_PREC_COMPENSATED><<<n_tiles, tile_size, 0, stream>>>(pos, start, tiles, scenes, wave_u,
-                                                                          rho_p, nbr, nbr_cnt, n_total, status, stage);
+    case CWA_PREC_FP32: dispatch_scan<CWA_PREC_FP32>(list_mode, a, stream); break;
+    case CWA_PREC_FP64: dispatch_scan<CWA_PREC_FP64>(list_mode, a, stream); break;
+    default: dispatch_scan<CWA_PREC_COMPENSATED>(list_mode, a, stream);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_force(int precision, const float4* pos, const float4* vel, const float2* rho_p,
-                         const int32_t* start, const Tile* tiles, int32_t n_tiles, int32_t tile_size,
-                         const SceneDev* scenes, const float* wave_u, float4* force, const uint16_t* nbr,
-                         const int32_t* nbr_cnt, int32_t n_total, cudaStream_t stream) {
-  if (n_tiles <= 0) return cudaSuccess;
+cudaError_t launch_rho_list(int precision, const NbArgs& a, cudaStream_t stream) {
+  if (a.n_tiles <= 0) return cudaSuccess;
+#define CWA_RHO_LIST(P)                                                                                     \
+  k_rho_list<P><<<a.n_tiles, a.tile_size, 0, stream>>>(a.pos, a.start, a.keys, a.tiles, a.scenes, a.wave,  \
+                                                       a.rho_p, a.vlist, a.vcnt, a.nbr, a.nbr_cnt, a.n_total)
   switch (precision) {
-    case CWA_PREC_FP32:
-      k_force<CWA_PREC_FP32><<<n_tiles, tile_size, 0, stream>>>(pos, vel, rho_p, start, tiles, scenes, wave_u,
-                                                                force, nbr, nbr_cnt, n_total);
-      break;
-    case CWA_PREC_FP64:
-      k_force<CWA_PREC_FP64><<<n_tiles, tile_size, 0, stream>>>(pos, vel, rho_p, start, tiles, scenes, wave_u,
-                                                                force, nbr, nbr_cnt, n_total);
-      break;
-    default:
-      k_force<CWA_PREC_COMPENSATED><<<n_tiles, tile_size, 0, stream>>>(pos, vel, rho_p, start, tiles, scenes,
-                                                                       wave_u, force, nbr, nbr_cnt, n_total);
+    case CWA_PREC_FP32: CWA_RHO_LIST(CWA_PREC_FP32); break;
+    case CWA_PREC_FP64: CWA_RHO_LIST(CWA_PREC_FP64); break;
+    default: CWA_RHO_LIST(CWA_PREC_COMPENSATED);
+  }
+#undef CWA_RHO_LIST
+  return cudaGetLastError();
+}
+
+cudaError_t launch_force(int precision, const NbArgs& a, cudaStream_t stream) {
+  if (a.n_tiles <= 0) return cudaSuccess;
+  switch (precision) {
+    case CWA_PREC_FP32: dispatch_force<CWA_PREC_FP32>(a, stream); break;
+    case CWA_PREC_FP64: dispatch_force<CWA_PREC_FP64>(a, stream); break;
+    default: dispatch_force<CWA_PREC_COMPENSATED>(a, stream);
   }
   return cudaGetLastError();
 }

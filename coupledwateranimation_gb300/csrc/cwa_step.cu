@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(128)
     k_integrate(float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ force,
                 float2* __restrict__ rho_p, const Tile* __restrict__ tiles,
                 const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
-                unsigned long long* __restrict__ deposits) {
+                unsigned long long* __restrict__ deposits, const float4* __restrict__ xref, int32_t* flag) {
   const Tile tl = tiles[blockIdx.x];
   const int i = tl.begin + threadIdx.x;
   if (i >= tl.end) return;
@@ -120,6 +120,12 @@ __global__ void __launch_bounds__(128)
   }
   pos[i] = make_float4(x[0], x[1], x[2], p.w);
   vel[i] = make_float4(v[0], v[1], v[2], v0.w);
+  if (xref) {  // Verlet mode: has this particle left its skin?
+    const float4 r = xref[i];
+    const float dx = x[0] - r.x, dy = x[1] - r.y, dz = x[2] - r.z;
+    const bool far = dx * dx + dy * dy + dz * dz > S->disp2;
+    if (__any_sync(__activemask(), far) && far) atomicOr(flag, 1);
+  }
 }
 
 // One cell of EvolveWave (wave_comp.glsl:348-383) with get_clamp borders,
@@ -335,9 +341,11 @@ inline int blocks_for(long n, int b) { return (int)((n + b - 1) / b); }
 
 cudaError_t launch_integrate(float4* pos, float4* vel, float4* force, float2* rho_p, const Tile* tiles,
                              int32_t n_tiles, int32_t tile_size, const SceneDev* scenes,
-                             const float* wave_u, unsigned long long* deposits, cudaStream_t stream) {
+                             const float* wave_u, unsigned long long* deposits, const float4* xref,
+                             int32_t* flag, cudaStream_t stream) {
   if (n_tiles <= 0) return cudaSuccess;
-  k_integrate<<<n_tiles, tile_size, 0, stream>>>(pos, vel, force, rho_p, tiles, scenes, wave_u, deposits);
+  k_integrate<<<n_tiles, tile_size, 0, stream>>>(pos, vel, force, rho_p, tiles, scenes, wave_u, deposits, xref,
+                                                 flag);
   return cudaGetLastError();
 }
 

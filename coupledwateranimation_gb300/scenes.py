@@ -69,10 +69,13 @@ def reference() -> Scene:
 
 
 def dam_break(lattice=(32, 32, 32), spacing=0.02, wave=(256, 256), box_hi=(1.0, 1.0, 1.0),
-              seed=BASE_SEED, n_bumps=8, jitter=0.05, zsub=1) -> Scene:
-    """zsub > 1 sorts by z cells of edge h / zsub (x and y cells stay h)."""
+              seed=BASE_SEED, n_bumps=8, jitter=0.05, zsub=1, skin=0.0) -> Scene:
+    """zsub > 1 sorts by z cells of edge cell / zsub; skin > 0 widens the x/y
+    cells to h (1 + skin), as Verlet mode with that skin needs."""
     lib = _abi.load()
     d = defaults(PRESET_MULLER, spacing)
+    if skin > 0.0:
+        d.cell_size = d.smoothing_length * (1.0 + skin) * (1.0 + 1e-6)  # never rounds below h (1 + skin)
     d.cell_size_z = d.cell_size / zsub
     for a in range(3):
         d.box_hi[a] = box_hi[a]
@@ -145,5 +148,15 @@ CONFIGS = {0: config0, 1: config1, 2: config2, 3: config3, 4: config4}
 def with_zsub(wl: Workload, zsub: int) -> Workload:
     """The same workload with the sort grid's z cells split zsub times."""
     for s in wl.scenes:
+        s.desc.cell_size_z = s.desc.cell_size / zsub
+    return wl
+
+
+def with_grid(wl: Workload, zsub: int = 1, skin: float = 0.0) -> Workload:
+    """The same workload with x/y cells of h (1 + skin) (as Verlet mode with
+    that skin needs) and z cells of that edge / zsub."""
+    for s in wl.scenes:
+        if skin > 0.0:
+            s.desc.cell_size = s.desc.smoothing_length * (1.0 + skin) * (1.0 + 1e-6)
         s.desc.cell_size_z = s.desc.cell_size / zsub
     return wl

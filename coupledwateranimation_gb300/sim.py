@@ -30,14 +30,16 @@ class Sim:
     """One or more independent scenes stepped together on one GPU."""
 
     def __init__(self, scenes, precision: int = PREC_COMPENSATED, use_graph: bool = True,
-                 device: int = 0, nb_threads: int = 0, nb_stage: int = 0):
+                 device: int = 0, nb_threads: int = 0, nb_stage: int = 0, verlet_skin: float = 0.0,
+                 nb_scan_minb: int = 0, nb_force_minb: int = 0):
         self._lib = _abi.load()
         if isinstance(scenes, SceneDesc):
             scenes = [scenes]
         self.scenes = [s.copy() for s in scenes]
         arr = (SceneDesc * len(self.scenes))(*self.scenes)
         opt = SimOptions(device=device, precision=precision, use_graph=int(use_graph),
-                         nb_threads=nb_threads, nb_stage=nb_stage)
+                         nb_threads=nb_threads, nb_stage=nb_stage, verlet_skin=verlet_skin,
+                         nb_scan_minb=nb_scan_minb, nb_force_minb=nb_force_minb)
         h = C.c_void_p()
         check(self._lib.cwa_create(C.byref(opt), arr, len(self.scenes), C.byref(h)), "cwa_create")
         self._h = h
@@ -123,6 +125,12 @@ class Sim:
         return v.value
 
     @property
+    def rebuild_count(self) -> int:
+        v = C.c_int64()
+        check(self._lib.cwa_get_rebuild_count(self._h, C.byref(v)), "cwa_get_rebuild_count")
+        return v.value
+
+    @property
     def launch_count(self) -> int:
         v = C.c_int64()
         check(self._lib.cwa_get_launch_count(self._h, C.byref(v)), "cwa_get_launch_count")
@@ -164,6 +172,22 @@ class Sim:
 
     def load(self, path: str) -> None:
         check(self._lib.cwa_load(self._h, str(path).encode()), "cwa_load")
+
+    def autotune(self, trial_steps: int = 5) -> dict:
+        """Pick the fastest neighbour-pass kernel variants for this sim's state
+        (see cwa_autotune); the state is restored afterwards."""
+        r = _abi.TuneReport()
+        check(self._lib.cwa_autotune(self._h, trial_steps, C.byref(r)), "cwa_autotune")
+        opt = lambda o: {"nb_stage": o.nb_stage, "nb_scan_minb": o.nb_scan_minb,  # noqa: E731
+                         "nb_force_minb": o.nb_force_minb, "nb_threads": o.nb_threads}
+        n = min(r.n_tried, 32)
+        return {"best": opt(r.best), "best_ms": r.best_ms, "entry_ms": r.entry_ms,
+                "tried": [dict(opt(r.tried[k]), ms=r.tried_ms[k]) for k in range(n)]}
+
+    def options(self) -> dict:
+        o = _abi.SimOptions()
+        check(self._lib.cwa_get_options(self._h, C.byref(o)), "cwa_get_options")
+        return {f: getattr(o, f) for f, _ in o._fields_ if f != "reserved"}
 
     def set_profiling(self, on: bool) -> None:
         check(self._lib.cwa_set_profiling(self._h, int(on)), "cwa_set_profiling")

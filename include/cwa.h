@@ -110,7 +110,14 @@ typedef struct cwa_sim_options {
   int32_t nb_threads;      /* threads per CTA of the neighbour passes; 0=auto */
   int32_t nb_stage;        /* density pass stages candidate rows in shared
                               memory: 0/1 = on (default), -1 = off         */
-  int32_t reserved[7];
+  float verlet_skin;       /* 0: sort and scan neighbours every step.  > 0:
+                              keep the grid and a list of pairs within
+                              h (1 + skin) until some particle has moved
+                              skin h / 2 (needs cell_size >= h (1 + skin)) */
+  int32_t nb_scan_minb;    /* density-scan kernel variant: min CTAs per SM
+                              (4, 6, 8; 0 = 4)                              */
+  int32_t nb_force_minb;   /* force kernel variant (6, 8; 0 = 8)              */
+  int32_t reserved[4];
 } cwa_sim_options;
 
 /* Borrowed device pointers of one scene, all in the current sorted order.
@@ -215,10 +222,13 @@ cwa_status cwa_pass_wave(cwa_sim* sim);
 /* Wait for the sim's stream; report a device-side status (timeout, NaN). */
 cwa_status cwa_synchronize(cwa_sim* sim);
 cwa_status cwa_get_step_count(cwa_sim* sim, int64_t* steps);
+/* Grid + Verlet-list rebuilds done by the device (Verlet mode). */
+cwa_status cwa_get_rebuild_count(cwa_sim* sim, int64_t* rebuilds);
 cwa_status cwa_get_device_view(cwa_sim* sim, int32_t scene, cwa_device_view* out);
 
-/* Grid of the last cwa_pass_grid: cell_start (n_cells+1, scene-local) and
- * sorted_id (upload index of each sorted particle). */
+/* Grid of the last grid build (every step, or the last Verlet rebuild):
+ * cell_start (n_cells+1, scene-local) and sorted_id (upload index of each
+ * sorted particle). */
 cwa_status cwa_download_grid(cwa_sim* sim, int32_t scene, int32_t* cell_start, int32_t n_cells_p1,
                              int32_t* sorted_id, int32_t n);
 /* Fixed-point deposits made by the last cwa_pass_integrate (before the wave
@@ -228,7 +238,8 @@ cwa_status cwa_download_deposits(cwa_sim* sim, int32_t scene, int64_t* out, int3
 /* FP64 on-device totals of one scene (CWA_TOTAL_* order). */
 cwa_status cwa_reduce_totals(cwa_sim* sim, int32_t scene, double out[CWA_TOTALS_COUNT]);
 
-/* Versioned little-endian checkpoint of every scene's state + step count. */
+/* Versioned little-endian checkpoint of the sim's state + step count; a
+ * resumed run is bit-identical to an uninterrupted one. */
 cwa_status cwa_save(cwa_sim* sim, const char* path);
 cwa_status cwa_load(cwa_sim* sim, const char* path);
 
@@ -237,6 +248,24 @@ cwa_status cwa_set_profiling(cwa_sim* sim, int32_t enable);
 cwa_status cwa_get_pass_times(cwa_sim* sim, float* ms, int32_t n);
 /* Number of kernels launched by the library on this sim since creation. */
 cwa_status cwa_get_launch_count(cwa_sim* sim, int64_t* launches);
+
+/* ---- autotuner ------------------------------------------------------------
+ * Tries the neighbour-pass kernel variants on the sim's current state
+ * (candidate staging on/off, launch-bound variants of the density scan and
+ * force, 128- or 64-particle CTAs), each from the same snapshot for
+ * trial_steps timed steps, keeps the fastest and restores the state.  It
+ * allocates a snapshot of the state while it runs. */
+#define CWA_TUNE_MAX_TRIED 32
+typedef struct cwa_tune_report {
+  cwa_sim_options best;
+  float best_ms;                 /* ms per step of the winner               */
+  float entry_ms;                /* ms per step of the options at entry      */
+  int32_t n_tried;
+  cwa_sim_options tried[CWA_TUNE_MAX_TRIED];
+  float tried_ms[CWA_TUNE_MAX_TRIED];
+} cwa_tune_report;
+cwa_status cwa_autotune(cwa_sim* sim, int32_t trial_steps, cwa_tune_report* out);
+cwa_status cwa_get_options(cwa_sim* sim, cwa_sim_options* out);
 
 /* ---- stand-alone operators on caller-owned device buffers ----------------
  * Exclusive prefix sum of int32 (replaces ParallelScan::Compute,

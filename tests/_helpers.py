@@ -27,8 +27,8 @@ def rel_inf(got: np.ndarray, want: np.ndarray) -> float:
     return float(np.abs(got - want).max() / (den if den > 0 else 1.0))
 
 
-def small_muller(lattice=(16, 16, 16), spacing=0.02, wave=(64, 64), seed=11, zsub=1) -> scenes.Scene:
-    return scenes.dam_break(lattice, spacing, wave, seed=seed, zsub=zsub)
+def small_muller(lattice=(16, 16, 16), spacing=0.02, wave=(64, 64), seed=11, zsub=1, skin=0.0) -> scenes.Scene:
+    return scenes.dam_break(lattice, spacing, wave, seed=seed, zsub=zsub, skin=skin)
 
 
 def small_reference(n: int = 5120) -> scenes.Scene:

@@ -468,3 +468,26 @@ def test_full_size_properties(lib):
     assert np.array_equal(np.sort(g.sorted_id), np.arange(n, dtype=np.int32))
     assert t0["mass"] == t1["mass"]
     assert np.all(np.isfinite(parts))
+
+
+def test_autotune_keeps_state_and_results(lib):
+    """The kernel variants change registers, staging and CTA size, never the
+    arithmetic order, so a tuned sim steps bit-identically to an untuned one;
+    the tuner must also restore the state it trialled on."""
+    sc = small_muller((16, 16, 16), 0.02, (64, 64), zsub=2)
+    with Sim(sc.desc) as sim:
+        load_scene(sim, 0, sc)
+        sim.step(3)
+        before = records_f32(sim.download_particles(0))
+        rep = sim.autotune(trial_steps=2)
+        assert len(rep["tried"]) == 24 and rep["best_ms"] > 0
+        assert np.array_equal(bits(records_f32(sim.download_particles(0))), bits(before))
+        assert sim.step_count == 3
+        sim.step(5)
+        tuned = records_f32(sim.download_particles(0))
+        assert sim.options()["nb_scan_minb"] == rep["best"]["nb_scan_minb"]
+    with Sim(sc.desc) as sim:
+        load_scene(sim, 0, sc)
+        sim.step(8)
+        plain = records_f32(sim.download_particles(0))
+    assert np.array_equal(bits(tuned), bits(plain))
