@@ -68,6 +68,13 @@ struct cwa_sim {
   float* U[3] = {nullptr, nullptr, nullptr};
   int wcur = 0;
   unsigned long long* D = nullptr;
+  // wave advance (cwa_wave_advance): physical buffers UB[0..3], slot -> buffer
+  // map uid (slots 0-2 are U[0..2], slot 3 the spare), per-buffer tensor maps
+  float* UB[4] = {nullptr, nullptr, nullptr, nullptr};
+  int uid[4] = {0, 1, 2, 3};
+  CUtensorMap* d_wmaps = nullptr;
+  WaveBlockTile* d_wbtiles = nullptr;
+  int32_t n_wbtiles = 0;
   // work tiles
   Tile* d_ptiles = nullptr;
   int32_t n_ptiles = 0, ptile = 128;
@@ -379,6 +386,84 @@ cwa_status run_wave(cwa_sim* s) {
   s->launches += 1;
   s->wcur = (w + 1) % 3;  // StencilImage2DTripleBuffered::PingPong (:33-40)
   s->steps += 1;
+  return CWA_OK;
+}
+
+// Lazily set up the blocked wave advance: the spare buffer, a tensor map of
+// every scene's field in each of the four buffers, and the block tiles.
+cwa_status prepare_wave_blocks(cwa_sim* s) {
+  if (s->d_wbtiles) return CWA_OK;
+  const int nsc = (int)s->sd.size();
+  float* spare = nullptr;
+  CWA_TRY(dev_alloc(s, &spare, (size_t)s->w_total));
+  for (int b = 0; b < 3; ++b) s->UB[b] = s->U[b];
+  s->UB[3] = spare;
+  for (int b = 0; b < 4; ++b) s->uid[b] = b;
+  std::vector<CUtensorMap> maps((size_t)4 * nsc);
+  memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
+  std::vector<WaveBlockTile> tiles;
+  for (int k = 0; k < nsc; ++k) {
+    const SceneDev& d = s->sd[k];
+    bool tma = true;
+    for (int b = 0; b < 4 && tma; ++b)
+      tma = wave_block_encode(&maps[(size_t)b * nsc + k], s->UB[b] + d.woff, d.nx, d.nz);
+    wave_block_tiles(d, k, tma, &tiles);
+  }
+  CUtensorMap* dm = nullptr;
+  WaveBlockTile* dt = nullptr;
+  CWA_TRY(dev_alloc(s, &dm, maps.size()));
+  CWA_TRY(dev_alloc(s, &dt, tiles.size()));
+  CWA_CUDA(cudaMemcpy(dm, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+  CWA_CUDA(cudaMemcpy(dt, tiles.data(), tiles.size() * sizeof(WaveBlockTile), cudaMemcpyHostToDevice));
+  CWA_CUDA(cudaDeviceSynchronize());  // the zero-fill memsets ran on the legacy stream
+  s->d_wmaps = dm;
+  s->n_wbtiles = (int32_t)tiles.size();
+  s->d_wbtiles = dt;
+  return CWA_OK;
+}
+
+// n wave passes: a single pass first when a scene takes deposits (it applies
+// and clears them), kWaveK-step blocks, single passes for the remainder.  A
+// block writes u^(n+4) into the free slot and u^(n+3) into the spare; the
+// slots are then renamed so U[wcur] / U[(wcur+2)%3] hold them, which is the
+// state kWaveK single passes leave (up to the rotation of wcur).
+cwa_status run_wave_advance(cwa_sim* s, int32_t n) {
+  int32_t done = 0;
+  bool coupled = false;
+  for (const SceneDev& d : s->sd) coupled = coupled || d.coupled;
+  if (coupled && n > 0) {
+    CWA_TRY(run_wave(s));
+    done = 1;
+  }
+  if (n - done >= kWaveK) {
+    CWA_TRY(prepare_wave_blocks(s));
+    const int w = s->wcur, cur = w, prev = (w + 2) % 3, nxt = (w + 1) % 3;
+    while (n - done >= kWaveK) {
+      const int ic = s->uid[cur], ip = s->uid[prev], oc = s->uid[nxt], op = s->uid[3];
+      const size_t nsc = s->sd.size();
+      WaveBlockArgs a;
+      a.in_cur = s->UB[ic];
+      a.in_prev = s->UB[ip];
+      a.out_cur = s->UB[oc];
+      a.out_prev = s->UB[op];
+      a.map_cur = s->d_wmaps + ic * nsc;
+      a.map_prev = s->d_wmaps + ip * nsc;
+      a.tiles = s->d_wbtiles;
+      a.scenes = s->d_scenes;
+      a.status = s->d_status;
+      CWA_CUDA(launch_wave_block(a, s->n_wbtiles, s->stream));
+      s->launches += s->n_wbtiles > 0;
+      s->uid[cur] = oc;
+      s->uid[prev] = op;
+      s->uid[nxt] = ic;
+      s->uid[3] = ip;
+      done += kWaveK;
+      s->steps += kWaveK;
+    }
+    for (int b = 0; b < 3; ++b) s->U[b] = s->UB[s->uid[b]];
+    drop_graphs(s);  // captured steps hold the old buffer pointers
+  }
+  for (; done < n; ++done) CWA_TRY(run_wave(s));
   return CWA_OK;
 }
 
@@ -788,6 +873,12 @@ cwa_status cwa_pass_integrate(cwa_sim* s) {
 cwa_status cwa_pass_wave(cwa_sim* s) {
   CWA_TRY(check_sim(s));
   return run_wave(s);
+}
+
+cwa_status cwa_wave_advance(cwa_sim* s, int32_t n_steps) {
+  CWA_TRY(check_sim(s));
+  if (n_steps < 0) return arg_error("n_steps < 0");
+  return run_wave_advance(s, n_steps);
 }
 
 cwa_status cwa_synchronize(cwa_sim* s) {

@@ -2,6 +2,7 @@
 // launchers shared by the translation units of libcwa.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -167,6 +168,34 @@ constexpr int kTotalsBlocks = 304;
 cudaError_t launch_totals(const float4* pos, const float4* vel, int32_t poff, int32_t n,
                           const float* u_n, const float* u_nm1, int32_t woff, int32_t nw,
                           const SceneDev* scenes, int32_t scene, double* out, cudaStream_t stream);
+
+// ---- temporally blocked wave advance (cwa_wave_tma.cu) ----
+constexpr int kWaveK = 4;  // wave steps per block launch (= halo width)
+
+// One block tile: patch (bx, by) of a scene's field; tma = rows load by TMA.
+struct WaveBlockTile {
+  int32_t scene, bx, by, tma;
+};
+
+struct WaveBlockArgs {
+  const float* in_cur;           // u^n (all scenes, woff-offset inside)
+  const float* in_prev;          // u^(n-1)
+  float* out_cur;                // receives u^(n+kWaveK)
+  float* out_prev;               // receives u^(n+kWaveK-1)
+  const CUtensorMap* map_cur;    // per-scene tiled maps of in_cur / in_prev,
+  const CUtensorMap* map_prev;   // in device memory
+  const WaveBlockTile* tiles;
+  const SceneDev* scenes;
+  int32_t* status;
+};
+
+int wave_block_rows();
+int wave_block_cols();
+// Encodes the tiled map of one scene's field in one buffer; false when the
+// row width is not a multiple of 4 floats (those scenes load without TMA).
+bool wave_block_encode(CUtensorMap* map, float* base, int W, int H);
+void wave_block_tiles(const SceneDev& d, int32_t scene, bool tma, std::vector<WaveBlockTile>* out);
+cudaError_t launch_wave_block(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t stream);
 
 // Host-side thread-local error text.
 void set_error(const std::string& msg);

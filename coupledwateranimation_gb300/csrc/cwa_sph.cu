@@ -264,11 +264,12 @@ __device__ __forceinline__ void plan_stage(const SceneDev* S, const int32_t* __r
 
 // Candidate test of one row.  DENSITY: q = max(h^2 - r^2, 0) and the sum of
 // q^3.  A hit (q > 0 for the radius hit2) is appended to the lane's code
-// list, the particle itself included; the list pointer advances one slot
-// per hit and is clamped at the overflow slot, so the loop has no branch.
-template <bool DENSITY, class T, class Load>
-__device__ __forceinline__ T scan_row(Load load, int len, uint32_t code0, T px, T py, T pz, T hit2,
-                                      uint16_t*& hp, uint16_t* hp_end) {
+// list, the particle itself included.  CLAMP: the list pointer is clamped
+// at the overflow slot after every candidate; rows that cannot reach it
+// (the common case, checked once per row) skip the clamp.
+template <bool DENSITY, bool CLAMP, class T, class Load>
+__device__ __forceinline__ T scan_row_impl(Load load, int len, uint32_t code0, T px, T py, T pz, T hit2,
+                                           uint16_t*& hp, uint16_t* hp_end) {
   T part = (T)0;
 #pragma unroll 4
   for (int o = 0; o < len; ++o) {
@@ -285,9 +286,17 @@ __device__ __forceinline__ T scan_row(Load load, int len, uint32_t code0, T px, 
       *hp = (uint16_t)(code0 + (uint32_t)o);
       hp += kNbThreads;
     }
-    hp = hp < hp_end ? hp : hp_end;
+    if (CLAMP) hp = hp < hp_end ? hp : hp_end;
   }
   return part;
+}
+
+template <bool DENSITY, class T, class Load>
+__device__ __forceinline__ T scan_row(Load load, int len, uint32_t code0, T px, T py, T pz, T hit2,
+                                      uint16_t*& hp, uint16_t* hp_end) {
+  if (hp + (size_t)len * kNbThreads <= hp_end)
+    return scan_row_impl<DENSITY, false, T>(load, len, code0, px, py, pz, hit2, hp, hp_end);
+  return scan_row_impl<DENSITY, true, T>(load, len, code0, px, py, pz, hit2, hp, hp_end);
 }
 
 // Candidate scan.  MODE_DENSITY (per-step mode): radius h, density + this

@@ -1,0 +1,192 @@
+// cwa_wave_tma.cu — temporally blocked wave stencil over every scene.
+//
+// Advances the height fields kWaveK leapfrog steps per launch with no new
+// particle deposits: the stand-alone wave module's job (the reference's
+// StencilImage2DTripleBuffered driving wave_comp.glsl EvolveWave, :348-383,
+// one dispatch per step; the 2D wave demo Wave2DSimp/Wave2D_cs.glsl:78-84).
+//
+// One launch covers all scenes through a list of block tiles.  A block tile
+// owns a 120 x 24 patch of one scene's field and works on a 128 x 32 box:
+// the patch plus a kWaveK-cell halo.  Scenes whose row width is a multiple of
+// 4 cells load the box of u^n and u^(n-1) with two 2D TMA copies
+// (cp.async.bulk.tensor, completion counted on an mbarrier; the box's x
+// origin is patch_x - 4, a multiple of 4 floats = 16 bytes); other widths load
+// it with plain loads.  The kWaveK steps then run in shared memory — step s
+// is computed on the box shrunk by s cells, which is exactly the region whose
+// inputs are still exact — and the patch of u^(n+4) and u^(n+3) is stored
+// with coalesced writes into two buffers that no CTA of this launch reads.
+// DRAM traffic per cell-step drops from 12 bytes (single step: read u^n,
+// u^(n-1), write u^(n+1)) to about 4.9.
+//
+// Each cell runs the single-step kernel's operation sequence with the same
+// clamped (Neumann) neighbour indices, so one launch equals kWaveK single
+// wave passes bit for bit.  Box cells outside the domain (TMA zero fill) are
+// never read by an in-domain cell: neighbour indices clamp to the domain.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+
+#include "cwa_internal.h"
+
+namespace cwa {
+namespace {
+
+constexpr int kBoxW = 128, kBoxH = 32;          // box (x, y) in cells
+constexpr int kTileW = kBoxW - 2 * kWaveK;      // 120 output columns
+constexpr int kTileH = kBoxH - 2 * kWaveK;      // 24 output rows
+constexpr int kWaveTmaThreads = 256;
+constexpr uint32_t kBoxBytes = kBoxW * kBoxH * sizeof(float);
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool bar_try_wait(uint32_t bar) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on phase 0 of the barrier: false after ~2^20 polls.
+__device__ __forceinline__ bool bar_wait_bounded(uint32_t bar) {
+  for (int k = 0; k < (1 << 20); ++k)
+    if (bar_try_wait(bar)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(kWaveTmaThreads)
+    k_wave_block(WaveBlockArgs a) {
+  __shared__ __align__(128) float box[2][kBoxH][kBoxW];
+  __shared__ __align__(8) uint64_t bar;
+  const WaveBlockTile t = a.tiles[blockIdx.x];
+  const SceneDev* S = a.scenes + t.scene;
+  const int W = S->nx, H = S->nz;
+  const int ox = t.bx * kTileW - kWaveK, oy = t.by * kTileH - kWaveK;  // box origin; ox % 4 == 0
+  if (t.tma) {
+    const uint32_t b = smem_u32(&bar);
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(2 * kBoxBytes)
+                   : "memory");
+      tma_load_2d(smem_u32(&box[0][0][0]), a.map_cur + t.scene, ox, oy, b);
+      tma_load_2d(smem_u32(&box[1][0][0]), a.map_prev + t.scene, ox, oy, b);
+    }
+    if (!bar_wait_bounded(b)) {
+      if (threadIdx.x == 0) atomicOr(a.status, kStatusTimeout);
+      bar_wait_bounded(b);  // give copies still in flight a chance to land before the CTA exits
+      return;
+    }
+  } else {
+    const float* uc = a.in_cur + S->woff;
+    const float* up = a.in_prev + S->woff;
+    for (int idx = threadIdx.x; idx < kBoxW * kBoxH; idx += kWaveTmaThreads) {
+      const int lx = idx % kBoxW, ly = idx / kBoxW;
+      const int gx = ox + lx, gy = oy + ly;
+      const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
+      box[0][ly][lx] = in ? __ldg(uc + (size_t)gy * W + gx) : 0.0f;
+      box[1][ly][lx] = in ? __ldg(up + (size_t)gy * W + gx) : 0.0f;
+    }
+    __syncthreads();
+  }
+  const float wa = S->wa, wb = S->wb, lam = S->lam, atten = S->atten;
+  const float zero_deposit = S->coupled ? fmul(S->gain, fmul(0.0f, S->dq)) : 0.0f;
+  const int src_x = S->line_source ? W / 2 : -1;
+  int c = 0;  // box[c] = u^t, box[c ^ 1] = u^(t-1), overwritten in place by u^(t+1)
+#pragma unroll 1
+  for (int s = 1; s <= kWaveK; ++s) {
+    const float(*A)[kBoxW] = box[c];
+    float(*B)[kBoxW] = box[c ^ 1];
+    for (int idx = threadIdx.x; idx < kBoxW * kBoxH; idx += kWaveTmaThreads) {
+      const int lx = idx % kBoxW, ly = idx / kBoxW;
+      if (lx < s || lx >= kBoxW - s || ly < s || ly >= kBoxH - s) continue;
+      const int gx = ox + lx, gy = oy + ly;
+      if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+      const int le = min(gx + 1, W - 1) - ox, lw = max(gx - 1, 0) - ox;
+      const int ln = min(gy + 1, H - 1) - oy, ls = max(gy - 1, 0) - oy;
+      const float nb = fadd(fadd(A[ln][lx], A[ls][lx]), fadd(A[ly][le], A[ly][lw]));
+      float w = fadd(fmul(wa, A[ly][lx]), fmul(lam, nb));
+      w = fsub(w, fmul(wb, B[ly][lx]));
+      w = fmul(atten, w);
+      if (gx == src_x && w > 0.0001f) w = fadd(w, 0.001f);
+      if (S->coupled) w = fadd(w, zero_deposit);
+      B[ly][lx] = w;
+    }
+    __syncthreads();
+    c ^= 1;
+  }
+  float* oc = a.out_cur + S->woff;
+  float* op = a.out_prev + S->woff;
+  for (int idx = threadIdx.x; idx < kTileW * kTileH; idx += kWaveTmaThreads) {
+    const int lx = kWaveK + idx % kTileW, ly = kWaveK + idx / kTileW;
+    const int gx = ox + lx, gy = oy + ly;
+    if (gx >= W || gy >= H) continue;
+    oc[(size_t)gy * W + gx] = box[c][ly][lx];
+    op[(size_t)gy * W + gx] = box[c ^ 1][ly][lx];
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+}  // namespace
+
+int wave_block_rows() { return kTileH; }
+int wave_block_cols() { return kTileW; }
+
+bool wave_block_encode(CUtensorMap* map, float* base, int W, int H) {
+  if (W < 1 || H < 1 || (W % 4) != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
+  const cuuint64_t strides[1] = {(cuuint64_t)W * sizeof(float)};
+  const cuuint32_t boxdim[2] = {kBoxW, kBoxH};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, boxdim, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+void wave_block_tiles(const SceneDev& d, int32_t scene, bool tma, std::vector<WaveBlockTile>* out) {
+  const int nbx = (d.nx + kTileW - 1) / kTileW, nby = (d.nz + kTileH - 1) / kTileH;
+  for (int by = 0; by < nby; ++by)
+    for (int bx = 0; bx < nbx; ++bx) out->push_back(WaveBlockTile{scene, bx, by, tma ? 1 : 0});
+}
+
+cudaError_t launch_wave_block(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t stream) {
+  if (n_tiles <= 0) return cudaSuccess;
+  k_wave_block<<<n_tiles, kWaveTmaThreads, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace cwa

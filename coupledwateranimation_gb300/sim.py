@@ -114,6 +114,10 @@ class Sim:
     def wave(self) -> None:
         check(self._lib.cwa_pass_wave(self._h), "cwa_pass_wave")
 
+    def wave_advance(self, n: int) -> None:
+        """n wave passes with no particle passes between them (4 per launch)."""
+        check(self._lib.cwa_wave_advance(self._h, int(n)), "cwa_wave_advance")
+
     def synchronize(self) -> None:
         check(self._lib.cwa_synchronize(self._h), "cwa_synchronize")
 

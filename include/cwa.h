@@ -219,6 +219,15 @@ cwa_status cwa_pass_rho_pres(cwa_sim* sim);
 cwa_status cwa_pass_force(cwa_sim* sim);
 cwa_status cwa_pass_integrate(cwa_sim* sim);
 cwa_status cwa_pass_wave(cwa_sim* sim);
+/* n_steps wave passes over every scene's height field, with no particle
+ * passes in between: the wave module stepped alone (Module::Compute in
+ * StencilImage2DTripleBuffered.cpp:22-31 and wave_comp.glsl EvolveWave
+ * :348-383, one dispatch per step).  Bit-identical to n_steps calls of
+ * cwa_pass_wave; deposits pending from an integrate pass land in the first
+ * step.  Steps run 4 at a time in shared memory (TMA-loaded tiles), so
+ * device pointers of the wave buffers may change: re-read cwa_get_device_view
+ * after it.  Asynchronous. */
+cwa_status cwa_wave_advance(cwa_sim* sim, int32_t n_steps);
 /* Wait for the sim's stream; report a device-side status (timeout, NaN). */
 cwa_status cwa_synchronize(cwa_sim* sim);
 cwa_status cwa_get_step_count(cwa_sim* sim, int64_t* steps);

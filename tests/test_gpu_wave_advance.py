@@ -1,0 +1,128 @@
+"""cwa_wave_advance: the temporally blocked wave stencil (4 steps per launch,
+TMA-loaded tiles) against single wave passes and the float32 oracle, bit for
+bit.  The wave module stepped alone is StencilImage2DTripleBuffered::Compute
+(StencilImage2DTripleBuffered.cpp:22-31) over wave_comp.glsl EvolveWave
+(:348-383)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from coupledwateranimation_gb300 import Sim
+
+from _helpers import bits, load_scene, small_muller, small_reference
+
+pytestmark = pytest.mark.gpu
+
+
+def _pending_deposits(sim: Sim) -> None:
+    """Leave the sim mid-step: integrate has deposited, the wave pass not run."""
+    sim.step(2)
+    sim.grid()
+    sim.rho_pres()
+    sim.force()
+    sim.integrate()
+
+
+def _compare(desc_list, load, n, pending=True, **kw):
+    sims = [Sim(desc_list, **kw), Sim(desc_list, **kw)]
+    try:
+        for s in sims:
+            load(s)
+            if pending:
+                _pending_deposits(s)
+        sims[0].wave_advance(n)
+        for _ in range(n):
+            sims[1].wave()
+        for s in sims:
+            s.synchronize()
+        for k in range(len(desc_list)):
+            a = sims[0].download_wave(k)
+            b = sims[1].download_wave(k)
+            assert np.array_equal(bits(a[0]), bits(b[0])), f"scene {k} u^n"
+            assert np.array_equal(bits(a[1]), bits(b[1])), f"scene {k} u^(n-1)"
+        assert sims[0].step_count == sims[1].step_count
+    finally:
+        for s in sims:
+            s.close()
+
+
+# widths: multiples of 4 take the TMA path, others the plain-load path;
+# sizes span one tile, ragged edges and several tiles in both directions
+@pytest.mark.parametrize("wave", [(64, 64), (256, 200), (240, 48), (250, 130), (37, 5), (4, 1), (1, 3)])
+@pytest.mark.parametrize("n", [1, 4, 9, 14])
+def test_wave_advance_equals_single_passes(lib, wave, n):
+    sc = small_muller((6, 6, 6), 0.03, wave, seed=5)
+    _compare([sc.desc], lambda s: load_scene(s, 0, sc), n)
+
+
+def test_wave_advance_batched_mixed_widths(lib):
+    scs = [small_muller((6, 6, 6), 0.03, w, seed=7 + i) for i, w in enumerate([(128, 96), (130, 77), (512, 24)])]
+
+    def load(s):
+        for k, sc in enumerate(scs):
+            load_scene(s, k, sc)
+
+    _compare([sc.desc for sc in scs], load, 13)
+
+
+def test_wave_advance_reference_line_source(lib):
+    sc = small_reference(640)
+    sc.desc.wave_mode = 0.5  # line source on (wave_comp.glsl:354-361)
+    sc.desc.wave_nx, sc.desc.wave_nz = 200, 120
+
+    def load(s):
+        s.upload_particles(0, sc.particles)
+        s.wave_reinit(0)
+
+    _compare([sc.desc], load, 12, pending=False)
+
+
+def test_wave_advance_matches_oracle(lib, orc):
+    sc = small_muller((6, 6, 6), 0.03, (248, 100), seed=3)
+    sc.desc.n_particles = 0
+    sc.particles = sc.particles[:0]
+    with Sim(sc.desc) as sim:
+        sim.upload_wave(0, sc.wave, sc.wave)
+        sim.wave_advance(8)
+        got_n, got_nm1 = sim.download_wave(0)
+    a = sc.wave.astype(np.float32)
+    b = a.copy()
+    for _ in range(8):
+        a, b = orc.wave_f32(sc.desc, a, b), a
+    assert np.array_equal(bits(got_n), bits(a))
+    assert np.array_equal(bits(got_nm1), bits(b))
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_steps_after_wave_advance(lib, use_graph):
+    # the buffer renaming invalidates captured graphs; later steps must agree
+    sc = small_muller((10, 10, 10), 0.03, (128, 128), seed=9)
+    sims = [Sim(sc.desc, use_graph=use_graph), Sim(sc.desc, use_graph=use_graph)]
+    try:
+        for s in sims:
+            load_scene(s, 0, sc)
+            s.step(3)
+        sims[0].wave_advance(5)
+        for _ in range(5):
+            sims[1].wave()
+        for s in sims:
+            s.step(4)
+            s.synchronize()
+        pa, pb = sims[0].download_particles(0), sims[1].download_particles(0)
+        assert np.array_equal(pa.view(np.uint8), pb.view(np.uint8))
+        ua, ub = sims[0].download_wave(0), sims[1].download_wave(0)
+        assert np.array_equal(bits(ua[0]), bits(ub[0])) and np.array_equal(bits(ua[1]), bits(ub[1]))
+    finally:
+        for s in sims:
+            s.close()
+
+
+def test_wave_advance_rejects_negative(lib):
+    from coupledwateranimation_gb300 import CwaError
+
+    sc = small_muller((4, 4, 4), 0.03, (64, 64))
+    with Sim(sc.desc) as sim:
+        with pytest.raises(CwaError):
+            sim.wave_advance(-1)
+        sim.wave_advance(0)
