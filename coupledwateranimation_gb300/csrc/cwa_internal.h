@@ -132,6 +132,10 @@ struct NbArgs {
   uint16_t* vlist;
   int32_t* vcnt;
   float4* xref;         // positions at the last rebuild (Verlet mode)
+  // (x, y, z, p) and (vx, vy, vz, 1/rho) of every particle, written by the
+  // density pass for force's neighbour gathers (FP32 modes; null in FP64)
+  float4* xpair;
+  float4* vpair;
   int32_t n_total;
   int32_t* status;
   const int32_t* flag;  // rebuild flag (Verlet mode), else null

@@ -122,7 +122,9 @@ __device__ __forceinline__ void row_bases(const SceneDev* S, const int32_t* __re
 // p, row by row.  A row whose column is farther than the radius in (x, y)
 // is empty; the others cover the z cells of the window
 // |z - pz| < sqrt(rad2 - d^2), d = the column's (x, y) distance.  The
-// radius carries a 2^-10 margin, so float rounding never drops a pair.
+// radius carries a 2^-10 margin (about h / 1024 of slack in the window), so
+// neither float rounding nor the approximate square root t * rsqrt(t)
+// (relative error ~1e-7) ever drops a pair.
 __device__ __forceinline__ void row_ranges(const SceneDev* S, const int32_t* __restrict__ start, float4 p,
                                            CellCoord c, float rad2, int b[9], int e[9]) {
   const int nz = S->dims[2];
@@ -138,7 +140,8 @@ __device__ __forceinline__ void row_ranges(const SceneDev* S, const int32_t* __r
     const float ddy = dy < 0 ? dym : (dy > 0 ? dyp : 0.0f);
     const float d2 = ddx * ddx + ddy * ddy;
     const bool ok = row_valid(S, c, r) && d2 < rad2;
-    const float w = sqrtf(fmaxf(rad2 - d2, 0.0f));
+    const float t = fmaxf(rad2 - d2, 0.0f);
+    const float w = ok ? t * rsqrtf(t) : 0.0f;  // ok implies t > 0
     const int z0 = (int)fminf(fmaxf(floorf((zl - w) * izc), 0.0f), zmax);
     const int z1 = (int)fminf(fmaxf(floorf((zl + w) * izc), 0.0f), zmax);
     const int row = row_id(S, c, r);
@@ -162,6 +165,16 @@ __device__ __forceinline__ float2 eos(const SceneDev* S, float rho, float4 pi, c
     rho = fmaxf(S->rho0, rho);
   }
   return make_float2(rho, p);
+}
+
+// Force's gather records of particle i: (x, y, z, p) and (vx, vy, vz, 1/rho),
+// so a pair costs two aligned 16-byte gathers; 1/rho uses force's recip.
+__device__ __forceinline__ void write_pair_rec(float4* __restrict__ xp, float4* __restrict__ vp,
+                                               const float4* __restrict__ vel, int i, float4 pi, float2 rp) {
+  if (!xp) return;
+  const float4 v = __ldg(vel + i);
+  xp[i] = make_float4(pi.x, pi.y, pi.z, rp.y);
+  vp[i] = make_float4(v.x, v.y, v.z, recip(rp.x));
 }
 
 // ---- shared-memory staging with bulk TMA copies --------------------------
@@ -278,11 +291,8 @@ __device__ __forceinline__ T scan_row_impl(Load load, int len, uint32_t code0, T
     T q = fma(-dx, dx, hit2);
     q = fma(-dy, dy, q);
     q = fma(-dz, dz, q);
-    if (DENSITY) {
-      const T qp = q > (T)0 ? q : (T)0;
-      part = fma(qp * qp, qp, part);
-    }
-    if (q > (T)0) {
+    if (q > (T)0) {  // a miss would add (+0)^3: the sum is unchanged
+      if (DENSITY) part = fma(q * q, q, part);
       *hp = (uint16_t)(code0 + (uint32_t)o);
       hp += kNbThreads;
     }
@@ -312,7 +322,8 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
                  const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
                  float2* __restrict__ rho_p, uint16_t* __restrict__ list, int32_t* __restrict__ list_cnt,
                  float4* __restrict__ xref, int32_t n_total, int32_t* status, const int32_t* __restrict__ flag,
-                 int32_t allow_stage) {
+                 int32_t allow_stage, const float4* __restrict__ vel, float4* __restrict__ xpair,
+                 float4* __restrict__ vpair) {
   using T = Real<P>;
   constexpr int kCap = MODE == MODE_LIST ? kMaxVerlet : kMaxNbr;
   // The list build (rare: Verlet rebuilds only) reads candidates from global
@@ -388,7 +399,9 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
     xref[i] = pi;
   } else {
     const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
-    rho_p[i] = eos(S, (float)rho_t, pi, wave);
+    const float2 rp = eos(S, (float)rho_t, pi, wave);
+    rho_p[i] = rp;
+    write_pair_rec(xpair, vpair, vel, i, pi, rp);
   }
 }
 
@@ -404,7 +417,8 @@ __global__ void __launch_bounds__(kNbThreads)
                const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
                float2* __restrict__ rho_p, const uint16_t* __restrict__ vlist,
                const int32_t* __restrict__ vcnt, uint16_t* __restrict__ nbr, int32_t* __restrict__ nbr_cnt,
-               int32_t n_total) {
+               int32_t n_total, const float4* __restrict__ vel, float4* __restrict__ xpair,
+               float4* __restrict__ vpair) {
   using T = Real<P>;
   __shared__ int32_t s_rb[9][kNbThreads];
   const Tile tl = tiles[blockIdx.x];
@@ -467,7 +481,9 @@ __global__ void __launch_bounds__(kNbThreads)
   }
   nbr_cnt[i] = (overflow || cnt > kMaxNbr) ? kMaxNbr + 1 : cnt;
   const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
-  rho_p[i] = eos(S, (float)rho_t, pi, wave);
+  const float2 rp = eos(S, (float)rho_t, pi, wave);
+  rho_p[i] = rp;
+  write_pair_rec(xpair, vpair, vel, i, pi, rp);
 }
 
 // Three-component sum in the precision mode: COMPENSATED adds pair terms
@@ -502,19 +518,25 @@ struct Acc3 {
 // force: spiky pressure gradient + viscosity Laplacian over the step's hit
 // list, then the preset's extra terms.  A particle whose list overflowed
 // rescans the rows of its cell over every z cell a neighbour can occupy.
+// Force over the density pass's hit list.  Neighbour data comes from global
+// memory (L1-resident for the most part: a CTA's particles share their
+// candidate rows).  Staging the rows' records in shared memory, as the
+// candidate scan does, measured slower here: 48 KB of stage per CTA halves
+// the resident warps this latency-bound loop needs.
 template <int P, int MINB>
 __global__ void __launch_bounds__(kNbThreads, MINB)
     k_force(const float4* __restrict__ pos, const float4* __restrict__ vel,
             const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
             const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
             const SceneDev* __restrict__ scenes, const float* __restrict__ wave, float4* __restrict__ force,
-            const uint16_t* __restrict__ nbr, const int32_t* __restrict__ nbr_cnt, int32_t n_total) {
+            const uint16_t* __restrict__ nbr, const int32_t* __restrict__ nbr_cnt, int32_t n_total,
+            const float4* __restrict__ xpair, const float4* __restrict__ vpair) {
   using T = Real<P>;
   __shared__ int32_t s_rb[9][kNbThreads];
   const Tile tl = tiles[blockIdx.x];
+  const SceneDev* S = scenes + tl.scene;
   const int i = tl.begin + threadIdx.x;
   if (i >= tl.end) return;
-  const SceneDev* S = scenes + tl.scene;
   const float4 pi = __ldg(pos + i);
   const float4 vi = __ldg(vel + i);
   const float2 rpi = __ldg(rho_p + i);
@@ -523,39 +545,48 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   const T px = pi.x, py = pi.y, pz = pi.z;
   const T vx = vi.x, vy = vi.y, vz = vi.z, pres_i = rpi.y;
   Acc3<P> fp, fv;
-  auto pair = [&](int j) {
-    const float4 pj = __ldg(pos + j);
-    const float4 vj = __ldg(vel + j);
-    const float2 rpj = __ldg(rho_p + j);
+  auto pair = [&](float4 pj, float4 vj, T irho, T pres_j) {
     const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
     const T r2 = dx * dx + dy * dy + dz * dz;
     const T inv_r = r2 > (T)0 ? inv_sqrt(r2) : (T)0;  // normalize(0) := 0
     const T r = r2 * inv_r;
     const T hr = hh - r;
-    const T irho = recip((T)rpj.x);
-    const T sp = (pres_i + (T)rpj.y) * irho * hr * hr * inv_r;
+    const T sp = (pres_i + pres_j) * irho * hr * hr * inv_r;
     fp.add(sp * dx, sp * dy, sp * dz);
     const T sv = irho * hr;
     fv.add(sv * ((T)vj.x - vx), sv * ((T)vj.y - vy), sv * ((T)vj.z - vz));
+  };
+  // FP32 modes read the density pass's records; FP64 gathers pos, vel and
+  // (rho, p) and divides in double.
+  auto pair_global = [&](int j) {
+    if (P == CWA_PREC_FP64) {
+      const float2 rpj = __ldg(rho_p + j);
+      pair(__ldg(pos + j), __ldg(vel + j), recip((T)rpj.x), (T)rpj.y);
+    } else {
+      const float4 xj = __ldg(xpair + j), vj = __ldg(vpair + j);
+      pair(xj, vj, (T)vj.w, (T)xj.w);
+    }
   };
   const int cnt = __ldg(nbr_cnt + i);
   const CellCoord c = cell_of_key(S, __ldg(keys + i));
   int base[9];
   row_bases(S, start, c, base);
   if (cnt <= kMaxNbr) {
+    // The list holds the particle itself: row 4 (its own column) at offset
+    // i - base[4]; that code is skipped.
+    const uint32_t self_code = (4u << kRowCodeBits) + (uint32_t)(i - base[4]);
 #pragma unroll
     for (int r = 0; r < 9; ++r) s_rb[r][threadIdx.x] = base[r];
     // Groups of 8 hits: the 8 codes are loaded first so the gathers overlap.
-    // The list holds the particle itself (r = 0), which is skipped.
     for (int k0 = 0; k0 < cnt; k0 += 8) {
       uint32_t code[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u)
-        code[u] = k0 + u < cnt ? __ldg(nbr + (size_t)(k0 + u) * n_total + i) : 0u;
+        code[u] = k0 + u < cnt ? __ldg(nbr + (size_t)(k0 + u) * n_total + i) : self_code;
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int j = s_rb[code[u] >> kRowCodeBits][threadIdx.x] + (int)(code[u] & (kRowCodeMax - 1));
-        if (k0 + u < cnt && j != i) pair(j);
+        if (code[u] != self_code) pair_global(j);
       }
       fp.flush();
       fv.flush();
@@ -572,7 +603,7 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
         T q = fma(-dx, dx, h2);
         q = fma(-dy, dy, q);
         q = fma(-dz, dz, q);
-        if (q > (T)0 && j != i) pair(j);
+        if (q > (T)0 && j != i) pair_global(j);
       }
       fp.flush();
       fv.flush();
@@ -634,7 +665,8 @@ void scan_variant(int minb, const NbArgs& a, uint16_t* list, int32_t* cnt, float
 #define CWA_SCAN(MB)                                                                                          \
   k_scan_cands<P, MODE, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.start, a.keys, a.tiles, a.scenes,    \
                                                                a.wave, a.rho_p, list, cnt, xref, a.n_total,   \
-                                                               a.status, flag, a.stage)
+                                                               a.status, flag, a.stage, a.vel, a.xpair,       \
+                                                               a.vpair)
   if (minb >= 8)
     CWA_SCAN(8);
   else if (minb >= 6)
@@ -652,16 +684,19 @@ void dispatch_scan(bool list_mode, const NbArgs& a, cudaStream_t st) {
     scan_variant<P, MODE_DENSITY>(a.scan_minb, a, a.nbr, a.nbr_cnt, nullptr, nullptr, st);
 }
 
+template <int P, int MB>
+void force_variant(const NbArgs& a, cudaStream_t st) {
+  k_force<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles, a.scenes,
+                                                    a.wave, a.force, a.nbr, a.nbr_cnt, a.n_total, a.xpair,
+                                                    a.vpair);
+}
+
 template <int P>
 void dispatch_force(const NbArgs& a, cudaStream_t st) {
-#define CWA_FORCE(MB)                                                                                         \
-  k_force<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles, a.scenes, \
-                                                    a.wave, a.force, a.nbr, a.nbr_cnt, a.n_total)
   if (a.force_minb >= 8)
-    CWA_FORCE(8);
+    force_variant<P, 8>(a, st);
   else
-    CWA_FORCE(6);
-#undef CWA_FORCE
+    force_variant<P, 6>(a, st);
 }
 
 }  // namespace
@@ -680,7 +715,8 @@ cudaError_t launch_rho_list(int precision, const NbArgs& a, cudaStream_t stream)
   if (a.n_tiles <= 0) return cudaSuccess;
 #define CWA_RHO_LIST(P)                                                                                     \
   k_rho_list<P><<<a.n_tiles, a.tile_size, 0, stream>>>(a.pos, a.start, a.keys, a.tiles, a.scenes, a.wave,  \
-                                                       a.rho_p, a.vlist, a.vcnt, a.nbr, a.nbr_cnt, a.n_total)
+                                                       a.rho_p, a.vlist, a.vcnt, a.nbr, a.nbr_cnt, a.n_total, \
+                                                       a.vel, a.xpair, a.vpair)
   switch (precision) {
     case CWA_PREC_FP32: CWA_RHO_LIST(CWA_PREC_FP32); break;
     case CWA_PREC_FP64: CWA_RHO_LIST(CWA_PREC_FP64); break;
