@@ -179,16 +179,21 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def batched_vs_plain(args, torch) -> dict:
+def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0) -> dict:
     """The 256-scene workload stepped as one batched sim (one launch per pass
     over all scenes, CUDA graph) and as 256 single-scene sims run one at a
     time (each its own graph).  Host wall-clock around the GPU work, with a
-    synchronise at the end of every scene's steps in the plain leg."""
-    from coupledwateranimation_gb300 import Sim, scenes
-    wl = scenes.with_zsub(scenes.config3(), args.zsub)
+    synchronise at the end of every scene's steps in the plain leg.  Under
+    N ranks each rank steps its shard of the scenes (greedy by device
+    footprint); times are the max over ranks, units the sum."""
+    from coupledwateranimation_gb300 import Sim, scenes, shard
+    full = scenes.with_zsub(scenes.config3(), args.zsub)
+    _, mine = shard.shard_scenes(full, rank, ws)
+    wl = scenes.Workload(full.name, mine, full.steps)
     steps = max(3, min(args.steps, 10))
-    n_units = wl.n_particles + wl.n_wave_cells
-    with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True) as sim:
+    dev = f"cuda:{local}"
+    n_units = shard.sum_over_ranks(wl.n_particles + wl.n_wave_cells, dev)
+    with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local) as sim:
         for k, s in enumerate(wl.scenes):
             sim.upload_particles(k, s.particles)
             sim.upload_wave(k, s.wave, s.wave)
@@ -199,12 +204,12 @@ def batched_vs_plain(args, torch) -> dict:
         t0 = time.perf_counter()
         sim.step(steps)
         sim.synchronize()
-        t_batched = time.perf_counter() - t0
+        t_batched = shard.max_over_ranks(time.perf_counter() - t0, dev)
         launches = sim.launch_count
     plain = []
     try:
         for s in wl.scenes:
-            p = Sim(s.desc, precision=args.precision, use_graph=True)
+            p = Sim(s.desc, precision=args.precision, use_graph=True, device=local)
             p.upload_particles(0, s.particles)
             p.upload_wave(0, s.wave, s.wave)
             p.step(3)
@@ -214,12 +219,13 @@ def batched_vs_plain(args, torch) -> dict:
         for p in plain:
             p.step(steps)
             p.synchronize()
-        t_plain = time.perf_counter() - t0
+        t_plain = shard.max_over_ranks(time.perf_counter() - t0, dev)
     finally:
         for p in plain:
             p.close()
-    return {"workload": wl.name, "scenes": len(wl.scenes), "particles": wl.n_particles,
-            "wave_cells": wl.n_wave_cells, "steps": steps,
+    return {"workload": wl.name, "scenes": len(full.scenes), "particles": full.n_particles,
+            "wave_cells": full.n_wave_cells, "steps": steps, "ranks": ws,
+            "scenes_per_rank_max": int(shard.max_over_ranks(len(wl.scenes), dev)),
             "batched_updates_per_s": n_units * steps / t_batched,
             "plain_updates_per_s": n_units * steps / t_plain,
             "speedup": t_plain / t_batched,
@@ -345,8 +351,8 @@ def run_gpu(args) -> None:
     clk.__exit__(None, None, None)
 
     batched = None
-    if rank == 0 and ws == 1 and not args.no_batched:
-        batched = batched_vs_plain(args, torch)
+    if not args.no_batched:
+        batched = batched_vs_plain(args, torch, ws, rank, local)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         v, steps, secs, cores = _cpu_leg(wl, float(os.environ.get("CWA_CPU_SECONDS", "20")))
