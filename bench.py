@@ -409,13 +409,53 @@ def run_profile(args) -> None:
                           "launches": sim.launch_count}))
 
 
+def run_wave(args) -> None:
+    """The wave module stepped alone (no particle passes) on an nx x nz field:
+    `--steps` single wave passes against cwa_wave_advance over the same
+    steps (4 per launch, TMA-loaded tiles), CUDA events on the sim's stream,
+    fields larger than L2 unless --wave-n is small.  Prints one JSON line."""
+    import torch
+
+    from coupledwateranimation_gb300 import Sim, scenes
+    n = args.wave_n
+    d = scenes.reference().desc  # the reference's wave module: no deposits, splash init
+    d.n_particles = 0
+    d.wave_nx = d.wave_nz = n
+    steps = max(4, args.steps // 4 * 4)
+    out = {"mode": "wave", "field": f"{n}x{n}", "steps": steps}
+    with Sim(d, use_graph=False) as sim:
+        sim.wave_reinit(0)
+        stream = torch.cuda.ExternalStream(sim.device_view(0).stream)
+        for label, fn in (("single", lambda: [sim.wave() for _ in range(steps)]),
+                          ("blocked", lambda: sim.wave_advance(steps))):
+            fn()  # warm-up
+            sim.synchronize()
+            best = None
+            for _ in range(max(3, args.warmup)):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                with torch.cuda.stream(stream):
+                    e0.record(stream)
+                    fn()
+                    e1.record(stream)
+                sim.synchronize()
+                ms = e0.elapsed_time(e1)
+                best = ms if best is None else min(best, ms)
+            cells = n * n * steps
+            out[label] = {"us_per_step": best / steps * 1e3, "cell_updates_per_s": cells / (best * 1e-3),
+                          "effective_gbs_at_12B": 12 * cells / (best * 1e-3) / 1e9}
+    out["speedup"] = out["single"]["us_per_step"] / out["blocked"]["us_per_step"]
+    print(json.dumps(out), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "wave"])
+    ap.add_argument("--wave-n", type=int, default=4096, help="field edge for --mode wave")
     ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2])
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2])
     ap.add_argument("--no-cpu", action="store_true")
@@ -429,6 +469,8 @@ def main() -> None:
         run_reference(args)
     elif args.mode == "profile":
         run_profile(args)
+    elif args.mode == "wave":
+        run_wave(args)
     else:
         run_gpu(args)
 

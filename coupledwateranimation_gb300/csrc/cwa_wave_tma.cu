@@ -35,7 +35,7 @@ namespace {
 constexpr int kBoxW = 128, kBoxH = 32;          // box (x, y) in cells
 constexpr int kTileW = kBoxW - 2 * kWaveK;      // 120 output columns
 constexpr int kTileH = kBoxH - 2 * kWaveK;      // 24 output rows
-constexpr int kWaveTmaThreads = 256;
+constexpr int kWaveTmaThreads = kBoxW;  // one thread per box column
 constexpr uint32_t kBoxBytes = kBoxW * kBoxH * sizeof(float);
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
@@ -98,49 +98,63 @@ __global__ void __launch_bounds__(kWaveTmaThreads)
   } else {
     const float* uc = a.in_cur + S->woff;
     const float* up = a.in_prev + S->woff;
-    for (int idx = threadIdx.x; idx < kBoxW * kBoxH; idx += kWaveTmaThreads) {
-      const int lx = idx % kBoxW, ly = idx / kBoxW;
-      const int gx = ox + lx, gy = oy + ly;
+    const int lx = threadIdx.x, gx = ox + lx;
+    for (int ly = 0; ly < kBoxH; ++ly) {
+      const int gy = oy + ly;
       const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
       box[0][ly][lx] = in ? __ldg(uc + (size_t)gy * W + gx) : 0.0f;
       box[1][ly][lx] = in ? __ldg(up + (size_t)gy * W + gx) : 0.0f;
     }
     __syncthreads();
   }
+  // Each thread owns one box column and walks it top to bottom with the
+  // column's north / centre / south values in registers; east and west come
+  // from the neighbouring columns in shared memory.  Domain borders clamp
+  // (the clamped neighbour is the cell itself).
   const float wa = S->wa, wb = S->wb, lam = S->lam, atten = S->atten;
-  const float zero_deposit = S->coupled ? fmul(S->gain, fmul(0.0f, S->dq)) : 0.0f;
-  const int src_x = S->line_source ? W / 2 : -1;
+  const bool coupled = S->coupled != 0;
+  const float zero_deposit = coupled ? fmul(S->gain, fmul(0.0f, S->dq)) : 0.0f;
+  const int lx = threadIdx.x, gx = ox + lx;
+  const bool src_col = S->line_source && gx == W / 2;
+  const bool col_in = gx >= 0 && gx < W;
+  const int le = gx + 1 < W ? lx + 1 : lx, lw = gx > 0 ? lx - 1 : lx;
   int c = 0;  // box[c] = u^t, box[c ^ 1] = u^(t-1), overwritten in place by u^(t+1)
 #pragma unroll 1
   for (int s = 1; s <= kWaveK; ++s) {
     const float(*A)[kBoxW] = box[c];
     float(*B)[kBoxW] = box[c ^ 1];
-    for (int idx = threadIdx.x; idx < kBoxW * kBoxH; idx += kWaveTmaThreads) {
-      const int lx = idx % kBoxW, ly = idx / kBoxW;
-      if (lx < s || lx >= kBoxW - s || ly < s || ly >= kBoxH - s) continue;
-      const int gx = ox + lx, gy = oy + ly;
-      if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
-      const int le = min(gx + 1, W - 1) - ox, lw = max(gx - 1, 0) - ox;
-      const int ln = min(gy + 1, H - 1) - oy, ls = max(gy - 1, 0) - oy;
-      const float nb = fadd(fadd(A[ln][lx], A[ls][lx]), fadd(A[ly][le], A[ly][lw]));
-      float w = fadd(fmul(wa, A[ly][lx]), fmul(lam, nb));
-      w = fsub(w, fmul(wb, B[ly][lx]));
-      w = fmul(atten, w);
-      if (gx == src_x && w > 0.0001f) w = fadd(w, 0.001f);
-      if (S->coupled) w = fadd(w, zero_deposit);
-      B[ly][lx] = w;
+    // rows whose inputs are still exact after s - 1 steps, inside the domain
+    const int r0 = max(s, -oy), r1 = min(kBoxH - s, H - oy);
+    if (col_in && lx >= s && lx < kBoxW - s && r0 < r1) {
+      float south = oy + r0 > 0 ? A[r0 - 1][lx] : A[r0][lx];
+      float mid = A[r0][lx];
+#pragma unroll 4
+      for (int ly = r0; ly < r1; ++ly) {
+        const int gy = oy + ly;
+        const float north = gy + 1 < H ? A[ly + 1][lx] : mid;
+        const float nb = fadd(fadd(north, south), fadd(A[ly][le], A[ly][lw]));
+        float w = fadd(fmul(wa, mid), fmul(lam, nb));
+        w = fsub(w, fmul(wb, B[ly][lx]));
+        w = fmul(atten, w);
+        if (src_col && w > 0.0001f) w = fadd(w, 0.001f);
+        if (coupled) w = fadd(w, zero_deposit);
+        B[ly][lx] = w;
+        south = mid;
+        mid = north;
+      }
     }
     __syncthreads();
     c ^= 1;
   }
   float* oc = a.out_cur + S->woff;
   float* op = a.out_prev + S->woff;
-  for (int idx = threadIdx.x; idx < kTileW * kTileH; idx += kWaveTmaThreads) {
-    const int lx = kWaveK + idx % kTileW, ly = kWaveK + idx / kTileW;
-    const int gx = ox + lx, gy = oy + ly;
-    if (gx >= W || gy >= H) continue;
-    oc[(size_t)gy * W + gx] = box[c][ly][lx];
-    op[(size_t)gy * W + gx] = box[c ^ 1][ly][lx];
+  if (lx >= kWaveK && lx < kBoxW - kWaveK && gx < W) {
+    const int r1 = min(kBoxH - kWaveK, H - oy);
+    for (int ly = kWaveK; ly < r1; ++ly) {
+      const size_t g = (size_t)(oy + ly) * W + gx;
+      oc[g] = box[c][ly][lx];
+      op[g] = box[c ^ 1][ly][lx];
+    }
   }
 }
 
