@@ -179,20 +179,25 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0) -> dict:
-    """The 256-scene workload stepped as one batched sim (one launch per pass
-    over all scenes, CUDA graph) and as 256 single-scene sims run one at a
-    time (each its own graph).  Host wall-clock around the GPU work, with a
-    synchronise at the end of every scene's steps in the plain leg.  Under
-    N ranks each rank steps its shard of the scenes (greedy by device
-    footprint); times are the max over ranks, units the sum."""
+def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0, config: int = 3) -> dict:
+    """A batched workload (256 small scenes, or 64 large ones) stepped as one
+    batched sim (one launch per pass over all scenes, CUDA graph) and as
+    single-scene sims run one at a time (each its own graph).  Host
+    wall-clock around the GPU work, with a synchronise at the end of every
+    scene's steps in the plain leg.  Under N ranks each rank steps its shard
+    of the scenes (greedy by device footprint); times are the max over
+    ranks, units the sum."""
     from coupledwateranimation_gb300 import Sim, scenes, shard
-    full = scenes.with_zsub(scenes.config3(), args.zsub)
+    full = scenes.with_zsub(scenes.CONFIGS[config](), args.zsub)
     _, mine = shard.shard_scenes(full, rank, ws)
     wl = scenes.Workload(full.name, mine, full.steps)
     steps = max(3, min(args.steps, 10))
     dev = f"cuda:{local}"
     n_units = shard.sum_over_ranks(wl.n_particles + wl.n_wave_cells, dev)
+    alg_bytes = shard.sum_over_ranks(sum(
+        sum(BYTES_PER_PARTICLE.values()) * s.desc.n_particles
+        + sum(BYTES_PER_GRID_CELL.values()) * shard.grid_cells(s.desc)
+        + sum(BYTES_PER_WAVE_CELL.values()) * s.desc.wave_nx * s.desc.wave_nz for s in wl.scenes), dev)
     with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local) as sim:
         for k, s in enumerate(wl.scenes):
             sim.upload_particles(k, s.particles)
@@ -229,6 +234,7 @@ def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0) ->
             "batched_updates_per_s": n_units * steps / t_batched,
             "plain_updates_per_s": n_units * steps / t_plain,
             "speedup": t_plain / t_batched,
+            "batched_algorithmic_gbs": alg_bytes * steps / t_batched / 1e9,
             "batched_ms_per_step": t_batched / steps * 1e3, "plain_ms_per_step": t_plain / steps * 1e3}
 
 
@@ -409,6 +415,27 @@ def run_profile(args) -> None:
                           "launches": sim.launch_count}))
 
 
+def run_batched(args) -> None:
+    """`--mode batched`: the batched-vs-plain comparison alone for --config 3
+    (256 small scenes) or 4 (64 large scenes), one JSON line."""
+    import torch
+    import torch.distributed as dist
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    cfg = args.config if args.config in (3, 4) else 3
+    r = batched_vs_plain(args, torch, ws, rank, local, cfg)
+    if rank == 0:
+        peak, kind = _peaks()
+        r["batched_hbm_frac"] = r["batched_algorithmic_gbs"] / peak
+        r["peak_gbs"] = peak
+        print(json.dumps({"mode": "batched", **r}), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
 def run_wave(args) -> None:
     """The wave module stepped alone (no particle passes) on an nx x nz field:
     `--steps` single wave passes against cwa_wave_advance over the same
@@ -454,9 +481,9 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "wave"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "wave", "batched"])
     ap.add_argument("--wave-n", type=int, default=4096, help="field edge for --mode wave")
-    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
@@ -471,6 +498,8 @@ def main() -> None:
         run_profile(args)
     elif args.mode == "wave":
         run_wave(args)
+    elif args.mode == "batched":
+        run_batched(args)
     else:
         run_gpu(args)
 
