@@ -92,6 +92,9 @@ struct cwa_sim {
   int64_t steps = 0;
   int64_t launches = 0;
   bool grid_fresh = false;
+  // per-step mode: integrate has already hashed and counted the current
+  // positions for the next grid build (count holds those counts)
+  bool counts_pending = false;
   bool profiling = false;
   bool pass_times_valid = false;
   cudaEvent_t ev[CWA_PASS_COUNT + 1] = {};
@@ -326,7 +329,25 @@ NbArgs nb_args(cwa_sim* s) {
   return a;
 }
 
-// Grid pass: hash + count, scan, stable insert, reorder.  Per-step mode
+// Counts of an earlier fused hash are stale once the particles change
+// outside a step (uploads, checkpoint loads, the autotuner's restores).
+cwa_status drop_pending_counts(cwa_sim* s) {
+  if (s->counts_pending) {
+    CWA_CUDA(cudaMemsetAsync(s->count, 0, (size_t)s->c_total * sizeof(int32_t), s->stream));
+    s->counts_pending = false;
+  }
+  return CWA_OK;
+}
+
+cwa_status run_hash(cwa_sim* s) {
+  CWA_CUDA(launch_hash_count(s->P[s->cur], s->d_ptiles, s->n_ptiles, s->ptile, s->d_scenes, s->key, s->slot,
+                             s->count, s->d_status, s->verlet ? s->d_flag : nullptr, s->stream));
+  s->launches += s->n_ptiles > 0;
+  return CWA_OK;
+}
+
+// Grid pass: hash + count (unless integrate has already done it), scan,
+// stable insert, reorder.  Per-step mode
 // flips the live buffers every step.  Verlet mode runs the same kernels
 // only when the device rebuild flag is up (each kernel checks it), copies
 // the reordered state back into the live buffers and rebuilds the Verlet
@@ -335,9 +356,8 @@ cwa_status run_grid(cwa_sim* s) {
   cudaStream_t st = s->stream;
   const int cur = s->cur, nxt = cur ^ 1;
   const int32_t* flag = s->verlet ? s->d_flag : nullptr;
-  CWA_CUDA(launch_hash_count(s->P[cur], s->d_ptiles, s->n_ptiles, s->ptile, s->d_scenes, s->key, s->slot,
-                             s->count, s->d_status, flag, st));
-  s->launches += s->n_ptiles > 0;
+  if (!s->counts_pending) CWA_TRY(run_hash(s));
+  s->counts_pending = false;  // the scan consumes (and clears) the counts
   CWA_CUDA(scan_launch(s->count, s->start, s->c_total, s->c_total + 1, true, s->scan, s->d_status, st,
                        &s->launches, flag));
   CWA_CUDA(launch_list_insert(s->key, s->slot, s->start, s->list, s->n_total, flag, st));
@@ -376,13 +396,20 @@ cwa_status run_force(cwa_sim* s) {
 
 cwa_status run_integrate(cwa_sim* s) {
   if (s->verlet) CWA_CUDA(cudaMemsetAsync(s->d_flag, 0, sizeof(int32_t), s->stream));
+  // Per-step mode hashes and counts the new positions here for the next
+  // grid build.  (Verlet mode rebuilds rarely and keeps the separate pass.)
+  const bool fuse = !s->verlet;
+  if (fuse) CWA_TRY(drop_pending_counts(s));  // integrate twice without a grid in between
   CWA_CUDA(launch_integrate(s->P[s->cur], s->V[s->cur], cur_force(s), s->RP, s->d_ptiles, s->n_ptiles,
                             s->ptile, s->d_scenes, s->U[s->wcur], s->D, s->verlet ? s->XR : nullptr,
-                            s->verlet ? s->d_flag : nullptr, s->stream));
+                            s->verlet ? s->d_flag : nullptr, fuse ? s->key : nullptr, fuse ? s->slot : nullptr,
+                            fuse ? s->count : nullptr, s->d_status, s->stream));
   s->launches += s->n_ptiles > 0;
+  s->counts_pending = fuse && s->n_ptiles > 0;
   if (!s->verlet) s->grid_fresh = false;  // a Verlet list stays usable
   return CWA_OK;
 }
+
 
 cwa_status run_wave(cwa_sim* s) {
   const int w = s->wcur;
@@ -496,6 +523,12 @@ cwa_status enqueue_step(cwa_sim* s) {
 // Capture one step for the current (cur, wcur) phase; the host-side state
 // the capture advanced is rolled back, the graph launch advances it again.
 cwa_status graph_step(cwa_sim* s) {
+  // Graphs start at the scan: in per-step mode the counts come from the
+  // previous step's integrate, or from this eager hash after an upload.
+  if (!s->verlet && !s->counts_pending && s->n_ptiles > 0) {
+    CWA_TRY(run_hash(s));
+    s->counts_pending = true;
+  }
   const int phase = s->cur * 3 + s->wcur;
   const int cur0 = s->cur, w0 = s->wcur;
   const int64_t steps0 = s->steps, launches0 = s->launches;
@@ -529,6 +562,7 @@ cwa_status graph_step(cwa_sim* s) {
   }
   s->wcur = (s->wcur + 1) % 3;
   s->steps += 1;
+  s->counts_pending = !s->verlet && s->n_ptiles > 0;
   return CWA_OK;
 }
 
@@ -770,6 +804,7 @@ cwa_status cwa_upload_particles(cwa_sim* s, int32_t scene, const cwa_particle* h
                          s->ID[s->cur], s->stream));
   s->launches += 1;
   s->grid_fresh = false;
+  CWA_TRY(drop_pending_counts(s));
   if (s->verlet) {  // the new particles need a fresh grid and Verlet list
     const int32_t one = 1;
     CWA_CUDA(cudaMemcpyAsync(s->d_flag, &one, sizeof(one), cudaMemcpyHostToDevice, s->stream));
@@ -1079,6 +1114,7 @@ cwa_status cwa_load(cwa_sim* s, const char* path) {
   }
   s->steps = steps;
   s->grid_fresh = s->verlet;  // per-step mode rebuilds its grid every step anyway
+  CWA_TRY(drop_pending_counts(s));
   return CWA_OK;
 }
 
@@ -1114,6 +1150,7 @@ cwa_status cwa_get_launch_count(cwa_sim* s, int64_t* launches) {
 cwa_status cwa_autotune(cwa_sim* s, int32_t trial_steps, cwa_tune_report* out) {
   CWA_TRY(check_sim(s));
   if (trial_steps < 1 || trial_steps > 1000) return arg_error("trial_steps must be in [1, 1000]");
+  CWA_TRY(drop_pending_counts(s));  // every trial starts from zero counts
   CWA_CUDA(cudaStreamSynchronize(s->stream));
   std::vector<StateItem> items = state_items(s);
   size_t total = 0;
@@ -1169,6 +1206,8 @@ cwa_status cwa_autotune(cwa_sim* s, int32_t trial_steps, cwa_tune_report* out) {
       err = copy_state(false);
       s->cur = cur0;
       s->wcur = w0;
+      s->counts_pending = true;  // the last trial's integrate counted its own positions
+      if (err == cudaSuccess && drop_pending_counts(s) != CWA_OK) err = cudaErrorUnknown;
       if (err != cudaSuccess) break;
       cwa_status st = enqueue_step(s);  // warm-up
       if (st == CWA_OK) err = cudaEventRecord(e0, s->stream);
@@ -1208,6 +1247,8 @@ cwa_status cwa_autotune(cwa_sim* s, int32_t trial_steps, cwa_tune_report* out) {
   if (s->ptile != want_ptile) set_particle_tiles(s, want_ptile);
   cudaError_t e2 = copy_state(false);
   if (err == cudaSuccess) err = e2;
+  s->counts_pending = true;
+  if (drop_pending_counts(s) != CWA_OK && err == cudaSuccess) err = cudaErrorUnknown;
   cudaStreamSynchronize(s->stream);
   s->cur = cur0;
   s->wcur = w0;

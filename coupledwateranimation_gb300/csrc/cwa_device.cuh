@@ -19,6 +19,24 @@ __device__ __forceinline__ int cell_axis(float p, float lo, float cell, int n) {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+__device__ __forceinline__ bool finite3(float4 p) {
+  return isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
+}
+
+// Warp-aggregated count: lanes with the same key share one atomicAdd; each
+// lane's slot is its arrival rank within the cell.
+__device__ __forceinline__ int count_slot(int32_t* count, int key) {
+  const unsigned int active = __activemask();
+  const unsigned int peers = __match_any_sync(active, key);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  const int rank = __popc(peers & ((1u << lane) - 1u));
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count + key, __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return base + rank;
+}
+
 // texture(wave_tex, uv) with GL_LINEAR / GL_CLAMP_TO_EDGE on an R32F image
 // (StencilImage2DTripleBuffered.cpp:21-26): texel centres at (i + 0.5) / W.
 struct Bilinear {

@@ -140,24 +140,6 @@ __global__ void __launch_bounds__(kScanBlock)
   }
 }
 
-__device__ __forceinline__ bool finite3(float4 p) {
-  return isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
-}
-
-// Warp-aggregated count: lanes with the same key share one atomicAdd; each
-// lane's slot is its arrival rank within the cell.
-__device__ __forceinline__ int count_slot(int32_t* count, int key) {
-  const unsigned int active = __activemask();
-  const unsigned int peers = __match_any_sync(active, key);
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(peers) - 1;
-  const int rank = __popc(peers & ((1u << lane) - 1u));
-  int base = 0;
-  if (lane == leader) base = atomicAdd(count + key, __popc(peers));
-  base = __shfl_sync(peers, base, leader);
-  return base + rank;
-}
-
 __global__ void __launch_bounds__(256)
     k_hash_count(const float4* __restrict__ pos, const Tile* __restrict__ tiles,
                  const SceneDev* __restrict__ scenes, int32_t* __restrict__ key,

@@ -152,11 +152,15 @@ cudaError_t launch_force(int precision, const NbArgs& a, cudaStream_t stream);
 
 // ---- integrate / wave / packing kernels (cwa_step.cu) ----
 // xref/flag (Verlet mode): raises *flag when a particle has moved more than
-// skin h / 2 from its rebuild position; null otherwise.
+// skin h / 2 from its rebuild position; null otherwise.  key/slot/count
+// (per-step mode): the next grid build's cell hash and warp-aggregated
+// count on the new positions (the work of the hash-count kernel), so that
+// build starts at the scan; null to skip.
 cudaError_t launch_integrate(float4* pos, float4* vel, float4* force, float2* rho_p, const Tile* tiles,
                              int32_t n_tiles, int32_t tile_size, const SceneDev* scenes,
                              const float* wave_u, unsigned long long* deposits, const float4* xref,
-                             int32_t* flag, cudaStream_t stream);
+                             int32_t* flag, int32_t* key, int32_t* slot, int32_t* count, int32_t* status,
+                             cudaStream_t stream);
 cudaError_t launch_wave(const float* u_n, const float* u_nm1, float* u_out, unsigned long long* deposits,
                         const Tile* wtiles, int32_t n_wtiles, int32_t wtile_size, const SceneDev* scenes,
                         cudaStream_t stream);

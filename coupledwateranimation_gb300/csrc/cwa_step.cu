@@ -28,7 +28,9 @@ __global__ void __launch_bounds__(128)
     k_integrate(float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ force,
                 float2* __restrict__ rho_p, const Tile* __restrict__ tiles,
                 const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
-                unsigned long long* __restrict__ deposits, const float4* __restrict__ xref, int32_t* flag) {
+                unsigned long long* __restrict__ deposits, const float4* __restrict__ xref, int32_t* flag,
+                int32_t* __restrict__ key, int32_t* __restrict__ slot, int32_t* __restrict__ count,
+                int32_t* status) {
   const Tile tl = tiles[blockIdx.x];
   const int i = tl.begin + threadIdx.x;
   if (i >= tl.end) return;
@@ -118,8 +120,18 @@ __global__ void __launch_bounds__(128)
       v[1] = fmul(v[1], -e);
     }
   }
-  pos[i] = make_float4(x[0], x[1], x[2], p.w);
+  const float4 pn = make_float4(x[0], x[1], x[2], p.w);
+  pos[i] = pn;
   vel[i] = make_float4(v[0], v[1], v[2], v0.w);
+  if (key) {  // the next grid build's cell hash + count, on the position just written
+    if (!finite3(pn)) atomicOr(status, kStatusNonFinite);
+    const int ny = S->dims[1], nz = S->dims[2];
+    const int k = S->coff + (cell_axis(pn.x, S->lo[0], S->cell, S->dims[0]) * ny +
+                             cell_axis(pn.y, S->lo[1], S->cell, ny)) * nz +
+                  cell_axis(pn.z, S->lo[2], S->cellz, nz);
+    key[i] = k;
+    slot[i] = count_slot(count, k);
+  }
   if (xref) {  // Verlet mode: has this particle left its skin?
     const float4 r = xref[i];
     const float dx = x[0] - r.x, dy = x[1] - r.y, dz = x[2] - r.z;
@@ -344,10 +356,11 @@ inline int blocks_for(long n, int b) { return (int)((n + b - 1) / b); }
 cudaError_t launch_integrate(float4* pos, float4* vel, float4* force, float2* rho_p, const Tile* tiles,
                              int32_t n_tiles, int32_t tile_size, const SceneDev* scenes,
                              const float* wave_u, unsigned long long* deposits, const float4* xref,
-                             int32_t* flag, cudaStream_t stream) {
+                             int32_t* flag, int32_t* key, int32_t* slot, int32_t* count, int32_t* status,
+                             cudaStream_t stream) {
   if (n_tiles <= 0) return cudaSuccess;
   k_integrate<<<n_tiles, tile_size, 0, stream>>>(pos, vel, force, rho_p, tiles, scenes, wave_u, deposits, xref,
-                                                 flag);
+                                                 flag, key, slot, count, status);
   return cudaGetLastError();
 }
 
