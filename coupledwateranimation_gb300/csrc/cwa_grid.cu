@@ -20,7 +20,7 @@ namespace cwa {
 namespace {
 
 constexpr int kScanBlock = 256;
-constexpr int kScanItems = 8;
+constexpr int kScanItems = 16;  // 4096-item tiles: half the look-back chain of 2048
 constexpr int kScanTile = kScanBlock * kScanItems;
 constexpr unsigned long long kFlagAgg = 1ull << 32;
 constexpr unsigned long long kFlagInc = 2ull << 32;
@@ -43,8 +43,10 @@ __device__ __forceinline__ int warp_sum(int v) {
 }
 
 // One tile of kScanTile items per CTA; tiles are ticketed in start order so a
-// CTA only ever waits on CTAs that are already running.
-template <bool kZero>
+// CTA only ever waits on CTAs that are already running.  kVec: in and out
+// are 16-byte aligned, so each thread moves its 16 items as four int4s
+// (a vector that would cross n_in / n_out falls back to scalar accesses).
+template <bool kZero, bool kVec>
 __global__ void __launch_bounds__(kScanBlock)
     k_scan(int32_t* in, int32_t* out, int32_t n_in, int32_t n_out, unsigned int* counter,
            unsigned long long* state, int32_t* status, const int32_t* flag) {
@@ -58,15 +60,36 @@ __global__ void __launch_bounds__(kScanBlock)
   const long base = (long)tile * kScanTile + (long)threadIdx.x * kScanItems;
 
   int v[kScanItems];
+  if (kVec) {
 #pragma unroll
-  for (int k = 0; k < kScanItems; ++k) {
-    long idx = base + k;
-    v[k] = idx < n_in ? in[idx] : 0;
-  }
-  if (kZero) {
+    for (int q = 0; q < kScanItems / 4; ++q) {
+      const long idx = base + 4 * q;
+      if (idx + 3 < n_in) {
+        const int4 x = *reinterpret_cast<const int4*>(in + idx);
+        v[4 * q] = x.x;
+        v[4 * q + 1] = x.y;
+        v[4 * q + 2] = x.z;
+        v[4 * q + 3] = x.w;
+        if (kZero) *reinterpret_cast<int4*>(in + idx) = make_int4(0, 0, 0, 0);
+      } else {
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k)
-      if (base + k < n_in) in[base + k] = 0;
+        for (int k = 0; k < 4; ++k) {
+          v[4 * q + k] = idx + k < n_in ? in[idx + k] : 0;
+          if (kZero && idx + k < n_in) in[idx + k] = 0;
+        }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      long idx = base + k;
+      v[k] = idx < n_in ? in[idx] : 0;
+    }
+    if (kZero) {
+#pragma unroll
+      for (int k = 0; k < kScanItems; ++k)
+        if (base + k < n_in) in[base + k] = 0;
+    }
   }
   int tsum = 0;
 #pragma unroll
@@ -133,10 +156,25 @@ __global__ void __launch_bounds__(kScanBlock)
   }
   __syncthreads();
   const int prefix = s_prefix + thread_excl;
+  if (kVec) {
 #pragma unroll
-  for (int k = 0; k < kScanItems; ++k) {
-    long idx = base + k;
-    if (idx < n_out) out[idx] = prefix + v[k];
+    for (int q = 0; q < kScanItems / 4; ++q) {
+      const long idx = base + 4 * q;
+      if (idx + 3 < n_out) {
+        *reinterpret_cast<int4*>(out + idx) =
+            make_int4(prefix + v[4 * q], prefix + v[4 * q + 1], prefix + v[4 * q + 2], prefix + v[4 * q + 3]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (idx + k < n_out) out[idx + k] = prefix + v[4 * q + k];
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      long idx = base + k;
+      if (idx < n_out) out[idx] = prefix + v[k];
+    }
   }
 }
 
@@ -265,12 +303,21 @@ cudaError_t scan_launch(const int32_t* in, int32_t* out, int32_t n_in, int32_t n
   cudaError_t e = cudaMemsetAsync(ws.counter, 0, 256 + (size_t)ws.n_tiles * 8, stream);
   if (e != cudaSuccess) return e;
   int32_t* inw = const_cast<int32_t*>(in);
-  if (zero_input)
-    k_scan<true><<<ws.n_tiles, kScanBlock, 0, stream>>>(inw, out, n_in, n_out, ws.counter, ws.state, status,
-                                                         flag);
-  else
-    k_scan<false><<<ws.n_tiles, kScanBlock, 0, stream>>>(inw, out, n_in, n_out, ws.counter, ws.state, status,
-                                                          flag);
+  const bool vec = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+#define CWA_SCAN_K(Z, V) \
+  k_scan<Z, V><<<ws.n_tiles, kScanBlock, 0, stream>>>(inw, out, n_in, n_out, ws.counter, ws.state, status, flag)
+  if (zero_input) {
+    if (vec)
+      CWA_SCAN_K(true, true);
+    else
+      CWA_SCAN_K(true, false);
+  } else {
+    if (vec)
+      CWA_SCAN_K(false, true);
+    else
+      CWA_SCAN_K(false, false);
+  }
+#undef CWA_SCAN_K
   if (launches) *launches += 1;
   return cudaGetLastError();
 }

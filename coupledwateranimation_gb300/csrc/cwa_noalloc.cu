@@ -32,8 +32,9 @@ namespace cwa {
 namespace {
 
 constexpr int32_t kNoAllocMaxN = CWA_NOALLOC_SCAN_MAX_N;
-// ticket + tile states for kNoAllocMaxN elements (256 + 8 per 2048-element
-// tile), then one status word in its own 256-byte line
+// ticket + tile states for kNoAllocMaxN elements (256 + 8 per tile; sized
+// for 2048-element tiles, twice what the 4096-element tiles use), then one
+// status word in its own 256-byte line
 constexpr size_t kNoAllocScratchBytes = 256 + (size_t)(kNoAllocMaxN / 2048) * 8 + 256;
 
 static __device__ __align__(256) unsigned char g_scan_scratch[kNoAllocScratchBytes];
