@@ -104,6 +104,7 @@ _PROTOS = {
     "cwa_pass_integrate": (C.c_int, [_P]),
     "cwa_pass_wave": (C.c_int, [_P]),
     "cwa_wave_advance": (C.c_int, [_P, _I32]),
+    "cwa_wave_init_from_image": (C.c_int, [_P, _I32, C.c_void_p, _I32, _I32]),
     "cwa_synchronize": (C.c_int, [_P]),
     "cwa_get_step_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "cwa_get_rebuild_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),

@@ -865,6 +865,30 @@ cwa_status cwa_wave_reinit(cwa_sim* s, int32_t scene) {
   return CWA_OK;
 }
 
+cwa_status cwa_wave_init_from_image(cwa_sim* s, int32_t scene, const uint8_t* rgba, int32_t width,
+                                    int32_t height) {
+  CWA_TRY(check_scene(s, scene));
+  if (width < 1 || height < 1 || !rgba) return arg_error("image must be at least 1x1 RGBA8 texels");
+  if ((int64_t)width * height > (1ll << 28)) return arg_error("image above 2^28 texels");
+  const SceneDev& d = s->sd[scene];
+  const size_t bytes = (size_t)width * height * 4;
+  const size_t cells = (size_t)d.nx * d.nz;
+  const int w = s->wcur;
+  uint8_t* img = nullptr;
+  CWA_CUDA(cudaMalloc((void**)&img, bytes));
+  cudaError_t e = cudaMemcpyAsync(img, rgba, bytes, cudaMemcpyHostToDevice, s->stream);
+  // the rotation for this scene alone: u^(n-1) <- u^n, then u^n <- image
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->U[(w + 2) % 3] + d.woff, s->U[w] + d.woff, cells * sizeof(float),
+                        cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) e = launch_wave_from_image(s->U[w] + d.woff, d.nx, d.nz, img, width, height, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  cudaFree(img);
+  CWA_CUDA(e);
+  s->launches += 1;
+  return CWA_OK;
+}
+
 cwa_status cwa_step(cwa_sim* s, int32_t n_steps) {
   CWA_TRY(check_sim(s));
   if (n_steps < 0) return arg_error("n_steps < 0");

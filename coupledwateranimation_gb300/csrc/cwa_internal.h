@@ -165,6 +165,9 @@ cudaError_t launch_wave(const float* u_n, const float* u_nm1, float* u_out, unsi
                         const Tile* wtiles, int32_t n_wtiles, int32_t wtile_size, const SceneDev* scenes,
                         cudaStream_t stream);
 cudaError_t launch_wave_init(float* u, int32_t nx, int32_t nz, float mode, cudaStream_t stream);
+// u(x, y) = red(2x, y) / 255 of a w x h RGBA8 image (device memory), 0 past it.
+cudaError_t launch_wave_from_image(float* u, int32_t nx, int32_t nz, const uint8_t* rgba, int32_t w, int32_t h,
+                                   cudaStream_t stream);
 cudaError_t launch_unpack(const cwa_particle* aos, int32_t n, int32_t poff, float4* pos, float4* vel,
                           float4* force, float2* rho_p, float2* extra, int32_t* id, cudaStream_t stream);
 cudaError_t launch_pack(cwa_particle* aos, int32_t n, int32_t poff, const float4* pos, const float4* vel,

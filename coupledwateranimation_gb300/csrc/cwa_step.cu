@@ -372,6 +372,26 @@ cudaError_t launch_wave(const float* u_n, const float* u_nm1, float* u_out, unsi
   return cudaGetLastError();
 }
 
+// InitFromImage (wave_comp.glsl:73-77): cell (x, y) takes the red channel of
+// texel (2x, y) of an RGBA8 texture as a normalised float, c / 255.  The
+// shader's texelFetch past the image is undefined; here it reads 0.
+__global__ void k_wave_from_image(float* __restrict__ u, int32_t nx, int32_t nz,
+                                  const uint8_t* __restrict__ rgba, int32_t w, int32_t h) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nx * nz) return;
+  const int y = c / nx, x = c - y * nx;
+  const int tx = 2 * x;
+  u[c] = (tx < w && y < h) ? __fdiv_rn((float)rgba[((size_t)y * w + tx) * 4], 255.0f) : 0.0f;
+}
+
+cudaError_t launch_wave_from_image(float* u, int32_t nx, int32_t nz, const uint8_t* rgba, int32_t w, int32_t h,
+                                   cudaStream_t stream) {
+  long n = (long)nx * nz;
+  if (n <= 0) return cudaSuccess;
+  k_wave_from_image<<<blocks_for(n, 256), 256, 0, stream>>>(u, nx, nz, rgba, w, h);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_wave_init(float* u, int32_t nx, int32_t nz, float mode, cudaStream_t stream) {
   long n = (long)nx * nz;
   if (n <= 0) return cudaSuccess;

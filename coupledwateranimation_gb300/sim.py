@@ -114,6 +114,15 @@ class Sim:
     def wave(self) -> None:
         check(self._lib.cwa_pass_wave(self._h), "cwa_pass_wave")
 
+    def wave_init_from_image(self, scene: int, rgba: np.ndarray) -> None:
+        """ReinitFromTexture: u^n <- red(2x, y) / 255 of an (h, w, 4) uint8
+        texture whose row 0 is texture row 0; u^(n-1) <- the old u^n."""
+        img = np.ascontiguousarray(rgba, dtype=np.uint8)
+        if img.ndim != 3 or img.shape[2] != 4:
+            raise ValueError("expected an (h, w, 4) RGBA8 image")
+        check(self._lib.cwa_wave_init_from_image(self._h, scene, img.ctypes.data, img.shape[1], img.shape[0]),
+              "cwa_wave_init_from_image")
+
     def wave_advance(self, n: int) -> None:
         """n wave passes with no particle passes between them (4 per launch)."""
         check(self._lib.cwa_wave_advance(self._h, int(n)), "cwa_wave_advance")

@@ -208,6 +208,15 @@ cwa_status cwa_download_wave(cwa_sim* sim, int32_t scene, float* u_n, float* u_n
 /* StencilImage2DTripleBuffered::Reinit (StencilImage2DTripleBuffered.cpp:42-59):
  * wave_comp.glsl InitWave (MODE_INIT, :259-317) into both history buffers. */
 cwa_status cwa_wave_reinit(cwa_sim* sim, int32_t scene);
+/* StencilImage2DTripleBuffered::ReinitFromTexture (StencilImage2DTripleBuffered.cpp:61-77):
+ * wave_comp.glsl InitFromImage (MODE_INIT_FROM_TEXTURE, :73-77) writes
+ * u(x, y) = red(2x, y) / 255 of an RGBA8 texture, then the buffers rotate,
+ * so u^n is the image field and u^(n-1) the old u^n.  `rgba` is host memory,
+ * width x height texels of 4 bytes, row 0 = texture row 0 (the bottom row of
+ * a bitmap loaded bottom-up, as the reference's loader does).  Texels past
+ * the image read 0 (undefined in the shader).  Synchronous. */
+cwa_status cwa_wave_init_from_image(cwa_sim* sim, int32_t scene, const uint8_t* rgba, int32_t width,
+                                    int32_t height);
 
 /* One full step per iteration: grid -> rho_pres -> force -> integrate -> wave
  * (idle(), Main.cpp:549-560, plus the uniform-grid sort).  Asynchronous. */

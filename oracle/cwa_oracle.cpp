@@ -830,6 +830,16 @@ void orc_wave_f32(const cwa_scene_desc* sc, const float* u_n, const float* u_nm1
     }
 }
 
+// InitFromImage (wave_comp.glsl:73-77): texelFetch(uInitImage, coord * (2, 1)).r
+// of an RGBA8 texture is c / 255 in float; past the image, 0.
+void orc_wave_from_image_f32(int32_t nx, int32_t nz, const uint8_t* rgba, int32_t w, int32_t h, float* u) {
+  for (int32_t y = 0; y < nz; ++y)
+    for (int32_t x = 0; x < nx; ++x) {
+      const int32_t tx = 2 * x;
+      u[(size_t)y * nx + x] = (tx < w && y < h) ? (float)rgba[((size_t)y * w + tx) * 4] / 255.0f : 0.0f;
+    }
+}
+
 // InitWave (wave_comp.glsl:259-317) in float32.
 void orc_wave_init_f32(const cwa_scene_desc* sc, float* u) {
   const int W = sc->wave_nx, H = sc->wave_nz;

@@ -56,6 +56,7 @@ def load() -> C.CDLL:
             "orc_integrate_f32": (None, [_P, _I, _P, _P, _P]),
             "orc_wave_f32": (None, [_P, _P, _P, _P, _P]),
             "orc_wave_init_f32": (None, [_P, _P]),
+            "orc_wave_from_image_f32": (None, [C.c_int32, C.c_int32, _P, C.c_int32, C.c_int32, _P]),
             "orc_sample_f32": (C.c_float, [_P, _I, _I, C.c_float, C.c_float]),
         }
         for name, (res, args) in protos.items():
@@ -207,6 +208,15 @@ def wave_f32(desc, u_n, u_nm1, deposits=None) -> np.ndarray:
     out = np.zeros_like(a)
     dep = None if deposits is None else np.ascontiguousarray(deposits, np.int64)
     load().orc_wave_f32(_d(desc), _p(a), _p(b), _p(out), _p(dep))
+    return out
+
+
+def wave_from_image_f32(nx: int, nz: int, rgba: np.ndarray) -> np.ndarray:
+    """InitFromImage on an (h, w, 4) uint8 texture (row 0 = texture row 0)."""
+    img = np.ascontiguousarray(rgba, np.uint8)
+    h, w = img.shape[:2]
+    out = np.zeros((nz, nx), np.float32)
+    load().orc_wave_from_image_f32(nx, nz, _p(img), w, h, _p(out))
     return out
 
 

@@ -6,6 +6,12 @@ variant at UniformGrid2D/ParallelScan.cpp:117), read from the reference's
 source text, with the truth computed by the test's own serial rule
 (SphWave2D/ParallelScan.cpp:130-137: truth[i] = sum of x[0..i-1]).
 
+init_textures.npz — the reference's three InitFromImage textures
+(CoupledWaterAnimation/init-textures/{splash,wake,breaking-wave}.png, 64x64)
+decoded to RGBA8 by coupledwateranimation_gb300.images (rows top-down, as
+stored in the files), so the GPU tests can run the init-from-image path on
+them without the reference checkout.
+
 oracle_regression.json — outputs of the CPU oracle on small fixed scenes
 (hashes of float32 bit patterns and int arrays).  These pin the oracle
 against accidental change; they are not reference outputs (the reference's
@@ -53,6 +59,15 @@ def make_kat(reference: Path) -> None:
     (HERE / "parallel_scan_kat.json").write_text(json.dumps({"cases": cases}, indent=1) + "\n")
 
 
+def make_init_textures(reference: Path) -> None:
+    from coupledwateranimation_gb300 import images
+
+    src = reference / "CoupledWaterAnimation" / "init-textures"
+    arrays = {name.replace("-", "_"): images.read_png(src / f"{name}.png")
+              for name in ("splash", "wake", "breaking-wave")}
+    np.savez_compressed(HERE / "init_textures.npz", **arrays)
+
+
 def _h(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
@@ -89,5 +104,6 @@ if __name__ == "__main__":
     ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
     if ref.exists():
         make_kat(ref)
+        make_init_textures(ref)
     make_oracle_regression()
     print("golden fixtures written to", HERE)
