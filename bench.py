@@ -436,6 +436,36 @@ def run_batched(args) -> None:
         dist.destroy_process_group()
 
 
+def run_render(args) -> None:
+    """`--mode render`: one headless frame (cwa_render, the reference's
+    display()) of the workload's first scene after --warmup steps, at
+    --width x --height with the reference's startup view; host wall-clock of
+    the synchronous call (best of --steps).  --png writes the last frame."""
+    from coupledwateranimation_gb300 import Sim, images, scenes
+    from coupledwateranimation_gb300.sim import render_defaults
+    wl = scenes.with_zsub(scenes.CONFIGS[args.config](), args.zsub)
+    sc = wl.scenes[0]
+    with Sim(sc.desc, precision=args.precision) as sim:
+        sim.upload_particles(0, sc.particles)
+        sim.upload_wave(0, sc.wave, sc.wave)
+        sim.step(args.warmup)
+        cam, prm = render_defaults(args.width, args.height)
+        img = sim.render(0, camera=cam, params=prm)  # warm-up
+        best = None
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            img = sim.render(0, camera=cam, params=prm)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+    if args.png:
+        with open(args.png, "wb") as f:
+            f.write(images.encode_png(images.gl_rows(img)))
+    print(json.dumps({"mode": "render", "workload": wl.name, "particles": sc.desc.n_particles,
+                      "image": f"{args.width}x{args.height}", "surface_res": prm.surface_res,
+                      "ms_per_frame": best * 1e3, "frames_per_s": 1.0 / best,
+                      "lit_pixels": int((img[..., :3] != 0).any(axis=2).sum())}), flush=True)
+
+
 def run_wave(args) -> None:
     """The wave module stepped alone (no particle passes) on an nx x nz field:
     `--steps` single wave passes against cwa_wave_advance over the same
@@ -481,7 +511,10 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "wave", "batched"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "wave", "batched", "render"])
+    ap.add_argument("--width", type=int, default=1920, help="image width for --mode render")
+    ap.add_argument("--height", type=int, default=1080, help="image height for --mode render")
+    ap.add_argument("--png", default="", help="--mode render: write the frame to this PNG")
     ap.add_argument("--wave-n", type=int, default=4096, help="field edge for --mode wave")
     ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2])
@@ -500,6 +533,8 @@ def main() -> None:
         run_wave(args)
     elif args.mode == "batched":
         run_batched(args)
+    elif args.mode == "render":
+        run_render(args)
     else:
         run_gpu(args)
 

@@ -62,6 +62,18 @@ class SimOptions(C.Structure):
                 ("nb_scan_minb", C.c_int32), ("nb_force_minb", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
+class Camera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("center", C.c_float * 3), ("up", C.c_float * 3), ("fovy", C.c_float),
+                ("near_z", C.c_float), ("far_z", C.c_float)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("angle", C.c_float), ("particle_scale", C.c_float),
+                ("wave_scale", C.c_float), ("point_size", C.c_float), ("surface_res", C.c_int32),
+                ("draw_surface", C.c_int32), ("draw_particles", C.c_int32), ("draw_skybox", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
+
+
 class TuneReport(C.Structure):
     _fields_ = [("best", SimOptions), ("best_ms", C.c_float), ("entry_ms", C.c_float),
                 ("n_tried", C.c_int32), ("tried", SimOptions * 32), ("tried_ms", C.c_float * 32)]
@@ -105,6 +117,9 @@ _PROTOS = {
     "cwa_pass_wave": (C.c_int, [_P]),
     "cwa_wave_advance": (C.c_int, [_P, _I32]),
     "cwa_wave_init_from_image": (C.c_int, [_P, _I32, C.c_void_p, _I32, _I32]),
+    "cwa_render_defaults": (C.c_int, [_I32, _I32, C.POINTER(Camera), C.POINTER(RenderParams)]),
+    "cwa_render_set_skybox": (C.c_int, [_P, C.c_void_p, _I32]),
+    "cwa_render": (C.c_int, [_P, _I32, C.POINTER(Camera), C.POINTER(RenderParams), C.c_void_p]),
     "cwa_synchronize": (C.c_int, [_P]),
     "cwa_get_step_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "cwa_get_rebuild_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),

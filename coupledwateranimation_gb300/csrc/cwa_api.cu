@@ -101,6 +101,7 @@ struct cwa_sim {
   cudaGraphExec_t graph[6] = {};
   int64_t graph_launches[6] = {};
   std::vector<void*> dev_allocs;
+  RenderState* render = nullptr;  // cube map for cwa_render, created on first use
 };
 
 namespace {
@@ -594,6 +595,7 @@ void free_sim(cwa_sim* s) {
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
   for (void* p : s->dev_allocs) cudaFree(p);
+  render_state_free(s->render);
   if (s->h_status) cudaFreeHost(s->h_status);
   if (s->h_totals) cudaFreeHost(s->h_totals);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -887,6 +889,59 @@ cwa_status cwa_wave_init_from_image(cwa_sim* s, int32_t scene, const uint8_t* rg
   CWA_CUDA(e);
   s->launches += 1;
   return CWA_OK;
+}
+
+cwa_status cwa_render_defaults(int32_t width, int32_t height, cwa_camera* cam, cwa_render_params* prm) {
+  if (!cam || !prm) return arg_error("null output");
+  if (width < 1 || height < 1) return arg_error("image must be at least 1x1");
+  *cam = cwa_camera{};
+  *prm = cwa_render_params{};
+  cam->eye[0] = 7.0f;
+  cam->eye[1] = 4.0f;
+  cam->eye[2] = 0.0f;
+  cam->center[0] = 0.0f;
+  cam->center[1] = -1.0f;
+  cam->center[2] = 0.0f;
+  cam->up[1] = 1.0f;
+  cam->fovy = 3.14159265358979323846f / 4.0f;
+  cam->near_z = 0.1f;
+  cam->far_z = 100.0f;
+  prm->width = width;
+  prm->height = height;
+  prm->angle = 0.75f;
+  prm->particle_scale = 5.0f;
+  prm->wave_scale = 0.047f;
+  prm->point_size = 8.0f;
+  prm->surface_res = 512;
+  prm->draw_surface = 1;
+  prm->draw_particles = 1;
+  prm->draw_skybox = 0;
+  return CWA_OK;
+}
+
+cwa_status cwa_render_set_skybox(cwa_sim* s, const uint8_t* faces, int32_t face_size) {
+  CWA_TRY(check_sim(s));
+  if (!faces || face_size < 1 || face_size > 8192) return arg_error("face_size must be in [1, 8192]");
+  if (!s->render) s->render = render_state_new();
+  CWA_CUDA(render_set_skybox(s->render, faces, face_size, s->stream));
+  return CWA_OK;
+}
+
+cwa_status cwa_render(cwa_sim* s, int32_t scene, const cwa_camera* cam, const cwa_render_params* prm,
+                      uint8_t* out) {
+  CWA_TRY(check_scene(s, scene));
+  if (!cam || !prm || !out) return arg_error("null camera, params or output");
+  if (prm->width < 1 || prm->height < 1 || (int64_t)prm->width * prm->height > (1ll << 26))
+    return arg_error("image size must be in [1, 2^26] pixels");
+  if (prm->surface_res < 3 || prm->surface_res > 8192) return arg_error("surface_res must be in [3, 8192]");
+  if (!(prm->point_size > 0.0f && prm->point_size <= 256.0f)) return arg_error("point_size must be in (0, 256]");
+  if (!(cam->near_z > 0.0f && cam->far_z > cam->near_z) || !(cam->fovy > 0.0f && cam->fovy < 3.14159f))
+    return arg_error("camera needs 0 < near < far and 0 < fovy < pi");
+  if (!s->render) s->render = render_state_new();
+  const SceneDev& d = s->sd[scene];
+  CWA_CUDA(render_frame(s->render, *cam, *prm, s->P[s->cur] + d.poff, s->ID[s->cur] + d.poff, d.n,
+                        s->U[s->wcur] + d.woff, d.nx, d.nz, out, s->d_status, s->stream, &s->launches));
+  return read_status(s);
 }
 
 cwa_status cwa_step(cwa_sim* s, int32_t n_steps) {

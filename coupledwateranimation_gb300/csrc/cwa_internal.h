@@ -208,6 +208,22 @@ bool wave_block_encode(CUtensorMap* map, float* base, int W, int H);
 void wave_block_tiles(const SceneDev& d, int32_t scene, bool tma, std::vector<WaveBlockTile>* out);
 cudaError_t launch_wave_block(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t stream);
 
+// ---- headless rendering (cwa_render.cu) ----
+struct RenderMatrices {  // row-major 4x4
+  float mvp_p[16], m_p[16], mvp_w[16], m_w[16], inv_p[16], inv_v[16];
+};
+struct RenderState;
+RenderState* render_state_new();
+void render_state_free(RenderState* r);
+cudaError_t render_set_skybox(RenderState* r, const uint8_t* faces, int size, cudaStream_t stream);
+void render_matrices(const cwa_camera& cam, const cwa_render_params& prm, RenderMatrices* m);
+// One frame: particles given in the sim's sorted order with their upload
+// indices (drawn in upload order), the scene's u^n, RGBA8 out to host memory.
+cudaError_t render_frame(RenderState* r, const cwa_camera& cam, const cwa_render_params& prm,
+                         const float4* sorted_pos, const int32_t* sorted_id, int32_t n, const float* wave,
+                         int32_t nx, int32_t nz, uint8_t* host_out, int32_t* status, cudaStream_t stream,
+                         int64_t* launches);
+
 // Host-side thread-local error text.
 void set_error(const std::string& msg);
 

@@ -1,0 +1,761 @@
+// cwa_render.cu — one frame of the reference's display() (Main.cpp:326-474)
+// rendered headless with CUDA kernels instead of GL.
+//
+// Primitives, in the reference's draw order:
+//   * the wave surface: the indexed triangle-strip mesh of Surf.cpp:68-190
+//     (WAVE_RES vertices per side; vertex (a, b) sits at
+//     (int(0.1 a), -1, int(0.1 b)) because START_INDEX * i is passed to int
+//     parameters), displaced to y = 50 * u(tex) by wave_vs.glsl:30-42 and
+//     shaded by wave_fs.glsl:30-88;
+//   * the particles: 8-pixel point sprites (particle_vs.glsl, particle_fs.glsl
+//     pass 0), with the depth image of pass 2 (eye_pos.z of the nearest
+//     sprite) giving screen-space normals.
+//
+// GB300 form: a fragment-list rasteriser built from the same pieces as the
+// grid sort.  Count fragments per pixel (atomics), scan the counts, fill
+// (primitive id, window depth) records, then resolve each pixel by walking
+// its fragments in primitive order with the GL_LESS depth test and
+// SRC_ALPHA / ONE_MINUS_SRC_ALPHA blending into an 8-bit target, so the
+// result follows GL's ordered blending, not just the nearest fragment.
+// Coverage, depths and projections use round-to-nearest intrinsics in a
+// fixed order (the CPU restatement repeats them bit for bit); shading uses
+// the CUDA math library.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "cwa_device.cuh"
+#include "cwa_internal.h"
+
+namespace cwa {
+
+namespace {
+
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fd(float a, float b) { return __fdiv_rn(a, b); }
+
+struct V3 {
+  float x, y, z;
+};
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(float k, V3 a) { return v3(k * a.x, k * a.y, k * a.z); }
+__device__ __forceinline__ V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 normalize(V3 a) { return rsqrtf(dot(a, a)) * a; }
+__device__ __forceinline__ V3 reflect(V3 i, V3 n) { return i - (2.0f * dot(n, i)) * n; }
+__device__ __forceinline__ V3 refract(V3 i, V3 n, float eta) {
+  const float d = dot(n, i);
+  const float k = 1.0f - eta * eta * (1.0f - d * d);
+  if (k < 0.0f) return v3(0.0f, 0.0f, 0.0f);
+  return eta * i - (eta * d + sqrtf(k)) * n;
+}
+
+// Projection with a fixed operation order: clip_r = ((m0 x + m1 y) + m2 z) + m3.
+__device__ __forceinline__ float row4(const float* m, float x, float y, float z) {
+  return fa(fa(fa(fm(m[0], x), fm(m[1], y)), fm(m[2], z)), m[3]);
+}
+
+struct Win {
+  float x, y, z, w;  // window x, y (pixels), window depth in [0, 1], clip w
+  float cz;          // clip z (the depth image's value)
+  bool ok;           // inside the clip volume (points) / in front of the eye
+};
+
+__device__ __forceinline__ Win project(const float* mvp, float x, float y, float z, int W, int H, bool point) {
+  Win o;
+  const float cx = row4(mvp, x, y, z), cy = row4(mvp + 4, x, y, z), cz = row4(mvp + 8, x, y, z),
+              cw = row4(mvp + 12, x, y, z);
+  o.w = cw;
+  o.cz = cz;
+  o.ok = cw > 0.0f && cz >= -cw && cz <= cw;
+  if (point) o.ok = o.ok && cx >= -cw && cx <= cw && cy >= -cw && cy <= cw;
+  const float nx = fd(cx, cw), ny = fd(cy, cw), nz = fd(cz, cw);
+  o.x = fm(fm(fa(nx, 1.0f), 0.5f), (float)W);
+  o.y = fm(fm(fa(ny, 1.0f), 0.5f), (float)H);
+  o.z = fm(fa(nz, 1.0f), 0.5f);
+  return o;
+}
+
+// Sprite pixel range: centres c with wx - S/2 <= c < wx + S/2.
+__device__ __forceinline__ void sprite_range(float c, float half, int n, int* lo, int* hi) {
+  *lo = max((int)ceilf(fs(fs(c, half), 0.5f)), 0);
+  *hi = min((int)ceilf(fs(fa(c, half), 0.5f)) - 1, n - 1);
+}
+
+// Squared sprite radius of pixel centre (px, py) in point-coordinate units.
+__device__ __forceinline__ float sprite_r2(int px, int py, float wx, float wy, float inv_s) {
+  const float dx = fm(fs(fa((float)px, 0.5f), wx), inv_s), dy = fm(fs(fa((float)py, 0.5f), wy), inv_s);
+  return fa(fm(dx, dx), fm(dy, dy));
+}
+
+// ---- the strip mesh ------------------------------------------------------
+// Row i of the strip holds vertices (i, j), (i+1, j) for j < n-1; its
+// triangles are consecutive vertex triples, 2n - 4 per row.
+__device__ __forceinline__ void tri_vertices(int t, int n, int va[3], int vb[3]) {
+  const int per_row = 2 * n - 4;
+  const int i = t / per_row, k0 = t - i * per_row;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const int k = k0 + q;
+    va[q] = i + (k & 1);
+    vb[q] = k >> 1;
+  }
+}
+
+struct MeshVert {
+  float wx, wy, wz, iw;  // window position, depth, 1 / clip w
+  float s, t;            // texture coordinates
+  float px, py, pz;      // world position of the undisplaced vertex (wave_vs pw)
+  int ok;
+};
+
+}  // namespace
+
+struct RenderFrame {
+  float mvp_p[16], m_p[16];  // particles: PV * M and M (row-major)
+  float mvp_w[16], m_w[16];  // wave surface
+  float inv_p[16], inv_v[16];
+  float eye[3];
+  int W, H;
+  float point_size;
+  int res, n_tris, n_particles;
+  int draw_surface, draw_particles, draw_skybox;
+  const float* wave;
+  int nx, nz;
+  const float4* pos;
+  const uint8_t* sky;
+  int sky_size;
+};
+
+namespace {
+
+// ---- cube map (GL cube-map face selection, GL_LINEAR, clamp within face) --
+__device__ V3 cube_texel(const RenderFrame& f, int face, int x, int y) {
+  const uint8_t* p = f.sky + (((size_t)face * f.sky_size + y) * f.sky_size + x) * 4;
+  return v3(p[0] / 255.0f, p[1] / 255.0f, p[2] / 255.0f);
+}
+
+__device__ V3 cube_sample(const RenderFrame& f, V3 r) {
+  if (!f.sky) return v3(0.0f, 0.0f, 0.0f);
+  const float ax = fabsf(r.x), ay = fabsf(r.y), az = fabsf(r.z);
+  int face;
+  float sc, tc, ma;
+  if (ax >= ay && ax >= az) {
+    face = r.x >= 0.0f ? 0 : 1;
+    sc = r.x >= 0.0f ? -r.z : r.z;
+    tc = -r.y;
+    ma = ax;
+  } else if (ay >= az) {
+    face = r.y >= 0.0f ? 2 : 3;
+    sc = r.x;
+    tc = r.y >= 0.0f ? r.z : -r.z;
+    ma = ay;
+  } else {
+    face = r.z >= 0.0f ? 4 : 5;
+    sc = r.z >= 0.0f ? r.x : -r.x;
+    tc = -r.y;
+    ma = az;
+  }
+  if (ma == 0.0f) return cube_texel(f, 0, f.sky_size / 2, f.sky_size / 2);
+  const float s = 0.5f * (sc / ma + 1.0f), t = 0.5f * (tc / ma + 1.0f);
+  const float u = s * f.sky_size - 0.5f, v = t * f.sky_size - 0.5f;
+  const float u0 = floorf(u), v0 = floorf(v);
+  const float au = u - u0, av = v - v0;
+  const int n1 = f.sky_size - 1;
+  const int x0 = min(max((int)u0, 0), n1), x1 = min(max((int)u0 + 1, 0), n1);
+  const int y0 = min(max((int)v0, 0), n1), y1 = min(max((int)v0 + 1, 0), n1);
+  const V3 c00 = cube_texel(f, face, x0, y0), c10 = cube_texel(f, face, x1, y0);
+  const V3 c01 = cube_texel(f, face, x0, y1), c11 = cube_texel(f, face, x1, y1);
+  return (1.0f - av) * ((1.0f - au) * c00 + au * c10) + av * ((1.0f - au) * c01 + au * c11);
+}
+
+__device__ __forceinline__ MeshVert mesh_vertex(const RenderFrame& f, int a, int b) {
+  MeshVert m;
+  const float fx = (float)(int)fm(0.1f, (float)a), fz = (float)(int)fm(0.1f, (float)b);
+  m.s = fd((float)a, (float)(f.res - 1));
+  m.t = fd((float)b, (float)(f.res - 1));
+  const float h = sample_height(f.wave, f.nx, f.nz, m.s, m.t);
+  const Win w = project(f.mvp_w, fx, fm(50.0f, h), fz, f.W, f.H, false);
+  m.wx = w.x;
+  m.wy = w.y;
+  m.wz = w.z;
+  m.iw = fd(1.0f, w.w);
+  m.ok = w.ok;
+  m.px = row4(f.m_w, fx, -1.0f, fz);
+  m.py = row4(f.m_w + 4, fx, -1.0f, fz);
+  m.pz = row4(f.m_w + 8, fx, -1.0f, fz);
+  return m;
+}
+
+__device__ __forceinline__ float edge(float ax, float ay, float bx, float by, float px, float py) {
+  return fs(fm(fs(bx, ax), fs(py, ay)), fm(fs(by, ay), fs(px, ax)));
+}
+
+// Pixel-centre coverage of a CCW-normalised triangle with the top-left rule.
+__device__ __forceinline__ bool top_left(float ax, float ay, float bx, float by) {
+  return (ay == by && bx < ax) || (by < ay);
+}
+
+struct TriSetup {
+  float x[3], y[3];
+  int order[3];  // mesh vertex slot of each CCW-normalised corner
+  float area;
+  int x0, x1, y0, y1;
+  bool ok;
+};
+
+__device__ TriSetup tri_setup(const MeshVert* mv, int t, int W, int H) {
+  TriSetup s;
+  int o[3] = {0, 1, 2};
+  float x[3] = {mv[0].wx, mv[1].wx, mv[2].wx}, y[3] = {mv[0].wy, mv[1].wy, mv[2].wy};
+  float area = edge(x[0], y[0], x[1], y[1], x[2], y[2]);
+  s.ok = mv[0].ok && mv[1].ok && mv[2].ok && area != 0.0f;
+  if (area < 0.0f) {  // make it counter-clockwise: swap corners 1 and 2
+    o[1] = 2;
+    o[2] = 1;
+    area = -area;
+  }
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    s.x[q] = x[o[q]];
+    s.y[q] = y[o[q]];
+    s.order[q] = o[q];
+  }
+  s.area = area;
+  const float minx = fminf(fminf(s.x[0], s.x[1]), s.x[2]), maxx = fmaxf(fmaxf(s.x[0], s.x[1]), s.x[2]);
+  const float miny = fminf(fminf(s.y[0], s.y[1]), s.y[2]), maxy = fmaxf(fmaxf(s.y[0], s.y[1]), s.y[2]);
+  s.x0 = max((int)floorf(minx - 0.5f), 0);
+  s.x1 = min((int)ceilf(maxx - 0.5f), W - 1);
+  s.y0 = max((int)floorf(miny - 0.5f), 0);
+  s.y1 = min((int)ceilf(maxy - 0.5f), H - 1);
+  if (s.x0 > s.x1 || s.y0 > s.y1) s.ok = false;
+  return s;
+}
+
+// Barycentric weights (of the CCW corners) of pixel (px, py), or false.
+__device__ __forceinline__ bool tri_cover(const TriSetup& s, int px, int py, float l[3]) {
+  const float cx = fa((float)px, 0.5f), cy = fa((float)py, 0.5f);
+  const float e0 = edge(s.x[1], s.y[1], s.x[2], s.y[2], cx, cy);
+  const float e1 = edge(s.x[2], s.y[2], s.x[0], s.y[0], cx, cy);
+  const float e2 = edge(s.x[0], s.y[0], s.x[1], s.y[1], cx, cy);
+  const bool in0 = e0 > 0.0f || (e0 == 0.0f && top_left(s.x[1], s.y[1], s.x[2], s.y[2]));
+  const bool in1 = e1 > 0.0f || (e1 == 0.0f && top_left(s.x[2], s.y[2], s.x[0], s.y[0]));
+  const bool in2 = e2 > 0.0f || (e2 == 0.0f && top_left(s.x[0], s.y[0], s.x[1], s.y[1]));
+  if (!(in0 && in1 && in2)) return false;
+  l[0] = fd(e0, s.area);
+  l[1] = fd(e1, s.area);
+  l[2] = fd(e2, s.area);
+  return true;
+}
+
+__device__ __forceinline__ void load_tri(const RenderFrame& f, const MeshVert* verts, int t, MeshVert mv[3]) {
+  int va[3], vb[3];
+  tri_vertices(t, f.res, va, vb);
+#pragma unroll
+  for (int q = 0; q < 3; ++q) mv[q] = verts[(size_t)va[q] * f.res + vb[q]];
+}
+
+// ---- kernels --------------------------------------------------------------
+// The sim keeps particles cell-sorted; the reference draws its SSBO in
+// upload order, which is what the blending order follows.
+__global__ void k_upload_order(const float4* __restrict__ sorted, const int32_t* __restrict__ id, int n,
+                               float4* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) out[id[k]] = sorted[k];
+}
+
+__global__ void k_mesh_vertices(RenderFrame f, MeshVert* __restrict__ verts) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= f.res * f.res) return;
+  verts[v] = mesh_vertex(f, v / f.res, v % f.res);
+}
+
+// Counts (fill == nullptr) or writes (prim, depth) fragment records.
+__global__ void k_raster(RenderFrame f, const MeshVert* __restrict__ verts, int32_t* __restrict__ cnt,
+                         const int32_t* __restrict__ off, uint2* __restrict__ frags) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n_tri = f.draw_surface ? f.n_tris : 0;
+  const int n_par = f.draw_particles ? f.n_particles : 0;
+  if (p >= n_tri + n_par) return;
+  if (p < n_tri) {
+    MeshVert mv[3];
+    load_tri(f, verts, p, mv);
+    const TriSetup s = tri_setup(mv, p, f.W, f.H);
+    if (!s.ok) return;
+    for (int py = s.y0; py <= s.y1; ++py)
+      for (int px = s.x0; px <= s.x1; ++px) {
+        float l[3];
+        if (!tri_cover(s, px, py, l)) continue;
+        const int pix = py * f.W + px;
+        const int slot = atomicAdd(cnt + pix, 1);
+        if (frags) {
+          const float z = fa(fa(fm(l[0], mv[s.order[0]].wz), fm(l[1], mv[s.order[1]].wz)),
+                             fm(l[2], mv[s.order[2]].wz));
+          frags[off[pix] + slot] = make_uint2((uint32_t)p, __float_as_uint(z));
+        }
+      }
+  } else {
+    const int i = p - n_tri;
+    const float4 q = f.pos[i];
+    const Win w = project(f.mvp_p, q.x, q.y, q.z, f.W, f.H, true);
+    if (!w.ok) return;
+    const float half = 0.5f * f.point_size, inv_s = fd(1.0f, f.point_size);
+    int x0, x1, y0, y1;
+    sprite_range(w.x, half, f.W, &x0, &x1);
+    sprite_range(w.y, half, f.H, &y0, &y1);
+    for (int py = y0; py <= y1; ++py)
+      for (int px = x0; px <= x1; ++px) {
+        if (!(sprite_r2(px, py, w.x, w.y, inv_s) < 0.25f)) continue;  // r >= 0.5 is discarded
+        const int pix = py * f.W + px;
+        const int slot = atomicAdd(cnt + pix, 1);
+        if (frags) frags[off[pix] + slot] = make_uint2((uint32_t)p, __float_as_uint(w.z));
+      }
+  }
+}
+
+// Sort each pixel's fragments into draw order; the depth image of pass 2:
+// eye_pos.z of the particle fragment that wins GL_LESS (0 where none).
+__global__ void k_resolve_depth(RenderFrame f, const int32_t* __restrict__ off, uint2* __restrict__ frags,
+                                float* __restrict__ depth_img) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= f.W * f.H) return;
+  const int b = off[pix], e = off[pix + 1];
+  for (int k = b + 1; k < e; ++k) {  // insertion sort by primitive id (ids are unique per pixel)
+    const uint2 x = frags[k];
+    int m = k - 1;
+    while (m >= b && frags[m].x > x.x) {
+      frags[m + 1] = frags[m];
+      --m;
+    }
+    frags[m + 1] = x;
+  }
+  const uint32_t first_particle = f.draw_surface ? (uint32_t)f.n_tris : 0u;
+  float best = 1.0f;
+  int win = -1;
+  for (int k = b; k < e; ++k) {
+    const uint2 x = frags[k];
+    if (x.x < first_particle) continue;
+    const float z = __uint_as_float(x.y);
+    if (z < best) {
+      best = z;
+      win = (int)(x.x - first_particle);
+    }
+  }
+  float d = 0.0f;
+  if (win >= 0) {
+    const float4 q = f.pos[win];
+    d = project(f.mvp_p, q.x, q.y, q.z, f.W, f.H, true).cz;
+  }
+  depth_img[pix] = d;
+}
+
+__device__ __forceinline__ float depth_at(const RenderFrame& f, const float* d, int x, int y) {
+  return (x < 0 || y < 0 || x >= f.W || y >= f.H) ? 0.0f : d[y * f.W + x];
+}
+
+__device__ __forceinline__ float mixf(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+
+__device__ __forceinline__ V3 mat3x(const float* m, V3 v, float w) {
+  return v3(m[0] * v.x + m[1] * v.y + m[2] * v.z + m[3] * w, m[4] * v.x + m[5] * v.y + m[6] * v.z + m[7] * w,
+            m[8] * v.x + m[9] * v.y + m[10] * v.z + m[11] * w);
+}
+
+// wave_fs.glsl:30-88 for the fragment of triangle t at pixel (px, py).
+__device__ void shade_surface(const RenderFrame& f, const MeshVert* verts, int t, int px, int py, V3* rgb,
+                              float* alpha) {
+  MeshVert mv[3];
+  load_tri(f, verts, t, mv);
+  const TriSetup s = tri_setup(mv, t, f.W, f.H);
+  float l[3];
+  tri_cover(s, px, py, l);
+  // perspective-correct varyings
+  float q[3], sum = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    q[k] = l[k] * mv[s.order[k]].iw;
+    sum += q[k];
+  }
+  float ts = 0.0f, tt = 0.0f;
+  V3 pw = v3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const MeshVert& m = mv[s.order[k]];
+    const float wgt = q[k] / sum;
+    ts += wgt * m.s;
+    tt += wgt * m.t;
+    pw = pw + wgt * v3(m.px, m.py, m.pz);
+  }
+  const float v = sample_height(f.wave, f.nx, f.nz, ts, tt);
+  const V3 eye = v3(f.eye[0], f.eye[1], f.eye[2]);
+  const V3 n = v3(0.0f, 1.0f, 0.0f);  // -normal_attrib of the flat strip mesh, normalised
+  const V3 i = normalize(pw - eye);
+  const V3 refl = cube_sample(f, reflect(i, n));
+  const V3 refr = cube_sample(f, refract(i, n, 1.0f / 1.33f));
+  const V3 light_col = v3(1.0f, 0.85f, 0.7f);
+  const V3 light_dir = normalize(v3(0.0f, 1.0f, 0.0f) - pw);
+  const float diff = fmaxf(dot(n, light_dir), 0.0f);
+  const V3 view_dir = normalize(eye - pw);
+  const V3 rdir = reflect(v3(-light_dir.x, -light_dir.y, -light_dir.z), n);
+  const float spec = powf(fmaxf(dot(view_dir, rdir), 0.0f), 32.0f);
+  const V3 lit = (0.8f * light_col + diff * light_col + (10.0f * spec) * light_col) * v3(0.6f, 0.8f, 1.0f);
+  const V3 combine = 0.75f * (refl + refr) + 0.1f * lit;
+  *rgb = v3(mixf(combine.x, 0.7f, v), mixf(combine.y, 0.9f, v), mixf(combine.z, 1.0f, v));
+  *alpha = mixf(0.2f, 0.0f, v);
+}
+
+// particle_fs.glsl pass 0 for particle i at pixel (px, py).
+__device__ void shade_particle(const RenderFrame& f, const float* dimg, int i, int px, int py, V3* rgb,
+                               float* alpha) {
+  const float4 q = f.pos[i];
+  const Win w = project(f.mvp_p, q.x, q.y, q.z, f.W, f.H, true);
+  const float r = sqrtf(sprite_r2(px, py, w.x, w.y, fd(1.0f, f.point_size)));
+  const V3 pp = v3(row4(f.m_p, q.x, q.y, q.z), row4(f.m_p + 4, q.x, q.y, q.z), row4(f.m_p + 8, q.x, q.y, q.z));
+  const V3 eye = v3(f.eye[0], f.eye[1], f.eye[2]);
+  const float spec = powf(fmaxf(dot(normalize(pp), normalize(v3(1.0f, 1.0f, 0.0f))), 0.0f), 16.0f);
+  const float a = expf(-12.0f * r) + 0.1f * expf(-2.0f * r);
+  // GetNormalFromDepth
+  const float dzdx = 0.5f * (depth_at(f, dimg, px + 1, py) - depth_at(f, dimg, px - 1, py));
+  const float dzdy = 0.5f * (depth_at(f, dimg, px, py + 1) - depth_at(f, dimg, px, py - 1));
+  const V3 n = normalize(v3(-dzdx, -dzdy, 1.0f));
+  const V3 iv = normalize(eye - pp);
+  const V3 refl = cube_sample(f, reflect(iv, n));
+  const V3 refr = cube_sample(f, refract(iv, n, 1.0f / 1.33f));
+  // lighting() with WorldPosFromDepth (gl_FragCoord * 2 - 1, as the shader writes it)
+  const float dz = depth_at(f, dimg, px, py);
+  const float cx = (px + 0.5f) * 2.0f - 1.0f, cy = (py + 0.5f) * 2.0f - 1.0f, cz = dz * 2.0f - 1.0f;
+  float vw = f.inv_p[12] * cx + f.inv_p[13] * cy + f.inv_p[14] * cz + f.inv_p[15];
+  V3 view = mat3x(f.inv_p, v3(cx, cy, cz), 1.0f);
+  view = (1.0f / vw) * view;
+  const V3 pos = mat3x(f.inv_v, view, 1.0f);
+  const V3 light_col = v3(1.0f, 0.85f, 0.7f);
+  const V3 light_dir = normalize(v3(1.0f, 1.0f, 0.0f) - pos);
+  const float diff = fmaxf(dot(n, light_dir), 0.0f);
+  const V3 view_dir = normalize(eye - pos);
+  const V3 rdir = reflect(v3(-light_dir.x, -light_dir.y, -light_dir.z), n);
+  const float spec2 = powf(fmaxf(dot(view_dir, rdir), 0.0f), 32.0f);
+  const V3 lit = (0.8f * light_col + diff * light_col + (0.9f * spec2) * light_col) * v3(0.4f, 0.7f, 1.0f);
+  const V3 combine = 0.75f * (refl + refr) + 0.1f * lit;
+  const float t = 2.0f * pp.y;
+  *rgb = v3(mixf(combine.x, 1.0f, t) + spec, mixf(combine.y, 1.0f, t) + spec, mixf(combine.z, 1.0f, t) + spec);
+  *alpha = mixf(0.1f, a, t);
+}
+
+__device__ __forceinline__ float unorm8(float x) { return floorf(fminf(fmaxf(x, 0.0f), 1.0f) * 255.0f + 0.5f); }
+
+__global__ void k_resolve_color(RenderFrame f, const MeshVert* __restrict__ verts, const int32_t* __restrict__ off,
+                                const uint2* __restrict__ frags, const float* __restrict__ dimg,
+                                uint8_t* __restrict__ out) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= f.W * f.H) return;
+  const int px = pix % f.W, py = pix / f.W;
+  // the colour target holds 8-bit values between blends
+  float c[3] = {0.0f, 0.0f, 0.0f};
+  if (f.draw_skybox) {
+    // view ray through the pixel centre: inverse(V) * inverse(P) * ndc
+    const float nx = (px + 0.5f) / f.W * 2.0f - 1.0f, ny = (py + 0.5f) / f.H * 2.0f - 1.0f;
+    const float vw = f.inv_p[12] * nx + f.inv_p[13] * ny + f.inv_p[14] + f.inv_p[15];
+    V3 view = mat3x(f.inv_p, v3(nx, ny, 1.0f), 1.0f);
+    view = (1.0f / vw) * view;
+    const V3 dir = mat3x(f.inv_v, view, 0.0f);
+    const V3 sky = cube_sample(f, dir);
+    c[0] = unorm8(sky.x);
+    c[1] = unorm8(sky.y);
+    c[2] = unorm8(sky.z);
+  }
+  float depth = 1.0f;
+  const uint32_t first_particle = f.draw_surface ? (uint32_t)f.n_tris : 0u;
+  for (int k = off[pix]; k < off[pix + 1]; ++k) {
+    const uint2 x = frags[k];
+    const float z = __uint_as_float(x.y);
+    if (!(z < depth)) continue;  // GL_LESS, depth writes on
+    depth = z;
+    V3 rgb;
+    float a;
+    if (x.x < first_particle)
+      shade_surface(f, verts, (int)x.x, px, py, &rgb, &a);
+    else
+      shade_particle(f, dimg, (int)(x.x - first_particle), px, py, &rgb, &a);
+    a = fminf(fmaxf(a, 0.0f), 1.0f);
+    const float src[3] = {rgb.x, rgb.y, rgb.z};
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      const float s = fminf(fmaxf(src[ch], 0.0f), 1.0f);
+      c[ch] = unorm8(s * a + (c[ch] / 255.0f) * (1.0f - a));
+    }
+  }
+  uint8_t* o = out + (size_t)pix * 4;
+  o[0] = (uint8_t)c[0];
+  o[1] = (uint8_t)c[1];
+  o[2] = (uint8_t)c[2];
+  o[3] = 255;
+}
+
+}  // namespace
+
+// ---- host side --------------------------------------------------------------
+
+struct RenderState {
+  uint8_t* sky = nullptr;
+  int sky_size = 0;
+};
+
+RenderState* render_state_new() { return new RenderState(); }
+
+void render_state_free(RenderState* r) {
+  if (!r) return;
+  if (r->sky) cudaFree(r->sky);
+  delete r;
+}
+
+cudaError_t render_set_skybox(RenderState* r, const uint8_t* faces, int size, cudaStream_t stream) {
+  if (r->sky) {
+    cudaFree(r->sky);
+    r->sky = nullptr;
+    r->sky_size = 0;
+  }
+  const size_t bytes = (size_t)6 * size * size * 4;
+  cudaError_t e = cudaMalloc((void**)&r->sky, bytes);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(r->sky, faces, bytes, cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e == cudaSuccess) r->sky_size = size;
+  return e;
+}
+
+// glm's float formulas (lookAt, perspective, rotate, scale, mat4 product),
+// column-major as glm stores them, in glm's operation order.
+namespace {
+struct F3 {
+  float x, y, z;
+};
+F3 f3sub(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+float f3dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+F3 f3norm(F3 v) {
+  const float inv = 1.0f / sqrtf(f3dot(v, v));
+  return F3{v.x * inv, v.y * inv, v.z * inv};
+}
+F3 f3cross(F3 a, F3 b) { return F3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+
+struct M4 {
+  float c[4][4];  // c[column][row]
+};
+M4 m4_zero() {
+  M4 m;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) m.c[i][j] = 0.0f;
+  return m;
+}
+M4 m4_identity() {
+  M4 m = m4_zero();
+  for (int i = 0; i < 4; ++i) m.c[i][i] = 1.0f;
+  return m;
+}
+M4 m4_mul(const M4& a, const M4& b) {
+  M4 r;
+  for (int j = 0; j < 4; ++j)
+    for (int row = 0; row < 4; ++row)
+      r.c[j][row] = ((a.c[0][row] * b.c[j][0] + a.c[1][row] * b.c[j][1]) + a.c[2][row] * b.c[j][2]) +
+                    a.c[3][row] * b.c[j][3];
+  return r;
+}
+M4 look_at(F3 eye, F3 center, F3 up) {
+  const F3 f = f3norm(f3sub(center, eye));
+  const F3 s = f3norm(f3cross(f, up));
+  const F3 u = f3cross(s, f);
+  M4 r = m4_identity();
+  r.c[0][0] = s.x;
+  r.c[1][0] = s.y;
+  r.c[2][0] = s.z;
+  r.c[0][1] = u.x;
+  r.c[1][1] = u.y;
+  r.c[2][1] = u.z;
+  r.c[0][2] = -f.x;
+  r.c[1][2] = -f.y;
+  r.c[2][2] = -f.z;
+  r.c[3][0] = -f3dot(s, eye);
+  r.c[3][1] = -f3dot(u, eye);
+  r.c[3][2] = f3dot(f, eye);
+  return r;
+}
+M4 perspective(float fovy, float aspect, float zn, float zf) {
+  const float th = tanf(fovy / 2.0f);
+  M4 r = m4_zero();
+  r.c[0][0] = 1.0f / (aspect * th);
+  r.c[1][1] = 1.0f / th;
+  r.c[2][2] = -(zf + zn) / (zf - zn);
+  r.c[2][3] = -1.0f;
+  r.c[3][2] = -(2.0f * zf * zn) / (zf - zn);
+  return r;
+}
+// rotate(angle, (0, 1, 0)) * scale(vec3(k)), expanded as glm evaluates it
+M4 rot_y_scale(float angle, float k) {
+  const float c = cosf(angle), s = sinf(angle);
+  M4 rot = m4_identity();
+  rot.c[0][0] = c;
+  rot.c[0][2] = -s;
+  rot.c[1][1] = c + (1.0f - c);
+  rot.c[2][0] = s;
+  rot.c[2][2] = c;
+  M4 sc = m4_identity();
+  sc.c[0][0] = sc.c[1][1] = sc.c[2][2] = k;
+  return m4_mul(rot, sc);
+}
+void to_rows(const M4& m, float* out) {
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) out[r * 4 + c] = m.c[c][r];
+}
+// General inverse (Gauss-Jordan in double), rows out.
+void inverse_rows(const M4& m, float* out) {
+  double a[4][8];
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      a[r][c] = m.c[c][r];
+      a[r][4 + c] = r == c ? 1.0 : 0.0;
+    }
+  for (int col = 0; col < 4; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < 4; ++r)
+      if (fabs(a[r][col]) > fabs(a[piv][col])) piv = r;
+    for (int c = 0; c < 8; ++c) {
+      const double t = a[col][c];
+      a[col][c] = a[piv][c];
+      a[piv][c] = t;
+    }
+    const double d = a[col][col];
+    for (int c = 0; c < 8; ++c) a[col][c] /= d;
+    for (int r = 0; r < 4; ++r)
+      if (r != col) {
+        const double k = a[r][col];
+        for (int c = 0; c < 8; ++c) a[r][c] -= k * a[col][c];
+      }
+  }
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) out[r * 4 + c] = (float)a[r][4 + c];
+}
+}  // namespace
+
+void render_matrices(const cwa_camera& cam, const cwa_render_params& prm, RenderMatrices* m) {
+  const F3 eye{cam.eye[0], cam.eye[1], cam.eye[2]}, ctr{cam.center[0], cam.center[1], cam.center[2]},
+      up{cam.up[0], cam.up[1], cam.up[2]};
+  const M4 V = look_at(eye, ctr, up);
+  const M4 P = perspective(cam.fovy, (float)prm.width / (float)prm.height, cam.near_z, cam.far_z);
+  const M4 PV = m4_mul(P, V);
+  const M4 Mp = rot_y_scale(prm.angle, prm.particle_scale);
+  const M4 Mw = rot_y_scale(prm.angle, prm.wave_scale);
+  to_rows(m4_mul(PV, Mp), m->mvp_p);
+  to_rows(Mp, m->m_p);
+  to_rows(m4_mul(PV, Mw), m->mvp_w);
+  to_rows(Mw, m->m_w);
+  inverse_rows(P, m->inv_p);
+  inverse_rows(V, m->inv_v);
+}
+
+cudaError_t render_frame(RenderState* r, const cwa_camera& cam, const cwa_render_params& prm,
+                         const float4* sorted_pos, const int32_t* sorted_id, int32_t n, const float* wave,
+                         int32_t nx, int32_t nz, uint8_t* host_out, int32_t* status, cudaStream_t stream,
+                         int64_t* launches) {
+  RenderMatrices mats;
+  render_matrices(cam, prm, &mats);
+  RenderFrame f{};
+  for (int k = 0; k < 16; ++k) {
+    f.mvp_p[k] = mats.mvp_p[k];
+    f.m_p[k] = mats.m_p[k];
+    f.mvp_w[k] = mats.mvp_w[k];
+    f.m_w[k] = mats.m_w[k];
+    f.inv_p[k] = mats.inv_p[k];
+    f.inv_v[k] = mats.inv_v[k];
+  }
+  for (int k = 0; k < 3; ++k) f.eye[k] = cam.eye[k];
+  f.W = prm.width;
+  f.H = prm.height;
+  f.point_size = prm.point_size;
+  f.res = prm.surface_res;
+  f.n_tris = (prm.surface_res - 1) * (2 * prm.surface_res - 4);
+  f.n_particles = n;
+  f.draw_surface = prm.draw_surface != 0;
+  f.draw_particles = prm.draw_particles != 0;
+  f.draw_skybox = prm.draw_skybox != 0 && r->sky != nullptr;
+  f.wave = wave;
+  f.nx = nx;
+  f.nz = nz;
+  f.pos = nullptr;
+  f.sky = r->sky;
+  f.sky_size = r->sky_size;
+
+  const int npix = f.W * f.H;
+  const int nprim = (f.draw_surface ? f.n_tris : 0) + (f.draw_particles ? n : 0);
+  MeshVert* verts = nullptr;
+  float4* upos = nullptr;
+  int32_t *cnt = nullptr, *off = nullptr;
+  uint2* frags = nullptr;
+  float* dimg = nullptr;
+  uint8_t* img = nullptr;
+  void* ws = nullptr;
+  cudaError_t e = cudaSuccess;
+  auto fail = [&](cudaError_t err) {
+    cudaStreamSynchronize(stream);
+    cudaFree(upos);
+    cudaFree(verts);
+    cudaFree(cnt);
+    cudaFree(off);
+    cudaFree(frags);
+    cudaFree(dimg);
+    cudaFree(img);
+    cudaFree(ws);
+    return err;
+  };
+  const size_t nverts = (size_t)f.res * f.res;
+  if ((e = cudaMalloc((void**)&verts, sizeof(MeshVert) * (nverts ? nverts : 1))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc((void**)&cnt, sizeof(int32_t) * npix)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc((void**)&off, sizeof(int32_t) * (npix + 1))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc((void**)&dimg, sizeof(float) * npix)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc((void**)&img, (size_t)npix * 4)) != cudaSuccess) return fail(e);
+  const size_t ws_bytes = scan_workspace_bytes(npix + 1);
+  if ((e = cudaMalloc(&ws, ws_bytes)) != cudaSuccess) return fail(e);
+  ScanWorkspace sw;
+  scan_bind_workspace(ws, npix + 1, &sw);
+  if ((e = cudaMalloc((void**)&upos, sizeof(float4) * (n > 0 ? n : 1))) != cudaSuccess) return fail(e);
+  if (n > 0) {
+    k_upload_order<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(sorted_pos, sorted_id, n, upos);
+    *launches += 1;
+  }
+  f.pos = upos;
+  if ((e = cudaMemsetAsync(cnt, 0, sizeof(int32_t) * npix, stream)) != cudaSuccess) return fail(e);
+  if (f.draw_surface && nverts) {
+    k_mesh_vertices<<<(unsigned)((nverts + 255) / 256), 256, 0, stream>>>(f, verts);
+    *launches += 1;
+  }
+  const unsigned pblocks = (unsigned)((nprim + 127) / 128);
+  if (nprim > 0) {
+    k_raster<<<pblocks, 128, 0, stream>>>(f, verts, cnt, nullptr, nullptr);
+    *launches += 1;
+  }
+  if ((e = scan_launch(cnt, off, npix, npix + 1, true, sw, status, stream, launches, nullptr)) != cudaSuccess)
+    return fail(e);
+  int32_t total = 0;
+  if ((e = cudaMemcpyAsync(&total, off + npix, sizeof(int32_t), cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
+    return fail(e);
+  if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return fail(e);
+  if (total < 0) return fail(cudaErrorInvalidValue);  // more than 2^31 fragments
+  if ((e = cudaMalloc((void**)&frags, sizeof(uint2) * (total > 0 ? total : 1))) != cudaSuccess) return fail(e);
+  if (nprim > 0) {  // the scan cleared cnt: it now counts each pixel's filled slots
+    k_raster<<<pblocks, 128, 0, stream>>>(f, verts, cnt, off, frags);
+    *launches += 1;
+  }
+  const unsigned xblocks = (unsigned)((npix + 255) / 256);
+  k_resolve_depth<<<xblocks, 256, 0, stream>>>(f, off, frags, dimg);
+  k_resolve_color<<<xblocks, 256, 0, stream>>>(f, verts, off, frags, dimg, img);
+  *launches += 2;
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+  if ((e = cudaMemcpyAsync(host_out, img, (size_t)npix * 4, cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
+    return fail(e);
+  return fail(cudaStreamSynchronize(stream));
+}
+
+}  // namespace cwa

@@ -26,6 +26,13 @@ class GridArrays:
     sorted_id: np.ndarray   # upload index of each sorted particle
 
 
+def render_defaults(width: int, height: int):
+    """(Camera, RenderParams) of the reference's startup view."""
+    cam, prm = _abi.Camera(), _abi.RenderParams()
+    check(_abi.load().cwa_render_defaults(width, height, C.byref(cam), C.byref(prm)), "cwa_render_defaults")
+    return cam, prm
+
+
 class Sim:
     """One or more independent scenes stepped together on one GPU."""
 
@@ -122,6 +129,32 @@ class Sim:
             raise ValueError("expected an (h, w, 4) RGBA8 image")
         check(self._lib.cwa_wave_init_from_image(self._h, scene, img.ctypes.data, img.shape[1], img.shape[0]),
               "cwa_wave_init_from_image")
+
+    def set_skybox(self, faces: np.ndarray) -> None:
+        """Environment cube map: (6, S, S, 4) uint8 faces +x, -x, +y, -y, +z, -z,
+        rows top-down as stored in the image files."""
+        f = np.ascontiguousarray(faces, dtype=np.uint8)
+        if f.ndim != 4 or f.shape[0] != 6 or f.shape[1] != f.shape[2] or f.shape[3] != 4:
+            raise ValueError("expected (6, S, S, 4) RGBA8 faces")
+        check(self._lib.cwa_render_set_skybox(self._h, f.ctypes.data, f.shape[1]), "cwa_render_set_skybox")
+
+    def render(self, scene: int = 0, width: int = 640, height: int = 360, camera=None, params=None,
+               **overrides) -> np.ndarray:
+        """One headless frame as an (height, width, 4) uint8 image, row 0 at the
+        bottom (glReadPixels order).  `camera` / `params` default to the
+        reference's startup view; keyword overrides set RenderParams fields
+        (angle, particle_scale, wave_scale, point_size, surface_res,
+        draw_surface, draw_particles, draw_skybox)."""
+        cam, prm = render_defaults(width, height)
+        if camera is not None:
+            cam = camera
+        if params is not None:
+            prm = params
+        for k, v in overrides.items():
+            setattr(prm, k, v)
+        out = np.zeros((prm.height, prm.width, 4), np.uint8)
+        check(self._lib.cwa_render(self._h, scene, C.byref(cam), C.byref(prm), out.ctypes.data), "cwa_render")
+        return out
 
     def wave_advance(self, n: int) -> None:
         """n wave passes with no particle passes between them (4 per launch)."""

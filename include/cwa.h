@@ -321,6 +321,53 @@ cwa_status cwa_grid_build(const float* d_pos4, int32_t n, const float lo[3], flo
                           int32_t* d_cell_of, void* d_workspace, size_t workspace_bytes,
                           void* stream);
 
+/* ---- headless rendering (the reference's display(), Main.cpp:326-474) ----
+ * One frame of the wave surface and the particles into an RGBA8 image, no
+ * GL: skybox / surface (wave_vs.glsl, wave_fs.glsl over the strip mesh of
+ * Surf.cpp) / particle sprites (particle_vs.glsl, particle_fs.glsl passes 0
+ * and 2) with the depth test and SRC_ALPHA / ONE_MINUS_SRC_ALPHA blending
+ * into an 8-bit colour target, fragments blended in draw order per pixel. */
+typedef struct cwa_camera {
+  float eye[3];     /* eye_persp, Main.cpp:138 */
+  float center[3];  /* center_persp, Main.cpp:139 */
+  float up[3];
+  float fovy;       /* radians (glm::perspective, Main.cpp:348) */
+  float near_z, far_z;
+} cwa_camera;
+
+typedef struct cwa_render_params {
+  int32_t width, height;
+  float angle;           /* model rotation about y (Main.cpp:153) */
+  float particle_scale;  /* Main.cpp:154 */
+  float wave_scale;      /* Main.cpp:155 */
+  float point_size;      /* sprite edge in pixels (glPointSize, Main.cpp:913) */
+  int32_t surface_res;   /* strip mesh vertices per side (WAVE_RES, Main.cpp:29) */
+  int32_t draw_surface;  /* drawSurface, Main.cpp:162 */
+  int32_t draw_particles;/* drawParticles, Main.cpp:163 */
+  int32_t draw_skybox;   /* 1: the cube map behind everything (see cwa_render) */
+  int32_t reserved[4];
+} cwa_render_params;
+
+/* The reference's startup view (Main.cpp:138-165, 913): eye (7, 4, 0),
+ * centre (0, -1, 0), 45-degree field of view, near 0.1, far 100, angle 0.75,
+ * particle scale 5, wave scale 0.047, 8-pixel sprites, a 512-vertex strip
+ * mesh, surface and particles drawn, skybox behind off. */
+cwa_status cwa_render_defaults(int32_t width, int32_t height, cwa_camera* camera, cwa_render_params* params);
+/* The environment cube map (LoadCubemap, LoadTexture.cpp:35-67): six
+ * face_size x face_size RGBA8 faces in the order +x, -x, +y, -y, +z, -z,
+ * rows top-down as stored in the image files.  Without one, cube-map
+ * lookups read (0, 0, 0, 1). */
+cwa_status cwa_render_set_skybox(cwa_sim* sim, const uint8_t* faces_rgba, int32_t face_size);
+/* Render one frame of `scene` into host memory (width * height * 4 bytes,
+ * row 0 = the bottom row, as glReadPixels returns it).  Departures, by
+ * design: particle normals come from this frame's depth image (the
+ * reference reads last frame's); the skybox, drawn at depth 1.0 and
+ * rejected by the default GL_LESS test against the cleared depth, appears
+ * only with draw_skybox = 1; triangles with a vertex outside the near/far
+ * planes or behind the eye are dropped instead of clipped.  Synchronous. */
+cwa_status cwa_render(cwa_sim* sim, int32_t scene, const cwa_camera* camera, const cwa_render_params* params,
+                      uint8_t* out_rgba);
+
 #ifdef __cplusplus
 }
 #endif

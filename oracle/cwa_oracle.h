@@ -90,6 +90,11 @@ void orc_wave_init_f32(const cwa_scene_desc* sc, float* u);
  * RGBA8 image, 0 past the image. */
 void orc_wave_from_image_f32(int32_t nx, int32_t nz, const uint8_t* rgba, int32_t w, int32_t h, float* u);
 float orc_sample_f32(const float* u, int32_t w, int32_t h, float s, float t);
+/* One headless frame of display() (cwa_render_oracle.cpp): pos4 = n float4
+ * particle positions in upload (draw) order, u^n of the scene, optional cube
+ * map (6 faces of sky_size^2 RGBA8, or NULL), out = width*height RGBA8. */
+void orc_render(const float* pos4, int32_t n, const float* wave, int32_t nx, int32_t nz, const cwa_camera* cam,
+                const cwa_render_params* prm, const uint8_t* sky, int32_t sky_size, uint8_t* out);
 
 #ifdef __cplusplus
 }

@@ -58,6 +58,7 @@ def load() -> C.CDLL:
             "orc_wave_init_f32": (None, [_P, _P]),
             "orc_wave_from_image_f32": (None, [C.c_int32, C.c_int32, _P, C.c_int32, C.c_int32, _P]),
             "orc_sample_f32": (C.c_float, [_P, _I, _I, C.c_float, C.c_float]),
+            "orc_render": (None, [_P, _I, _P, _I, _I, _P, _P, _P, _I, _P]),
         }
         for name, (res, args) in protos.items():
             fn = getattr(lib, name)
@@ -233,3 +234,16 @@ def sample_f32(u, s, t) -> float:
 
 def omp_threads_env() -> int:
     return int(os.environ.get("OMP_NUM_THREADS", "0") or 0)
+
+
+def render(pos4: np.ndarray, wave: np.ndarray, camera, params, sky: np.ndarray | None = None) -> np.ndarray:
+    """One frame (height, width, 4) uint8, row 0 at the bottom.  pos4: (n, 4)
+    float32 positions in upload order; wave: (nz, nx) u^n; camera / params:
+    the ABI's cwa_camera / cwa_render_params ctypes structures; sky: (6, S, S, 4)."""
+    p = np.ascontiguousarray(pos4, np.float32)
+    u = np.ascontiguousarray(wave, np.float32)
+    out = np.zeros((params.height, params.width, 4), np.uint8)
+    sk = None if sky is None else np.ascontiguousarray(sky, np.uint8)
+    load().orc_render(_p(p), p.shape[0], _p(u), u.shape[1], u.shape[0], C.cast(C.pointer(camera), C.c_void_p),
+                      C.cast(C.pointer(params), C.c_void_p), _p(sk), 0 if sk is None else sk.shape[1], _p(out))
+    return out
