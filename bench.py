@@ -466,6 +466,47 @@ def run_render(args) -> None:
                       "lit_pixels": int((img[..., :3] != 0).any(axis=2).sum())}), flush=True)
 
 
+def run_sph2d(args) -> None:
+    """`--mode sph2d`: the 2D solver family (SphWave2D's scene: 4096 particles,
+    32 x 32 grid, 128 wave cells), frames per second on the GPU (CUDA-graph
+    frames, host clock around a synchronised batch) and of the CPU
+    restatement on the host cores (the same passes, bounded sample)."""
+    import torch  # noqa: F401 (CUDA context first, as the other modes)
+
+    from coupledwateranimation_gb300 import _abi
+    from coupledwateranimation_gb300.sim2d import Sim2D, defaults2d
+    p = defaults2d()
+    frames = max(10, args.steps)
+    with Sim2D(p) as sim:
+        sim.splash()
+        sim.step(max(3, args.warmup))
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.step(frames)
+        sim.synchronize()
+        gpu_s = (time.perf_counter() - t0) / frames
+        parts = sim.download_particles()
+        wave = sim.download_wave()
+    out = {"mode": "sph2d", "particles": p.n_particles, "wave_cells": p.wave_cells,
+           "sph_substeps": p.sph_substeps, "frames": frames, "gpu_ms_per_frame": gpu_s * 1e3,
+           "gpu_frames_per_s": 1.0 / gpu_s, "gpu_particle_substeps_per_s": p.n_particles * p.sph_substeps / gpu_s}
+    if not args.no_cpu:
+        from oracle import oracle as orc
+        cpu_frames, t0 = 0, time.perf_counter()
+        while cpu_frames < 3 or time.perf_counter() - t0 < 5.0:
+            for _ in range(p.sph_substeps):
+                parts = orc.force_2d(p, orc.density_2d(p, parts, wave), wave)
+            a = orc.wave_iter_2d_f32(p, wave, 0)
+            wave = orc.wave_iter_2d_f32(p, a, 1, out_prev=wave)
+            cpu_frames += 1
+        cpu_s = (time.perf_counter() - t0) / cpu_frames
+        out["cpu_baseline"] = {"ms_per_frame": cpu_s * 1e3, "cores": orc.threads(), "kind": "port",
+                               "sample": f"{cpu_frames} frames of the FP64/float32 restatement (oracle/)"}
+        out["gpu_vs_cpu"] = cpu_s / gpu_s
+    assert _abi.PARTICLE2D_DTYPE.itemsize == 48
+    print(json.dumps(out), flush=True)
+
+
 def run_wave(args) -> None:
     """The wave module stepped alone (no particle passes) on an nx x nz field:
     `--steps` single wave passes against cwa_wave_advance over the same
@@ -511,7 +552,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "wave", "batched", "render"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "wave", "batched", "render", "sph2d"])
     ap.add_argument("--width", type=int, default=1920, help="image width for --mode render")
     ap.add_argument("--height", type=int, default=1080, help="image height for --mode render")
     ap.add_argument("--png", default="", help="--mode render: write the frame to this PNG")
@@ -535,6 +576,8 @@ def main() -> None:
         run_batched(args)
     elif args.mode == "render":
         run_render(args)
+    elif args.mode == "sph2d":
+        run_sph2d(args)
     else:
         run_gpu(args)
 

@@ -74,6 +74,18 @@ class RenderParams(C.Structure):
                 ("reserved", C.c_int32 * 4)]
 
 
+class Params2D(C.Structure):
+    _fields_ = [("n_particles", C.c_int32), ("wave_cells", C.c_int32), ("sph_substeps", C.c_int32),
+                ("wave_substeps", C.c_int32), ("grid_cells", C.c_int32 * 2), ("init_columns", C.c_int32),
+                ("view_size", C.c_float * 2), ("particle_radius", C.c_float), ("rest_density", C.c_float),
+                ("visc", C.c_float), ("dt", C.c_float), ("gas_const", C.c_float), ("bottom", C.c_float),
+                ("wave_lambda", C.c_float), ("wave_dx", C.c_float), ("reserved", C.c_int32 * 4)]
+
+
+PARTICLE2D_DTYPE = np.dtype([("pos", "<f4", 4), ("vel", "<f4", 4), ("acc", "<f4", 4)])
+PASS2D = {"grid": 0, "density": 1, "force": 2, "wave_predict": 3, "wave_correct": 4}
+
+
 class TuneReport(C.Structure):
     _fields_ = [("best", SimOptions), ("best_ms", C.c_float), ("entry_ms", C.c_float),
                 ("n_tried", C.c_int32), ("tried", SimOptions * 32), ("tried_ms", C.c_float * 32)]
@@ -120,6 +132,18 @@ _PROTOS = {
     "cwa_render_defaults": (C.c_int, [_I32, _I32, C.POINTER(Camera), C.POINTER(RenderParams)]),
     "cwa_render_set_skybox": (C.c_int, [_P, C.c_void_p, _I32]),
     "cwa_render": (C.c_int, [_P, _I32, C.POINTER(Camera), C.POINTER(RenderParams), C.c_void_p]),
+    "cwa2d_defaults": (C.c_int, [C.POINTER(Params2D)]),
+    "cwa2d_create": (C.c_int, [C.POINTER(Params2D), _I32, C.POINTER(_P)]),
+    "cwa2d_destroy": (C.c_int, [_P]),
+    "cwa2d_reinit": (C.c_int, [_P]),
+    "cwa2d_splash": (C.c_int, [_P]),
+    "cwa2d_step": (C.c_int, [_P, _I32]),
+    "cwa2d_pass": (C.c_int, [_P, _I32]),
+    "cwa2d_upload_particles": (C.c_int, [_P, C.c_void_p, _I32]),
+    "cwa2d_download_particles": (C.c_int, [_P, C.c_void_p, _I32]),
+    "cwa2d_upload_wave": (C.c_int, [_P, C.c_void_p, _I32]),
+    "cwa2d_download_wave": (C.c_int, [_P, C.c_void_p, _I32]),
+    "cwa2d_synchronize": (C.c_int, [_P]),
     "cwa_synchronize": (C.c_int, [_P]),
     "cwa_get_step_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "cwa_get_rebuild_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
@@ -195,4 +219,4 @@ def declared_functions(header: Path | None = None) -> list[str]:
     header = header or (Path(__file__).resolve().parent.parent / "include" / "cwa.h")
     text = header.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(cwa_[a-z0-9_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(cwa2?d?_[a-z0-9_]+)\s*\(", text)))

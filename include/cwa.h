@@ -368,6 +368,66 @@ cwa_status cwa_render_set_skybox(cwa_sim* sim, const uint8_t* faces_rgba, int32_
 cwa_status cwa_render(cwa_sim* sim, int32_t scene, const cwa_camera* camera, const cwa_render_params* params,
                       uint8_t* out_rgba);
 
+/* ---- the 2D solver family (SphWave2D) ----
+ * The reference's 2D predecessor: cubic-spline SPH (SphWaveKoschier2D_grid_cs.glsl)
+ * with signed-distance walls over a 32 x 32 uniform grid (SphUgrid,
+ * StencilBuffer.cpp:138-179, two substeps of grid build + density + forces
+ * per frame), coupled one way to a 1D shallow-water field advanced by a
+ * two-phase Lax-Wendroff step (Shallow1D_cs.glsl, ImageStencil::Compute,
+ * StencilImage2D.cpp:141-163).  Each frame runs the SPH substeps on the
+ * field of the previous frame, then the wave step (SphWave2D/Main.cpp:220-241). */
+typedef struct cwa2d_particle {
+  float pos[4];  /* x, y, 0, enabled (1) / disabled (0) */
+  float vel[4];  /* vx, vy, 0, pressure */
+  float acc[4];  /* ax, ay, 0, density */
+} cwa2d_particle;  /* SphWave2D Particle, Main.cpp:34-39 (48 bytes) */
+
+typedef struct cwa2d_params {
+  int32_t n_particles;    /* num_particles = 32*128 (Main.cpp:41) */
+  int32_t wave_cells;     /* 128 (Main.cpp:89) */
+  int32_t sph_substeps;   /* 2 (Main.cpp:302) */
+  int32_t wave_substeps;  /* 1 (StencilImage2D.h:55) */
+  int32_t grid_cells[2];  /* 32 x 32 (StencilBuffer.cpp:138) */
+  int32_t init_columns;   /* WIDTH = 128, the initial lattice's columns */
+  float view_size[2];     /* VIEW_WIDTH, VIEW_HEIGHT = 9.6 */
+  float particle_radius;  /* 0.025; support H = 4 r */
+  float rest_density;     /* 1000 */
+  float visc;             /* 0.05 */
+  float dt;               /* 0.002 */
+  float gas_const;        /* 35000 (weakly compressible, gamma 3) */
+  float bottom;           /* 0.3: floor plane offset */
+  float wave_lambda;      /* 0.001 (Shallow1D_cs.glsl:23) */
+  float wave_dx;          /* 0.1 */
+  int32_t reserved[4];
+} cwa2d_params;
+
+typedef struct cwa2d_sim cwa2d_sim;
+enum {
+  CWA2D_PASS_GRID = 0,          /* uniform grid of the current positions */
+  CWA2D_PASS_DENSITY = 1,       /* MODE_COMPUTE_DENSITY_PRESSURE */
+  CWA2D_PASS_FORCE = 2,         /* MODE_COMPUTE_FORCES (integrates) */
+  CWA2D_PASS_WAVE_PREDICT = 3,  /* Shallow1D MODE_ITERATE0 */
+  CWA2D_PASS_WAVE_CORRECT = 4   /* Shallow1D MODE_ITERATE1 */
+};
+
+cwa_status cwa2d_defaults(cwa2d_params* out);
+cwa_status cwa2d_create(const cwa2d_params* params, int32_t device, cwa2d_sim** out);
+cwa_status cwa2d_destroy(cwa2d_sim* sim);
+/* InitParticle (MODE_INIT) and InitWave (Shallow1D MODE_INIT_0). */
+cwa_status cwa2d_reinit(cwa2d_sim* sim);
+/* The "Splash" button: Shallow1D MODE_INIT_1 on the current field. */
+cwa_status cwa2d_splash(cwa2d_sim* sim);
+/* n frames (SPH substeps, then the wave substeps), one CUDA graph each. */
+cwa_status cwa2d_step(cwa2d_sim* sim, int32_t n_steps);
+/* One pass of a frame (CWA2D_PASS_*), eager; density needs a grid pass first. */
+cwa_status cwa2d_pass(cwa2d_sim* sim, int32_t pass);
+cwa_status cwa2d_upload_particles(cwa2d_sim* sim, const cwa2d_particle* host, int32_t n);
+cwa_status cwa2d_download_particles(cwa2d_sim* sim, cwa2d_particle* host, int32_t n);
+/* The wave field: n cells of (h, uh, h_half, uh_half). */
+cwa_status cwa2d_upload_wave(cwa2d_sim* sim, const float* cells4, int32_t n);
+cwa_status cwa2d_download_wave(cwa2d_sim* sim, float* cells4, int32_t n);
+cwa_status cwa2d_synchronize(cwa2d_sim* sim);
+
 #ifdef __cplusplus
 }
 #endif

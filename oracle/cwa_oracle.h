@@ -96,6 +96,15 @@ float orc_sample_f32(const float* u, int32_t w, int32_t h, float s, float t);
 void orc_render(const float* pos4, int32_t n, const float* wave, int32_t nx, int32_t nz, const cwa_camera* cam,
                 const cwa_render_params* prm, const uint8_t* sky, int32_t sky_size, uint8_t* out);
 
+/* The 2D solver family (cwa2d_oracle.cpp): SphWave2D's initialisers, one
+ * phase of the shallow-water step (float32 op by op), and the two SPH passes
+ * in FP64 from an input particle array to an output array. */
+void orc2d_init_particles(const cwa2d_params* prm, cwa2d_particle* out);
+void orc2d_wave_init_f32(const cwa2d_params* prm, const float* in4, float* out4, int32_t splash);
+void orc2d_wave_iter_f32(const cwa2d_params* prm, const float* in4, float* out4, int32_t phase);
+void orc2d_density(const cwa2d_params* prm, const cwa2d_particle* in, const float* wave4, cwa2d_particle* out);
+void orc2d_force(const cwa2d_params* prm, const cwa2d_particle* in, const float* wave4, cwa2d_particle* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,11 @@ def load() -> C.CDLL:
             "orc_wave_from_image_f32": (None, [C.c_int32, C.c_int32, _P, C.c_int32, C.c_int32, _P]),
             "orc_sample_f32": (C.c_float, [_P, _I, _I, C.c_float, C.c_float]),
             "orc_render": (None, [_P, _I, _P, _I, _I, _P, _P, _P, _I, _P]),
+            "orc2d_init_particles": (None, [_P, _P]),
+            "orc2d_wave_init_f32": (None, [_P, _P, _P, _I]),
+            "orc2d_wave_iter_f32": (None, [_P, _P, _P, _I]),
+            "orc2d_density": (None, [_P, _P, _P, _P]),
+            "orc2d_force": (None, [_P, _P, _P, _P]),
         }
         for name, (res, args) in protos.items():
             fn = getattr(lib, name)
@@ -246,4 +251,44 @@ def render(pos4: np.ndarray, wave: np.ndarray, camera, params, sky: np.ndarray |
     sk = None if sky is None else np.ascontiguousarray(sky, np.uint8)
     load().orc_render(_p(p), p.shape[0], _p(u), u.shape[1], u.shape[0], C.cast(C.pointer(camera), C.c_void_p),
                       C.cast(C.pointer(params), C.c_void_p), _p(sk), 0 if sk is None else sk.shape[1], _p(out))
+    return out
+
+
+# ---- the 2D solver family ----
+def _pp(params):
+    return C.cast(C.pointer(params), C.c_void_p)
+
+
+def init_particles_2d(params, dtype) -> np.ndarray:
+    out = np.zeros(params.n_particles, dtype)
+    load().orc2d_init_particles(_pp(params), _p(out))
+    return out
+
+
+def wave_init_2d_f32(params, prev=None, splash=False) -> np.ndarray:
+    inp = np.zeros((params.wave_cells, 4), np.float32) if prev is None else np.ascontiguousarray(prev, np.float32)
+    out = np.zeros((params.wave_cells, 4), np.float32)
+    load().orc2d_wave_init_f32(_pp(params), _p(inp), _p(out), int(splash))
+    return out
+
+
+def wave_iter_2d_f32(params, cells4, phase: int, out_prev=None) -> np.ndarray:
+    """One Lax-Wendroff phase; out_prev = the write buffer's previous contents."""
+    inp = np.ascontiguousarray(cells4, np.float32)
+    out = np.zeros_like(inp) if out_prev is None else np.ascontiguousarray(out_prev, np.float32).copy()
+    load().orc2d_wave_iter_f32(_pp(params), _p(inp), _p(out), phase)
+    return out
+
+
+def density_2d(params, particles, wave4) -> np.ndarray:
+    inp = np.ascontiguousarray(particles)
+    out = np.zeros_like(inp)
+    load().orc2d_density(_pp(params), _p(inp), _p(np.ascontiguousarray(wave4, np.float32)), _p(out))
+    return out
+
+
+def force_2d(params, particles, wave4) -> np.ndarray:
+    inp = np.ascontiguousarray(particles)
+    out = np.zeros_like(inp)
+    load().orc2d_force(_pp(params), _p(inp), _p(np.ascontiguousarray(wave4, np.float32)), _p(out))
     return out
