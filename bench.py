@@ -507,6 +507,43 @@ def run_sph2d(args) -> None:
     print(json.dumps(out), flush=True)
 
 
+def run_pbd(args) -> None:
+    """`--mode pbd`: the PBD box demo (4096 boxes, 16^3 grid) and, with
+    --boxes, larger piles; frames per second on the GPU (CUDA-graph frames)
+    and of the float32 CPU restatement on the host (bounded sample)."""
+    import torch  # noqa: F401 (CUDA context first, as the other modes)
+
+    from coupledwateranimation_gb300.pbd import PbdSim, make_boxes, pbd_defaults
+    p = pbd_defaults()
+    if args.boxes:
+        p.n_boxes = args.boxes
+        p.max_contacts = 256  # the demo's initial block gets denser with the count
+    boxes = make_boxes(p, 12345)
+    frames = max(10, args.steps)
+    with PbdSim(p) as sim:
+        sim.upload(boxes)
+        sim.step(max(3, args.warmup))
+        sim.download()
+        t0 = time.perf_counter()
+        sim.step(frames)
+        state = sim.download()
+        gpu_s = (time.perf_counter() - t0) / frames
+        pairs = sim.pair_count()
+    out = {"mode": "pbd", "boxes": p.n_boxes, "frames": frames, "contacts_last_frame": pairs,
+           "gpu_ms_per_frame": gpu_s * 1e3, "gpu_box_updates_per_s": p.n_boxes / gpu_s}
+    if not args.no_cpu:
+        from oracle import oracle as orc
+        cpu_frames, t0 = 0, time.perf_counter()
+        while cpu_frames < 2 or time.perf_counter() - t0 < 5.0:
+            state = orc.pbd_step(p, state, 1)
+            cpu_frames += 1
+        cpu_s = (time.perf_counter() - t0) / cpu_frames
+        out["cpu_baseline"] = {"ms_per_frame": cpu_s * 1e3, "cores": 1, "kind": "port",
+                               "sample": f"{cpu_frames} frames of the float32 restatement (oracle/), one thread"}
+        out["gpu_vs_cpu"] = cpu_s / gpu_s
+    print(json.dumps(out), flush=True)
+
+
 def run_wave(args) -> None:
     """The wave module stepped alone (no particle passes) on an nx x nz field:
     `--steps` single wave passes against cwa_wave_advance over the same
@@ -552,7 +589,9 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "wave", "batched", "render", "sph2d"])
+    ap.add_argument("--mode", default="bench",
+                    choices=["bench", "profile", "wave", "batched", "render", "sph2d", "pbd"])
+    ap.add_argument("--boxes", type=int, default=0, help="--mode pbd: number of boxes (default 4096)")
     ap.add_argument("--width", type=int, default=1920, help="image width for --mode render")
     ap.add_argument("--height", type=int, default=1080, help="image height for --mode render")
     ap.add_argument("--png", default="", help="--mode render: write the frame to this PNG")
@@ -578,6 +617,8 @@ def main() -> None:
         run_render(args)
     elif args.mode == "sph2d":
         run_sph2d(args)
+    elif args.mode == "pbd":
+        run_pbd(args)
     else:
         run_gpu(args)
 

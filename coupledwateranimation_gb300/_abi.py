@@ -82,6 +82,17 @@ class Params2D(C.Structure):
                 ("wave_lambda", C.c_float), ("wave_dx", C.c_float), ("reserved", C.c_int32 * 4)]
 
 
+class PbdParams(C.Structure):
+    _fields_ = [("n_boxes", C.c_int32), ("grid_cells", C.c_int32 * 3), ("extents_lo", C.c_float * 3),
+                ("extents_hi", C.c_float * 3), ("g", C.c_float * 3), ("dt", C.c_float), ("damping", C.c_float),
+                ("k", C.c_float), ("k_static", C.c_float), ("sleep_thresh", C.c_float), ("mu_k", C.c_float),
+                ("mu_s", C.c_float), ("e", C.c_float), ("substeps", C.c_int32), ("max_contacts", C.c_int32),
+                ("reserved", C.c_int32 * 3)]
+
+
+PBD_BOX_DTYPE = np.dtype([("color", "<f4", 4), ("x", "<f4", 4), ("v", "<f4", 4), ("p", "<f4", 4),
+                          ("dp_t", "<f4", 4), ("dp_n", "<f4", 4), ("hw", "<f4", 4), ("rm", "<f4"), ("n", "<f4"),
+                          ("e", "<f4"), ("padding", "<f4")])
 PARTICLE2D_DTYPE = np.dtype([("pos", "<f4", 4), ("vel", "<f4", 4), ("acc", "<f4", 4)])
 PASS2D = {"grid": 0, "density": 1, "force": 2, "wave_predict": 3, "wave_correct": 4}
 
@@ -144,6 +155,14 @@ _PROTOS = {
     "cwa2d_upload_wave": (C.c_int, [_P, C.c_void_p, _I32]),
     "cwa2d_download_wave": (C.c_int, [_P, C.c_void_p, _I32]),
     "cwa2d_synchronize": (C.c_int, [_P]),
+    "cwa_pbd_defaults": (C.c_int, [C.POINTER(PbdParams)]),
+    "cwa_pbd_make_boxes": (C.c_int, [C.POINTER(PbdParams), C.c_uint64, C.c_void_p, _I32]),
+    "cwa_pbd_create": (C.c_int, [C.POINTER(PbdParams), _I32, C.POINTER(_P)]),
+    "cwa_pbd_destroy": (C.c_int, [_P]),
+    "cwa_pbd_upload": (C.c_int, [_P, C.c_void_p, _I32]),
+    "cwa_pbd_download": (C.c_int, [_P, C.c_void_p, _I32]),
+    "cwa_pbd_step": (C.c_int, [_P, _I32]),
+    "cwa_pbd_pair_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "cwa_synchronize": (C.c_int, [_P]),
     "cwa_get_step_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "cwa_get_rebuild_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
@@ -219,4 +238,4 @@ def declared_functions(header: Path | None = None) -> list[str]:
     header = header or (Path(__file__).resolve().parent.parent / "include" / "cwa.h")
     text = header.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(cwa2?d?_[a-z0-9_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(cwa(?:2d)?_[a-z0-9_]+)\s*\(", text)))

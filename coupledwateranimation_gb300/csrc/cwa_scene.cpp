@@ -228,4 +228,58 @@ cwa_status cwa_make_bumps(const cwa_scene_desc* sc, int32_t n_bumps, uint64_t se
   return CWA_OK;
 }
 
+cwa_status cwa_pbd_defaults(cwa_pbd_params* p) {
+  if (!p) return CWA_ERR_INVALID_ARG;
+  *p = cwa_pbd_params{};
+  p->n_boxes = 4 * 1024;
+  p->grid_cells[0] = p->grid_cells[1] = p->grid_cells[2] = 16;
+  for (int c = 0; c < 3; ++c) {
+    p->extents_lo[c] = -1.0f;
+    p->extents_hi[c] = 1.0f;
+  }
+  p->g[1] = -0.1f;
+  p->dt = 0.02f;
+  p->damping = 0.999f;
+  p->k = 1.75f;
+  p->k_static = 10.0f;
+  p->sleep_thresh = 0.0005f;
+  p->mu_k = 0.4f;
+  p->mu_s = 0.5f;
+  p->e = 0.75f;
+  p->substeps = 1;
+  return CWA_OK;
+}
+
+cwa_status cwa_pbd_make_boxes(const cwa_pbd_params* p, uint64_t seed, cwa_pbd_box* out, int32_t n) {
+  if (!p || !out || n < 0 || p->grid_cells[0] < 1) return CWA_ERR_INVALID_ARG;
+  Xoshiro256ss rng(seed);
+  // UniformGridPbdGpu3D: cell edge = extent / cells; half widths drawn from
+  // [0.15, 0.45] cell edges (x axis), positions 0.5 U(-1, 1), velocities 0.1 U(-1, 1)
+  const float cell = (p->extents_hi[0] - p->extents_lo[0]) / (float)p->grid_cells[0];
+  auto upos = [&]() { return (float)(2.0 * rng.uniform() - 1.0); };
+  auto usize = [&]() { return (float)(0.15 * cell + (0.45 * cell - 0.15 * cell) * rng.uniform()); };
+  for (int32_t i = 0; i < n; ++i) {
+    cwa_pbd_box& b = out[i];
+    memset(&b, 0, sizeof(b));
+    const float x = 0.5f * upos(), y = 0.5f * upos(), z = 0.5f * upos();
+    const float vx = upos(), vy = upos(), vz = upos();
+    const float hx = usize(), hy = usize(), hz = usize();
+    for (int c = 0; c < 4; ++c) b.color[c] = 1.0f;
+    b.x[0] = b.p[0] = x;
+    b.x[1] = b.p[1] = y;
+    b.x[2] = b.p[2] = z;
+    b.x[3] = b.p[3] = 1.0f;
+    b.v[0] = 0.1f * vx;
+    b.v[1] = 0.1f * vy;
+    b.v[2] = 0.1f * vz;
+    b.hw[0] = hx;
+    b.hw[1] = hy;
+    b.hw[2] = hz;
+    b.rm = 1.0f / (hx * hy * hz);
+    b.n = 0.0f;
+    b.e = 1.0f;
+  }
+  return CWA_OK;
+}
+
 }  // extern "C"

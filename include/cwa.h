@@ -428,6 +428,62 @@ cwa_status cwa2d_upload_wave(cwa2d_sim* sim, const float* cells4, int32_t n);
 cwa_status cwa2d_download_wave(cwa2d_sim* sim, float* cells4, int32_t n);
 cwa_status cwa2d_synchronize(cwa2d_sim* sim);
 
+/* ---- position-based box collisions on the uniform grid ----
+ * The reference's GridTestPbdGpu3D demo (UniformGrid2D/UniformGridGpu3D.cpp:
+ * 292-350 and uniform_grid_pbd_3D_cs.glsl): axis-aligned boxes inserted into
+ * every grid cell they overlap, one Jacobi PBD iteration per substep
+ * (PreAnimate, collision query against the extents and the other boxes with
+ * friction, PostAnimate with SOR factor k and restitution e).  The shader
+ * accumulates every constraint with float atomics, so its sums depend on
+ * thread order; here each box gathers its contributions in a fixed order
+ * (partners by index), which makes a step deterministic. */
+typedef struct cwa_pbd_box {
+  float color[4];  /* (1, 1, 1, 1), red (1, 0, 0, 1) after a contact */
+  float x[4];      /* position, w = 1 */
+  float v[4];      /* velocity */
+  float p[4];      /* predicted position */
+  float dp_t[4];   /* friction displacement sum */
+  float dp_n[4];   /* normal displacement sum */
+  float hw[4];     /* half widths */
+  float rm;        /* 1 / mass = 1 / (hw.x hw.y hw.z) */
+  float n;         /* constraint count */
+  float e;
+  float padding;
+} cwa_pbd_box;  /* PbdObj, UniformGridGpu3D.h:27-39 (128 bytes) */
+
+typedef struct cwa_pbd_params {
+  int32_t n_boxes;      /* 4 * 1024 (UniformGrid2D/Main.cpp:49) */
+  int32_t grid_cells[3];/* 16^3 over the extents (UniformGridGpu3D.cpp:292) */
+  float extents_lo[3], extents_hi[3];  /* [-1, 1]^3 */
+  float g[3];           /* (0, -0.1, 0) (UniformGridGpu3D.h:45-55) */
+  float dt;             /* 0.02 */
+  float damping;        /* 0.999 */
+  float k;              /* SOR factor 1.75 */
+  float k_static;       /* 10 */
+  float sleep_thresh;   /* 0.0005 */
+  float mu_k, mu_s;     /* 0.4, 0.5 */
+  float e;              /* restitution 0.75 */
+  int32_t substeps;     /* 1 */
+  int32_t max_contacts; /* contact slots per box (0 = 64); more in one step is CWA_ERR_CAPACITY */
+  int32_t reserved[3];
+} cwa_pbd_params;
+
+typedef struct cwa_pbd_sim cwa_pbd_sim;
+cwa_status cwa_pbd_defaults(cwa_pbd_params* out);
+/* GridTestPbdGpu3D::Init (UniformGridGpu3D.cpp:299-336): positions
+ * 0.5 U(-1, 1)^3, velocities 0.1 U(-1, 1)^3, half widths U(0.15, 0.45) cell
+ * edges per axis, drawn from the library's seeded generator. */
+cwa_status cwa_pbd_make_boxes(const cwa_pbd_params* params, uint64_t seed, cwa_pbd_box* out, int32_t n);
+cwa_status cwa_pbd_create(const cwa_pbd_params* params, int32_t device, cwa_pbd_sim** out);
+cwa_status cwa_pbd_destroy(cwa_pbd_sim* sim);
+cwa_status cwa_pbd_upload(cwa_pbd_sim* sim, const cwa_pbd_box* host, int32_t n);
+cwa_status cwa_pbd_download(cwa_pbd_sim* sim, cwa_pbd_box* host, int32_t n);
+/* n frames of Animate (UniformGridGpu3D.cpp:338-346): substeps x
+ * (grid build, PreAnimate, collision query, PostAnimate). */
+cwa_status cwa_pbd_step(cwa_pbd_sim* sim, int32_t n_steps);
+/* Contact pairs found by the last collision query. */
+cwa_status cwa_pbd_pair_count(cwa_pbd_sim* sim, int64_t* pairs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -105,6 +105,10 @@ void orc2d_wave_iter_f32(const cwa2d_params* prm, const float* in4, float* out4,
 void orc2d_density(const cwa2d_params* prm, const cwa2d_particle* in, const float* wave4, cwa2d_particle* out);
 void orc2d_force(const cwa2d_params* prm, const cwa2d_particle* in, const float* wave4, cwa2d_particle* out);
 
+/* PBD box collisions (cwa_pbd_oracle.cpp): `steps` frames in place, float32
+ * op by op with the library's accumulation order. */
+void orc_pbd_step(const cwa_pbd_params* p, cwa_pbd_box* boxes, int32_t n, int32_t steps);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,6 +64,7 @@ def load() -> C.CDLL:
             "orc2d_wave_iter_f32": (None, [_P, _P, _P, _I]),
             "orc2d_density": (None, [_P, _P, _P, _P]),
             "orc2d_force": (None, [_P, _P, _P, _P]),
+            "orc_pbd_step": (None, [_P, _P, _I, _I]),
         }
         for name, (res, args) in protos.items():
             fn = getattr(lib, name)
@@ -291,4 +292,11 @@ def force_2d(params, particles, wave4) -> np.ndarray:
     inp = np.ascontiguousarray(particles)
     out = np.zeros_like(inp)
     load().orc2d_force(_pp(params), _p(inp), _p(np.ascontiguousarray(wave4, np.float32)), _p(out))
+    return out
+
+
+def pbd_step(params, boxes, steps: int):
+    """`steps` PBD frames of a copy of `boxes` (numpy records, 128 bytes each)."""
+    out = np.ascontiguousarray(boxes).copy()
+    load().orc_pbd_step(_pp(params), _p(out), len(out), steps)
     return out
