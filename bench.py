@@ -41,7 +41,9 @@ sys.path.insert(0, str(ROOT))
 METRIC = "particle+wave-cell updates/s on 1 GB300, batched vs plain, % of HBM roofline"
 UNIT = "updates/s"
 # Algorithmic bytes per unit of work (one particle or grid/wave cell per step).
-BYTES_PER_PARTICLE = {"grid": 20 + 140, "rho_pres": 24, "force": 64, "integrate": 100}
+# Per-step mode: integrate also hashes and counts the new positions (20 B of
+# the sort's 160), so the grid pass carries the reorder's 140.
+BYTES_PER_PARTICLE = {"grid": 140, "rho_pres": 24, "force": 64, "integrate": 100 + 20}
 BYTES_PER_GRID_CELL = {"grid": 28}
 BYTES_PER_WAVE_CELL = {"wave": 20}
 FALLBACK_HBM_GBS = 6800.0
