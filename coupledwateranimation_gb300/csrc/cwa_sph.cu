@@ -224,6 +224,16 @@ constexpr int kRowCodeBits = 12;  // a hit is (row << 12) | offset from the row'
 constexpr int kRowCodeMax = 1 << kRowCodeBits;
 constexpr int kMaxSegs = 18;      // 2 columns x 9 rows
 
+// Hit lists hold codes in pairs: code k of particle i is half (k & 1) of the
+// 32-bit word (k >> 1) * n + i, so a warp writes its lanes' k-th pairs as one
+// 128-byte store and readers load two codes per load.
+__device__ __forceinline__ size_t code_slot(int k, int i, int n) {
+  return ((size_t)(k >> 1) * n + i) * 2 + (k & 1);
+}
+__device__ __forceinline__ uint32_t code_pair(const uint16_t* __restrict__ list, int k, int i, int n) {
+  return __ldg(reinterpret_cast<const uint32_t*>(list) + (size_t)(k >> 1) * n + i);
+}
+
 struct StagePlan {
   int32_t seg_b[kMaxSegs];        // global sorted index of each staged segment
   int32_t seg_off[kMaxSegs + 1];  // staged offset (prefix of lengths)
@@ -390,10 +400,14 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
     }
     if (MODE == MODE_DENSITY) acc.add(part);
   }
-  // Coalesced list write: entry k of every lane is one 64-byte store per warp.
+  // Coalesced list write: the pair (k, k+1) of every lane is one 128-byte
+  // store per warp.  (Row k+1 <= kCap exists: s_hit has the overflow row.)
   const int cnt = (int)(hp - hit_col) / kNbThreads;
   overflow |= cnt >= kCap;
-  for (int k = 0; k < cnt; ++k) list[(size_t)k * n_total + i] = hit_col[k * kNbThreads];
+  uint32_t* const list32 = reinterpret_cast<uint32_t*>(list);
+  for (int k = 0; k < cnt; k += 2)
+    list32[(size_t)(k >> 1) * n_total + i] =
+        (uint32_t)hit_col[k * kNbThreads] | ((uint32_t)hit_col[(k + 1) * kNbThreads] << 16);
   list_cnt[i] = overflow ? kCap + 1 : cnt;
   if (MODE == MODE_LIST) {
     xref[i] = pi;
@@ -411,7 +425,7 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
 // step's hit list for force.  A particle whose Verlet list overflowed rescans
 // the rows of its rebuild cell.
 template <int P>
-__global__ void __launch_bounds__(kNbThreads)
+__global__ void __launch_bounds__(kNbThreads, 8)
     k_rho_list(const float4* __restrict__ pos, const int32_t* __restrict__ start,
                const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
                const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
@@ -443,7 +457,7 @@ __global__ void __launch_bounds__(kNbThreads)
     q = fma(-dz, dz, q);
     const T qp = q > (T)0 ? q : (T)0;
     if (q > (T)0) {
-      if (cnt < kMaxNbr) nbr[(size_t)cnt * n_total + i] = (uint16_t)code;
+      if (cnt < kMaxNbr) nbr[code_slot(cnt, i, n_total)] = (uint16_t)code;
       ++cnt;
     }
     return qp * qp * qp;
@@ -455,7 +469,11 @@ __global__ void __launch_bounds__(kNbThreads)
     for (int k0 = 0; k0 < vn; k0 += 8) {
       uint32_t code[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) code[u] = k0 + u < vn ? __ldg(vlist + (size_t)(k0 + u) * n_total + i) : 0u;
+      for (int u = 0; u < 8; u += 2) {
+        const uint32_t w = k0 + u < vn ? code_pair(vlist, k0 + u, i, n_total) : 0u;
+        code[u] = w & 0xFFFFu;
+        code[u + 1] = k0 + u + 1 < vn ? w >> 16 : 0u;
+      }
       T part = (T)0;
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
@@ -581,8 +599,11 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
     for (int k0 = 0; k0 < cnt; k0 += 8) {
       uint32_t code[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u)
-        code[u] = k0 + u < cnt ? __ldg(nbr + (size_t)(k0 + u) * n_total + i) : self_code;
+      for (int u = 0; u < 8; u += 2) {
+        const uint32_t w = k0 + u < cnt ? code_pair(nbr, k0 + u, i, n_total) : 0u;
+        code[u] = k0 + u < cnt ? (w & 0xFFFFu) : self_code;
+        code[u + 1] = k0 + u + 1 < cnt ? (w >> 16) : self_code;
+      }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int j = s_rb[code[u] >> kRowCodeBits][threadIdx.x] + (int)(code[u] & (kRowCodeMax - 1));
