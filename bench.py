@@ -548,39 +548,50 @@ def run_pbd(args) -> None:
 
 def run_wave(args) -> None:
     """The wave module stepped alone (no particle passes) on an nx x nz field:
-    `--steps` single wave passes against cwa_wave_advance over the same
-    steps (4 per launch, TMA-loaded tiles), CUDA events on the sim's stream,
-    fields larger than L2 unless --wave-n is small.  Prints one JSON line."""
+    `--steps` single wave passes against cwa_wave_advance over the same steps
+    with each blocked variant (128 x H boxes, K steps per launch, TMA-loaded
+    tiles) and the wave tuner's pick; CUDA events on the sim's stream, fields
+    larger than L2 unless --wave-n is small.  Prints one JSON line."""
     import torch
 
     from coupledwateranimation_gb300 import Sim, scenes
+    from coupledwateranimation_gb300._abi import WAVE_BLOCKS
     n = args.wave_n
     d = scenes.reference().desc  # the reference's wave module: no deposits, splash init
     d.n_particles = 0
     d.wave_nx = d.wave_nz = n
-    steps = max(4, args.steps // 4 * 4)
+    steps = max(8, args.steps // 8 * 8)
     out = {"mode": "wave", "field": f"{n}x{n}", "steps": steps}
+
+    def timed(sim, fn):
+        stream = torch.cuda.ExternalStream(sim.device_view(0).stream)
+        fn()  # warm-up
+        sim.synchronize()
+        best = None
+        for _ in range(max(3, args.warmup)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+            sim.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        cells = n * n * steps
+        return {"us_per_step": best / steps * 1e3, "cell_updates_per_s": cells / (best * 1e-3),
+                "effective_gbs_at_12B": 12 * cells / (best * 1e-3) / 1e9}
+
     with Sim(d, use_graph=False) as sim:
         sim.wave_reinit(0)
-        stream = torch.cuda.ExternalStream(sim.device_view(0).stream)
-        for label, fn in (("single", lambda: [sim.wave() for _ in range(steps)]),
-                          ("blocked", lambda: sim.wave_advance(steps))):
-            fn()  # warm-up
-            sim.synchronize()
-            best = None
-            for _ in range(max(3, args.warmup)):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                torch.cuda.synchronize()
-                with torch.cuda.stream(stream):
-                    e0.record(stream)
-                    fn()
-                    e1.record(stream)
-                sim.synchronize()
-                ms = e0.elapsed_time(e1)
-                best = ms if best is None else min(best, ms)
-            cells = n * n * steps
-            out[label] = {"us_per_step": best / steps * 1e3, "cell_updates_per_s": cells / (best * 1e-3),
-                          "effective_gbs_at_12B": 12 * cells / (best * 1e-3) / 1e9}
+        out["single"] = timed(sim, lambda: [sim.wave() for _ in range(steps)])
+        tune = sim.autotune_wave(steps)
+        out["tuner"] = {"pick": tune["best_name"], "ms_per_step": tune["ms_per_step"]}
+    for v, name in enumerate(WAVE_BLOCKS):
+        with Sim(d, use_graph=False, wave_block=v) as sim:
+            sim.wave_reinit(0)
+            out[f"blocked_{name}"] = timed(sim, lambda: sim.wave_advance(steps))
+    out["blocked"] = out[f"blocked_{tune['best_name']}"]
     out["speedup"] = out["single"]["us_per_step"] / out["blocked"]["us_per_step"]
     print(json.dumps(out), flush=True)
 

@@ -59,7 +59,15 @@ class SceneDesc(C.Structure):
 class SimOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("use_graph", C.c_int32),
                 ("nb_threads", C.c_int32), ("nb_stage", C.c_int32), ("verlet_skin", C.c_float),
-                ("nb_scan_minb", C.c_int32), ("nb_force_minb", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("nb_scan_minb", C.c_int32), ("nb_force_minb", C.c_int32), ("wave_block", C.c_int32),
+                ("reserved", C.c_int32 * 3)]
+
+
+WAVE_BLOCKS = ("32x4", "64x4", "64x8")  # CWA_WAVE_BLOCK_*: box rows x steps per launch
+
+
+class WaveTuneReport(C.Structure):
+    _fields_ = [("best", C.c_int32), ("steps", C.c_int32), ("ms_per_step", C.c_float * len(WAVE_BLOCKS))]
 
 
 class Camera(C.Structure):
@@ -176,6 +184,7 @@ _PROTOS = {
     "cwa_get_pass_times": (C.c_int, [_P, _P, _I32]),
     "cwa_get_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "cwa_autotune": (C.c_int, [_P, _I32, C.POINTER(TuneReport)]),
+    "cwa_autotune_wave": (C.c_int, [_P, _I32, C.POINTER(WaveTuneReport)]),
     "cwa_get_options": (C.c_int, [_P, C.POINTER(SimOptions)]),
     "cwa_scan_workspace_bytes": (C.c_size_t, [_I32]),
     "cwa_exclusive_scan_i32": (C.c_int, [_P, _P, _I32, _P, C.c_size_t, _P]),

@@ -72,12 +72,13 @@ struct cwa_sim {
   int wcur = 0;
   unsigned long long* D = nullptr;
   // wave advance (cwa_wave_advance): physical buffers UB[0..3], slot -> buffer
-  // map uid (slots 0-2 are U[0..2], slot 3 the spare), per-buffer tensor maps
+  // map uid (slots 0-2 are U[0..2], slot 3 the spare); per variant, tensor
+  // maps [variant][buffer][scene] and block tiles wb_off[v] .. wb_off[v+1]
   float* UB[4] = {nullptr, nullptr, nullptr, nullptr};
   int uid[4] = {0, 1, 2, 3};
   CUtensorMap* d_wmaps = nullptr;
   WaveBlockTile* d_wbtiles = nullptr;
-  int32_t n_wbtiles = 0;
+  int32_t wb_off[kWaveVariants + 1] = {};
   // work tiles
   Tile* d_ptiles = nullptr;
   int32_t n_ptiles = 0, ptile = 128;
@@ -95,6 +96,8 @@ struct cwa_sim {
   // per-step mode: integrate has already hashed and counted the current
   // positions for the next grid build (count holds those counts)
   bool counts_pending = false;
+  // an integrate pass has deposited into D since the last wave pass
+  bool deposits_pending = false;
   bool profiling = false;
   bool pass_times_valid = false;
   cudaEvent_t ev[CWA_PASS_COUNT + 1] = {};
@@ -407,6 +410,7 @@ cwa_status run_integrate(cwa_sim* s) {
                             fuse ? s->count : nullptr, s->d_status, s->stream));
   s->launches += s->n_ptiles > 0;
   s->counts_pending = fuse && s->n_ptiles > 0;
+  s->deposits_pending = true;
   if (!s->verlet) s->grid_fresh = false;  // a Verlet list stays usable
   return CWA_OK;
 }
@@ -419,11 +423,13 @@ cwa_status run_wave(cwa_sim* s) {
   s->launches += 1;
   s->wcur = (w + 1) % 3;  // StencilImage2DTripleBuffered::PingPong (:33-40)
   s->steps += 1;
+  s->deposits_pending = false;  // read and cleared
   return CWA_OK;
 }
 
-// Lazily set up the blocked wave advance: the spare buffer, a tensor map of
-// every scene's field in each of the four buffers, and the block tiles.
+// Lazily set up the blocked wave advance: the spare buffer and, for every
+// variant, a tensor map of every scene's field in each of the four buffers
+// and the block tiles.
 cwa_status prepare_wave_blocks(cwa_sim* s) {
   if (s->d_wbtiles) return CWA_OK;
   const int nsc = (int)s->sd.size();
@@ -432,16 +438,20 @@ cwa_status prepare_wave_blocks(cwa_sim* s) {
   for (int b = 0; b < 3; ++b) s->UB[b] = s->U[b];
   s->UB[3] = spare;
   for (int b = 0; b < 4; ++b) s->uid[b] = b;
-  std::vector<CUtensorMap> maps((size_t)4 * nsc);
+  std::vector<CUtensorMap> maps((size_t)kWaveVariants * 4 * nsc);
   memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
   std::vector<WaveBlockTile> tiles;
-  for (int k = 0; k < nsc; ++k) {
-    const SceneDev& d = s->sd[k];
-    bool tma = true;
-    for (int b = 0; b < 4 && tma; ++b)
-      tma = wave_block_encode(&maps[(size_t)b * nsc + k], s->UB[b] + d.woff, d.nx, d.nz);
-    wave_block_tiles(d, k, tma, &tiles);
+  for (int v = 0; v < kWaveVariants; ++v) {
+    s->wb_off[v] = (int32_t)tiles.size();
+    for (int k = 0; k < nsc; ++k) {
+      const SceneDev& d = s->sd[k];
+      bool tma = true;
+      for (int b = 0; b < 4 && tma; ++b)
+        tma = wave_block_encode(&maps[((size_t)v * 4 + b) * nsc + k], s->UB[b] + d.woff, d.nx, d.nz, v);
+      wave_block_tiles(d, k, tma, v, &tiles);
+    }
   }
+  s->wb_off[kWaveVariants] = (int32_t)tiles.size();
   CUtensorMap* dm = nullptr;
   WaveBlockTile* dt = nullptr;
   CWA_TRY(dev_alloc(s, &dm, maps.size()));
@@ -450,28 +460,30 @@ cwa_status prepare_wave_blocks(cwa_sim* s) {
   CWA_CUDA(cudaMemcpy(dt, tiles.data(), tiles.size() * sizeof(WaveBlockTile), cudaMemcpyHostToDevice));
   CWA_CUDA(cudaDeviceSynchronize());  // the zero-fill memsets ran on the legacy stream
   s->d_wmaps = dm;
-  s->n_wbtiles = (int32_t)tiles.size();
   s->d_wbtiles = dt;
   return CWA_OK;
 }
 
-// n wave passes: a single pass first when a scene takes deposits (it applies
-// and clears them), kWaveK-step blocks, single passes for the remainder.  A
-// block writes u^(n+4) into the free slot and u^(n+3) into the spare; the
-// slots are then renamed so U[wcur] / U[(wcur+2)%3] hold them, which is the
-// state kWaveK single passes leave (up to the rotation of wcur).
+// n wave passes: a single pass first when deposits are pending (it applies
+// and clears them), K-step blocks of the sim's wave_block variant, single
+// passes for the remainder.  A block writes u^(n+K) into the free slot and
+// u^(n+K-1) into the spare; the slots are then renamed so U[wcur] /
+// U[(wcur+2)%3] hold them, which is the state K single passes leave (up to
+// the rotation of wcur).
 cwa_status run_wave_advance(cwa_sim* s, int32_t n) {
   int32_t done = 0;
   bool coupled = false;
   for (const SceneDev& d : s->sd) coupled = coupled || d.coupled;
-  if (coupled && n > 0) {
+  if (coupled && s->deposits_pending && n > 0) {
     CWA_TRY(run_wave(s));
     done = 1;
   }
-  if (n - done >= kWaveK) {
+  const int v = s->opt.wave_block, K = wave_variant_steps(v);
+  if (n - done >= K) {
     CWA_TRY(prepare_wave_blocks(s));
     const int w = s->wcur, cur = w, prev = (w + 2) % 3, nxt = (w + 1) % 3;
-    while (n - done >= kWaveK) {
+    const int32_t n_tiles = s->wb_off[v + 1] - s->wb_off[v];
+    while (n - done >= K) {
       const int ic = s->uid[cur], ip = s->uid[prev], oc = s->uid[nxt], op = s->uid[3];
       const size_t nsc = s->sd.size();
       WaveBlockArgs a;
@@ -479,19 +491,19 @@ cwa_status run_wave_advance(cwa_sim* s, int32_t n) {
       a.in_prev = s->UB[ip];
       a.out_cur = s->UB[oc];
       a.out_prev = s->UB[op];
-      a.map_cur = s->d_wmaps + ic * nsc;
-      a.map_prev = s->d_wmaps + ip * nsc;
-      a.tiles = s->d_wbtiles;
+      a.map_cur = s->d_wmaps + ((size_t)v * 4 + ic) * nsc;
+      a.map_prev = s->d_wmaps + ((size_t)v * 4 + ip) * nsc;
+      a.tiles = s->d_wbtiles + s->wb_off[v];
       a.scenes = s->d_scenes;
       a.status = s->d_status;
-      CWA_CUDA(launch_wave_block(a, s->n_wbtiles, s->stream));
-      s->launches += s->n_wbtiles > 0;
+      CWA_CUDA(launch_wave_block(a, n_tiles, v, s->stream));
+      s->launches += n_tiles > 0;
       s->uid[cur] = oc;
       s->uid[prev] = op;
       s->uid[nxt] = ic;
       s->uid[3] = ip;
-      done += kWaveK;
-      s->steps += kWaveK;
+      done += K;
+      s->steps += K;
     }
     for (int b = 0; b < 3; ++b) s->U[b] = s->UB[s->uid[b]];
     drop_graphs(s);  // captured steps hold the old buffer pointers
@@ -564,6 +576,7 @@ cwa_status graph_step(cwa_sim* s) {
   s->wcur = (s->wcur + 1) % 3;
   s->steps += 1;
   s->counts_pending = !s->verlet && s->n_ptiles > 0;
+  s->deposits_pending = false;  // the step ends with its wave pass
   return CWA_OK;
 }
 
@@ -641,6 +654,7 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
     return arg_error("nb_scan_minb and nb_force_minb must be 0..8");
   if (o.nb_threads != 0 && (o.nb_threads < 32 || o.nb_threads > 128 || (o.nb_threads & 31)))
     return arg_error("nb_threads must be 0 or a multiple of 32 in [32, 128]");
+  if (o.wave_block < 0 || o.wave_block >= CWA_WAVE_BLOCK_COUNT) return arg_error("unknown wave_block variant");
   std::vector<int32_t> dims(3 * (size_t)n_scenes);
   int64_t np = 0, nc = 0, nw = 0;
   int32_t nmax = 0;
@@ -1341,6 +1355,87 @@ cwa_status cwa_autotune(cwa_sim* s, int32_t trial_steps, cwa_tune_report* out) {
   if (out) *out = rep;
   CWA_CUDA(err);
   return CWA_OK;
+}
+
+// Wave tuner: every blocked variant from the same snapshot of the two live
+// wave slots (and the deposit buffer, when a pending integrate filled it),
+// trial_steps wave steps each (rounded up to a multiple of 8, so every
+// variant runs whole blocks), best of two rounds; keeps the fastest in
+// opt.wave_block and restores the state, the slot map included.
+cwa_status cwa_autotune_wave(cwa_sim* s, int32_t trial_steps, cwa_wave_tune_report* out) {
+  CWA_TRY(check_sim(s));
+  if (trial_steps < 1 || trial_steps > 4096) return arg_error("trial_steps must be in [1, 4096]");
+  const int32_t steps = (trial_steps + 7) & ~7;
+  CWA_TRY(prepare_wave_blocks(s));
+  CWA_CUDA(cudaStreamSynchronize(s->stream));
+  const size_t W = (size_t)s->w_total;
+  const int w0 = s->wcur;
+  int uid0[4];
+  for (int b = 0; b < 4; ++b) uid0[b] = s->uid[b];
+  float* live[2] = {s->U[w0], s->U[(w0 + 2) % 3]};
+  const bool dep0 = s->deposits_pending;
+  const int64_t steps0 = s->steps, launches0 = s->launches;
+  const int32_t entry = s->opt.wave_block;
+  char* snap = nullptr;
+  CWA_CUDA(cudaMalloc((void**)&snap, W * 16 + 256));
+  float* snap_u = reinterpret_cast<float*>(snap);
+  unsigned long long* snap_d = reinterpret_cast<unsigned long long*>(snap + W * 8);
+  auto copy_state = [&](bool save) -> cudaError_t {
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+      e = save ? cudaMemcpyAsync(snap_u + k * W, live[k], W * 4, cudaMemcpyDeviceToDevice, s->stream)
+               : cudaMemcpyAsync(live[k], snap_u + k * W, W * 4, cudaMemcpyDeviceToDevice, s->stream);
+    if (e == cudaSuccess && dep0)
+      e = save ? cudaMemcpyAsync(snap_d, s->D, W * 8, cudaMemcpyDeviceToDevice, s->stream)
+               : cudaMemcpyAsync(s->D, snap_d, W * 8, cudaMemcpyDeviceToDevice, s->stream);
+    for (int b = 0; b < 4; ++b) s->uid[b] = uid0[b];
+    for (int b = 0; b < 3; ++b) s->U[b] = s->UB[uid0[b]];
+    s->wcur = w0;
+    s->deposits_pending = dep0;
+    return e;
+  };
+  cwa_wave_tune_report rep;
+  memset(&rep, 0, sizeof(rep));
+  rep.steps = steps;
+  for (float& m : rep.ms_per_step) m = 1e30f;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t err = copy_state(true);
+  if (err == cudaSuccess) err = cudaEventCreate(&e0);
+  if (err == cudaSuccess) err = cudaEventCreate(&e1);
+  for (int round = 0; round < 2 && err == cudaSuccess; ++round)
+    for (int q = 0; q < CWA_WAVE_BLOCK_COUNT && err == cudaSuccess; ++q) {
+      const int v = round == 0 ? q : CWA_WAVE_BLOCK_COUNT - 1 - q;
+      s->opt.wave_block = v;
+      err = copy_state(false);
+      if (err != cudaSuccess) break;
+      // a pending deposit is applied by an untimed single pass first
+      if (dep0 && run_wave(s) != CWA_OK) err = cudaErrorLaunchFailure;
+      if (err == cudaSuccess && run_wave_advance(s, 8) != CWA_OK) err = cudaErrorLaunchFailure;  // warm-up
+      if (err == cudaSuccess) err = cudaEventRecord(e0, s->stream);
+      if (err == cudaSuccess && run_wave_advance(s, steps) != CWA_OK) err = cudaErrorLaunchFailure;
+      if (err == cudaSuccess) err = cudaEventRecord(e1, s->stream);
+      if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+      if (err == cudaSuccess) rep.ms_per_step[v] = std::min(rep.ms_per_step[v], ms / (float)steps);
+    }
+  rep.best = entry;
+  if (err == cudaSuccess)
+    for (int v = 0; v < CWA_WAVE_BLOCK_COUNT; ++v)
+      if (rep.ms_per_step[v] < rep.ms_per_step[rep.best]) rep.best = v;
+  s->opt.wave_block = rep.best;
+  cudaError_t e2 = copy_state(false);
+  if (err == cudaSuccess) err = e2;
+  cudaStreamSynchronize(s->stream);
+  s->steps = steps0;
+  s->launches = launches0;
+  drop_graphs(s);  // captured steps hold the trials' buffer pointers
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(snap);
+  if (out) *out = rep;
+  CWA_CUDA(err);
+  return read_status(s);
 }
 
 cwa_status cwa_get_options(cwa_sim* s, cwa_sim_options* out) {

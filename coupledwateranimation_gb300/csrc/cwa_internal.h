@@ -181,7 +181,10 @@ cudaError_t launch_totals(const float4* pos, const float4* vel, int32_t poff, in
                           const SceneDev* scenes, int32_t scene, double* out, cudaStream_t stream);
 
 // ---- temporally blocked wave advance (cwa_wave_tma.cu) ----
-constexpr int kWaveK = 4;  // wave steps per block launch (= halo width)
+// Block variants (box 128 x 32 / K 4, 128 x 64 / K 4, 128 x 64 / K 8): K wave
+// steps per launch, equal to the halo width.
+constexpr int kWaveVariants = 3;
+int wave_variant_steps(int variant);
 
 // One block tile: patch (bx, by) of a scene's field; tma = rows load by TMA.
 struct WaveBlockTile {
@@ -191,8 +194,8 @@ struct WaveBlockTile {
 struct WaveBlockArgs {
   const float* in_cur;           // u^n (all scenes, woff-offset inside)
   const float* in_prev;          // u^(n-1)
-  float* out_cur;                // receives u^(n+kWaveK)
-  float* out_prev;               // receives u^(n+kWaveK-1)
+  float* out_cur;                // receives u^(n+K)
+  float* out_prev;               // receives u^(n+K-1)
   const CUtensorMap* map_cur;    // per-scene tiled maps of in_cur / in_prev,
   const CUtensorMap* map_prev;   // in device memory
   const WaveBlockTile* tiles;
@@ -200,13 +203,12 @@ struct WaveBlockArgs {
   int32_t* status;
 };
 
-int wave_block_rows();
-int wave_block_cols();
-// Encodes the tiled map of one scene's field in one buffer; false when the
-// row width is not a multiple of 4 floats (those scenes load without TMA).
-bool wave_block_encode(CUtensorMap* map, float* base, int W, int H);
-void wave_block_tiles(const SceneDev& d, int32_t scene, bool tma, std::vector<WaveBlockTile>* out);
-cudaError_t launch_wave_block(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t stream);
+// Encodes the tiled map of one scene's field in one buffer for a variant's
+// box; false when the row width is not a multiple of 4 floats (those scenes
+// load without TMA).
+bool wave_block_encode(CUtensorMap* map, float* base, int W, int H, int variant);
+void wave_block_tiles(const SceneDev& d, int32_t scene, bool tma, int variant, std::vector<WaveBlockTile>* out);
+cudaError_t launch_wave_block(const WaveBlockArgs& a, int32_t n_tiles, int variant, cudaStream_t stream);
 
 // ---- headless rendering (cwa_render.cu) ----
 struct RenderMatrices {  // row-major 4x4

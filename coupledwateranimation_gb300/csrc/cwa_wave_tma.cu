@@ -1,26 +1,29 @@
 // cwa_wave_tma.cu — temporally blocked wave stencil over every scene.
 //
-// Advances the height fields kWaveK leapfrog steps per launch with no new
+// Advances the height fields K leapfrog steps per launch with no new
 // particle deposits: the stand-alone wave module's job (the reference's
 // StencilImage2DTripleBuffered driving wave_comp.glsl EvolveWave, :348-383,
 // one dispatch per step; the 2D wave demo Wave2DSimp/Wave2D_cs.glsl:78-84).
 //
 // One launch covers all scenes through a list of block tiles.  A block tile
-// owns a 120 x 24 patch of one scene's field and works on a 128 x 32 box:
-// the patch plus a kWaveK-cell halo.  Scenes whose row width is a multiple of
-// 4 cells load the box of u^n and u^(n-1) with two 2D TMA copies
-// (cp.async.bulk.tensor, completion counted on an mbarrier; the box's x
-// origin is patch_x - 4, a multiple of 4 floats = 16 bytes); other widths load
-// it with plain loads.  The kWaveK steps then run in shared memory — step s
-// is computed on the box shrunk by s cells, which is exactly the region whose
-// inputs are still exact — and the patch of u^(n+4) and u^(n+3) is stored
-// with coalesced writes into two buffers that no CTA of this launch reads.
-// DRAM traffic per cell-step drops from 12 bytes (single step: read u^n,
-// u^(n-1), write u^(n+1)) to about 4.9.
+// owns a (128 - 2K) x (BOX_H - 2K) patch of one scene's field and works on a
+// 128 x BOX_H box: the patch plus a K-cell halo.  Three variants exist
+// (BOX_H, K) = (32, 4), (64, 4), (64, 8); the wave tuner times them and keeps
+// the fastest.  Scenes whose row width is a multiple of 4 cells load the box
+// of u^n and u^(n-1) with two 2D TMA copies (cp.async.bulk.tensor, completion
+// counted on an mbarrier; the box's x origin is patch_x - K, a multiple of 4
+// floats = 16 bytes for K = 4 and 8); other widths load it with plain loads.
+// The K steps then run in shared memory — step s is computed on the box
+// shrunk by s cells, which is exactly the region whose inputs are still
+// exact — and the patch of u^(n+K) and u^(n+K-1) is stored with coalesced
+// writes into two buffers that no CTA of this launch reads.  DRAM traffic
+// per cell-step drops from 12 bytes (single step: read u^n, u^(n-1), write
+// u^(n+1)) to 16 x box / (K x patch) bytes: 4.9 for (32, 4), 4.1 for (64, 4),
+// 2.6 for (64, 8).
 //
 // Each cell runs the single-step kernel's operation sequence with the same
-// clamped (Neumann) neighbour indices, so one launch equals kWaveK single
-// wave passes bit for bit.  Box cells outside the domain (TMA zero fill) are
+// clamped (Neumann) neighbour indices, so one launch equals K single wave
+// passes bit for bit.  Box cells outside the domain (TMA zero fill) are
 // never read by an in-domain cell: neighbour indices clamp to the domain.
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -32,11 +35,13 @@
 namespace cwa {
 namespace {
 
-constexpr int kBoxW = 128, kBoxH = 32;          // box (x, y) in cells
-constexpr int kTileW = kBoxW - 2 * kWaveK;      // 120 output columns
-constexpr int kTileH = kBoxH - 2 * kWaveK;      // 24 output rows
+constexpr int kBoxW = 128;               // box width in cells
 constexpr int kWaveTmaThreads = kBoxW;  // one thread per box column
-constexpr uint32_t kBoxBytes = kBoxW * kBoxH * sizeof(float);
+
+// The block variants the tuner chooses from: box height and steps per launch
+// (= halo).  Output patch (128 - 2K) x (BOX_H - 2K).
+constexpr int kVarBoxH[kWaveVariants] = {32, 64, 64};
+constexpr int kVarK[kWaveVariants] = {4, 4, 8};
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
@@ -69,14 +74,20 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
+template <int kBoxH, int kK>
 __global__ void __launch_bounds__(kWaveTmaThreads)
     k_wave_block(WaveBlockArgs a) {
-  __shared__ __align__(128) float box[2][kBoxH][kBoxW];
-  __shared__ __align__(8) uint64_t bar;
+  constexpr int kTileW = kBoxW - 2 * kK, kTileH = kBoxH - 2 * kK;
+  constexpr uint32_t kBoxBytes = kBoxW * kBoxH * sizeof(float);
+  // Dynamic shared memory only, so the boxes start at the window's base
+  // (the TMA destinations want 128-byte alignment); the mbarrier follows them.
+  extern __shared__ __align__(128) float box_mem[];  // [2][kBoxH][kBoxW], then the barrier
+  float(*box)[kBoxH][kBoxW] = reinterpret_cast<float(*)[kBoxH][kBoxW]>(box_mem);
+  uint64_t& bar = *reinterpret_cast<uint64_t*>(box_mem + 2 * kBoxH * kBoxW);
   const WaveBlockTile t = a.tiles[blockIdx.x];
   const SceneDev* S = a.scenes + t.scene;
   const int W = S->nx, H = S->nz;
-  const int ox = t.bx * kTileW - kWaveK, oy = t.by * kTileH - kWaveK;  // box origin; ox % 4 == 0
+  const int ox = t.bx * kTileW - kK, oy = t.by * kTileH - kK;  // box origin; ox % 4 == 0
   if (t.tma) {
     const uint32_t b = smem_u32(&bar);
     if (threadIdx.x == 0) {
@@ -120,7 +131,7 @@ __global__ void __launch_bounds__(kWaveTmaThreads)
   const int le = gx + 1 < W ? lx + 1 : lx, lw = gx > 0 ? lx - 1 : lx;
   int c = 0;  // box[c] = u^t, box[c ^ 1] = u^(t-1), overwritten in place by u^(t+1)
 #pragma unroll 1
-  for (int s = 1; s <= kWaveK; ++s) {
+  for (int s = 1; s <= kK; ++s) {
     const float(*A)[kBoxW] = box[c];
     float(*B)[kBoxW] = box[c ^ 1];
     // rows whose inputs are still exact after s - 1 steps, inside the domain
@@ -148,9 +159,9 @@ __global__ void __launch_bounds__(kWaveTmaThreads)
   }
   float* oc = a.out_cur + S->woff;
   float* op = a.out_prev + S->woff;
-  if (lx >= kWaveK && lx < kBoxW - kWaveK && gx < W) {
-    const int r1 = min(kBoxH - kWaveK, H - oy);
-    for (int ly = kWaveK; ly < r1; ++ly) {
+  if (lx >= kK && lx < kBoxW - kK && gx < W) {
+    const int r1 = min(kBoxH - kK, H - oy);
+    for (int ly = kK; ly < r1; ++ly) {
       const size_t g = (size_t)(oy + ly) * W + gx;
       oc[g] = box[c][ly][lx];
       op[g] = box[c ^ 1][ly][lx];
@@ -175,32 +186,50 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 }  // namespace
 
-int wave_block_rows() { return kTileH; }
-int wave_block_cols() { return kTileW; }
+int wave_variant_steps(int v) { return kVarK[v]; }
 
-bool wave_block_encode(CUtensorMap* map, float* base, int W, int H) {
+bool wave_block_encode(CUtensorMap* map, float* base, int W, int H, int variant) {
   if (W < 1 || H < 1 || (W % 4) != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
   PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
   if (!fn) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
   const cuuint64_t strides[1] = {(cuuint64_t)W * sizeof(float)};
-  const cuuint32_t boxdim[2] = {kBoxW, kBoxH};
+  const cuuint32_t boxdim[2] = {kBoxW, (cuuint32_t)kVarBoxH[variant]};
   const cuuint32_t estr[2] = {1, 1};
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, boxdim, estr,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-void wave_block_tiles(const SceneDev& d, int32_t scene, bool tma, std::vector<WaveBlockTile>* out) {
-  const int nbx = (d.nx + kTileW - 1) / kTileW, nby = (d.nz + kTileH - 1) / kTileH;
+void wave_block_tiles(const SceneDev& d, int32_t scene, bool tma, int variant, std::vector<WaveBlockTile>* out) {
+  const int tw = kBoxW - 2 * kVarK[variant], th = kVarBoxH[variant] - 2 * kVarK[variant];
+  const int nbx = (d.nx + tw - 1) / tw, nby = (d.nz + th - 1) / th;
   for (int by = 0; by < nby; ++by)
     for (int bx = 0; bx < nbx; ++bx) out->push_back(WaveBlockTile{scene, bx, by, tma ? 1 : 0});
 }
 
-cudaError_t launch_wave_block(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t stream) {
-  if (n_tiles <= 0) return cudaSuccess;
-  k_wave_block<<<n_tiles, kWaveTmaThreads, 0, stream>>>(a);
+namespace {
+template <int kBoxH, int kK>
+cudaError_t launch_variant(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t stream) {
+  constexpr int bytes = 2 * kBoxH * kBoxW * (int)sizeof(float) + 16;
+  static bool raised = false;  // dynamic shared memory above 48 KB needs the opt-in
+  if (bytes > 48 * 1024 && !raised) {
+    cudaError_t e = cudaFuncSetAttribute(k_wave_block<kBoxH, kK>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    raised = true;
+  }
+  k_wave_block<kBoxH, kK><<<n_tiles, kWaveTmaThreads, bytes, stream>>>(a);
   return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_wave_block(const WaveBlockArgs& a, int32_t n_tiles, int variant, cudaStream_t stream) {
+  if (n_tiles <= 0) return cudaSuccess;
+  switch (variant) {
+    case 1: return launch_variant<64, 4>(a, n_tiles, stream);
+    case 2: return launch_variant<64, 8>(a, n_tiles, stream);
+    default: return launch_variant<32, 4>(a, n_tiles, stream);
+  }
 }
 
 }  // namespace cwa

@@ -38,7 +38,7 @@ class Sim:
 
     def __init__(self, scenes, precision: int = PREC_COMPENSATED, use_graph: bool = True,
                  device: int = 0, nb_threads: int = 0, nb_stage: int = 0, verlet_skin: float = 0.0,
-                 nb_scan_minb: int = 0, nb_force_minb: int = 0):
+                 nb_scan_minb: int = 0, nb_force_minb: int = 0, wave_block: int = 0):
         self._lib = _abi.load()
         if isinstance(scenes, SceneDesc):
             scenes = [scenes]
@@ -46,7 +46,7 @@ class Sim:
         arr = (SceneDesc * len(self.scenes))(*self.scenes)
         opt = SimOptions(device=device, precision=precision, use_graph=int(use_graph),
                          nb_threads=nb_threads, nb_stage=nb_stage, verlet_skin=verlet_skin,
-                         nb_scan_minb=nb_scan_minb, nb_force_minb=nb_force_minb)
+                         nb_scan_minb=nb_scan_minb, nb_force_minb=nb_force_minb, wave_block=wave_block)
         h = C.c_void_p()
         check(self._lib.cwa_create(C.byref(opt), arr, len(self.scenes), C.byref(h)), "cwa_create")
         self._h = h
@@ -157,7 +157,8 @@ class Sim:
         return out
 
     def wave_advance(self, n: int) -> None:
-        """n wave passes with no particle passes between them (4 per launch)."""
+        """n wave passes with no particle passes between them (K per launch,
+        K from the wave_block option)."""
         check(self._lib.cwa_wave_advance(self._h, int(n)), "cwa_wave_advance")
 
     def synchronize(self) -> None:
@@ -229,6 +230,14 @@ class Sim:
         n = min(r.n_tried, 32)
         return {"best": opt(r.best), "best_ms": r.best_ms, "entry_ms": r.entry_ms,
                 "tried": [dict(opt(r.tried[k]), ms=r.tried_ms[k]) for k in range(n)]}
+
+    def autotune_wave(self, trial_steps: int = 64) -> dict:
+        """Pick the fastest blocked wave-advance variant for this sim's wave
+        state (see cwa_autotune_wave); the state is restored afterwards."""
+        r = _abi.WaveTuneReport()
+        check(self._lib.cwa_autotune_wave(self._h, trial_steps, C.byref(r)), "cwa_autotune_wave")
+        return {"best": r.best, "best_name": _abi.WAVE_BLOCKS[r.best], "steps": r.steps,
+                "ms_per_step": dict(zip(_abi.WAVE_BLOCKS, list(r.ms_per_step)))}
 
     def options(self) -> dict:
         o = _abi.SimOptions()

@@ -117,8 +117,18 @@ typedef struct cwa_sim_options {
   int32_t nb_scan_minb;    /* density-scan kernel variant: min CTAs per SM
                               (4, 6, 8; 0 = 4)                              */
   int32_t nb_force_minb;   /* force kernel variant (6, 8; 0 = 8)              */
-  int32_t reserved[4];
+  int32_t wave_block;      /* blocked wave advance variant (CWA_WAVE_BLOCK_*)  */
+  int32_t reserved[3];
 } cwa_sim_options;
+
+/* Blocked wave advance variants: box of 128 x H cells advanced K steps per
+ * launch in shared memory. */
+enum {
+  CWA_WAVE_BLOCK_32x4 = 0, /* default: H 32, K 4 */
+  CWA_WAVE_BLOCK_64x4 = 1, /* H 64, K 4 */
+  CWA_WAVE_BLOCK_64x8 = 2, /* H 64, K 8 */
+  CWA_WAVE_BLOCK_COUNT = 3
+};
 
 /* Borrowed device pointers of one scene, all in the current sorted order.
  * pos/vel/force are float4 arrays; rho_p is float2 (rho, pressure);
@@ -233,9 +243,9 @@ cwa_status cwa_pass_wave(cwa_sim* sim);
  * StencilImage2DTripleBuffered.cpp:22-31 and wave_comp.glsl EvolveWave
  * :348-383, one dispatch per step).  Bit-identical to n_steps calls of
  * cwa_pass_wave; deposits pending from an integrate pass land in the first
- * step.  Steps run 4 at a time in shared memory (TMA-loaded tiles), so
- * device pointers of the wave buffers may change: re-read cwa_get_device_view
- * after it.  Asynchronous. */
+ * step.  Steps run K at a time in shared memory (TMA-loaded tiles; K from
+ * the sim's wave_block option), so device pointers of the wave buffers may
+ * change: re-read cwa_get_device_view after it.  Asynchronous. */
 cwa_status cwa_wave_advance(cwa_sim* sim, int32_t n_steps);
 /* Wait for the sim's stream; report a device-side status (timeout, NaN). */
 cwa_status cwa_synchronize(cwa_sim* sim);
@@ -283,6 +293,16 @@ typedef struct cwa_tune_report {
   float tried_ms[CWA_TUNE_MAX_TRIED];
 } cwa_tune_report;
 cwa_status cwa_autotune(cwa_sim* sim, int32_t trial_steps, cwa_tune_report* out);
+/* Times every blocked wave advance variant (CWA_WAVE_BLOCK_*) on the sim's
+ * current wave state, each from the same snapshot for trial_steps wave steps
+ * (rounded up to a multiple of 8, best of two rounds), keeps the fastest in
+ * the sim's wave_block option and restores the state. */
+typedef struct cwa_wave_tune_report {
+  int32_t best;                               /* CWA_WAVE_BLOCK_*          */
+  int32_t steps;                              /* timed wave steps / trial  */
+  float ms_per_step[CWA_WAVE_BLOCK_COUNT];
+} cwa_wave_tune_report;
+cwa_status cwa_autotune_wave(cwa_sim* sim, int32_t trial_steps, cwa_wave_tune_report* out);
 cwa_status cwa_get_options(cwa_sim* sim, cwa_sim_options* out);
 
 /* ---- stand-alone operators on caller-owned device buffers ----------------

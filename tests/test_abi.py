@@ -36,7 +36,8 @@ def test_struct_layouts_match_header(tmp_path):
     """ctypes mirrors of the ABI structs have the C compiler's size and offsets."""
     structs = {"cwa_scene_desc": _abi.SceneDesc, "cwa_sim_options": _abi.SimOptions,
                "cwa_device_view": _abi.DeviceView, "cwa_camera": _abi.Camera,
-               "cwa_render_params": _abi.RenderParams, "cwa_tune_report": _abi.TuneReport}
+               "cwa_render_params": _abi.RenderParams, "cwa_tune_report": _abi.TuneReport,
+               "cwa_wave_tune_report": _abi.WaveTuneReport}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{_abi.LIB_PATH.parent.parent}/include/cwa.h"',
              "int main(void) {"]
     for cname, py in structs.items():

@@ -1,6 +1,7 @@
-"""cwa_wave_advance: the temporally blocked wave stencil (4 steps per launch,
-TMA-loaded tiles) against single wave passes and the float32 oracle, bit for
-bit.  The wave module stepped alone is StencilImage2DTripleBuffered::Compute
+"""cwa_wave_advance: the temporally blocked wave stencil (K steps per launch
+in 128 x H boxes, TMA-loaded tiles; every (H, K) variant) against single wave
+passes and the float32 oracle, bit for bit, and the wave tuner.  The wave
+module stepped alone is StencilImage2DTripleBuffered::Compute
 (StencilImage2DTripleBuffered.cpp:22-31) over wave_comp.glsl EvolveWave
 (:348-383)."""
 from __future__ import annotations
@@ -49,21 +50,62 @@ def _compare(desc_list, load, n, pending=True, **kw):
 
 # widths: multiples of 4 take the TMA path, others the plain-load path;
 # sizes span one tile, ragged edges and several tiles in both directions
+@pytest.mark.parametrize("wave_block", [0, 1, 2])
 @pytest.mark.parametrize("wave", [(64, 64), (256, 200), (240, 48), (250, 130), (37, 5), (4, 1), (1, 3)])
-@pytest.mark.parametrize("n", [1, 4, 9, 14])
-def test_wave_advance_equals_single_passes(lib, wave, n):
+@pytest.mark.parametrize("n", [1, 4, 9, 14, 17])
+def test_wave_advance_equals_single_passes(lib, wave, n, wave_block):
     sc = small_muller((6, 6, 6), 0.03, wave, seed=5)
-    _compare([sc.desc], lambda s: load_scene(s, 0, sc), n)
+    _compare([sc.desc], lambda s: load_scene(s, 0, sc), n, wave_block=wave_block)
 
 
-def test_wave_advance_batched_mixed_widths(lib):
+@pytest.mark.parametrize("wave_block", [0, 1, 2])
+def test_wave_advance_batched_mixed_widths(lib, wave_block):
     scs = [small_muller((6, 6, 6), 0.03, w, seed=7 + i) for i, w in enumerate([(128, 96), (130, 77), (512, 24)])]
 
     def load(s):
         for k, sc in enumerate(scs):
             load_scene(s, k, sc)
 
-    _compare([sc.desc for sc in scs], load, 13)
+    _compare([sc.desc for sc in scs], load, 21, wave_block=wave_block)
+
+
+@pytest.mark.parametrize("pending", [False, True])
+def test_wave_tuner_keeps_state_and_picks_fastest(lib, pending):
+    # the tuner restores the wave state (and pending deposits) bit for bit;
+    # advancing with the chosen variant then equals single passes
+    sc = small_muller((6, 6, 6), 0.03, (500, 300), seed=11)
+    sims = [Sim(sc.desc), Sim(sc.desc)]
+    try:
+        for s in sims:
+            load_scene(s, 0, sc)
+            if pending:
+                _pending_deposits(s)
+            else:
+                s.step(2)
+        before = sims[0].download_wave(0), sims[0].step_count
+        rep = sims[0].autotune_wave(12)
+        assert rep["steps"] == 16
+        ms = rep["ms_per_step"]
+        assert set(ms) == {"32x4", "64x4", "64x8"} and all(0 < v < 1e3 for v in ms.values())
+        assert ms[rep["best_name"]] == min(ms.values())
+        assert sims[0].options()["wave_block"] == rep["best"]
+        after = sims[0].download_wave(0), sims[0].step_count
+        assert np.array_equal(bits(before[0][0]), bits(after[0][0]))
+        assert np.array_equal(bits(before[0][1]), bits(after[0][1]))
+        assert before[1] == after[1]
+        sims[0].wave_advance(19)
+        for _ in range(19):
+            sims[1].wave()
+        for s in sims:
+            s.step(2)
+            s.synchronize()
+        a, b = sims[0].download_wave(0), sims[1].download_wave(0)
+        assert np.array_equal(bits(a[0]), bits(b[0])) and np.array_equal(bits(a[1]), bits(b[1]))
+        pa, pb = sims[0].download_particles(0), sims[1].download_particles(0)
+        assert np.array_equal(pa.view(np.uint8), pb.view(np.uint8))
+    finally:
+        for s in sims:
+            s.close()
 
 
 def test_wave_advance_reference_line_source(lib):
@@ -118,11 +160,15 @@ def test_steps_after_wave_advance(lib, use_graph):
             s.close()
 
 
-def test_wave_advance_rejects_negative(lib):
+def test_wave_advance_rejects_bad_arguments(lib):
     from coupledwateranimation_gb300 import CwaError
 
     sc = small_muller((4, 4, 4), 0.03, (64, 64))
     with Sim(sc.desc) as sim:
         with pytest.raises(CwaError):
             sim.wave_advance(-1)
+        with pytest.raises(CwaError):
+            sim.autotune_wave(0)
         sim.wave_advance(0)
+    with pytest.raises(CwaError):
+        Sim(sc.desc, wave_block=3)
