@@ -63,7 +63,8 @@ class SimOptions(C.Structure):
                 ("reserved", C.c_int32 * 3)]
 
 
-WAVE_BLOCKS = ("32x4", "64x4", "64x8")  # CWA_WAVE_BLOCK_*: box rows x steps per launch
+# CWA_WAVE_BLOCK_*: box rows x steps per launch; R = box column in registers
+WAVE_BLOCKS = ("32x4", "64x4", "64x8", "R32x4", "R64x4", "R64x8")
 
 
 class WaveTuneReport(C.Structure):

@@ -40,8 +40,8 @@ constexpr int kWaveTmaThreads = kBoxW;  // one thread per box column
 
 // The block variants the tuner chooses from: box height and steps per launch
 // (= halo).  Output patch (128 - 2K) x (BOX_H - 2K).
-constexpr int kVarBoxH[kWaveVariants] = {32, 64, 64};
-constexpr int kVarK[kWaveVariants] = {4, 4, 8};
+constexpr int kVarBoxH[kWaveVariants] = {32, 64, 64, 32, 64, 64};
+constexpr int kVarK[kWaveVariants] = {4, 4, 8, 4, 4, 8};
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
@@ -72,6 +72,55 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       "[%4];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
       : "memory");
+}
+
+// The column walk of an interior box: every step's row range is a constant,
+// so the walks unroll completely and need no domain clamps (the box lies
+// inside the domain's rows).
+template <int kBoxH, int kK>
+__device__ __forceinline__ void walk_interior(float (*box)[kBoxH][kBoxW], int lx, int le, int lw, bool col_in,
+                                              float wa, float wb, float lam, float atten, bool coupled,
+                                              float zero_deposit) {
+#pragma unroll
+  for (int s = 1; s <= kK; ++s) {
+    const float(*A)[kBoxW] = box[(s - 1) & 1];
+    float(*B)[kBoxW] = box[s & 1];
+    if (col_in && lx >= s && lx < kBoxW - s) {
+      float south = A[s - 1][lx];
+      float mid = A[s][lx];
+#pragma unroll
+      for (int ly = s; ly < kBoxH - s; ++ly) {
+        const float north = A[ly + 1][lx];
+        const float nb = fadd(fadd(north, south), fadd(A[ly][le], A[ly][lw]));
+        float w = fadd(fmul(wa, mid), fmul(lam, nb));
+        w = fsub(w, fmul(wb, B[ly][lx]));
+        w = fmul(atten, w);
+        if (coupled) w = fadd(w, zero_deposit);
+        B[ly][lx] = w;
+        south = mid;
+        mid = north;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Stores the patch of u^(n+K) (box[0]; K is even) and u^(n+K-1) (box[1]).
+template <int kBoxH, int kK>
+__device__ __forceinline__ void store_patch(const WaveBlockArgs& a, const SceneDev* S, float (*box)[kBoxH][kBoxW],
+                                            int oy, int gx, int W, int H) {
+  static_assert(kK % 2 == 0, "u^(n+K) lands in box[0] for even K");
+  const int lx = threadIdx.x;
+  float* oc = a.out_cur + S->woff;
+  float* op = a.out_prev + S->woff;
+  if (lx >= kK && lx < kBoxW - kK && gx < W) {
+    const int r1 = min(kBoxH - kK, H - oy);
+    for (int ly = kK; ly < r1; ++ly) {
+      const size_t g = (size_t)(oy + ly) * W + gx;
+      oc[g] = box[0][ly][lx];
+      op[g] = box[1][ly][lx];
+    }
+  }
 }
 
 template <int kBoxH, int kK>
@@ -129,6 +178,13 @@ __global__ void __launch_bounds__(kWaveTmaThreads)
   const bool src_col = S->line_source && gx == W / 2;
   const bool col_in = gx >= 0 && gx < W;
   const int le = gx + 1 < W ? lx + 1 : lx, lw = gx > 0 ? lx - 1 : lx;
+  // Interior boxes (inside the domain's rows, no line-source column) take
+  // the unrolled walk without row clamps.
+  if (!(oy < 0 || oy + kBoxH > H || (S->line_source && W / 2 >= ox && W / 2 < ox + kBoxW))) {
+    walk_interior<kBoxH, kK>(box, lx, le, lw, col_in, wa, wb, lam, atten, coupled, zero_deposit);
+    store_patch<kBoxH, kK>(a, S, box, oy, gx, W, H);
+    return;
+  }
   int c = 0;  // box[c] = u^t, box[c ^ 1] = u^(t-1), overwritten in place by u^(t+1)
 #pragma unroll 1
   for (int s = 1; s <= kK; ++s) {
@@ -157,14 +213,137 @@ __global__ void __launch_bounds__(kWaveTmaThreads)
     __syncthreads();
     c ^= 1;
   }
+  store_patch<kBoxH, kK>(a, S, box, oy, gx, W, H);  // K even: box[0] = u^(n+K)
+}
+
+// Register-column form of the same block: each thread keeps its box column
+// of u^t and u^(t-1) in registers (rows fully unrolled), so a cell update
+// reads only its east and west neighbours from shared memory and writes its
+// own new value there for the neighbours' next step: 2 loads + 1 store per
+// cell-step instead of 4 + 1.  Every box cell is updated every step (the
+// invalid rim grows by one cell per step and is never stored); neighbour
+// indices clamp at the domain border exactly as the single pass does and at
+// the box border, where the values are outside the stored patch anyway.
+// kEdge = false is the interior form: the box lies inside the domain's rows
+// (no north / south clamp) and holds no line-source column.
+template <int kBoxH, bool kEdge>
+__device__ __forceinline__ void reg_step(const float (&cu)[kBoxH], float (&pv)[kBoxH], const float (*src)[kBoxW],
+                                         float (*dst)[kBoxW], int lx, int le, int lw, int ytop, int ybot,
+                                         float wa, float wb, float lam, float atten, bool src_col, bool coupled,
+                                         float zero_deposit) {
+#pragma unroll
+  for (int ly = 0; ly < kBoxH; ++ly) {
+    const float mid = cu[ly];
+    float north = ly + 1 < kBoxH ? cu[ly + 1 < kBoxH ? ly + 1 : ly] : mid;
+    float south = ly > 0 ? cu[ly > 0 ? ly - 1 : 0] : mid;
+    if (kEdge) {
+      if (ly + 1 >= ytop) north = mid;
+      if (ly <= ybot) south = mid;
+    }
+    const float nb = fadd(fadd(north, south), fadd(src[ly][le], src[ly][lw]));
+    float w = fadd(fmul(wa, mid), fmul(lam, nb));
+    w = fsub(w, fmul(wb, pv[ly]));
+    w = fmul(atten, w);
+    if (kEdge && src_col && w > 0.0001f) w = fadd(w, 0.001f);
+    if (coupled) w = fadd(w, zero_deposit);
+    pv[ly] = w;
+    dst[ly][lx] = w;
+  }
+}
+
+template <int kBoxH, int kK, bool kEdge>
+__device__ __forceinline__ void reg_steps(float (&cu)[kBoxH], float (&pv)[kBoxH], float (*b0)[kBoxW],
+                                          float (*b1)[kBoxW], int lx, int le, int lw, int ytop, int ybot, float wa,
+                                          float wb, float lam, float atten, bool src_col, bool coupled,
+                                          float zero_deposit) {
+#pragma unroll 1
+  for (int s = 0; s < kK; s += 2) {
+    reg_step<kBoxH, kEdge>(cu, pv, b0, b1, lx, le, lw, ytop, ybot, wa, wb, lam, atten, src_col, coupled,
+                           zero_deposit);
+    __syncthreads();
+    reg_step<kBoxH, kEdge>(pv, cu, b1, b0, lx, le, lw, ytop, ybot, wa, wb, lam, atten, src_col, coupled,
+                           zero_deposit);
+    __syncthreads();
+  }
+}
+
+template <int kBoxH, int kK>
+__global__ void __launch_bounds__(kWaveTmaThreads)
+    k_wave_reg(WaveBlockArgs a) {
+  static_assert(kK % 2 == 0, "steps run in pairs");
+  constexpr int kTileW = kBoxW - 2 * kK, kTileH = kBoxH - 2 * kK;
+  constexpr uint32_t kBoxBytes = kBoxW * kBoxH * sizeof(float);
+  extern __shared__ __align__(128) float box_mem[];  // [2][kBoxH][kBoxW], then the barrier
+  float(*box)[kBoxH][kBoxW] = reinterpret_cast<float(*)[kBoxH][kBoxW]>(box_mem);
+  uint64_t& bar = *reinterpret_cast<uint64_t*>(box_mem + 2 * kBoxH * kBoxW);
+  const WaveBlockTile t = a.tiles[blockIdx.x];
+  const SceneDev* S = a.scenes + t.scene;
+  const int W = S->nx, H = S->nz;
+  const int ox = t.bx * kTileW - kK, oy = t.by * kTileH - kK;  // box origin; ox % 4 == 0
+  const int lx = threadIdx.x, gx = ox + lx;
+  if (t.tma) {
+    const uint32_t b = smem_u32(&bar);
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(2 * kBoxBytes)
+                   : "memory");
+      tma_load_2d(smem_u32(&box[0][0][0]), a.map_cur + t.scene, ox, oy, b);
+      tma_load_2d(smem_u32(&box[1][0][0]), a.map_prev + t.scene, ox, oy, b);
+    }
+    if (!bar_wait_bounded(b)) {
+      if (threadIdx.x == 0) atomicOr(a.status, kStatusTimeout);
+      bar_wait_bounded(b);  // give copies still in flight a chance to land before the CTA exits
+      return;
+    }
+  } else {
+    const float* uc = a.in_cur + S->woff;
+    const float* up = a.in_prev + S->woff;
+    for (int ly = 0; ly < kBoxH; ++ly) {
+      const int gy = oy + ly;
+      const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
+      box[0][ly][lx] = in ? __ldg(uc + (size_t)gy * W + gx) : 0.0f;
+      box[1][ly][lx] = in ? __ldg(up + (size_t)gy * W + gx) : 0.0f;
+    }
+    __syncthreads();
+  }
+  float cu[kBoxH], pv[kBoxH];
+#pragma unroll
+  for (int ly = 0; ly < kBoxH; ++ly) {
+    cu[ly] = box[0][ly][lx];
+    pv[ly] = box[1][ly][lx];
+  }
+  __syncthreads();  // box[1] is overwritten by the first step
+  const float wa = S->wa, wb = S->wb, lam = S->lam, atten = S->atten;
+  const bool coupled = S->coupled != 0;
+  const float zero_deposit = coupled ? fmul(S->gain, fmul(0.0f, S->dq)) : 0.0f;
+  const bool src_col = S->line_source && gx == W / 2;
+  // east / west: the neighbour column inside the domain and the box, else the
+  // column itself (the single pass's clamp at the domain border)
+  const int le = (gx + 1 < W && lx + 1 < kBoxW) ? lx + 1 : lx;
+  const int lw = (gx > 0 && lx > 0) ? lx - 1 : lx;
+  const int ytop = H - oy, ybot = -oy;  // local rows in the domain: (ybot - 1, ytop)
+  const bool edge = oy < 0 || oy + kBoxH > H || (S->line_source && W / 2 >= ox && W / 2 < ox + kBoxW);
+  if (edge)
+    reg_steps<kBoxH, kK, true>(cu, pv, box[0], box[1], lx, le, lw, ytop, ybot, wa, wb, lam, atten, src_col, coupled,
+                               zero_deposit);
+  else
+    reg_steps<kBoxH, kK, false>(cu, pv, box[0], box[1], lx, le, lw, ytop, ybot, wa, wb, lam, atten, src_col,
+                                coupled, zero_deposit);
+  // cu = u^(n+K), pv = u^(n+K-1)
   float* oc = a.out_cur + S->woff;
   float* op = a.out_prev + S->woff;
   if (lx >= kK && lx < kBoxW - kK && gx < W) {
-    const int r1 = min(kBoxH - kK, H - oy);
-    for (int ly = kK; ly < r1; ++ly) {
-      const size_t g = (size_t)(oy + ly) * W + gx;
-      oc[g] = box[c][ly][lx];
-      op[g] = box[c ^ 1][ly][lx];
+#pragma unroll
+    for (int ly = kK; ly < kBoxH - kK; ++ly) {
+      if (ly < ytop) {
+        const size_t g = (size_t)(oy + ly) * W + gx;
+        oc[g] = cu[ly];
+        op[g] = pv[ly];
+      }
     }
   }
 }
@@ -209,16 +388,17 @@ void wave_block_tiles(const SceneDev& d, int32_t scene, bool tma, int variant, s
 }
 
 namespace {
-template <int kBoxH, int kK>
+template <int kBoxH, int kK, bool kReg>
 cudaError_t launch_variant(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t stream) {
   constexpr int bytes = 2 * kBoxH * kBoxW * (int)sizeof(float) + 16;
+  auto kern = kReg ? k_wave_reg<kBoxH, kK> : k_wave_block<kBoxH, kK>;
   static bool raised = false;  // dynamic shared memory above 48 KB needs the opt-in
   if (bytes > 48 * 1024 && !raised) {
-    cudaError_t e = cudaFuncSetAttribute(k_wave_block<kBoxH, kK>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
     raised = true;
   }
-  k_wave_block<kBoxH, kK><<<n_tiles, kWaveTmaThreads, bytes, stream>>>(a);
+  kern<<<n_tiles, kWaveTmaThreads, bytes, stream>>>(a);
   return cudaGetLastError();
 }
 }  // namespace
@@ -226,9 +406,12 @@ cudaError_t launch_variant(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t
 cudaError_t launch_wave_block(const WaveBlockArgs& a, int32_t n_tiles, int variant, cudaStream_t stream) {
   if (n_tiles <= 0) return cudaSuccess;
   switch (variant) {
-    case 1: return launch_variant<64, 4>(a, n_tiles, stream);
-    case 2: return launch_variant<64, 8>(a, n_tiles, stream);
-    default: return launch_variant<32, 4>(a, n_tiles, stream);
+    case 1: return launch_variant<64, 4, false>(a, n_tiles, stream);
+    case 2: return launch_variant<64, 8, false>(a, n_tiles, stream);
+    case 3: return launch_variant<32, 4, true>(a, n_tiles, stream);
+    case 4: return launch_variant<64, 4, true>(a, n_tiles, stream);
+    case 5: return launch_variant<64, 8, true>(a, n_tiles, stream);
+    default: return launch_variant<32, 4, false>(a, n_tiles, stream);
   }
 }
 

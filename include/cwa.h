@@ -122,12 +122,17 @@ typedef struct cwa_sim_options {
 } cwa_sim_options;
 
 /* Blocked wave advance variants: box of 128 x H cells advanced K steps per
- * launch in shared memory. */
+ * launch in shared memory; the R variants hold each thread's box column in
+ * registers and exchange only the east / west neighbours through shared
+ * memory. */
 enum {
-  CWA_WAVE_BLOCK_32x4 = 0, /* default: H 32, K 4 */
-  CWA_WAVE_BLOCK_64x4 = 1, /* H 64, K 4 */
-  CWA_WAVE_BLOCK_64x8 = 2, /* H 64, K 8 */
-  CWA_WAVE_BLOCK_COUNT = 3
+  CWA_WAVE_BLOCK_32x4 = 0,  /* default: H 32, K 4 */
+  CWA_WAVE_BLOCK_64x4 = 1,  /* H 64, K 4 */
+  CWA_WAVE_BLOCK_64x8 = 2,  /* H 64, K 8 */
+  CWA_WAVE_BLOCK_R32x4 = 3, /* registers, H 32, K 4 */
+  CWA_WAVE_BLOCK_R64x4 = 4, /* registers, H 64, K 4 */
+  CWA_WAVE_BLOCK_R64x8 = 5, /* registers, H 64, K 8 */
+  CWA_WAVE_BLOCK_COUNT = 6
 };
 
 /* Borrowed device pointers of one scene, all in the current sorted order.

@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from coupledwateranimation_gb300 import Sim
+from coupledwateranimation_gb300._abi import WAVE_BLOCKS
 
 from _helpers import bits, load_scene, small_muller, small_reference
 
@@ -50,7 +51,7 @@ def _compare(desc_list, load, n, pending=True, **kw):
 
 # widths: multiples of 4 take the TMA path, others the plain-load path;
 # sizes span one tile, ragged edges and several tiles in both directions
-@pytest.mark.parametrize("wave_block", [0, 1, 2])
+@pytest.mark.parametrize("wave_block", range(len(WAVE_BLOCKS)))
 @pytest.mark.parametrize("wave", [(64, 64), (256, 200), (240, 48), (250, 130), (37, 5), (4, 1), (1, 3)])
 @pytest.mark.parametrize("n", [1, 4, 9, 14, 17])
 def test_wave_advance_equals_single_passes(lib, wave, n, wave_block):
@@ -58,7 +59,7 @@ def test_wave_advance_equals_single_passes(lib, wave, n, wave_block):
     _compare([sc.desc], lambda s: load_scene(s, 0, sc), n, wave_block=wave_block)
 
 
-@pytest.mark.parametrize("wave_block", [0, 1, 2])
+@pytest.mark.parametrize("wave_block", range(len(WAVE_BLOCKS)))
 def test_wave_advance_batched_mixed_widths(lib, wave_block):
     scs = [small_muller((6, 6, 6), 0.03, w, seed=7 + i) for i, w in enumerate([(128, 96), (130, 77), (512, 24)])]
 
@@ -86,7 +87,7 @@ def test_wave_tuner_keeps_state_and_picks_fastest(lib, pending):
         rep = sims[0].autotune_wave(12)
         assert rep["steps"] == 16
         ms = rep["ms_per_step"]
-        assert set(ms) == {"32x4", "64x4", "64x8"} and all(0 < v < 1e3 for v in ms.values())
+        assert set(ms) == set(WAVE_BLOCKS) and all(0 < v < 1e3 for v in ms.values())
         assert ms[rep["best_name"]] == min(ms.values())
         assert sims[0].options()["wave_block"] == rep["best"]
         after = sims[0].download_wave(0), sims[0].step_count
@@ -118,6 +119,23 @@ def test_wave_advance_reference_line_source(lib):
         s.wave_reinit(0)
 
     _compare([sc.desc], load, 12, pending=False)
+
+
+@pytest.mark.parametrize("wave_block", range(len(WAVE_BLOCKS)))
+@pytest.mark.parametrize("wave_mode", [0.0, 0.5])
+def test_wave_advance_uncoupled_interior_boxes(lib, wave_block, wave_mode):
+    # an uncoupled scene large enough for interior boxes (no row clamps), with
+    # and without the line-source column
+    sc = small_reference(640)
+    sc.desc.wave_mode = wave_mode
+    sc.desc.wave_nx, sc.desc.wave_nz = 372, 300
+
+    def load(s):
+        s.upload_particles(0, sc.particles)
+        s.wave_reinit(0)
+        s.wave_advance(3)  # a non-trivial field first (single passes)
+
+    _compare([sc.desc], load, 24, pending=False, wave_block=wave_block)
 
 
 def test_wave_advance_matches_oracle(lib, orc):
@@ -171,4 +189,4 @@ def test_wave_advance_rejects_bad_arguments(lib):
             sim.autotune_wave(0)
         sim.wave_advance(0)
     with pytest.raises(CwaError):
-        Sim(sc.desc, wave_block=3)
+        Sim(sc.desc, wave_block=len(WAVE_BLOCKS))
