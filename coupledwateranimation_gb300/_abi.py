@@ -63,8 +63,9 @@ class SimOptions(C.Structure):
                 ("reserved", C.c_int32 * 3)]
 
 
-# CWA_WAVE_BLOCK_*: box rows x steps per launch; R = box column in registers
-WAVE_BLOCKS = ("32x4", "64x4", "64x8", "R32x4", "R64x4", "R64x8")
+# CWA_WAVE_BLOCK_*: box rows x steps per launch; R = box column in registers,
+# P = 256-wide box with column pairs in registers
+WAVE_BLOCKS = ("32x4", "64x4", "64x8", "R32x4", "R64x4", "R64x8", "P32x4")
 
 
 class WaveTuneReport(C.Structure):

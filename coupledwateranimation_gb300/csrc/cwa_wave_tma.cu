@@ -40,8 +40,9 @@ constexpr int kWaveTmaThreads = kBoxW;  // one thread per box column
 
 // The block variants the tuner chooses from: box height and steps per launch
 // (= halo).  Output patch (128 - 2K) x (BOX_H - 2K).
-constexpr int kVarBoxH[kWaveVariants] = {32, 64, 64, 32, 64, 64};
-constexpr int kVarK[kWaveVariants] = {4, 4, 8, 4, 4, 8};
+constexpr int kVarBoxW[kWaveVariants] = {128, 128, 128, 128, 128, 128, 256};
+constexpr int kVarBoxH[kWaveVariants] = {32, 64, 64, 32, 64, 64, 32};
+constexpr int kVarK[kWaveVariants] = {4, 4, 8, 4, 4, 8, 4};
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
@@ -72,6 +73,50 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       "[%4];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
       : "memory");
+}
+
+// Loads the box of u^n (box 0) and u^(n-1) (box 1) at origin (ox, oy): two
+// TMA copies counted on the mbarrier, or plain loads with zero fill outside
+// the domain.  Returns false (after flagging a timeout) when the copies do
+// not land within the bounded wait; the caller's CTA then exits.
+template <int kBoxH, int kBW>
+__device__ __forceinline__ bool load_box(const WaveBlockArgs& a, const WaveBlockTile& t, const SceneDev* S,
+                                         float (*box)[kBoxH][kBW], uint64_t& bar, int ox, int oy) {
+  const int W = S->nx, H = S->nz;
+  if (t.tma) {
+    constexpr uint32_t kBoxBytes = kBW * kBoxH * sizeof(float);
+    const uint32_t b = smem_u32(&bar);
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(2 * kBoxBytes)
+                   : "memory");
+      tma_load_2d(smem_u32(&box[0][0][0]), a.map_cur + t.scene, ox, oy, b);
+      tma_load_2d(smem_u32(&box[1][0][0]), a.map_prev + t.scene, ox, oy, b);
+    }
+    if (!bar_wait_bounded(b)) {
+      if (threadIdx.x == 0) atomicOr(a.status, kStatusTimeout);
+      bar_wait_bounded(b);  // give copies still in flight a chance to land before the CTA exits
+      return false;
+    }
+  } else {
+    const float* uc = a.in_cur + S->woff;
+    const float* up = a.in_prev + S->woff;
+    for (int lx = threadIdx.x; lx < kBW; lx += kWaveTmaThreads) {
+      const int gx = ox + lx;
+      for (int ly = 0; ly < kBoxH; ++ly) {
+        const int gy = oy + ly;
+        const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
+        box[0][ly][lx] = in ? __ldg(uc + (size_t)gy * W + gx) : 0.0f;
+        box[1][ly][lx] = in ? __ldg(up + (size_t)gy * W + gx) : 0.0f;
+      }
+    }
+    __syncthreads();
+  }
+  return true;
 }
 
 // The column walk of an interior box: every step's row range is a constant,
@@ -127,7 +172,6 @@ template <int kBoxH, int kK>
 __global__ void __launch_bounds__(kWaveTmaThreads)
     k_wave_block(WaveBlockArgs a) {
   constexpr int kTileW = kBoxW - 2 * kK, kTileH = kBoxH - 2 * kK;
-  constexpr uint32_t kBoxBytes = kBoxW * kBoxH * sizeof(float);
   // Dynamic shared memory only, so the boxes start at the window's base
   // (the TMA destinations want 128-byte alignment); the mbarrier follows them.
   extern __shared__ __align__(128) float box_mem[];  // [2][kBoxH][kBoxW], then the barrier
@@ -137,36 +181,7 @@ __global__ void __launch_bounds__(kWaveTmaThreads)
   const SceneDev* S = a.scenes + t.scene;
   const int W = S->nx, H = S->nz;
   const int ox = t.bx * kTileW - kK, oy = t.by * kTileH - kK;  // box origin; ox % 4 == 0
-  if (t.tma) {
-    const uint32_t b = smem_u32(&bar);
-    if (threadIdx.x == 0) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(2 * kBoxBytes)
-                   : "memory");
-      tma_load_2d(smem_u32(&box[0][0][0]), a.map_cur + t.scene, ox, oy, b);
-      tma_load_2d(smem_u32(&box[1][0][0]), a.map_prev + t.scene, ox, oy, b);
-    }
-    if (!bar_wait_bounded(b)) {
-      if (threadIdx.x == 0) atomicOr(a.status, kStatusTimeout);
-      bar_wait_bounded(b);  // give copies still in flight a chance to land before the CTA exits
-      return;
-    }
-  } else {
-    const float* uc = a.in_cur + S->woff;
-    const float* up = a.in_prev + S->woff;
-    const int lx = threadIdx.x, gx = ox + lx;
-    for (int ly = 0; ly < kBoxH; ++ly) {
-      const int gy = oy + ly;
-      const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
-      box[0][ly][lx] = in ? __ldg(uc + (size_t)gy * W + gx) : 0.0f;
-      box[1][ly][lx] = in ? __ldg(up + (size_t)gy * W + gx) : 0.0f;
-    }
-    __syncthreads();
-  }
+  if (!load_box<kBoxH, kBoxW>(a, t, S, box, bar, ox, oy)) return;
   // Each thread owns one box column and walks it top to bottom with the
   // column's north / centre / south values in registers; east and west come
   // from the neighbouring columns in shared memory.  Domain borders clamp
@@ -272,7 +287,6 @@ __global__ void __launch_bounds__(kWaveTmaThreads)
     k_wave_reg(WaveBlockArgs a) {
   static_assert(kK % 2 == 0, "steps run in pairs");
   constexpr int kTileW = kBoxW - 2 * kK, kTileH = kBoxH - 2 * kK;
-  constexpr uint32_t kBoxBytes = kBoxW * kBoxH * sizeof(float);
   extern __shared__ __align__(128) float box_mem[];  // [2][kBoxH][kBoxW], then the barrier
   float(*box)[kBoxH][kBoxW] = reinterpret_cast<float(*)[kBoxH][kBoxW]>(box_mem);
   uint64_t& bar = *reinterpret_cast<uint64_t*>(box_mem + 2 * kBoxH * kBoxW);
@@ -281,35 +295,7 @@ __global__ void __launch_bounds__(kWaveTmaThreads)
   const int W = S->nx, H = S->nz;
   const int ox = t.bx * kTileW - kK, oy = t.by * kTileH - kK;  // box origin; ox % 4 == 0
   const int lx = threadIdx.x, gx = ox + lx;
-  if (t.tma) {
-    const uint32_t b = smem_u32(&bar);
-    if (threadIdx.x == 0) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(2 * kBoxBytes)
-                   : "memory");
-      tma_load_2d(smem_u32(&box[0][0][0]), a.map_cur + t.scene, ox, oy, b);
-      tma_load_2d(smem_u32(&box[1][0][0]), a.map_prev + t.scene, ox, oy, b);
-    }
-    if (!bar_wait_bounded(b)) {
-      if (threadIdx.x == 0) atomicOr(a.status, kStatusTimeout);
-      bar_wait_bounded(b);  // give copies still in flight a chance to land before the CTA exits
-      return;
-    }
-  } else {
-    const float* uc = a.in_cur + S->woff;
-    const float* up = a.in_prev + S->woff;
-    for (int ly = 0; ly < kBoxH; ++ly) {
-      const int gy = oy + ly;
-      const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
-      box[0][ly][lx] = in ? __ldg(uc + (size_t)gy * W + gx) : 0.0f;
-      box[1][ly][lx] = in ? __ldg(up + (size_t)gy * W + gx) : 0.0f;
-    }
-    __syncthreads();
-  }
+  if (!load_box<kBoxH, kBoxW>(a, t, S, box, bar, ox, oy)) return;
   float cu[kBoxH], pv[kBoxH];
 #pragma unroll
   for (int ly = 0; ly < kBoxH; ++ly) {
@@ -348,6 +334,170 @@ __global__ void __launch_bounds__(kWaveTmaThreads)
   }
 }
 
+// Column-pair form: a 256 x kBoxH box, each of the 128 threads holding two
+// adjacent columns (2t, 2t+1) of u^t and u^(t-1) in registers.  Inside the
+// pair the east / west neighbours are registers; across pairs a thread reads
+// the right column of thread t-1 and the left column of thread t+1 from two
+// exchange arrays, written once per row and side.  A cell-step costs one
+// shared-memory access (the shared walk: 5, the one-column register form:
+// 3).  The exchange arrays reuse the boxes' shared memory once the columns
+// are in registers.
+constexpr int kPairW = 2 * kWaveTmaThreads;
+
+struct PairCtx {
+  int th, tw, te;             // this thread, the thread west / east of it
+  bool self_w, self_e, pair_in;  // domain clamps of column 2t's west, 2t+1's east, 2t's east
+  int ytop, ybot;
+  float wa, wb, lam, atten, zero_deposit;
+  bool src0, src1, coupled;
+};
+
+template <int kBoxH, bool kEdge>
+__device__ __forceinline__ void pair_step(const float (&c0)[kBoxH], const float (&c1)[kBoxH], float (&p0)[kBoxH],
+                                          float (&p1)[kBoxH], const float (*sl)[kWaveTmaThreads],
+                                          const float (*sr)[kWaveTmaThreads], float (*dl)[kWaveTmaThreads],
+                                          float (*dr)[kWaveTmaThreads], const PairCtx& c) {
+#pragma unroll
+  for (int ly = 0; ly < kBoxH; ++ly) {
+    const float m0 = c0[ly], m1 = c1[ly];
+    float n0 = ly + 1 < kBoxH ? c0[ly + 1 < kBoxH ? ly + 1 : ly] : m0;
+    float n1 = ly + 1 < kBoxH ? c1[ly + 1 < kBoxH ? ly + 1 : ly] : m1;
+    float s0 = ly > 0 ? c0[ly > 0 ? ly - 1 : 0] : m0;
+    float s1 = ly > 0 ? c1[ly > 0 ? ly - 1 : 0] : m1;
+    float w0 = sr[ly][c.tw];  // column 2t - 1
+    float e1 = sl[ly][c.te];  // column 2t + 2
+    float e0 = m1, w1 = m0;
+    if (kEdge) {
+      if (ly + 1 >= c.ytop) {
+        n0 = m0;
+        n1 = m1;
+      }
+      if (ly <= c.ybot) {
+        s0 = m0;
+        s1 = m1;
+      }
+      if (c.self_w) w0 = m0;
+      if (c.self_e) e1 = m1;
+      if (!c.pair_in) e0 = m0;
+    }
+    const float nb0 = fadd(fadd(n0, s0), fadd(e0, w0));
+    const float nb1 = fadd(fadd(n1, s1), fadd(e1, w1));
+    float u0 = fadd(fmul(c.wa, m0), fmul(c.lam, nb0));
+    float u1 = fadd(fmul(c.wa, m1), fmul(c.lam, nb1));
+    u0 = fmul(c.atten, fsub(u0, fmul(c.wb, p0[ly])));
+    u1 = fmul(c.atten, fsub(u1, fmul(c.wb, p1[ly])));
+    if (kEdge) {
+      if (c.src0 && u0 > 0.0001f) u0 = fadd(u0, 0.001f);
+      if (c.src1 && u1 > 0.0001f) u1 = fadd(u1, 0.001f);
+    }
+    if (c.coupled) {
+      u0 = fadd(u0, c.zero_deposit);
+      u1 = fadd(u1, c.zero_deposit);
+    }
+    p0[ly] = u0;
+    p1[ly] = u1;
+    dl[ly][c.th] = u0;
+    dr[ly][c.th] = u1;
+  }
+}
+
+template <int kBoxH, int kK, bool kEdge>
+__device__ __forceinline__ void pair_steps(float (&c0)[kBoxH], float (&c1)[kBoxH], float (&p0)[kBoxH],
+                                           float (&p1)[kBoxH], float (*ex)[2][kBoxH][kWaveTmaThreads],
+                                           const PairCtx& c) {
+#pragma unroll 1
+  for (int s = 0; s < kK; s += 2) {
+    pair_step<kBoxH, kEdge>(c0, c1, p0, p1, ex[0][0], ex[0][1], ex[1][0], ex[1][1], c);
+    __syncthreads();
+    pair_step<kBoxH, kEdge>(p0, p1, c0, c1, ex[1][0], ex[1][1], ex[0][0], ex[0][1], c);
+    __syncthreads();
+  }
+}
+
+template <int kBoxH, int kK>
+__global__ void __launch_bounds__(kWaveTmaThreads)
+    k_wave_pair(WaveBlockArgs a) {
+  static_assert(kK % 2 == 0, "steps run in pairs");
+  constexpr int kTileW = kPairW - 2 * kK, kTileH = kBoxH - 2 * kK;
+  extern __shared__ __align__(128) float box_mem[];  // [2][kBoxH][kPairW], then the barrier
+  float(*box)[kBoxH][kPairW] = reinterpret_cast<float(*)[kBoxH][kPairW]>(box_mem);
+  uint64_t& bar = *reinterpret_cast<uint64_t*>(box_mem + 2 * kBoxH * kPairW);
+  const WaveBlockTile t = a.tiles[blockIdx.x];
+  const SceneDev* S = a.scenes + t.scene;
+  const int W = S->nx, H = S->nz;
+  const int ox = t.bx * kTileW - kK, oy = t.by * kTileH - kK;  // box origin; ox % 4 == 0
+  if (!load_box<kBoxH, kPairW>(a, t, S, box, bar, ox, oy)) return;
+  const int th = threadIdx.x, lx0 = 2 * th, gx0 = ox + lx0;
+  float c0[kBoxH], c1[kBoxH], p0[kBoxH], p1[kBoxH];
+#pragma unroll
+  for (int ly = 0; ly < kBoxH; ++ly) {
+    const float2 u = *reinterpret_cast<const float2*>(&box[0][ly][lx0]);
+    const float2 v = *reinterpret_cast<const float2*>(&box[1][ly][lx0]);
+    c0[ly] = u.x;
+    c1[ly] = u.y;
+    p0[ly] = v.x;
+    p1[ly] = v.y;
+  }
+  __syncthreads();  // the exchange arrays overwrite the boxes
+  float(*ex)[2][kBoxH][kWaveTmaThreads] = reinterpret_cast<float(*)[2][kBoxH][kWaveTmaThreads]>(box_mem);
+#pragma unroll
+  for (int ly = 0; ly < kBoxH; ++ly) {
+    ex[0][0][ly][th] = c0[ly];
+    ex[0][1][ly][th] = c1[ly];
+  }
+  __syncthreads();
+  PairCtx c;
+  c.th = th;
+  c.tw = th > 0 ? th - 1 : th;
+  c.te = th + 1 < kWaveTmaThreads ? th + 1 : th;
+  c.self_w = !(gx0 > 0) || th == 0;
+  c.self_e = !(gx0 + 2 < W) || th + 1 == kWaveTmaThreads;
+  c.pair_in = gx0 + 1 < W;
+  c.ytop = H - oy;
+  c.ybot = -oy;
+  c.wa = S->wa;
+  c.wb = S->wb;
+  c.lam = S->lam;
+  c.atten = S->atten;
+  c.coupled = S->coupled != 0;
+  c.zero_deposit = c.coupled ? fmul(S->gain, fmul(0.0f, S->dq)) : 0.0f;
+  c.src0 = S->line_source && gx0 == W / 2;
+  c.src1 = S->line_source && gx0 + 1 == W / 2;
+  // interior: TMA scene (even width), the box clear of the domain's first and
+  // last columns and inside its rows, no line-source column
+  const bool edge = !t.tma || ox <= 0 || ox + kPairW >= W || oy < 0 || oy + kBoxH > H ||
+                    (S->line_source && W / 2 >= ox && W / 2 < ox + kPairW);
+  if (edge)
+    pair_steps<kBoxH, kK, true>(c0, c1, p0, p1, ex, c);
+  else
+    pair_steps<kBoxH, kK, false>(c0, c1, p0, p1, ex, c);
+  // c = u^(n+K), p = u^(n+K-1)
+  float* oc = a.out_cur + S->woff;
+  float* op = a.out_prev + S->woff;
+  const bool st0 = lx0 >= kK && lx0 < kPairW - kK && gx0 < W;
+  const bool st1 = lx0 + 1 >= kK && lx0 + 1 < kPairW - kK && gx0 + 1 < W;
+  const bool vec = t.tma && st0 && st1;  // 8-byte aligned: gx0 even, width a multiple of 4, base 16-byte aligned
+#pragma unroll
+  for (int ly = kK; ly < kBoxH - kK; ++ly) {
+    if (ly < c.ytop) {
+      const size_t g = (size_t)(oy + ly) * W + gx0;
+      if (vec) {
+        *reinterpret_cast<float2*>(oc + g) = make_float2(c0[ly], c1[ly]);
+        *reinterpret_cast<float2*>(op + g) = make_float2(p0[ly], p1[ly]);
+      } else {
+        if (st0) {
+          oc[g] = c0[ly];
+          op[g] = p0[ly];
+        }
+        if (st1) {
+          oc[g + 1] = c1[ly];
+          op[g + 1] = p1[ly];
+        }
+      }
+    }
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static bool tried = false;
@@ -373,7 +523,7 @@ bool wave_block_encode(CUtensorMap* map, float* base, int W, int H, int variant)
   if (!fn) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
   const cuuint64_t strides[1] = {(cuuint64_t)W * sizeof(float)};
-  const cuuint32_t boxdim[2] = {kBoxW, (cuuint32_t)kVarBoxH[variant]};
+  const cuuint32_t boxdim[2] = {(cuuint32_t)kVarBoxW[variant], (cuuint32_t)kVarBoxH[variant]};
   const cuuint32_t estr[2] = {1, 1};
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, boxdim, estr,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -381,17 +531,25 @@ bool wave_block_encode(CUtensorMap* map, float* base, int W, int H, int variant)
 }
 
 void wave_block_tiles(const SceneDev& d, int32_t scene, bool tma, int variant, std::vector<WaveBlockTile>* out) {
-  const int tw = kBoxW - 2 * kVarK[variant], th = kVarBoxH[variant] - 2 * kVarK[variant];
+  const int tw = kVarBoxW[variant] - 2 * kVarK[variant], th = kVarBoxH[variant] - 2 * kVarK[variant];
   const int nbx = (d.nx + tw - 1) / tw, nby = (d.nz + th - 1) / th;
   for (int by = 0; by < nby; ++by)
     for (int bx = 0; bx < nbx; ++bx) out->push_back(WaveBlockTile{scene, bx, by, tma ? 1 : 0});
 }
 
 namespace {
-template <int kBoxH, int kK, bool kReg>
+enum Form { kShared, kReg, kPair };
+
+template <int kBoxH, int kK, Form kForm>
 cudaError_t launch_variant(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t stream) {
-  constexpr int bytes = 2 * kBoxH * kBoxW * (int)sizeof(float) + 16;
-  auto kern = kReg ? k_wave_reg<kBoxH, kK> : k_wave_block<kBoxH, kK>;
+  constexpr int bytes = 2 * kBoxH * (kForm == kPair ? kPairW : kBoxW) * (int)sizeof(float) + 16;
+  void (*kern)(WaveBlockArgs);
+  if constexpr (kForm == kPair)
+    kern = k_wave_pair<kBoxH, kK>;
+  else if constexpr (kForm == kReg)
+    kern = k_wave_reg<kBoxH, kK>;
+  else
+    kern = k_wave_block<kBoxH, kK>;
   static bool raised = false;  // dynamic shared memory above 48 KB needs the opt-in
   if (bytes > 48 * 1024 && !raised) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -406,12 +564,13 @@ cudaError_t launch_variant(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t
 cudaError_t launch_wave_block(const WaveBlockArgs& a, int32_t n_tiles, int variant, cudaStream_t stream) {
   if (n_tiles <= 0) return cudaSuccess;
   switch (variant) {
-    case 1: return launch_variant<64, 4, false>(a, n_tiles, stream);
-    case 2: return launch_variant<64, 8, false>(a, n_tiles, stream);
-    case 3: return launch_variant<32, 4, true>(a, n_tiles, stream);
-    case 4: return launch_variant<64, 4, true>(a, n_tiles, stream);
-    case 5: return launch_variant<64, 8, true>(a, n_tiles, stream);
-    default: return launch_variant<32, 4, false>(a, n_tiles, stream);
+    case 1: return launch_variant<64, 4, kShared>(a, n_tiles, stream);
+    case 2: return launch_variant<64, 8, kShared>(a, n_tiles, stream);
+    case 3: return launch_variant<32, 4, kReg>(a, n_tiles, stream);
+    case 4: return launch_variant<64, 4, kReg>(a, n_tiles, stream);
+    case 5: return launch_variant<64, 8, kReg>(a, n_tiles, stream);
+    case 6: return launch_variant<32, 4, kPair>(a, n_tiles, stream);
+    default: return launch_variant<32, 4, kShared>(a, n_tiles, stream);
   }
 }
 

@@ -121,10 +121,10 @@ typedef struct cwa_sim_options {
   int32_t reserved[3];
 } cwa_sim_options;
 
-/* Blocked wave advance variants: box of 128 x H cells advanced K steps per
- * launch in shared memory; the R variants hold each thread's box column in
- * registers and exchange only the east / west neighbours through shared
- * memory. */
+/* Blocked wave advance variants: box of 128 x H cells (P: 256 x H) advanced
+ * K steps per launch in shared memory; the R and P variants hold each
+ * thread's box column (P: column pair) in registers and exchange only the
+ * east / west neighbours through shared memory. */
 enum {
   CWA_WAVE_BLOCK_32x4 = 0,  /* default: H 32, K 4 */
   CWA_WAVE_BLOCK_64x4 = 1,  /* H 64, K 4 */
@@ -132,7 +132,8 @@ enum {
   CWA_WAVE_BLOCK_R32x4 = 3, /* registers, H 32, K 4 */
   CWA_WAVE_BLOCK_R64x4 = 4, /* registers, H 64, K 4 */
   CWA_WAVE_BLOCK_R64x8 = 5, /* registers, H 64, K 8 */
-  CWA_WAVE_BLOCK_COUNT = 6
+  CWA_WAVE_BLOCK_P32x4 = 6, /* registers, 256 x 32 box, two columns a thread, K 4 */
+  CWA_WAVE_BLOCK_COUNT = 7
 };
 
 /* Borrowed device pointers of one scene, all in the current sorted order.

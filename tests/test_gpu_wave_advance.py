@@ -128,7 +128,7 @@ def test_wave_advance_uncoupled_interior_boxes(lib, wave_block, wave_mode):
     # and without the line-source column
     sc = small_reference(640)
     sc.desc.wave_mode = wave_mode
-    sc.desc.wave_nx, sc.desc.wave_nz = 372, 300
+    sc.desc.wave_nx, sc.desc.wave_nz = 760, 300  # wide enough for interior 256-column boxes too
 
     def load(s):
         s.upload_particles(0, sc.particles)
