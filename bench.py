@@ -476,8 +476,9 @@ def run_sph2d(args) -> None:
     import torch  # noqa: F401 (CUDA context first, as the other modes)
 
     from coupledwateranimation_gb300 import _abi
-    from coupledwateranimation_gb300.sim2d import Sim2D, defaults2d
-    p = defaults2d()
+    from coupledwateranimation_gb300.sim2d import WAVE2D_1D, WAVE2D_SHALLOW, Sim2D, defaults2d
+    wave1d = args.wave_kind == "wave1d"
+    p = defaults2d(WAVE2D_1D if wave1d else WAVE2D_SHALLOW)
     frames = max(10, args.steps)
     with Sim2D(p) as sim:
         sim.splash()
@@ -489,17 +490,23 @@ def run_sph2d(args) -> None:
         gpu_s = (time.perf_counter() - t0) / frames
         parts = sim.download_particles()
         wave = sim.download_wave()
-    out = {"mode": "sph2d", "particles": p.n_particles, "wave_cells": p.wave_cells,
-           "sph_substeps": p.sph_substeps, "frames": frames, "gpu_ms_per_frame": gpu_s * 1e3,
+    out = {"mode": "sph2d", "wave_kind": args.wave_kind, "particles": p.n_particles, "wave_cells": p.wave_cells,
+           "sph_substeps": p.sph_substeps, "wave_substeps": p.wave_substeps, "frames": frames,
+           "gpu_ms_per_frame": gpu_s * 1e3,
            "gpu_frames_per_s": 1.0 / gpu_s, "gpu_particle_substeps_per_s": p.n_particles * p.sph_substeps / gpu_s}
     if not args.no_cpu:
         from oracle import oracle as orc
         cpu_frames, t0 = 0, time.perf_counter()
+        older = wave.copy()
         while cpu_frames < 3 or time.perf_counter() - t0 < 5.0:
             for _ in range(p.sph_substeps):
                 parts = orc.force_2d(p, orc.density_2d(p, parts, wave), wave)
-            a = orc.wave_iter_2d_f32(p, wave, 0)
-            wave = orc.wave_iter_2d_f32(p, a, 1, out_prev=wave)
+            for _ in range(p.wave_substeps):
+                if wave1d:
+                    wave, older = orc.wave1d_iter_2d_f32(p, wave, older), wave
+                else:
+                    a = orc.wave_iter_2d_f32(p, wave, 0)
+                    wave = orc.wave_iter_2d_f32(p, a, 1, out_prev=wave)
             cpu_frames += 1
         cpu_s = (time.perf_counter() - t0) / cpu_frames
         out["cpu_baseline"] = {"ms_per_frame": cpu_s * 1e3, "cores": orc.threads(), "kind": "port",
@@ -609,6 +616,8 @@ def main() -> None:
     ap.add_argument("--height", type=int, default=1080, help="image height for --mode render")
     ap.add_argument("--png", default="", help="--mode render: write the frame to this PNG")
     ap.add_argument("--wave-n", type=int, default=4096, help="field edge for --mode wave")
+    ap.add_argument("--wave-kind", default="shallow", choices=["shallow", "wave1d"],
+                    help="--mode sph2d: the 1D field the SPH samples")
     ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2])
     ap.add_argument("--no-cpu", action="store_true")

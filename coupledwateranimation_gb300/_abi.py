@@ -89,7 +89,11 @@ class Params2D(C.Structure):
                 ("wave_substeps", C.c_int32), ("grid_cells", C.c_int32 * 2), ("init_columns", C.c_int32),
                 ("view_size", C.c_float * 2), ("particle_radius", C.c_float), ("rest_density", C.c_float),
                 ("visc", C.c_float), ("dt", C.c_float), ("gas_const", C.c_float), ("bottom", C.c_float),
-                ("wave_lambda", C.c_float), ("wave_dx", C.c_float), ("reserved", C.c_int32 * 4)]
+                ("wave_lambda", C.c_float), ("wave_dx", C.c_float), ("wave_kind", C.c_int32),
+                ("wave_atten", C.c_float), ("wave_beta", C.c_float), ("reserved", C.c_int32 * 1)]
+
+
+WAVE2D_SHALLOW, WAVE2D_1D = 0, 1  # CWA2D_WAVE_*
 
 
 class PbdParams(C.Structure):
@@ -104,7 +108,7 @@ PBD_BOX_DTYPE = np.dtype([("color", "<f4", 4), ("x", "<f4", 4), ("v", "<f4", 4),
                           ("dp_t", "<f4", 4), ("dp_n", "<f4", 4), ("hw", "<f4", 4), ("rm", "<f4"), ("n", "<f4"),
                           ("e", "<f4"), ("padding", "<f4")])
 PARTICLE2D_DTYPE = np.dtype([("pos", "<f4", 4), ("vel", "<f4", 4), ("acc", "<f4", 4)])
-PASS2D = {"grid": 0, "density": 1, "force": 2, "wave_predict": 3, "wave_correct": 4}
+PASS2D = {"grid": 0, "density": 1, "force": 2, "wave_predict": 3, "wave_correct": 4, "wave_iterate": 5}
 
 
 class TuneReport(C.Structure):
@@ -164,6 +168,8 @@ _PROTOS = {
     "cwa2d_download_particles": (C.c_int, [_P, C.c_void_p, _I32]),
     "cwa2d_upload_wave": (C.c_int, [_P, C.c_void_p, _I32]),
     "cwa2d_download_wave": (C.c_int, [_P, C.c_void_p, _I32]),
+    "cwa2d_upload_wave_prev": (C.c_int, [_P, C.c_void_p, _I32]),
+    "cwa2d_download_wave_prev": (C.c_int, [_P, C.c_void_p, _I32]),
     "cwa2d_synchronize": (C.c_int, [_P]),
     "cwa_pbd_defaults": (C.c_int, [C.POINTER(PbdParams)]),
     "cwa_pbd_make_boxes": (C.c_int, [C.POINTER(PbdParams), C.c_uint64, C.c_void_p, _I32]),

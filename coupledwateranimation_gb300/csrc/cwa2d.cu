@@ -42,6 +42,8 @@ struct Sph2dConst {
   float cell_x, cell_y;
   float plane0_c;  // floor plane offset: -0.5 VIEW_HEIGHT + 15 R - R + bottom
   float lambda, dx;
+  int wave_kind;
+  float w1_a, w1_b, w1_atten, w1_half;  // Wave1D: 2 - 2 lambda - beta, 1 - beta, atten, 0.5 lambda
 };
 
 __device__ __forceinline__ float w_cubic(const Sph2dConst& c, float r) {
@@ -339,6 +341,68 @@ __global__ void k2_wave_iter(Sph2dConst c, const float4* __restrict__ in, float4
   }
 }
 
+// Wave1D_cs.glsl (the 2D app's other wave kind), one rounding per operation.
+// get_n (:198-207): c1 from the older field, c0 / e0 / w0 from the newest,
+// out-of-range loads read zero.  FreeBC (:148-166): cells 0 and n-1 store
+// nothing themselves; cells 1 and n-2 copy their value outward.
+__device__ __forceinline__ void w1_vel_acc(float4& w, float c0x, float c1x) {
+  const float v = __fdiv_rn(__fsub_rn(w.x, c1x), 2.0f);
+  const float a = __fadd_rn(__fsub_rn(w.x, __fmul_rn(2.0f, c0x)), c1x);
+  w.y = v;
+  w.z = a;
+}
+
+__device__ __forceinline__ void w1_store_free(float4* out, int i, int n, const float4& w) {
+  if (i == 0 || i == n - 1) return;
+  out[i] = w;
+  if (i == 1) out[0] = w;
+  if (i == n - 2) out[n - 1] = w;
+}
+
+// InitWave (:98-118).  Mode 0: the Gaussian bump at int(0.25 n).  Mode 1:
+// the invocation's Gaussian store is overwritten by its later FreeBC stores
+// of w = c0 - 0.5 lambda (e0 - 2 c0 + w0), so only those are made.
+__global__ void k1_wave_init(Sph2dConst c, const float4* __restrict__ cur, const float4* __restrict__ prev,
+                             float4* __restrict__ out, int mode) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = c.wave_n;
+  if (i >= n) return;
+  if (mode == 0) {
+    const int x = (int)(0.25f * (float)n) - i;
+    const int xx = (int)((uint32_t)(-x) * (uint32_t)x);  // the shader's int product, wrapping
+    const float h = __fadd_rn(0.0f, __fmul_rn(0.1f, expf(__fdiv_rn((float)xx, 5000.0f))));
+    out[i] = make_float4(h, 0.0f, 0.0f, 0.0f);
+    return;
+  }
+  const float4 c0 = cur[i], c1 = prev[i];
+  const float4 e0 = load_or_zero(cur, i + 1, n), w0 = load_or_zero(cur, i - 1, n);
+  auto half = [&c](float cc, float e, float w) {
+    return __fsub_rn(cc, __fmul_rn(c.w1_half, __fadd_rn(__fsub_rn(e, __fmul_rn(2.0f, cc)), w)));
+  };
+  float4 w = make_float4(half(c0.x, e0.x, w0.x), half(c0.y, e0.y, w0.y), half(c0.z, e0.z, w0.z),
+                         half(c0.w, e0.w, w0.w));
+  w1_vel_acc(w, c0.x, c1.x);
+  w1_store_free(out, i, n, w);
+}
+
+// IterateWave (:120-131): w = atten ((2 - 2 lambda - beta) c0 + lambda (e0 + w0)
+// - (1 - beta) c1), then velocity and acceleration, then FreeBC.
+__global__ void k1_wave_iter(Sph2dConst c, const float4* __restrict__ cur, const float4* __restrict__ prev,
+                             float4* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = c.wave_n;
+  if (i >= n || i == 0 || i == n - 1) return;  // FreeBC: cells 0 and n-1 are written by their neighbours
+  const float4 c0 = cur[i], c1 = prev[i], e0 = cur[i + 1], w0 = cur[i - 1];
+  auto step = [&c](float cc, float cp, float e, float w) {
+    const float t = __fadd_rn(__fmul_rn(c.w1_a, cc), __fmul_rn(c.lambda, __fadd_rn(e, w)));
+    return __fmul_rn(c.w1_atten, __fsub_rn(t, __fmul_rn(c.w1_b, cp)));
+  };
+  float4 w = make_float4(step(c0.x, c1.x, e0.x, w0.x), step(c0.y, c1.y, e0.y, w0.y), step(c0.z, c1.z, e0.z, w0.z),
+                         step(c0.w, c1.w, e0.w, w0.w));
+  w1_vel_acc(w, c0.x, c1.x);
+  w1_store_free(out, i, n, w);
+}
+
 constexpr int kBlock = 256;
 inline unsigned blocks(int n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 
@@ -353,14 +417,17 @@ struct cwa2d_sim {
   Sph2dConst k{};
   cudaStream_t stream = nullptr;
   float4 *P[2] = {}, *V[2] = {}, *A[2] = {};
-  float4* W[2] = {};
+  // wave buffers: W[wcur] is the newest field; the shallow-water kind
+  // writes W[wcur ^ 1], Wave1D writes W[(wcur + 1) % 3] and reads the older
+  // field from W[(wcur + 2) % 3]
+  float4* W[3] = {};
   int cur = 0, wcur = 0;
   int32_t *key = nullptr, *slot = nullptr, *count = nullptr, *start = nullptr, *list = nullptr, *sorted = nullptr;
   void* scan_ws = nullptr;
   ScanWorkspace scan{};
   int32_t* d_status = nullptr;
   bool grid_fresh = false;
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph[3] = {};  // one frame, per wave-buffer phase wcur
   cwa2d_particle* staging = nullptr;
 };
 
@@ -384,13 +451,14 @@ void free2d(cwa2d_sim* s) {
   if (!s) return;
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
-  if (s->graph) cudaGraphExecDestroy(s->graph);
+  for (cudaGraphExec_t& g : s->graph)
+    if (g) cudaGraphExecDestroy(g);
   for (int b = 0; b < 2; ++b) {
     cudaFree(s->P[b]);
     cudaFree(s->V[b]);
     cudaFree(s->A[b]);
-    cudaFree(s->W[b]);
   }
+  for (float4* w : s->W) cudaFree(w);
   cudaFree(s->key);
   cudaFree(s->slot);
   cudaFree(s->count);
@@ -438,6 +506,28 @@ cwa_status pass_wave(cwa2d_sim* s, int phase) {
   return CWA_OK;
 }
 
+// Wave1D: one dispatch into the write buffer, then the three-buffer rotation
+// (ImageStencil::PingPong with two read images: the new field becomes the
+// newest, the newest the older one).
+cwa_status pass_wave1d(cwa2d_sim* s, int init_mode) {
+  const int w = s->wcur, nxt = (w + 1) % 3, old = (w + 2) % 3;
+  if (init_mode >= 0)
+    k1_wave_init<<<blocks(s->k.wave_n), kBlock, 0, s->stream>>>(s->k, s->W[w], s->W[old], s->W[nxt], init_mode);
+  else
+    k1_wave_iter<<<blocks(s->k.wave_n), kBlock, 0, s->stream>>>(s->k, s->W[w], s->W[old], s->W[nxt]);
+  CWA2_CUDA(cudaGetLastError());
+  s->wcur = nxt;
+  return CWA_OK;
+}
+
+void drop_graphs2(cwa2d_sim* s) {
+  for (cudaGraphExec_t& g : s->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
 cwa_status enqueue_frame(cwa2d_sim* s) {
   for (int sub = 0; sub < s->prm.sph_substeps; ++sub) {
     cwa_status st = pass_grid(s);
@@ -446,8 +536,13 @@ cwa_status enqueue_frame(cwa2d_sim* s) {
     if (st != CWA_OK) return st;
   }
   for (int sub = 0; sub < s->prm.wave_substeps; ++sub) {
-    cwa_status st = pass_wave(s, 0);
-    if (st == CWA_OK) st = pass_wave(s, 1);
+    cwa_status st = CWA_OK;
+    if (s->k.wave_kind == CWA2D_WAVE_1D) {
+      st = pass_wave1d(s, -1);
+    } else {
+      st = pass_wave(s, 0);
+      if (st == CWA_OK) st = pass_wave(s, 1);
+    }
     if (st != CWA_OK) return st;
   }
   return CWA_OK;
@@ -494,6 +589,9 @@ cwa_status cwa2d_defaults(cwa2d_params* p) {
   p->bottom = 0.3f;
   p->wave_lambda = 0.001f;
   p->wave_dx = 0.1f;
+  p->wave_kind = CWA2D_WAVE_SHALLOW;
+  p->wave_atten = 0.9995f;
+  p->wave_beta = 0.001f;
   return CWA_OK;
 }
 
@@ -506,6 +604,7 @@ cwa_status cwa2d_create(const cwa2d_params* p, int32_t device, cwa2d_sim** out) 
   if (p->grid_cells[0] < 1 || p->grid_cells[1] < 1 || (int64_t)p->grid_cells[0] * p->grid_cells[1] > (1 << 26))
     return err2("grid_cells must be positive, at most 2^26 cells");
   if (p->sph_substeps < 0 || p->wave_substeps < 0) return err2("substeps must be >= 0");
+  if (p->wave_kind != CWA2D_WAVE_SHALLOW && p->wave_kind != CWA2D_WAVE_1D) return err2("unknown wave_kind");
   if (!(p->view_size[0] > 0.0f && p->view_size[1] > 0.0f && p->particle_radius > 0.0f && p->rest_density > 0.0f &&
         p->dt > 0.0f && p->wave_dx > 0.0f))
     return err2("sizes, radius, rest density, dt and dx must be positive");
@@ -539,6 +638,12 @@ cwa_status cwa2d_create(const cwa2d_params* p, int32_t device, cwa2d_sim** out) 
   k.plane0_c = -0.5f * k.view_h + 15.0f * k.R - k.R + p->bottom;
   k.lambda = p->wave_lambda;
   k.dx = p->wave_dx;
+  k.wave_kind = p->wave_kind;
+  // Wave1D's coefficients as the shader forms them (Wave1D_cs.glsl:109, 125)
+  k.w1_a = (2.0f - 2.0f * p->wave_lambda) - p->wave_beta;
+  k.w1_b = 1.0f - p->wave_beta;
+  k.w1_atten = p->wave_atten;
+  k.w1_half = 0.5f * p->wave_lambda;
   const int nc = k.ncx * k.ncy;
   auto fail = [&](cudaError_t e) {
     cwa::set_error(std::string("cwa2d_create: ") + cudaGetErrorString(e));
@@ -551,7 +656,10 @@ cwa_status cwa2d_create(const cwa2d_params* p, int32_t device, cwa2d_sim** out) 
     e = cudaMalloc((void**)&s->P[b], sizeof(float4) * k.n);
     if (e == cudaSuccess) e = cudaMalloc((void**)&s->V[b], sizeof(float4) * k.n);
     if (e == cudaSuccess) e = cudaMalloc((void**)&s->A[b], sizeof(float4) * k.n);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&s->W[b], sizeof(float4) * k.wave_n);
+  }
+  for (int b = 0; b < 3 && e == cudaSuccess; ++b) {
+    e = cudaMalloc((void**)&s->W[b], sizeof(float4) * k.wave_n);
+    if (e == cudaSuccess) e = cudaMemset(s->W[b], 0, sizeof(float4) * k.wave_n);  // images start at zero
   }
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->key, 4 * (size_t)k.n);
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->slot, 4 * (size_t)k.n);
@@ -586,27 +694,32 @@ cwa_status cwa2d_reinit(cwa2d_sim* s) {
   cwa_status st = check2(s);
   if (st != CWA_OK) return st;
   k2_init_particles<<<blocks(s->k.n), kBlock, 0, s->stream>>>(s->k, s->P[s->cur], s->V[s->cur], s->A[s->cur]);
-  // ImageStencil::Reinit: MODE_INIT_0 into the write image, then PingPong
-  k2_wave_init<<<blocks(s->k.wave_n), kBlock, 0, s->stream>>>(s->k, s->W[s->wcur], s->W[s->wcur ^ 1], 0);
-  CWA2_CUDA(cudaGetLastError());
-  s->wcur ^= 1;
-  s->grid_fresh = false;
-  if (s->graph) {  // the phase (cur, wcur) may have changed
-    cudaGraphExecDestroy(s->graph);
-    s->graph = nullptr;
+  // ImageStencil::Reinit: MODE_INIT_FIRST + i into the write image, then
+  // PingPong, for each read image (one for shallow water, two for Wave1D)
+  if (s->k.wave_kind == CWA2D_WAVE_1D) {
+    st = pass_wave1d(s, 0);
+    if (st == CWA_OK) st = pass_wave1d(s, 1);
+    if (st != CWA_OK) return st;
+  } else {
+    k2_wave_init<<<blocks(s->k.wave_n), kBlock, 0, s->stream>>>(s->k, s->W[s->wcur], s->W[s->wcur ^ 1], 0);
+    CWA2_CUDA(cudaGetLastError());
+    s->wcur ^= 1;
   }
+  s->grid_fresh = false;
+  drop_graphs2(s);  // the particle phase may have changed
   return read_status2(s);
 }
 
 cwa_status cwa2d_splash(cwa2d_sim* s) {
   cwa_status st = check2(s);
   if (st != CWA_OK) return st;
-  k2_wave_init<<<blocks(s->k.wave_n), kBlock, 0, s->stream>>>(s->k, s->W[s->wcur], s->W[s->wcur ^ 1], 1);
-  CWA2_CUDA(cudaGetLastError());
-  s->wcur ^= 1;
-  if (s->graph) {
-    cudaGraphExecDestroy(s->graph);
-    s->graph = nullptr;
+  if (s->k.wave_kind == CWA2D_WAVE_1D) {
+    st = pass_wave1d(s, 1);
+    if (st != CWA_OK) return st;
+  } else {
+    k2_wave_init<<<blocks(s->k.wave_n), kBlock, 0, s->stream>>>(s->k, s->W[s->wcur], s->W[s->wcur ^ 1], 1);
+    CWA2_CUDA(cudaGetLastError());
+    s->wcur ^= 1;
   }
   return CWA_OK;
 }
@@ -615,9 +728,16 @@ cwa_status cwa2d_step(cwa2d_sim* s, int32_t n) {
   cwa_status st = check2(s);
   if (st != CWA_OK) return st;
   if (n < 0) return err2("n_steps < 0");
-  const int cur0 = s->cur, w0 = s->wcur;
   for (int32_t k = 0; k < n; ++k) {
-    if (!s->graph) {
+    // A frame flips the particle buffers an even number of times (two passes
+    // per substep); the wave phase advances by 0 (shallow water: two passes
+    // per substep) or by wave_substeps mod 3 (Wave1D), so frames replay one
+    // graph per wave phase.
+    const int cur0 = s->cur, w0 = s->wcur;
+    cudaGraphExec_t& ge = s->graph[w0];
+    int w1 = w0;
+    if (s->k.wave_kind == CWA2D_WAVE_1D) w1 = (w0 + s->prm.wave_substeps) % 3;
+    if (!ge) {
       cudaGraph_t g = nullptr;
       CWA2_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
       st = enqueue_frame(s);
@@ -629,13 +749,12 @@ cwa_status cwa2d_step(cwa2d_sim* s, int32_t n) {
         return st;
       }
       CWA2_CUDA(e);
-      e = cudaGraphInstantiate(&s->graph, g, 0);
+      e = cudaGraphInstantiate(&ge, g, 0);
       cudaGraphDestroy(g);
       CWA2_CUDA(e);
     }
-    // a frame flips both buffer pairs an even number of times (two passes
-    // per substep), so every frame replays the same graph
-    CWA2_CUDA(cudaGraphLaunch(s->graph, s->stream));
+    CWA2_CUDA(cudaGraphLaunch(ge, s->stream));
+    s->wcur = w1;
     s->grid_fresh = false;
   }
   return CWA_OK;
@@ -644,10 +763,11 @@ cwa_status cwa2d_step(cwa2d_sim* s, int32_t n) {
 cwa_status cwa2d_pass(cwa2d_sim* s, int32_t pass) {
   cwa_status st = check2(s);
   if (st != CWA_OK) return st;
-  if (pass != CWA2D_PASS_GRID && s->graph) {  // single passes change the buffer phase
-    cudaGraphExecDestroy(s->graph);
-    s->graph = nullptr;
-  }
+  if (pass != CWA2D_PASS_GRID) drop_graphs2(s);  // single passes change the particle phase
+  const bool w1 = s->k.wave_kind == CWA2D_WAVE_1D;
+  if ((pass == CWA2D_PASS_WAVE_PREDICT || pass == CWA2D_PASS_WAVE_CORRECT) && w1)
+    return err2("the predictor and corrector passes belong to the shallow-water kind");
+  if (pass == CWA2D_PASS_WAVE_ITERATE && !w1) return err2("the iterate pass belongs to the Wave1D kind");
   switch (pass) {
     case CWA2D_PASS_GRID: return pass_grid(s);
     case CWA2D_PASS_DENSITY:
@@ -658,6 +778,7 @@ cwa_status cwa2d_pass(cwa2d_sim* s, int32_t pass) {
       return pass_sph(s, false);
     case CWA2D_PASS_WAVE_PREDICT: return pass_wave(s, 0);
     case CWA2D_PASS_WAVE_CORRECT: return pass_wave(s, 1);
+    case CWA2D_PASS_WAVE_ITERATE: return pass_wave1d(s, -1);
     default: return err2("unknown pass");
   }
 }
@@ -702,6 +823,28 @@ cwa_status cwa2d_download_wave(cwa2d_sim* s, float* cells4, int32_t n) {
   if (st != CWA_OK) return st;
   if (!cells4 || n != s->k.wave_n) return err2("download size must equal wave_cells");
   CWA2_CUDA(cudaMemcpyAsync(cells4, s->W[s->wcur], sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
+  CWA2_CUDA(cudaStreamSynchronize(s->stream));
+  return CWA_OK;
+}
+
+cwa_status cwa2d_upload_wave_prev(cwa2d_sim* s, const float* cells4, int32_t n) {
+  cwa_status st = check2(s);
+  if (st != CWA_OK) return st;
+  if (s->k.wave_kind != CWA2D_WAVE_1D) return err2("only the Wave1D kind keeps an older field");
+  if (!cells4 || n != s->k.wave_n) return err2("upload size must equal wave_cells");
+  CWA2_CUDA(cudaMemcpyAsync(s->W[(s->wcur + 2) % 3], cells4, sizeof(float4) * n, cudaMemcpyHostToDevice,
+                            s->stream));
+  CWA2_CUDA(cudaStreamSynchronize(s->stream));
+  return CWA_OK;
+}
+
+cwa_status cwa2d_download_wave_prev(cwa2d_sim* s, float* cells4, int32_t n) {
+  cwa_status st = check2(s);
+  if (st != CWA_OK) return st;
+  if (s->k.wave_kind != CWA2D_WAVE_1D) return err2("only the Wave1D kind keeps an older field");
+  if (!cells4 || n != s->k.wave_n) return err2("download size must equal wave_cells");
+  CWA2_CUDA(cudaMemcpyAsync(cells4, s->W[(s->wcur + 2) % 3], sizeof(float4) * n, cudaMemcpyDeviceToHost,
+                            s->stream));
   CWA2_CUDA(cudaStreamSynchronize(s->stream));
   return CWA_OK;
 }

@@ -422,10 +422,22 @@ typedef struct cwa2d_params {
   float dt;               /* 0.002 */
   float gas_const;        /* 35000 (weakly compressible, gamma 3) */
   float bottom;           /* 0.3: floor plane offset */
-  float wave_lambda;      /* 0.001 (Shallow1D_cs.glsl:23) */
-  float wave_dx;          /* 0.1 */
-  int32_t reserved[4];
+  float wave_lambda;      /* 0.001 (Shallow1D_cs.glsl:23); Wave1D: 0.01 (Wave1D_cs.glsl:21) */
+  float wave_dx;          /* 0.1 (shallow water only) */
+  int32_t wave_kind;      /* CWA2D_WAVE_SHALLOW (default) or CWA2D_WAVE_1D */
+  float wave_atten;       /* Wave1D attenuation 0.9995 (Wave1D_cs.glsl:22) */
+  float wave_beta;        /* Wave1D damping 0.001 (Wave1D_cs.glsl:23) */
+  int32_t reserved[1];
 } cwa2d_params;
+
+/* The 1D field the SPH samples.  CWA2D_WAVE_SHALLOW: Shallow1D_cs.glsl, two
+ * buffers, cells (h, uh, h_half, uh_half), the app's active choice
+ * (InitShallowWaterEquation, SphWave2D/Main.cpp:77-97).  CWA2D_WAVE_1D:
+ * Wave1D_cs.glsl, the damped wave equation on three buffers with free
+ * boundaries, cells (h, velocity, acceleration, 0); the app's
+ * InitWaveEquation (Main.cpp:63-75) runs it on 1024 cells with 10 substeps
+ * and lambda 0.01. */
+enum { CWA2D_WAVE_SHALLOW = 0, CWA2D_WAVE_1D = 1 };
 
 typedef struct cwa2d_sim cwa2d_sim;
 enum {
@@ -433,15 +445,18 @@ enum {
   CWA2D_PASS_DENSITY = 1,       /* MODE_COMPUTE_DENSITY_PRESSURE */
   CWA2D_PASS_FORCE = 2,         /* MODE_COMPUTE_FORCES (integrates) */
   CWA2D_PASS_WAVE_PREDICT = 3,  /* Shallow1D MODE_ITERATE0 */
-  CWA2D_PASS_WAVE_CORRECT = 4   /* Shallow1D MODE_ITERATE1 */
+  CWA2D_PASS_WAVE_CORRECT = 4,  /* Shallow1D MODE_ITERATE1 */
+  CWA2D_PASS_WAVE_ITERATE = 5   /* Wave1D MODE_ITERATE */
 };
 
 cwa_status cwa2d_defaults(cwa2d_params* out);
 cwa_status cwa2d_create(const cwa2d_params* params, int32_t device, cwa2d_sim** out);
 cwa_status cwa2d_destroy(cwa2d_sim* sim);
-/* InitParticle (MODE_INIT) and InitWave (Shallow1D MODE_INIT_0). */
+/* InitParticle (MODE_INIT) and the wave's ImageStencil::Reinit: Shallow1D
+ * MODE_INIT_0, or Wave1D MODE_INIT_0 then MODE_INIT_1. */
 cwa_status cwa2d_reinit(cwa2d_sim* sim);
-/* The "Splash" button: Shallow1D MODE_INIT_1 on the current field. */
+/* The "Splash" button (ImageStencil::ComputeFunc(1)): MODE_INIT_1 on the
+ * current field. */
 cwa_status cwa2d_splash(cwa2d_sim* sim);
 /* n frames (SPH substeps, then the wave substeps), one CUDA graph each. */
 cwa_status cwa2d_step(cwa2d_sim* sim, int32_t n_steps);
@@ -449,9 +464,12 @@ cwa_status cwa2d_step(cwa2d_sim* sim, int32_t n_steps);
 cwa_status cwa2d_pass(cwa2d_sim* sim, int32_t pass);
 cwa_status cwa2d_upload_particles(cwa2d_sim* sim, const cwa2d_particle* host, int32_t n);
 cwa_status cwa2d_download_particles(cwa2d_sim* sim, cwa2d_particle* host, int32_t n);
-/* The wave field: n cells of (h, uh, h_half, uh_half). */
+/* The newest wave field: n cells of 4 floats (see CWA2D_WAVE_*). */
 cwa_status cwa2d_upload_wave(cwa2d_sim* sim, const float* cells4, int32_t n);
 cwa_status cwa2d_download_wave(cwa2d_sim* sim, float* cells4, int32_t n);
+/* CWA2D_WAVE_1D only: the field one step older (the iteration's c1). */
+cwa_status cwa2d_upload_wave_prev(cwa2d_sim* sim, const float* cells4, int32_t n);
+cwa_status cwa2d_download_wave_prev(cwa2d_sim* sim, float* cells4, int32_t n);
 cwa_status cwa2d_synchronize(cwa2d_sim* sim);
 
 /* ---- position-based box collisions on the uniform grid ----

@@ -176,6 +176,79 @@ void orc2d_wave_iter_f32(const cwa2d_params* prm, const float* in4, float* out4,
   }
 }
 
+// Wave1D_cs.glsl, float32 op by op.  get_n (:198-207) reads c1 from the
+// older field and c0, e0, w0 from the newest; loads outside the field read
+// zero (imageLoad out of range).  FreeBC (:148-166): cells 0 and n-1 keep no
+// value of their own; cells 1 and n-2 copy theirs outward.
+static void wave1d_store_free(const float (*w)[4], int n, float* out4) {
+  for (int i = 1; i <= n - 2; ++i) {
+    for (int k = 0; k < 4; ++k) out4[4 * i + k] = w[i][k];
+    if (i == 1)
+      for (int k = 0; k < 4; ++k) out4[k] = w[i][k];
+    if (i == n - 2)
+      for (int k = 0; k < 4; ++k) out4[4 * (n - 1) + k] = w[i][k];
+  }
+}
+
+// ComputeVelocityAcceleration (:73-79) on w.
+static void wave1d_vel_acc(float* w, float c0x, float c1x) {
+  const float v = (w[0] - c1x) / 2.0f;
+  const float a = (w[0] - 2.0f * c0x) + c1x;
+  w[1] = v;
+  w[2] = a;
+}
+
+// InitWave (:98-118).  Mode 0 stores the Gaussian bump centred at
+// int(0.25 n); mode 1's Gaussian store is overwritten by FreeBC's stores of
+// the half-step estimate w = c0 - 0.5 lambda (e0 - 2 c0 + w0) in every cell,
+// which come later in each invocation.
+void orc2d_wave1d_init_f32(const cwa2d_params* prm, const float* cur4, const float* prev4, float* out4, int32_t mode) {
+  const int n = prm->wave_cells;
+  const float lam = prm->wave_lambda;
+  auto at = [&](const float* f, int i, int k) { return (i >= 0 && i < n) ? f[4 * i + k] : 0.0f; };
+  if (mode == 0) {
+    const int cen = (int)(0.25f * (float)n);
+    for (int i = 0; i < n; ++i) {
+      const int x = cen - i;
+      const int xx = (int)((uint32_t)(-x) * (uint32_t)x);  // the shader's int product, wrapping
+      const float h = 0.0f + 0.1f * expf((float)xx / 5000.0f);
+      out4[4 * i + 0] = h;
+      out4[4 * i + 1] = out4[4 * i + 2] = out4[4 * i + 3] = 0.0f;
+    }
+    return;
+  }
+  std::vector<float> w((size_t)4 * n);
+  float(*wp)[4] = reinterpret_cast<float(*)[4]>(w.data());
+  const float s = 0.5f * lam;
+  for (int i = 0; i < n; ++i) {
+    for (int k = 0; k < 4; ++k) {
+      const float c0 = at(cur4, i, k), e0 = at(cur4, i + 1, k), w0 = at(cur4, i - 1, k);
+      wp[i][k] = c0 - s * ((e0 - 2.0f * c0) + w0);
+    }
+    wave1d_vel_acc(wp[i], at(cur4, i, 0), at(prev4, i, 0));
+  }
+  wave1d_store_free(wp, n, out4);
+}
+
+// IterateWave (:120-131).
+void orc2d_wave1d_iter_f32(const cwa2d_params* prm, const float* cur4, const float* prev4, float* out4) {
+  const int n = prm->wave_cells;
+  const float lam = prm->wave_lambda, beta = prm->wave_beta, atten = prm->wave_atten;
+  const float a = (2.0f - 2.0f * lam) - beta, b = 1.0f - beta;
+  auto at = [&](const float* f, int i, int k) { return (i >= 0 && i < n) ? f[4 * i + k] : 0.0f; };
+  std::vector<float> w((size_t)4 * n);
+  float(*wp)[4] = reinterpret_cast<float(*)[4]>(w.data());
+  for (int i = 0; i < n; ++i) {
+    for (int k = 0; k < 4; ++k) {
+      const float c0 = at(cur4, i, k), c1 = at(prev4, i, k);
+      const float e0 = at(cur4, i + 1, k), w0 = at(cur4, i - 1, k);
+      wp[i][k] = atten * ((a * c0 + lam * (e0 + w0)) - b * c1);
+    }
+    wave1d_vel_acc(wp[i], at(cur4, i, 0), at(prev4, i, 0));
+  }
+  wave1d_store_free(wp, n, out4);
+}
+
 // ComputeDensityPressure in FP64: reads `in`, writes `out` (positions after
 // the wall projection, enable flag, density, pressure).
 void orc2d_density(const cwa2d_params* prm, const cwa2d_particle* in, const float* wave4, cwa2d_particle* out) {

@@ -102,6 +102,11 @@ void orc_render(const float* pos4, int32_t n, const float* wave, int32_t nx, int
 void orc2d_init_particles(const cwa2d_params* prm, cwa2d_particle* out);
 void orc2d_wave_init_f32(const cwa2d_params* prm, const float* in4, float* out4, int32_t splash);
 void orc2d_wave_iter_f32(const cwa2d_params* prm, const float* in4, float* out4, int32_t phase);
+/* Wave1D (the 2D family's second wave kind): MODE_INIT_0 / MODE_INIT_1 and
+ * one MODE_ITERATE step with free boundaries, float32 op by op; cur4 is the
+ * newest field, prev4 the one before. */
+void orc2d_wave1d_init_f32(const cwa2d_params* prm, const float* cur4, const float* prev4, float* out4, int32_t mode);
+void orc2d_wave1d_iter_f32(const cwa2d_params* prm, const float* cur4, const float* prev4, float* out4);
 void orc2d_density(const cwa2d_params* prm, const cwa2d_particle* in, const float* wave4, cwa2d_particle* out);
 void orc2d_force(const cwa2d_params* prm, const cwa2d_particle* in, const float* wave4, cwa2d_particle* out);
 

@@ -62,6 +62,8 @@ def load() -> C.CDLL:
             "orc2d_init_particles": (None, [_P, _P]),
             "orc2d_wave_init_f32": (None, [_P, _P, _P, _I]),
             "orc2d_wave_iter_f32": (None, [_P, _P, _P, _I]),
+            "orc2d_wave1d_init_f32": (None, [_P, _P, _P, _P, _I]),
+            "orc2d_wave1d_iter_f32": (None, [_P, _P, _P, _P]),
             "orc2d_density": (None, [_P, _P, _P, _P]),
             "orc2d_force": (None, [_P, _P, _P, _P]),
             "orc_pbd_step": (None, [_P, _P, _I, _I]),
@@ -278,6 +280,25 @@ def wave_iter_2d_f32(params, cells4, phase: int, out_prev=None) -> np.ndarray:
     inp = np.ascontiguousarray(cells4, np.float32)
     out = np.zeros_like(inp) if out_prev is None else np.ascontiguousarray(out_prev, np.float32).copy()
     load().orc2d_wave_iter_f32(_pp(params), _p(inp), _p(out), phase)
+    return out
+
+
+def wave1d_init_2d_f32(params, mode: int, cur=None, prev=None) -> np.ndarray:
+    """Wave1D MODE_INIT_0 / MODE_INIT_1 on (newest, older) fields."""
+    n = params.wave_cells
+    c = np.zeros((n, 4), np.float32) if cur is None else np.ascontiguousarray(cur, np.float32)
+    q = np.zeros((n, 4), np.float32) if prev is None else np.ascontiguousarray(prev, np.float32)
+    out = np.zeros((n, 4), np.float32)
+    load().orc2d_wave1d_init_f32(_pp(params), _p(c), _p(q), _p(out), int(mode))
+    return out
+
+
+def wave1d_iter_2d_f32(params, cur, prev) -> np.ndarray:
+    """One Wave1D MODE_ITERATE step with free boundaries."""
+    c = np.ascontiguousarray(cur, np.float32)
+    q = np.ascontiguousarray(prev, np.float32)
+    out = np.zeros_like(c)
+    load().orc2d_wave1d_iter_f32(_pp(params), _p(c), _p(q), _p(out))
     return out
 
 

@@ -35,6 +35,7 @@ def test_abi_version_and_status_strings(lib):
 def test_struct_layouts_match_header(tmp_path):
     """ctypes mirrors of the ABI structs have the C compiler's size and offsets."""
     structs = {"cwa_scene_desc": _abi.SceneDesc, "cwa_sim_options": _abi.SimOptions,
+               "cwa2d_params": _abi.Params2D, "cwa_pbd_params": _abi.PbdParams,
                "cwa_device_view": _abi.DeviceView, "cwa_camera": _abi.Camera,
                "cwa_render_params": _abi.RenderParams, "cwa_tune_report": _abi.TuneReport,
                "cwa_wave_tune_report": _abi.WaveTuneReport}

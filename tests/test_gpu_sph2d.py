@@ -127,3 +127,85 @@ def test_errors(lib):
     with Sim2D(defaults2d()) as sim:
         with pytest.raises(CwaError):
             sim.run_pass("density")  # needs a grid pass first
+
+
+# ---- the Wave1D kind (Wave1D_cs.glsl, the app's InitWaveEquation) ----
+
+def _w1():
+    from coupledwateranimation_gb300.sim2d import WAVE2D_1D
+    return defaults2d(WAVE2D_1D)
+
+
+def test_wave1d_reinit_and_iterate_bit_exact(lib, orc):
+    p = _w1()
+    with Sim2D(p) as sim:
+        newest, older = sim.download_wave(), sim.download_wave_prev()
+        # Reinit: MODE_INIT_0 (exp: within float rounding), then MODE_INIT_1
+        # on it with a zero older field (bit for bit from the device's bump)
+        assert np.allclose(older, orc.wave1d_init_2d_f32(p, 0), rtol=1e-5, atol=1e-37)
+        want1 = orc.wave1d_init_2d_f32(p, 1, cur=older, prev=np.zeros_like(older))
+        assert np.array_equal(_bits(newest), _bits(want1))
+        sim.run_pass("wave_iterate")
+        a, a_old = sim.download_wave(), sim.download_wave_prev()
+        sim.splash()  # MODE_INIT_1 on the current field
+        b, b_old = sim.download_wave(), sim.download_wave_prev()
+    assert np.array_equal(_bits(a), _bits(orc.wave1d_iter_2d_f32(p, newest, older)))
+    assert np.array_equal(_bits(a_old), _bits(newest))
+    assert np.array_equal(_bits(b), _bits(orc.wave1d_init_2d_f32(p, 1, cur=a, prev=a_old)))
+    assert np.array_equal(_bits(b_old), _bits(a))
+
+
+@pytest.mark.parametrize("frames", [1, 5])
+def test_wave1d_frames_bit_exact(lib, orc, frames):
+    # ten substeps per frame rotate the three buffers by one each frame, so
+    # frames replay one graph per buffer phase
+    p = _w1()
+    rng = np.random.default_rng(frames)
+    cur = (0.05 * rng.standard_normal((p.wave_cells, 4))).astype(np.float32)
+    old = (0.05 * rng.standard_normal((p.wave_cells, 4))).astype(np.float32)
+    with Sim2D(p) as sim:
+        sim.upload_wave(cur)
+        sim.upload_wave_prev(old)
+        sim.step(frames)
+        got, got_old = sim.download_wave(), sim.download_wave_prev()
+    for _ in range(frames * p.wave_substeps):
+        cur, old = orc.wave1d_iter_2d_f32(p, cur, old), cur
+    assert np.array_equal(_bits(got), _bits(cur))
+    assert np.array_equal(_bits(got_old), _bits(old))
+
+
+def test_wave1d_graph_frames_equal_eager_passes(lib):
+    p = _w1()
+    with Sim2D(p) as a, Sim2D(p) as b:
+        a.step(4)
+        for _ in range(4):
+            for _ in range(p.sph_substeps):
+                b.run_pass("grid")
+                b.run_pass("density")
+                b.run_pass("force")
+            for _ in range(p.wave_substeps):
+                b.run_pass("wave_iterate")
+        pa, pb = a.download_particles(), b.download_particles()
+        assert np.array_equal(pa.view(np.uint8), pb.view(np.uint8))
+        assert np.array_equal(_bits(a.download_wave()), _bits(b.download_wave()))
+        assert np.array_equal(_bits(a.download_wave_prev()), _bits(b.download_wave_prev()))
+
+
+def test_wave_kind_errors(lib):
+    from coupledwateranimation_gb300 import CwaError
+
+    p = defaults2d()
+    p.wave_kind = 7
+    with pytest.raises(CwaError):
+        Sim2D(p)
+    with Sim2D(defaults2d()) as sim:
+        with pytest.raises(CwaError):
+            sim.run_pass("wave_iterate")
+        with pytest.raises(CwaError):
+            sim.download_wave_prev()
+    with Sim2D(_w1()) as sim:
+        with pytest.raises(CwaError):
+            sim.run_pass("wave_predict")
+        sim.step(2)
+        w = sim.download_wave()
+        assert np.isfinite(w).all()
