@@ -193,6 +193,7 @@ _PROTOS = {
     "cwa_get_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "cwa_autotune": (C.c_int, [_P, _I32, C.POINTER(TuneReport)]),
     "cwa_autotune_wave": (C.c_int, [_P, _I32, C.POINTER(WaveTuneReport)]),
+    "cwa_debug_fail_alloc": (C.c_int, [_I32]),
     "cwa_get_options": (C.c_int, [_P, C.POINTER(SimOptions)]),
     "cwa_scan_workspace_bytes": (C.c_size_t, [_I32]),
     "cwa_exclusive_scan_i32": (C.c_int, [_P, _P, _I32, _P, C.c_size_t, _P]),

@@ -10,10 +10,12 @@
 // per-scene tiles.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdio.h>
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -133,10 +135,26 @@ constexpr int kMaxScenes = 1 << 20;
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kShaderPi = 3.141592741;  // PI #define of the reference shaders
 
+// Fault injection for tests (cwa_debug_fail_alloc): the countdown's n-th
+// device allocation from now on fails as if the device were out of memory.
+std::atomic<int64_t> g_fail_alloc_in{-1};
+
+bool injected_alloc_failure() {
+  int64_t v = g_fail_alloc_in.load();
+  while (v >= 0) {
+    if (g_fail_alloc_in.compare_exchange_weak(v, v - 1)) return v == 0;
+  }
+  return false;
+}
+
 template <class T>
 cwa_status dev_alloc(cwa_sim* s, T** p, size_t count) {
   *p = nullptr;
   if (count == 0) count = 1;
+  if (injected_alloc_failure()) {
+    set_error("cudaMalloc: out of memory (injected by cwa_debug_fail_alloc)");
+    return CWA_ERR_OOM;
+  }
   cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
   if (e != cudaSuccess) {
     set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
@@ -517,17 +535,30 @@ cwa_status record(cwa_sim* s, int idx) {
   return CWA_OK;
 }
 
+// One NVTX range per pass on the host thread that enqueues it (eager steps;
+// a graph replay shows as the enclosing cwa_step range).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+
+template <class F>
+cwa_status traced(const char* name, F&& f) {
+  NvtxRange r(name);
+  return f();
+}
+
 cwa_status enqueue_step(cwa_sim* s) {
   CWA_TRY(record(s, 0));
-  CWA_TRY(run_grid(s));
+  CWA_TRY(traced("cwa grid", [&] { return run_grid(s); }));
   CWA_TRY(record(s, 1));
-  CWA_TRY(run_rho_pres(s));
+  CWA_TRY(traced("cwa rho_pres", [&] { return run_rho_pres(s); }));
   CWA_TRY(record(s, 2));
-  CWA_TRY(run_force(s));
+  CWA_TRY(traced("cwa force", [&] { return run_force(s); }));
   CWA_TRY(record(s, 3));
-  CWA_TRY(run_integrate(s));
+  CWA_TRY(traced("cwa integrate", [&] { return run_integrate(s); }));
   CWA_TRY(record(s, 4));
-  CWA_TRY(run_wave(s));
+  CWA_TRY(traced("cwa wave", [&] { return run_wave(s); }));
   CWA_TRY(record(s, 5));
   if (s->profiling) s->pass_times_valid = true;
   return CWA_OK;
@@ -961,6 +992,7 @@ cwa_status cwa_render(cwa_sim* s, int32_t scene, const cwa_camera* cam, const cw
 cwa_status cwa_step(cwa_sim* s, int32_t n_steps) {
   CWA_TRY(check_sim(s));
   if (n_steps < 0) return arg_error("n_steps < 0");
+  NvtxRange range("cwa_step");
   for (int32_t k = 0; k < n_steps; ++k) {
     if (s->opt.use_graph && !s->profiling)
       CWA_TRY(graph_step(s));
@@ -1015,6 +1047,7 @@ cwa_status cwa_pass_wave(cwa_sim* s) {
 cwa_status cwa_wave_advance(cwa_sim* s, int32_t n_steps) {
   CWA_TRY(check_sim(s));
   if (n_steps < 0) return arg_error("n_steps < 0");
+  NvtxRange range("cwa_wave_advance");
   return run_wave_advance(s, n_steps);
 }
 
@@ -1224,6 +1257,12 @@ cwa_status cwa_get_pass_times(cwa_sim* s, float* ms, int32_t n) {
   if (!s->pass_times_valid) return arg_error("no profiled step yet (cwa_set_profiling, then cwa_step)");
   CWA_CUDA(cudaEventSynchronize(s->ev[CWA_PASS_COUNT]));
   for (int k = 0; k < CWA_PASS_COUNT; ++k) CWA_CUDA(cudaEventElapsedTime(ms + k, s->ev[k], s->ev[k + 1]));
+  return CWA_OK;
+}
+
+cwa_status cwa_debug_fail_alloc(int32_t n) {
+  if (n < -1) return arg_error("n must be -1 (off) or >= 0");
+  g_fail_alloc_in.store(n);
   return CWA_OK;
 }
 

@@ -138,3 +138,10 @@ def test_generated_scenes_shapes():
         assert 1000 <= sc.desc.n_particles <= 80000
         assert sc.desc.wave_nx in (64, 128, 256, 512)
         assert sc.desc.cell_size >= sc.desc.smoothing_length
+
+
+def test_fault_injection_hook_arguments(lib):
+    """cwa_debug_fail_alloc validates its argument without touching a GPU."""
+    f = _abi.load().cwa_debug_fail_alloc
+    assert f(-2) == 1  # CWA_ERR_INVALID_ARG
+    assert f(5) == 0 and f(-1) == 0
