@@ -64,8 +64,9 @@ class SimOptions(C.Structure):
 
 
 # CWA_WAVE_BLOCK_*: box rows x steps per launch; R = box column in registers,
-# P = 256-wide box with column pairs in registers
-WAVE_BLOCKS = ("32x4", "64x4", "64x8", "R32x4", "R64x4", "R64x8", "P32x4")
+# P = 256-wide box with column pairs in registers, S = persistent register
+# form with the next box prefetched
+WAVE_BLOCKS = ("32x4", "64x4", "64x8", "R32x4", "R64x4", "R64x8", "P32x4", "S32x4")
 
 
 class WaveTuneReport(C.Structure):

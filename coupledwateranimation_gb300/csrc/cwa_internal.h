@@ -183,9 +183,10 @@ cudaError_t launch_totals(const float4* pos, const float4* vel, int32_t poff, in
 // ---- temporally blocked wave advance (cwa_wave_tma.cu) ----
 // Block variants (box 128 x 32 / K 4, 128 x 64 / K 4, 128 x 64 / K 8, each
 // with the column walk in shared memory or held in registers, and a 256 x 32
-// / K 4 box with column pairs in registers): K wave steps per launch, equal
-// to the halo width.
-constexpr int kWaveVariants = 7;
+// / K 4 box with column pairs in registers, and a persistent register-column
+// form that prefetches each CTA's next 128 x 32 box): K wave steps per
+// launch, equal to the halo width.
+constexpr int kWaveVariants = 8;
 int wave_variant_steps(int variant);
 
 // One block tile: patch (bx, by) of a scene's field; tma = rows load by TMA.

@@ -40,9 +40,9 @@ constexpr int kWaveTmaThreads = kBoxW;  // one thread per box column
 
 // The block variants the tuner chooses from: box height and steps per launch
 // (= halo).  Output patch (128 - 2K) x (BOX_H - 2K).
-constexpr int kVarBoxW[kWaveVariants] = {128, 128, 128, 128, 128, 128, 256};
-constexpr int kVarBoxH[kWaveVariants] = {32, 64, 64, 32, 64, 64, 32};
-constexpr int kVarK[kWaveVariants] = {4, 4, 8, 4, 4, 8, 4};
+constexpr int kVarBoxW[kWaveVariants] = {128, 128, 128, 128, 128, 128, 256, 128};
+constexpr int kVarBoxH[kWaveVariants] = {32, 64, 64, 32, 64, 64, 32, 32};
+constexpr int kVarK[kWaveVariants] = {4, 4, 8, 4, 4, 8, 4, 4};
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
@@ -50,20 +50,21 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ bool bar_try_wait(uint32_t bar) {
+__device__ __forceinline__ bool bar_try_wait(uint32_t bar, uint32_t parity = 0) {
   uint32_t ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
       : "=r"(ok)
-      : "r"(bar)
+      : "r"(bar), "r"(parity)
       : "memory");
   return ok != 0;
 }
 
-// Bounded wait on phase 0 of the barrier: false after ~2^20 polls.
-__device__ __forceinline__ bool bar_wait_bounded(uint32_t bar) {
+// Bounded wait on the barrier's phase with the given parity: false after
+// ~2^20 polls.
+__device__ __forceinline__ bool bar_wait_bounded(uint32_t bar, uint32_t parity = 0) {
   for (int k = 0; k < (1 << 20); ++k)
-    if (bar_try_wait(bar)) return true;
+    if (bar_try_wait(bar, parity)) return true;
   return false;
 }
 
@@ -498,6 +499,129 @@ __global__ void __launch_bounds__(kWaveTmaThreads)
   }
 }
 
+// Persistent form of the register-column block: a grid of resident CTAs,
+// each taking tiles blockIdx.x, blockIdx.x + gridDim.x, ... .  A CTA owns two
+// box stages; while it walks the box of one tile, the TMA copies of its next
+// tile land in the other stage (completion on that stage's mbarrier, whose
+// phase parity flips at each reuse).  The stage of the current tile, once
+// its columns are in registers, serves as the east / west exchange arrays.
+template <int kBoxH, int kK>
+__global__ void __launch_bounds__(kWaveTmaThreads)
+    k_wave_stream(WaveBlockArgs a, int32_t n_tiles) {
+  static_assert(kK % 2 == 0, "steps run in pairs");
+  constexpr int kTileW = kBoxW - 2 * kK, kTileH = kBoxH - 2 * kK;
+  constexpr uint32_t kBoxBytes = kBoxW * kBoxH * sizeof(float);
+  extern __shared__ __align__(128) float box_mem[];  // [stage][2][kBoxH][kBoxW], then two barriers
+  float(*stage_box)[2][kBoxH][kBoxW] = reinterpret_cast<float(*)[2][kBoxH][kBoxW]>(box_mem);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(box_mem + 4 * kBoxH * kBoxW);
+  const int lx = threadIdx.x;
+  if (lx == 0) {
+    for (int st = 0; st < 2; ++st)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[st])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto origin = [](const WaveBlockTile& t, int& ox, int& oy) {
+    ox = t.bx * kTileW - kK;  // a multiple of 4 floats: 16-byte TMA x coordinate
+    oy = t.by * kTileH - kK;
+  };
+  // thread 0: the two TMA copies of tile t into stage st.  The stage last
+  // held the previous tile's exchange arrays (generic-proxy stores, ordered
+  // by that tile's final barrier); the proxy fence orders them before the
+  // async-proxy writes of the copies.
+  auto issue = [&](const WaveBlockTile& t, int st) {
+    int ox, oy;
+    origin(t, ox, oy);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    const uint32_t b = smem_u32(&bars[st]);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(2 * kBoxBytes) : "memory");
+    tma_load_2d(smem_u32(&stage_box[st][0][0][0]), a.map_cur + t.scene, ox, oy, b);
+    tma_load_2d(smem_u32(&stage_box[st][1][0][0]), a.map_prev + t.scene, ox, oy, b);
+  };
+  // bit st: parity of the next phase of stage st's barrier / copies of
+  // stage st in flight (thread 0 issues them; every thread tracks them)
+  uint32_t parity = 0, inflight = 0;
+  int tile = blockIdx.x;
+  if (tile < n_tiles && a.tiles[tile].tma) {
+    if (lx == 0) issue(a.tiles[tile], 0);
+    inflight |= 1u;
+  }
+  for (int i = 0; tile < n_tiles; ++i, tile += gridDim.x) {
+    const int st = i & 1;
+    const WaveBlockTile t = a.tiles[tile];
+    const int next = tile + gridDim.x;
+    // prefetch the next tile into the other stage (its last use, as the
+    // exchange arrays of the previous tile, ended at that tile's final sync)
+    if (next < n_tiles && a.tiles[next].tma) {
+      if (lx == 0) issue(a.tiles[next], st ^ 1);
+      inflight |= 2u >> st;  // bit st ^ 1
+    }
+    const SceneDev* S = a.scenes + t.scene;
+    const int W = S->nx, H = S->nz;
+    int ox, oy;
+    origin(t, ox, oy);
+    float(*box)[kBoxH][kBoxW] = stage_box[st];
+    if (t.tma) {
+      const uint32_t b = smem_u32(&bars[st]);
+      const uint32_t ph = (parity >> st) & 1u;
+      if (!bar_wait_bounded(b, ph)) {
+        if (lx == 0) atomicOr(a.status, kStatusTimeout);
+        // let every copy this CTA issued land before it exits
+        bar_wait_bounded(b, ph);
+        if ((inflight >> (st ^ 1)) & 1u) bar_wait_bounded(smem_u32(&bars[st ^ 1]), (parity >> (st ^ 1)) & 1u);
+        return;
+      }
+      parity ^= 1u << st;
+      inflight &= ~(1u << st);
+    } else {
+      const float* uc = a.in_cur + S->woff;
+      const float* up = a.in_prev + S->woff;
+      const int gx = ox + lx;
+      for (int ly = 0; ly < kBoxH; ++ly) {
+        const int gy = oy + ly;
+        const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
+        box[0][ly][lx] = in ? __ldg(uc + (size_t)gy * W + gx) : 0.0f;
+        box[1][ly][lx] = in ? __ldg(up + (size_t)gy * W + gx) : 0.0f;
+      }
+      __syncthreads();
+    }
+    float cu[kBoxH], pv[kBoxH];
+#pragma unroll
+    for (int ly = 0; ly < kBoxH; ++ly) {
+      cu[ly] = box[0][ly][lx];
+      pv[ly] = box[1][ly][lx];
+    }
+    __syncthreads();  // the stage becomes the exchange arrays
+    const int gx = ox + lx;
+    const float wa = S->wa, wb = S->wb, lam = S->lam, atten = S->atten;
+    const bool coupled = S->coupled != 0;
+    const float zero_deposit = coupled ? fmul(S->gain, fmul(0.0f, S->dq)) : 0.0f;
+    const bool src_col = S->line_source && gx == W / 2;
+    const int le = (gx + 1 < W && lx + 1 < kBoxW) ? lx + 1 : lx;
+    const int lw = (gx > 0 && lx > 0) ? lx - 1 : lx;
+    const int ytop = H - oy, ybot = -oy;
+    const bool edge = oy < 0 || oy + kBoxH > H || (S->line_source && W / 2 >= ox && W / 2 < ox + kBoxW);
+    if (edge)
+      reg_steps<kBoxH, kK, true>(cu, pv, box[0], box[1], lx, le, lw, ytop, ybot, wa, wb, lam, atten, src_col,
+                                 coupled, zero_deposit);
+    else
+      reg_steps<kBoxH, kK, false>(cu, pv, box[0], box[1], lx, le, lw, ytop, ybot, wa, wb, lam, atten, src_col,
+                                  coupled, zero_deposit);
+    float* oc = a.out_cur + S->woff;
+    float* op = a.out_prev + S->woff;
+    if (lx >= kK && lx < kBoxW - kK && gx < W) {
+#pragma unroll
+      for (int ly = kK; ly < kBoxH - kK; ++ly) {
+        if (ly < ytop) {
+          const size_t g = (size_t)(oy + ly) * W + gx;
+          oc[g] = cu[ly];
+          op[g] = pv[ly];
+        }
+      }
+    }
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static bool tried = false;
@@ -561,9 +685,30 @@ cudaError_t launch_variant(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t
 }
 }  // namespace
 
+// The persistent form: as many resident CTAs as fit, at most one per tile.
+cudaError_t launch_stream(const WaveBlockArgs& a, int32_t n_tiles, cudaStream_t stream) {
+  constexpr int kH = 32, kK = 4;
+  constexpr int bytes = 4 * kH * kBoxW * (int)sizeof(float) + 16;
+  static int grid_cap = 0;
+  if (grid_cap == 0) {
+    cudaError_t e = cudaFuncSetAttribute(k_wave_stream<kH, kK>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    int dev = 0, sms = 0, per_sm = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wave_stream<kH, kK>, kWaveTmaThreads, bytes);
+    if (e != cudaSuccess) return e;
+    grid_cap = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  const int grid = n_tiles < grid_cap ? n_tiles : grid_cap;
+  k_wave_stream<kH, kK><<<grid, kWaveTmaThreads, bytes, stream>>>(a, n_tiles);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_wave_block(const WaveBlockArgs& a, int32_t n_tiles, int variant, cudaStream_t stream) {
   if (n_tiles <= 0) return cudaSuccess;
   switch (variant) {
+    case 7: return launch_stream(a, n_tiles, stream);
     case 1: return launch_variant<64, 4, kShared>(a, n_tiles, stream);
     case 2: return launch_variant<64, 8, kShared>(a, n_tiles, stream);
     case 3: return launch_variant<32, 4, kReg>(a, n_tiles, stream);

@@ -133,7 +133,9 @@ enum {
   CWA_WAVE_BLOCK_R64x4 = 4, /* registers, H 64, K 4 */
   CWA_WAVE_BLOCK_R64x8 = 5, /* registers, H 64, K 8 */
   CWA_WAVE_BLOCK_P32x4 = 6, /* registers, 256 x 32 box, two columns a thread, K 4 */
-  CWA_WAVE_BLOCK_COUNT = 7
+  CWA_WAVE_BLOCK_S32x4 = 7, /* registers, H 32, K 4, persistent CTAs that prefetch
+                               their next box while walking the current one */
+  CWA_WAVE_BLOCK_COUNT = 8
 };
 
 /* Borrowed device pointers of one scene, all in the current sorted order.
