@@ -5,11 +5,15 @@ Loading fails loudly when the library is missing: there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
 
-LIB_PATH = Path(__file__).resolve().parent / "libcwa.so"
+# CWA_LIBRARY=debug selects the index-checked build (libcwa_debug.so, made by
+# build.build(debug=True)); the default is the release library.
+LIB_PATH = Path(__file__).resolve().parent / (
+    "libcwa_debug.so" if os.environ.get("CWA_LIBRARY") == "debug" else "libcwa.so")
 
 # status codes
 CWA_OK = 0
@@ -21,6 +25,7 @@ CWA_ERR_NONFINITE = 5
 CWA_ERR_IO = 6
 CWA_ERR_NO_DEVICE = 7
 CWA_ERR_CAPACITY = 8
+CWA_ERR_BOUNDS = 9
 
 PRESET_REFERENCE_3D = 0
 PRESET_MULLER = 1

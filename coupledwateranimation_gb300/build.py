@@ -18,6 +18,9 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 OBJDIR = PKG / "_build"
 LIB = PKG / "libcwa.so"
+# the index-checked build (CWA_DEBUG_CHECKS): separate objects and library
+OBJDIR_DEBUG = PKG / "_build_debug"
+LIB_DEBUG = PKG / "libcwa_debug.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-O3", "-fPIC", "-ffp-contract=off", "-fno-fast-math"]
@@ -51,35 +54,39 @@ def _compile(cmd: list[str]) -> None:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
+def build(force: bool = False, verbose: bool = False, debug: bool = False) -> Path:
+    """Compile and link libcwa.so; with debug=True, libcwa_debug.so, the same
+    sources with the device index checks of CWA_DEBUG_CHECKS compiled in."""
     nvcc = _nvcc()
-    OBJDIR.mkdir(exist_ok=True)
+    objdir, lib_out = (OBJDIR_DEBUG, LIB_DEBUG) if debug else (OBJDIR, LIB)
+    defs = ["-DCWA_DEBUG_CHECKS"] if debug else []
+    objdir.mkdir(exist_ok=True)
     deps = _headers()
     jobs = []
     objs = []
     for src in sorted(CSRC.glob("*.cu")):
-        obj = OBJDIR / (src.stem + ".o")
+        obj = objdir / (src.stem + ".o")
         objs.append(obj)
         if force or _stale(src, obj, deps):
-            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler",
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", *defs, "-Xcompiler",
                          ",".join(HOST_FLAGS), "-c", str(src), "-o", str(obj)])
     cxx = os.environ.get("CXX", "g++")
     for src in sorted(CSRC.glob("*.cpp")):
-        obj = OBJDIR / (src.stem + ".o")
+        obj = objdir / (src.stem + ".o")
         objs.append(obj)
         if force or _stale(src, obj, deps):
-            jobs.append([cxx, *HOST_FLAGS, "-std=c++17", "-I", _cuda_include(nvcc), "-c", str(src),
+            jobs.append([cxx, *HOST_FLAGS, "-std=c++17", *defs, "-I", _cuda_include(nvcc), "-c", str(src),
                          "-o", str(obj)])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(_compile, jobs))
-    if force or jobs or not LIB.exists():
-        tmp = LIB.with_suffix(".so.tmp")
+    if force or jobs or not lib_out.exists():
+        tmp = lib_out.with_suffix(".so.tmp")
         _compile([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fPIC"])
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib_out)
     if verbose:
-        print(f"built {LIB}")
-    return LIB
+        print(f"built {lib_out}")
+    return lib_out
 
 
 if __name__ == "__main__":

@@ -382,7 +382,7 @@ cwa_status run_grid(cwa_sim* s) {
   s->counts_pending = false;  // the scan consumes (and clears) the counts
   CWA_CUDA(scan_launch(s->count, s->start, s->c_total, s->c_total + 1, true, s->scan, s->d_status, st,
                        &s->launches, flag));
-  CWA_CUDA(launch_list_insert(s->key, s->slot, s->start, s->list, s->n_total, flag, st));
+  CWA_CUDA(launch_list_insert(s->key, s->slot, s->start, s->list, s->n_total, flag, st, s->d_status));
   CWA_CUDA(launch_rank_reorder(s->key, s->slot, s->start, s->list, s->P[cur], s->V[cur],
                                s->move_force ? s->F[cur] : nullptr, s->ID[cur], s->P[nxt], s->V[nxt],
                                s->move_force ? s->F[nxt] : nullptr, s->ID[nxt], s->KS, s->n_total, s->d_status,
@@ -437,7 +437,7 @@ cwa_status run_integrate(cwa_sim* s) {
 cwa_status run_wave(cwa_sim* s) {
   const int w = s->wcur;
   CWA_CUDA(launch_wave(s->U[w], s->U[(w + 2) % 3], s->U[(w + 1) % 3], s->D, s->d_wtiles, s->n_wtiles, s->wtile,
-                       s->d_scenes, s->stream));
+                       s->d_scenes, s->stream, s->d_status));
   s->launches += 1;
   s->wcur = (w + 1) % 3;  // StencilImage2DTripleBuffered::PingPong (:33-40)
   s->steps += 1;
@@ -618,6 +618,10 @@ cwa_status read_status(cwa_sim* s) {
   if (v == 0) return CWA_OK;
   CWA_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(int32_t), s->stream));
   CWA_CUDA(cudaStreamSynchronize(s->stream));
+  if (v & kStatusBounds) {
+    set_error("an index check of the debug build failed; the access was skipped");
+    return CWA_ERR_BOUNDS;
+  }
   if (v & kStatusTimeout) {
     set_error("a bounded device wait (scan look-back) timed out");
     return CWA_ERR_TIMEOUT;
@@ -661,6 +665,7 @@ const char* cwa_status_str(cwa_status s) {
     case CWA_ERR_IO: return "I/O error";
     case CWA_ERR_NO_DEVICE: return "no CUDA device";
     case CWA_ERR_CAPACITY: return "capacity exceeded";
+    case CWA_ERR_BOUNDS: return "debug index check failed";
   }
   return "unknown status";
 }

@@ -19,6 +19,20 @@ __device__ __forceinline__ int cell_axis(float p, float lo, float cell, int n) {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// Index checks of the debug build (compiled with CWA_DEBUG_CHECKS): a failed
+// check records kStatusBounds in the status word and evaluates to true, so
+// the caller skips the access; release builds compile every check to false.
+// They stand in for a memory checker: no trap, the context stays usable.
+__device__ __forceinline__ bool dcheck_failed(bool ok, int32_t* status) {
+  if (!ok && status) atomicOr(status, kStatusBounds);
+  return !ok;
+}
+#ifdef CWA_DEBUG_CHECKS
+#define CWA_DCHECK_FAILED(cond, status) (::cwa::dcheck_failed((cond), (status)))
+#else
+#define CWA_DCHECK_FAILED(cond, status) (false)
+#endif
+
 __device__ __forceinline__ bool finite3(float4 p) {
   return isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
 }

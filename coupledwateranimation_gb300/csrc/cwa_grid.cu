@@ -195,6 +195,7 @@ __global__ void __launch_bounds__(256)
     int cy = cell_axis(p.y, ly, cs, ny);
     int cz = cell_axis(p.z, lz, csz, nz);
     int k = coff + (cx * ny + cy) * nz + cz;
+    if (CWA_DCHECK_FAILED(k >= coff && k < coff + nx * ny * nz, status)) continue;
     key[i] = k;
     slot[i] = count_slot(count, k);
   }
@@ -214,11 +215,13 @@ __global__ void k_point_hash(const float4* __restrict__ pos, int32_t n, float lx
 
 __global__ void k_list_insert(const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
                               const int32_t* __restrict__ start, int32_t* __restrict__ list, int32_t n,
-                              const int32_t* flag) {
+                              const int32_t* flag, int32_t* status) {
   if (flag && __ldg(flag) == 0) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  list[start[key[i]] + slot[i]] = i;
+  const int k = key[i], dst = start[k] + slot[i];
+  if (CWA_DCHECK_FAILED(k >= 0 && dst >= start[k] && dst < start[k + 1] && dst < n, status)) return;
+  list[dst] = i;
 }
 
 // Stable rank of particle i in its cell = members with a smaller index.
@@ -247,6 +250,7 @@ __global__ void __launch_bounds__(256)
   int k = key[i];
   int b = start[k], e = start[k + 1];
   int dst = b + stable_rank(list, b, e, i, slot[i], status);
+  if (CWA_DCHECK_FAILED(dst >= b && dst < e && dst < n, status)) return;
   pout[dst] = pin[i];
   vout[dst] = vin[i];
   if (fout) fout[dst] = fin[i];
@@ -331,9 +335,9 @@ cudaError_t launch_hash_count(const float4* pos, const Tile* tiles, int32_t n_ti
 }
 
 cudaError_t launch_list_insert(const int32_t* key, const int32_t* slot, const int32_t* start, int32_t* list,
-                               int32_t n, const int32_t* flag, cudaStream_t stream) {
+                               int32_t n, const int32_t* flag, cudaStream_t stream, int32_t* status) {
   if (n <= 0) return cudaSuccess;
-  k_list_insert<<<blocks_for(n, 256), 256, 0, stream>>>(key, slot, start, list, n, flag);
+  k_list_insert<<<blocks_for(n, 256), 256, 0, stream>>>(key, slot, start, list, n, flag, status);
   return cudaGetLastError();
 }
 

@@ -17,7 +17,8 @@ namespace cwa {
 enum : int32_t {
   kStatusNonFinite = 1,  // a NaN/Inf position reached the cell hash
   kStatusTimeout = 2,    // a bounded spin (scan look-back) gave up
-  kStatusBigCell = 4     // a cell above kMaxStableCell members: insert order not stable
+  kStatusBigCell = 4,    // a cell above kMaxStableCell members: insert order not stable
+  kStatusBounds = 8      // a debug-build index check failed (the access was skipped)
 };
 
 // Members above which a cell's insert order falls back to arrival order.
@@ -86,7 +87,7 @@ cudaError_t launch_hash_count(const float4* pos, const Tile* tiles, int32_t n_ti
                               const SceneDev* scenes, int32_t* key, int32_t* slot, int32_t* count,
                               int32_t* status, const int32_t* flag, cudaStream_t stream);
 cudaError_t launch_list_insert(const int32_t* key, const int32_t* slot, const int32_t* start, int32_t* list,
-                               int32_t n, const int32_t* flag, cudaStream_t stream);
+                               int32_t n, const int32_t* flag, cudaStream_t stream, int32_t* status = nullptr);
 // Moves the particle state into sorted order and writes each particle's cell
 // key (kout) in that order.
 cudaError_t launch_rank_reorder(const int32_t* key, const int32_t* slot, const int32_t* start,
@@ -163,7 +164,7 @@ cudaError_t launch_integrate(float4* pos, float4* vel, float4* force, float2* rh
                              cudaStream_t stream);
 cudaError_t launch_wave(const float* u_n, const float* u_nm1, float* u_out, unsigned long long* deposits,
                         const Tile* wtiles, int32_t n_wtiles, int32_t wtile_size, const SceneDev* scenes,
-                        cudaStream_t stream);
+                        cudaStream_t stream, int32_t* status = nullptr);
 cudaError_t launch_wave_init(float* u, int32_t nx, int32_t nz, float mode, cudaStream_t stream);
 // u(x, y) = red(2x, y) / 255 of a w x h RGBA8 image (device memory), 0 past it.
 cudaError_t launch_wave_from_image(float* u, int32_t nx, int32_t nz, const uint8_t* rgba, int32_t w, int32_t h,

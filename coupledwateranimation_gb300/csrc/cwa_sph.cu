@@ -382,14 +382,18 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   bool overflow = false;
 #pragma unroll
   for (int r = 0; r < 9; ++r) {
-    const int len = e[r] - b[r];
+    int len = e[r] - b[r];
+    if (CWA_DCHECK_FAILED(len == 0 || (b[r] >= 0 && len > 0 && e[r] <= n_total), status)) len = 0;
     const int off0 = b[r] - base[r];
     overflow |= off0 + len > kRowCodeMax;
     const uint32_t code0 = ((uint32_t)r << kRowCodeBits) + (uint32_t)off0;
     T part = (T)0;
     if (len > 0) {
       if (staged) {
-        const float4* cand = s_cand + (sp.seg_off[g * 9 + r] + (b[r] - sp.seg_b[g * 9 + r]));
+        const int so = sp.seg_off[g * 9 + r] + (b[r] - sp.seg_b[g * 9 + r]);
+        if (CWA_DCHECK_FAILED(g >= 0 && g < sp.ncols && so >= 0 && so + len <= sp.seg_off[kMaxSegs], status))
+          continue;
+        const float4* cand = s_cand + so;
         part = scan_row<MODE == MODE_DENSITY, T>([&](int o) { return cand[o]; }, len, code0, px, py, pz, hit2,
                                                  hp, hp_end);
       } else {
@@ -548,7 +552,7 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
             const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
             const SceneDev* __restrict__ scenes, const float* __restrict__ wave, float4* __restrict__ force,
             const uint16_t* __restrict__ nbr, const int32_t* __restrict__ nbr_cnt, int32_t n_total,
-            const float4* __restrict__ xpair, const float4* __restrict__ vpair) {
+            const float4* __restrict__ xpair, const float4* __restrict__ vpair, int32_t* status) {
   using T = Real<P>;
   __shared__ int32_t s_rb[9][kNbThreads];
   const Tile tl = tiles[blockIdx.x];
@@ -607,7 +611,8 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int j = s_rb[code[u] >> kRowCodeBits][threadIdx.x] + (int)(code[u] & (kRowCodeMax - 1));
-        if (code[u] != self_code) pair_global(j);
+        if (code[u] != self_code && !CWA_DCHECK_FAILED((code[u] >> kRowCodeBits) < 9 && j >= 0 && j < n_total, status))
+          pair_global(j);
       }
       fp.flush();
       fv.flush();
@@ -709,7 +714,7 @@ template <int P, int MB>
 void force_variant(const NbArgs& a, cudaStream_t st) {
   k_force<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles, a.scenes,
                                                     a.wave, a.force, a.nbr, a.nbr_cnt, a.n_total, a.xpair,
-                                                    a.vpair);
+                                                    a.vpair, a.status);
 }
 
 template <int P>

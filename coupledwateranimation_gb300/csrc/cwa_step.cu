@@ -86,7 +86,8 @@ __global__ void __launch_bounds__(128)
         const float lim = 4611686018427387904.0f;  // 2^62
         sq = fminf(fmaxf(sq, -lim), lim);
         const long long q = __float2ll_rn(sq);
-        atomicAdd(deposits + S->woff + (size_t)ck * W + ci, (unsigned long long)q);
+        if (!CWA_DCHECK_FAILED(ci >= 0 && ci < W && ck >= 0 && ck < Hn, status))
+          atomicAdd(deposits + S->woff + (size_t)ck * W + ci, (unsigned long long)q);
       }
       const float nx = -fmul(gx, fmul((float)W, S->uvs[0]));
       const float nz = -fmul(gz, fmul((float)Hn, S->uvs[1]));
@@ -129,6 +130,7 @@ __global__ void __launch_bounds__(128)
     const int k = S->coff + (cell_axis(pn.x, S->lo[0], S->cell, S->dims[0]) * ny +
                              cell_axis(pn.y, S->lo[1], S->cell, ny)) * nz +
                   cell_axis(pn.z, S->lo[2], S->cellz, nz);
+    if (CWA_DCHECK_FAILED(k >= S->coff && k < S->coff + S->ncells, status)) return;
     key[i] = k;
     slot[i] = count_slot(count, k);
   }
@@ -164,12 +166,13 @@ constexpr int kWaveCellsPerThread = 4;
 __global__ void __launch_bounds__(256)
     k_wave(const float* __restrict__ un, const float* __restrict__ unm1, float* __restrict__ uout,
            unsigned long long* __restrict__ deposits, const Tile* __restrict__ tiles,
-           const SceneDev* __restrict__ scenes) {
+           const SceneDev* __restrict__ scenes, int32_t* status) {
   const Tile tl = tiles[blockIdx.x];
   const SceneDev* S = scenes + tl.scene;
   const int W = S->nx, H = S->nz, woff = S->woff;
   const int local0 = tl.begin - woff + threadIdx.x * kWaveCellsPerThread;
   if (local0 + woff >= tl.end) return;
+  if (CWA_DCHECK_FAILED(local0 >= 0 && local0 < W * H && ((W & 3) != 0 || local0 + 3 < W * H), status)) return;
   const float* u = un + woff;
   const float* um = unm1 + woff;
   float* uo = uout + woff;
@@ -366,9 +369,10 @@ cudaError_t launch_integrate(float4* pos, float4* vel, float4* force, float2* rh
 
 cudaError_t launch_wave(const float* u_n, const float* u_nm1, float* u_out, unsigned long long* deposits,
                         const Tile* wtiles, int32_t n_wtiles, int32_t wtile_size, const SceneDev* scenes,
-                        cudaStream_t stream) {
+                        cudaStream_t stream, int32_t* status) {
   if (n_wtiles <= 0) return cudaSuccess;
-  k_wave<<<n_wtiles, wtile_size / kWaveCellsPerThread, 0, stream>>>(u_n, u_nm1, u_out, deposits, wtiles, scenes);
+  k_wave<<<n_wtiles, wtile_size / kWaveCellsPerThread, 0, stream>>>(u_n, u_nm1, u_out, deposits, wtiles, scenes,
+                                                                    status);
   return cudaGetLastError();
 }
 

@@ -38,7 +38,9 @@ typedef enum cwa_status {
   CWA_ERR_NONFINITE = 5,   /* a NaN/Inf particle position was met            */
   CWA_ERR_IO = 6,          /* checkpoint file could not be read or written   */
   CWA_ERR_NO_DEVICE = 7,   /* no CUDA device / driver                        */
-  CWA_ERR_CAPACITY = 8     /* size beyond a stated maximum                   */
+  CWA_ERR_CAPACITY = 8,    /* size beyond a stated maximum                   */
+  CWA_ERR_BOUNDS = 9       /* an index check of a debug build failed (the
+                              access was skipped); release builds do not check */
 } cwa_status;
 
 /* Physics presets.

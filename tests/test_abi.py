@@ -27,7 +27,7 @@ def test_exports_every_declared_symbol(lib):
 
 def test_abi_version_and_status_strings(lib):
     assert lib.cwa_abi_version() == 1
-    for s in range(9):
+    for s in range(10):
         assert _abi.status_str(s) != "unknown status"
     assert _abi.status_str(99) == "unknown status"
 
