@@ -49,6 +49,12 @@ UNIT = "updates/s"
 # the sort's 160), so the grid pass carries the reorder's 140.
 BYTES_PER_PARTICLE = {"grid": 140, "rho_pres": 24, "force": 64, "integrate": 100 + 20}
 BYTES_PER_GRID_CELL = {"grid": 28}
+# The neighbour passes' second bound: algorithmic FP32 flops per particle of
+# the 27-cell search (216 candidates x 7 flop for the distance test, plus
+# ~33 hits x 10 for the density or x 40 for the pressure/viscosity pair).
+FLOP_PER_PARTICLE = {"rho_pres": 216 * 7 + 33 * 10, "force": 216 * 7 + 33 * 40}
+# FP32 non-tensor peak: 152 SMs x 128 lanes x 2 flop (FMA) x the maximum SM clock
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 BYTES_PER_WAVE_CELL = {"wave": 20}
 FALLBACK_HBM_GBS = 6800.0
 
@@ -338,6 +344,8 @@ def run_gpu(args) -> None:
            + BYTES_PER_WAVE_CELL.get(p, 0) * n_w for p in cwa.PASSES}
     peak, peak_kind = _peaks()
     achieved = alg[top] / (pass_ms[top] * 1e-3) / 1e9
+    fp32_achieved = (FLOP_PER_PARTICLE[top] * n_p / (pass_ms[top] * 1e-3) / 1e12
+                     if top in FLOP_PER_PARTICLE else None)
     traffic = _profiled_traffic().get(top)
 
     # end-to-end through the C ABI with pinned host buffers
@@ -406,6 +414,10 @@ def run_gpu(args) -> None:
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": alg[top],
                          "ms_per_launch": pass_ms[top]},
+            "roofline_fp32": {"bound": "fp32", "kernel": top, "unit": "TFLOP/s",
+                              "achieved": fp32_achieved, "peak": FP32_PEAK_TFLOPS, "peak_kind": "nominal",
+                              "frac": fp32_achieved / FP32_PEAK_TFLOPS if fp32_achieved else None,
+                              "flop_per_particle": FLOP_PER_PARTICLE.get(top)},
             "pass_ms": pass_ms,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps},
