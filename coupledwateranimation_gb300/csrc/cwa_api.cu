@@ -54,7 +54,7 @@ struct cwa_sim {
   int32_t* list = nullptr;
   int32_t* count = nullptr;
   int32_t* start = nullptr;
-  uint16_t* nbr = nullptr;     // this step's hit lists, kMaxNbr x n_total codes
+  uint64_t* nbm = nullptr;     // this step's hits: kNbRows row masks per particle
   int32_t* nbr_cnt = nullptr;
   int32_t* KS = nullptr;       // sorted cell key of each particle (last grid build)
   // Verlet mode
@@ -335,7 +335,7 @@ NbArgs nb_args(cwa_sim* s) {
   a.tile_size = s->ptile;
   a.scenes = s->d_scenes;
   a.wave = s->U[s->wcur];
-  a.nbr = s->nbr;
+  a.nbm = s->nbm;
   a.nbr_cnt = s->nbr_cnt;
   a.vlist = s->vlist;
   a.vcnt = s->vcnt;
@@ -775,7 +775,7 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   ALLOC(s->key, N);
   ALLOC(s->slot, N);
   ALLOC(s->list, N);
-  ALLOC(s->nbr, N * kMaxNbr);
+  ALLOC(s->nbm, N * kNbRows);
   ALLOC(s->nbr_cnt, N);
   ALLOC(s->KS, N);
   if (s->opt.precision != CWA_PREC_FP64) {

@@ -109,13 +109,18 @@ cudaError_t launch_point_rank(const int32_t* key, const int32_t* slot, const int
                               cudaStream_t stream);
 
 // ---- SPH kernels (cwa_sph.cu) ----
-// Neighbour lists hold 16-bit codes (row << 12 | offset from the row's
-// cell-based start), entry k of particle i at list[k * n_total + i].
-// nbr / nbr_cnt: this step's hits (r < h, the particle itself included),
-// written by the density pass and read by force.  vlist / vcnt: the Verlet
-// list (pairs within h (1 + skin) at the last rebuild).  A count of cap + 1
-// marks an overflowed list; its reader rescans the particle's rows.
-constexpr int kMaxNbr = 64;
+// This step's hits (r < h, the particle itself included), written by the
+// density pass and read by force: nine row masks per particle, word
+// r * n_total + i holding particle i's hits in candidate row r as bits
+// (bit b = the candidate at the row's cell-based start + b).  nbr_cnt holds
+// the rows with a nonzero mask (bit r), or -1 when some row's window reaches
+// past bit 63 (force then rescans the particle's rows).
+// The Verlet list (pairs within h (1 + skin) at the last rebuild) holds
+// 16-bit codes (row << 12 | offset from the row's cell-based start), entry k
+// of particle i at list[k * n_total + i]; a count of kMaxVerlet + 1 marks an
+// overflowed list, whose reader rescans the particle's rows.
+constexpr int kNbRows = 9;
+constexpr int kMaskBits = 64;
 constexpr int kMaxVerlet = 128;
 struct NbArgs {
   const float4* pos;
@@ -128,7 +133,7 @@ struct NbArgs {
   int32_t n_tiles, tile_size;
   const SceneDev* scenes;
   const float* wave;
-  uint16_t* nbr;
+  uint64_t* nbm;        // row masks, kNbRows x n_total
   int32_t* nbr_cnt;
   uint16_t* vlist;
   int32_t* vcnt;

@@ -22,11 +22,14 @@
 //    k_rho_list walks that list each step, tests r < h and keeps the hits.
 // Either way force runs its pair terms over the step's hit list only.
 //
-// Neighbour lists hold 16-bit codes (row << 12 | offset from the row's
-// cell-based start = start[row + max(cz - rz, 0)]), decodable from the
-// particle's sorted cell key alone, so a Verlet list stays valid while the
-// particles move.  The candidate scan can stage the CTA's rows in shared
-// memory with bulk TMA copies (cp.async.bulk, completion on an mbarrier).
+// A row's cell-based start is start[row + max(cz - rz, 0)], decodable from
+// the particle's sorted cell key alone.  The step's hits are nine 64-bit
+// row masks per particle (bit b = the row's candidate at that start + b):
+// the density pass sets bits in registers, with no per-hit store, and force
+// walks the set bits.  The Verlet list holds 16-bit codes (row << 12 |
+// offset from the same start), so it stays valid while the particles move.
+// The candidate scan can stage the CTA's rows in shared memory with bulk
+// TMA copies (cp.async.bulk, completion on an mbarrier).
 //
 // Sums are accumulated in one of three precisions (template P):
 //   CWA_PREC_FP32 plain float; CWA_PREC_COMPENSATED float partial sums (per
@@ -80,14 +83,6 @@ __device__ __forceinline__ double recip(double x) { return 1.0 / x; }
 struct CellCoord {
   int x, y, z;
 };
-
-__device__ __forceinline__ CellCoord cell_of(const SceneDev* S, float4 p) {
-  CellCoord c;
-  c.x = cell_axis(p.x, S->lo[0], S->cell, S->dims[0]);
-  c.y = cell_axis(p.y, S->lo[1], S->cell, S->dims[1]);
-  c.z = cell_axis(p.z, S->lo[2], S->cellz, S->dims[2]);
-  return c;
-}
 
 // Cell coordinates of a global cell id.
 __device__ __forceinline__ CellCoord cell_of_key(const SceneDev* S, int key) {
@@ -182,6 +177,15 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
+// One 128-bit shared load of a staged candidate, so a quarter warp's eight
+// lanes move 128 bytes per wavefront (the compiler would otherwise split the
+// load when the fourth component is unused).
+__device__ __forceinline__ float4 lds128(const float4* p) {
+  float4 v;
+  asm("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(smem_u32(p)));
+  return v;
+}
+
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -227,9 +231,6 @@ constexpr int kMaxSegs = 18;      // 2 columns x 9 rows
 // Hit lists hold codes in pairs: code k of particle i is half (k & 1) of the
 // 32-bit word (k >> 1) * n + i, so a warp writes its lanes' k-th pairs as one
 // 128-byte store and readers load two codes per load.
-__device__ __forceinline__ size_t code_slot(int k, int i, int n) {
-  return ((size_t)(k >> 1) * n + i) * 2 + (k & 1);
-}
 __device__ __forceinline__ uint32_t code_pair(const uint16_t* __restrict__ list, int k, int i, int n) {
   return __ldg(reinterpret_cast<const uint32_t*>(list) + (size_t)(k >> 1) * n + i);
 }
@@ -319,6 +320,39 @@ __device__ __forceinline__ T scan_row(Load load, int len, uint32_t code0, T px, 
   return scan_row_impl<DENSITY, true, T>(load, len, code0, px, py, pz, hit2, hp, hp_end);
 }
 
+// Candidate test of one row for the density pass: the sum of q^3 over the
+// hits and the hits themselves as bits of the row window (bit o = candidate
+// o; candidates 64 and up are tested and summed but get no bit).  The tests
+// only set register bits, so no lane stores anything per candidate.
+template <class T, class Load>
+__device__ __forceinline__ T scan_row_bits(Load load, int len, T px, T py, T pz, T hit2, uint64_t& bits) {
+  T part = (T)0;
+  uint32_t lo = 0u, hi = 0u;
+  for (int c0 = 0; c0 < len; c0 += 32) {
+    const int n = min(len - c0, 32);
+    uint32_t m = 0u, bit = 1u;
+#pragma unroll 4
+    for (int o = 0; o < n; ++o) {
+      const float4 pj = load(c0 + o);
+      const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
+      T q = fma(-dx, dx, hit2);
+      q = fma(-dy, dy, q);
+      q = fma(-dz, dz, q);
+      if (q > (T)0) {  // a miss would add (+0)^3: the sum is unchanged
+        part = fma(q * q, q, part);
+        m |= bit;
+      }
+      bit <<= 1;
+    }
+    if (c0 == 0)
+      lo = m;
+    else if (c0 == 32)
+      hi = m;
+  }
+  bits = ((uint64_t)hi << 32) | lo;
+  return part;
+}
+
 // Candidate scan.  MODE_DENSITY (per-step mode): radius h, density + this
 // step's hit list.  MODE_LIST (Verlet mode, only when the rebuild flag is
 // up): radius h (1 + skin), the Verlet list and the rebuild positions.
@@ -331,16 +365,19 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
                  const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
                  const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
                  float2* __restrict__ rho_p, uint16_t* __restrict__ list, int32_t* __restrict__ list_cnt,
-                 float4* __restrict__ xref, int32_t n_total, int32_t* status, const int32_t* __restrict__ flag,
+                 uint64_t* __restrict__ masks, float4* __restrict__ xref, int32_t n_total, int32_t* status,
+                 const int32_t* __restrict__ flag,
                  int32_t allow_stage, const float4* __restrict__ vel, float4* __restrict__ xpair,
                  float4* __restrict__ vpair) {
   using T = Real<P>;
-  constexpr int kCap = MODE == MODE_LIST ? kMaxVerlet : kMaxNbr;
+  constexpr int kCap = kMaxVerlet;  // the Verlet list build's codes per particle
   // The list build (rare: Verlet rebuilds only) reads candidates from global
   // memory, which keeps its static shared memory under 48 KB.
   constexpr bool kCanStage = MODE == MODE_DENSITY;
   __shared__ __align__(128) float4 s_cand[kCanStage ? kStageCap : 1];
-  __shared__ uint16_t s_hit[kCap + 1][kNbThreads];  // + the overflow slot
+  // the Verlet list build stages its codes (+ the overflow slot); the
+  // density pass keeps its hits in registers
+  __shared__ uint16_t s_hit[MODE == MODE_LIST ? kCap + 1 : 1][kNbThreads];
   __shared__ StagePlan sp;
   __shared__ __align__(8) uint64_t s_bar;
   if (MODE == MODE_LIST && flag && __ldg(flag) == 0) return;  // no rebuild this step
@@ -376,46 +413,63 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   row_bases(S, start, c, base);
   const int g = staged ? c.x * S->dims[1] + c.y - sp.col0 : 0;
   uint16_t* const hit_col = &s_hit[0][threadIdx.x];
-  uint16_t* const hp_end = hit_col + kCap * kNbThreads;  // the overflow slot
+  uint16_t* const hp_end = hit_col + kCap * kNbThreads;  // the overflow slot (list build)
   uint16_t* hp = hit_col;
   Sum<P> acc;
   bool overflow = false;
+  int hits = 0;  // rows with a nonzero mask (bit r)
 #pragma unroll
   for (int r = 0; r < 9; ++r) {
     int len = e[r] - b[r];
     if (CWA_DCHECK_FAILED(len == 0 || (b[r] >= 0 && len > 0 && e[r] <= n_total), status)) len = 0;
     const int off0 = b[r] - base[r];
-    overflow |= off0 + len > kRowCodeMax;
-    const uint32_t code0 = ((uint32_t)r << kRowCodeBits) + (uint32_t)off0;
-    T part = (T)0;
-    if (len > 0) {
-      if (staged) {
-        const int so = sp.seg_off[g * 9 + r] + (b[r] - sp.seg_b[g * 9 + r]);
-        if (CWA_DCHECK_FAILED(g >= 0 && g < sp.ncols && so >= 0 && so + len <= sp.seg_off[kMaxSegs], status))
-          continue;
-        const float4* cand = s_cand + so;
-        part = scan_row<MODE == MODE_DENSITY, T>([&](int o) { return cand[o]; }, len, code0, px, py, pz, hit2,
-                                                 hp, hp_end);
-      } else {
-        const float4* cand = pos + b[r];
-        part = scan_row<MODE == MODE_DENSITY, T>([&](int o) { return __ldg(cand + o); }, len, code0, px, py,
-                                                 pz, hit2, hp, hp_end);
+    const float4* cand = pos + b[r];
+    bool in_stage = staged && len > 0;
+    if (in_stage) {
+      const int so = sp.seg_off[g * 9 + r] + (b[r] - sp.seg_b[g * 9 + r]);
+      if (CWA_DCHECK_FAILED(g >= 0 && g < sp.ncols && so >= 0 && so + len <= sp.seg_off[kMaxSegs], status))
+        len = 0;
+      cand = s_cand + so;
+    }
+    if (MODE == MODE_DENSITY) {
+      // row r's hits as bits relative to the row's cell-based start
+      uint64_t bits = 0ull;
+      T part = (T)0;
+      if (len > 0) {
+        if (in_stage)
+          part = scan_row_bits<T>([&](int o) { return lds128(cand + o); }, len, px, py, pz, hit2, bits);
+        else
+          part = scan_row_bits<T>([&](int o) { return __ldg(cand + o); }, len, px, py, pz, hit2, bits);
+      }
+      overflow |= off0 + len > kMaskBits;
+      const uint64_t m = off0 < kMaskBits ? bits << off0 : 0ull;
+      masks[(size_t)r * n_total + i] = m;
+      if (m != 0ull) hits |= 1 << r;
+      acc.add(part);
+    } else {
+      overflow |= off0 + len > kRowCodeMax;
+      const uint32_t code0 = ((uint32_t)r << kRowCodeBits) + (uint32_t)off0;
+      if (len > 0) {
+        if (in_stage)
+          scan_row<false, T>([&](int o) { return cand[o]; }, len, code0, px, py, pz, hit2, hp, hp_end);
+        else
+          scan_row<false, T>([&](int o) { return __ldg(cand + o); }, len, code0, px, py, pz, hit2, hp, hp_end);
       }
     }
-    if (MODE == MODE_DENSITY) acc.add(part);
   }
-  // Coalesced list write: the pair (k, k+1) of every lane is one 128-byte
-  // store per warp.  (Row k+1 <= kCap exists: s_hit has the overflow row.)
-  const int cnt = (int)(hp - hit_col) / kNbThreads;
-  overflow |= cnt >= kCap;
-  uint32_t* const list32 = reinterpret_cast<uint32_t*>(list);
-  for (int k = 0; k < cnt; k += 2)
-    list32[(size_t)(k >> 1) * n_total + i] =
-        (uint32_t)hit_col[k * kNbThreads] | ((uint32_t)hit_col[(k + 1) * kNbThreads] << 16);
-  list_cnt[i] = overflow ? kCap + 1 : cnt;
   if (MODE == MODE_LIST) {
+    // Coalesced list write: the pair (k, k+1) of every lane is one 128-byte
+    // store per warp.  (Row k+1 <= kCap exists: s_hit has the overflow row.)
+    const int cnt = (int)(hp - hit_col) / kNbThreads;
+    overflow |= cnt >= kCap;
+    uint32_t* const list32 = reinterpret_cast<uint32_t*>(list);
+    for (int k = 0; k < cnt; k += 2)
+      list32[(size_t)(k >> 1) * n_total + i] =
+          (uint32_t)hit_col[k * kNbThreads] | ((uint32_t)hit_col[(k + 1) * kNbThreads] << 16);
+    list_cnt[i] = overflow ? kCap + 1 : cnt;
     xref[i] = pi;
   } else {
+    list_cnt[i] = overflow ? -1 : hits;
     const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
     const float2 rp = eos(S, (float)rho_t, pi, wave);
     rho_p[i] = rp;
@@ -426,19 +480,20 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
 // Verlet density: walks the particle's list (pairs within h (1 + skin) at
 // the last rebuild), accumulates the poly6 sum over r < h in groups of 8
 // (partials folded into the precision mode's accumulator), and writes this
-// step's hit list for force.  A particle whose Verlet list overflowed rescans
-// the rows of its rebuild cell.
+// step's row masks for force.  A particle whose Verlet list overflowed
+// rescans the rows of its rebuild cell.
 template <int P>
 __global__ void __launch_bounds__(kNbThreads, 8)
     k_rho_list(const float4* __restrict__ pos, const int32_t* __restrict__ start,
                const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
                const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
                float2* __restrict__ rho_p, const uint16_t* __restrict__ vlist,
-               const int32_t* __restrict__ vcnt, uint16_t* __restrict__ nbr, int32_t* __restrict__ nbr_cnt,
+               const int32_t* __restrict__ vcnt, uint64_t* __restrict__ nbm, int32_t* __restrict__ nbr_cnt,
                int32_t n_total, const float4* __restrict__ vel, float4* __restrict__ xpair,
                float4* __restrict__ vpair) {
   using T = Real<P>;
   __shared__ int32_t s_rb[9][kNbThreads];
+  __shared__ uint64_t s_m[kNbRows][kNbThreads];  // this step's row masks
   const Tile tl = tiles[blockIdx.x];
   const int i = tl.begin + threadIdx.x;
   if (i >= tl.end) return;
@@ -451,9 +506,13 @@ __global__ void __launch_bounds__(kNbThreads, 8)
   int base[9];
   row_bases(S, start, c, base);
   Sum<P> acc;
-  int cnt = 0;
+  bool overflow = false;
   const int vn = __ldg(vcnt + i);
-  auto test = [&](int j, uint32_t code) {
+#pragma unroll
+  for (int r = 0; r < kNbRows; ++r) s_m[r][threadIdx.x] = 0ull;
+  // candidate j at offset off of row r (r < 9): a hit sets its row-mask
+  // bit, or marks the particle overflowed when off is past bit 63
+  auto test = [&](int j, int r, uint32_t off) {
     const float4 pj = __ldg(pos + j);
     const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
     T q = fma(-dx, dx, h2);
@@ -461,12 +520,13 @@ __global__ void __launch_bounds__(kNbThreads, 8)
     q = fma(-dz, dz, q);
     const T qp = q > (T)0 ? q : (T)0;
     if (q > (T)0) {
-      if (cnt < kMaxNbr) nbr[code_slot(cnt, i, n_total)] = (uint16_t)code;
-      ++cnt;
+      if (off < (uint32_t)kMaskBits)
+        s_m[r][threadIdx.x] |= 1ull << off;
+      else
+        overflow = true;
     }
     return qp * qp * qp;
   };
-  bool overflow = false;
   if (vn <= kMaxVerlet) {
 #pragma unroll
     for (int r = 0; r < 9; ++r) s_rb[r][threadIdx.x] = base[r];
@@ -481,27 +541,34 @@ __global__ void __launch_bounds__(kNbThreads, 8)
       T part = (T)0;
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        const int j = s_rb[code[u] >> kRowCodeBits][threadIdx.x] + (int)(code[u] & (kRowCodeMax - 1));
-        if (k0 + u < vn) part += test(j, code[u]);
+        const int rr = (int)(code[u] >> kRowCodeBits);
+        const uint32_t off = code[u] & (kRowCodeMax - 1);
+        const int j = s_rb[rr][threadIdx.x] + (int)off;
+        if (k0 + u < vn) part += test(j, rr, off);
       }
       acc.add(part);
     }
   } else {
     // the rows of the rebuild cell over every z cell a pair within
-    // h (1 + skin) could occupy; hits are coded against the same bases
+    // h (1 + skin) could occupy; hits take bits against the same bases
     const int z1 = min(c.z + S->rz, S->dims[2] - 1);
 #pragma unroll
     for (int r = 0; r < 9; ++r) {
       if (!row_valid(S, c, r)) continue;
       const int e = __ldg(start + row_id(S, c, r) + z1 + 1);
-      overflow |= e - base[r] > kRowCodeMax;
       T part = (T)0;
-      for (int j = base[r]; j < e; ++j)
-        part += test(j, ((uint32_t)r << kRowCodeBits) + (uint32_t)(j - base[r]));
+      for (int j = base[r]; j < e; ++j) part += test(j, r, (uint32_t)(j - base[r]));
       acc.add(part);
     }
   }
-  nbr_cnt[i] = (overflow || cnt > kMaxNbr) ? kMaxNbr + 1 : cnt;
+  int rows = 0;  // rows with a nonzero mask (bit r)
+#pragma unroll
+  for (int r = 0; r < kNbRows; ++r) {
+    const uint64_t m = s_m[r][threadIdx.x];
+    nbm[(size_t)r * n_total + i] = m;
+    if (m != 0ull) rows |= 1 << r;
+  }
+  nbr_cnt[i] = overflow ? -1 : rows;
   const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
   const float2 rp = eos(S, (float)rho_t, pi, wave);
   rho_p[i] = rp;
@@ -551,10 +618,12 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
             const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
             const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
             const SceneDev* __restrict__ scenes, const float* __restrict__ wave, float4* __restrict__ force,
-            const uint16_t* __restrict__ nbr, const int32_t* __restrict__ nbr_cnt, int32_t n_total,
+            const uint64_t* __restrict__ nbm, const int32_t* __restrict__ nbr_cnt, int32_t n_total,
             const float4* __restrict__ xpair, const float4* __restrict__ vpair, int32_t* status) {
   using T = Real<P>;
-  __shared__ int32_t s_rb[9][kNbThreads];
+  // the particle's nonzero 32-bit hit words and the index of each word's bit 0
+  __shared__ uint32_t s_w[2 * kNbRows][kNbThreads];
+  __shared__ int32_t s_jb[2 * kNbRows][kNbThreads];
   const Tile tl = tiles[blockIdx.x];
   const SceneDev* S = scenes + tl.scene;
   const int i = tl.begin + threadIdx.x;
@@ -593,27 +662,52 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   const CellCoord c = cell_of_key(S, __ldg(keys + i));
   int base[9];
   row_bases(S, start, c, base);
-  if (cnt <= kMaxNbr) {
-    // The list holds the particle itself: row 4 (its own column) at offset
-    // i - base[4]; that code is skipped.
-    const uint32_t self_code = (4u << kRowCodeBits) + (uint32_t)(i - base[4]);
+  if (cnt >= 0) {
+    // The row masks hold the particle itself: row 4 (its own column) at bit
+    // i - base[4], cleared here.  The nonzero 32-bit halves are compacted in
+    // row then bit order (all nine masks are loaded, back to back); hits are
+    // then popped in that order, in groups of 8 whose neighbour indexes are
+    // found first so the gathers overlap.
+    int nw = 0, left = 0;
 #pragma unroll
-    for (int r = 0; r < 9; ++r) s_rb[r][threadIdx.x] = base[r];
-    // Groups of 8 hits: the 8 codes are loaded first so the gathers overlap.
-    for (int k0 = 0; k0 < cnt; k0 += 8) {
-      uint32_t code[8];
-#pragma unroll
-      for (int u = 0; u < 8; u += 2) {
-        const uint32_t w = k0 + u < cnt ? code_pair(nbr, k0 + u, i, n_total) : 0u;
-        code[u] = k0 + u < cnt ? (w & 0xFFFFu) : self_code;
-        code[u + 1] = k0 + u + 1 < cnt ? (w >> 16) : self_code;
+    for (int r = 0; r < kNbRows; ++r) {
+      uint64_t m = __ldg(nbm + (size_t)r * n_total + i);
+      if (r == 4) m &= ~(1ull << (i - base[4]));
+      const uint32_t lo = (uint32_t)m, hi = (uint32_t)(m >> 32);
+      if (lo) {
+        s_w[nw][threadIdx.x] = lo;
+        s_jb[nw][threadIdx.x] = base[r];
+        ++nw;
       }
+      if (hi) {
+        s_w[nw][threadIdx.x] = hi;
+        s_jb[nw][threadIdx.x] = base[r] + 32;
+        ++nw;
+      }
+      left += __popc(lo) + __popc(hi);
+    }
+    int wi = 0;
+    uint32_t cw = nw > 0 ? s_w[0][threadIdx.x] : 0u;
+    int jb = nw > 0 ? s_jb[0][threadIdx.x] : 0;
+    for (int k0 = 0; k0 < left; k0 += 8) {
+      int js[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        const int j = s_rb[code[u] >> kRowCodeBits][threadIdx.x] + (int)(code[u] & (kRowCodeMax - 1));
-        if (code[u] != self_code && !CWA_DCHECK_FAILED((code[u] >> kRowCodeBits) < 9 && j >= 0 && j < n_total, status))
-          pair_global(j);
+        js[u] = -1;
+        if (k0 + u < left) {
+          if (cw == 0u) {  // the next word (every compacted word holds a hit)
+            ++wi;
+            cw = s_w[wi][threadIdx.x];
+            jb = s_jb[wi][threadIdx.x];
+          }
+          const int t = __ffs(cw) - 1;
+          cw &= cw - 1u;
+          js[u] = jb + t;
+        }
       }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (js[u] >= 0 && !CWA_DCHECK_FAILED(js[u] < n_total, status)) pair_global(js[u]);
       fp.flush();
       fv.flush();
     }
@@ -686,13 +780,13 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
 // Launch-bound variants (min CTAs per SM): the register budget trades
 // occupancy against loads in flight per warp; the autotuner picks one.
 template <int P, int MODE>
-void scan_variant(int minb, const NbArgs& a, uint16_t* list, int32_t* cnt, float4* xref, const int32_t* flag,
-                  cudaStream_t st) {
+void scan_variant(int minb, const NbArgs& a, uint16_t* list, int32_t* cnt, uint64_t* masks, float4* xref,
+                  const int32_t* flag, cudaStream_t st) {
 #define CWA_SCAN(MB)                                                                                          \
   k_scan_cands<P, MODE, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.start, a.keys, a.tiles, a.scenes,    \
-                                                               a.wave, a.rho_p, list, cnt, xref, a.n_total,   \
-                                                               a.status, flag, a.stage, a.vel, a.xpair,       \
-                                                               a.vpair)
+                                                               a.wave, a.rho_p, list, cnt, masks, xref,       \
+                                                               a.n_total, a.status, flag, a.stage, a.vel,     \
+                                                               a.xpair, a.vpair)
   if (minb >= 8)
     CWA_SCAN(8);
   else if (minb >= 6)
@@ -705,15 +799,15 @@ void scan_variant(int minb, const NbArgs& a, uint16_t* list, int32_t* cnt, float
 template <int P>
 void dispatch_scan(bool list_mode, const NbArgs& a, cudaStream_t st) {
   if (list_mode)
-    scan_variant<P, MODE_LIST>(a.scan_minb, a, a.vlist, a.vcnt, a.xref, a.flag, st);
+    scan_variant<P, MODE_LIST>(a.scan_minb, a, a.vlist, a.vcnt, nullptr, a.xref, a.flag, st);
   else
-    scan_variant<P, MODE_DENSITY>(a.scan_minb, a, a.nbr, a.nbr_cnt, nullptr, nullptr, st);
+    scan_variant<P, MODE_DENSITY>(a.scan_minb, a, nullptr, a.nbr_cnt, a.nbm, nullptr, nullptr, st);
 }
 
 template <int P, int MB>
 void force_variant(const NbArgs& a, cudaStream_t st) {
   k_force<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles, a.scenes,
-                                                    a.wave, a.force, a.nbr, a.nbr_cnt, a.n_total, a.xpair,
+                                                    a.wave, a.force, a.nbm, a.nbr_cnt, a.n_total, a.xpair,
                                                     a.vpair, a.status);
 }
 
@@ -741,7 +835,7 @@ cudaError_t launch_rho_list(int precision, const NbArgs& a, cudaStream_t stream)
   if (a.n_tiles <= 0) return cudaSuccess;
 #define CWA_RHO_LIST(P)                                                                                     \
   k_rho_list<P><<<a.n_tiles, a.tile_size, 0, stream>>>(a.pos, a.start, a.keys, a.tiles, a.scenes, a.wave,  \
-                                                       a.rho_p, a.vlist, a.vcnt, a.nbr, a.nbr_cnt, a.n_total, \
+                                                       a.rho_p, a.vlist, a.vcnt, a.nbm, a.nbr_cnt, a.n_total, \
                                                        a.vel, a.xpair, a.vpair)
   switch (precision) {
     case CWA_PREC_FP32: CWA_RHO_LIST(CWA_PREC_FP32); break;
