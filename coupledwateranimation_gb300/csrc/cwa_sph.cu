@@ -621,9 +621,11 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
             const uint64_t* __restrict__ nbm, const int32_t* __restrict__ nbr_cnt, int32_t n_total,
             const float4* __restrict__ xpair, const float4* __restrict__ vpair, int32_t* status) {
   using T = Real<P>;
-  // the particle's nonzero 32-bit hit words and the index of each word's bit 0
-  __shared__ uint32_t s_w[2 * kNbRows][kNbThreads];
-  __shared__ int32_t s_jb[2 * kNbRows][kNbThreads];
+  // the particle's nonzero row masks and the index of each mask's bit 0
+  // (13.8 KB a CTA: eight CTAs fit the 132 KB shared carveout, which leaves
+  // the L1 more room for the gathers)
+  __shared__ uint64_t s_w[kNbRows][kNbThreads];
+  __shared__ int32_t s_jb[kNbRows][kNbThreads];
   const Tile tl = tiles[blockIdx.x];
   const SceneDev* S = scenes + tl.scene;
   const int i = tl.begin + threadIdx.x;
@@ -664,30 +666,24 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   row_bases(S, start, c, base);
   if (cnt >= 0) {
     // The row masks hold the particle itself: row 4 (its own column) at bit
-    // i - base[4], cleared here.  The nonzero 32-bit halves are compacted in
-    // row then bit order (all nine masks are loaded, back to back); hits are
-    // then popped in that order, in groups of 8 whose neighbour indexes are
-    // found first so the gathers overlap.
+    // i - base[4], cleared here.  The nonzero masks are compacted in row
+    // order (all nine are loaded, back to back); hits are then popped in row
+    // then bit order, in groups of 8 whose neighbour indexes are found first
+    // so the gathers overlap.
     int nw = 0, left = 0;
 #pragma unroll
     for (int r = 0; r < kNbRows; ++r) {
       uint64_t m = __ldg(nbm + (size_t)r * n_total + i);
       if (r == 4) m &= ~(1ull << (i - base[4]));
-      const uint32_t lo = (uint32_t)m, hi = (uint32_t)(m >> 32);
-      if (lo) {
-        s_w[nw][threadIdx.x] = lo;
+      if (m) {
+        s_w[nw][threadIdx.x] = m;
         s_jb[nw][threadIdx.x] = base[r];
         ++nw;
       }
-      if (hi) {
-        s_w[nw][threadIdx.x] = hi;
-        s_jb[nw][threadIdx.x] = base[r] + 32;
-        ++nw;
-      }
-      left += __popc(lo) + __popc(hi);
+      left += __popcll(m);
     }
     int wi = 0;
-    uint32_t cw = nw > 0 ? s_w[0][threadIdx.x] : 0u;
+    uint64_t cw = nw > 0 ? s_w[0][threadIdx.x] : 0ull;
     int jb = nw > 0 ? s_jb[0][threadIdx.x] : 0;
     for (int k0 = 0; k0 < left; k0 += 8) {
       int js[8];
@@ -695,14 +691,13 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
       for (int u = 0; u < 8; ++u) {
         js[u] = -1;
         if (k0 + u < left) {
-          if (cw == 0u) {  // the next word (every compacted word holds a hit)
+          if (cw == 0ull) {  // the next mask (every compacted mask holds a hit)
             ++wi;
             cw = s_w[wi][threadIdx.x];
             jb = s_jb[wi][threadIdx.x];
           }
-          const int t = __ffs(cw) - 1;
-          cw &= cw - 1u;
-          js[u] = jb + t;
+          js[u] = jb + __ffsll((long long)cw) - 1;
+          cw &= cw - 1ull;
         }
       }
 #pragma unroll
