@@ -25,6 +25,7 @@ constexpr int kScanTile = kScanBlock * kScanItems;
 constexpr unsigned long long kFlagAgg = 1ull << 32;
 constexpr unsigned long long kFlagInc = 2ull << 32;
 constexpr long kSpinLimit = 1l << 22;
+constexpr int kLookBack = 128;  // predecessor states a look-back round reads (4 a lane)
 
 __device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
   unsigned long long v;
@@ -123,14 +124,31 @@ __global__ void __launch_bounds__(kScanBlock)
       }
     } else {
       if (lane == 0) st_relaxed(state + tile, kFlagAgg | (unsigned int)total);
+      // Look back over windows of kLookBack predecessors (4 a lane, one
+      // round trip of loads): sum the aggregates nearer than the nearest
+      // inclusive prefix, plus that prefix; wait only while one of those
+      // nearer tiles has published nothing.  Tiles before 0 read as an
+      // inclusive prefix of 0.
       int pred = tile - 1;
       int excl = 0;
       long spins = 0;
       while (true) {
-        int idx = pred - lane;
-        unsigned long long s = idx >= 0 ? ld_relaxed(state + idx) : kFlagInc;
-        unsigned int flag = (unsigned int)(s >> 32);
-        if (__any_sync(0xffffffffu, flag == 0)) {
+        unsigned long long sv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int idx = pred - (q * 32 + lane);
+          sv[q] = idx >= 0 ? ld_relaxed(state + idx) : kFlagInc;
+        }
+        int near_inc = kLookBack;  // distance of the nearest inclusive prefix
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if ((unsigned int)(sv[q] >> 32) == 2u) near_inc = min(near_inc, q * 32 + lane);
+        near_inc = __reduce_min_sync(0xffffffffu, near_inc);
+        bool pending = false;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          pending |= q * 32 + lane < near_inc && (unsigned int)(sv[q] >> 32) == 0u;
+        if (__any_sync(0xffffffffu, pending)) {
           if (++spins > kSpinLimit) {
             if (lane == 0) atomicOr(status, kStatusTimeout);
             break;
@@ -138,15 +156,13 @@ __global__ void __launch_bounds__(kScanBlock)
           __nanosleep(32);
           continue;
         }
-        int val = (int)(unsigned int)s;
-        unsigned int inc = __ballot_sync(0xffffffffu, flag == 2u);
-        if (inc) {
-          int first = __ffs(inc) - 1;
-          excl += warp_sum(lane <= first ? val : 0);
-          break;
-        }
-        excl += warp_sum(val);
-        pred -= 32;
+        int part = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (q * 32 + lane <= near_inc) part += (int)(unsigned int)sv[q];
+        excl += warp_sum(part);
+        if (near_inc < kLookBack) break;
+        pred -= kLookBack;
       }
       if (lane == 0) {
         st_relaxed(state + tile, kFlagInc | (unsigned int)(excl + total));
