@@ -149,10 +149,10 @@ struct NbArgs {
   int32_t scan_minb;    // launch-bound variant of the candidate scan (4, 6, 8)
   int32_t force_minb;   // launch-bound variant of force (6, 8, 10)
 };
-// Candidate scan: the per-step density + hit list, or (list_mode) the
+// Candidate scan: the per-step density + row masks, or (list_mode) the
 // Verlet list, run only when *flag is set.
 cudaError_t launch_scan_cands(int precision, bool list_mode, const NbArgs& a, cudaStream_t stream);
-// Verlet-mode density over the Verlet list; writes the step's hit list.
+// Verlet-mode density over the Verlet list; writes the step's row masks.
 cudaError_t launch_rho_list(int precision, const NbArgs& a, cudaStream_t stream);
 cudaError_t launch_force(int precision, const NbArgs& a, cudaStream_t stream);
 

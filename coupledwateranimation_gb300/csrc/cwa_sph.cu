@@ -20,7 +20,7 @@
 //    h (1 + skin) are rebuilt only when some particle has moved more than
 //    skin h / 2 since the last rebuild (integrate raises a device flag);
 //    k_rho_list walks that list each step, tests r < h and keeps the hits.
-// Either way force runs its pair terms over the step's hit list only.
+// Either way force runs its pair terms over the step's hits only.
 //
 // A row's cell-based start is start[row + max(cz - rz, 0)], decodable from
 // the particle's sorted cell key alone.  The step's hits are nine 64-bit
@@ -104,7 +104,7 @@ __device__ __forceinline__ int row_id(const SceneDev* S, CellCoord c, int r) {
   return S->coff + ((c.x + r / 3 - 1) * S->dims[1] + (c.y + r % 3 - 1)) * S->dims[2];
 }
 
-// Cell-based start of each row: the base that neighbour codes are relative
+// Cell-based start of each row: the base that row-mask bits and Verlet codes are relative
 // to.  rz z cells below the particle's cell cover every window.
 __device__ __forceinline__ void row_bases(const SceneDev* S, const int32_t* __restrict__ start, CellCoord c,
                                           int base[9]) {
@@ -228,9 +228,9 @@ constexpr int kRowCodeBits = 12;  // a hit is (row << 12) | offset from the row'
 constexpr int kRowCodeMax = 1 << kRowCodeBits;
 constexpr int kMaxSegs = 18;      // 2 columns x 9 rows
 
-// Hit lists hold codes in pairs: code k of particle i is half (k & 1) of the
-// 32-bit word (k >> 1) * n + i, so a warp writes its lanes' k-th pairs as one
-// 128-byte store and readers load two codes per load.
+// Verlet lists hold codes in pairs: code k of particle i is half (k & 1) of
+// the 32-bit word (k >> 1) * n + i, so a warp writes its lanes' k-th pairs as
+// one 128-byte store and readers load two codes per load.
 __device__ __forceinline__ uint32_t code_pair(const uint16_t* __restrict__ list, int k, int i, int n) {
   return __ldg(reinterpret_cast<const uint32_t*>(list) + (size_t)(k >> 1) * n + i);
 }
@@ -354,7 +354,7 @@ __device__ __forceinline__ T scan_row_bits(Load load, int len, T px, T py, T pz,
 }
 
 // Candidate scan.  MODE_DENSITY (per-step mode): radius h, density + this
-// step's hit list.  MODE_LIST (Verlet mode, only when the rebuild flag is
+// step's row masks.  MODE_LIST (Verlet mode, only when the rebuild flag is
 // up): radius h (1 + skin), the Verlet list and the rebuild positions.
 constexpr int MODE_DENSITY = 0;
 constexpr int MODE_LIST = 1;
@@ -604,14 +604,14 @@ struct Acc3 {
   }
 };
 
-// force: spiky pressure gradient + viscosity Laplacian over the step's hit
-// list, then the preset's extra terms.  A particle whose list overflowed
-// rescans the rows of its cell over every z cell a neighbour can occupy.
-// Force over the density pass's hit list.  Neighbour data comes from global
-// memory (L1-resident for the most part: a CTA's particles share their
-// candidate rows).  Staging the rows' records in shared memory, as the
-// candidate scan does, measured slower here: 48 KB of stage per CTA halves
-// the resident warps this latency-bound loop needs.
+// force: spiky pressure gradient + viscosity Laplacian over the step's hits
+// (the row masks), then the preset's extra terms.  A particle whose masks
+// overflowed rescans the rows of its cell over every z cell a neighbour can
+// occupy.  Neighbour data comes from global memory (L1-resident for the most
+// part: a CTA's particles share their candidate rows).  Staging the rows'
+// records in shared memory, as the candidate scan does, measured slower
+// here: 48 KB of stage per CTA halves the resident warps this latency-bound
+// loop needs.
 template <int P, int MINB>
 __global__ void __launch_bounds__(kNbThreads, MINB)
     k_force(const float4* __restrict__ pos, const float4* __restrict__ vel,
