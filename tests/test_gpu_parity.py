@@ -149,6 +149,37 @@ def test_rho_pres_force_parity(lib, orc, preset, prec, zsub, stage):
             assert e <= TOL, f"force[{c}] normwise rel err {e:.3e}"
 
 
+@pytest.mark.parametrize("prec", [PREC_FP32, PREC_COMPENSATED, PREC_FP64])
+@pytest.mark.parametrize("zsub,skin", [(1, 0.0), (2, 0.0), (1, 0.2)])
+def test_dense_rows_take_the_rescan_path(lib, orc, prec, zsub, skin):
+    """h = 4 lattice spacings: a candidate row holds ~128 particles, past the
+    64 bits of a row mask, so force rescans those particles' rows (and the
+    Verlet density its overflowed lists).  Results still match the oracle."""
+    sp = 0.02
+    sc = small_muller((14, 14, 14), sp, (32, 32), seed=21, zsub=zsub, skin=skin)
+    h = 4.0 * sp
+    sc.desc.smoothing_length = h
+    sc.desc.cell_size = h * (1.0 + skin) * (1.0 + 1e-6) if skin else h
+    sc.desc.cell_size_z = sc.desc.cell_size / zsub
+    with Sim(sc.desc, precision=prec, verlet_skin=skin) as sim:
+        load_scene(sim, 0, sc)
+        u_n, _ = sim.download_wave(0)
+        p0 = records_f32(sim.download_particles(0))
+        sim.grid()
+        sim.rho_pres()
+        got = records_f32(sim.download_particles(0))
+        ref = orc.to_f64(p0)
+        orc.rho_pres(sc.desc, ref, u_n.astype(np.float64))
+        rho_err = np.max(np.abs(got[:, 12] - ref[:, 12]) / np.abs(ref[:, 12]))
+        assert rho_err <= TOL, f"rho per-particle rel err {rho_err:.3e}"
+        sim.force()
+        got = records_f32(sim.download_particles(0))
+        orc.force(sc.desc, ref, u_n.astype(np.float64))
+        for c in range(3):
+            e = rel_inf(got[:, 8 + c], ref[:, 8 + c])
+            assert e <= TOL, f"force[{c}] normwise rel err {e:.3e}"
+
+
 # --------------------------------------------- bit-exact element-wise -------
 @pytest.mark.parametrize("preset", ["reference", "muller"])
 def test_integrate_and_deposits_bit_exact(lib, orc, preset):
