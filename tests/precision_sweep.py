@@ -13,7 +13,7 @@ lattice at s = 0.004 with a 2048^2 wave) this measures, per precision mode:
   the density histogram to the FP64 run's.
 
 The oracle is the checker only.  Usage (GPU required):
-    python tests/precision_sweep.py [--config 2] [--steps 100] [--warm 20] [--zsub 2]
+    python tests/precision_sweep.py [--config 2] [--steps 100] [--warm 20] [--zsub 4]
 Prints one JSON line per mode and a summary line.
 """
 from __future__ import annotations
@@ -45,7 +45,7 @@ def _load(sim, wl, parts=None, waves=None) -> None:
             sim.upload_wave(k, waves[k][0], waves[k][1])
 
 
-def sweep(config: int = 2, steps: int = 100, warm: int = 20, zsub: int = 2, workload=None) -> list[dict]:
+def sweep(config: int = 2, steps: int = 100, warm: int = 20, zsub: int = 4, workload=None) -> list[dict]:
     import torch
 
     from coupledwateranimation_gb300 import Sim, scenes
@@ -125,7 +125,7 @@ def main() -> None:
     ap.add_argument("--config", type=int, default=2)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warm", type=int, default=20)
-    ap.add_argument("--zsub", type=int, default=2)
+    ap.add_argument("--zsub", type=int, default=4)
     a = ap.parse_args()
     for row in sweep(a.config, a.steps, a.warm, a.zsub):
         print(json.dumps(row), flush=True)
