@@ -226,7 +226,8 @@ constexpr int kNbThreads = 128;
 constexpr int kStageCap = 1536;   // staged candidates per CTA (24 KB)
 constexpr int kRowCodeBits = 12;  // a hit is (row << 12) | offset from the row's cell-based start
 constexpr int kRowCodeMax = 1 << kRowCodeBits;
-constexpr int kMaxSegs = 18;      // 2 columns x 9 rows
+constexpr int kMaxCols = 3;       // columns a CTA's particles may span and still be staged
+constexpr int kMaxSegs = 9 * kMaxCols;  // 27 row segments: one planning warp covers them
 
 // Verlet lists hold codes in pairs: code k of particle i is half (k & 1) of
 // the 32-bit word (k >> 1) * n + i, so a warp writes its lanes' k-th pairs as
@@ -239,7 +240,7 @@ struct StagePlan {
   int32_t seg_b[kMaxSegs];        // global sorted index of each staged segment
   int32_t seg_off[kMaxSegs + 1];  // staged offset (prefix of lengths)
   int32_t col0;                   // first column (x*ny + y) of the CTA
-  int32_t ncols;                  // 1 or 2; 0 = read from global memory
+  int32_t ncols;                  // 1 .. kMaxCols; 0 = read from global memory
 };
 
 // Warp 0 plans the CTA's staging: the columns its particles occupy and, per
@@ -255,7 +256,7 @@ __device__ __forceinline__ void plan_stage(const SceneDev* S, const int32_t* __r
   const int ncols = colB - colA + 1;
   const int R = S->rz;
   int len = 0, gb = 0;
-  if (ncols <= 2 && lane < 9 * ncols) {
+  if (ncols <= kMaxCols && lane < 9 * ncols) {
     const int g = lane / 9, r = lane % 9;
     const int col = colA + g;
     const int cx = col / ny, cy = col - cx * ny;
@@ -282,7 +283,7 @@ __device__ __forceinline__ void plan_stage(const SceneDev* S, const int32_t* __r
   if (lane == 0) {
     sp.seg_off[kMaxSegs] = total;
     sp.col0 = colA;
-    sp.ncols = (ncols <= 2 && total <= kStageCap) ? ncols : 0;
+    sp.ncols = (ncols <= kMaxCols && total <= kStageCap) ? ncols : 0;
   }
 }
 
