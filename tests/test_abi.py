@@ -145,3 +145,25 @@ def test_fault_injection_hook_arguments(lib):
     f = _abi.load().cwa_debug_fail_alloc
     assert f(-2) == 1  # CWA_ERR_INVALID_ARG
     assert f(5) == 0 and f(-1) == 0
+
+
+def _build_c_host(tmp_path):
+    """Compile tests/c_host/host_cycle.c against include/cwa.h and libcwa.so."""
+    root = _abi.LIB_PATH.parent.parent
+    exe = tmp_path / "host_cycle"
+    subprocess.run(["gcc", "-std=c11", "-O2", "-Wall", "-Werror", "-I", str(root / "include"), "-o", str(exe),
+                    str(root / "tests" / "c_host" / "host_cycle.c"), "-L", str(_abi.LIB_PATH.parent), "-lcwa",
+                    f"-Wl,-rpath,{_abi.LIB_PATH.parent}", "-lm"], check=True)
+    return exe
+
+
+def test_c_host_without_a_device(lib, tmp_path):
+    """A plain C host links the library and gets CWA_ERR_NO_DEVICE (not a
+    crash) from cwa_create on a machine without a GPU."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present; tests/test_gpu_c_host.py covers this host there")
+    exe = _build_c_host(tmp_path)
+    r = subprocess.run([str(exe), "nodevice"], capture_output=True, text=True)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    assert "ok nodevice" in r.stdout
