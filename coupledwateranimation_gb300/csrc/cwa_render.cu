@@ -11,12 +11,15 @@
 //     pass 0), with the depth image of pass 2 (eye_pos.z of the nearest
 //     sprite) giving screen-space normals.
 //
-// GB300 form: a fragment-list rasteriser built from the same pieces as the
-// grid sort.  Count fragments per pixel (atomics), scan the counts, fill
-// (primitive id, window depth) records, then resolve each pixel by walking
-// its fragments in primitive order with the GL_LESS depth test and
-// SRC_ALPHA / ONE_MINUS_SRC_ALPHA blending into an 8-bit target, so the
-// result follows GL's ordered blending, not just the nearest fragment.
+// GB300 form: a tiled rasteriser.  Primitives are binned into 8 x 4 pixel
+// tiles (count, scan, fill: the grid sort's pieces); one warp then owns a
+// tile, lane = pixel.  The depth image is the nearest particle fragment, an
+// order-free minimum over the tile's list.  The colour pass sorts the tile's
+// list into draw order (in shared memory; long lists by a radix sort in
+// global scratch) and replays GL_LESS with depth writes and SRC_ALPHA /
+// ONE_MINUS_SRC_ALPHA blending into an 8-bit target per pixel, so the result
+// follows GL's ordered blending, not just the nearest fragment.  Fragments
+// that pass the depth test are queued and shaded 32 at a time.
 // Coverage, depths and projections use round-to-nearest intrinsics in a
 // fixed order (the CPU restatement repeats them bit for bit); shading uses
 // the CUDA math library.
@@ -238,20 +241,25 @@ __device__ TriSetup tri_setup(const MeshVert* mv, int t, int W, int H) {
   return s;
 }
 
-// Barycentric weights (of the CCW corners) of pixel (px, py), or false.
-__device__ __forceinline__ bool tri_cover(const TriSetup& s, int px, int py, float l[3]) {
+// Barycentric weights (of the CCW corners x, y) of pixel (px, py), or false.
+__device__ __forceinline__ bool tri_cover(const float* x, const float* y, float area, int px, int py,
+                                          float l[3]) {
   const float cx = fa((float)px, 0.5f), cy = fa((float)py, 0.5f);
-  const float e0 = edge(s.x[1], s.y[1], s.x[2], s.y[2], cx, cy);
-  const float e1 = edge(s.x[2], s.y[2], s.x[0], s.y[0], cx, cy);
-  const float e2 = edge(s.x[0], s.y[0], s.x[1], s.y[1], cx, cy);
-  const bool in0 = e0 > 0.0f || (e0 == 0.0f && top_left(s.x[1], s.y[1], s.x[2], s.y[2]));
-  const bool in1 = e1 > 0.0f || (e1 == 0.0f && top_left(s.x[2], s.y[2], s.x[0], s.y[0]));
-  const bool in2 = e2 > 0.0f || (e2 == 0.0f && top_left(s.x[0], s.y[0], s.x[1], s.y[1]));
+  const float e0 = edge(x[1], y[1], x[2], y[2], cx, cy);
+  const float e1 = edge(x[2], y[2], x[0], y[0], cx, cy);
+  const float e2 = edge(x[0], y[0], x[1], y[1], cx, cy);
+  const bool in0 = e0 > 0.0f || (e0 == 0.0f && top_left(x[1], y[1], x[2], y[2]));
+  const bool in1 = e1 > 0.0f || (e1 == 0.0f && top_left(x[2], y[2], x[0], y[0]));
+  const bool in2 = e2 > 0.0f || (e2 == 0.0f && top_left(x[0], y[0], x[1], y[1]));
   if (!(in0 && in1 && in2)) return false;
-  l[0] = fd(e0, s.area);
-  l[1] = fd(e1, s.area);
-  l[2] = fd(e2, s.area);
+  l[0] = fd(e0, area);
+  l[1] = fd(e1, area);
+  l[2] = fd(e2, area);
   return true;
+}
+
+__device__ __forceinline__ bool tri_cover(const TriSetup& s, int px, int py, float l[3]) {
+  return tri_cover(s.x, s.y, s.area, px, py, l);
 }
 
 __device__ __forceinline__ void load_tri(const RenderFrame& f, const MeshVert* verts, int t, MeshVert mv[3]) {
@@ -276,87 +284,220 @@ __global__ void k_mesh_vertices(RenderFrame f, MeshVert* __restrict__ verts) {
   verts[v] = mesh_vertex(f, v / f.res, v % f.res);
 }
 
-// Counts (fill == nullptr) or writes (prim, depth) fragment records.
-__global__ void k_raster(RenderFrame f, const MeshVert* __restrict__ verts, int32_t* __restrict__ cnt,
-                         const int32_t* __restrict__ off, uint2* __restrict__ frags) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  const int n_tri = f.draw_surface ? f.n_tris : 0;
-  const int n_par = f.draw_particles ? f.n_particles : 0;
-  if (p >= n_tri + n_par) return;
-  if (p < n_tri) {
+// ---- tiled rasteriser ---------------------------------------------------------
+// The screen is cut into 8 x 4 pixel tiles, one warp each: lane l owns pixel
+// (l & 7, l >> 3) of its tile.  Every primitive is binned into each tile its
+// pixel bounds touch; a tile's warp then tests its 32 pixels against the
+// tile's primitives.  The depth image only needs the nearest particle, so its
+// walk takes the list in any order; the colour walk sorts the list into draw
+// order first and replays the depth test and blending per pixel, as GL does.
+constexpr int kTileW = 8, kTileH = 4;
+constexpr int kTileWarps = 4;     // tiles per block
+constexpr int kTileCap = 512;     // longer tile lists are sorted in global memory
+constexpr int kHaloW = kTileW + 2, kHaloH = kTileH + 2;  // a tile's depth image with a one-pixel border
+
+enum : int { kPrimNone = 0, kPrimTri = 1, kPrimSprite = 2 };
+
+// A primitive's coverage set-up (64 bytes, staged in shared memory).
+struct __align__(16) PrimSetup {
+  float x[3], y[3];  // triangle: CCW corners; sprite: centre x[0], y[0], position x[1], x[2], y[1]
+  float area;        // triangle: twice the area; sprite: 1 / point size
+  float z[3];        // triangle: window depth of each corner; sprite: z[0] depth, z[1] clip z
+  int x0, x1, y0, y1;  // pixel bounds, inclusive, on screen
+  int type;
+  uint32_t prim;
+};
+
+// Primitive p: triangles first (p < n_tri), then the particles in upload order.
+__device__ PrimSetup prim_setup(const RenderFrame& f, const MeshVert* __restrict__ verts, uint32_t p, int n_tri) {
+  PrimSetup s;
+  s.type = kPrimNone;
+  s.prim = p;
+  if ((int)p < n_tri) {
     MeshVert mv[3];
-    load_tri(f, verts, p, mv);
-    const TriSetup s = tri_setup(mv, p, f.W, f.H);
-    if (!s.ok) return;
-    for (int py = s.y0; py <= s.y1; ++py)
-      for (int px = s.x0; px <= s.x1; ++px) {
-        float l[3];
-        if (!tri_cover(s, px, py, l)) continue;
-        const int pix = py * f.W + px;
-        const int slot = atomicAdd(cnt + pix, 1);
-        if (frags) {
-          const float z = fa(fa(fm(l[0], mv[s.order[0]].wz), fm(l[1], mv[s.order[1]].wz)),
-                             fm(l[2], mv[s.order[2]].wz));
-          frags[off[pix] + slot] = make_uint2((uint32_t)p, __float_as_uint(z));
+    load_tri(f, verts, (int)p, mv);
+    const TriSetup t = tri_setup(mv, (int)p, f.W, f.H);
+    if (!t.ok) return s;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      s.x[q] = t.x[q];
+      s.y[q] = t.y[q];
+      s.z[q] = mv[t.order[q]].wz;
+    }
+    s.area = t.area;
+    s.x0 = t.x0;
+    s.x1 = t.x1;
+    s.y0 = t.y0;
+    s.y1 = t.y1;
+    s.type = kPrimTri;
+  } else {
+    const float4 q = f.pos[p - n_tri];
+    const Win w = project(f.mvp_p, q.x, q.y, q.z, f.W, f.H, true);
+    if (!w.ok) return s;
+    const float half = 0.5f * f.point_size;
+    sprite_range(w.x, half, f.W, &s.x0, &s.x1);
+    sprite_range(w.y, half, f.H, &s.y0, &s.y1);
+    if (s.x0 > s.x1 || s.y0 > s.y1) return s;
+    s.x[0] = w.x;
+    s.y[0] = w.y;
+    s.z[0] = w.z;
+    s.z[1] = w.cz;
+    s.x[1] = q.x;  // the position, for the shading
+    s.x[2] = q.y;
+    s.y[1] = q.z;
+    s.area = fd(1.0f, f.point_size);
+    s.type = kPrimSprite;
+  }
+  return s;
+}
+
+// Window depth of s's fragment at pixel (px, py), or false where s does not
+// cover the pixel centre.
+__device__ __forceinline__ bool prim_fragment(const PrimSetup& s, int px, int py, float* z) {
+  if (px < s.x0 || px > s.x1 || py < s.y0 || py > s.y1) return false;
+  if (s.type == kPrimSprite) {
+    if (!(sprite_r2(px, py, s.x[0], s.y[0], s.area) < 0.25f)) return false;  // r >= 0.5 is discarded
+    *z = s.z[0];
+    return true;
+  }
+  float l[3];
+  if (!tri_cover(s.x, s.y, s.area, px, py, l)) return false;
+  *z = fa(fa(fm(l[0], s.z[0]), fm(l[1], s.z[1])), fm(l[2], s.z[2]));
+  return true;
+}
+
+// Counts (pairs == nullptr) or fills each tile's primitive list.
+__global__ void k_bin(RenderFrame f, const MeshVert* __restrict__ verts, int n_tri, int n_prim, int tiles_x,
+                      int32_t* __restrict__ cnt, const int32_t* __restrict__ off, uint32_t* __restrict__ pairs,
+                      int32_t* __restrict__ status) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_prim) return;
+  const PrimSetup s = prim_setup(f, verts, (uint32_t)p, n_tri);
+  if (s.type == kPrimNone) return;
+  const int tx0 = s.x0 / kTileW, tx1 = s.x1 / kTileW, ty0 = s.y0 / kTileH, ty1 = s.y1 / kTileH;
+  for (int ty = ty0; ty <= ty1; ++ty)
+    for (int tx = tx0; tx <= tx1; ++tx) {
+      const int t = ty * tiles_x + tx;
+      const int slot = atomicAdd(cnt + t, 1);
+      if (pairs) {
+        const int k = off[t] + slot;
+        if (CWA_DCHECK_FAILED(k < off[t + 1], status)) continue;
+        pairs[k] = (uint32_t)p;
+      }
+    }
+}
+
+// Ascending bitonic sort of a[0, m) by one warp (m a power of two).
+__device__ void warp_bitonic(uint32_t* a, int m, int lane) {
+  for (int k = 2; k <= m; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int c = lane; c < (m >> 1); c += 32) {
+        const int i = ((c & ~(j - 1)) << 1) | (c & (j - 1)), l = i + j;
+        const uint32_t x = a[i], y = a[l];
+        if ((x > y) == ((i & k) == 0)) {
+          a[i] = y;
+          a[l] = x;
         }
       }
-  } else {
-    const int i = p - n_tri;
-    const float4 q = f.pos[i];
-    const Win w = project(f.mvp_p, q.x, q.y, q.z, f.W, f.H, true);
-    if (!w.ok) return;
-    const float half = 0.5f * f.point_size, inv_s = fd(1.0f, f.point_size);
-    int x0, x1, y0, y1;
-    sprite_range(w.x, half, f.W, &x0, &x1);
-    sprite_range(w.y, half, f.H, &y0, &y1);
-    for (int py = y0; py <= y1; ++py)
-      for (int px = x0; px <= x1; ++px) {
-        if (!(sprite_r2(px, py, w.x, w.y, inv_s) < 0.25f)) continue;  // r >= 0.5 is discarded
-        const int pix = py * f.W + px;
-        const int slot = atomicAdd(cnt + pix, 1);
-        if (frags) frags[off[pix] + slot] = make_uint2((uint32_t)p, __float_as_uint(w.z));
-      }
-  }
+      __syncwarp();
+    }
 }
 
-// Sort each pixel's fragments into draw order; the depth image of pass 2:
-// eye_pos.z of the particle fragment that wins GL_LESS (0 where none).
-__global__ void k_resolve_depth(RenderFrame f, const int32_t* __restrict__ off, uint2* __restrict__ frags,
-                                float* __restrict__ depth_img) {
-  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= f.W * f.H) return;
-  const int b = off[pix], e = off[pix + 1];
-  for (int k = b + 1; k < e; ++k) {  // insertion sort by primitive id (ids are unique per pixel)
-    const uint2 x = frags[k];
-    int m = k - 1;
-    while (m >= b && frags[m].x > x.x) {
-      frags[m + 1] = frags[m];
-      --m;
+// Stable LSD radix sort (8-bit digits) of a[0, n) by one warp, through
+// tmp[0, n); hist holds 256 counters.  Returns the buffer holding the result.
+__device__ const uint32_t* warp_radix(uint32_t* a, uint32_t* tmp, int n, int bits, uint32_t* hist, int lane) {
+  uint32_t *src = a, *dst = tmp;
+  for (int shift = 0; shift < bits; shift += 8) {
+    for (int d = lane; d < 256; d += 32) hist[d] = 0;
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) atomicAdd(&hist[(src[i] >> shift) & 255u], 1u);
+    __syncwarp();
+    uint32_t v[8], sum = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      v[q] = hist[lane * 8 + q];
+      sum += v[q];
     }
-    frags[m + 1] = x;
-  }
-  const uint32_t first_particle = f.draw_surface ? (uint32_t)f.n_tris : 0u;
-  float best = 1.0f;
-  int win = -1;
-  for (int k = b; k < e; ++k) {
-    const uint2 x = frags[k];
-    if (x.x < first_particle) continue;
-    const float z = __uint_as_float(x.y);
-    if (z < best) {
-      best = z;
-      win = (int)(x.x - first_particle);
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
     }
+    uint32_t run = incl - sum;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      hist[lane * 8 + q] = run;
+      run += v[q];
+    }
+    __syncwarp();
+    for (int base = 0; base < n; base += 32) {
+      const int i = base + lane;
+      const bool valid = i < n;
+      uint32_t x = 0, dg = 256u + (uint32_t)lane;  // lanes past the end never match a digit
+      if (valid) {
+        x = src[i];
+        dg = (x >> shift) & 255u;
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, dg);
+      const int rank = __popc(peers & ((1u << lane) - 1u));
+      uint32_t pos = 0;
+      if (valid) pos = hist[dg] + (uint32_t)rank;
+      __syncwarp();
+      if (valid) {
+        dst[pos] = x;
+        if (rank == 0) hist[dg] += (uint32_t)__popc(peers);
+      }
+      __syncwarp();
+    }
+    uint32_t* t = src;
+    src = dst;
+    dst = t;
   }
+  return src;
+}
+
+// The depth image of pass 2: eye_pos.z (clip z) of the particle fragment
+// that wins GL_LESS, the first drawn among equal depths (0 where none).
+__global__ void __launch_bounds__(kTileWarps * 32)
+    k_tile_depth(RenderFrame f, int n_tri, int tiles_x, int n_tiles, const int32_t* __restrict__ off,
+                 const uint32_t* __restrict__ pairs, float* __restrict__ depth_img) {
+  __shared__ PrimSetup stage[kTileWarps][32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x * kTileWarps + w;
+  if (t >= n_tiles) return;
+  const int px = (t % tiles_x) * kTileW + (lane & 7), py = (t / tiles_x) * kTileH + (lane >> 3);
+  const uint64_t none = (uint64_t)__float_as_uint(1.0f) << 32;
+  uint64_t best = none;  // (depth bits, particle): window depths are in [0, 1]
+  const int b = off[t], e = off[t + 1];
+  for (int base = b; base < e; base += 32) {
+    PrimSetup s;
+    s.type = kPrimNone;
+    if (base + lane < e) {
+      const uint32_t p = pairs[base + lane];
+      if ((int)p >= n_tri) s = prim_setup(f, nullptr, p, n_tri);
+    }
+    stage[w][lane] = s;
+    __syncwarp();
+    const int m = min(32, e - base);
+    for (int j = 0; j < m; ++j) {
+      const PrimSetup q = stage[w][j];  // one 64-byte copy: the loads issue together
+      if (q.type != kPrimSprite) continue;
+      float z;
+      if (prim_fragment(q, px, py, &z)) {
+        const uint64_t key = ((uint64_t)__float_as_uint(z) << 32) | (q.prim - (uint32_t)n_tri);
+        best = key < best ? key : best;
+      }
+    }
+    __syncwarp();
+  }
+  if (px >= f.W || py >= f.H) return;
   float d = 0.0f;
-  if (win >= 0) {
-    const float4 q = f.pos[win];
+  if (best < none) {
+    const float4 q = f.pos[(uint32_t)best];
     d = project(f.mvp_p, q.x, q.y, q.z, f.W, f.H, true).cz;
   }
-  depth_img[pix] = d;
-}
-
-__device__ __forceinline__ float depth_at(const RenderFrame& f, const float* d, int x, int y) {
-  return (x < 0 || y < 0 || x >= f.W || y >= f.H) ? 0.0f : d[y * f.W + x];
+  depth_img[py * f.W + px] = d;
 }
 
 __device__ __forceinline__ float mixf(float a, float b, float t) { return a * (1.0f - t) + b * t; }
@@ -410,24 +551,23 @@ __device__ void shade_surface(const RenderFrame& f, const MeshVert* verts, int t
 }
 
 // particle_fs.glsl pass 0 for particle i at pixel (px, py).
-__device__ void shade_particle(const RenderFrame& f, const float* dimg, int i, int px, int py, V3* rgb,
-                               float* alpha) {
-  const float4 q = f.pos[i];
-  const Win w = project(f.mvp_p, q.x, q.y, q.z, f.W, f.H, true);
-  const float r = sqrtf(sprite_r2(px, py, w.x, w.y, fd(1.0f, f.point_size)));
-  const V3 pp = v3(row4(f.m_p, q.x, q.y, q.z), row4(f.m_p + 4, q.x, q.y, q.z), row4(f.m_p + 8, q.x, q.y, q.z));
+// particle_fs.glsl pass 0 splits into terms of the pixel alone, which come
+// from the depth image (the normal of GetNormalFromDepth and lighting() at
+// WorldPosFromDepth), and terms of the particle.
+//
+// The pixel's terms.  sd is the depth image around the pixel's tile (a
+// one-pixel halo, kHaloW floats a row, 0 off screen) and (hx, hy) the
+// pixel's place in it.
+__device__ void particle_pixel_terms(const RenderFrame& f, const float* sd, int hx, int hy, int px, int py,
+                                     V3* n_out, V3* lit_out) {
   const V3 eye = v3(f.eye[0], f.eye[1], f.eye[2]);
-  const float spec = powf(fmaxf(dot(normalize(pp), normalize(v3(1.0f, 1.0f, 0.0f))), 0.0f), 16.0f);
-  const float a = expf(-12.0f * r) + 0.1f * expf(-2.0f * r);
   // GetNormalFromDepth
-  const float dzdx = 0.5f * (depth_at(f, dimg, px + 1, py) - depth_at(f, dimg, px - 1, py));
-  const float dzdy = 0.5f * (depth_at(f, dimg, px, py + 1) - depth_at(f, dimg, px, py - 1));
+  const float* d = sd + hy * kHaloW + hx;
+  const float dzdx = 0.5f * (d[1] - d[-1]);
+  const float dzdy = 0.5f * (d[kHaloW] - d[-kHaloW]);
   const V3 n = normalize(v3(-dzdx, -dzdy, 1.0f));
-  const V3 iv = normalize(eye - pp);
-  const V3 refl = cube_sample(f, reflect(iv, n));
-  const V3 refr = cube_sample(f, refract(iv, n, 1.0f / 1.33f));
   // lighting() with WorldPosFromDepth (gl_FragCoord * 2 - 1, as the shader writes it)
-  const float dz = depth_at(f, dimg, px, py);
+  const float dz = d[0];
   const float cx = (px + 0.5f) * 2.0f - 1.0f, cy = (py + 0.5f) * 2.0f - 1.0f, cz = dz * 2.0f - 1.0f;
   float vw = f.inv_p[12] * cx + f.inv_p[13] * cy + f.inv_p[14] * cz + f.inv_p[15];
   V3 view = mat3x(f.inv_p, v3(cx, cy, cz), 1.0f);
@@ -439,7 +579,22 @@ __device__ void shade_particle(const RenderFrame& f, const float* dimg, int i, i
   const V3 view_dir = normalize(eye - pos);
   const V3 rdir = reflect(v3(-light_dir.x, -light_dir.y, -light_dir.z), n);
   const float spec2 = powf(fmaxf(dot(view_dir, rdir), 0.0f), 32.0f);
-  const V3 lit = (0.8f * light_col + diff * light_col + (0.9f * spec2) * light_col) * v3(0.4f, 0.7f, 1.0f);
+  *n_out = n;
+  *lit_out = (0.8f * light_col + diff * light_col + (0.9f * spec2) * light_col) * v3(0.4f, 0.7f, 1.0f);
+}
+
+// The particle's terms and the fragment's colour: q is the particle's
+// position, (wx, wy) its window position, n and lit the pixel's terms.
+__device__ void shade_particle(const RenderFrame& f, V3 n, V3 lit, float3 q, int px, int py, float wx, float wy,
+                               float inv_s, V3* rgb, float* alpha) {
+  const float r = sqrtf(sprite_r2(px, py, wx, wy, inv_s));
+  const V3 pp = v3(row4(f.m_p, q.x, q.y, q.z), row4(f.m_p + 4, q.x, q.y, q.z), row4(f.m_p + 8, q.x, q.y, q.z));
+  const V3 eye = v3(f.eye[0], f.eye[1], f.eye[2]);
+  const float spec = powf(fmaxf(dot(normalize(pp), normalize(v3(1.0f, 1.0f, 0.0f))), 0.0f), 16.0f);
+  const float a = expf(-12.0f * r) + 0.1f * expf(-2.0f * r);
+  const V3 iv = normalize(eye - pp);
+  const V3 refl = cube_sample(f, reflect(iv, n));
+  const V3 refr = cube_sample(f, refract(iv, n, 1.0f / 1.33f));
   const V3 combine = 0.75f * (refl + refr) + 0.1f * lit;
   const float t = 2.0f * pp.y;
   *rgb = v3(mixf(combine.x, 1.0f, t) + spec, mixf(combine.y, 1.0f, t) + spec, mixf(combine.z, 1.0f, t) + spec);
@@ -448,52 +603,187 @@ __device__ void shade_particle(const RenderFrame& f, const float* dimg, int i, i
 
 __device__ __forceinline__ float unorm8(float x) { return floorf(fminf(fmaxf(x, 0.0f), 1.0f) * 255.0f + 0.5f); }
 
-__global__ void k_resolve_color(RenderFrame f, const MeshVert* __restrict__ verts, const int32_t* __restrict__ off,
-                                const uint2* __restrict__ frags, const float* __restrict__ dimg,
-                                uint8_t* __restrict__ out) {
-  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= f.W * f.H) return;
-  const int px = pix % f.W, py = pix / f.W;
+// SRC_ALPHA / ONE_MINUS_SRC_ALPHA into an 8-bit target: c holds 8-bit
+// values, va = clamp(src) * clamp(alpha), oma = 1 - clamp(alpha) and
+// div255[k] = k / 255 (the division, tabulated).
+__device__ __forceinline__ float blend_channel(float c, float va, float oma, const float* div255) {
+  return unorm8(va + div255[(int)c] * oma);
+}
+
+// The colour pass: the tile's list sorted into draw order, each pixel's
+// fragments through GL_LESS (depth writes on) and SRC_ALPHA /
+// ONE_MINUS_SRC_ALPHA blending into an 8-bit target.  Fragments that pass
+// the depth test are queued per warp and shaded 32 at a time, one per lane;
+// the lanes then blend their fragments into the tile's colours (shared
+// memory) in rounds, a pixel's fragments in queue order, which is draw order.
+__global__ void __launch_bounds__(kTileWarps * 32, 6)
+    k_tile_color(RenderFrame f, const MeshVert* __restrict__ verts, int n_tri, int tiles_x, int n_tiles,
+                 const int32_t* __restrict__ off, uint32_t* __restrict__ pairs, int32_t n_pairs, int sort_bits,
+                 const float* __restrict__ dimg, uint8_t* __restrict__ out) {
+  __shared__ uint32_t s_list[kTileWarps][kTileCap];
+  __shared__ PrimSetup stage[kTileWarps][32];
+  __shared__ uint32_t q_prim[kTileWarps][64];
+  __shared__ int32_t q_lane[kTileWarps][64];
+  __shared__ uint32_t s_mask[kTileWarps][32];  // per pixel: the flush's entries for it
+  __shared__ float4 q_win[kTileWarps][64];   // sprites: window x, y and position x, y
+  __shared__ float q_pz[kTileWarps][64];      // and position z
+  __shared__ float s_depth[kTileWarps][kHaloW * kHaloH];
+  __shared__ float s_px[kTileWarps][6][32];  // each pixel's particle terms: normal, lighting
+  __shared__ float div255[256];
+  for (int k = threadIdx.x; k < 256; k += blockDim.x) div255[k] = (float)k / 255.0f;
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x * kTileWarps + w;
+  if (t >= n_tiles) return;
+  const int tx0 = (t % tiles_x) * kTileW, ty0 = (t / tiles_x) * kTileH;
+  const int px = tx0 + (lane & 7), py = ty0 + (lane >> 3);
+  const bool inside = px < f.W && py < f.H;
+  const float inv_s = fd(1.0f, f.point_size);
+  for (int k = lane; k < kHaloW * kHaloH; k += 32) {
+    const int x = tx0 - 1 + k % kHaloW, y = ty0 - 1 + k / kHaloW;
+    s_depth[w][k] = (x < 0 || y < 0 || x >= f.W || y >= f.H) ? 0.0f : dimg[y * f.W + x];
+  }
+  __syncwarp();
+  if (f.draw_particles) {
+    V3 n, lit;
+    particle_pixel_terms(f, s_depth[w], (lane & 7) + 1, (lane >> 3) + 1, px, py, &n, &lit);
+    s_px[w][0][lane] = n.x;
+    s_px[w][1][lane] = n.y;
+    s_px[w][2][lane] = n.z;
+    s_px[w][3][lane] = lit.x;
+    s_px[w][4][lane] = lit.y;
+    s_px[w][5][lane] = lit.z;
+  }
   // the colour target holds 8-bit values between blends
   float c[3] = {0.0f, 0.0f, 0.0f};
-  if (f.draw_skybox) {
-    // view ray through the pixel centre: inverse(V) * inverse(P) * ndc
-    const float nx = (px + 0.5f) / f.W * 2.0f - 1.0f, ny = (py + 0.5f) / f.H * 2.0f - 1.0f;
-    const float vw = f.inv_p[12] * nx + f.inv_p[13] * ny + f.inv_p[14] + f.inv_p[15];
-    V3 view = mat3x(f.inv_p, v3(nx, ny, 1.0f), 1.0f);
-    view = (1.0f / vw) * view;
-    const V3 dir = mat3x(f.inv_v, view, 0.0f);
-    const V3 sky = cube_sample(f, dir);
-    c[0] = unorm8(sky.x);
-    c[1] = unorm8(sky.y);
-    c[2] = unorm8(sky.z);
-  }
-  float depth = 1.0f;
-  const uint32_t first_particle = f.draw_surface ? (uint32_t)f.n_tris : 0u;
-  for (int k = off[pix]; k < off[pix + 1]; ++k) {
-    const uint2 x = frags[k];
-    const float z = __uint_as_float(x.y);
-    if (!(z < depth)) continue;  // GL_LESS, depth writes on
-    depth = z;
-    V3 rgb;
-    float a;
-    if (x.x < first_particle)
-      shade_surface(f, verts, (int)x.x, px, py, &rgb, &a);
-    else
-      shade_particle(f, dimg, (int)(x.x - first_particle), px, py, &rgb, &a);
-    a = fminf(fmaxf(a, 0.0f), 1.0f);
-    const float src[3] = {rgb.x, rgb.y, rgb.z};
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-      const float s = fminf(fmaxf(src[ch], 0.0f), 1.0f);
-      c[ch] = unorm8(s * a + (c[ch] / 255.0f) * (1.0f - a));
+  {
+    if (f.draw_skybox && inside) {
+      // view ray through the pixel centre: inverse(V) * inverse(P) * ndc
+      const float nx = (px + 0.5f) / f.W * 2.0f - 1.0f, ny = (py + 0.5f) / f.H * 2.0f - 1.0f;
+      const float vw = f.inv_p[12] * nx + f.inv_p[13] * ny + f.inv_p[14] + f.inv_p[15];
+      V3 view = mat3x(f.inv_p, v3(nx, ny, 1.0f), 1.0f);
+      view = (1.0f / vw) * view;
+      const V3 dir = mat3x(f.inv_v, view, 0.0f);
+      const V3 sky = cube_sample(f, dir);
+      c[0] = unorm8(sky.x);
+      c[1] = unorm8(sky.y);
+      c[2] = unorm8(sky.z);
     }
   }
-  uint8_t* o = out + (size_t)pix * 4;
-  o[0] = (uint8_t)c[0];
-  o[1] = (uint8_t)c[1];
-  o[2] = (uint8_t)c[2];
-  o[3] = 255;
+  const int b = off[t], n = off[t + 1] - b;
+  const uint32_t* list;
+  if (n <= kTileCap) {
+    int m = 1;
+    while (m < n) m <<= 1;
+    for (int i = lane; i < m; i += 32) s_list[w][i] = i < n ? pairs[b + i] : 0xffffffffu;
+    __syncwarp();
+    warp_bitonic(s_list[w], m, lane);
+    list = s_list[w];
+  } else {  // the second half of the pair buffer is this list's scratch
+    list = warp_radix(pairs + b, pairs + n_pairs + b, n, sort_bits, s_list[w], lane);
+  }
+  float depth = 1.0f;
+  int qn = 0;  // queued fragments (warp-uniform)
+  auto flush = [&](int cnt) {
+    __syncwarp();
+    const bool mine = lane < cnt;
+    const uint32_t p = mine ? q_prim[w][lane] : 0u;
+    const int ql = mine ? q_lane[w][lane] : 32 + lane;  // lanes without an entry match nobody
+    V3 rgb = v3(0.0f, 0.0f, 0.0f);
+    float a = 0.0f;
+    if (mine) {
+      const int qx = tx0 + (ql & 7), qy = ty0 + (ql >> 3);
+      if ((int)p < n_tri)
+        shade_surface(f, verts, (int)p, qx, qy, &rgb, &a);
+      else
+      {
+        const float4 v = q_win[w][lane];
+        const float* pt = &s_px[w][0][ql];
+        shade_particle(f, v3(pt[0], pt[32], pt[64]), v3(pt[96], pt[128], pt[160]),
+                       make_float3(v.z, v.w, q_pz[w][lane]), qx, qy, v.x, v.y, inv_s, &rgb, &a);
+      }
+    }
+    // premultiplied source terms, then each pixel's owner lane blends its
+    // entries in queue order, one per round
+    a = fminf(fmaxf(a, 0.0f), 1.0f);
+    const float va0 = fminf(fmaxf(rgb.x, 0.0f), 1.0f) * a, va1 = fminf(fmaxf(rgb.y, 0.0f), 1.0f) * a,
+                va2 = fminf(fmaxf(rgb.z, 0.0f), 1.0f) * a, oma = 1.0f - a;
+    s_mask[w][lane] = 0u;
+    __syncwarp();
+    const unsigned peers = __match_any_sync(0xffffffffu, ql);
+    if (mine && (peers & ((1u << lane) - 1u)) == 0u) s_mask[w][ql] = peers;
+    __syncwarp();
+    unsigned todo = s_mask[w][lane];
+    const int rounds = (int)__reduce_max_sync(0xffffffffu, (unsigned)__popc(todo));
+    for (int r = 0; r < rounds; ++r) {
+      const int e = todo ? __ffs((int)todo) - 1 : lane;
+      const float s0 = __shfl_sync(0xffffffffu, va0, e), s1 = __shfl_sync(0xffffffffu, va1, e),
+                  s2 = __shfl_sync(0xffffffffu, va2, e), so = __shfl_sync(0xffffffffu, oma, e);
+      if (todo) {
+        c[0] = blend_channel(c[0], s0, so, div255);
+        c[1] = blend_channel(c[1], s1, so, div255);
+        c[2] = blend_channel(c[2], s2, so, div255);
+        todo &= todo - 1u;
+      }
+    }
+    const int rest = qn - cnt;
+    uint32_t mp = 0;
+    int ml = 0;
+    float4 mv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float mz = 0.0f;
+    if (lane < rest) {
+      mp = q_prim[w][cnt + lane];
+      ml = q_lane[w][cnt + lane];
+      mv = q_win[w][cnt + lane];
+      mz = q_pz[w][cnt + lane];
+    }
+    __syncwarp();
+    if (lane < rest) {
+      q_prim[w][lane] = mp;
+      q_lane[w][lane] = ml;
+      q_win[w][lane] = mv;
+      q_pz[w][lane] = mz;
+    }
+    __syncwarp();
+    qn = rest;
+  };
+  for (int base = 0; base < n; base += 32) {
+    PrimSetup s;
+    s.type = kPrimNone;
+    if (base + lane < n) s = prim_setup(f, verts, list[base + lane], n_tri);
+    stage[w][lane] = s;
+    __syncwarp();
+    const int m = min(32, n - base);
+    for (int j = 0; j < m; ++j) {
+      const PrimSetup q = stage[w][j];  // one 64-byte copy: the loads issue together
+      if (q.type == kPrimNone) continue;
+      float z;
+      const bool pass = prim_fragment(q, px, py, &z) && z < depth;  // GL_LESS
+      if (pass) depth = z;
+      const unsigned bal = __ballot_sync(0xffffffffu, pass);
+      if (bal) {
+        if (pass) {
+          const int slot = qn + __popc(bal & ((1u << lane) - 1u));
+          q_prim[w][slot] = q.prim;
+          q_lane[w][slot] = lane;
+          q_win[w][slot] = make_float4(q.x[0], q.y[0], q.x[1], q.x[2]);  // sprites only
+          q_pz[w][slot] = q.y[1];
+        }
+        qn += __popc(bal);
+        if (qn >= 32) flush(32);
+      }
+    }
+    __syncwarp();
+  }
+  while (qn > 0) flush(min(qn, 32));
+  __syncwarp();
+  if (!inside) return;
+  uchar4 o;
+  o.x = (uint8_t)c[0];
+  o.y = (uint8_t)c[1];
+  o.z = (uint8_t)c[2];
+  o.w = 255;
+  reinterpret_cast<uchar4*>(out)[py * f.W + px] = o;
 }
 
 }  // namespace
@@ -503,13 +793,35 @@ __global__ void k_resolve_color(RenderFrame f, const MeshVert* __restrict__ vert
 struct RenderState {
   uint8_t* sky = nullptr;
   int sky_size = 0;
+  // per-frame work buffers, kept between frames and grown on demand
+  struct Buf {
+    void* p = nullptr;
+    size_t cap = 0;
+  };
+  Buf verts, upos, cnt, off, pairs, dimg, img, ws;
 };
+
+namespace {
+cudaError_t ensure(RenderState::Buf& b, size_t bytes, size_t slack_div = 0) {
+  if (b.p && bytes <= b.cap) return cudaSuccess;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+  size_t want = bytes > 16 ? bytes : 16;
+  if (slack_div) want += want / slack_div;
+  const cudaError_t e = cudaMalloc(&b.p, want);
+  if (e == cudaSuccess) b.cap = want;
+  return e;
+}
+}  // namespace
 
 RenderState* render_state_new() { return new RenderState(); }
 
 void render_state_free(RenderState* r) {
   if (!r) return;
   if (r->sky) cudaFree(r->sky);
+  for (RenderState::Buf* b : {&r->verts, &r->upos, &r->cnt, &r->off, &r->pairs, &r->dimg, &r->img, &r->ws})
+    if (b->p) cudaFree(b->p);
   delete r;
 }
 
@@ -684,73 +996,72 @@ cudaError_t render_frame(RenderState* r, const cwa_camera& cam, const cwa_render
   f.wave = wave;
   f.nx = nx;
   f.nz = nz;
-  f.pos = nullptr;
   f.sky = r->sky;
   f.sky_size = r->sky_size;
 
   const int npix = f.W * f.H;
-  const int nprim = (f.draw_surface ? f.n_tris : 0) + (f.draw_particles ? n : 0);
-  MeshVert* verts = nullptr;
-  float4* upos = nullptr;
-  int32_t *cnt = nullptr, *off = nullptr;
-  uint2* frags = nullptr;
-  float* dimg = nullptr;
-  uint8_t* img = nullptr;
-  void* ws = nullptr;
+  const int tiles_x = (f.W + kTileW - 1) / kTileW, tiles_y = (f.H + kTileH - 1) / kTileH;
+  const int n_tiles = tiles_x * tiles_y;
+  const int n_tri = f.draw_surface ? f.n_tris : 0;
+  const int nprim = n_tri + (f.draw_particles ? n : 0);
+  const size_t nverts = (size_t)f.res * f.res;
   cudaError_t e = cudaSuccess;
   auto fail = [&](cudaError_t err) {
     cudaStreamSynchronize(stream);
-    cudaFree(upos);
-    cudaFree(verts);
-    cudaFree(cnt);
-    cudaFree(off);
-    cudaFree(frags);
-    cudaFree(dimg);
-    cudaFree(img);
-    cudaFree(ws);
     return err;
   };
-  const size_t nverts = (size_t)f.res * f.res;
-  if ((e = cudaMalloc((void**)&verts, sizeof(MeshVert) * (nverts ? nverts : 1))) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc((void**)&cnt, sizeof(int32_t) * npix)) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc((void**)&off, sizeof(int32_t) * (npix + 1))) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc((void**)&dimg, sizeof(float) * npix)) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc((void**)&img, (size_t)npix * 4)) != cudaSuccess) return fail(e);
-  const size_t ws_bytes = scan_workspace_bytes(npix + 1);
-  if ((e = cudaMalloc(&ws, ws_bytes)) != cudaSuccess) return fail(e);
+  if ((e = ensure(r->verts, sizeof(MeshVert) * nverts)) != cudaSuccess) return fail(e);
+  if ((e = ensure(r->upos, sizeof(float4) * (size_t)n)) != cudaSuccess) return fail(e);
+  if ((e = ensure(r->cnt, sizeof(int32_t) * (size_t)n_tiles)) != cudaSuccess) return fail(e);
+  if ((e = ensure(r->off, sizeof(int32_t) * ((size_t)n_tiles + 1))) != cudaSuccess) return fail(e);
+  if ((e = ensure(r->dimg, sizeof(float) * (size_t)npix)) != cudaSuccess) return fail(e);
+  if ((e = ensure(r->img, (size_t)npix * 4)) != cudaSuccess) return fail(e);
+  if ((e = ensure(r->ws, scan_workspace_bytes(n_tiles + 1))) != cudaSuccess) return fail(e);
+  MeshVert* verts = static_cast<MeshVert*>(r->verts.p);
+  float4* upos = static_cast<float4*>(r->upos.p);
+  int32_t* cnt = static_cast<int32_t*>(r->cnt.p);
+  int32_t* off = static_cast<int32_t*>(r->off.p);
   ScanWorkspace sw;
-  scan_bind_workspace(ws, npix + 1, &sw);
-  if ((e = cudaMalloc((void**)&upos, sizeof(float4) * (n > 0 ? n : 1))) != cudaSuccess) return fail(e);
+  scan_bind_workspace(r->ws.p, n_tiles + 1, &sw);
   if (n > 0) {
     k_upload_order<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(sorted_pos, sorted_id, n, upos);
     *launches += 1;
   }
   f.pos = upos;
-  if ((e = cudaMemsetAsync(cnt, 0, sizeof(int32_t) * npix, stream)) != cudaSuccess) return fail(e);
+  if ((e = cudaMemsetAsync(cnt, 0, sizeof(int32_t) * n_tiles, stream)) != cudaSuccess) return fail(e);
   if (f.draw_surface && nverts) {
     k_mesh_vertices<<<(unsigned)((nverts + 255) / 256), 256, 0, stream>>>(f, verts);
     *launches += 1;
   }
   const unsigned pblocks = (unsigned)((nprim + 127) / 128);
   if (nprim > 0) {
-    k_raster<<<pblocks, 128, 0, stream>>>(f, verts, cnt, nullptr, nullptr);
+    k_bin<<<pblocks, 128, 0, stream>>>(f, verts, n_tri, nprim, tiles_x, cnt, nullptr, nullptr, status);
     *launches += 1;
   }
-  if ((e = scan_launch(cnt, off, npix, npix + 1, true, sw, status, stream, launches, nullptr)) != cudaSuccess)
+  if ((e = scan_launch(cnt, off, n_tiles, n_tiles + 1, true, sw, status, stream, launches, nullptr)) !=
+      cudaSuccess)
     return fail(e);
   int32_t total = 0;
-  if ((e = cudaMemcpyAsync(&total, off + npix, sizeof(int32_t), cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
+  if ((e = cudaMemcpyAsync(&total, off + n_tiles, sizeof(int32_t), cudaMemcpyDeviceToHost, stream)) !=
+      cudaSuccess)
     return fail(e);
   if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return fail(e);
-  if (total < 0) return fail(cudaErrorInvalidValue);  // more than 2^31 fragments
-  if ((e = cudaMalloc((void**)&frags, sizeof(uint2) * (total > 0 ? total : 1))) != cudaSuccess) return fail(e);
-  if (nprim > 0) {  // the scan cleared cnt: it now counts each pixel's filled slots
-    k_raster<<<pblocks, 128, 0, stream>>>(f, verts, cnt, off, frags);
+  if (total < 0 || total > (1 << 30)) return fail(cudaErrorInvalidValue);  // pair buffer plus its sort scratch
+  // the second half is the sort scratch of tile lists longer than kTileCap
+  if ((e = ensure(r->pairs, sizeof(uint32_t) * 2 * (size_t)total, 8)) != cudaSuccess) return fail(e);
+  uint32_t* pairs = static_cast<uint32_t*>(r->pairs.p);
+  if (nprim > 0) {  // the scan cleared cnt: it now counts each tile's filled slots
+    k_bin<<<pblocks, 128, 0, stream>>>(f, verts, n_tri, nprim, tiles_x, cnt, off, pairs, status);
     *launches += 1;
   }
-  const unsigned xblocks = (unsigned)((npix + 255) / 256);
-  k_resolve_depth<<<xblocks, 256, 0, stream>>>(f, off, frags, dimg);
-  k_resolve_color<<<xblocks, 256, 0, stream>>>(f, verts, off, frags, dimg, img);
+  const unsigned tblocks = (unsigned)((n_tiles + kTileWarps - 1) / kTileWarps);
+  int sort_bits = 0;
+  while (nprim > 1 && ((nprim - 1) >> sort_bits) != 0) ++sort_bits;
+  float* dimg = static_cast<float*>(r->dimg.p);
+  uint8_t* img = static_cast<uint8_t*>(r->img.p);
+  k_tile_depth<<<tblocks, kTileWarps * 32, 0, stream>>>(f, n_tri, tiles_x, n_tiles, off, pairs, dimg);
+  k_tile_color<<<tblocks, kTileWarps * 32, 0, stream>>>(f, verts, n_tri, tiles_x, n_tiles, off, pairs, total,
+                                                         sort_bits, dimg, img);
   *launches += 2;
   if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
   if ((e = cudaMemcpyAsync(host_out, img, (size_t)npix * 4, cudaMemcpyDeviceToHost, stream)) != cudaSuccess)

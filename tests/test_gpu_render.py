@@ -70,3 +70,30 @@ def test_render_toggles_and_errors(lib):
             sim.render(0, 64, 48, point_size=0.0)
         with pytest.raises(CwaError):
             sim.render(5, 64, 48)
+
+
+@pytest.mark.parametrize("point_size", [8.0, 40.0])
+def test_render_dense_tiles(lib, orc, point_size):
+    # 4096 particles drawn into a few pixels: the tiles under them hold more
+    # primitives than a warp sorts in shared memory, so their lists take the
+    # radix sort through global scratch; the result must not change
+    sc = small_muller((16, 16, 16), 0.03, (64, 64))
+    sky = _sky()
+    with Sim(sc.desc) as sim:
+        load_scene(sim, 0, sc)
+        sim.step(2)
+        sim.set_skybox(sky)
+        cam, prm = render_defaults(96, 64)
+        prm.surface_res = 64
+        prm.draw_skybox = 1
+        prm.particle_scale = 0.05
+        prm.wave_scale = 0.02
+        prm.point_size = point_size
+        got = sim.render(0, camera=cam, params=prm)
+        pos = records_f32(sim.download_particles(0))[:, :4]
+        u_n, _ = sim.download_wave(0)
+    want = orc.render(pos, u_n, cam, prm, sky)
+    _compare(got, want)
+    # the sprites' colour reached the image (not only sky and surface)
+    no_particles = orc.render(pos[:0], u_n, cam, prm, sky)
+    assert (np.abs(got.astype(np.int32) - no_particles.astype(np.int32)).max(axis=2) > 2).sum() >= 16
