@@ -652,6 +652,10 @@ void free_sim(cwa_sim* s) {
 
 }  // namespace
 
+namespace cwa {
+bool debug_alloc_should_fail() { return injected_alloc_failure(); }
+}  // namespace cwa
+
 extern "C" {
 
 const char* cwa_status_str(cwa_status s) {

@@ -225,6 +225,8 @@ struct RenderMatrices {  // row-major 4x4
 };
 struct RenderState;
 RenderState* render_state_new();
+// True when cwa_debug_fail_alloc's countdown says this device allocation fails.
+bool debug_alloc_should_fail();
 void render_state_free(RenderState* r);
 cudaError_t render_set_skybox(RenderState* r, const uint8_t* faces, int size, cudaStream_t stream);
 void render_matrices(const cwa_camera& cam, const cwa_render_params& prm, RenderMatrices* m);

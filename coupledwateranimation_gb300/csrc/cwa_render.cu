@@ -809,6 +809,7 @@ cudaError_t ensure(RenderState::Buf& b, size_t bytes, size_t slack_div = 0) {
   b.cap = 0;
   size_t want = bytes > 16 ? bytes : 16;
   if (slack_div) want += want / slack_div;
+  if (debug_alloc_should_fail()) return cudaErrorMemoryAllocation;
   const cudaError_t e = cudaMalloc(&b.p, want);
   if (e == cudaSuccess) b.cap = want;
   return e;
@@ -832,6 +833,7 @@ cudaError_t render_set_skybox(RenderState* r, const uint8_t* faces, int size, cu
     r->sky_size = 0;
   }
   const size_t bytes = (size_t)6 * size * size * 4;
+  if (debug_alloc_should_fail()) return cudaErrorMemoryAllocation;
   cudaError_t e = cudaMalloc((void**)&r->sky, bytes);
   if (e != cudaSuccess) return e;
   e = cudaMemcpyAsync(r->sky, faces, bytes, cudaMemcpyHostToDevice, stream);

@@ -288,7 +288,8 @@ cwa_status cwa_get_pass_times(cwa_sim* sim, float* ms, int32_t n);
  * allocation of a cwa_sim from now on (counting from 0, process-wide) fails
  * with CWA_ERR_OOM, as if the device were out of memory; -1 turns it off.
  * Lets tests drive every allocation-failure path of cwa_create and of the
- * lazy allocations without exhausting a shared GPU. */
+ * lazy allocations (wave advance scratch, the renderer's work buffers and
+ * cube map) without exhausting a shared GPU. */
 cwa_status cwa_debug_fail_alloc(int32_t n);
 /* Number of kernels launched by the library on this sim since creation. */
 cwa_status cwa_get_launch_count(cwa_sim* sim, int64_t* launches);

@@ -74,3 +74,40 @@ def test_lazy_wave_allocation_failure_keeps_the_sim(hook):
             s.synchronize()
         wa, wb = a.download_wave(0), b.download_wave(0)
         assert np.array_equal(bits(wa[0]), bits(wb[0])) and np.array_equal(bits(wa[1]), bits(wb[1]))
+
+
+def test_render_allocation_failures_and_steady_frames(hook):
+    # every work-buffer allocation of a first frame (and of the cube map)
+    # fails cleanly; a later frame rebuilds what is missing; a frame of an
+    # already-seen size allocates nothing
+    from coupledwateranimation_gb300.sim import render_defaults
+
+    sc = small_muller((8, 8, 8), 0.03, (64, 64), seed=4)
+    sky = np.full((6, 8, 8, 4), 90, np.uint8)
+    with Sim(sc.desc) as ref:
+        load_scene(ref, 0, sc)
+        ref.set_skybox(sky)
+        cam, prm = render_defaults(80, 60)
+        prm.surface_res = 32
+        prm.draw_skybox = 1
+        want = ref.render(0, camera=cam, params=prm)
+    n_fail = 0
+    for n in range(12):
+        with Sim(sc.desc) as sim:
+            load_scene(sim, 0, sc)
+            assert hook(n) == 0
+            try:
+                sim.set_skybox(sky)
+                got = sim.render(0, camera=cam, params=prm)
+            except CwaError as e:
+                assert e.status == OOM
+                n_fail += 1
+                assert hook(-1) == 0
+                sim.set_skybox(sky)
+                got = sim.render(0, camera=cam, params=prm)
+            assert hook(-1) == 0
+            assert np.array_equal(got, want)
+            assert hook(0) == 0  # the next allocation would fail: the same frame needs none
+            assert np.array_equal(sim.render(0, camera=cam, params=prm), want)
+            assert hook(-1) == 0
+    assert n_fail >= 8
