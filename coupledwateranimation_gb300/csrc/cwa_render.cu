@@ -405,7 +405,8 @@ __device__ void warp_bitonic(uint32_t* a, int m, int lane) {
 
 // Stable LSD radix sort (8-bit digits) of a[0, n) by one warp, through
 // tmp[0, n); hist holds 256 counters.  Returns the buffer holding the result.
-__device__ const uint32_t* warp_radix(uint32_t* a, uint32_t* tmp, int n, int bits, uint32_t* hist, int lane) {
+__device__ const uint32_t* warp_radix(uint32_t* a, uint32_t* tmp, int n, int bits, uint32_t* hist, int lane,
+                                      int32_t* status) {
   uint32_t *src = a, *dst = tmp;
   for (int shift = 0; shift < bits; shift += 8) {
     for (int d = lane; d < 256; d += 32) hist[d] = 0;
@@ -445,7 +446,7 @@ __device__ const uint32_t* warp_radix(uint32_t* a, uint32_t* tmp, int n, int bit
       if (valid) pos = hist[dg] + (uint32_t)rank;
       __syncwarp();
       if (valid) {
-        dst[pos] = x;
+        if (!CWA_DCHECK_FAILED(pos < (uint32_t)n, status)) dst[pos] = x;
         if (rank == 0) hist[dg] += (uint32_t)__popc(peers);
       }
       __syncwarp();
@@ -461,7 +462,7 @@ __device__ const uint32_t* warp_radix(uint32_t* a, uint32_t* tmp, int n, int bit
 // that wins GL_LESS, the first drawn among equal depths (0 where none).
 __global__ void __launch_bounds__(kTileWarps * 32)
     k_tile_depth(RenderFrame f, int n_tri, int tiles_x, int n_tiles, const int32_t* __restrict__ off,
-                 const uint32_t* __restrict__ pairs, float* __restrict__ depth_img) {
+                 const uint32_t* __restrict__ pairs, float* __restrict__ depth_img, int32_t* __restrict__ status) {
   __shared__ PrimSetup stage[kTileWarps][32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int t = blockIdx.x * kTileWarps + w;
@@ -493,7 +494,7 @@ __global__ void __launch_bounds__(kTileWarps * 32)
   }
   if (px >= f.W || py >= f.H) return;
   float d = 0.0f;
-  if (best < none) {
+  if (best < none && !CWA_DCHECK_FAILED((uint32_t)best < (uint32_t)f.n_particles, status)) {
     const float4 q = f.pos[(uint32_t)best];
     d = project(f.mvp_p, q.x, q.y, q.z, f.W, f.H, true).cz;
   }
@@ -619,7 +620,7 @@ __device__ __forceinline__ float blend_channel(float c, float va, float oma, con
 __global__ void __launch_bounds__(kTileWarps * 32, 6)
     k_tile_color(RenderFrame f, const MeshVert* __restrict__ verts, int n_tri, int tiles_x, int n_tiles,
                  const int32_t* __restrict__ off, uint32_t* __restrict__ pairs, int32_t n_pairs, int sort_bits,
-                 const float* __restrict__ dimg, uint8_t* __restrict__ out) {
+                 const float* __restrict__ dimg, uint8_t* __restrict__ out, int32_t* __restrict__ status) {
   __shared__ uint32_t s_list[kTileWarps][kTileCap];
   __shared__ PrimSetup stage[kTileWarps][32];
   __shared__ uint32_t q_prim[kTileWarps][64];
@@ -680,7 +681,7 @@ __global__ void __launch_bounds__(kTileWarps * 32, 6)
     warp_bitonic(s_list[w], m, lane);
     list = s_list[w];
   } else {  // the second half of the pair buffer is this list's scratch
-    list = warp_radix(pairs + b, pairs + n_pairs + b, n, sort_bits, s_list[w], lane);
+    list = warp_radix(pairs + b, pairs + n_pairs + b, n, sort_bits, s_list[w], lane, status);
   }
   float depth = 1.0f;
   int qn = 0;  // queued fragments (warp-uniform)
@@ -750,7 +751,11 @@ __global__ void __launch_bounds__(kTileWarps * 32, 6)
   for (int base = 0; base < n; base += 32) {
     PrimSetup s;
     s.type = kPrimNone;
-    if (base + lane < n) s = prim_setup(f, verts, list[base + lane], n_tri);
+    if (base + lane < n) {
+      const uint32_t p = list[base + lane];
+      const uint32_t n_prim = (uint32_t)n_tri + (f.draw_particles ? (uint32_t)f.n_particles : 0u);
+      if (!CWA_DCHECK_FAILED(p < n_prim, status)) s = prim_setup(f, verts, p, n_tri);
+    }
     stage[w][lane] = s;
     __syncwarp();
     const int m = min(32, n - base);
@@ -1061,9 +1066,9 @@ cudaError_t render_frame(RenderState* r, const cwa_camera& cam, const cwa_render
   while (nprim > 1 && ((nprim - 1) >> sort_bits) != 0) ++sort_bits;
   float* dimg = static_cast<float*>(r->dimg.p);
   uint8_t* img = static_cast<uint8_t*>(r->img.p);
-  k_tile_depth<<<tblocks, kTileWarps * 32, 0, stream>>>(f, n_tri, tiles_x, n_tiles, off, pairs, dimg);
+  k_tile_depth<<<tblocks, kTileWarps * 32, 0, stream>>>(f, n_tri, tiles_x, n_tiles, off, pairs, dimg, status);
   k_tile_color<<<tblocks, kTileWarps * 32, 0, stream>>>(f, verts, n_tri, tiles_x, n_tiles, off, pairs, total,
-                                                         sort_bits, dimg, img);
+                                                         sort_bits, dimg, img, status);
   *launches += 2;
   if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
   if ((e = cudaMemcpyAsync(host_out, img, (size_t)npix * 4, cudaMemcpyDeviceToHost, stream)) != cudaSuccess)

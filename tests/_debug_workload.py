@@ -1,7 +1,8 @@
 """A mixed workload run by test_gpu_debug_checks.py under both the release
 and the index-checked library (chosen by CWA_LIBRARY in the environment):
 per-step and Verlet modes, both presets, a batch of scenes with ragged
-sizes, every wave-advance variant, the three precisions and a PBD frame.
+sizes, every wave-advance variant, the three precisions, a PBD frame and
+two rendered frames (tile lists sorted in shared and in global memory).
 Prints one digest of every result; a failed device index check surfaces as
 CwaError (CWA_ERR_BOUNDS) from a synchronising call and a non-zero exit."""
 from __future__ import annotations
@@ -53,6 +54,21 @@ def main() -> None:
             sim.wave_advance(16)
             sim.synchronize()
             feed(sim.download_wave(0)[0])
+    # headless frames: tiles sorted in shared memory, then a block drawn a
+    # few pixels wide, whose tile lists take the radix sort in global scratch
+    from coupledwateranimation_gb300.sim import render_defaults
+    img = small_muller((16, 16, 16), 0.03, (64, 64), seed=6)
+    with Sim(img.desc) as sim:
+        load_scene(sim, 0, img)
+        sim.step(2)
+        sim.set_skybox(np.full((6, 8, 8, 4), 120, np.uint8))
+        for scale in (1.5, 0.05):
+            cam, prm = render_defaults(130, 97)
+            prm.surface_res = 48
+            prm.draw_skybox = 1
+            prm.particle_scale = scale
+            prm.wave_scale = 0.02
+            feed(sim.render(0, camera=cam, params=prm))
     p = pbd_defaults()
     p.n_boxes = 512
     with PbdSim(p) as sim:

@@ -97,3 +97,25 @@ def test_render_dense_tiles(lib, orc, point_size):
     # the sprites' colour reached the image (not only sky and surface)
     no_particles = orc.render(pos[:0], u_n, cam, prm, sky)
     assert (np.abs(got.astype(np.int32) - no_particles.astype(np.int32)).max(axis=2) > 2).sum() >= 16
+
+
+@pytest.mark.parametrize("size", [(1, 1), (7, 3), (130, 97), (257, 9)])
+def test_render_ragged_image_sizes(lib, orc, size):
+    # image edges that cut through 8 x 4 tiles, and images smaller than one tile
+    sc = small_reference(2048)
+    sky = _sky()
+    w, h = size
+    with Sim(sc.desc) as sim:
+        load_scene(sim, 0, sc)
+        sim.step(3)
+        sim.set_skybox(sky)
+        cam, prm = render_defaults(w, h)
+        prm.surface_res = 64
+        prm.draw_skybox = 1
+        prm.point_size = 3.0 if max(w, h) < 16 else 8.0
+        got = sim.render(0, camera=cam, params=prm)
+        pos = records_f32(sim.download_particles(0))[:, :4]
+        u_n, _ = sim.download_wave(0)
+    want = orc.render(pos, u_n, cam, prm, sky)
+    assert got.shape == (h, w, 4)
+    _compare(got, want)
