@@ -401,7 +401,9 @@ cwa_status cwa_render_set_skybox(cwa_sim* sim, const uint8_t* faces_rgba, int32_
  * reference reads last frame's); the skybox, drawn at depth 1.0 and
  * rejected by the default GL_LESS test against the cleared depth, appears
  * only with draw_skybox = 1; triangles with a vertex outside the near/far
- * planes or behind the eye are dropped instead of clipped.  Synchronous. */
+ * planes or behind the eye are dropped instead of clipped.  Synchronous.
+ * The frame's device work buffers stay with the sim and only grow, so
+ * frames of a size already rendered allocate no device memory. */
 cwa_status cwa_render(cwa_sim* sim, int32_t scene, const cwa_camera* camera, const cwa_render_params* params,
                       uint8_t* out_rgba);
 
