@@ -753,8 +753,8 @@ __global__ void __launch_bounds__(kTileWarps * 32, 6)
     s.type = kPrimNone;
     if (base + lane < n) {
       const uint32_t p = list[base + lane];
-      const uint32_t n_prim = (uint32_t)n_tri + (f.draw_particles ? (uint32_t)f.n_particles : 0u);
-      if (!CWA_DCHECK_FAILED(p < n_prim, status)) s = prim_setup(f, verts, p, n_tri);
+      if (!CWA_DCHECK_FAILED(p < (uint32_t)n_tri + (f.draw_particles ? (uint32_t)f.n_particles : 0u), status))
+        s = prim_setup(f, verts, p, n_tri);
     }
     stage[w][lane] = s;
     __syncwarp();
