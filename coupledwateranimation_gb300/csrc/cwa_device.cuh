@@ -19,6 +19,18 @@ __device__ __forceinline__ int cell_axis(float p, float lo, float cell, int n) {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// Programmatic dependent launch across a step's kernel chain.  Every kernel
+// of the chain first waits for the kernel before it to complete (a no-op
+// when it was launched without the chaining attribute), then lets the next
+// kernel be launched, whose blocks take the SMs this grid's last wave frees
+// and wait there: launch latency and ramp-up overlap this grid's tail.  The
+// wait covers every earlier kernel, since each one waited for its own
+// predecessor before it could complete.
+__device__ __forceinline__ void chain_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Index checks of the debug build (compiled with CWA_DEBUG_CHECKS): a failed
 // check records kStatusBounds in the status word and evaluates to true, so
 // the caller skips the access; release builds compile every check to false.

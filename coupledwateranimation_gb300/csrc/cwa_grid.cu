@@ -51,6 +51,7 @@ template <bool kZero, bool kVec>
 __global__ void __launch_bounds__(kScanBlock)
     k_scan(int32_t* in, int32_t* out, int32_t n_in, int32_t n_out, unsigned int* counter,
            unsigned long long* state, int32_t* status, const int32_t* flag) {
+  chain_enter();
   __shared__ int s_tile, s_prefix;
   if (flag && __ldg(flag) == 0) return;  // grid kept this step (Verlet mode)
   __shared__ int s_warp[kScanBlock / 32];
@@ -199,6 +200,7 @@ __global__ void __launch_bounds__(256)
                  const SceneDev* __restrict__ scenes, int32_t* __restrict__ key,
                  int32_t* __restrict__ slot, int32_t* __restrict__ count, int32_t* status,
                  const int32_t* flag) {
+  chain_enter();
   if (flag && __ldg(flag) == 0) return;
   const Tile t = tiles[blockIdx.x];
   const SceneDev* S = scenes + t.scene;
@@ -232,6 +234,7 @@ __global__ void k_point_hash(const float4* __restrict__ pos, int32_t n, float lx
 __global__ void k_list_insert(const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
                               const int32_t* __restrict__ start, int32_t* __restrict__ list, int32_t n,
                               const int32_t* flag, int32_t* status) {
+  chain_enter();
   if (flag && __ldg(flag) == 0) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -260,6 +263,7 @@ __global__ void __launch_bounds__(256)
                    float4* __restrict__ pout, float4* __restrict__ vout, float4* __restrict__ fout,
                    int32_t* __restrict__ idout, int32_t* __restrict__ kout, int32_t n, int32_t* status,
                    const int32_t* flag) {
+  chain_enter();
   if (flag && __ldg(flag) == 0) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -279,6 +283,7 @@ __global__ void __launch_bounds__(256)
                 const int32_t* __restrict__ id2, float4* __restrict__ p, float4* __restrict__ v,
                 float4* __restrict__ f, int32_t* __restrict__ id, int32_t n, const int32_t* flag,
                 unsigned long long* rebuilds) {
+  chain_enter();
   if (__ldg(flag) == 0) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rebuilds, 1ull);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -346,14 +351,16 @@ cudaError_t launch_hash_count(const float4* pos, const Tile* tiles, int32_t n_ti
                               const SceneDev* scenes, int32_t* key, int32_t* slot, int32_t* count,
                               int32_t* status, const int32_t* flag, cudaStream_t stream) {
   if (n_tiles <= 0) return cudaSuccess;
-  k_hash_count<<<n_tiles, tile_size, 0, stream>>>(pos, tiles, scenes, key, slot, count, status, flag);
+  launch_chained(k_hash_count, dim3(n_tiles), dim3(tile_size), 0, stream, pos, tiles, scenes, key, slot, count,
+                 status, flag);
   return cudaGetLastError();
 }
 
 cudaError_t launch_list_insert(const int32_t* key, const int32_t* slot, const int32_t* start, int32_t* list,
                                int32_t n, const int32_t* flag, cudaStream_t stream, int32_t* status) {
   if (n <= 0) return cudaSuccess;
-  k_list_insert<<<blocks_for(n, 256), 256, 0, stream>>>(key, slot, start, list, n, flag, status);
+  launch_chained(k_list_insert, dim3(blocks_for(n, 256)), dim3(256), 0, stream, key, slot, start, list, n, flag,
+                 status);
   return cudaGetLastError();
 }
 
@@ -363,8 +370,8 @@ cudaError_t launch_rank_reorder(const int32_t* key, const int32_t* slot, const i
                                 float4* fout, int32_t* idout, int32_t* kout, int32_t n, int32_t* status,
                                 const int32_t* flag, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  k_rank_reorder<<<blocks_for(n, 256), 256, 0, stream>>>(key, slot, start, list, pin, vin, fin, idin, pout,
-                                                         vout, fout, idout, kout, n, status, flag);
+  launch_chained(k_rank_reorder, dim3(blocks_for(n, 256)), dim3(256), 0, stream, key, slot, start, list, pin,
+                 vin, fin, idin, pout, vout, fout, idout, kout, n, status, flag);
   return cudaGetLastError();
 }
 
@@ -372,8 +379,8 @@ cudaError_t launch_copy_back(const float4* p2, const float4* v2, const float4* f
                              float4* p, float4* v, float4* f, int32_t* id, int32_t n, const int32_t* flag,
                              unsigned long long* rebuilds, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  k_copy_back<<<min(blocks_for(n, 256), 1216), 256, 0, stream>>>(p2, v2, f2, id2, p, v, f, id, n, flag,
-                                                                 rebuilds);
+  launch_chained(k_copy_back, dim3(min(blocks_for(n, 256), 1216)), dim3(256), 0, stream, p2, v2, f2, id2, p, v,
+                 f, id, n, flag, rebuilds);
   return cudaGetLastError();
 }
 

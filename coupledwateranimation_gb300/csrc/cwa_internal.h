@@ -13,6 +13,26 @@
 
 namespace cwa {
 
+// Launches `kernel` as a link of the step's chain (programmatic stream
+// serialization): it may start while the previous kernel drains, and waits
+// for it in chain_enter().  Only kernels that call chain_enter() first are
+// launched this way.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                           Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // Device status bits (atomicOr'ed by kernels, read by cwa_synchronize).
 enum : int32_t {
   kStatusNonFinite = 1,  // a NaN/Inf position reached the cell hash

@@ -31,6 +31,7 @@ __global__ void __launch_bounds__(128)
                 unsigned long long* __restrict__ deposits, const float4* __restrict__ xref, int32_t* flag,
                 int32_t* __restrict__ key, int32_t* __restrict__ slot, int32_t* __restrict__ count,
                 int32_t* status) {
+  chain_enter();
   const Tile tl = tiles[blockIdx.x];
   const int i = tl.begin + threadIdx.x;
   if (i >= tl.end) return;
@@ -167,6 +168,7 @@ __global__ void __launch_bounds__(256)
     k_wave(const float* __restrict__ un, const float* __restrict__ unm1, float* __restrict__ uout,
            unsigned long long* __restrict__ deposits, const Tile* __restrict__ tiles,
            const SceneDev* __restrict__ scenes, int32_t* status) {
+  chain_enter();
   const Tile tl = tiles[blockIdx.x];
   const SceneDev* S = scenes + tl.scene;
   const int W = S->nx, H = S->nz, woff = S->woff;
@@ -371,8 +373,8 @@ cudaError_t launch_wave(const float* u_n, const float* u_nm1, float* u_out, unsi
                         const Tile* wtiles, int32_t n_wtiles, int32_t wtile_size, const SceneDev* scenes,
                         cudaStream_t stream, int32_t* status) {
   if (n_wtiles <= 0) return cudaSuccess;
-  k_wave<<<n_wtiles, wtile_size / kWaveCellsPerThread, 0, stream>>>(u_n, u_nm1, u_out, deposits, wtiles, scenes,
-                                                                    status);
+  launch_chained(k_wave, dim3(n_wtiles), dim3(wtile_size / kWaveCellsPerThread), 0, stream, u_n, u_nm1, u_out,
+                 deposits, wtiles, scenes, status);
   return cudaGetLastError();
 }
 
