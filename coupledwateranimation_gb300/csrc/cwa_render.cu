@@ -604,19 +604,21 @@ __device__ void shade_particle(const RenderFrame& f, V3 n, V3 lit, float3 q, int
 
 __device__ __forceinline__ float unorm8(float x) { return floorf(fminf(fmaxf(x, 0.0f), 1.0f) * 255.0f + 0.5f); }
 
-// SRC_ALPHA / ONE_MINUS_SRC_ALPHA into an 8-bit target: c holds 8-bit
-// values, va = clamp(src) * clamp(alpha), oma = 1 - clamp(alpha) and
-// div255[k] = k / 255 (the division, tabulated).
-__device__ __forceinline__ float blend_channel(float c, float va, float oma, const float* div255) {
-  return unorm8(va + div255[(int)c] * oma);
+// SRC_ALPHA / ONE_MINUS_SRC_ALPHA into an 8-bit target: c is the 8-bit
+// value, va = clamp(src) * clamp(alpha), oma = 1 - clamp(alpha) and
+// div255[k] = k / 255 (the division, tabulated).  Every term is
+// non-negative, so unorm8's lower clamp never acts and is left out; the
+// floor and the conversion are one rounding-down conversion.
+__device__ __forceinline__ int blend_channel(int c, float va, float oma, const float* div255) {
+  return __float2int_rd(fminf(va + div255[c] * oma, 1.0f) * 255.0f + 0.5f);
 }
 
 // The colour pass: the tile's list sorted into draw order, each pixel's
 // fragments through GL_LESS (depth writes on) and SRC_ALPHA /
 // ONE_MINUS_SRC_ALPHA blending into an 8-bit target.  Fragments that pass
-// the depth test are queued per warp and shaded 32 at a time, one per lane;
-// the lanes then blend their fragments into the tile's colours (shared
-// memory) in rounds, a pixel's fragments in queue order, which is draw order.
+// the depth test are queued per warp (a 64-entry ring) and shaded 32 at a
+// time, one per lane; each pixel's owner lane then blends that pixel's
+// fragments into its colour in rounds, in queue order, which is draw order.
 __global__ void __launch_bounds__(kTileWarps * 32, 6)
     k_tile_color(RenderFrame f, const MeshVert* __restrict__ verts, int n_tri, int tiles_x, int n_tiles,
                  const int32_t* __restrict__ off, uint32_t* __restrict__ pairs, int32_t n_pairs, int sort_bits,
@@ -656,7 +658,7 @@ __global__ void __launch_bounds__(kTileWarps * 32, 6)
     s_px[w][5][lane] = lit.z;
   }
   // the colour target holds 8-bit values between blends
-  float c[3] = {0.0f, 0.0f, 0.0f};
+  int c[3] = {0, 0, 0};
   {
     if (f.draw_skybox && inside) {
       // view ray through the pixel centre: inverse(V) * inverse(P) * ndc
@@ -666,9 +668,9 @@ __global__ void __launch_bounds__(kTileWarps * 32, 6)
       view = (1.0f / vw) * view;
       const V3 dir = mat3x(f.inv_v, view, 0.0f);
       const V3 sky = cube_sample(f, dir);
-      c[0] = unorm8(sky.x);
-      c[1] = unorm8(sky.y);
-      c[2] = unorm8(sky.z);
+      c[0] = (int)unorm8(sky.x);
+      c[1] = (int)unorm8(sky.y);
+      c[2] = (int)unorm8(sky.z);
     }
   }
   const int b = off[t], n = off[t + 1] - b;
@@ -684,12 +686,13 @@ __global__ void __launch_bounds__(kTileWarps * 32, 6)
     list = warp_radix(pairs + b, pairs + n_pairs + b, n, sort_bits, s_list[w], lane, status);
   }
   float depth = 1.0f;
-  int qn = 0;  // queued fragments (warp-uniform)
+  int qh = 0, qn = 0;  // the queue's head and length (warp-uniform)
   auto flush = [&](int cnt) {
     __syncwarp();
     const bool mine = lane < cnt;
-    const uint32_t p = mine ? q_prim[w][lane] : 0u;
-    const int ql = mine ? q_lane[w][lane] : 32 + lane;  // lanes without an entry match nobody
+    const int qe = (qh + lane) & 63;
+    const uint32_t p = mine ? q_prim[w][qe] : 0u;
+    const int ql = mine ? q_lane[w][qe] : 32 + lane;  // lanes without an entry match nobody
     V3 rgb = v3(0.0f, 0.0f, 0.0f);
     float a = 0.0f;
     if (mine) {
@@ -698,10 +701,10 @@ __global__ void __launch_bounds__(kTileWarps * 32, 6)
         shade_surface(f, verts, (int)p, qx, qy, &rgb, &a);
       else
       {
-        const float4 v = q_win[w][lane];
+        const float4 v = q_win[w][qe];
         const float* pt = &s_px[w][0][ql];
         shade_particle(f, v3(pt[0], pt[32], pt[64]), v3(pt[96], pt[128], pt[160]),
-                       make_float3(v.z, v.w, q_pz[w][lane]), qx, qy, v.x, v.y, inv_s, &rgb, &a);
+                       make_float3(v.z, v.w, q_pz[w][qe]), qx, qy, v.x, v.y, inv_s, &rgb, &a);
       }
     }
     // premultiplied source terms, then each pixel's owner lane blends its
@@ -727,26 +730,9 @@ __global__ void __launch_bounds__(kTileWarps * 32, 6)
         todo &= todo - 1u;
       }
     }
-    const int rest = qn - cnt;
-    uint32_t mp = 0;
-    int ml = 0;
-    float4 mv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    float mz = 0.0f;
-    if (lane < rest) {
-      mp = q_prim[w][cnt + lane];
-      ml = q_lane[w][cnt + lane];
-      mv = q_win[w][cnt + lane];
-      mz = q_pz[w][cnt + lane];
-    }
-    __syncwarp();
-    if (lane < rest) {
-      q_prim[w][lane] = mp;
-      q_lane[w][lane] = ml;
-      q_win[w][lane] = mv;
-      q_pz[w][lane] = mz;
-    }
-    __syncwarp();
-    qn = rest;
+    __syncwarp();  // the ring's slots are free for new entries
+    qh = (qh + cnt) & 63;
+    qn -= cnt;
   };
   for (int base = 0; base < n; base += 32) {
     PrimSetup s;
@@ -768,7 +754,7 @@ __global__ void __launch_bounds__(kTileWarps * 32, 6)
       const unsigned bal = __ballot_sync(0xffffffffu, pass);
       if (bal) {
         if (pass) {
-          const int slot = qn + __popc(bal & ((1u << lane) - 1u));
+          const int slot = (qh + qn + __popc(bal & ((1u << lane) - 1u))) & 63;
           q_prim[w][slot] = q.prim;
           q_lane[w][slot] = lane;
           q_win[w][slot] = make_float4(q.x[0], q.y[0], q.x[1], q.x[2]);  // sprites only
