@@ -619,7 +619,7 @@ __device__ __forceinline__ int blend_channel(int c, float va, float oma, const f
 // the depth test are queued per warp (a 64-entry ring) and shaded 32 at a
 // time, one per lane; each pixel's owner lane then blends that pixel's
 // fragments into its colour in rounds, in queue order, which is draw order.
-__global__ void __launch_bounds__(kTileWarps * 32, 6)
+__global__ void __launch_bounds__(kTileWarps * 32, 7)
     k_tile_color(RenderFrame f, const MeshVert* __restrict__ verts, int n_tri, int tiles_x, int n_tiles,
                  const int32_t* __restrict__ off, uint32_t* __restrict__ pairs, int32_t n_pairs, int sort_bits,
                  const float* __restrict__ dimg, uint8_t* __restrict__ out, int32_t* __restrict__ status) {
