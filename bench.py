@@ -516,11 +516,26 @@ def run_batched(args) -> None:
         dist.destroy_process_group()
 
 
+def _synthetic_cube_map(size: int, seed: int = 12345) -> np.ndarray:
+    """Six size x size RGBA8 faces: a seeded base colour per face plus
+    smooth ramps along both texel axes."""
+    rng = np.random.default_rng(seed)
+    base = rng.integers(40, 200, (6, 1, 1, 3))
+    ramp = np.linspace(0, 40, size)[None, :, None, None] + np.linspace(0, 25, size)[None, None, :, None]
+    faces = np.empty((6, size, size, 4), np.uint8)
+    faces[..., :3] = np.clip(base + ramp, 0, 255).astype(np.uint8)
+    faces[..., 3] = 255
+    return faces
+
+
 def run_render(args) -> None:
     """`--mode render`: one headless frame (cwa_render, the reference's
     display()) of the workload's first scene after --warmup steps, at
     --width x --height with the reference's startup view; host wall-clock of
-    the synchronous call (best of --steps).  --png writes the last frame."""
+    the synchronous call (best of --steps).  --png writes the last frame.
+    --skybox N sets a synthetic N x N cube map (smooth colour ramps, seeded)
+    and draws it, so every fragment samples the cube map twice, as the
+    reference's shaders do with its LoadCubemap textures."""
     from coupledwateranimation_gb300 import Sim, images, scenes
     from coupledwateranimation_gb300.sim import render_defaults
     wl = scenes.with_zsub(scenes.CONFIGS[args.config](), args.zsub)
@@ -530,6 +545,9 @@ def run_render(args) -> None:
         sim.upload_wave(0, sc.wave, sc.wave)
         sim.step(args.warmup)
         cam, prm = render_defaults(args.width, args.height)
+        if args.skybox > 0:
+            sim.set_skybox(_synthetic_cube_map(args.skybox))
+            prm.draw_skybox = 1
         img = sim.render(0, camera=cam, params=prm)  # warm-up
         best = None
         for _ in range(max(1, args.steps)):
@@ -542,6 +560,7 @@ def run_render(args) -> None:
             f.write(images.encode_png(images.gl_rows(img)))
     print(json.dumps({"mode": "render", "workload": wl.name, "particles": sc.desc.n_particles,
                       "image": f"{args.width}x{args.height}", "surface_res": prm.surface_res,
+                      "skybox": args.skybox,
                       "ms_per_frame": best * 1e3, "frames_per_s": 1.0 / best,
                       "lit_pixels": int((img[..., :3] != 0).any(axis=2).sum())}), flush=True)
 
@@ -693,6 +712,8 @@ def main() -> None:
     ap.add_argument("--width", type=int, default=1920, help="image width for --mode render")
     ap.add_argument("--height", type=int, default=1080, help="image height for --mode render")
     ap.add_argument("--png", default="", help="--mode render: write the frame to this PNG")
+    ap.add_argument("--skybox", type=int, default=0,
+                    help="--mode render: draw a synthetic cube map with faces of this many texels a side")
     ap.add_argument("--wave-n", type=int, default=4096, help="field edge for --mode wave")
     ap.add_argument("--wave-kind", default="shallow", choices=["shallow", "wave1d"],
                     help="--mode sph2d: the 1D field the SPH samples")

@@ -139,9 +139,10 @@ struct RenderFrame {
 namespace {
 
 // ---- cube map (GL cube-map face selection, GL_LINEAR, clamp within face) --
+// One 4-byte load per RGBA8 texel (the cube map's base is cudaMalloc-aligned).
 __device__ V3 cube_texel(const RenderFrame& f, int face, int x, int y) {
-  const uint8_t* p = f.sky + (((size_t)face * f.sky_size + y) * f.sky_size + x) * 4;
-  return v3(p[0] / 255.0f, p[1] / 255.0f, p[2] / 255.0f);
+  const uchar4 p = __ldg(reinterpret_cast<const uchar4*>(f.sky) + (((size_t)face * f.sky_size + y) * f.sky_size + x));
+  return v3(p.x / 255.0f, p.y / 255.0f, p.z / 255.0f);
 }
 
 __device__ V3 cube_sample(const RenderFrame& f, V3 r) {
