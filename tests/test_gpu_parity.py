@@ -293,7 +293,7 @@ def test_full_step_matches_oracle_one_step(lib, orc, zsub):
 
 
 def test_multistep_invariants(lib, orc):
-    """Chaotic SPH: judged by exact mass, energy drift and density histograms."""
+    """Chaotic SPH: checked through exact mass, energy drift and density histograms."""
     sc = small_muller((16, 16, 16), 0.02, (64, 64))
     steps = 60
     with Sim(sc.desc) as sim:
