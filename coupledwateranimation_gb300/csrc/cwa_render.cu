@@ -461,35 +461,45 @@ __device__ const uint32_t* warp_radix(uint32_t* a, uint32_t* tmp, int n, int bit
 
 // The depth image of pass 2: eye_pos.z (clip z) of the particle fragment
 // that wins GL_LESS, the first drawn among equal depths (0 where none).
+// A sprite's set-up as the depth walk needs it (32 bytes): window position
+// and depth, particle index, pixel bounds (empty for anything else).
+struct __align__(16) SpriteStage {
+  float wx, wy, z;
+  uint32_t i;
+  int x0, x1, y0, y1;
+};
+
 __global__ void __launch_bounds__(kTileWarps * 32)
     k_tile_depth(RenderFrame f, int n_tri, int tiles_x, int n_tiles, const int32_t* __restrict__ off,
                  const uint32_t* __restrict__ pairs, float* __restrict__ depth_img, int32_t* __restrict__ status) {
-  __shared__ PrimSetup stage[kTileWarps][32];
+  __shared__ SpriteStage stage[kTileWarps][32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int t = blockIdx.x * kTileWarps + w;
   if (t >= n_tiles) return;
   const int px = (t % tiles_x) * kTileW + (lane & 7), py = (t / tiles_x) * kTileH + (lane >> 3);
+  const float inv_s = fd(1.0f, f.point_size);
   const uint64_t none = (uint64_t)__float_as_uint(1.0f) << 32;
   uint64_t best = none;  // (depth bits, particle): window depths are in [0, 1]
   const int b = off[t], e = off[t + 1];
   for (int base = b; base < e; base += 32) {
-    PrimSetup s;
-    s.type = kPrimNone;
+    SpriteStage g = {0.0f, 0.0f, 0.0f, 0u, 1, 0, 1, 0};  // empty bounds: covers nothing
     if (base + lane < e) {
       const uint32_t p = pairs[base + lane];
-      if ((int)p >= n_tri) s = prim_setup(f, nullptr, p, n_tri);
+      if ((int)p >= n_tri) {
+        const PrimSetup s = prim_setup(f, nullptr, p, n_tri);
+        if (s.type == kPrimSprite)
+          g = SpriteStage{s.x[0], s.y[0], s.z[0], p - (uint32_t)n_tri, s.x0, s.x1, s.y0, s.y1};
+      }
     }
-    stage[w][lane] = s;
+    stage[w][lane] = g;
     __syncwarp();
     const int m = min(32, e - base);
     for (int j = 0; j < m; ++j) {
-      const PrimSetup q = stage[w][j];  // one 64-byte copy: the loads issue together
-      if (q.type != kPrimSprite) continue;
-      float z;
-      if (prim_fragment(q, px, py, &z)) {
-        const uint64_t key = ((uint64_t)__float_as_uint(z) << 32) | (q.prim - (uint32_t)n_tri);
-        best = key < best ? key : best;
-      }
+      const SpriteStage q = stage[w][j];  // two 16-byte loads
+      if (px < q.x0 || px > q.x1 || py < q.y0 || py > q.y1) continue;
+      if (!(sprite_r2(px, py, q.wx, q.wy, inv_s) < 0.25f)) continue;  // r >= 0.5 is discarded
+      const uint64_t key = ((uint64_t)__float_as_uint(q.z) << 32) | q.i;
+      best = key < best ? key : best;
     }
     __syncwarp();
   }
