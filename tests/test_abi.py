@@ -167,3 +167,24 @@ def test_c_host_without_a_device(lib, tmp_path):
     r = subprocess.run([str(exe), "nodevice"], capture_output=True, text=True)
     assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
     assert "ok nodevice" in r.stdout
+
+
+def test_readme_c_example_builds_and_stops_without_a_device(lib, tmp_path):
+    """The C example on the README's front page compiles against
+    include/cwa.h, links libcwa.so, and on a machine without a GPU reports
+    cwa_create's error and stops instead of using the sim."""
+    import re
+    import torch
+    root = _abi.LIB_PATH.parent.parent
+    readme = (root / "README.md").read_text()
+    body = re.search(r"```c\n(.*?)```", readme, re.S).group(1).replace('#include "cwa.h"\n', "")
+    src = tmp_path / "readme_example.c"
+    src.write_text('#include <stdio.h>\n#include <stdlib.h>\n#include "cwa.h"\n'
+                   "int main(void) {\n" + body + "free(p);\nreturn 0;\n}\n")
+    exe = tmp_path / "readme_example"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", str(root / "include"), "-o", str(exe), str(src),
+                    "-L", str(_abi.LIB_PATH.parent), "-lcwa", f"-Wl,-rpath,{_abi.LIB_PATH.parent}"], check=True)
+    if torch.cuda.is_available():
+        return  # running it would step the reference scene on the GPU; building it is the check here
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 1 and "cwa_create:" in r.stderr, (r.returncode, r.stdout, r.stderr)
