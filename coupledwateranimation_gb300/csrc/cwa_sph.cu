@@ -4,7 +4,7 @@
 //             density / pressure terms — CoupledWaterAnimation/rho_pres_comp.glsl:49-81.
 //   force:    spiky pressure gradient + viscosity Laplacian, then either the
 //             reference's crest / torque / drag / wave-normal terms
-//             (force_comp.glsl:160-237) or gravity only (MULLER).
+//             (force_comp.glsl:62-139) or gravity only (MULLER).
 //
 // The reference loops over all N particles per particle (O(N^2)).  Here the
 // particles are sorted by uniform-grid cell (x/y cell edge >= the search
@@ -734,7 +734,7 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   const float rho = rpi.x;
   float4 out;
   if (S->preset == CWA_PRESET_REFERENCE_3D) {
-    // force_comp.glsl:188-212
+    // force_comp.glsl:90-114
     float4 fprev = force[i];
     float vs = S->visc;
     if (pi.y > S->crest) {

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// One cell of EvolveWave (wave_comp.glsl:348-383) with get_clamp borders,
+// One cell of EvolveWave (wave_comp.glsl:171-206) with get_clamp borders,
 // plus the particle deposit d: one rounding per operation, in the order the
 // float32 restatement uses.
 __device__ __forceinline__ float evolve_cell(const SceneDev* S, float c0, float c1, float nn, float ss, float ee,
@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// InitWave (wave_comp.glsl:259-317): peak * smoothstep(5, 0, d) around two
+// InitWave (wave_comp.glsl:82-140): peak * smoothstep(5, 0, d) around two
 // (splash) or three (wave, wake) centres.
 __global__ void k_wave_init(float* __restrict__ u, int32_t nx, int32_t nz, float mode) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -378,7 +378,7 @@ cudaError_t launch_wave(const float* u_n, const float* u_nm1, float* u_out, unsi
   return cudaGetLastError();
 }
 
-// InitFromImage (wave_comp.glsl:73-77): cell (x, y) takes the red channel of
+// InitFromImage (wave_comp.glsl:76-80): cell (x, y) takes the red channel of
 // texel (2x, y) of an RGBA8 texture as a normalised float, c / 255.  The
 // shader's texelFetch past the image is undefined; here it reads 0.
 __global__ void k_wave_from_image(float* __restrict__ u, int32_t nx, int32_t nz,

@@ -2,7 +2,7 @@
 //
 // Advances the height fields K leapfrog steps per launch with no new
 // particle deposits: the stand-alone wave module's job (the reference's
-// StencilImage2DTripleBuffered driving wave_comp.glsl EvolveWave, :348-383,
+// StencilImage2DTripleBuffered driving wave_comp.glsl EvolveWave, :171-206,
 // one dispatch per step; the 2D wave demo Wave2DSimp/Wave2D_cs.glsl:78-84).
 //
 // One launch covers all scenes through a list of block tiles.  A block tile

@@ -45,8 +45,8 @@ typedef enum cwa_status {
 
 /* Physics presets.
  * REFERENCE_3D: the shaders' own constants and rules
- *   (rho_pres_comp.glsl:49-81, force_comp.glsl:160-237,
- *    integrate_comp.glsl:56-178, wave_comp.glsl:348-383).
+ *   (rho_pres_comp.glsl:49-81, force_comp.glsl:62-139,
+ *    integrate_comp.glsl:56-178, wave_comp.glsl:171-206).
  * MULLER: the 3D Mueller-2003 SPH of the benchmark configurations (poly6
  *   density, spiky pressure gradient -45/(pi h^6), viscosity Laplacian,
  *   p = k(rho - rho0), reflective walls) with two-way particle<->heightfield
@@ -226,10 +226,10 @@ cwa_status cwa_upload_wave(cwa_sim* sim, int32_t scene, const float* u_n, const 
 cwa_status cwa_download_wave(cwa_sim* sim, int32_t scene, float* u_n, float* u_nm1, int32_t nx,
                              int32_t nz);
 /* StencilImage2DTripleBuffered::Reinit (StencilImage2DTripleBuffered.cpp:42-59):
- * wave_comp.glsl InitWave (MODE_INIT, :259-317) into both history buffers. */
+ * wave_comp.glsl InitWave (MODE_INIT, :82-140) into both history buffers. */
 cwa_status cwa_wave_reinit(cwa_sim* sim, int32_t scene);
 /* StencilImage2DTripleBuffered::ReinitFromTexture (StencilImage2DTripleBuffered.cpp:61-77):
- * wave_comp.glsl InitFromImage (MODE_INIT_FROM_TEXTURE, :73-77) writes
+ * wave_comp.glsl InitFromImage (MODE_INIT_FROM_TEXTURE, :76-80) writes
  * u(x, y) = red(2x, y) / 255 of an RGBA8 texture, then the buffers rotate,
  * so u^n is the image field and u^(n-1) the old u^n.  `rgba` is host memory,
  * width x height texels of 4 bytes, row 0 = texture row 0 (the bottom row of
@@ -251,7 +251,7 @@ cwa_status cwa_pass_wave(cwa_sim* sim);
 /* n_steps wave passes over every scene's height field, with no particle
  * passes in between: the wave module stepped alone (Module::Compute in
  * StencilImage2DTripleBuffered.cpp:22-31 and wave_comp.glsl EvolveWave
- * :348-383, one dispatch per step).  Bit-identical to n_steps calls of
+ * :171-206, one dispatch per step).  Bit-identical to n_steps calls of
  * cwa_pass_wave; deposits pending from an integrate pass land in the first
  * step.  Steps run K at a time in shared memory (TMA-loaded tiles; K from
  * the sim's wave_block option), so device pointers of the wave buffers may

@@ -488,7 +488,7 @@ void orc_rho_pres(const cwa_scene_desc* sc, int32_t n, double* p16, const double
 }
 
 // ------------------------------------------------------------ force ----
-// force_comp.glsl:160-237 (REFERENCE_3D: spiky constant -20/(pi h^6), crest,
+// force_comp.glsl:62-139 (REFERENCE_3D: spiky constant -20/(pi h^6), crest,
 // torque, drag, wave normal) / Mueller: -45/(pi h^6), viscosity, gravity.
 void orc_force(const cwa_scene_desc* sc, int32_t n, double* p16, const double* u_n,
                int32_t brute) {
@@ -540,10 +540,10 @@ void orc_force(const cwa_scene_desc* sc, int32_t n, double* p16, const double* u
       double torque[3] = {0.25 * (a[1] * fprev[2] - a[2] * fprev[1]),
                           0.25 * (a[2] * fprev[0] - a[0] * fprev[2]),
                           0.25 * (a[0] * fprev[1] - a[1] * fprev[0])};
-      // WaveVelocity (force_comp.glsl:215-226): step 0.01 in uv, shader dt.
+      // WaveVelocity (force_comp.glsl:117-128): step 0.01 in uv, shader dt.
       double hx = sample64(u_n, W, Hh, s + 0.01, t), hy = sample64(u_n, W, Hh, s, t + 0.01);
       double wv[3] = {(hx - H) / sc->dt, (hy - H) / sc->dt, (hx - hy) / 0.01};
-      // WaveNormal (force_comp.glsl:229-237): cross((0,1,hT-h),(1,0,hR-h)).
+      // WaveNormal (force_comp.glsl:130-139): cross((0,1,hT-h),(1,0,hR-h)).
       double hR = sample64(u_n, W, Hh, s + 1.0, t) - H;
       double hT = sample64(u_n, W, Hh, s, t + 1.0) - H;
       double nrm[3] = {hR, hT, -1.0};
@@ -648,7 +648,7 @@ void orc_integrate(const cwa_scene_desc* sc, int32_t n, double* p16, const doubl
 }
 
 // ------------------------------------------------------------- wave ----
-// wave_comp.glsl:348-383: EvolveWave with get_clamp (clamped 5-point
+// wave_comp.glsl:171-206: EvolveWave with get_clamp (clamped 5-point
 // neighbourhood) and the line source of modes 0 < w < 1; plus the particle
 // deposits of the MULLER coupling.
 void orc_wave(const cwa_scene_desc* sc, const double* u_n, const double* u_nm1, double* u_out,
@@ -799,7 +799,7 @@ void orc_integrate_f32(const cwa_scene_desc* sc, int32_t n, float* p16f, const f
   }
 }
 
-// EvolveWave in float32 (wave_comp.glsl:348-364) with the deposit source:
+// EvolveWave in float32 (wave_comp.glsl:171-187) with the deposit source:
 // w = atten*((a*c0 + lam*((n+s)+(e+w))) - b*c1); line source; + gain*dep.
 void orc_wave_f32(const cwa_scene_desc* sc, const float* u_n, const float* u_nm1, float* u_out,
                   const int64_t* deposits) {
@@ -830,7 +830,7 @@ void orc_wave_f32(const cwa_scene_desc* sc, const float* u_n, const float* u_nm1
     }
 }
 
-// InitFromImage (wave_comp.glsl:73-77): texelFetch(uInitImage, coord * (2, 1)).r
+// InitFromImage (wave_comp.glsl:76-80): texelFetch(uInitImage, coord * (2, 1)).r
 // of an RGBA8 texture is c / 255 in float; past the image, 0.
 void orc_wave_from_image_f32(int32_t nx, int32_t nz, const uint8_t* rgba, int32_t w, int32_t h, float* u) {
   for (int32_t y = 0; y < nz; ++y)
@@ -840,7 +840,7 @@ void orc_wave_from_image_f32(int32_t nx, int32_t nz, const uint8_t* rgba, int32_
     }
 }
 
-// InitWave (wave_comp.glsl:259-317) in float32.
+// InitWave (wave_comp.glsl:82-140) in float32.
 void orc_wave_init_f32(const cwa_scene_desc* sc, float* u) {
   const int W = sc->wave_nx, H = sc->wave_nz;
   const float mode = sc->wave_mode;

@@ -86,7 +86,7 @@ void orc_integrate_f32(const cwa_scene_desc* sc, int32_t n, float* p16f, const f
 void orc_wave_f32(const cwa_scene_desc* sc, const float* u_n, const float* u_nm1, float* u_out,
                   const int64_t* deposits);
 void orc_wave_init_f32(const cwa_scene_desc* sc, float* u);
-/* InitFromImage (wave_comp.glsl:73-77): u(x, y) = red(2x, y) / 255 of an
+/* InitFromImage (wave_comp.glsl:76-80): u(x, y) = red(2x, y) / 255 of an
  * RGBA8 image, 0 past the image. */
 void orc_wave_from_image_f32(int32_t nx, int32_t nz, const uint8_t* rgba, int32_t w, int32_t h, float* u);
 float orc_sample_f32(const float* u, int32_t w, int32_t h, float s, float t);

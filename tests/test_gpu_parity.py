@@ -260,7 +260,7 @@ def test_wave_1000_steps_l2(lib, orc):
 
 
 def test_reference_line_source_mode(lib, orc):
-    # mode in (0, 1) switches on the line source of EvolveWave (wave_comp.glsl:354-361)
+    # mode in (0, 1) switches on the line source of EvolveWave (wave_comp.glsl:177-184)
     sc = small_reference(640)
     sc.desc.wave_mode = 0.5
     with Sim(sc.desc) as sim:

@@ -3,7 +3,7 @@ in 128 x H boxes, TMA-loaded tiles; every (H, K) variant) against single wave
 passes and the float32 oracle, bit for bit, and the wave tuner.  The wave
 module stepped alone is StencilImage2DTripleBuffered::Compute
 (StencilImage2DTripleBuffered.cpp:22-31) over wave_comp.glsl EvolveWave
-(:348-383)."""
+(:171-206)."""
 from __future__ import annotations
 
 import numpy as np
@@ -111,7 +111,7 @@ def test_wave_tuner_keeps_state_and_picks_fastest(lib, pending):
 
 def test_wave_advance_reference_line_source(lib):
     sc = small_reference(640)
-    sc.desc.wave_mode = 0.5  # line source on (wave_comp.glsl:354-361)
+    sc.desc.wave_mode = 0.5  # line source on (wave_comp.glsl:177-184)
     sc.desc.wave_nx, sc.desc.wave_nz = 200, 120
 
     def load(s):

@@ -1,5 +1,5 @@
 """cwa_wave_init_from_image (StencilImage2DTripleBuffered::ReinitFromTexture,
-StencilImage2DTripleBuffered.cpp:61-77; wave_comp.glsl InitFromImage :73-77)
+StencilImage2DTripleBuffered.cpp:61-77; wave_comp.glsl InitFromImage :76-80)
 on the reference's three init textures: bit-exact against the oracle, the
 old u^n moved to u^(n-1), other scenes of the sim untouched."""
 from __future__ import annotations

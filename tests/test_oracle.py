@@ -94,7 +94,7 @@ def _small_muller(orc, lattice=(8, 8, 8), spacing=0.05, wave=(32, 32), seed=7):
 
 
 def test_brute_force_equals_grid_neighbours(orc):
-    # The shaders loop over all N (rho_pres_comp.glsl:60-68, force_comp.glsl:172-186);
+    # The shaders loop over all N (rho_pres_comp.glsl:60-68, force_comp.glsl:74-88);
     # the grid loop must see the same neighbour set.
     for preset in (0, 1):
         if preset == 0:
