@@ -2,27 +2,30 @@
 
 Metric: particle + wave-cell updates per second (one update = one particle
 or one wave cell advanced one step).  Workload: the 1,048,576-particle
-dam-break (128x64x128 lattice, s = 0.0075, h = 2s, 67^3 grid cells) coupled to a
-1024^2 height field, float32 with compensated neighbour sums, synthetic
-seeded inputs.  Each timed step is one full cwa_step (grid sort -> rho_pres
--> force -> integrate + coupling -> wave) with the state resident in HBM;
-L2 is flushed (256 MiB write on the sim's stream) before every step, outside
-the per-step CUDA events.  The timed steps are steps warmup + 2 ..
-warmup + steps + 1 of the run: a checkpoint taken after the warm-up is
-reloaded once the clock sampler is logging, and the per-pass profile
-restarts from it, so both cover the same simulated steps.
+dam-break (128x64x128 lattice, s = 0.0075, h = 2s) coupled to a 1024^2
+height field over its stated 500 steps, float32 with cascaded two-sum
+neighbour sums, synthetic seeded inputs.  Each timed step is one full
+cwa_step (grid sort -> rho_pres -> force -> integrate + coupling -> wave)
+with the state resident in HBM; L2 is flushed (256 MiB write on the sim's
+stream) before every timed step, outside its CUDA events.  After --warmup
+untimed steps the run continues to the workload's last step, and exactly
+--steps of those steps, evenly spaced from warmup + 1 to the last, are
+timed, so the figure covers the early dam-break, the collapse and the late
+sloshing state alike (config.timed_steps lists them).
 
-`e2e` runs the same steps through the public C ABI with host buffers: each
+`e2e` runs the same step through the public C ABI with host buffers: each
 step uploads the particle records and both wave fields from pinned host
 memory, steps, and downloads the particle records and u^n.
 
-N > 1 (torchrun): every rank runs an independent replica (the single-scene
-step does not shard); value = all ranks' updates / the slowest rank's time.
+`--gpus N` without torchrun re-launches itself under torch.distributed.run
+with N ranks; every rank runs an independent replica (the single-scene step
+does not shard) and value = all ranks' updates / the slowest rank's time.
 
 `--impl reference` times the reference algorithm on the host cores instead:
 the reference's GLSL cannot run here (no graphics stack), so its CPU
-restatement (oracle/, FP64, OpenMP over all host threads) runs on the same
-workload, a bounded number of steps.
+restatement (oracle/, FP64, OpenMP over all host threads), with inputs from
+the oracle's own generators, runs --warmup untimed and exactly --steps timed
+steps of the same workload.
 """
 from __future__ import annotations
 
@@ -86,6 +89,12 @@ def _fp32_gemm_tflops(dev) -> float | None:
     finally:
         torch.backends.cuda.matmul.allow_tf32 = prev
 BYTES_PER_WAVE_CELL = {"wave": 20}
+WORKLOAD_NAMES = {0: "c0: 32^3 particles s=0.02, 256^2 wave",
+                  1: "c1: 1,048,576 particles (128x64x128, s=0.0075), 1024^2 wave",
+                  2: "c2: 256x128x128 particles s=0.004, 2048^2 wave",
+                  3: "c3: 256 batched small scenes", 4: "c4: 64 batched large scenes"}
+WORKLOAD_STEPS = {0: 200, 1: 500, 2: 100, 3: 200, 4: 100}
+PRECISION_NAMES = ["fp32", "fp32 with cascaded two-sum neighbour sums", "fp64"]
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -177,76 +186,155 @@ def _dist():
     return ws, rank, local
 
 
+def _free_port() -> int:
+    import socket
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+def _launch_ranks(n: int) -> int:
+    """Re-runs this command under torch.distributed.run with n ranks on this
+    node (rendezvous on 127.0.0.1); returns the launcher's exit code."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), str(Path(__file__).resolve())]
+    return subprocess.call(cmd + sys.argv[1:])
+
+
 # The CPU legs time the oracle on its own fastest sort grid (z cells of h/2;
 # measured per step on 8 cores: 0.47 / 0.45 / 0.57 s for z cells of h, h/2,
 # h/4), which need not be the GPU's.
 CPU_ZSUB = 2
 
 
-def _cpu_leg(workload, max_seconds: float, min_steps: int = 1):
-    """Time the oracle (FP64 CPU restatement) on the workload's first scene."""
+def _oracle_workload(config: int):
+    """The workload built by the oracle's own generators (no library code)."""
+    from oracle import workloads
+    return workloads.with_zsub(workloads.CONFIGS[config](), CPU_ZSUB)
+
+
+def _cpu_steps(wl, warmup: int, steps: int | None, max_seconds: float, timed: list[int] | None = None):
+    """Times the oracle (FP64 CPU restatement) on the workload's first scene
+    from its initial state.  timed: the step numbers (1-based) to time, the
+    others run untimed up to the last of them.  Otherwise `warmup` untimed
+    steps, then exactly `steps` timed steps, or (steps None) as many as fit
+    in about max_seconds.  Returns (updates/s, timed steps, seconds, threads)."""
     from oracle import oracle as orc
-    sc = workload.scenes[0]
+    orc.set_threads(os.cpu_count() or 1)  # every host thread (torchrun sets OMP_NUM_THREADS=1 per rank)
+    sc = wl.scenes[0]
     d = sc.desc
-    p16 = orc.to_f64(sc.particles.view(np.float32).reshape(-1, 16))
+    p16 = orc.to_f64(sc.particles)
     un = sc.wave.astype(np.float64)
     unm1 = un.copy()
-    orc.step(d, p16, un, unm1, 1)  # warm-up (page-in, thread pool)
-    steps, t0 = 0, time.perf_counter()
-    while steps < min_steps or (time.perf_counter() - t0) < max_seconds * 0.5:
-        orc.step(d, p16, un, unm1, 1)
-        steps += 1
-        if time.perf_counter() - t0 > max_seconds:
-            break
-    dt = time.perf_counter() - t0
-    units = (d.n_particles + d.wave_nx * d.wave_nz) * steps
-    return units / dt, steps, dt, orc.threads()
+    if timed is not None:
+        want, n, dt = set(timed), 0, 0.0
+        for k in range(1, max(timed) + 1):
+            if k in want:
+                t0 = time.perf_counter()
+                orc.step(d, p16, un, unm1, 1)
+                dt += time.perf_counter() - t0
+                n += 1
+            else:
+                orc.step(d, p16, un, unm1, 1)
+    else:
+        orc.step(d, p16, un, unm1, max(1, warmup))  # untimed (page-in, thread pool)
+        n, t0 = 0, time.perf_counter()
+        while True:
+            orc.step(d, p16, un, unm1, 1)
+            n += 1
+            if steps is not None:
+                if n >= steps:
+                    break
+            elif time.perf_counter() - t0 > max_seconds * 0.5:
+                break
+        dt = time.perf_counter() - t0
+    units = (d.n_particles + d.wave_nx * d.wave_nz) * n
+    return units / dt, n, dt, orc.threads()
+
+
+def _config(args, n_particles: int, n_wave: int, grid_cells: int, timed: list[int], ws: int) -> dict:
+    """The bench line's `config`: the same dict on both arms."""
+    return {"workload": WORKLOAD_NAMES.get(args.config, str(args.config)), "particles": n_particles,
+            "wave_cells": n_wave, "grid_cells": grid_cells, "workload_steps": WORKLOAD_STEPS[args.config],
+            "precision": PRECISION_NAMES[args.precision], "grid_cell": f"h x h x h/{args.zsub}",
+            "l2": "flushed before every timed step (256 MiB write, outside the step events)",
+            "timed_steps": timed, "parallelism": f"replicas x{ws}"}
+
+
+def _timed_steps(warmup: int, k: int, last: int) -> list[int]:
+    """k step numbers evenly spaced over warmup + 1 .. last (1-based)."""
+    first = warmup + 1
+    last = max(last, first + k - 1)
+    if k == 1:
+        return [last]
+    return sorted({first + round(i * (last - first) / (k - 1)) for i in range(k)})
 
 
 def run_reference(args) -> None:
+    """The reference arm: the same workload, the same warm-up and the same
+    timed step numbers as the GPU arm, on the FP64 CPU restatement."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
-    from coupledwateranimation_gb300 import scenes
-    wl = scenes.with_zsub(scenes.CONFIGS[args.config](), CPU_ZSUB)
-    budget = float(os.environ.get("CWA_REF_SECONDS", "120"))
-    value, steps, secs, cores = _cpu_leg(wl, budget, min_steps=1)
+    wl = _oracle_workload(args.config)
+    timed = _timed_steps(args.warmup, args.steps, max(wl.steps, args.warmup + args.steps))
+    value, steps, secs, cores = _cpu_steps(wl, args.warmup, None, 0.0, timed=timed)
     d = wl.scenes[0].desc
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / steps * 1e3,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": secs / steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded dam-break + Gaussian bumps)",
-        "config": {"workload": wl.name, "particles": d.n_particles, "wave": f"{d.wave_nx}x{d.wave_nz}"},
+        "config": _config(args, wl.n_particles, wl.n_wave_cells, orc_grid_cells(d, args.zsub), timed, ws),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{steps} full steps of the workload ({secs:.1f} s; sort grid z cells "
-                                   f"of h/{CPU_ZSUB}, the oracle's fastest) on the FP64 OpenMP "
-                                   f"restatement of the reference shaders; the GLSL itself cannot run "
-                                   f"(no graphics stack)"},
+                         "sample": f"the {steps} timed steps of the workload's run (the GPU arm's step numbers; "
+                                   f"{secs:.1f} s timed; sort grid z cells of h/{CPU_ZSUB}, the oracle's "
+                                   f"fastest) on the FP64 OpenMP restatement of the reference shaders, inputs "
+                                   f"from the oracle's own generators; the GLSL itself cannot run (no graphics "
+                                   f"stack)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0, config: int = 3) -> dict:
+def orc_grid_cells(desc, zsub: int) -> int:
+    """Cells of the scene's sort grid with z cells of h / zsub (oracle's count)."""
+    from oracle import oracle as orc
+    d = type(desc).from_buffer_copy(desc)
+    d.cell_size_z = d.cell_size / zsub
+    return int(np.prod(orc.grid_dims(d)))
+
+
+def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0, config: int = 3,
+                     steps: int | None = None) -> dict:
     """A batched workload (256 small scenes, or 64 large ones) stepped as one
     batched sim (one launch per pass over all scenes, CUDA graph) and as
-    single-scene sims run one at a time (each its own graph).  Host
-    wall-clock around the GPU work, with a synchronise at the end of every
-    scene's steps in the plain leg.  Under N ranks each rank steps its shard
-    of the scenes (greedy by device footprint); times are the max over
+    single-scene sims run one at a time (each its own graph), both over the
+    workload's stated step count unless `steps` is given.  Device time: CUDA
+    events on each sim's stream around its steps (summed over the plain
+    sims), after 3 untimed steps each.  Under N ranks each rank steps its
+    shard of the scenes (greedy by device footprint); times are the max over
     ranks, units the sum."""
     from coupledwateranimation_gb300 import Sim, scenes, shard
     full = scenes.with_zsub(scenes.CONFIGS[config](), args.zsub)
     _, mine = shard.shard_scenes(full, rank, ws)
     wl = scenes.Workload(full.name, mine, full.steps)
-    steps = max(3, min(args.steps, 10))
+    steps = steps or full.steps
     dev = f"cuda:{local}"
     n_units = shard.sum_over_ranks(wl.n_particles + wl.n_wave_cells, dev)
     alg_bytes = shard.sum_over_ranks(sum(
         sum(BYTES_PER_PARTICLE.values()) * s.desc.n_particles
         + sum(BYTES_PER_GRID_CELL.values()) * shard.grid_cells(s.desc)
         + sum(BYTES_PER_WAVE_CELL.values()) * s.desc.wave_nx * s.desc.wave_nz for s in wl.scenes), dev)
+
+    def timed(sim, n):
+        stream = torch.cuda.ExternalStream(sim.device_view(0).stream, device=torch.device("cuda", local))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.step(n)
+        e1.record(stream)
+        return e0, e1
+
     with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local) as sim:
         for k, s in enumerate(wl.scenes):
             sim.upload_particles(k, s.particles)
@@ -255,12 +343,12 @@ def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0, co
             sim.autotune(trial_steps=2)
         sim.step(3)
         sim.synchronize()
-        t0 = time.perf_counter()
-        sim.step(steps)
+        w0 = time.perf_counter()
+        e0, e1 = timed(sim, steps)
         sim.synchronize()
-        t_batched = shard.max_over_ranks(time.perf_counter() - t0, dev)
-        launches = sim.launch_count
-    plain = []
+        wall_b = time.perf_counter() - w0
+        t_batched = shard.max_over_ranks(e0.elapsed_time(e1) * 1e-3, dev)
+    plain, evs = [], []
     try:
         for s in wl.scenes:
             p = Sim(s.desc, precision=args.precision, use_graph=True, device=local)
@@ -269,11 +357,12 @@ def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0, co
             p.step(3)
             p.synchronize()
             plain.append(p)
-        t0 = time.perf_counter()
-        for p in plain:
-            p.step(steps)
+        w0 = time.perf_counter()
+        for p in plain:  # one scene after another, as a caller of the plain path steps them
+            evs.append(timed(p, steps))
             p.synchronize()
-        t_plain = shard.max_over_ranks(time.perf_counter() - t0, dev)
+        wall_p = time.perf_counter() - w0
+        t_plain = shard.max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) * 1e-3, dev)
     finally:
         for p in plain:
             p.close()
@@ -284,7 +373,8 @@ def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0, co
             "plain_updates_per_s": n_units * steps / t_plain,
             "speedup": t_plain / t_batched,
             "batched_algorithmic_gbs": alg_bytes * steps / t_batched / 1e9,
-            "batched_ms_per_step": t_batched / steps * 1e3, "plain_ms_per_step": t_plain / steps * 1e3}
+            "batched_ms_per_step": t_batched / steps * 1e3, "plain_ms_per_step": t_plain / steps * 1e3,
+            "host_wall_ms_per_step": {"batched": wall_b / steps * 1e3, "plain": wall_p / steps * 1e3}}
 
 
 def run_gpu(args) -> None:
@@ -292,21 +382,23 @@ def run_gpu(args) -> None:
     import torch.distributed as dist
 
     import coupledwateranimation_gb300 as cwa
-    from coupledwateranimation_gb300 import PARTICLE_DTYPE, Sim, scenes
+    from coupledwateranimation_gb300 import Sim, scenes
 
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     if ws > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
     wl = scenes.with_zsub(scenes.CONFIGS[args.config](), args.zsub)
-    sims = []
+    last_step = max(wl.steps, args.warmup + args.steps)
+    timed_steps = _timed_steps(args.warmup, args.steps, last_step)
     sim = Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local)
     for k, s in enumerate(wl.scenes):
         sim.upload_particles(k, s.particles)
         sim.upload_wave(k, s.wave, s.wave)
     view = sim.device_view(0)
-    stream = torch.cuda.ExternalStream(view.stream, device=torch.device("cuda", local))
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    stream = torch.cuda.ExternalStream(view.stream, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     n_units = wl.n_particles + wl.n_wave_cells
 
     tune = None
@@ -315,8 +407,8 @@ def run_gpu(args) -> None:
     clk = ClockSampler(local).__enter__()  # samples across warm-up, timed steps, profile and e2e
     # warm-up (graph capture happens here), then a checkpoint: the GPU is kept
     # loaded until the clock sampler is logging (at most ~5 s), and the timed
-    # and profiled windows both restart from the checkpoint, so they cover the
-    # same steps (warmup + 1 .. warmup + steps) of the run on every call
+    # run and the per-pass profile both restart from the checkpoint, so they
+    # cover the same steps of the workload
     sim.step(args.warmup)
     sim.synchronize()
     ckpt_fd, ckpt = tempfile.mkstemp(prefix=f"cwa_bench_r{rank}_", suffix=".ckpt")
@@ -327,53 +419,69 @@ def run_gpu(args) -> None:
         sim.step(20)
         sim.synchronize()
 
-    def rewind():
-        """Back to the checkpoint, then one untimed step (it hashes the
-        loaded positions and replays the step graph of that phase)."""
+    def run_to_end(on_timed):
+        """From the checkpoint (step warmup) to the workload's last step;
+        on_timed(k) brackets the k-th timed step, the rest run untimed."""
         sim.load(ckpt)
-        sim.step(1)
         sim.synchronize()
+        want = set(timed_steps)
+        k = 0
+        with torch.cuda.stream(stream):
+            for n in range(args.warmup + 1, last_step + 1):
+                if n in want:
+                    on_timed(k)
+                    k += 1
+                else:
+                    sim.step(1)
 
-    rewind()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in timed_steps]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in timed_steps]
 
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    def one_timed(k):
+        flush.fill_(k & 0xFF)
+        starts[k].record(stream)
+        sim.step(1)
+        ends[k].record(stream)
+
     if ws > 1:
         dist.barrier()
     torch.cuda.synchronize()
     l0 = sim.launch_count
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            flush.fill_(k & 0xFF)
-            starts[k].record(stream)
-            sim.step(1)
-            ends[k].record(stream)
+    w0 = time.perf_counter()
+    run_to_end(one_timed)
     torch.cuda.synchronize()
-    launches = sim.launch_count - l0
+    run_wall = time.perf_counter() - w0
+    launches_run = sim.launch_count - l0
     sim.synchronize()
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    ms = sum(step_ms)
     if ws > 1:
-        t = torch.tensor([ms], device=f"cuda:{local}", dtype=torch.float64)
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
         dist.barrier()
-    value = n_units * ws * args.steps / (ms * 1e-3)
+    value = n_units * ws * len(timed_steps) / (ms * 1e-3)
+    # one graph replay per step: the timed steps' share of the run's launches
+    launches = launches_run * len(timed_steps) // max(1, last_step - args.warmup)
+    thirds = np.array_split(np.array(step_ms), 3)
+    window = {"early_ms": float(thirds[0].mean()), "mid_ms": float(thirds[1].mean()),
+              "late_ms": float(thirds[2].mean()), "min_ms": min(step_ms), "max_ms": max(step_ms)}
 
-    # per-pass profile over the first steps of the same window (CUDA events
-    # on the sim's stream, eager launches)
-    rewind()
-    os.unlink(ckpt)
+    # per-pass profile over the same timed steps (CUDA events on the sim's
+    # stream, eager launches)
     sim.set_profiling(True)
     acc = {p: 0.0 for p in cwa.PASSES}
-    prof_steps = max(3, min(args.steps, 10))
-    with torch.cuda.stream(stream):
-        for k in range(prof_steps):
-            flush.fill_(k & 0xFF)
-            sim.step(1)
-            for p, v in sim.pass_times().items():
-                acc[p] += v
+
+    def one_profiled(k):
+        flush.fill_(k & 0xFF)
+        sim.step(1)
+        for p, v in sim.pass_times().items():
+            acc[p] += v
+
+    run_to_end(one_profiled)
     sim.set_profiling(False)
-    pass_ms = {p: v / prof_steps for p, v in acc.items()}
+    os.unlink(ckpt)
+    pass_ms = {p: v / len(timed_steps) for p, v in acc.items()}
     top = max(pass_ms, key=pass_ms.get)
     n_p, n_c, n_w = wl.n_particles, sum(int(np.prod(sim.grid_dims(k))) for k in range(len(wl.scenes))), \
         wl.n_wave_cells
@@ -385,20 +493,24 @@ def run_gpu(args) -> None:
                      if top in FLOP_PER_PARTICLE else None)
     traffic = _profiled_traffic().get(top)
 
-    # end-to-end through the C ABI with pinned host buffers
+    # end-to-end through the C ABI with pinned host buffers (from the
+    # workload's last state)
     e2e_steps = max(3, min(args.steps, 10))
     pin = []
     for s in wl.scenes:
         hp = torch.empty(s.desc.n_particles * 64, dtype=torch.uint8, pin_memory=True)
-        hp.numpy()[:] = s.particles.view(np.uint8)
         hu = torch.empty((s.desc.wave_nz, s.desc.wave_nx), dtype=torch.float32, pin_memory=True)
-        hu.numpy()[:] = s.wave
-        hu2 = hu.clone().pin_memory()
+        hu2 = torch.empty((s.desc.wave_nz, s.desc.wave_nx), dtype=torch.float32, pin_memory=True)
         pin.append((hp, hu, hu2))
-    h2d = sum(hp.numel() + hu.numel() * 8 for hp, hu, _ in pin)
-    d2h = sum(hp.numel() + hu.numel() * 4 for hp, hu, _ in pin)
     lib = cwa.load()
     import ctypes as C
+    for k, (hp, hu, hu2) in enumerate(pin):  # the host copy of the current state
+        cwa._abi.check(lib.cwa_download_particles(sim.handle, k, C.c_void_p(hp.data_ptr()),
+                                                  wl.scenes[k].desc.n_particles), "download")
+        cwa._abi.check(lib.cwa_download_wave(sim.handle, k, C.c_void_p(hu.data_ptr()), C.c_void_p(hu2.data_ptr()),
+                                             hu.shape[1], hu.shape[0]), "download_wave")
+    h2d = sum(hp.numel() + hu.numel() * 8 for hp, hu, _ in pin)
+    d2h = sum(hp.numel() + hu.numel() * 4 for hp, hu, _ in pin)
     torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
@@ -412,13 +524,15 @@ def run_gpu(args) -> None:
                            "upload_wave")
         sim.step(1)
         for k, (hp, hu, hu2) in enumerate(pin):
+            # u^n becomes the next upload's u^(n-1): the old u^n moves first
+            hu2.copy_(hu)
             cwa._abi.check(lib.cwa_download_particles(sim.handle, k, C.c_void_p(hp.data_ptr()),
                                                       wl.scenes[k].desc.n_particles), "download")
             cwa._abi.check(lib.cwa_download_wave(sim.handle, k, C.c_void_p(hu.data_ptr()), None,
                                                  hu.shape[1], hu.shape[0]), "download_wave")
     e2e_s = time.perf_counter() - t0
     if ws > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}", dtype=torch.float64)
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e_value = n_units * ws * e2e_steps / e2e_s
@@ -427,32 +541,28 @@ def run_gpu(args) -> None:
     fp32_peak = _fp32_gemm_tflops(f"cuda:{local}") if rank == 0 else None
     fp32_peak_kind = "measured (cuBLAS FP32 GEMM, TF32 off)" if fp32_peak else "nominal"
     fp32_peak = fp32_peak or FP32_PEAK_TFLOPS
+    sim.close()
 
-    batched = None
+    batched = []
     if not args.no_batched:
-        batched = batched_vs_plain(args, torch, ws, rank, local)
+        for cfg in (3, 4):
+            batched.append(batched_vs_plain(args, torch, ws, rank, local, cfg))
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu_wl = scenes.with_zsub(scenes.CONFIGS[args.config](), CPU_ZSUB)
-        v, steps, secs, cores = _cpu_leg(cpu_wl, float(os.environ.get("CWA_CPU_SECONDS", "20")))
+        v, steps, secs, cores = _cpu_steps(_oracle_workload(args.config), 1, None,
+                                           float(os.environ.get("CWA_CPU_SECONDS", "20")))
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{steps} full step(s) of the same workload ({secs:.1f} s; sort grid z cells "
+               "sample": f"steps 2-{steps + 1} of the same workload ({secs:.1f} s; sort grid z cells "
                          f"of h/{CPU_ZSUB}, the oracle's fastest), FP64 OpenMP restatement of the "
-                         f"reference shaders (oracle/)"}
-    sim.close()
-    del sims
+                         f"reference shaders (oracle/), inputs from the oracle's own generators"}
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": len(timed_steps),
+            "warmup": args.warmup, "ms_per_step": ms / len(timed_steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded dam-break + Gaussian bumps)",
-            "config": {"workload": wl.name, "particles": wl.n_particles, "wave_cells": wl.n_wave_cells,
-                       "grid_cells": n_c, "precision": ["fp32", "fp32-compensated", "fp64"][args.precision],
-                       "grid_cell": f"h x h x h/{args.zsub}",
-                       "l2": "flushed before every step (256 MiB write, outside the step events)",
-                       "timed_steps": [args.warmup + 2, args.warmup + args.steps + 1],
-                       "parallelism": f"replicas x{ws}"},
+            "config": _config(args, wl.n_particles, wl.n_wave_cells, n_c, timed_steps, ws),
+            "window": window,
             "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": alg[top],
@@ -466,6 +576,7 @@ def run_gpu(args) -> None:
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps},
             "gpu_launches": launches,
+            "run": {"steps": [args.warmup + 1, last_step], "wall_s": run_wall, "launches": launches_run},
             "autotune": None if tune is None else {"best": tune["best"], "best_ms": tune["best_ms"],
                                                   "entry_ms": tune["entry_ms"], "tried": len(tune["tried"])},
             "clocks": clk.summary(),
@@ -475,6 +586,25 @@ def run_gpu(args) -> None:
         if batched:
             line["batched_vs_plain"] = batched
         print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def run_dry(args) -> None:
+    """`--dry-run`: the rank plumbing alone, on CPU (gloo): every rank joins
+    the group, the timing reductions run, rank 0 prints a line with the
+    rank count.  No GPU work; used to test the --gpus launcher."""
+    import torch.distributed as dist
+
+    from coupledwateranimation_gb300 import shard
+    ws, rank, _ = _dist()
+    if ws > 1:
+        dist.init_process_group("gloo")
+    slowest = shard.max_over_ranks(1.0 + rank, None)
+    total = shard.sum_over_ranks(1.0, None)
+    if rank == 0:
+        print(json.dumps({"mode": "dry-run", "n_gpus": ws, "ranks_reporting": int(total), "slowest": slowest,
+                          "config": {"parallelism": f"replicas x{ws}"}}), flush=True)
     if ws > 1:
         dist.destroy_process_group()
 
@@ -723,10 +853,15 @@ def main() -> None:
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--zsub", type=int, default=4, help="z sub-cells per h of the sort grid")
+    ap.add_argument("--dry-run", action="store_true", help="rank plumbing only, on CPU (tests the launcher)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(_launch_ranks(args.gpus))
+    if args.dry_run:
+        run_dry(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.mode == "profile":
         run_profile(args)

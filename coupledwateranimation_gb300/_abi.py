@@ -204,6 +204,9 @@ _PROTOS = {
     "cwa_scan_workspace_bytes": (C.c_size_t, [_I32]),
     "cwa_exclusive_scan_i32": (C.c_int, [_P, _P, _I32, _P, C.c_size_t, _P]),
     "cwa_exclusive_scan_i32_noalloc": (C.c_int, [_P, _P, _I32, _P]),
+    "cwa_scan_status": (C.c_int, [_I32, _P, _P]),
+    "cwa_scan_noalloc_status": (C.c_int, [_P]),
+    "cwa_grid_status": (C.c_int, [_I32, _I32, _P, _P]),
     "cwa_grid_workspace_bytes": (C.c_size_t, [_I32, _I32]),
     "cwa_grid_build": (C.c_int, [_P, _I32, C.POINTER(C.c_float), C.c_float, C.POINTER(_I32), _P, _P,
                                  _P, _P, C.c_size_t, _P]),

@@ -618,20 +618,16 @@ cwa_status read_status(cwa_sim* s) {
   if (v == 0) return CWA_OK;
   CWA_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(int32_t), s->stream));
   CWA_CUDA(cudaStreamSynchronize(s->stream));
-  if (v & kStatusBounds) {
-    set_error("an index check of the debug build failed; the access was skipped");
-    return CWA_ERR_BOUNDS;
-  }
-  if (v & kStatusTimeout) {
-    set_error("a bounded device wait (scan look-back) timed out");
-    return CWA_ERR_TIMEOUT;
-  }
-  if (v & kStatusNonFinite) {
-    set_error("non-finite particle position");
-    return CWA_ERR_NONFINITE;
-  }
-  set_error("a grid cell held more than 1024 particles; its insert order fell back to arrival order");
-  return CWA_ERR_CAPACITY;
+  return status_from_bits(v);
+}
+
+// Waits for `stream`, then maps the status word at d_word (device memory)
+// to a cwa_status.
+cwa_status read_status_word(const int32_t* d_word, void* stream) {
+  int32_t v = 0;
+  CWA_CUDA(cudaMemcpyAsync(&v, d_word, sizeof(int32_t), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  CWA_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  return status_from_bits(v);
 }
 
 void free_sim(cwa_sim* s) {
@@ -654,6 +650,24 @@ void free_sim(cwa_sim* s) {
 
 namespace cwa {
 bool debug_alloc_should_fail() { return injected_alloc_failure(); }
+
+cwa_status status_from_bits(int32_t v) {
+  if (v == 0) return CWA_OK;
+  if (v & kStatusBounds) {
+    set_error("an index check of the debug build failed; the access was skipped");
+    return CWA_ERR_BOUNDS;
+  }
+  if (v & kStatusTimeout) {
+    set_error("a bounded device wait (scan look-back) timed out");
+    return CWA_ERR_TIMEOUT;
+  }
+  if (v & kStatusNonFinite) {
+    set_error("non-finite particle position");
+    return CWA_ERR_NONFINITE;
+  }
+  set_error("a grid cell held more than 1024 particles; its insert order fell back to arrival order");
+  return CWA_ERR_CAPACITY;
+}
 }  // namespace cwa
 
 extern "C" {
@@ -1512,6 +1526,13 @@ cwa_status cwa_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int32_t n
   return CWA_OK;
 }
 
+cwa_status cwa_scan_status(int32_t n, const void* d_workspace, void* stream) {
+  if (n < 0 || !d_workspace) return arg_error("bad arguments");
+  if (n == 0) return CWA_OK;
+  return read_status_word(
+      reinterpret_cast<const int32_t*>(reinterpret_cast<const char*>(d_workspace) + scan_workspace_bytes(n)), stream);
+}
+
 size_t cwa_grid_workspace_bytes(int32_t n, int32_t n_cells) {
   if (n < 0 || n_cells < 1) return 0;
   auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
@@ -1541,7 +1562,7 @@ cwa_status cwa_grid_build(const float* d_pos4, int32_t n, const float lo[3], flo
   w += up((size_t)n * 4 + 4);
   int32_t* list = reinterpret_cast<int32_t*>(w);
   w += up((size_t)n * 4 + 4);
-  int32_t* status = reinterpret_cast<int32_t*>(w);
+  int32_t* status = reinterpret_cast<int32_t*>(w);  // cwa_grid_status reads it
   if (d_cell_of) key = d_cell_of;
   cudaStream_t st = (cudaStream_t)stream;
   CWA_CUDA(cudaMemsetAsync(count, 0, (size_t)nc * 4, st));
@@ -1552,6 +1573,14 @@ cwa_status cwa_grid_build(const float* d_pos4, int32_t n, const float lo[3], flo
   CWA_CUDA(launch_list_insert(key, slot, d_cell_start, list, n, nullptr, st));
   CWA_CUDA(launch_point_rank(key, slot, d_cell_start, list, n, d_sorted_index, status, st));
   return CWA_OK;
+}
+
+cwa_status cwa_grid_status(int32_t n, int32_t n_cells, const void* d_workspace, void* stream) {
+  if (n < 0 || n_cells < 1 || !d_workspace) return arg_error("bad arguments");
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t off = up(scan_workspace_bytes(n_cells + 1)) + up((size_t)n_cells * 4) + 3 * up((size_t)n * 4 + 4);
+  return read_status_word(reinterpret_cast<const int32_t*>(reinterpret_cast<const char*>(d_workspace) + off),
+                          stream);
 }
 
 }  // extern "C"

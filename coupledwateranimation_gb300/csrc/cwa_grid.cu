@@ -22,6 +22,7 @@ namespace {
 constexpr int kScanBlock = 256;
 constexpr int kScanItems = 16;  // 4096-item tiles: half the look-back chain of 2048
 constexpr int kScanTile = kScanBlock * kScanItems;
+static_assert(kScanTile == kScanTileItems, "workspace sizes assume kScanTileItems items a tile");
 constexpr unsigned long long kFlagAgg = 1ull << 32;
 constexpr unsigned long long kFlagInc = 2ull << 32;
 constexpr long kSpinLimit = 1l << 22;
@@ -44,13 +45,16 @@ __device__ __forceinline__ int warp_sum(int v) {
 }
 
 // One tile of kScanTile items per CTA; tiles are ticketed in start order so a
-// CTA only ever waits on CTAs that are already running.  kVec: in and out
+// CTA only ever waits on CTAs that are already running.  A ticket at or past
+// n_tiles (possible only when scans sharing one workspace overlap on the GPU)
+// sets the time-out bit and touches nothing, so the tile-state writes never
+// leave the workspace.  kVec: in and out
 // are 16-byte aligned, so each thread moves its 16 items as four int4s
 // (a vector that would cross n_in / n_out falls back to scalar accesses).
 template <bool kZero, bool kVec>
 __global__ void __launch_bounds__(kScanBlock)
     k_scan(int32_t* in, int32_t* out, int32_t n_in, int32_t n_out, unsigned int* counter,
-           unsigned long long* state, int32_t* status, const int32_t* flag) {
+           unsigned long long* state, int32_t n_tiles, int32_t* status, const int32_t* flag) {
   chain_enter();
   __shared__ int s_tile, s_prefix;
   if (flag && __ldg(flag) == 0) return;  // grid kept this step (Verlet mode)
@@ -59,6 +63,10 @@ __global__ void __launch_bounds__(kScanBlock)
   if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
   __syncthreads();
   const int tile = s_tile;
+  if (tile >= n_tiles) {
+    if (threadIdx.x == 0) atomicOr(status, kStatusTimeout);
+    return;
+  }
   const long base = (long)tile * kScanTile + (long)threadIdx.x * kScanItems;
 
   int v[kScanItems];
@@ -330,7 +338,8 @@ cudaError_t scan_launch(const int32_t* in, int32_t* out, int32_t n_in, int32_t n
   int32_t* inw = const_cast<int32_t*>(in);
   const bool vec = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
 #define CWA_SCAN_K(Z, V) \
-  k_scan<Z, V><<<ws.n_tiles, kScanBlock, 0, stream>>>(inw, out, n_in, n_out, ws.counter, ws.state, status, flag)
+  k_scan<Z, V><<<ws.n_tiles, kScanBlock, 0, stream>>>(inw, out, n_in, n_out, ws.counter, ws.state, ws.n_tiles, \
+                                                       status, flag)
   if (zero_input) {
     if (vec)
       CWA_SCAN_K(true, true);

@@ -91,7 +91,13 @@ struct ScanWorkspace {
   int32_t n_tiles;
 };
 
+// Maps a nonzero device status word to its cwa_status (and sets the error
+// text); 0 maps to CWA_OK.
+cwa_status status_from_bits(int32_t bits);
+
 // ---- grid / sort kernels (cwa_grid.cu) ----
+// Items per scan tile: the workspace holds one 8-byte state per tile.
+constexpr int kScanTileItems = 4096;
 int scan_tile_items();
 size_t scan_workspace_bytes(int32_t n_out);
 void scan_bind_workspace(void* ws, int32_t n_out, ScanWorkspace* out);

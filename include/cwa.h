@@ -326,10 +326,17 @@ cwa_status cwa_get_options(cwa_sim* sim, cwa_sim_options* out);
  * Exclusive prefix sum of int32 (replaces ParallelScan::Compute,
  * SphWave2D/ParallelScan.cpp:43-95 and prefix_sum_cs.glsl:18-43).  Any n >= 0
  * (the reference requires a power of two).  d_out may equal d_in.  The
- * workspace must hold cwa_scan_workspace_bytes(n) bytes of device memory. */
+ * workspace must hold cwa_scan_workspace_bytes(n) bytes of device memory.
+ * The call is asynchronous on `stream`; its look-back waits are bounded, and
+ * one that gives up (the output is then wrong) sets a status word in the
+ * workspace, which cwa_scan_status reads. */
 size_t cwa_scan_workspace_bytes(int32_t n);
 cwa_status cwa_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int32_t n, void* d_workspace,
                                   size_t workspace_bytes, void* stream);
+/* Waits for `stream`, then reports the last cwa_exclusive_scan_i32 that used
+ * this workspace with this n: CWA_OK, or CWA_ERR_TIMEOUT when its look-back
+ * gave up. */
+cwa_status cwa_scan_status(int32_t n, const void* d_workspace, void* stream);
 
 /* Exclusive scan that allocates nothing.  No counterpart in the reference:
  * it exists for callers that cannot lend the workspace the scan above needs
@@ -338,12 +345,18 @@ cwa_status cwa_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int32_t n
  * risk the device synchronisation an allocation may cause).  The scan's
  * scratch is a fixed 66,048-byte array declared by the library, held on
  * every GPU that loads it until the process exits.  n above
- * CWA_NOALLOC_SCAN_MAX_N is rejected with CWA_ERR_CAPACITY.  The first call
- * on a device looks up the array's device address; make it before any
- * stream capture.  All calls on a device share the array: calls whose
- * kernels overlap on the GPU race, so order them (e.g. one stream). */
+ * CWA_NOALLOC_SCAN_MAX_N is rejected with CWA_ERR_CAPACITY.  A call made
+ * outside a stream capture looks up the array's device address on the
+ * current device; a call inside a capture reuses the last address found on
+ * that device, so make one call on each device before any stream capture.
+ * All calls on a device share the array: calls whose kernels overlap on the
+ * GPU race (wrong sums, possibly a time-out, but no write outside the array),
+ * so order them (e.g. one stream).  cwa_scan_noalloc_status waits for
+ * `stream` and reports the last call on the current device: CWA_OK, or
+ * CWA_ERR_TIMEOUT when its look-back gave up. */
 #define CWA_NOALLOC_SCAN_MAX_N 16777216
 cwa_status cwa_exclusive_scan_i32_noalloc(const int32_t* d_in, int32_t* d_out, int32_t n, void* stream);
+cwa_status cwa_scan_noalloc_status(void* stream);
 
 /* Uniform-grid build of n points (float4 xyz, stride 16 B): cell =
  * clamp(floor((p-lo)/cell), 0, dims-1), cell id (k*dims[1]+j)*dims[0]+i,
@@ -357,6 +370,11 @@ cwa_status cwa_grid_build(const float* d_pos4, int32_t n, const float lo[3], flo
                           const int32_t dims[3], int32_t* d_cell_start, int32_t* d_sorted_index,
                           int32_t* d_cell_of, void* d_workspace, size_t workspace_bytes,
                           void* stream);
+/* Waits for `stream`, then reports the last cwa_grid_build on this
+ * workspace with these sizes: CWA_OK, CWA_ERR_NONFINITE (a NaN/Inf point),
+ * CWA_ERR_TIMEOUT (a scan look-back gave up) or CWA_ERR_CAPACITY (a cell
+ * above 1024 points: that cell's order fell back to arrival order). */
+cwa_status cwa_grid_status(int32_t n, int32_t n_cells, const void* d_workspace, void* stream);
 
 /* ---- headless rendering (the reference's display(), Main.cpp:326-474) ----
  * One frame of the wave surface and the particles into an RGBA8 image, no

@@ -103,6 +103,10 @@ def test_invalid_arguments_rejected(lib):
     assert lib.cwa_exclusive_scan_i32(None, None, -1, None, 0, None) == _abi.CWA_ERR_INVALID_ARG
     assert lib.cwa_exclusive_scan_i32(None, None, 0, None, 0, None) == _abi.CWA_OK
     assert lib.cwa_scan_workspace_bytes(1 << 20) > lib.cwa_scan_workspace_bytes(16)
+    # the status queries check their arguments before touching the device
+    assert lib.cwa_scan_status(-1, None, None) == _abi.CWA_ERR_INVALID_ARG
+    assert lib.cwa_scan_status(5, None, None) == _abi.CWA_ERR_INVALID_ARG
+    assert lib.cwa_grid_status(5, 0, None, None) == _abi.CWA_ERR_INVALID_ARG
 
 
 def test_create_without_gpu_reports_no_device(lib):

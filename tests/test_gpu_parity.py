@@ -38,9 +38,10 @@ def _scan_gpu(lib, x: np.ndarray, inplace=False) -> np.ndarray:
     d_in = torch.from_numpy(x.astype(np.int32)).cuda()
     d_out = d_in if inplace else torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
     ws = torch.empty(lib.cwa_scan_workspace_bytes(n), dtype=torch.uint8, device="cuda")
-    st = lib.cwa_exclusive_scan_i32(_abi.ptr(d_in), _abi.ptr(d_out), n, _abi.ptr(ws), ws.numel(),
-                                    C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    st = lib.cwa_exclusive_scan_i32(_abi.ptr(d_in), _abi.ptr(d_out), n, _abi.ptr(ws), ws.numel(), stream)
     assert st == 0, _abi.last_error()
+    assert lib.cwa_scan_status(n, _abi.ptr(ws), stream) == 0, _abi.last_error()
     torch.cuda.synchronize()
     return d_out[:n].cpu().numpy()
 
@@ -85,6 +86,8 @@ def test_grid_build_operator(lib, orc):
                             _abi.ptr(d_cell), _abi.ptr(ws), ws.numel(),
                             C.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert st == 0, _abi.last_error()
+    assert lib.cwa_grid_status(n, nc, _abi.ptr(ws), C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0, \
+        _abi.last_error()
     torch.cuda.synchronize()
     start, order, cell_of = orc.grid_build(pos, [0.0, 0.0, 0.0], cell, (40, 30, 50))
     assert np.array_equal(d_cell.cpu().numpy(), cell_of)

@@ -246,3 +246,27 @@ def test_z_subcells_keep_the_neighbour_set(orc):
     assert np.abs(a[:, 8:11] - b[:, 8:11]).max() <= 1e-11 * np.abs(a[:, 8:11]).max()
     dims = orc.grid_dims(d4)
     assert dims[2] == 4 * orc.grid_dims(d)[2]
+
+
+def test_oracle_workloads_match_library(orc, lib):
+    """The CPU legs of bench.py build their workloads with the oracle's
+    generators (oracle/workloads.py); those must be the library's bytes."""
+    import ctypes as C
+    from coupledwateranimation_gb300 import scenes
+    from oracle import workloads
+    assert C.sizeof(workloads.SceneDesc) == C.sizeof(_abi.SceneDesc)
+    for (a, _), (b, _) in zip(workloads.SceneDesc._fields_, _abi.SceneDesc._fields_):
+        assert a == b and getattr(workloads.SceneDesc, a).offset == getattr(_abi.SceneDesc, b).offset
+    pairs = [(workloads.config0(), scenes.config0()),
+             (workloads.config3(n_scenes=5), scenes.config3(n_scenes=5)),
+             (workloads.config4(n_scenes=2), scenes.config4(n_scenes=2))]
+    for ow, lw in pairs:
+        assert ow.name == lw.name and ow.steps == lw.steps and len(ow.scenes) == len(lw.scenes)
+        for o, s in zip(ow.scenes, lw.scenes):
+            assert bytes(o.desc) == bytes(s.desc)
+            assert np.array_equal(o.particles.view(np.uint32),
+                                  s.particles.view(np.float32).reshape(-1, 16).view(np.uint32))
+            assert np.array_equal(o.wave.view(np.uint32), s.wave.view(np.uint32))
+    r, rl = workloads.reference_preset(), scenes.reference()
+    assert bytes(r.desc) == bytes(rl.desc) and r.desc.n_particles == 20480
+    assert np.array_equal(r.particles.view(np.uint32), rl.particles.view(np.float32).reshape(-1, 16).view(np.uint32))

@@ -31,14 +31,17 @@ def _with_workspace(lib, torch, d_in, n):
     return out
 
 
-def _no_alloc(lib, torch, d_in, n):
-    out = torch.empty(n, dtype=torch.int32, device="cuda")
+def _no_alloc(lib, torch, d_in, n, out=None):
+    out = torch.empty(n, dtype=torch.int32, device="cuda") if out is None else out
     assert lib.cwa_exclusive_scan_i32_noalloc(_abi.ptr(d_in), _abi.ptr(out), n, _stream(torch)) == 0, \
         _abi.last_error()
+    # the look-back's bounded waits all ended in time
+    assert lib.cwa_scan_noalloc_status(_stream(torch)) == 0, _abi.last_error()
     return out
 
 
-@pytest.mark.parametrize("n", [16, 2049, 300_763])
+# 16_777_216 = CWA_NOALLOC_SCAN_MAX_N: the scratch array's tightest fit
+@pytest.mark.parametrize("n", [16, 2049, 300_763, 16_777_216])
 def test_no_alloc_scan_matches_workspace_scan_twice(lib, n):
     import torch
     assert torch.cuda.is_available()
@@ -50,6 +53,23 @@ def test_no_alloc_scan_matches_workspace_scan_twice(lib, n):
         got = _no_alloc(lib, torch, x, n)
         torch.cuda.synchronize()
         assert torch.equal(got, want), f"call {call}: no-allocation scan differs"
+
+
+def test_no_alloc_scan_unaligned_buffers(lib):
+    """Input and output one element past a 16-byte boundary: the scan takes
+    its scalar load / store path; two calls in a row, as above."""
+    import torch
+    n = 100_003
+    rng = np.random.default_rng(7)
+    for call in range(2):
+        xs = torch.from_numpy(rng.integers(0, 50, n + 1).astype(np.int32)).cuda()
+        x = xs[1:]
+        want = _with_workspace(lib, torch, x, n)
+        outs = torch.full((n + 1,), -1, dtype=torch.int32, device="cuda")
+        got = _no_alloc(lib, torch, x, n, out=outs[1:])
+        torch.cuda.synchronize()
+        assert torch.equal(got, want), f"call {call}: unaligned no-allocation scan differs"
+        assert int(outs[0]) == -1, "wrote before the output"
 
 
 def test_no_alloc_scan_rejects_sizes_above_its_limit(lib):
