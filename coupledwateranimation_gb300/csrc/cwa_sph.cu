@@ -145,6 +145,27 @@ __device__ __forceinline__ void row_ranges(const SceneDev* S, const int32_t* __r
   }
 }
 
+// Row r of row_ranges alone (the same arithmetic, so the same window).
+__device__ __forceinline__ void row_range(const SceneDev* S, const int32_t* __restrict__ start, float4 p,
+                                          CellCoord c, float rad2, int r, int& b, int& e) {
+  const int nz = S->dims[2];
+  const float x0f = S->lo[0] + (float)c.x * S->cell;
+  const float y0f = S->lo[1] + (float)c.y * S->cell;
+  const int dx = r / 3 - 1, dy = r % 3 - 1;
+  const float ddx = dx < 0 ? fmaxf(p.x - x0f, 0.0f) : (dx > 0 ? fmaxf(x0f + S->cell - p.x, 0.0f) : 0.0f);
+  const float ddy = dy < 0 ? fmaxf(p.y - y0f, 0.0f) : (dy > 0 ? fmaxf(y0f + S->cell - p.y, 0.0f) : 0.0f);
+  const float d2 = ddx * ddx + ddy * ddy;
+  const bool ok = row_valid(S, c, r) && d2 < rad2;
+  const float t = fmaxf(rad2 - d2, 0.0f);
+  const float w = ok ? t * rsqrtf(t) : 0.0f;
+  const float zl = p.z - S->lo[2], izc = S->inv_cellz, zmax = (float)(nz - 1);
+  const int z0 = (int)fminf(fmaxf(floorf((zl - w) * izc), 0.0f), zmax);
+  const int z1 = (int)fminf(fmaxf(floorf((zl + w) * izc), 0.0f), zmax);
+  const int row = row_id(S, c, r);
+  b = ok ? __ldg(start + row + z0) : 0;
+  e = ok ? __ldg(start + row + z1 + 1) : 0;
+}
+
 __device__ __forceinline__ float uv_s(const SceneDev* S, float x) { return x * S->uvs[0] + S->uvo[0]; }
 __device__ __forceinline__ float uv_t(const SceneDev* S, float z) { return z * S->uvs[1] + S->uvo[1]; }
 
@@ -576,6 +597,52 @@ __global__ void __launch_bounds__(kNbThreads, 8)
   write_pair_rec(xpair, vpair, vel, i, pi, rp);
 }
 
+// The force a particle stores: pressure + viscosity sums (already scaled,
+// fpr / fvr) plus gravity, and for REFERENCE_3D the shader's crest, torque,
+// drag and wave-normal terms (force_comp.glsl:90-114).
+__device__ __forceinline__ float4 force_out(const SceneDev* S, int i, float4 pi, float4 vi, float rho,
+                                            const float fpr[3], const float fvr[3], const float4* force,
+                                            const float* __restrict__ wave) {
+  float4 out;
+  if (S->preset == CWA_PRESET_REFERENCE_3D) {
+    float4 fprev = force[i];
+    float vs = S->visc;
+    if (pi.y > S->crest) {
+      fprev.x /= 0.25f;
+      fprev.y /= 0.25f;
+      fprev.z /= 0.25f;
+      fprev.w /= 0.25f;
+      vs *= 0.5f;
+    }
+    const float* u = wave + S->woff;
+    const int W = S->nx, Hn = S->nz;
+    const float s = uv_s(S, pi.x), t = uv_t(S, pi.z);
+    const float H = sample_height(u, W, Hn, s, t);
+    const float tq[3] = {0.25f * (pi.y * fprev.z - pi.z * fprev.y), 0.25f * (pi.z * fprev.x - pi.x * fprev.z),
+                         0.25f * (pi.x * fprev.y - pi.y * fprev.x)};
+    // WaveVelocity (:117-128) and WaveNormal (:130-139)
+    const float hx = sample_height(u, W, Hn, s + 0.01f, t);
+    const float hy = sample_height(u, W, Hn, s, t + 0.01f);
+    const float wv[3] = {(hx - H) / S->dt, (hy - H) / S->dt, (hx - hy) / 0.01f};
+    const float hR = sample_height(u, W, Hn, s + 1.0f, t) - H;
+    const float hT = sample_height(u, W, Hn, s, t + 1.0f) - H;
+    const float nrm[3] = {hR, hT, -1.0f};
+    const float vv[3] = {vi.x, vi.y, vi.z};
+    float f[3];
+#pragma unroll
+    for (int c2 = 0; c2 < 3; ++c2) {
+      const float drag = -0.25f * (vv[c2] - wv[c2]);
+      const float wf = -H * nrm[c2] * 0.5f;
+      f[c2] = fpr[c2] + fvr[c2] * vs + rho * S->g[c2] + tq[c2] + drag + wf;
+    }
+    out = make_float4(f[0], f[1], f[2], fprev.w);
+  } else {
+    out = make_float4(fpr[0] + fvr[0] * S->visc + rho * S->g[0], fpr[1] + fvr[1] * S->visc + rho * S->g[1],
+                      fpr[2] + fvr[2] * S->visc + rho * S->g[2], 0.0f);
+  }
+  return out;
+}
+
 // Three-component sum in the precision mode: COMPENSATED adds pair terms
 // in float into a partial that the caller folds into a two-sum accumulator
 // after every group of 8 pairs (cascaded summation); FP32 is plain; FP64 is
@@ -731,46 +798,375 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   const T cp = (T)0.5 * cg;
   float fpr[3] = {(float)(cp * fp.x.get()), (float)(cp * fp.y.get()), (float)(cp * fp.z.get())};
   float fvr[3] = {(float)(cg * fv.x.get()), (float)(cg * fv.y.get()), (float)(cg * fv.z.get())};
-  const float rho = rpi.x;
-  float4 out;
-  if (S->preset == CWA_PRESET_REFERENCE_3D) {
-    // force_comp.glsl:90-114
-    float4 fprev = force[i];
-    float vs = S->visc;
-    if (pi.y > S->crest) {
-      fprev.x /= 0.25f;
-      fprev.y /= 0.25f;
-      fprev.z /= 0.25f;
-      fprev.w /= 0.25f;
-      vs *= 0.5f;
+  force[i] = force_out(S, i, pi, vi, rpi.x, fpr, fvr, force, wave);
+}
+
+// ---- streaming neighbour passes (per-step mode, FP32 and compensated) ----
+//
+// Both passes walk every candidate of the particle's nine row windows and
+// keep no hit list: a miss contributes exactly zero (density: min(r^2 - h^2,
+// 0) = 0; force: h - r clamped at 0), so force needs no record of the
+// density pass's hits.  Candidates are taken two at a time with packed
+// float pairs (add / sub / mul / fma .f32x2), which halves the
+// floating-point instructions of a candidate.  A pair is two neighbouring
+// sorted particles of a scene (local indexes 2m, 2m+1), so the pairing, and
+// with it every rounding, depends on the scene's particles alone: not on the
+// CTA that runs them, nor on the other scenes of a batch.  A row window
+// [b, e) is widened to whole pairs; a widened slot is either a particle of
+// the same column outside the window (farther than h, so it adds zero) or,
+// at the edge of a staged segment, a sentinel far away (adds zero).
+//
+// The CTA stages its candidate rows in shared memory in pair-major order
+// (x_a x_b y_a y_b | z_a z_b ...), so one 16-byte and one 8-byte shared load
+// bring the coordinates of two candidates into register pairs.
+
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float2 upk2(uint64_t v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+// (no packed min / max instruction: two scalar ones on the halves)
+__device__ __forceinline__ uint64_t min2(uint64_t a, float b) {
+  const float2 x = upk2(a);
+  return pk2(fminf(x.x, b), fminf(x.y, b));
+}
+__device__ __forceinline__ uint64_t max2(uint64_t a, float b) {
+  const float2 x = upk2(a);
+  return pk2(fmaxf(x.x, b), fmaxf(x.y, b));
+}
+// shared loads of packed pairs
+__device__ __forceinline__ void lds_2x64(const void* p, uint64_t& a, uint64_t& b) {
+  asm volatile("ld.shared.v2.b64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ uint64_t lds_64(const void* p) {
+  uint64_t a;
+  asm volatile("ld.shared.b64 %0, [%1];" : "=l"(a) : "r"(smem_u32(p)));
+  return a;
+}
+
+constexpr float kSentinel = 1.0e18f;  // position of a padding slot: r^2 ~ 3e36, never within h
+constexpr float kTinyR2 = 1.0e-30f;   // r^2 floor of the force pair (self pair: r = 0, dx = 0)
+constexpr int kDenStageCap = 1536;    // staged candidate slots of the density pass (18 KB)
+constexpr int kForStageCap = 1408;    // staged candidate slots of force (44 KB: 5 CTAs a SM)
+
+// Stage plan of a CTA: up to kMaxCols columns x 9 rows, each segment the
+// sorted range [gb, ge) widened to whole pairs of the scene (pairs start at
+// even offsets from the scene's first particle, poff); seg_off is the prefix
+// of the widened lengths (even, so pairs stay aligned).  ncols 0: not staged
+// (too many columns or slots).
+struct PairPlan {
+  int32_t gb[kMaxSegs], ge[kMaxSegs];
+  int32_t seg_off[kMaxSegs + 1];
+  int32_t col0;
+  int32_t ncols;
+};
+
+__device__ __forceinline__ void plan_pairs(const SceneDev* S, const int32_t* __restrict__ start,
+                                           const int32_t* __restrict__ keys, const Tile& tl, int cap,
+                                           PairPlan& sp) {
+  const int lane = threadIdx.x & 31;
+  const CellCoord a = cell_of_key(S, __ldg(keys + tl.begin));
+  const CellCoord b = cell_of_key(S, __ldg(keys + tl.end - 1));
+  const int nx = S->dims[0], ny = S->dims[1], nz = S->dims[2];
+  const int colA = a.x * ny + a.y, colB = b.x * ny + b.y;
+  const int ncols = colB - colA + 1;
+  const int R = S->rz;
+  int len = 0, gb = 0, ge = 0;
+  if (ncols <= kMaxCols && lane < 9 * ncols) {
+    const int g = lane / 9, r = lane % 9;
+    const int col = colA + g;
+    const int cx = col / ny, cy = col - cx * ny;
+    const int zlo = g == 0 ? max(a.z - R, 0) : 0;
+    const int zhi = (g == ncols - 1) ? min(b.z + R, nz - 1) : nz - 1;
+    const int x = cx + r / 3 - 1, y = cy + r % 3 - 1;
+    if (x >= 0 && x < nx && y >= 0 && y < ny) {
+      const int row = S->coff + (x * ny + y) * nz;
+      gb = __ldg(start + row + zlo);
+      ge = __ldg(start + row + zhi + 1);
+      if (ge > gb) len = 2 * (((ge - S->poff + 1) >> 1) - ((gb - S->poff) >> 1));
     }
-    const float* u = wave + S->woff;
-    const int W = S->nx, Hn = S->nz;
-    const float s = uv_s(S, pi.x), t = uv_t(S, pi.z);
-    const float H = sample_height(u, W, Hn, s, t);
-    const float tq[3] = {0.25f * (pi.y * fprev.z - pi.z * fprev.y), 0.25f * (pi.z * fprev.x - pi.x * fprev.z),
-                         0.25f * (pi.x * fprev.y - pi.y * fprev.x)};
-    // WaveVelocity (:215-226) and WaveNormal (:229-237)
-    const float hx = sample_height(u, W, Hn, s + 0.01f, t);
-    const float hy = sample_height(u, W, Hn, s, t + 0.01f);
-    const float wv[3] = {(hx - H) / S->dt, (hy - H) / S->dt, (hx - hy) / 0.01f};
-    const float hR = sample_height(u, W, Hn, s + 1.0f, t) - H;
-    const float hT = sample_height(u, W, Hn, s, t + 1.0f) - H;
-    const float nrm[3] = {hR, hT, -1.0f};
-    const float vv[3] = {vi.x, vi.y, vi.z};
-    float f[3];
-#pragma unroll
-    for (int c2 = 0; c2 < 3; ++c2) {
-      const float drag = -0.25f * (vv[c2] - wv[c2]);
-      const float wf = -H * nrm[c2] * 0.5f;
-      f[c2] = fpr[c2] + fvr[c2] * vs + rho * S->g[c2] + tq[c2] + drag + wf;
-    }
-    out = make_float4(f[0], f[1], f[2], fprev.w);
-  } else {
-    out = make_float4(fpr[0] + fvr[0] * S->visc + rho * S->g[0], fpr[1] + fvr[1] * S->visc + rho * S->g[1],
-                      fpr[2] + fvr[2] * S->visc + rho * S->g[2], 0.0f);
   }
-  force[i] = out;
+  int incl = len;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  if (lane < kMaxSegs) {
+    sp.gb[lane] = gb;
+    sp.ge[lane] = ge;
+    sp.seg_off[lane] = incl - len;
+  }
+  if (lane == 0) {
+    sp.seg_off[kMaxSegs] = total;
+    sp.col0 = colA;
+    sp.ncols = (ncols <= kMaxCols && total <= cap) ? ncols : 0;
+  }
+}
+
+// Segment of staged slot `slot` (seg_off[s] <= slot < seg_off[s + 1]).
+__device__ __forceinline__ int seg_of_slot(const PairPlan& sp, int nseg, int slot) {
+  int lo = 0, hi = nseg;  // invariant: seg_off[lo] <= slot < seg_off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (sp.seg_off[mid] <= slot)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// First sorted index of the pair that holds sorted index j (scene-local pairs).
+__device__ __forceinline__ int pair_floor(int j, int poff) { return j - ((j - poff) & 1); }
+
+// Global sorted index held by staged slot `slot`, or -1 for a padding slot.
+__device__ __forceinline__ int slot_source(const PairPlan& sp, int nseg, int slot, int poff) {
+  const int s = seg_of_slot(sp, nseg, slot);
+  const int g = pair_floor(sp.gb[s], poff) + (slot - sp.seg_off[s]);
+  return (g >= sp.gb[s] && g < sp.ge[s]) ? g : -1;
+}
+
+// A lane's row r: the widened window as a range of pair indexes, staged
+// (pair index into the stage) or global (2 * index = sorted particle).
+struct PairRange {
+  int p0, p1;     // pairs [p0, p1)
+  int lo, hi;     // valid sorted indexes [lo, hi) (global mode masks the rest)
+};
+
+template <int P>
+struct RowSum;  // folds per-row partials in the precision mode
+template <>
+struct RowSum<CWA_PREC_FP32> {
+  float s = 0.0f;
+  __device__ __forceinline__ void add(float x) { s += x; }
+  __device__ __forceinline__ float get() const { return s; }
+};
+template <>
+struct RowSum<CWA_PREC_COMPENSATED> : Sum<CWA_PREC_COMPENSATED> {};
+
+// Density pass, streaming form: rho (poly6 over r < h, self included), the
+// equation of state, the force gather records.
+template <int P, int MINB>
+__global__ void __launch_bounds__(kNbThreads, MINB)
+    k_density(const float4* __restrict__ pos, const int32_t* __restrict__ start, const int32_t* __restrict__ keys,
+              const Tile* __restrict__ tiles, const SceneDev* __restrict__ scenes,
+              const float* __restrict__ wave, float2* __restrict__ rho_p, int32_t n_total, int32_t* status,
+              int32_t allow_stage, const float4* __restrict__ vel, float4* __restrict__ xpair,
+              float4* __restrict__ vpair) {
+  __shared__ __align__(16) float4 s_xy[kDenStageCap / 2];  // (x_a, x_b, y_a, y_b)
+  __shared__ __align__(16) float2 s_z[kDenStageCap / 2];   // (z_a, z_b)
+  __shared__ PairPlan sp;
+  const Tile tl = tiles[blockIdx.x];
+  const SceneDev* S = scenes + tl.scene;
+  if (threadIdx.x < 32) plan_pairs(S, start, keys, tl, kDenStageCap, sp);
+  __syncthreads();
+  const bool staged = allow_stage && sp.ncols > 0;
+  if (staged) {
+    const int nseg = 9 * sp.ncols, npairs = sp.seg_off[nseg] >> 1;
+    for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
+      const int g0 = slot_source(sp, nseg, 2 * q, S->poff), g1 = slot_source(sp, nseg, 2 * q + 1, S->poff);
+      const float4 a = g0 >= 0 ? __ldg(pos + g0) : make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
+      const float4 b = g1 >= 0 ? __ldg(pos + g1) : make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
+      s_xy[q] = make_float4(a.x, b.x, a.y, b.y);
+      s_z[q] = make_float2(a.z, b.z);
+    }
+  }
+  __syncthreads();
+  const int i = tl.begin + threadIdx.x;
+  if (i >= tl.end) return;
+  const float4 pi = __ldg(pos + i);
+  const float h = S->h;
+  const uint64_t PX = pk2(pi.x, pi.x), PY = pk2(pi.y, pi.y), PZ = pk2(pi.z, pi.z);
+  const uint64_t NH2 = pk2(-(h * h), -(h * h)), ZERO = pk2(0.0f, 0.0f);
+  const CellCoord c = cell_of_key(S, __ldg(keys + i));
+  int b[9], e[9];
+  row_ranges(S, start, pi, c, S->hl2, b, e);
+  const int g = staged ? c.x * S->dims[1] + c.y - sp.col0 : 0;
+  RowSum<P> acc;
+#pragma unroll
+  for (int r = 0; r < 9; ++r) {
+    if (e[r] <= b[r]) continue;
+    // scene-local pairs [pb, pe) cover the window
+    const int pb = (b[r] - S->poff) >> 1, pe = (e[r] - S->poff + 1) >> 1;
+    uint64_t part = ZERO;  // accumulates -(h^2 - r^2)^3 over the hits
+    if (staged) {
+      const int s = g * 9 + r;
+      const int q0 = (sp.seg_off[s] >> 1) + (pb - ((sp.gb[s] - S->poff) >> 1));
+      if (CWA_DCHECK_FAILED(g >= 0 && g < sp.ncols && q0 >= 0 && q0 + (pe - pb) <= (sp.seg_off[9 * sp.ncols] >> 1),
+                            status))
+        continue;
+#pragma unroll 4
+      for (int q = q0; q < q0 + (pe - pb); ++q) {
+        uint64_t xx, yy;
+        lds_2x64(&s_xy[q], xx, yy);
+        const uint64_t zz = lds_64(&s_z[q]);
+        const uint64_t dx = sub2(PX, xx), dy = sub2(PY, yy), dz = sub2(PZ, zz);
+        uint64_t qq = fma2(dx, dx, NH2);
+        qq = fma2(dy, dy, qq);
+        qq = fma2(dz, dz, qq);
+        qq = min2(qq, 0.0f);
+        part = fma2(mul2(qq, qq), qq, part);
+      }
+    } else {
+      // global loads; the widened slots outside the window read as far away
+      for (int q = pb; q < pe; ++q) {
+        const int j0 = S->poff + 2 * q, j1 = j0 + 1;
+        const float4 a = (j0 >= b[r] && !CWA_DCHECK_FAILED(j0 < n_total, status)) ? __ldg(pos + j0)
+                                                                                  : make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
+        const float4 bb = (j1 < e[r] && !CWA_DCHECK_FAILED(j1 < n_total, status)) ? __ldg(pos + j1)
+                                                                                 : make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
+        const uint64_t dx = sub2(PX, pk2(a.x, bb.x)), dy = sub2(PY, pk2(a.y, bb.y)), dz = sub2(PZ, pk2(a.z, bb.z));
+        uint64_t qq = fma2(dx, dx, NH2);
+        qq = fma2(dy, dy, qq);
+        qq = fma2(dz, dz, qq);
+        qq = min2(qq, 0.0f);
+        part = fma2(mul2(qq, qq), qq, part);
+      }
+    }
+    const float2 pp = upk2(part);
+    acc.add(-(pp.x + pp.y));
+  }
+  const float rho_t = S->c_poly6 * acc.get();
+  const float2 rp = eos(S, rho_t, pi, wave);
+  rho_p[i] = rp;
+  write_pair_rec(xpair, vpair, vel, i, pi, rp);
+}
+
+// Force pass, streaming form: spiky pressure gradient + viscosity
+// Laplacian over every candidate of the rows (misses add zero), then the
+// preset's per-particle terms.
+template <int P, int MINB>
+__global__ void __launch_bounds__(kNbThreads, MINB)
+    k_force_stream(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                   const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
+                   const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
+                   const SceneDev* __restrict__ scenes, const float* __restrict__ wave, float4* __restrict__ force,
+                   int32_t n_total, const float4* __restrict__ xpair, const float4* __restrict__ vpair,
+                   int32_t* status, int32_t allow_stage) {
+  // pair-major records: (x_a x_b y_a y_b) (z_a z_b p_a p_b) (vx_a vx_b vy_a vy_b) (vz_a vz_b ir_a ir_b)
+  __shared__ __align__(16) float4 s_rec[kForStageCap / 2][4];
+  __shared__ PairPlan sp;
+  const Tile tl = tiles[blockIdx.x];
+  const SceneDev* S = scenes + tl.scene;
+  if (threadIdx.x < 32) plan_pairs(S, start, keys, tl, kForStageCap, sp);
+  __syncthreads();
+  const bool staged = allow_stage && sp.ncols > 0;
+  const float4 far4 = make_float4(kSentinel, kSentinel, kSentinel, 0.0f), zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (staged) {
+    const int nseg = 9 * sp.ncols, npairs = sp.seg_off[nseg] >> 1;
+    for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
+      const int g0 = slot_source(sp, nseg, 2 * q, S->poff), g1 = slot_source(sp, nseg, 2 * q + 1, S->poff);
+      const float4 xa = g0 >= 0 ? __ldg(xpair + g0) : far4, xb = g1 >= 0 ? __ldg(xpair + g1) : far4;
+      const float4 va = g0 >= 0 ? __ldg(vpair + g0) : zero4, vb = g1 >= 0 ? __ldg(vpair + g1) : zero4;
+      s_rec[q][0] = make_float4(xa.x, xb.x, xa.y, xb.y);
+      s_rec[q][1] = make_float4(xa.z, xb.z, xa.w, xb.w);
+      s_rec[q][2] = make_float4(va.x, vb.x, va.y, vb.y);
+      s_rec[q][3] = make_float4(va.z, vb.z, va.w, vb.w);
+    }
+  }
+  __syncthreads();
+  const int i = tl.begin + threadIdx.x;
+  if (i >= tl.end) return;
+  const float4 pi = __ldg(pos + i);
+  const float4 vi = __ldg(vel + i);
+  const float2 rpi = __ldg(rho_p + i);
+  const float h = S->h;
+  const uint64_t PX = pk2(pi.x, pi.x), PY = pk2(pi.y, pi.y), PZ = pk2(pi.z, pi.z);
+  const uint64_t VX = pk2(vi.x, vi.x), VY = pk2(vi.y, vi.y), VZ = pk2(vi.z, vi.z);
+  const uint64_t PI = pk2(rpi.y, rpi.y), H = pk2(h, h), ZERO = pk2(0.0f, 0.0f);
+  const CellCoord c = cell_of_key(S, __ldg(keys + i));
+  const int g = staged ? c.x * S->dims[1] + c.y - sp.col0 : 0;
+  RowSum<P> fp[3], fv[3];
+  auto pair = [&](uint64_t xx, uint64_t yy, uint64_t zz, uint64_t pp, uint64_t vx, uint64_t vy, uint64_t vz,
+                  uint64_t ir, uint64_t (&ap)[3], uint64_t (&av)[3]) {
+    const uint64_t dx = sub2(PX, xx), dy = sub2(PY, yy), dz = sub2(PZ, zz);
+    uint64_t r2 = mul2(dx, dx);
+    r2 = fma2(dy, dy, r2);
+    r2 = fma2(dz, dz, r2);
+    const float2 rm = upk2(max2(r2, kTinyR2));
+    const uint64_t inv = pk2(rsqrtf(rm.x), rsqrtf(rm.y));
+    const uint64_t hr = max2(sub2(H, mul2(r2, inv)), 0.0f);
+    const uint64_t sp2 = mul2(mul2(mul2(mul2(add2(PI, pp), ir), hr), hr), inv);
+    ap[0] = fma2(sp2, dx, ap[0]);
+    ap[1] = fma2(sp2, dy, ap[1]);
+    ap[2] = fma2(sp2, dz, ap[2]);
+    const uint64_t sv = mul2(ir, hr);
+    av[0] = fma2(sv, sub2(vx, VX), av[0]);
+    av[1] = fma2(sv, sub2(vy, VY), av[1]);
+    av[2] = fma2(sv, sub2(vz, VZ), av[2]);
+  };
+#pragma unroll 1
+  for (int r = 0; r < 9; ++r) {
+    int rb, re;
+    row_range(S, start, pi, c, S->hl2, r, rb, re);
+    if (re <= rb) continue;
+    const int pb = (rb - S->poff) >> 1, pe = (re - S->poff + 1) >> 1;
+    uint64_t ap[3] = {ZERO, ZERO, ZERO}, av[3] = {ZERO, ZERO, ZERO};
+    if (staged) {
+      const int s = g * 9 + r;
+      const int q0 = (sp.seg_off[s] >> 1) + (pb - ((sp.gb[s] - S->poff) >> 1));
+      if (CWA_DCHECK_FAILED(g >= 0 && g < sp.ncols && q0 >= 0 && q0 + (pe - pb) <= (sp.seg_off[9 * sp.ncols] >> 1),
+                            status))
+        continue;
+#pragma unroll 2
+      for (int q = q0; q < q0 + (pe - pb); ++q) {
+        uint64_t xx, yy, zz, pp, vx, vy, vz, ir;
+        lds_2x64(&s_rec[q][0], xx, yy);
+        lds_2x64(&s_rec[q][1], zz, pp);
+        lds_2x64(&s_rec[q][2], vx, vy);
+        lds_2x64(&s_rec[q][3], vz, ir);
+        pair(xx, yy, zz, pp, vx, vy, vz, ir, ap, av);
+      }
+    } else {
+      for (int q = pb; q < pe; ++q) {
+        const int j0 = S->poff + 2 * q, j1 = j0 + 1;
+        const bool ok0 = j0 >= rb && !CWA_DCHECK_FAILED(j0 < n_total, status);
+        const bool ok1 = j1 < re && !CWA_DCHECK_FAILED(j1 < n_total, status);
+        const float4 xa = ok0 ? __ldg(xpair + j0) : far4, xb = ok1 ? __ldg(xpair + j1) : far4;
+        const float4 va = ok0 ? __ldg(vpair + j0) : zero4, vb = ok1 ? __ldg(vpair + j1) : zero4;
+        pair(pk2(xa.x, xb.x), pk2(xa.y, xb.y), pk2(xa.z, xb.z), pk2(xa.w, xb.w), pk2(va.x, vb.x), pk2(va.y, vb.y),
+             pk2(va.z, vb.z), pk2(va.w, vb.w), ap, av);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float2 a = upk2(ap[k]), v = upk2(av[k]);
+      fp[k].add(a.x + a.y);
+      fv[k].add(v.x + v.y);
+    }
+  }
+  const float cg = S->k_grad * S->mass;
+  const float cp = 0.5f * cg;
+  const float fpr[3] = {cp * fp[0].get(), cp * fp[1].get(), cp * fp[2].get()};
+  const float fvr[3] = {cg * fv[0].get(), cg * fv[1].get(), cg * fv[2].get()};
+  force[i] = force_out(S, i, pi, vi, rpi.x, fpr, fvr, force, wave);
 }
 
 // Launch-bound variants (min CTAs per SM): the register budget trades
@@ -815,6 +1211,42 @@ void dispatch_force(const NbArgs& a, cudaStream_t st) {
     force_variant<P, 6>(a, st);
 }
 
+template <int P>
+void dispatch_density(const NbArgs& a, cudaStream_t st) {
+#define CWA_DEN(MB)                                                                                       \
+  k_density<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.start, a.keys, a.tiles, a.scenes, a.wave,  \
+                                                      a.rho_p, a.n_total, a.status, a.stage, a.vel,        \
+                                                      a.xpair, a.vpair)
+  if (a.scan_minb >= 8)
+    CWA_DEN(8);
+  else if (a.scan_minb >= 6)
+    CWA_DEN(6);
+  else
+    CWA_DEN(4);
+#undef CWA_DEN
+}
+
+template <int P, int MB>
+void force_stream_variant(const NbArgs& a, cudaStream_t st) {
+  static bool carveout = false;  // shared memory for five 44 KB stages a SM
+  if (!carveout) {
+    cudaFuncSetAttribute(k_force_stream<P, MB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    carveout = true;
+  }
+  k_force_stream<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles,
+                                                           a.scenes, a.wave, a.force, a.n_total, a.xpair,
+                                                           a.vpair, a.status, a.stage);
+}
+
+template <int P>
+void dispatch_force_stream(const NbArgs& a, cudaStream_t st) {
+  if (a.force_minb >= 8)
+    force_stream_variant<P, 5>(a, st);
+  else
+    force_stream_variant<P, 4>(a, st);
+}
+
 }  // namespace
 
 cudaError_t launch_scan_cands(int precision, bool list_mode, const NbArgs& a, cudaStream_t stream) {
@@ -852,4 +1284,24 @@ cudaError_t launch_force(int precision, const NbArgs& a, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
+}  // namespace cwa
+
+namespace cwa {
+cudaError_t launch_density_stream(int precision, const NbArgs& a, cudaStream_t stream) {
+  if (a.n_tiles <= 0) return cudaSuccess;
+  if (precision == CWA_PREC_FP32)
+    dispatch_density<CWA_PREC_FP32>(a, stream);
+  else
+    dispatch_density<CWA_PREC_COMPENSATED>(a, stream);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_force_stream(int precision, const NbArgs& a, cudaStream_t stream) {
+  if (a.n_tiles <= 0) return cudaSuccess;
+  if (precision == CWA_PREC_FP32)
+    dispatch_force_stream<CWA_PREC_FP32>(a, stream);
+  else
+    dispatch_force_stream<CWA_PREC_COMPENSATED>(a, stream);
+  return cudaGetLastError();
+}
 }  // namespace cwa

@@ -53,7 +53,14 @@ typedef enum cwa_status {
  *   coupling through fixed-point deposits. */
 enum { CWA_PRESET_REFERENCE_3D = 0, CWA_PRESET_MULLER = 1 };
 
-/* Accumulation precision of the density / force neighbour sums. */
+/* Accumulation precision of the density / force neighbour sums.
+ * CWA_PREC_FP32: plain float sums.
+ * CWA_PREC_COMPENSATED: cascaded compensated summation.  Pair terms are
+ *   summed in float into short partials (one per candidate row for the
+ *   density, one per group of pairs for the force), and each partial is
+ *   folded into a Knuth two-sum accumulator.  The two-sum is applied to the
+ *   partials, not to every pair term.
+ * CWA_PREC_FP64: pair arithmetic and sums in double. */
 enum { CWA_PREC_FP32 = 0, CWA_PREC_COMPENSATED = 1, CWA_PREC_FP64 = 2 };
 
 /* std430 `struct Particle {vec4 pos, vel, force, extras;}`
@@ -110,18 +117,29 @@ typedef struct cwa_sim_options {
   int32_t precision;       /* CWA_PREC_*                                      */
   int32_t use_graph;       /* capture cwa_step into CUDA graphs               */
   int32_t nb_threads;      /* threads per CTA of the neighbour passes; 0=auto */
-  int32_t nb_stage;        /* density pass stages candidate rows in shared
+  int32_t nb_stage;        /* neighbour passes stage candidate rows in shared
                               memory: 0/1 = on (default), -1 = off         */
   float verlet_skin;       /* 0: sort and scan neighbours every step.  > 0:
                               keep the grid and a list of pairs within
                               h (1 + skin) until some particle has moved
                               skin h / 2 (needs cell_size >= h (1 + skin)) */
-  int32_t nb_scan_minb;    /* density-scan kernel variant: min CTAs per SM
+  int32_t nb_scan_minb;    /* density-pass kernel variant: min CTAs per SM
                               (4, 6, 8; 0 = 4)                              */
   int32_t nb_force_minb;   /* force kernel variant (6, 8; 0 = 8)              */
   int32_t wave_block;      /* blocked wave advance variant (CWA_WAVE_BLOCK_*)  */
-  int32_t reserved[3];
+  int32_t nb_kernel;       /* neighbour passes in per-step FP32 / compensated
+                              mode: CWA_NB_STREAM (default) or
+                              CWA_NB_HIT_LISTS (FP64 and Verlet mode always
+                              use the hit lists)                            */
+  int32_t reserved[2];
 } cwa_sim_options;
+
+/* Neighbour-pass forms.  STREAM: both passes evaluate every candidate of a
+ * particle's row windows, two at a time in packed float pairs; a miss adds
+ * zero, so the density pass hands force no hit list.  HIT_LISTS: the
+ * density pass records each particle's hits as nine 64-bit row masks and
+ * force evaluates only those. */
+enum { CWA_NB_STREAM = 0, CWA_NB_HIT_LISTS = 1 };
 
 /* Blocked wave advance variants: box of 128 x H cells (P: 256 x H) advanced
  * K steps per launch in shared memory; the R and P variants hold each

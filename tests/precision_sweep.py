@@ -1,4 +1,5 @@
-"""Precision sweep of the neighbour sums (FP32, FP32-compensated, FP64).
+"""Precision sweep of the neighbour sums (FP32, FP32 with cascaded two-sum
+accumulation, FP64).
 
 For one workload (default: the 4,194,304-particle dam-break, 256x128x128
 lattice at s = 0.004 with a 2048^2 wave) this measures, per precision mode:
@@ -29,7 +30,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent.parent
 sys.path.insert(0, str(ROOT))
 
-MODES = (("fp32", 0), ("fp32-compensated", 1), ("fp64", 2))
+MODES = (("fp32", 0), ("fp32-cascaded-two-sum", 1), ("fp64", 2))
 
 
 def _records(p: np.ndarray) -> np.ndarray:

@@ -129,10 +129,13 @@ def _oracle_state(orc, parts_records):
 @pytest.mark.parametrize("preset", ["reference", "muller"])
 @pytest.mark.parametrize("prec", [PREC_FP32, PREC_COMPENSATED, PREC_FP64])
 @pytest.mark.parametrize("zsub,stage", [(1, 0), (4, 0), (4, -1)])
-def test_rho_pres_force_parity(lib, orc, preset, prec, zsub, stage):
+@pytest.mark.parametrize("nb", [_abi.NB_STREAM, _abi.NB_HIT_LISTS])
+def test_rho_pres_force_parity(lib, orc, preset, prec, zsub, stage, nb):
+    if prec == PREC_FP64 and nb == _abi.NB_STREAM:
+        pytest.skip("FP64 always runs the hit lists")
     sc = small_reference() if preset == "reference" else small_muller()
     sc.desc.cell_size_z = sc.desc.cell_size / zsub
-    with Sim(sc.desc, precision=prec, nb_stage=stage) as sim:
+    with Sim(sc.desc, precision=prec, nb_stage=stage, nb_kernel=nb) as sim:
         load_scene(sim, 0, sc)
         u_n, _ = sim.download_wave(0)
         p0 = records_f32(sim.download_particles(0))
@@ -525,3 +528,23 @@ def test_autotune_keeps_state_and_results(lib):
         sim.step(8)
         plain = records_f32(sim.download_particles(0))
     assert np.array_equal(bits(tuned), bits(plain))
+
+
+@pytest.mark.parametrize("prec", [PREC_FP32, PREC_COMPENSATED])
+def test_streaming_passes_invariant_to_staging_tiles_and_batching(lib, prec):
+    """The streaming passes pair candidates by their index inside the scene,
+    so staging on or off, 64- or 128-particle CTAs and the scene's place in
+    a batch (here behind a scene of odd size) leave every bit unchanged."""
+    sc = small_muller((14, 15, 13), 0.02, (48, 40), zsub=4, seed=31)
+    odd = small_muller((5, 7, 9), 0.03, (32, 32), seed=32)  # 315 particles: the next scene starts at an odd index
+    def run(scene_list, k, **kw):
+        with Sim([s.desc for s in scene_list], precision=prec, **kw) as sim:
+            for j, s in enumerate(scene_list):
+                load_scene(sim, j, s)
+            sim.step(6)
+            sim.synchronize()
+            return records_f32(sim.download_particles(k))
+    base = run([sc], 0)
+    for kw in ({"nb_stage": -1}, {"nb_threads": 64}, {"nb_threads": 96, "nb_stage": -1}):
+        assert np.array_equal(bits(run([sc], 0, **kw)), bits(base)), kw
+    assert np.array_equal(bits(run([odd, sc], 1)), bits(base)), "batched behind an odd-sized scene"
