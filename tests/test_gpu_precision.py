@@ -17,7 +17,7 @@ def test_precision_sweep_small(lib, orc):
     wl = scenes.Workload("small dam-break", [small_muller((20, 20, 20), 0.02, (128, 128), seed=21, zsub=2)], 8)
     rows = sweep(steps=8, warm=5, workload=wl)
     modes = {r["mode"]: r for r in rows if "mode" in r}
-    assert set(modes) == {"fp32", "fp32-compensated", "fp64"}
+    assert set(modes) == {"fp32", "fp32-cascaded-two-sum", "fp64"}
     for r in modes.values():
         assert r["rho_max_rel"] <= 1e-5
         assert r["p_normwise"] <= 1e-5
