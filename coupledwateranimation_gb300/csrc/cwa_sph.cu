@@ -145,22 +145,30 @@ __device__ __forceinline__ void row_ranges(const SceneDev* S, const int32_t* __r
   }
 }
 
-// Row r of row_ranges alone (the same arithmetic, so the same window).
+// Row r of row_ranges, with every rounding pinned (explicit _rn
+// intrinsics, no contraction left to the compiler): the density pass and
+// force both call it, and force's reading of the density pass's pair masks
+// relies on the two computing bit-identical windows.
 __device__ __forceinline__ void row_range(const SceneDev* S, const int32_t* __restrict__ start, float4 p,
                                           CellCoord c, float rad2, int r, int& b, int& e) {
   const int nz = S->dims[2];
-  const float x0f = S->lo[0] + (float)c.x * S->cell;
-  const float y0f = S->lo[1] + (float)c.y * S->cell;
   const int dx = r / 3 - 1, dy = r % 3 - 1;
-  const float ddx = dx < 0 ? fmaxf(p.x - x0f, 0.0f) : (dx > 0 ? fmaxf(x0f + S->cell - p.x, 0.0f) : 0.0f);
-  const float ddy = dy < 0 ? fmaxf(p.y - y0f, 0.0f) : (dy > 0 ? fmaxf(y0f + S->cell - p.y, 0.0f) : 0.0f);
-  const float d2 = ddx * ddx + ddy * ddy;
+  float ddx = 0.0f, ddy = 0.0f;
+  if (dx != 0) {
+    const float x0f = __fadd_rn(S->lo[0], __fmul_rn((float)c.x, S->cell));
+    ddx = dx < 0 ? fmaxf(__fsub_rn(p.x, x0f), 0.0f) : fmaxf(__fsub_rn(__fadd_rn(x0f, S->cell), p.x), 0.0f);
+  }
+  if (dy != 0) {
+    const float y0f = __fadd_rn(S->lo[1], __fmul_rn((float)c.y, S->cell));
+    ddy = dy < 0 ? fmaxf(__fsub_rn(p.y, y0f), 0.0f) : fmaxf(__fsub_rn(__fadd_rn(y0f, S->cell), p.y), 0.0f);
+  }
+  const float d2 = __fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy));
   const bool ok = row_valid(S, c, r) && d2 < rad2;
-  const float t = fmaxf(rad2 - d2, 0.0f);
-  const float w = ok ? t * rsqrtf(t) : 0.0f;
-  const float zl = p.z - S->lo[2], izc = S->inv_cellz, zmax = (float)(nz - 1);
-  const int z0 = (int)fminf(fmaxf(floorf((zl - w) * izc), 0.0f), zmax);
-  const int z1 = (int)fminf(fmaxf(floorf((zl + w) * izc), 0.0f), zmax);
+  const float t = fmaxf(__fsub_rn(rad2, d2), 0.0f);
+  const float w = ok ? __fmul_rn(t, rsqrtf(t)) : 0.0f;
+  const float zl = __fsub_rn(p.z, S->lo[2]), izc = S->inv_cellz, zmax = (float)(nz - 1);
+  const int z0 = (int)fminf(fmaxf(floorf(__fmul_rn(__fsub_rn(zl, w), izc)), 0.0f), zmax);
+  const int z1 = (int)fminf(fmaxf(floorf(__fmul_rn(__fadd_rn(zl, w), izc)), 0.0f), zmax);
   const int row = row_id(S, c, r);
   b = ok ? __ldg(start + row + z0) : 0;
   e = ok ? __ldg(start + row + z1 + 1) : 0;
@@ -801,24 +809,24 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   force[i] = force_out(S, i, pi, vi, rpi.x, fpr, fvr, force, wave);
 }
 
-// ---- streaming neighbour passes (per-step mode, FP32 and compensated) ----
+// ---- pair-mask neighbour passes (per-step mode, FP32 and compensated) ----
 //
-// Both passes walk every candidate of the particle's nine row windows and
-// keep no hit list: a miss contributes exactly zero (density: min(r^2 - h^2,
-// 0) = 0; force: h - r clamped at 0), so force needs no record of the
-// density pass's hits.  Candidates are taken two at a time with packed
-// float pairs (add / sub / mul / fma .f32x2), which halves the
-// floating-point instructions of a candidate.  A pair is two neighbouring
-// sorted particles of a scene (local indexes 2m, 2m+1), so the pairing, and
-// with it every rounding, depends on the scene's particles alone: not on the
-// CTA that runs them, nor on the other scenes of a batch.  A row window
-// [b, e) is widened to whole pairs; a widened slot is either a particle of
-// the same column outside the window (farther than h, so it adds zero) or,
-// at the edge of a staged segment, a sentinel far away (adds zero).
+// Candidates are taken two at a time: a pair is two neighbouring sorted
+// particles of a scene (local indexes 2m, 2m+1), so the pairing, and with
+// it every rounding, depends on the scene's particles alone: not on the CTA
+// that runs them, nor on the other scenes of a batch.  A row window [b, e)
+// is widened to whole pairs; a widened slot is either a particle of the
+// same column outside the window (farther than h, so it adds exactly zero)
+// or, at the edge of a staged segment, a sentinel far away (adds zero).
 //
-// The CTA stages its candidate rows in shared memory in pair-major order
-// (x_a x_b y_a y_b | z_a z_b ...), so one 16-byte and one 8-byte shared load
-// bring the coordinates of two candidates into register pairs.
+// Density pass: every pair of a particle's nine row windows, in packed float
+// pairs (add / sub / mul / fma .f32x2), from a pair-major shared-memory
+// stage (x_a x_b y_a y_b | z_a z_b); a miss adds min(r^2 - h^2, 0)^3 = 0.
+// Per row it records which pairs hold a hit as a 32-bit pair mask (bit k =
+// the row's k-th pair), so force evaluates only those pairs (about 30 of a
+// particle's ~85), both candidates at once, a miss again adding zero.
+// Force stages the CTA's rows as four structure-of-arrays float4 streams,
+// so neighbouring lanes' pair loads fall in neighbouring 16-byte slots.
 
 __device__ __forceinline__ uint64_t pk2(float a, float b) {
   uint64_t r;
@@ -872,23 +880,30 @@ __device__ __forceinline__ uint64_t lds_64(const void* p) {
 constexpr float kSentinel = 1.0e18f;  // position of a padding slot: r^2 ~ 3e36, never within h
 constexpr float kTinyR2 = 1.0e-30f;   // r^2 floor of the force pair (self pair: r = 0, dx = 0)
 constexpr int kDenStageCap = 1536;    // staged candidate slots of the density pass (18 KB)
-constexpr int kForStageCap = 1408;    // staged candidate slots of force (44 KB: 5 CTAs a SM)
+constexpr int kForStageCap = 1376;    // staged candidate slots of force (43 KB: 5 CTAs a SM)
+constexpr int kPairMaskBits = 32;     // pairs a row's window may span (else force rescans)
 
 // Stage plan of a CTA: up to kMaxCols columns x 9 rows, each segment the
 // sorted range [gb, ge) widened to whole pairs of the scene (pairs start at
 // even offsets from the scene's first particle, poff); seg_off is the prefix
-// of the widened lengths (even, so pairs stay aligned).  ncols 0: not staged
-// (too many columns or slots).
+// of the widened lengths in slots (even, so pairs stay aligned).  ncols 0:
+// not staged (too many columns or slots).  pseg: the segment of every
+// staged pair.
+template <int CAP>
 struct PairPlan {
   int32_t gb[kMaxSegs], ge[kMaxSegs];
   int32_t seg_off[kMaxSegs + 1];
   int32_t col0;
   int32_t ncols;
+  uint8_t pseg[CAP / 2];
 };
 
+// First sorted index of the pair that holds sorted index j (scene-local pairs).
+__device__ __forceinline__ int pair_floor(int j, int poff) { return j - ((j - poff) & 1); }
+
+template <int CAP>
 __device__ __forceinline__ void plan_pairs(const SceneDev* S, const int32_t* __restrict__ start,
-                                           const int32_t* __restrict__ keys, const Tile& tl, int cap,
-                                           PairPlan& sp) {
+                                           const int32_t* __restrict__ keys, const Tile& tl, PairPlan<CAP>& sp) {
   const int lane = threadIdx.x & 31;
   const CellCoord a = cell_of_key(S, __ldg(keys + tl.begin));
   const CellCoord b = cell_of_key(S, __ldg(keys + tl.end - 1));
@@ -918,47 +933,28 @@ __device__ __forceinline__ void plan_pairs(const SceneDev* S, const int32_t* __r
     if (lane >= o) incl += y;
   }
   const int total = __shfl_sync(0xffffffffu, incl, 31);
+  const bool fits = ncols <= kMaxCols && total <= CAP;
   if (lane < kMaxSegs) {
     sp.gb[lane] = gb;
     sp.ge[lane] = ge;
     sp.seg_off[lane] = incl - len;
+    if (fits)  // this segment's pairs
+      for (int q = (incl - len) >> 1; q < incl >> 1; ++q) sp.pseg[q] = (uint8_t)lane;
   }
   if (lane == 0) {
     sp.seg_off[kMaxSegs] = total;
     sp.col0 = colA;
-    sp.ncols = (ncols <= kMaxCols && total <= cap) ? ncols : 0;
+    sp.ncols = fits ? ncols : 0;
   }
 }
 
-// Segment of staged slot `slot` (seg_off[s] <= slot < seg_off[s + 1]).
-__device__ __forceinline__ int seg_of_slot(const PairPlan& sp, int nseg, int slot) {
-  int lo = 0, hi = nseg;  // invariant: seg_off[lo] <= slot < seg_off[hi]
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (sp.seg_off[mid] <= slot)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  return lo;
+// Global sorted indexes held by staged pair q (-1: padding slot).
+template <int CAP>
+__device__ __forceinline__ int2 pair_source(const PairPlan<CAP>& sp, int q, int poff) {
+  const int s = sp.pseg[q];
+  const int g0 = pair_floor(sp.gb[s], poff) + (2 * q - sp.seg_off[s]);
+  return make_int2((g0 >= sp.gb[s] && g0 < sp.ge[s]) ? g0 : -1, (g0 + 1 >= sp.gb[s] && g0 + 1 < sp.ge[s]) ? g0 + 1 : -1);
 }
-
-// First sorted index of the pair that holds sorted index j (scene-local pairs).
-__device__ __forceinline__ int pair_floor(int j, int poff) { return j - ((j - poff) & 1); }
-
-// Global sorted index held by staged slot `slot`, or -1 for a padding slot.
-__device__ __forceinline__ int slot_source(const PairPlan& sp, int nseg, int slot, int poff) {
-  const int s = seg_of_slot(sp, nseg, slot);
-  const int g = pair_floor(sp.gb[s], poff) + (slot - sp.seg_off[s]);
-  return (g >= sp.gb[s] && g < sp.ge[s]) ? g : -1;
-}
-
-// A lane's row r: the widened window as a range of pair indexes, staged
-// (pair index into the stage) or global (2 * index = sorted particle).
-struct PairRange {
-  int p0, p1;     // pairs [p0, p1)
-  int lo, hi;     // valid sorted indexes [lo, hi) (global mode masks the rest)
-};
 
 template <int P>
 struct RowSum;  // folds per-row partials in the precision mode
@@ -971,29 +967,32 @@ struct RowSum<CWA_PREC_FP32> {
 template <>
 struct RowSum<CWA_PREC_COMPENSATED> : Sum<CWA_PREC_COMPENSATED> {};
 
-// Density pass, streaming form: rho (poly6 over r < h, self included), the
-// equation of state, the force gather records.
+// Density pass, pair form: rho (poly6 over r < h, self included), the
+// equation of state, force's gather records, and per row the mask of pairs
+// that hold a hit (masks[r * n_total + i]; rows[i] = rows with a nonzero
+// mask as bits, or -1 when some window spans more than 32 pairs).
 template <int P, int MINB>
 __global__ void __launch_bounds__(kNbThreads, MINB)
     k_density(const float4* __restrict__ pos, const int32_t* __restrict__ start, const int32_t* __restrict__ keys,
               const Tile* __restrict__ tiles, const SceneDev* __restrict__ scenes,
-              const float* __restrict__ wave, float2* __restrict__ rho_p, int32_t n_total, int32_t* status,
-              int32_t allow_stage, const float4* __restrict__ vel, float4* __restrict__ xpair,
-              float4* __restrict__ vpair) {
+              const float* __restrict__ wave, float2* __restrict__ rho_p, uint32_t* __restrict__ masks,
+              int32_t* __restrict__ rows_out, int32_t n_total, int32_t* status, int32_t allow_stage,
+              const float4* __restrict__ vel, float4* __restrict__ xpair, float4* __restrict__ vpair) {
   __shared__ __align__(16) float4 s_xy[kDenStageCap / 2];  // (x_a, x_b, y_a, y_b)
   __shared__ __align__(16) float2 s_z[kDenStageCap / 2];   // (z_a, z_b)
-  __shared__ PairPlan sp;
+  __shared__ PairPlan<kDenStageCap> sp;
   const Tile tl = tiles[blockIdx.x];
   const SceneDev* S = scenes + tl.scene;
-  if (threadIdx.x < 32) plan_pairs(S, start, keys, tl, kDenStageCap, sp);
+  if (threadIdx.x < 32) plan_pairs(S, start, keys, tl, sp);
   __syncthreads();
   const bool staged = allow_stage && sp.ncols > 0;
   if (staged) {
-    const int nseg = 9 * sp.ncols, npairs = sp.seg_off[nseg] >> 1;
+    const int npairs = sp.seg_off[9 * sp.ncols] >> 1;
+    const float4 far4 = make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
     for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
-      const int g0 = slot_source(sp, nseg, 2 * q, S->poff), g1 = slot_source(sp, nseg, 2 * q + 1, S->poff);
-      const float4 a = g0 >= 0 ? __ldg(pos + g0) : make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
-      const float4 b = g1 >= 0 ? __ldg(pos + g1) : make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
+      const int2 g = pair_source(sp, q, S->poff);
+      const float4 a = g.x >= 0 ? __ldg(pos + g.x) : far4;
+      const float4 b = g.y >= 0 ? __ldg(pos + g.y) : far4;
       s_xy[q] = make_float4(a.x, b.x, a.y, b.y);
       s_z[q] = make_float2(a.z, b.z);
     }
@@ -1005,90 +1004,105 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   const float h = S->h;
   const uint64_t PX = pk2(pi.x, pi.x), PY = pk2(pi.y, pi.y), PZ = pk2(pi.z, pi.z);
   const uint64_t NH2 = pk2(-(h * h), -(h * h)), ZERO = pk2(0.0f, 0.0f);
+  const float4 far4 = make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
   const CellCoord c = cell_of_key(S, __ldg(keys + i));
-  int b[9], e[9];
-  row_ranges(S, start, pi, c, S->hl2, b, e);
   const int g = staged ? c.x * S->dims[1] + c.y - sp.col0 : 0;
   RowSum<P> acc;
-#pragma unroll
+  int rows = 0;
+  bool overflow = false;
+#pragma unroll 1
   for (int r = 0; r < 9; ++r) {
-    if (e[r] <= b[r]) continue;
-    // scene-local pairs [pb, pe) cover the window
-    const int pb = (b[r] - S->poff) >> 1, pe = (e[r] - S->poff + 1) >> 1;
-    uint64_t part = ZERO;  // accumulates -(h^2 - r^2)^3 over the hits
-    if (staged) {
-      const int s = g * 9 + r;
-      const int q0 = (sp.seg_off[s] >> 1) + (pb - ((sp.gb[s] - S->poff) >> 1));
-      if (CWA_DCHECK_FAILED(g >= 0 && g < sp.ncols && q0 >= 0 && q0 + (pe - pb) <= (sp.seg_off[9 * sp.ncols] >> 1),
-                            status))
-        continue;
-#pragma unroll 4
-      for (int q = q0; q < q0 + (pe - pb); ++q) {
-        uint64_t xx, yy;
-        lds_2x64(&s_xy[q], xx, yy);
-        const uint64_t zz = lds_64(&s_z[q]);
+    uint32_t pm = 0u;  // pairs of the row holding a hit
+    int rb, re;
+    row_range(S, start, pi, c, S->hl2, r, rb, re);
+    if (re > rb) {
+      // scene-local pairs [pb, pe) cover the window
+      const int pb = (rb - S->poff) >> 1, pe = (re - S->poff + 1) >> 1;
+      overflow |= pe - pb > kPairMaskBits;
+      uint64_t part = ZERO;  // accumulates -(h^2 - r^2)^3 over the hits
+      uint32_t bit = 1u;
+      auto test = [&](uint64_t xx, uint64_t yy, uint64_t zz) {
         const uint64_t dx = sub2(PX, xx), dy = sub2(PY, yy), dz = sub2(PZ, zz);
         uint64_t qq = fma2(dx, dx, NH2);
         qq = fma2(dy, dy, qq);
         qq = fma2(dz, dz, qq);
-        qq = min2(qq, 0.0f);
-        part = fma2(mul2(qq, qq), qq, part);
+        const float2 m = upk2(qq);
+        const float mx = fminf(m.x, 0.0f), my = fminf(m.y, 0.0f);
+        if (fminf(mx, my) < 0.0f) pm |= bit;
+        bit <<= 1;
+        const uint64_t mm = pk2(mx, my);
+        part = fma2(mul2(mm, mm), mm, part);
+      };
+      if (staged) {
+        const int s = g * 9 + r;
+        const int q0 = (sp.seg_off[s] >> 1) + (pb - ((sp.gb[s] - S->poff) >> 1));
+        if (!CWA_DCHECK_FAILED(
+                g >= 0 && g < sp.ncols && q0 >= 0 && q0 + (pe - pb) <= (sp.seg_off[9 * sp.ncols] >> 1), status)) {
+#pragma unroll 4
+          for (int q = q0; q < q0 + (pe - pb); ++q) {
+            uint64_t xx, yy;
+            lds_2x64(&s_xy[q], xx, yy);
+            test(xx, yy, lds_64(&s_z[q]));
+          }
+        }
+      } else {
+        // global loads; the widened slots outside the window read as far away
+        for (int q = pb; q < pe; ++q) {
+          const int j0 = S->poff + 2 * q, j1 = j0 + 1;
+          const float4 a = (j0 >= rb && !CWA_DCHECK_FAILED(j0 < n_total, status)) ? __ldg(pos + j0) : far4;
+          const float4 bb = (j1 < re && !CWA_DCHECK_FAILED(j1 < n_total, status)) ? __ldg(pos + j1) : far4;
+          test(pk2(a.x, bb.x), pk2(a.y, bb.y), pk2(a.z, bb.z));
+        }
       }
-    } else {
-      // global loads; the widened slots outside the window read as far away
-      for (int q = pb; q < pe; ++q) {
-        const int j0 = S->poff + 2 * q, j1 = j0 + 1;
-        const float4 a = (j0 >= b[r] && !CWA_DCHECK_FAILED(j0 < n_total, status)) ? __ldg(pos + j0)
-                                                                                  : make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
-        const float4 bb = (j1 < e[r] && !CWA_DCHECK_FAILED(j1 < n_total, status)) ? __ldg(pos + j1)
-                                                                                 : make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
-        const uint64_t dx = sub2(PX, pk2(a.x, bb.x)), dy = sub2(PY, pk2(a.y, bb.y)), dz = sub2(PZ, pk2(a.z, bb.z));
-        uint64_t qq = fma2(dx, dx, NH2);
-        qq = fma2(dy, dy, qq);
-        qq = fma2(dz, dz, qq);
-        qq = min2(qq, 0.0f);
-        part = fma2(mul2(qq, qq), qq, part);
-      }
+      const float2 pp = upk2(part);
+      acc.add(-(pp.x + pp.y));
     }
-    const float2 pp = upk2(part);
-    acc.add(-(pp.x + pp.y));
+    masks[(size_t)r * n_total + i] = pm;
+    if (pm) rows |= 1 << r;
   }
+  rows_out[i] = overflow ? -1 : rows;
   const float rho_t = S->c_poly6 * acc.get();
   const float2 rp = eos(S, rho_t, pi, wave);
   rho_p[i] = rp;
   write_pair_rec(xpair, vpair, vel, i, pi, rp);
 }
 
-// Force pass, streaming form: spiky pressure gradient + viscosity
-// Laplacian over every candidate of the rows (misses add zero), then the
-// preset's per-particle terms.
+// Force pass, pair form: spiky pressure gradient + viscosity Laplacian over
+// the pairs the density pass marked (both candidates of a pair at once; a
+// miss and the particle itself add zero), then the preset's per-particle
+// terms.  A particle with an overflowed row rescans its rows from global
+// memory.
 template <int P, int MINB>
 __global__ void __launch_bounds__(kNbThreads, MINB)
-    k_force_stream(const float4* __restrict__ pos, const float4* __restrict__ vel,
-                   const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
-                   const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
-                   const SceneDev* __restrict__ scenes, const float* __restrict__ wave, float4* __restrict__ force,
-                   int32_t n_total, const float4* __restrict__ xpair, const float4* __restrict__ vpair,
-                   int32_t* status, int32_t allow_stage) {
-  // pair-major records: (x_a x_b y_a y_b) (z_a z_b p_a p_b) (vx_a vx_b vy_a vy_b) (vz_a vz_b ir_a ir_b)
-  __shared__ __align__(16) float4 s_rec[kForStageCap / 2][4];
-  __shared__ PairPlan sp;
+    k_force_pairs(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                  const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
+                  const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
+                  const SceneDev* __restrict__ scenes, const float* __restrict__ wave, float4* __restrict__ force,
+                  const uint32_t* __restrict__ masks, const int32_t* __restrict__ rows_in, int32_t n_total,
+                  const float4* __restrict__ xpair, const float4* __restrict__ vpair, int32_t* status,
+                  int32_t allow_stage) {
+  // four pair-major streams: (x_a x_b y_a y_b) (z_a z_b p_a p_b) (vx_a vx_b vy_a vy_b) (vz_a vz_b ir_a ir_b)
+  __shared__ __align__(16) float4 s_a[kForStageCap / 2];
+  __shared__ __align__(16) float4 s_b[kForStageCap / 2];
+  __shared__ __align__(16) float4 s_c[kForStageCap / 2];
+  __shared__ __align__(16) float4 s_d[kForStageCap / 2];
+  __shared__ PairPlan<kForStageCap> sp;
   const Tile tl = tiles[blockIdx.x];
   const SceneDev* S = scenes + tl.scene;
-  if (threadIdx.x < 32) plan_pairs(S, start, keys, tl, kForStageCap, sp);
+  if (threadIdx.x < 32) plan_pairs(S, start, keys, tl, sp);
   __syncthreads();
   const bool staged = allow_stage && sp.ncols > 0;
   const float4 far4 = make_float4(kSentinel, kSentinel, kSentinel, 0.0f), zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
   if (staged) {
-    const int nseg = 9 * sp.ncols, npairs = sp.seg_off[nseg] >> 1;
+    const int npairs = sp.seg_off[9 * sp.ncols] >> 1;
     for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
-      const int g0 = slot_source(sp, nseg, 2 * q, S->poff), g1 = slot_source(sp, nseg, 2 * q + 1, S->poff);
-      const float4 xa = g0 >= 0 ? __ldg(xpair + g0) : far4, xb = g1 >= 0 ? __ldg(xpair + g1) : far4;
-      const float4 va = g0 >= 0 ? __ldg(vpair + g0) : zero4, vb = g1 >= 0 ? __ldg(vpair + g1) : zero4;
-      s_rec[q][0] = make_float4(xa.x, xb.x, xa.y, xb.y);
-      s_rec[q][1] = make_float4(xa.z, xb.z, xa.w, xb.w);
-      s_rec[q][2] = make_float4(va.x, vb.x, va.y, vb.y);
-      s_rec[q][3] = make_float4(va.z, vb.z, va.w, vb.w);
+      const int2 g = pair_source(sp, q, S->poff);
+      const float4 xa = g.x >= 0 ? __ldg(xpair + g.x) : far4, xb = g.y >= 0 ? __ldg(xpair + g.y) : far4;
+      const float4 va = g.x >= 0 ? __ldg(vpair + g.x) : zero4, vb = g.y >= 0 ? __ldg(vpair + g.y) : zero4;
+      s_a[q] = make_float4(xa.x, xb.x, xa.y, xb.y);
+      s_b[q] = make_float4(xa.z, xb.z, xa.w, xb.w);
+      s_c[q] = make_float4(va.x, vb.x, va.y, vb.y);
+      s_d[q] = make_float4(va.z, vb.z, va.w, vb.w);
     }
   }
   __syncthreads();
@@ -1122,44 +1136,71 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
     av[1] = fma2(sv, sub2(vy, VY), av[1]);
     av[2] = fma2(sv, sub2(vz, VZ), av[2]);
   };
-#pragma unroll 1
-  for (int r = 0; r < 9; ++r) {
-    int rb, re;
-    row_range(S, start, pi, c, S->hl2, r, rb, re);
-    if (re <= rb) continue;
-    const int pb = (rb - S->poff) >> 1, pe = (re - S->poff + 1) >> 1;
-    uint64_t ap[3] = {ZERO, ZERO, ZERO}, av[3] = {ZERO, ZERO, ZERO};
-    if (staged) {
-      const int s = g * 9 + r;
-      const int q0 = (sp.seg_off[s] >> 1) + (pb - ((sp.gb[s] - S->poff) >> 1));
-      if (CWA_DCHECK_FAILED(g >= 0 && g < sp.ncols && q0 >= 0 && q0 + (pe - pb) <= (sp.seg_off[9 * sp.ncols] >> 1),
-                            status))
-        continue;
-#pragma unroll 2
-      for (int q = q0; q < q0 + (pe - pb); ++q) {
-        uint64_t xx, yy, zz, pp, vx, vy, vz, ir;
-        lds_2x64(&s_rec[q][0], xx, yy);
-        lds_2x64(&s_rec[q][1], zz, pp);
-        lds_2x64(&s_rec[q][2], vx, vy);
-        lds_2x64(&s_rec[q][3], vz, ir);
-        pair(xx, yy, zz, pp, vx, vy, vz, ir, ap, av);
-      }
-    } else {
-      for (int q = pb; q < pe; ++q) {
-        const int j0 = S->poff + 2 * q, j1 = j0 + 1;
-        const bool ok0 = j0 >= rb && !CWA_DCHECK_FAILED(j0 < n_total, status);
-        const bool ok1 = j1 < re && !CWA_DCHECK_FAILED(j1 < n_total, status);
-        const float4 xa = ok0 ? __ldg(xpair + j0) : far4, xb = ok1 ? __ldg(xpair + j1) : far4;
-        const float4 va = ok0 ? __ldg(vpair + j0) : zero4, vb = ok1 ? __ldg(vpair + j1) : zero4;
-        pair(pk2(xa.x, xb.x), pk2(xa.y, xb.y), pk2(xa.z, xb.z), pk2(xa.w, xb.w), pk2(va.x, vb.x), pk2(va.y, vb.y),
-             pk2(va.z, vb.z), pk2(va.w, vb.w), ap, av);
-      }
-    }
+  auto global_pair = [&](int j0, bool ok0, bool ok1, uint64_t (&ap)[3], uint64_t (&av)[3]) {
+    const int j1 = j0 + 1;
+    ok0 = ok0 && !CWA_DCHECK_FAILED(j0 >= 0 && j0 < n_total, status);
+    ok1 = ok1 && !CWA_DCHECK_FAILED(j1 >= 0 && j1 < n_total, status);
+    const float4 xa = ok0 ? __ldg(xpair + j0) : far4, xb = ok1 ? __ldg(xpair + j1) : far4;
+    const float4 va = ok0 ? __ldg(vpair + j0) : zero4, vb = ok1 ? __ldg(vpair + j1) : zero4;
+    pair(pk2(xa.x, xb.x), pk2(xa.y, xb.y), pk2(xa.z, xb.z), pk2(xa.w, xb.w), pk2(va.x, vb.x), pk2(va.y, vb.y),
+         pk2(va.z, vb.z), pk2(va.w, vb.w), ap, av);
+  };
+  const int rows = __ldg(rows_in + i);
+  auto fold = [&](uint64_t (&ap)[3], uint64_t (&av)[3]) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const float2 a = upk2(ap[k]), v = upk2(av[k]);
       fp[k].add(a.x + a.y);
       fv[k].add(v.x + v.y);
+    }
+  };
+  if (rows >= 0) {
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+      uint32_t pm = (rows >> r) & 1 ? __ldg(masks + (size_t)r * n_total + i) : 0u;
+      if (!pm) continue;
+      int rb, re;
+      row_range(S, start, pi, c, S->hl2, r, rb, re);
+      const int pb = (rb - S->poff) >> 1;
+      uint64_t ap[3] = {ZERO, ZERO, ZERO}, av[3] = {ZERO, ZERO, ZERO};
+      if (staged) {
+        const int s = g * 9 + r;
+        const int q0 = (sp.seg_off[s] >> 1) + (pb - ((sp.gb[s] - S->poff) >> 1));
+        const int npairs = sp.seg_off[9 * sp.ncols] >> 1;
+        while (pm) {
+          const int q = q0 + __ffs(pm) - 1;
+          pm &= pm - 1u;
+          if (CWA_DCHECK_FAILED(g >= 0 && g < sp.ncols && q >= 0 && q < npairs, status)) continue;
+          uint64_t xx, yy, zz, pp, vx, vy, vz, ir;
+          lds_2x64(&s_a[q], xx, yy);
+          lds_2x64(&s_b[q], zz, pp);
+          lds_2x64(&s_c[q], vx, vy);
+          lds_2x64(&s_d[q], vz, ir);
+          pair(xx, yy, zz, pp, vx, vy, vz, ir, ap, av);
+        }
+      } else {
+        while (pm) {
+          const int j0 = S->poff + 2 * (pb + __ffs(pm) - 1);
+          pm &= pm - 1u;
+          global_pair(j0, j0 >= rb, j0 + 1 < re, ap, av);
+        }
+      }
+      fold(ap, av);
+    }
+  } else {
+    // a window spans more than 32 pairs: every pair of every row, from global memory
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+      int rb, re;
+      row_range(S, start, pi, c, S->hl2, r, rb, re);
+      if (re <= rb) continue;
+      uint64_t ap[3] = {ZERO, ZERO, ZERO}, av[3] = {ZERO, ZERO, ZERO};
+      const int pb = (rb - S->poff) >> 1, pe = (re - S->poff + 1) >> 1;
+      for (int q = pb; q < pe; ++q) {
+        const int j0 = S->poff + 2 * q;
+        global_pair(j0, j0 >= rb, j0 + 1 < re, ap, av);
+      }
+      fold(ap, av);
     }
   }
   const float cg = S->k_grad * S->mass;
@@ -1213,10 +1254,11 @@ void dispatch_force(const NbArgs& a, cudaStream_t st) {
 
 template <int P>
 void dispatch_density(const NbArgs& a, cudaStream_t st) {
+  uint32_t* masks = reinterpret_cast<uint32_t*>(a.nbm);
 #define CWA_DEN(MB)                                                                                       \
   k_density<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.start, a.keys, a.tiles, a.scenes, a.wave,  \
-                                                      a.rho_p, a.n_total, a.status, a.stage, a.vel,        \
-                                                      a.xpair, a.vpair)
+                                                      a.rho_p, masks, a.nbr_cnt, a.n_total, a.status,      \
+                                                      a.stage, a.vel, a.xpair, a.vpair)
   if (a.scan_minb >= 8)
     CWA_DEN(8);
   else if (a.scan_minb >= 6)
@@ -1227,24 +1269,24 @@ void dispatch_density(const NbArgs& a, cudaStream_t st) {
 }
 
 template <int P, int MB>
-void force_stream_variant(const NbArgs& a, cudaStream_t st) {
+void force_pairs_variant(const NbArgs& a, cudaStream_t st) {
   static bool carveout = false;  // shared memory for five 44 KB stages a SM
   if (!carveout) {
-    cudaFuncSetAttribute(k_force_stream<P, MB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    cudaFuncSetAttribute(k_force_pairs<P, MB>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
     carveout = true;
   }
-  k_force_stream<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles,
-                                                           a.scenes, a.wave, a.force, a.n_total, a.xpair,
-                                                           a.vpair, a.status, a.stage);
+  k_force_pairs<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(
+      a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles, a.scenes, a.wave, a.force,
+      reinterpret_cast<const uint32_t*>(a.nbm), a.nbr_cnt, a.n_total, a.xpair, a.vpair, a.status, a.stage);
 }
 
 template <int P>
-void dispatch_force_stream(const NbArgs& a, cudaStream_t st) {
+void dispatch_force_pairs(const NbArgs& a, cudaStream_t st) {
   if (a.force_minb >= 8)
-    force_stream_variant<P, 5>(a, st);
+    force_pairs_variant<P, 5>(a, st);
   else
-    force_stream_variant<P, 4>(a, st);
+    force_pairs_variant<P, 4>(a, st);
 }
 
 }  // namespace
@@ -1299,9 +1341,9 @@ cudaError_t launch_density_stream(int precision, const NbArgs& a, cudaStream_t s
 cudaError_t launch_force_stream(int precision, const NbArgs& a, cudaStream_t stream) {
   if (a.n_tiles <= 0) return cudaSuccess;
   if (precision == CWA_PREC_FP32)
-    dispatch_force_stream<CWA_PREC_FP32>(a, stream);
+    dispatch_force_pairs<CWA_PREC_FP32>(a, stream);
   else
-    dispatch_force_stream<CWA_PREC_COMPENSATED>(a, stream);
+    dispatch_force_pairs<CWA_PREC_COMPENSATED>(a, stream);
   return cudaGetLastError();
 }
 }  // namespace cwa
