@@ -257,7 +257,7 @@ def _config(args, n_particles: int, n_wave: int, grid_cells: int, timed: list[in
     return {"workload": WORKLOAD_NAMES.get(args.config, str(args.config)), "particles": n_particles,
             "wave_cells": n_wave, "grid_cells": grid_cells, "workload_steps": WORKLOAD_STEPS[args.config],
             "precision": PRECISION_NAMES[args.precision], "grid_cell": f"h x h x h/{args.zsub}",
-            "neighbour_passes": ["streaming", "row-mask hit lists"][args.nb_kernel],
+            "density_pass": ["packed f32x2", "scalar"][args.nb_kernel],
             "l2": "flushed before every timed step (256 MiB write, outside the step events)",
             "timed_steps": timed, "parallelism": f"replicas x{ws}"}
 
@@ -858,7 +858,7 @@ def main() -> None:
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--zsub", type=int, default=4, help="z sub-cells per h of the sort grid")
     ap.add_argument("--nb-kernel", type=int, default=0, choices=[0, 1],
-                    help="neighbour passes: 0 streaming (default), 1 row-mask hit lists")
+                    help="density pass: 0 packed f32x2 (default), 1 scalar")
     ap.add_argument("--dry-run", action="store_true", help="rank plumbing only, on CPU (tests the launcher)")
     args = ap.parse_args()
     if args.warmup < 3:

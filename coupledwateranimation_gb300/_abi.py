@@ -68,7 +68,7 @@ class SimOptions(C.Structure):
                 ("nb_kernel", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
-NB_STREAM, NB_HIT_LISTS = 0, 1  # CWA_NB_*
+NB_PACKED, NB_SCALAR = 0, 1  # CWA_NB_*
 
 
 # CWA_WAVE_BLOCK_*: box rows x steps per launch; R = box column in registers,

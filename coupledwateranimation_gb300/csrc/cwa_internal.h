@@ -181,11 +181,10 @@ cudaError_t launch_scan_cands(int precision, bool list_mode, const NbArgs& a, cu
 // Verlet-mode density over the Verlet list; writes the step's row masks.
 cudaError_t launch_rho_list(int precision, const NbArgs& a, cudaStream_t stream);
 cudaError_t launch_force(int precision, const NbArgs& a, cudaStream_t stream);
-// Streaming neighbour passes (per-step mode, FP32 and compensated only):
-// every candidate of the row windows is evaluated with packed float pairs,
-// misses add zero, and no hit list passes from the density pass to force.
-cudaError_t launch_density_stream(int precision, const NbArgs& a, cudaStream_t stream);
-cudaError_t launch_force_stream(int precision, const NbArgs& a, cudaStream_t stream);
+// Packed density pass (per-step mode, FP32 and compensated only): the
+// candidates two at a time in packed float pairs; writes the same row masks
+// as the scalar density pass, for the same force pass.
+cudaError_t launch_density_packed(int precision, const NbArgs& a, cudaStream_t stream);
 
 // ---- integrate / wave / packing kernels (cwa_step.cu) ----
 // xref/flag (Verlet mode): raises *flag when a particle has moved more than

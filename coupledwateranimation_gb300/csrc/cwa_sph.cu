@@ -809,24 +809,22 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   force[i] = force_out(S, i, pi, vi, rpi.x, fpr, fvr, force, wave);
 }
 
-// ---- pair-mask neighbour passes (per-step mode, FP32 and compensated) ----
+// ---- packed density pass (per-step mode, FP32 and compensated) ----
 //
-// Candidates are taken two at a time: a pair is two neighbouring sorted
-// particles of a scene (local indexes 2m, 2m+1), so the pairing, and with
-// it every rounding, depends on the scene's particles alone: not on the CTA
-// that runs them, nor on the other scenes of a batch.  A row window [b, e)
-// is widened to whole pairs; a widened slot is either a particle of the
-// same column outside the window (farther than h, so it adds exactly zero)
-// or, at the edge of a staged segment, a sentinel far away (adds zero).
-//
-// Density pass: every pair of a particle's nine row windows, in packed float
-// pairs (add / sub / mul / fma .f32x2), from a pair-major shared-memory
-// stage (x_a x_b y_a y_b | z_a z_b); a miss adds min(r^2 - h^2, 0)^3 = 0.
-// Per row it records which pairs hold a hit as a 32-bit pair mask (bit k =
-// the row's k-th pair), so force evaluates only those pairs (about 30 of a
-// particle's ~85), both candidates at once, a miss again adding zero.
-// Force stages the CTA's rows as four structure-of-arrays float4 streams,
-// so neighbouring lanes' pair loads fall in neighbouring 16-byte slots.
+// The density pass takes a particle's candidates two at a time with packed
+// float pairs (add / sub / mul / fma .f32x2), which halves the issued
+// floating-point instructions of a candidate.  A pair is two neighbouring
+// sorted particles of a scene (local indexes 2m, 2m+1), so the pairing, and
+// with it every rounding, depends on the scene's particles alone: not on the
+// CTA that runs them, nor on the other scenes of a batch.  A row window
+// [b, e) is widened to whole pairs; a widened slot is either a particle of
+// the same column outside the window (farther than h, so it adds exactly
+// zero and is never a hit) or, at the edge of a staged segment, a sentinel
+// far away.  The CTA stages its candidate rows pair-major in shared memory
+// (x_a x_b y_a y_b | z_a z_b), so one 16-byte and one 8-byte shared load
+// bring the coordinates of two candidates into register pairs.  The hits go
+// to force as the nine 64-bit row masks the scalar density pass writes
+// (bit b = the candidate at the row's cell-based start + b).
 
 __device__ __forceinline__ uint64_t pk2(float a, float b) {
   uint64_t r;
@@ -878,10 +876,7 @@ __device__ __forceinline__ uint64_t lds_64(const void* p) {
 }
 
 constexpr float kSentinel = 1.0e18f;  // position of a padding slot: r^2 ~ 3e36, never within h
-constexpr float kTinyR2 = 1.0e-30f;   // r^2 floor of the force pair (self pair: r = 0, dx = 0)
 constexpr int kDenStageCap = 1536;    // staged candidate slots of the density pass (18 KB)
-constexpr int kForStageCap = 1376;    // staged candidate slots of force (43 KB: 5 CTAs a SM)
-constexpr int kPairMaskBits = 32;     // pairs a row's window may span (else force rescans)
 
 // Stage plan of a CTA: up to kMaxCols columns x 9 rows, each segment the
 // sorted range [gb, ge) widened to whole pairs of the scene (pairs start at
@@ -967,15 +962,15 @@ struct RowSum<CWA_PREC_FP32> {
 template <>
 struct RowSum<CWA_PREC_COMPENSATED> : Sum<CWA_PREC_COMPENSATED> {};
 
-// Density pass, pair form: rho (poly6 over r < h, self included), the
-// equation of state, force's gather records, and per row the mask of pairs
-// that hold a hit (masks[r * n_total + i]; rows[i] = rows with a nonzero
-// mask as bits, or -1 when some window spans more than 32 pairs).
+// Density pass, packed form: rho (poly6 over r < h, self included), the
+// equation of state, force's gather records, and this step's row masks
+// (nbm[r * n_total + i]; nbr_cnt[i] = rows with a nonzero mask as bits, or
+// -1 when some row's window reaches past bit 63: force then rescans).
 template <int P, int MINB>
 __global__ void __launch_bounds__(kNbThreads, MINB)
     k_density(const float4* __restrict__ pos, const int32_t* __restrict__ start, const int32_t* __restrict__ keys,
               const Tile* __restrict__ tiles, const SceneDev* __restrict__ scenes,
-              const float* __restrict__ wave, float2* __restrict__ rho_p, uint32_t* __restrict__ masks,
+              const float* __restrict__ wave, float2* __restrict__ rho_p, uint64_t* __restrict__ masks,
               int32_t* __restrict__ rows_out, int32_t n_total, int32_t* status, int32_t allow_stage,
               const float4* __restrict__ vel, float4* __restrict__ xpair, float4* __restrict__ vpair) {
   __shared__ __align__(16) float4 s_xy[kDenStageCap / 2];  // (x_a, x_b, y_a, y_b)
@@ -1007,29 +1002,37 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   const float4 far4 = make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
   const CellCoord c = cell_of_key(S, __ldg(keys + i));
   const int g = staged ? c.x * S->dims[1] + c.y - sp.col0 : 0;
+  const int zb = max(c.z - S->rz, 0);  // z cell of every row's cell-based start
   RowSum<P> acc;
   int rows = 0;
   bool overflow = false;
 #pragma unroll 1
   for (int r = 0; r < 9; ++r) {
-    uint32_t pm = 0u;  // pairs of the row holding a hit
+    uint64_t m = 0ull;  // the row's hits: bit b = the candidate at the row's cell-based start + b
     int rb, re;
     row_range(S, start, pi, c, S->hl2, r, rb, re);
     if (re > rb) {
-      // scene-local pairs [pb, pe) cover the window
+      // scene-local pairs [pb, pe) cover the window; w0 = first sorted index they hold
       const int pb = (rb - S->poff) >> 1, pe = (re - S->poff + 1) >> 1;
-      overflow |= pe - pb > kPairMaskBits;
+      const int w0 = S->poff + 2 * pb;
       uint64_t part = ZERO;  // accumulates -(h^2 - r^2)^3 over the hits
-      uint32_t bit = 1u;
+      uint32_t lo = 0u, hi = 0u, cur = 1u;  // hits of pairs 0-15 / 16-31, two bits a pair
+      int k = 0;
       auto test = [&](uint64_t xx, uint64_t yy, uint64_t zz) {
         const uint64_t dx = sub2(PX, xx), dy = sub2(PY, yy), dz = sub2(PZ, zz);
         uint64_t qq = fma2(dx, dx, NH2);
         qq = fma2(dy, dy, qq);
         qq = fma2(dz, dz, qq);
-        const float2 m = upk2(qq);
-        const float mx = fminf(m.x, 0.0f), my = fminf(m.y, 0.0f);
-        if (fminf(mx, my) < 0.0f) pm |= bit;
-        bit <<= 1;
+        const float2 q2 = upk2(qq);
+        const float mx = fminf(q2.x, 0.0f), my = fminf(q2.y, 0.0f);
+        uint32_t two = mx < 0.0f ? cur : 0u;
+        if (my < 0.0f) two |= cur << 1;
+        if (k < 16)
+          lo |= two;
+        else
+          hi |= two;
+        cur = k == 15 ? 1u : cur << 2;
+        ++k;
         const uint64_t mm = pk2(mx, my);
         part = fma2(mul2(mm, mm), mm, part);
       };
@@ -1056,158 +1059,21 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
       }
       const float2 pp = upk2(part);
       acc.add(-(pp.x + pp.y));
+      // place the window's bits at their offset from the row's cell-based start
+      const int base = __ldg(start + row_id(S, c, r) + zb);
+      const int off = w0 - base;  // >= -1 (the widened slot before the window is never a hit)
+      const uint64_t wb = ((uint64_t)hi << 32) | lo;
+      overflow |= pe - pb > 32 || off + 2 * (pe - pb) > kMaskBits;
+      m = off >= 0 ? (off < kMaskBits ? wb << off : 0ull) : wb >> 1;
     }
-    masks[(size_t)r * n_total + i] = pm;
-    if (pm) rows |= 1 << r;
+    masks[(size_t)r * n_total + i] = m;
+    if (m) rows |= 1 << r;
   }
   rows_out[i] = overflow ? -1 : rows;
   const float rho_t = S->c_poly6 * acc.get();
   const float2 rp = eos(S, rho_t, pi, wave);
   rho_p[i] = rp;
   write_pair_rec(xpair, vpair, vel, i, pi, rp);
-}
-
-// Force pass, pair form: spiky pressure gradient + viscosity Laplacian over
-// the pairs the density pass marked (both candidates of a pair at once; a
-// miss and the particle itself add zero), then the preset's per-particle
-// terms.  A particle with an overflowed row rescans its rows from global
-// memory.
-template <int P, int MINB>
-__global__ void __launch_bounds__(kNbThreads, MINB)
-    k_force_pairs(const float4* __restrict__ pos, const float4* __restrict__ vel,
-                  const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
-                  const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
-                  const SceneDev* __restrict__ scenes, const float* __restrict__ wave, float4* __restrict__ force,
-                  const uint32_t* __restrict__ masks, const int32_t* __restrict__ rows_in, int32_t n_total,
-                  const float4* __restrict__ xpair, const float4* __restrict__ vpair, int32_t* status,
-                  int32_t allow_stage) {
-  // four pair-major streams: (x_a x_b y_a y_b) (z_a z_b p_a p_b) (vx_a vx_b vy_a vy_b) (vz_a vz_b ir_a ir_b)
-  __shared__ __align__(16) float4 s_a[kForStageCap / 2];
-  __shared__ __align__(16) float4 s_b[kForStageCap / 2];
-  __shared__ __align__(16) float4 s_c[kForStageCap / 2];
-  __shared__ __align__(16) float4 s_d[kForStageCap / 2];
-  __shared__ PairPlan<kForStageCap> sp;
-  const Tile tl = tiles[blockIdx.x];
-  const SceneDev* S = scenes + tl.scene;
-  if (threadIdx.x < 32) plan_pairs(S, start, keys, tl, sp);
-  __syncthreads();
-  const bool staged = allow_stage && sp.ncols > 0;
-  const float4 far4 = make_float4(kSentinel, kSentinel, kSentinel, 0.0f), zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (staged) {
-    const int npairs = sp.seg_off[9 * sp.ncols] >> 1;
-    for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
-      const int2 g = pair_source(sp, q, S->poff);
-      const float4 xa = g.x >= 0 ? __ldg(xpair + g.x) : far4, xb = g.y >= 0 ? __ldg(xpair + g.y) : far4;
-      const float4 va = g.x >= 0 ? __ldg(vpair + g.x) : zero4, vb = g.y >= 0 ? __ldg(vpair + g.y) : zero4;
-      s_a[q] = make_float4(xa.x, xb.x, xa.y, xb.y);
-      s_b[q] = make_float4(xa.z, xb.z, xa.w, xb.w);
-      s_c[q] = make_float4(va.x, vb.x, va.y, vb.y);
-      s_d[q] = make_float4(va.z, vb.z, va.w, vb.w);
-    }
-  }
-  __syncthreads();
-  const int i = tl.begin + threadIdx.x;
-  if (i >= tl.end) return;
-  const float4 pi = __ldg(pos + i);
-  const float4 vi = __ldg(vel + i);
-  const float2 rpi = __ldg(rho_p + i);
-  const float h = S->h;
-  const uint64_t PX = pk2(pi.x, pi.x), PY = pk2(pi.y, pi.y), PZ = pk2(pi.z, pi.z);
-  const uint64_t VX = pk2(vi.x, vi.x), VY = pk2(vi.y, vi.y), VZ = pk2(vi.z, vi.z);
-  const uint64_t PI = pk2(rpi.y, rpi.y), H = pk2(h, h), ZERO = pk2(0.0f, 0.0f);
-  const CellCoord c = cell_of_key(S, __ldg(keys + i));
-  const int g = staged ? c.x * S->dims[1] + c.y - sp.col0 : 0;
-  RowSum<P> fp[3], fv[3];
-  auto pair = [&](uint64_t xx, uint64_t yy, uint64_t zz, uint64_t pp, uint64_t vx, uint64_t vy, uint64_t vz,
-                  uint64_t ir, uint64_t (&ap)[3], uint64_t (&av)[3]) {
-    const uint64_t dx = sub2(PX, xx), dy = sub2(PY, yy), dz = sub2(PZ, zz);
-    uint64_t r2 = mul2(dx, dx);
-    r2 = fma2(dy, dy, r2);
-    r2 = fma2(dz, dz, r2);
-    const float2 rm = upk2(max2(r2, kTinyR2));
-    const uint64_t inv = pk2(rsqrtf(rm.x), rsqrtf(rm.y));
-    const uint64_t hr = max2(sub2(H, mul2(r2, inv)), 0.0f);
-    const uint64_t sp2 = mul2(mul2(mul2(mul2(add2(PI, pp), ir), hr), hr), inv);
-    ap[0] = fma2(sp2, dx, ap[0]);
-    ap[1] = fma2(sp2, dy, ap[1]);
-    ap[2] = fma2(sp2, dz, ap[2]);
-    const uint64_t sv = mul2(ir, hr);
-    av[0] = fma2(sv, sub2(vx, VX), av[0]);
-    av[1] = fma2(sv, sub2(vy, VY), av[1]);
-    av[2] = fma2(sv, sub2(vz, VZ), av[2]);
-  };
-  auto global_pair = [&](int j0, bool ok0, bool ok1, uint64_t (&ap)[3], uint64_t (&av)[3]) {
-    const int j1 = j0 + 1;
-    ok0 = ok0 && !CWA_DCHECK_FAILED(j0 >= 0 && j0 < n_total, status);
-    ok1 = ok1 && !CWA_DCHECK_FAILED(j1 >= 0 && j1 < n_total, status);
-    const float4 xa = ok0 ? __ldg(xpair + j0) : far4, xb = ok1 ? __ldg(xpair + j1) : far4;
-    const float4 va = ok0 ? __ldg(vpair + j0) : zero4, vb = ok1 ? __ldg(vpair + j1) : zero4;
-    pair(pk2(xa.x, xb.x), pk2(xa.y, xb.y), pk2(xa.z, xb.z), pk2(xa.w, xb.w), pk2(va.x, vb.x), pk2(va.y, vb.y),
-         pk2(va.z, vb.z), pk2(va.w, vb.w), ap, av);
-  };
-  const int rows = __ldg(rows_in + i);
-  auto fold = [&](uint64_t (&ap)[3], uint64_t (&av)[3]) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const float2 a = upk2(ap[k]), v = upk2(av[k]);
-      fp[k].add(a.x + a.y);
-      fv[k].add(v.x + v.y);
-    }
-  };
-  if (rows >= 0) {
-#pragma unroll 1
-    for (int r = 0; r < 9; ++r) {
-      uint32_t pm = (rows >> r) & 1 ? __ldg(masks + (size_t)r * n_total + i) : 0u;
-      if (!pm) continue;
-      int rb, re;
-      row_range(S, start, pi, c, S->hl2, r, rb, re);
-      const int pb = (rb - S->poff) >> 1;
-      uint64_t ap[3] = {ZERO, ZERO, ZERO}, av[3] = {ZERO, ZERO, ZERO};
-      if (staged) {
-        const int s = g * 9 + r;
-        const int q0 = (sp.seg_off[s] >> 1) + (pb - ((sp.gb[s] - S->poff) >> 1));
-        const int npairs = sp.seg_off[9 * sp.ncols] >> 1;
-        while (pm) {
-          const int q = q0 + __ffs(pm) - 1;
-          pm &= pm - 1u;
-          if (CWA_DCHECK_FAILED(g >= 0 && g < sp.ncols && q >= 0 && q < npairs, status)) continue;
-          uint64_t xx, yy, zz, pp, vx, vy, vz, ir;
-          lds_2x64(&s_a[q], xx, yy);
-          lds_2x64(&s_b[q], zz, pp);
-          lds_2x64(&s_c[q], vx, vy);
-          lds_2x64(&s_d[q], vz, ir);
-          pair(xx, yy, zz, pp, vx, vy, vz, ir, ap, av);
-        }
-      } else {
-        while (pm) {
-          const int j0 = S->poff + 2 * (pb + __ffs(pm) - 1);
-          pm &= pm - 1u;
-          global_pair(j0, j0 >= rb, j0 + 1 < re, ap, av);
-        }
-      }
-      fold(ap, av);
-    }
-  } else {
-    // a window spans more than 32 pairs: every pair of every row, from global memory
-#pragma unroll 1
-    for (int r = 0; r < 9; ++r) {
-      int rb, re;
-      row_range(S, start, pi, c, S->hl2, r, rb, re);
-      if (re <= rb) continue;
-      uint64_t ap[3] = {ZERO, ZERO, ZERO}, av[3] = {ZERO, ZERO, ZERO};
-      const int pb = (rb - S->poff) >> 1, pe = (re - S->poff + 1) >> 1;
-      for (int q = pb; q < pe; ++q) {
-        const int j0 = S->poff + 2 * q;
-        global_pair(j0, j0 >= rb, j0 + 1 < re, ap, av);
-      }
-      fold(ap, av);
-    }
-  }
-  const float cg = S->k_grad * S->mass;
-  const float cp = 0.5f * cg;
-  const float fpr[3] = {cp * fp[0].get(), cp * fp[1].get(), cp * fp[2].get()};
-  const float fvr[3] = {cg * fv[0].get(), cg * fv[1].get(), cg * fv[2].get()};
-  force[i] = force_out(S, i, pi, vi, rpi.x, fpr, fvr, force, wave);
 }
 
 // Launch-bound variants (min CTAs per SM): the register budget trades
@@ -1254,10 +1120,9 @@ void dispatch_force(const NbArgs& a, cudaStream_t st) {
 
 template <int P>
 void dispatch_density(const NbArgs& a, cudaStream_t st) {
-  uint32_t* masks = reinterpret_cast<uint32_t*>(a.nbm);
 #define CWA_DEN(MB)                                                                                       \
   k_density<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.start, a.keys, a.tiles, a.scenes, a.wave,  \
-                                                      a.rho_p, masks, a.nbr_cnt, a.n_total, a.status,      \
+                                                      a.rho_p, a.nbm, a.nbr_cnt, a.n_total, a.status,      \
                                                       a.stage, a.vel, a.xpair, a.vpair)
   if (a.scan_minb >= 8)
     CWA_DEN(8);
@@ -1266,27 +1131,6 @@ void dispatch_density(const NbArgs& a, cudaStream_t st) {
   else
     CWA_DEN(4);
 #undef CWA_DEN
-}
-
-template <int P, int MB>
-void force_pairs_variant(const NbArgs& a, cudaStream_t st) {
-  static bool carveout = false;  // shared memory for five 44 KB stages a SM
-  if (!carveout) {
-    cudaFuncSetAttribute(k_force_pairs<P, MB>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         cudaSharedmemCarveoutMaxShared);
-    carveout = true;
-  }
-  k_force_pairs<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(
-      a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles, a.scenes, a.wave, a.force,
-      reinterpret_cast<const uint32_t*>(a.nbm), a.nbr_cnt, a.n_total, a.xpair, a.vpair, a.status, a.stage);
-}
-
-template <int P>
-void dispatch_force_pairs(const NbArgs& a, cudaStream_t st) {
-  if (a.force_minb >= 8)
-    force_pairs_variant<P, 5>(a, st);
-  else
-    force_pairs_variant<P, 4>(a, st);
 }
 
 }  // namespace
@@ -1329,7 +1173,7 @@ cudaError_t launch_force(int precision, const NbArgs& a, cudaStream_t stream) {
 }  // namespace cwa
 
 namespace cwa {
-cudaError_t launch_density_stream(int precision, const NbArgs& a, cudaStream_t stream) {
+cudaError_t launch_density_packed(int precision, const NbArgs& a, cudaStream_t stream) {
   if (a.n_tiles <= 0) return cudaSuccess;
   if (precision == CWA_PREC_FP32)
     dispatch_density<CWA_PREC_FP32>(a, stream);
@@ -1338,12 +1182,4 @@ cudaError_t launch_density_stream(int precision, const NbArgs& a, cudaStream_t s
   return cudaGetLastError();
 }
 
-cudaError_t launch_force_stream(int precision, const NbArgs& a, cudaStream_t stream) {
-  if (a.n_tiles <= 0) return cudaSuccess;
-  if (precision == CWA_PREC_FP32)
-    dispatch_force_pairs<CWA_PREC_FP32>(a, stream);
-  else
-    dispatch_force_pairs<CWA_PREC_COMPENSATED>(a, stream);
-  return cudaGetLastError();
-}
 }  // namespace cwa

@@ -127,19 +127,18 @@ typedef struct cwa_sim_options {
                               (4, 6, 8; 0 = 4)                              */
   int32_t nb_force_minb;   /* force kernel variant (6, 8; 0 = 8)              */
   int32_t wave_block;      /* blocked wave advance variant (CWA_WAVE_BLOCK_*)  */
-  int32_t nb_kernel;       /* neighbour passes in per-step FP32 / compensated
-                              mode: CWA_NB_STREAM (default) or
-                              CWA_NB_HIT_LISTS (FP64 and Verlet mode always
-                              use the hit lists)                            */
+  int32_t nb_kernel;       /* density pass in per-step FP32 / compensated
+                              mode: CWA_NB_PACKED (default) or
+                              CWA_NB_SCALAR (FP64 and Verlet mode always
+                              use the scalar scan)                          */
   int32_t reserved[2];
 } cwa_sim_options;
 
-/* Neighbour-pass forms.  STREAM: both passes evaluate every candidate of a
- * particle's row windows, two at a time in packed float pairs; a miss adds
- * zero, so the density pass hands force no hit list.  HIT_LISTS: the
- * density pass records each particle's hits as nine 64-bit row masks and
- * force evaluates only those. */
-enum { CWA_NB_STREAM = 0, CWA_NB_HIT_LISTS = 1 };
+/* Density-pass forms.  Both test every candidate of a particle's nine row
+ * windows and record its hits as nine 64-bit row masks, which force then
+ * evaluates.  PACKED takes the candidates two at a time in packed float
+ * pairs from a pair-major shared-memory stage; SCALAR one at a time. */
+enum { CWA_NB_PACKED = 0, CWA_NB_SCALAR = 1 };
 
 /* Blocked wave advance variants: box of 128 x H cells (P: 256 x H) advanced
  * K steps per launch in shared memory; the R and P variants hold each

@@ -129,10 +129,10 @@ def _oracle_state(orc, parts_records):
 @pytest.mark.parametrize("preset", ["reference", "muller"])
 @pytest.mark.parametrize("prec", [PREC_FP32, PREC_COMPENSATED, PREC_FP64])
 @pytest.mark.parametrize("zsub,stage", [(1, 0), (4, 0), (4, -1)])
-@pytest.mark.parametrize("nb", [_abi.NB_STREAM, _abi.NB_HIT_LISTS])
+@pytest.mark.parametrize("nb", [_abi.NB_PACKED, _abi.NB_SCALAR])
 def test_rho_pres_force_parity(lib, orc, preset, prec, zsub, stage, nb):
-    if prec == PREC_FP64 and nb == _abi.NB_STREAM:
-        pytest.skip("FP64 always runs the hit lists")
+    if prec == PREC_FP64 and nb == _abi.NB_PACKED:
+        pytest.skip("FP64 always runs the scalar density pass")
     sc = small_reference() if preset == "reference" else small_muller()
     sc.desc.cell_size_z = sc.desc.cell_size / zsub
     with Sim(sc.desc, precision=prec, nb_stage=stage, nb_kernel=nb) as sim:
@@ -531,8 +531,8 @@ def test_autotune_keeps_state_and_results(lib):
 
 
 @pytest.mark.parametrize("prec", [PREC_FP32, PREC_COMPENSATED])
-def test_streaming_passes_invariant_to_staging_tiles_and_batching(lib, prec):
-    """The streaming passes pair candidates by their index inside the scene,
+def test_packed_density_invariant_to_staging_tiles_and_batching(lib, prec):
+    """The packed density pass pairs candidates by their index inside the scene,
     so staging on or off, 64- or 128-particle CTAs and the scene's place in
     a batch (here behind a scene of odd size) leave every bit unchanged."""
     sc = small_muller((14, 15, 13), 0.02, (48, 40), zsub=4, seed=31)
