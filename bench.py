@@ -257,7 +257,6 @@ def _config(args, n_particles: int, n_wave: int, grid_cells: int, timed: list[in
     return {"workload": WORKLOAD_NAMES.get(args.config, str(args.config)), "particles": n_particles,
             "wave_cells": n_wave, "grid_cells": grid_cells, "workload_steps": WORKLOAD_STEPS[args.config],
             "precision": PRECISION_NAMES[args.precision], "grid_cell": f"h x h x h/{args.zsub}",
-            "density_pass": ["packed f32x2", "scalar"][args.nb_kernel],
             "l2": "flushed before every timed step (256 MiB write, outside the step events)",
             "timed_steps": timed, "parallelism": f"replicas x{ws}"}
 
@@ -336,8 +335,7 @@ def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0, co
         e1.record(stream)
         return e0, e1
 
-    with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local,
-             nb_kernel=args.nb_kernel) as sim:
+    with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local) as sim:
         for k, s in enumerate(wl.scenes):
             sim.upload_particles(k, s.particles)
             sim.upload_wave(k, s.wave, s.wave)
@@ -353,7 +351,7 @@ def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0, co
     plain, evs = [], []
     try:
         for s in wl.scenes:
-            p = Sim(s.desc, precision=args.precision, use_graph=True, device=local, nb_kernel=args.nb_kernel)
+            p = Sim(s.desc, precision=args.precision, use_graph=True, device=local)
             p.upload_particles(0, s.particles)
             p.upload_wave(0, s.wave, s.wave)
             p.step(3)
@@ -394,8 +392,7 @@ def run_gpu(args) -> None:
     wl = scenes.with_zsub(scenes.CONFIGS[args.config](), args.zsub)
     last_step = max(wl.steps, args.warmup + args.steps)
     timed_steps = _timed_steps(args.warmup, args.steps, last_step)
-    sim = Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local,
-              nb_kernel=args.nb_kernel)
+    sim = Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local)
     for k, s in enumerate(wl.scenes):
         sim.upload_particles(k, s.particles)
         sim.upload_wave(k, s.wave, s.wave)
@@ -618,8 +615,7 @@ def run_profile(args) -> None:
     hash, scan, list insert, reorder, rho_pres, force, integrate, wave)."""
     from coupledwateranimation_gb300 import Sim, scenes
     wl = scenes.with_zsub(scenes.CONFIGS[args.config](), args.zsub)
-    with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=False,
-             nb_kernel=args.nb_kernel) as sim:
+    with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=False) as sim:
         for k, s in enumerate(wl.scenes):
             sim.upload_particles(k, s.particles)
             sim.upload_wave(k, s.wave, s.wave)
@@ -857,8 +853,6 @@ def main() -> None:
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--zsub", type=int, default=4, help="z sub-cells per h of the sort grid")
-    ap.add_argument("--nb-kernel", type=int, default=0, choices=[0, 1],
-                    help="density pass: 0 packed f32x2 (default), 1 scalar")
     ap.add_argument("--dry-run", action="store_true", help="rank plumbing only, on CPU (tests the launcher)")
     args = ap.parse_args()
     if args.warmup < 3:

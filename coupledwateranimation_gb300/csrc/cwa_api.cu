@@ -54,7 +54,7 @@ struct cwa_sim {
   int32_t* list = nullptr;
   int32_t* count = nullptr;
   int32_t* start = nullptr;
-  uint64_t* nbm = nullptr;     // this step's hits: kNbRows row masks per particle
+  RowMask* nbm = nullptr;      // this step's hits: kNbRows row masks per particle
   int32_t* nbr_cnt = nullptr;
   int32_t* KS = nullptr;       // sorted cell key of each particle (last grid build)
   // Verlet mode
@@ -401,18 +401,9 @@ cwa_status run_grid(cwa_sim* s) {
   return CWA_OK;
 }
 
-// The packed density pass serves per-step mode in FP32 and compensated
-// precision; FP64 and Verlet mode (and nb_kernel = CWA_NB_SCALAR) use the
-// scalar candidate scan.  Both write the row masks force reads.
-bool packed_density(const cwa_sim* s) {
-  return !s->verlet && s->opt.precision != CWA_PREC_FP64 && s->opt.nb_kernel == CWA_NB_PACKED;
-}
-
 cwa_status run_rho_pres(cwa_sim* s) {
   if (s->verlet)
     CWA_CUDA(launch_rho_list(s->opt.precision, nb_args(s), s->stream));
-  else if (packed_density(s))
-    CWA_CUDA(launch_density_packed(s->opt.precision, nb_args(s), s->stream));
   else
     CWA_CUDA(launch_scan_cands(s->opt.precision, false, nb_args(s), s->stream));
   s->launches += s->n_ptiles > 0;
@@ -718,7 +709,6 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   if (o.nb_threads != 0 && (o.nb_threads < 32 || o.nb_threads > 128 || (o.nb_threads & 31)))
     return arg_error("nb_threads must be 0 or a multiple of 32 in [32, 128]");
   if (o.wave_block < 0 || o.wave_block >= CWA_WAVE_BLOCK_COUNT) return arg_error("unknown wave_block variant");
-  if (o.nb_kernel != CWA_NB_PACKED && o.nb_kernel != CWA_NB_SCALAR) return arg_error("unknown nb_kernel");
   std::vector<int32_t> dims(3 * (size_t)n_scenes);
   int64_t np = 0, nc = 0, nw = 0;
   int32_t nmax = 0;

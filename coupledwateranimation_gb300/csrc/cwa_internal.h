@@ -140,13 +140,14 @@ cudaError_t launch_point_rank(const int32_t* key, const int32_t* slot, const int
 // r * n_total + i holding particle i's hits in candidate row r as bits
 // (bit b = the candidate at the row's cell-based start + b).  nbr_cnt holds
 // the rows with a nonzero mask (bit r), or -1 when some row's window reaches
-// past bit 63 (force then rescans the particle's rows).
+// past bit 31 (force then rescans the particle's rows).
 // The Verlet list (pairs within h (1 + skin) at the last rebuild) holds
 // 16-bit codes (row << 12 | offset from the row's cell-based start), entry k
 // of particle i at list[k * n_total + i]; a count of kMaxVerlet + 1 marks an
 // overflowed list, whose reader rescans the particle's rows.
 constexpr int kNbRows = 9;
-constexpr int kMaskBits = 64;
+constexpr int kMaskBits = 32;
+typedef uint32_t RowMask;  // one candidate row's hits, bit b = the candidate at the row's cell-based start + b
 constexpr int kMaxVerlet = 128;
 struct NbArgs {
   const float4* pos;
@@ -159,7 +160,7 @@ struct NbArgs {
   int32_t n_tiles, tile_size;
   const SceneDev* scenes;
   const float* wave;
-  uint64_t* nbm;        // row masks, kNbRows x n_total
+  RowMask* nbm;         // row masks, kNbRows x n_total
   int32_t* nbr_cnt;
   uint16_t* vlist;
   int32_t* vcnt;
@@ -181,10 +182,6 @@ cudaError_t launch_scan_cands(int precision, bool list_mode, const NbArgs& a, cu
 // Verlet-mode density over the Verlet list; writes the step's row masks.
 cudaError_t launch_rho_list(int precision, const NbArgs& a, cudaStream_t stream);
 cudaError_t launch_force(int precision, const NbArgs& a, cudaStream_t stream);
-// Packed density pass (per-step mode, FP32 and compensated only): the
-// candidates two at a time in packed float pairs; writes the same row masks
-// as the scalar density pass, for the same force pass.
-cudaError_t launch_density_packed(int precision, const NbArgs& a, cudaStream_t stream);
 
 // ---- integrate / wave / packing kernels (cwa_step.cu) ----
 // xref/flag (Verlet mode): raises *flag when a particle has moved more than

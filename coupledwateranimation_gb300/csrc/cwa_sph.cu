@@ -23,8 +23,9 @@
 // Either way force runs its pair terms over the step's hits only.
 //
 // A row's cell-based start is start[row + max(cz - rz, 0)], decodable from
-// the particle's sorted cell key alone.  The step's hits are nine 64-bit
-// row masks per particle (bit b = the row's candidate at that start + b):
+// the particle's sorted cell key alone.  The step's hits are nine 32-bit
+// row masks per particle (bit b = the row's candidate at that start + b;
+// with z cells of h/4 a window ends by bit 24 at the benchmark densities):
 // the density pass sets bits in registers, with no per-hit store, and force
 // walks the set bits.  The Verlet list holds 16-bit codes (row << 12 |
 // offset from the same start), so it stays valid while the particles move.
@@ -143,35 +144,6 @@ __device__ __forceinline__ void row_ranges(const SceneDev* S, const int32_t* __r
     b[r] = ok ? __ldg(start + row + z0) : 0;
     e[r] = ok ? __ldg(start + row + z1 + 1) : 0;
   }
-}
-
-// Row r of row_ranges, with every rounding pinned (explicit _rn
-// intrinsics, no contraction left to the compiler): the density pass and
-// force both call it, and force's reading of the density pass's pair masks
-// relies on the two computing bit-identical windows.
-__device__ __forceinline__ void row_range(const SceneDev* S, const int32_t* __restrict__ start, float4 p,
-                                          CellCoord c, float rad2, int r, int& b, int& e) {
-  const int nz = S->dims[2];
-  const int dx = r / 3 - 1, dy = r % 3 - 1;
-  float ddx = 0.0f, ddy = 0.0f;
-  if (dx != 0) {
-    const float x0f = __fadd_rn(S->lo[0], __fmul_rn((float)c.x, S->cell));
-    ddx = dx < 0 ? fmaxf(__fsub_rn(p.x, x0f), 0.0f) : fmaxf(__fsub_rn(__fadd_rn(x0f, S->cell), p.x), 0.0f);
-  }
-  if (dy != 0) {
-    const float y0f = __fadd_rn(S->lo[1], __fmul_rn((float)c.y, S->cell));
-    ddy = dy < 0 ? fmaxf(__fsub_rn(p.y, y0f), 0.0f) : fmaxf(__fsub_rn(__fadd_rn(y0f, S->cell), p.y), 0.0f);
-  }
-  const float d2 = __fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy));
-  const bool ok = row_valid(S, c, r) && d2 < rad2;
-  const float t = fmaxf(__fsub_rn(rad2, d2), 0.0f);
-  const float w = ok ? __fmul_rn(t, rsqrtf(t)) : 0.0f;
-  const float zl = __fsub_rn(p.z, S->lo[2]), izc = S->inv_cellz, zmax = (float)(nz - 1);
-  const int z0 = (int)fminf(fmaxf(floorf(__fmul_rn(__fsub_rn(zl, w), izc)), 0.0f), zmax);
-  const int z1 = (int)fminf(fmaxf(floorf(__fmul_rn(__fadd_rn(zl, w), izc)), 0.0f), zmax);
-  const int row = row_id(S, c, r);
-  b = ok ? __ldg(start + row + z0) : 0;
-  e = ok ? __ldg(start + row + z1 + 1) : 0;
 }
 
 __device__ __forceinline__ float uv_s(const SceneDev* S, float x) { return x * S->uvs[0] + S->uvo[0]; }
@@ -352,12 +324,12 @@ __device__ __forceinline__ T scan_row(Load load, int len, uint32_t code0, T px, 
 
 // Candidate test of one row for the density pass: the sum of q^3 over the
 // hits and the hits themselves as bits of the row window (bit o = candidate
-// o; candidates 64 and up are tested and summed but get no bit).  The tests
+// o; candidates 32 and up are tested and summed but get no bit).  The tests
 // only set register bits, so no lane stores anything per candidate.
 template <class T, class Load>
-__device__ __forceinline__ T scan_row_bits(Load load, int len, T px, T py, T pz, T hit2, uint64_t& bits) {
+__device__ __forceinline__ T scan_row_bits(Load load, int len, T px, T py, T pz, T hit2, RowMask& bits) {
   T part = (T)0;
-  uint32_t lo = 0u, hi = 0u;
+  uint32_t lo = 0u;
   for (int c0 = 0; c0 < len; c0 += 32) {
     const int n = min(len - c0, 32);
     uint32_t m = 0u, bit = 1u;
@@ -374,12 +346,9 @@ __device__ __forceinline__ T scan_row_bits(Load load, int len, T px, T py, T pz,
       }
       bit <<= 1;
     }
-    if (c0 == 0)
-      lo = m;
-    else if (c0 == 32)
-      hi = m;
+    if (c0 == 0) lo = m;
   }
-  bits = ((uint64_t)hi << 32) | lo;
+  bits = lo;
   return part;
 }
 
@@ -395,7 +364,7 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
                  const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
                  const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
                  float2* __restrict__ rho_p, uint16_t* __restrict__ list, int32_t* __restrict__ list_cnt,
-                 uint64_t* __restrict__ masks, float4* __restrict__ xref, int32_t n_total, int32_t* status,
+                 RowMask* __restrict__ masks, float4* __restrict__ xref, int32_t n_total, int32_t* status,
                  const int32_t* __restrict__ flag,
                  int32_t allow_stage, const float4* __restrict__ vel, float4* __restrict__ xpair,
                  float4* __restrict__ vpair) {
@@ -463,7 +432,7 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
     }
     if (MODE == MODE_DENSITY) {
       // row r's hits as bits relative to the row's cell-based start
-      uint64_t bits = 0ull;
+      RowMask bits = 0u;
       T part = (T)0;
       if (len > 0) {
         if (in_stage)
@@ -472,9 +441,9 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
           part = scan_row_bits<T>([&](int o) { return __ldg(cand + o); }, len, px, py, pz, hit2, bits);
       }
       overflow |= off0 + len > kMaskBits;
-      const uint64_t m = off0 < kMaskBits ? bits << off0 : 0ull;
+      const RowMask m = off0 < kMaskBits ? bits << off0 : 0u;
       masks[(size_t)r * n_total + i] = m;
-      if (m != 0ull) hits |= 1 << r;
+      if (m != 0u) hits |= 1 << r;
       acc.add(part);
     } else {
       overflow |= off0 + len > kRowCodeMax;
@@ -518,12 +487,12 @@ __global__ void __launch_bounds__(kNbThreads, 8)
                const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
                const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
                float2* __restrict__ rho_p, const uint16_t* __restrict__ vlist,
-               const int32_t* __restrict__ vcnt, uint64_t* __restrict__ nbm, int32_t* __restrict__ nbr_cnt,
+               const int32_t* __restrict__ vcnt, RowMask* __restrict__ nbm, int32_t* __restrict__ nbr_cnt,
                int32_t n_total, const float4* __restrict__ vel, float4* __restrict__ xpair,
                float4* __restrict__ vpair) {
   using T = Real<P>;
   __shared__ int32_t s_rb[9][kNbThreads];
-  __shared__ uint64_t s_m[kNbRows][kNbThreads];  // this step's row masks
+  __shared__ RowMask s_m[kNbRows][kNbThreads];  // this step's row masks
   const Tile tl = tiles[blockIdx.x];
   const int i = tl.begin + threadIdx.x;
   if (i >= tl.end) return;
@@ -539,9 +508,9 @@ __global__ void __launch_bounds__(kNbThreads, 8)
   bool overflow = false;
   const int vn = __ldg(vcnt + i);
 #pragma unroll
-  for (int r = 0; r < kNbRows; ++r) s_m[r][threadIdx.x] = 0ull;
+  for (int r = 0; r < kNbRows; ++r) s_m[r][threadIdx.x] = 0u;
   // candidate j at offset off of row r (r < 9): a hit sets its row-mask
-  // bit, or marks the particle overflowed when off is past bit 63
+  // bit, or marks the particle overflowed when off is past the mask's last bit
   auto test = [&](int j, int r, uint32_t off) {
     const float4 pj = __ldg(pos + j);
     const T dx = px - (T)pj.x, dy = py - (T)pj.y, dz = pz - (T)pj.z;
@@ -551,7 +520,7 @@ __global__ void __launch_bounds__(kNbThreads, 8)
     const T qp = q > (T)0 ? q : (T)0;
     if (q > (T)0) {
       if (off < (uint32_t)kMaskBits)
-        s_m[r][threadIdx.x] |= 1ull << off;
+        s_m[r][threadIdx.x] |= (RowMask)1u << off;
       else
         overflow = true;
     }
@@ -594,9 +563,9 @@ __global__ void __launch_bounds__(kNbThreads, 8)
   int rows = 0;  // rows with a nonzero mask (bit r)
 #pragma unroll
   for (int r = 0; r < kNbRows; ++r) {
-    const uint64_t m = s_m[r][threadIdx.x];
+    const RowMask m = s_m[r][threadIdx.x];
     nbm[(size_t)r * n_total + i] = m;
-    if (m != 0ull) rows |= 1 << r;
+    if (m != 0u) rows |= 1 << r;
   }
   nbr_cnt[i] = overflow ? -1 : rows;
   const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
@@ -694,13 +663,13 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
             const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
             const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
             const SceneDev* __restrict__ scenes, const float* __restrict__ wave, float4* __restrict__ force,
-            const uint64_t* __restrict__ nbm, const int32_t* __restrict__ nbr_cnt, int32_t n_total,
+            const RowMask* __restrict__ nbm, const int32_t* __restrict__ nbr_cnt, int32_t n_total,
             const float4* __restrict__ xpair, const float4* __restrict__ vpair, int32_t* status) {
   using T = Real<P>;
   // the particle's nonzero row masks and the index of each mask's bit 0
-  // (13.8 KB a CTA: eight CTAs fit the 132 KB shared carveout, which leaves
-  // the L1 more room for the gathers)
-  __shared__ uint64_t s_w[kNbRows][kNbThreads];
+  // (9.2 KB a CTA: eight CTAs fit well inside the shared carveout, which
+  // leaves the L1 more room for the gathers)
+  __shared__ RowMask s_w[kNbRows][kNbThreads];
   __shared__ int32_t s_jb[kNbRows][kNbThreads];
   const Tile tl = tiles[blockIdx.x];
   const SceneDev* S = scenes + tl.scene;
@@ -749,17 +718,17 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
     int nw = 0, left = 0;
 #pragma unroll
     for (int r = 0; r < kNbRows; ++r) {
-      uint64_t m = __ldg(nbm + (size_t)r * n_total + i);
-      if (r == 4) m &= ~(1ull << (i - base[4]));
+      RowMask m = __ldg(nbm + (size_t)r * n_total + i);
+      if (r == 4 && i - base[4] < kMaskBits) m &= ~((RowMask)1u << (i - base[4]));
       if (m) {
         s_w[nw][threadIdx.x] = m;
         s_jb[nw][threadIdx.x] = base[r];
         ++nw;
       }
-      left += __popcll(m);
+      left += __popc(m);
     }
     int wi = 0;
-    uint64_t cw = nw > 0 ? s_w[0][threadIdx.x] : 0ull;
+    RowMask cw = nw > 0 ? s_w[0][threadIdx.x] : 0u;
     int jb = nw > 0 ? s_jb[0][threadIdx.x] : 0;
     for (int k0 = 0; k0 < left; k0 += 8) {
       int js[8];
@@ -767,13 +736,13 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
       for (int u = 0; u < 8; ++u) {
         js[u] = -1;
         if (k0 + u < left) {
-          if (cw == 0ull) {  // the next mask (every compacted mask holds a hit)
+          if (cw == 0u) {  // the next mask (every compacted mask holds a hit)
             ++wi;
             cw = s_w[wi][threadIdx.x];
             jb = s_jb[wi][threadIdx.x];
           }
-          js[u] = jb + __ffsll((long long)cw) - 1;
-          cw &= cw - 1ull;
+          js[u] = jb + __ffs(cw) - 1;
+          cw &= cw - 1u;
         }
       }
 #pragma unroll
@@ -809,277 +778,10 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   force[i] = force_out(S, i, pi, vi, rpi.x, fpr, fvr, force, wave);
 }
 
-// ---- packed density pass (per-step mode, FP32 and compensated) ----
-//
-// The density pass takes a particle's candidates two at a time with packed
-// float pairs (add / sub / mul / fma .f32x2), which halves the issued
-// floating-point instructions of a candidate.  A pair is two neighbouring
-// sorted particles of a scene (local indexes 2m, 2m+1), so the pairing, and
-// with it every rounding, depends on the scene's particles alone: not on the
-// CTA that runs them, nor on the other scenes of a batch.  A row window
-// [b, e) is widened to whole pairs; a widened slot is either a particle of
-// the same column outside the window (farther than h, so it adds exactly
-// zero and is never a hit) or, at the edge of a staged segment, a sentinel
-// far away.  The CTA stages its candidate rows pair-major in shared memory
-// (x_a x_b y_a y_b | z_a z_b), so one 16-byte and one 8-byte shared load
-// bring the coordinates of two candidates into register pairs.  The hits go
-// to force as the nine 64-bit row masks the scalar density pass writes
-// (bit b = the candidate at the row's cell-based start + b).
-
-__device__ __forceinline__ uint64_t pk2(float a, float b) {
-  uint64_t r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ float2 upk2(uint64_t v) {
-  float2 r;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-  return r;
-}
-__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
-  uint64_t r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
-  uint64_t r;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
-  uint64_t r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
-  uint64_t r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-  return r;
-}
-// (no packed min / max instruction: two scalar ones on the halves)
-__device__ __forceinline__ uint64_t min2(uint64_t a, float b) {
-  const float2 x = upk2(a);
-  return pk2(fminf(x.x, b), fminf(x.y, b));
-}
-__device__ __forceinline__ uint64_t max2(uint64_t a, float b) {
-  const float2 x = upk2(a);
-  return pk2(fmaxf(x.x, b), fmaxf(x.y, b));
-}
-// shared loads of packed pairs
-__device__ __forceinline__ void lds_2x64(const void* p, uint64_t& a, uint64_t& b) {
-  asm volatile("ld.shared.v2.b64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(smem_u32(p)));
-}
-__device__ __forceinline__ uint64_t lds_64(const void* p) {
-  uint64_t a;
-  asm volatile("ld.shared.b64 %0, [%1];" : "=l"(a) : "r"(smem_u32(p)));
-  return a;
-}
-
-constexpr float kSentinel = 1.0e18f;  // position of a padding slot: r^2 ~ 3e36, never within h
-constexpr int kDenStageCap = 1536;    // staged candidate slots of the density pass (18 KB)
-
-// Stage plan of a CTA: up to kMaxCols columns x 9 rows, each segment the
-// sorted range [gb, ge) widened to whole pairs of the scene (pairs start at
-// even offsets from the scene's first particle, poff); seg_off is the prefix
-// of the widened lengths in slots (even, so pairs stay aligned).  ncols 0:
-// not staged (too many columns or slots).  pseg: the segment of every
-// staged pair.
-template <int CAP>
-struct PairPlan {
-  int32_t gb[kMaxSegs], ge[kMaxSegs];
-  int32_t seg_off[kMaxSegs + 1];
-  int32_t col0;
-  int32_t ncols;
-  uint8_t pseg[CAP / 2];
-};
-
-// First sorted index of the pair that holds sorted index j (scene-local pairs).
-__device__ __forceinline__ int pair_floor(int j, int poff) { return j - ((j - poff) & 1); }
-
-template <int CAP>
-__device__ __forceinline__ void plan_pairs(const SceneDev* S, const int32_t* __restrict__ start,
-                                           const int32_t* __restrict__ keys, const Tile& tl, PairPlan<CAP>& sp) {
-  const int lane = threadIdx.x & 31;
-  const CellCoord a = cell_of_key(S, __ldg(keys + tl.begin));
-  const CellCoord b = cell_of_key(S, __ldg(keys + tl.end - 1));
-  const int nx = S->dims[0], ny = S->dims[1], nz = S->dims[2];
-  const int colA = a.x * ny + a.y, colB = b.x * ny + b.y;
-  const int ncols = colB - colA + 1;
-  const int R = S->rz;
-  int len = 0, gb = 0, ge = 0;
-  if (ncols <= kMaxCols && lane < 9 * ncols) {
-    const int g = lane / 9, r = lane % 9;
-    const int col = colA + g;
-    const int cx = col / ny, cy = col - cx * ny;
-    const int zlo = g == 0 ? max(a.z - R, 0) : 0;
-    const int zhi = (g == ncols - 1) ? min(b.z + R, nz - 1) : nz - 1;
-    const int x = cx + r / 3 - 1, y = cy + r % 3 - 1;
-    if (x >= 0 && x < nx && y >= 0 && y < ny) {
-      const int row = S->coff + (x * ny + y) * nz;
-      gb = __ldg(start + row + zlo);
-      ge = __ldg(start + row + zhi + 1);
-      if (ge > gb) len = 2 * (((ge - S->poff + 1) >> 1) - ((gb - S->poff) >> 1));
-    }
-  }
-  int incl = len;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += y;
-  }
-  const int total = __shfl_sync(0xffffffffu, incl, 31);
-  const bool fits = ncols <= kMaxCols && total <= CAP;
-  if (lane < kMaxSegs) {
-    sp.gb[lane] = gb;
-    sp.ge[lane] = ge;
-    sp.seg_off[lane] = incl - len;
-    if (fits)  // this segment's pairs
-      for (int q = (incl - len) >> 1; q < incl >> 1; ++q) sp.pseg[q] = (uint8_t)lane;
-  }
-  if (lane == 0) {
-    sp.seg_off[kMaxSegs] = total;
-    sp.col0 = colA;
-    sp.ncols = fits ? ncols : 0;
-  }
-}
-
-// Global sorted indexes held by staged pair q (-1: padding slot).
-template <int CAP>
-__device__ __forceinline__ int2 pair_source(const PairPlan<CAP>& sp, int q, int poff) {
-  const int s = sp.pseg[q];
-  const int g0 = pair_floor(sp.gb[s], poff) + (2 * q - sp.seg_off[s]);
-  return make_int2((g0 >= sp.gb[s] && g0 < sp.ge[s]) ? g0 : -1, (g0 + 1 >= sp.gb[s] && g0 + 1 < sp.ge[s]) ? g0 + 1 : -1);
-}
-
-template <int P>
-struct RowSum;  // folds per-row partials in the precision mode
-template <>
-struct RowSum<CWA_PREC_FP32> {
-  float s = 0.0f;
-  __device__ __forceinline__ void add(float x) { s += x; }
-  __device__ __forceinline__ float get() const { return s; }
-};
-template <>
-struct RowSum<CWA_PREC_COMPENSATED> : Sum<CWA_PREC_COMPENSATED> {};
-
-// Density pass, packed form: rho (poly6 over r < h, self included), the
-// equation of state, force's gather records, and this step's row masks
-// (nbm[r * n_total + i]; nbr_cnt[i] = rows with a nonzero mask as bits, or
-// -1 when some row's window reaches past bit 63: force then rescans).
-template <int P, int MINB>
-__global__ void __launch_bounds__(kNbThreads, MINB)
-    k_density(const float4* __restrict__ pos, const int32_t* __restrict__ start, const int32_t* __restrict__ keys,
-              const Tile* __restrict__ tiles, const SceneDev* __restrict__ scenes,
-              const float* __restrict__ wave, float2* __restrict__ rho_p, uint64_t* __restrict__ masks,
-              int32_t* __restrict__ rows_out, int32_t n_total, int32_t* status, int32_t allow_stage,
-              const float4* __restrict__ vel, float4* __restrict__ xpair, float4* __restrict__ vpair) {
-  __shared__ __align__(16) float4 s_xy[kDenStageCap / 2];  // (x_a, x_b, y_a, y_b)
-  __shared__ __align__(16) float2 s_z[kDenStageCap / 2];   // (z_a, z_b)
-  __shared__ PairPlan<kDenStageCap> sp;
-  const Tile tl = tiles[blockIdx.x];
-  const SceneDev* S = scenes + tl.scene;
-  if (threadIdx.x < 32) plan_pairs(S, start, keys, tl, sp);
-  __syncthreads();
-  const bool staged = allow_stage && sp.ncols > 0;
-  if (staged) {
-    const int npairs = sp.seg_off[9 * sp.ncols] >> 1;
-    const float4 far4 = make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
-    for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
-      const int2 g = pair_source(sp, q, S->poff);
-      const float4 a = g.x >= 0 ? __ldg(pos + g.x) : far4;
-      const float4 b = g.y >= 0 ? __ldg(pos + g.y) : far4;
-      s_xy[q] = make_float4(a.x, b.x, a.y, b.y);
-      s_z[q] = make_float2(a.z, b.z);
-    }
-  }
-  __syncthreads();
-  const int i = tl.begin + threadIdx.x;
-  if (i >= tl.end) return;
-  const float4 pi = __ldg(pos + i);
-  const float h = S->h;
-  const uint64_t PX = pk2(pi.x, pi.x), PY = pk2(pi.y, pi.y), PZ = pk2(pi.z, pi.z);
-  const uint64_t NH2 = pk2(-(h * h), -(h * h)), ZERO = pk2(0.0f, 0.0f);
-  const float4 far4 = make_float4(kSentinel, kSentinel, kSentinel, 0.0f);
-  const CellCoord c = cell_of_key(S, __ldg(keys + i));
-  const int g = staged ? c.x * S->dims[1] + c.y - sp.col0 : 0;
-  const int zb = max(c.z - S->rz, 0);  // z cell of every row's cell-based start
-  RowSum<P> acc;
-  int rows = 0;
-  bool overflow = false;
-#pragma unroll 1
-  for (int r = 0; r < 9; ++r) {
-    uint64_t m = 0ull;  // the row's hits: bit b = the candidate at the row's cell-based start + b
-    int rb, re;
-    row_range(S, start, pi, c, S->hl2, r, rb, re);
-    if (re > rb) {
-      // scene-local pairs [pb, pe) cover the window; w0 = first sorted index they hold
-      const int pb = (rb - S->poff) >> 1, pe = (re - S->poff + 1) >> 1;
-      const int w0 = S->poff + 2 * pb;
-      uint64_t part = ZERO;  // accumulates -(h^2 - r^2)^3 over the hits
-      uint32_t lo = 0u, hi = 0u, cur = 1u;  // hits of pairs 0-15 / 16-31, two bits a pair
-      int k = 0;
-      auto test = [&](uint64_t xx, uint64_t yy, uint64_t zz) {
-        const uint64_t dx = sub2(PX, xx), dy = sub2(PY, yy), dz = sub2(PZ, zz);
-        uint64_t qq = fma2(dx, dx, NH2);
-        qq = fma2(dy, dy, qq);
-        qq = fma2(dz, dz, qq);
-        const float2 q2 = upk2(qq);
-        const float mx = fminf(q2.x, 0.0f), my = fminf(q2.y, 0.0f);
-        uint32_t two = mx < 0.0f ? cur : 0u;
-        if (my < 0.0f) two |= cur << 1;
-        if (k < 16)
-          lo |= two;
-        else
-          hi |= two;
-        cur = k == 15 ? 1u : cur << 2;
-        ++k;
-        const uint64_t mm = pk2(mx, my);
-        part = fma2(mul2(mm, mm), mm, part);
-      };
-      if (staged) {
-        const int s = g * 9 + r;
-        const int q0 = (sp.seg_off[s] >> 1) + (pb - ((sp.gb[s] - S->poff) >> 1));
-        if (!CWA_DCHECK_FAILED(
-                g >= 0 && g < sp.ncols && q0 >= 0 && q0 + (pe - pb) <= (sp.seg_off[9 * sp.ncols] >> 1), status)) {
-#pragma unroll 4
-          for (int q = q0; q < q0 + (pe - pb); ++q) {
-            uint64_t xx, yy;
-            lds_2x64(&s_xy[q], xx, yy);
-            test(xx, yy, lds_64(&s_z[q]));
-          }
-        }
-      } else {
-        // global loads; the widened slots outside the window read as far away
-        for (int q = pb; q < pe; ++q) {
-          const int j0 = S->poff + 2 * q, j1 = j0 + 1;
-          const float4 a = (j0 >= rb && !CWA_DCHECK_FAILED(j0 < n_total, status)) ? __ldg(pos + j0) : far4;
-          const float4 bb = (j1 < re && !CWA_DCHECK_FAILED(j1 < n_total, status)) ? __ldg(pos + j1) : far4;
-          test(pk2(a.x, bb.x), pk2(a.y, bb.y), pk2(a.z, bb.z));
-        }
-      }
-      const float2 pp = upk2(part);
-      acc.add(-(pp.x + pp.y));
-      // place the window's bits at their offset from the row's cell-based start
-      const int base = __ldg(start + row_id(S, c, r) + zb);
-      const int off = w0 - base;  // >= -1 (the widened slot before the window is never a hit)
-      const uint64_t wb = ((uint64_t)hi << 32) | lo;
-      overflow |= pe - pb > 32 || off + 2 * (pe - pb) > kMaskBits;
-      m = off >= 0 ? (off < kMaskBits ? wb << off : 0ull) : wb >> 1;
-    }
-    masks[(size_t)r * n_total + i] = m;
-    if (m) rows |= 1 << r;
-  }
-  rows_out[i] = overflow ? -1 : rows;
-  const float rho_t = S->c_poly6 * acc.get();
-  const float2 rp = eos(S, rho_t, pi, wave);
-  rho_p[i] = rp;
-  write_pair_rec(xpair, vpair, vel, i, pi, rp);
-}
-
 // Launch-bound variants (min CTAs per SM): the register budget trades
 // occupancy against loads in flight per warp; the autotuner picks one.
 template <int P, int MODE>
-void scan_variant(int minb, const NbArgs& a, uint16_t* list, int32_t* cnt, uint64_t* masks, float4* xref,
+void scan_variant(int minb, const NbArgs& a, uint16_t* list, int32_t* cnt, RowMask* masks, float4* xref,
                   const int32_t* flag, cudaStream_t st) {
 #define CWA_SCAN(MB)                                                                                          \
   k_scan_cands<P, MODE, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.start, a.keys, a.tiles, a.scenes,    \
@@ -1118,21 +820,6 @@ void dispatch_force(const NbArgs& a, cudaStream_t st) {
     force_variant<P, 6>(a, st);
 }
 
-template <int P>
-void dispatch_density(const NbArgs& a, cudaStream_t st) {
-#define CWA_DEN(MB)                                                                                       \
-  k_density<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.start, a.keys, a.tiles, a.scenes, a.wave,  \
-                                                      a.rho_p, a.nbm, a.nbr_cnt, a.n_total, a.status,      \
-                                                      a.stage, a.vel, a.xpair, a.vpair)
-  if (a.scan_minb >= 8)
-    CWA_DEN(8);
-  else if (a.scan_minb >= 6)
-    CWA_DEN(6);
-  else
-    CWA_DEN(4);
-#undef CWA_DEN
-}
-
 }  // namespace
 
 cudaError_t launch_scan_cands(int precision, bool list_mode, const NbArgs& a, cudaStream_t stream) {
@@ -1167,18 +854,6 @@ cudaError_t launch_force(int precision, const NbArgs& a, cudaStream_t stream) {
     case CWA_PREC_FP64: dispatch_force<CWA_PREC_FP64>(a, stream); break;
     default: dispatch_force<CWA_PREC_COMPENSATED>(a, stream);
   }
-  return cudaGetLastError();
-}
-
-}  // namespace cwa
-
-namespace cwa {
-cudaError_t launch_density_packed(int precision, const NbArgs& a, cudaStream_t stream) {
-  if (a.n_tiles <= 0) return cudaSuccess;
-  if (precision == CWA_PREC_FP32)
-    dispatch_density<CWA_PREC_FP32>(a, stream);
-  else
-    dispatch_density<CWA_PREC_COMPENSATED>(a, stream);
   return cudaGetLastError();
 }
 

@@ -117,28 +117,18 @@ typedef struct cwa_sim_options {
   int32_t precision;       /* CWA_PREC_*                                      */
   int32_t use_graph;       /* capture cwa_step into CUDA graphs               */
   int32_t nb_threads;      /* threads per CTA of the neighbour passes; 0=auto */
-  int32_t nb_stage;        /* neighbour passes stage candidate rows in shared
+  int32_t nb_stage;        /* density pass stages candidate rows in shared
                               memory: 0/1 = on (default), -1 = off         */
   float verlet_skin;       /* 0: sort and scan neighbours every step.  > 0:
                               keep the grid and a list of pairs within
                               h (1 + skin) until some particle has moved
                               skin h / 2 (needs cell_size >= h (1 + skin)) */
-  int32_t nb_scan_minb;    /* density-pass kernel variant: min CTAs per SM
+  int32_t nb_scan_minb;    /* density-scan kernel variant: min CTAs per SM
                               (4, 6, 8; 0 = 4)                              */
   int32_t nb_force_minb;   /* force kernel variant (6, 8; 0 = 8)              */
   int32_t wave_block;      /* blocked wave advance variant (CWA_WAVE_BLOCK_*)  */
-  int32_t nb_kernel;       /* density pass in per-step FP32 / compensated
-                              mode: CWA_NB_PACKED (default) or
-                              CWA_NB_SCALAR (FP64 and Verlet mode always
-                              use the scalar scan)                          */
-  int32_t reserved[2];
+  int32_t reserved[3];
 } cwa_sim_options;
-
-/* Density-pass forms.  Both test every candidate of a particle's nine row
- * windows and record its hits as nine 64-bit row masks, which force then
- * evaluates.  PACKED takes the candidates two at a time in packed float
- * pairs from a pair-major shared-memory stage; SCALAR one at a time. */
-enum { CWA_NB_PACKED = 0, CWA_NB_SCALAR = 1 };
 
 /* Blocked wave advance variants: box of 128 x H cells (P: 256 x H) advanced
  * K steps per launch in shared memory; the R and P variants hold each

@@ -129,13 +129,10 @@ def _oracle_state(orc, parts_records):
 @pytest.mark.parametrize("preset", ["reference", "muller"])
 @pytest.mark.parametrize("prec", [PREC_FP32, PREC_COMPENSATED, PREC_FP64])
 @pytest.mark.parametrize("zsub,stage", [(1, 0), (4, 0), (4, -1)])
-@pytest.mark.parametrize("nb", [_abi.NB_PACKED, _abi.NB_SCALAR])
-def test_rho_pres_force_parity(lib, orc, preset, prec, zsub, stage, nb):
-    if prec == PREC_FP64 and nb == _abi.NB_PACKED:
-        pytest.skip("FP64 always runs the scalar density pass")
+def test_rho_pres_force_parity(lib, orc, preset, prec, zsub, stage):
     sc = small_reference() if preset == "reference" else small_muller()
     sc.desc.cell_size_z = sc.desc.cell_size / zsub
-    with Sim(sc.desc, precision=prec, nb_stage=stage, nb_kernel=nb) as sim:
+    with Sim(sc.desc, precision=prec, nb_stage=stage) as sim:
         load_scene(sim, 0, sc)
         u_n, _ = sim.download_wave(0)
         p0 = records_f32(sim.download_particles(0))
@@ -159,7 +156,7 @@ def test_rho_pres_force_parity(lib, orc, preset, prec, zsub, stage, nb):
 @pytest.mark.parametrize("zsub,skin", [(1, 0.0), (2, 0.0), (1, 0.2)])
 def test_dense_rows_take_the_rescan_path(lib, orc, prec, zsub, skin):
     """h = 4 lattice spacings: a candidate row holds ~128 particles, past the
-    64 bits of a row mask, so force rescans those particles' rows (and the
+    32 bits of a row mask, so force rescans those particles' rows (and the
     Verlet density its overflowed lists).  Results still match the oracle."""
     sp = 0.02
     sc = small_muller((14, 14, 14), sp, (32, 32), seed=21, zsub=zsub, skin=skin)
@@ -531,10 +528,11 @@ def test_autotune_keeps_state_and_results(lib):
 
 
 @pytest.mark.parametrize("prec", [PREC_FP32, PREC_COMPENSATED])
-def test_packed_density_invariant_to_staging_tiles_and_batching(lib, prec):
-    """The packed density pass pairs candidates by their index inside the scene,
-    so staging on or off, 64- or 128-particle CTAs and the scene's place in
-    a batch (here behind a scene of odd size) leave every bit unchanged."""
+def test_neighbour_passes_invariant_to_staging_tiles_and_batching(lib, prec):
+    """Every particle's neighbour sums run in an order fixed by the particle
+    alone, so staging on or off, 64- or 128-particle CTAs and the scene's
+    place in a batch (here behind a scene of odd size) leave every bit
+    unchanged."""
     sc = small_muller((14, 15, 13), 0.02, (48, 40), zsub=4, seed=31)
     odd = small_muller((5, 7, 9), 0.03, (32, 32), seed=32)  # 315 particles: the next scene starts at an odd index
     def run(scene_list, k, **kw):
