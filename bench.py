@@ -830,6 +830,73 @@ def run_wave(args) -> None:
     print(json.dumps(out), flush=True)
 
 
+def run_refscene(args) -> None:
+    """`--mode refscene`: the reference app's own scene (20,480 particles on
+    its 64 x 5 x 64 cube, 64^2 wave, the shaders' constants,
+    CoupledWaterAnimation/Main.cpp:28-35, 184-204): updates/s of the GPU step
+    (CUDA events around --steps graph-launched steps after --warmup) beside
+    the reference's own algorithm on the host cores, the O(N^2) all-pairs
+    loops of rho_pres_comp.glsl:60-68 / force_comp.glsl:74-88 in the FP64
+    restatement (bounded sample), and the same restatement on its grid."""
+    import torch
+
+    from coupledwateranimation_gb300 import Sim, scenes
+    sc = scenes.reference()
+    d = sc.desc
+    units = d.n_particles + d.wave_nx * d.wave_nz
+    with Sim(d) as sim:
+        sim.upload_particles(0, sc.particles)
+        sim.wave_reinit(0)
+        stream = torch.cuda.ExternalStream(sim.device_view(0).stream)
+        sim.step(args.warmup)
+        sim.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.step(args.steps)
+        e1.record(stream)
+        sim.synchronize()
+        gpu_ms = e0.elapsed_time(e1) / args.steps
+    out = {"mode": "refscene", "particles": d.n_particles, "wave": f"{d.wave_nx}x{d.wave_nz}",
+           "gpu_ms_per_step": gpu_ms, "gpu_updates_per_s": units / (gpu_ms * 1e-3)}
+    if not args.no_cpu:
+        from oracle import oracle as orc
+        from oracle import workloads
+        orc.set_threads(os.cpu_count() or 1)
+        for brute, key in ((True, "cpu_all_pairs"), (False, "cpu_grid")):
+            r = workloads.reference_preset()
+            p16 = orc.to_f64(r.particles)
+            un = r.wave.astype(np.float64)
+            unm1 = un.copy()
+            orc.step(r.desc, p16, un, unm1, 1, brute=brute)  # untimed
+            n, t0 = 0, time.perf_counter()
+            while n < 2 or time.perf_counter() - t0 < float(os.environ.get("CWA_CPU_SECONDS", "10")):
+                orc.step(r.desc, p16, un, unm1, 1, brute=brute)
+                n += 1
+            sec = (time.perf_counter() - t0) / n
+            out[key] = {"ms_per_step": sec * 1e3, "updates_per_s": units / sec, "steps": n,
+                        "cores": orc.threads(), "kind": "port"}
+        out["gpu_vs_cpu_all_pairs"] = out["cpu_all_pairs"]["ms_per_step"] / gpu_ms
+    print(json.dumps(out), flush=True)
+
+
+def run_wave_profile(args) -> None:
+    """`--mode wave-profile`: a capture target for ncu.  A sim with
+    wave_block = --wave-block on an --wave-n squared field of the reference
+    preset (InitWave splash, no particles) calls wave_advance(8) four times;
+    no timing."""
+    from coupledwateranimation_gb300 import Sim, scenes
+    d = scenes.reference().desc
+    d.n_particles = 0
+    d.wave_nx = d.wave_nz = args.wave_n
+    with Sim(d, use_graph=False, wave_block=args.wave_block) as sim:
+        sim.wave_reinit(0)
+        for _ in range(4):
+            sim.wave_advance(8)
+        sim.synchronize()
+    print(json.dumps({"mode": "wave-profile", "field": f"{args.wave_n}x{args.wave_n}",
+                      "wave_block": args.wave_block, "advances": 4, "steps_each": 8}), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -837,7 +904,9 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="bench",
-                    choices=["bench", "profile", "wave", "batched", "render", "sph2d", "pbd"])
+                    choices=["bench", "profile", "wave", "wave-profile", "refscene", "batched", "render", "sph2d",
+                             "pbd"])
+    ap.add_argument("--wave-block", type=int, default=0, help="--mode wave-profile: CWA_WAVE_BLOCK_* variant")
     ap.add_argument("--boxes", type=int, default=0, help="--mode pbd: number of boxes (default 4096)")
     ap.add_argument("--width", type=int, default=1920, help="image width for --mode render")
     ap.add_argument("--height", type=int, default=1080, help="image height for --mode render")
@@ -867,6 +936,10 @@ def main() -> None:
         run_profile(args)
     elif args.mode == "wave":
         run_wave(args)
+    elif args.mode == "wave-profile":
+        run_wave_profile(args)
+    elif args.mode == "refscene":
+        run_refscene(args)
     elif args.mode == "batched":
         run_batched(args)
     elif args.mode == "render":

@@ -140,14 +140,14 @@ cudaError_t launch_point_rank(const int32_t* key, const int32_t* slot, const int
 // r * n_total + i holding particle i's hits in candidate row r as bits
 // (bit b = the candidate at the row's cell-based start + b).  nbr_cnt holds
 // the rows with a nonzero mask (bit r), or -1 when some row's window reaches
-// past bit 31 (force then rescans the particle's rows).
+// past bit 63 (force then rescans the particle's rows).
 // The Verlet list (pairs within h (1 + skin) at the last rebuild) holds
 // 16-bit codes (row << 12 | offset from the row's cell-based start), entry k
 // of particle i at list[k * n_total + i]; a count of kMaxVerlet + 1 marks an
 // overflowed list, whose reader rescans the particle's rows.
 constexpr int kNbRows = 9;
-constexpr int kMaskBits = 32;
-typedef uint32_t RowMask;  // one candidate row's hits, bit b = the candidate at the row's cell-based start + b
+constexpr int kMaskBits = 64;
+typedef uint64_t RowMask;  // one candidate row's hits, bit b = the candidate at the row's cell-based start + b
 constexpr int kMaxVerlet = 128;
 struct NbArgs {
   const float4* pos;

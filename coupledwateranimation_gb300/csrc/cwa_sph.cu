@@ -23,9 +23,8 @@
 // Either way force runs its pair terms over the step's hits only.
 //
 // A row's cell-based start is start[row + max(cz - rz, 0)], decodable from
-// the particle's sorted cell key alone.  The step's hits are nine 32-bit
-// row masks per particle (bit b = the row's candidate at that start + b;
-// with z cells of h/4 a window ends by bit 24 at the benchmark densities):
+// the particle's sorted cell key alone.  The step's hits are nine 64-bit
+// row masks per particle (bit b = the row's candidate at that start + b):
 // the density pass sets bits in registers, with no per-hit store, and force
 // walks the set bits.  The Verlet list holds 16-bit codes (row << 12 |
 // offset from the same start), so it stays valid while the particles move.
@@ -324,12 +323,12 @@ __device__ __forceinline__ T scan_row(Load load, int len, uint32_t code0, T px, 
 
 // Candidate test of one row for the density pass: the sum of q^3 over the
 // hits and the hits themselves as bits of the row window (bit o = candidate
-// o; candidates 32 and up are tested and summed but get no bit).  The tests
+// o; candidates 64 and up are tested and summed but get no bit).  The tests
 // only set register bits, so no lane stores anything per candidate.
 template <class T, class Load>
 __device__ __forceinline__ T scan_row_bits(Load load, int len, T px, T py, T pz, T hit2, RowMask& bits) {
   T part = (T)0;
-  uint32_t lo = 0u;
+  uint32_t lo = 0u, hi = 0u;
   for (int c0 = 0; c0 < len; c0 += 32) {
     const int n = min(len - c0, 32);
     uint32_t m = 0u, bit = 1u;
@@ -346,9 +345,12 @@ __device__ __forceinline__ T scan_row_bits(Load load, int len, T px, T py, T pz,
       }
       bit <<= 1;
     }
-    if (c0 == 0) lo = m;
+    if (c0 == 0)
+      lo = m;
+    else if (c0 == 32)
+      hi = m;
   }
-  bits = lo;
+  bits = ((RowMask)hi << 32) | lo;
   return part;
 }
 
@@ -667,8 +669,9 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
             const float4* __restrict__ xpair, const float4* __restrict__ vpair, int32_t* status) {
   using T = Real<P>;
   // the particle's nonzero row masks and the index of each mask's bit 0
-  // (9.2 KB a CTA: eight CTAs fit well inside the shared carveout, which
-  // leaves the L1 more room for the gathers)
+  // (13.8 KB a CTA: eight CTAs fit the 132 KB shared carveout, which leaves
+  // the L1 more room for the gathers; 32-bit masks, 9.2 KB a CTA, measured
+  // slower: 209 against 143 us over the C1 run)
   __shared__ RowMask s_w[kNbRows][kNbThreads];
   __shared__ int32_t s_jb[kNbRows][kNbThreads];
   const Tile tl = tiles[blockIdx.x];
@@ -725,7 +728,7 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
         s_jb[nw][threadIdx.x] = base[r];
         ++nw;
       }
-      left += __popc(m);
+      left += __popcll(m);
     }
     int wi = 0;
     RowMask cw = nw > 0 ? s_w[0][threadIdx.x] : 0u;
@@ -741,7 +744,7 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
             cw = s_w[wi][threadIdx.x];
             jb = s_jb[wi][threadIdx.x];
           }
-          js[u] = jb + __ffs(cw) - 1;
+          js[u] = jb + __ffsll((long long)cw) - 1;
           cw &= cw - 1u;
         }
       }

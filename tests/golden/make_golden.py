@@ -101,8 +101,13 @@ def make_oracle_regression() -> None:
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
-    if ref.exists():
+    # usage: make_golden.py [REFERENCE_CHECKOUT]
+    # With the reference's source tree given, the scan KAT and the init
+    # textures are read from it; the oracle regression needs no reference.
+    if len(sys.argv) > 1:
+        ref = Path(sys.argv[1])
+        if not ref.is_dir():
+            sys.exit(f"not a directory: {ref}")
         make_kat(ref)
         make_init_textures(ref)
     make_oracle_regression()

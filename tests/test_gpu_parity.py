@@ -156,7 +156,7 @@ def test_rho_pres_force_parity(lib, orc, preset, prec, zsub, stage):
 @pytest.mark.parametrize("zsub,skin", [(1, 0.0), (2, 0.0), (1, 0.2)])
 def test_dense_rows_take_the_rescan_path(lib, orc, prec, zsub, skin):
     """h = 4 lattice spacings: a candidate row holds ~128 particles, past the
-    32 bits of a row mask, so force rescans those particles' rows (and the
+    64 bits of a row mask, so force rescans those particles' rows (and the
     Verlet density its overflowed lists).  Results still match the oracle."""
     sp = 0.02
     sc = small_muller((14, 14, 14), sp, (32, 32), seed=21, zsub=zsub, skin=skin)
