@@ -392,8 +392,7 @@ def run_gpu(args) -> None:
     wl = scenes.with_zsub(scenes.CONFIGS[args.config](), args.zsub)
     last_step = max(wl.steps, args.warmup + args.steps)
     timed_steps = _timed_steps(args.warmup, args.steps, last_step)
-    sim = Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local,
-              nb_force_minb=args.nb_force_minb)
+    sim = Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local)
     for k, s in enumerate(wl.scenes):
         sim.upload_particles(k, s.particles)
         sim.upload_wave(k, s.wave, s.wave)
@@ -616,8 +615,7 @@ def run_profile(args) -> None:
     hash, scan, list insert, reorder, rho_pres, force, integrate, wave)."""
     from coupledwateranimation_gb300 import Sim, scenes
     wl = scenes.with_zsub(scenes.CONFIGS[args.config](), args.zsub)
-    with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=False,
-             nb_force_minb=args.nb_force_minb) as sim:
+    with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=False) as sim:
         for k, s in enumerate(wl.scenes):
             sim.upload_particles(k, s.particles)
             sim.upload_wave(k, s.wave, s.wave)
@@ -924,8 +922,6 @@ def main() -> None:
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--zsub", type=int, default=4, help="z sub-cells per h of the sort grid")
-    ap.add_argument("--nb-force-minb", type=int, default=0,
-                    help="force kernel variant (cwa_sim_options.nb_force_minb; 0 = library default)")
     ap.add_argument("--dry-run", action="store_true", help="rank plumbing only, on CPU (tests the launcher)")
     args = ap.parse_args()
     if args.warmup < 3:

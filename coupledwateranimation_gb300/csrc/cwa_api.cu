@@ -1335,7 +1335,7 @@ cwa_status cwa_autotune(cwa_sim* s, int32_t trial_steps, cwa_tune_report* out) {
   cudaError_t err = copy_state(true);
   if (err == cudaSuccess) err = cudaEventCreate(&e0);
   if (err == cudaSuccess) err = cudaEventCreate(&e1);
-  const int stages[2] = {0, -1}, scans[3] = {4, 6, 8}, forces[2] = {4, 8}, ctas[2] = {128, 64};
+  const int stages[2] = {0, -1}, scans[3] = {4, 6, 8}, forces[2] = {6, 8}, ctas[2] = {128, 64};
   constexpr int kCombos = 2 * 3 * 2 * 2;
   // Two rounds, the second in reverse order; each combination keeps its
   // faster round, which damps clock and neighbour-load noise.

@@ -186,15 +186,6 @@ __device__ __forceinline__ float4 lds128(const float4* p) {
   return v;
 }
 
-// 16-byte global -> shared copy that completes asynchronously (cp.async,
-// cached in L1 as well); commit / wait act on this thread's copies.
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -668,13 +659,7 @@ struct Acc3 {
 // records in shared memory, as the candidate scan does, measured slower
 // here: 48 KB of stage per CTA halves the resident warps this latency-bound
 // loop needs.
-// PIPE (FP32 modes): the gathers of each group of hits go through a
-// per-thread ring in shared memory filled by cp.async, two half-groups of 4
-// hits in flight, so the loads of the next hits overlap the arithmetic of
-// the current ones without holding registers; the hits, their order and
-// every rounding are the same as without it.
-constexpr int kPipeHits = 4;  // hits a ring stage holds
-template <int P, int MINB, bool PIPE = false>
+template <int P, int MINB>
 __global__ void __launch_bounds__(kNbThreads, MINB)
     k_force(const float4* __restrict__ pos, const float4* __restrict__ vel,
             const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
@@ -689,9 +674,6 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   // slower: 209 against 143 us over the C1 run)
   __shared__ RowMask s_w[kNbRows][kNbThreads];
   __shared__ int32_t s_jb[kNbRows][kNbThreads];
-  // ring[stage][hit][record][thread]: each warp's lanes write and read 32
-  // consecutive 16-byte slots (32 KB a CTA)
-  __shared__ __align__(16) float4 s_ring[PIPE ? 2 * kPipeHits * 2 * kNbThreads : 1];
   const Tile tl = tiles[blockIdx.x];
   const SceneDev* S = scenes + tl.scene;
   const int i = tl.begin + threadIdx.x;
@@ -751,56 +733,6 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
     int wi = 0;
     RowMask cw = nw > 0 ? s_w[0][threadIdx.x] : 0u;
     int jb = nw > 0 ? s_jb[0][threadIdx.x] : 0;
-    // index of the next hit in row then bit order (-1 once all are taken)
-    auto next_hit = [&](int k) {
-      if (k >= left) return -1;
-      if (cw == 0u) {  // the next mask (every compacted mask holds a hit)
-        ++wi;
-        cw = s_w[wi][threadIdx.x];
-        jb = s_jb[wi][threadIdx.x];
-      }
-      const int j = jb + __ffsll((long long)cw) - 1;
-      cw &= cw - 1u;
-      return j;
-    };
-    if constexpr (PIPE && P != CWA_PREC_FP64) {
-      int js[2][kPipeHits];
-      auto issue = [&](int stage, int k0) {
-#pragma unroll
-        for (int u = 0; u < kPipeHits; ++u) {
-          int j = next_hit(k0 + u);
-          if (j >= 0 && CWA_DCHECK_FAILED(j < n_total, status)) j = -1;
-          js[stage][u] = j;
-          if (j >= 0) {
-            float4* slot = &s_ring[((stage * kPipeHits + u) * 2) * kNbThreads + threadIdx.x];
-            cp_async16(slot, xpair + j);
-            cp_async16(slot + kNbThreads, vpair + j);
-          }
-        }
-        cp_async_commit();
-      };
-      auto consume = [&](int stage) {
-        cp_async_wait1();  // this thread's copies of the older stage have landed
-#pragma unroll
-        for (int u = 0; u < kPipeHits; ++u)
-          if (js[stage][u] >= 0) {
-            const float4* slot = &s_ring[((stage * kPipeHits + u) * 2) * kNbThreads + threadIdx.x];
-            const float4 xj = slot[0], vj = slot[kNbThreads];
-            pair(xj, vj, (T)vj.w, (T)xj.w);
-          }
-      };
-      issue(0, 0);
-      issue(1, kPipeHits);
-      for (int k0 = 0; k0 < left; k0 += 2 * kPipeHits) {  // a group of 8 hits, two stages
-        consume(0);
-        issue(0, k0 + 2 * kPipeHits);
-        consume(1);
-        fp.flush();  // per group of 8, as the gathering form folds them
-        fv.flush();
-        issue(1, k0 + 3 * kPipeHits);
-      }
-      cp_async_wait0();
-    } else
     for (int k0 = 0; k0 < left; k0 += 8) {
       int js[8];
 #pragma unroll
@@ -885,15 +817,10 @@ void force_variant(const NbArgs& a, cudaStream_t st) {
 
 template <int P>
 void dispatch_force(const NbArgs& a, cudaStream_t st) {
-  if (a.force_minb >= 8) {
+  if (a.force_minb >= 8)
     force_variant<P, 8>(a, st);
-  } else if (a.force_minb >= 6 || P == CWA_PREC_FP64) {
+  else
     force_variant<P, 6>(a, st);
-  } else {
-    k_force<P, 4, true><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles,
-                                                          a.scenes, a.wave, a.force, a.nbm, a.nbr_cnt, a.n_total,
-                                                          a.xpair, a.vpair, a.status);
-  }
 }
 
 }  // namespace

@@ -125,10 +125,7 @@ typedef struct cwa_sim_options {
                               skin h / 2 (needs cell_size >= h (1 + skin)) */
   int32_t nb_scan_minb;    /* density-scan kernel variant: min CTAs per SM
                               (4, 6, 8; 0 = 4)                              */
-  int32_t nb_force_minb;   /* force kernel variant: 8 or 6 CTAs a SM gathering
-                              from global memory (0 = 8); 4 = FP32 modes
-                              gather through a shared-memory ring filled by
-                              cp.async, 4 CTAs a SM (same results)         */
+  int32_t nb_force_minb;   /* force kernel variant (6, 8; 0 = 8)              */
   int32_t wave_block;      /* blocked wave advance variant (CWA_WAVE_BLOCK_*)  */
   int32_t reserved[3];
 } cwa_sim_options;
