@@ -308,7 +308,9 @@ def orc_grid_cells(desc, zsub: int) -> int:
 def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0, config: int = 3,
                      steps: int | None = None) -> dict:
     """A batched workload (256 small scenes, or 64 large ones) stepped as one
-    batched sim (one launch per pass over all scenes, CUDA graph) and as
+    batched sim (one launch per pass over all scenes, CUDA graph; the
+    neighbour passes once with one CTA a tile and once as persistent CTAs fed
+    by the work queue, the faster form reported) and as
     single-scene sims run one at a time (each its own graph), both over the
     workload's stated step count unless `steps` is given.  Device time: CUDA
     events on each sim's stream around its steps (summed over the plain
@@ -335,19 +337,24 @@ def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0, co
         e1.record(stream)
         return e0, e1
 
-    with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local) as sim:
-        for k, s in enumerate(wl.scenes):
-            sim.upload_particles(k, s.particles)
-            sim.upload_wave(k, s.wave, s.wave)
-        if not args.no_tune:
-            sim.autotune(trial_steps=2)
-        sim.step(3)
-        sim.synchronize()
-        w0 = time.perf_counter()
-        e0, e1 = timed(sim, steps)
-        sim.synchronize()
-        wall_b = time.perf_counter() - w0
-        t_batched = shard.max_over_ranks(e0.elapsed_time(e1) * 1e-3, dev)
+    t_forms, wall_forms = {}, {}
+    for form, queue in (("tile_list", 0), ("work_queue", 1)):
+        with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=True, device=local,
+                 nb_queue=queue) as sim:
+            for k, s in enumerate(wl.scenes):
+                sim.upload_particles(k, s.particles)
+                sim.upload_wave(k, s.wave, s.wave)
+            if not args.no_tune:
+                sim.autotune(trial_steps=2)
+            sim.step(3)
+            sim.synchronize()
+            w0 = time.perf_counter()
+            e0, e1 = timed(sim, steps)
+            sim.synchronize()
+            wall_forms[form] = time.perf_counter() - w0
+            t_forms[form] = shard.max_over_ranks(e0.elapsed_time(e1) * 1e-3, dev)
+    best = min(t_forms, key=t_forms.get)
+    t_batched, wall_b = t_forms[best], wall_forms[best]
     plain, evs = [], []
     try:
         for s in wl.scenes:
@@ -374,6 +381,8 @@ def batched_vs_plain(args, torch, ws: int = 1, rank: int = 0, local: int = 0, co
             "speedup": t_plain / t_batched,
             "batched_algorithmic_gbs": alg_bytes * steps / t_batched / 1e9,
             "batched_ms_per_step": t_batched / steps * 1e3, "plain_ms_per_step": t_plain / steps * 1e3,
+            "batched_form": best,
+            "batched_ms_per_step_by_form": {f: t / steps * 1e3 for f, t in t_forms.items()},
             "host_wall_ms_per_step": {"batched": wall_b / steps * 1e3, "plain": wall_p / steps * 1e3}}
 
 

@@ -65,7 +65,7 @@ class SimOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("use_graph", C.c_int32),
                 ("nb_threads", C.c_int32), ("nb_stage", C.c_int32), ("verlet_skin", C.c_float),
                 ("nb_scan_minb", C.c_int32), ("nb_force_minb", C.c_int32), ("wave_block", C.c_int32),
-                ("reserved", C.c_int32 * 3)]
+                ("nb_queue", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 # CWA_WAVE_BLOCK_*: box rows x steps per launch; R = box column in registers,

@@ -83,6 +83,9 @@ struct cwa_sim {
   int32_t wb_off[kWaveVariants + 1] = {};
   // work tiles
   Tile* d_ptiles = nullptr;
+  int32_t* d_porder = nullptr;  // work-queue order of the particle tiles (capacity porder_cap)
+  size_t porder_cap = 0;
+  int32_t* d_queue = nullptr;   // work-queue counters: density, force
   int32_t n_ptiles = 0, ptile = 128;
   Tile* d_wtiles = nullptr;
   int32_t n_wtiles = 0, wtile = 1024;
@@ -291,8 +294,32 @@ std::vector<Tile> particle_tiles(const cwa_sim* s, int32_t size) {
   return t;
 }
 
+// Work-queue order of the tiles: the scenes from the most particles to the
+// fewest (the longest work first, so the short scenes fill the tail), each
+// scene's tiles in sorted order.
+std::vector<int32_t> tile_order(const cwa_sim* s, const std::vector<Tile>& t) {
+  std::vector<int32_t> scene_rank(s->sd.size());
+  for (size_t i = 0; i < scene_rank.size(); ++i) scene_rank[i] = (int32_t)i;
+  std::stable_sort(scene_rank.begin(), scene_rank.end(),
+                   [&](int32_t a, int32_t b) { return s->sd[a].n > s->sd[b].n; });
+  std::vector<int32_t> pos_of(s->sd.size());
+  for (size_t k = 0; k < scene_rank.size(); ++k) pos_of[scene_rank[k]] = (int32_t)k;
+  std::vector<int32_t> o(t.size());
+  for (size_t k = 0; k < o.size(); ++k) o[k] = (int32_t)k;
+  std::stable_sort(o.begin(), o.end(), [&](int32_t a, int32_t b) { return pos_of[t[a].scene] < pos_of[t[b].scene]; });
+  return o;
+}
+
+cwa_status upload_tile_order(cwa_sim* s, const std::vector<Tile>& t) {
+  const std::vector<int32_t> o = tile_order(s, t);
+  if (o.size() > s->porder_cap) return arg_error("tile order above its capacity");
+  if (!o.empty()) CWA_CUDA(cudaMemcpy(s->d_porder, o.data(), o.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  return CWA_OK;
+}
+
 cwa_status set_particle_tiles(cwa_sim* s, int32_t size) {
   std::vector<Tile> t = particle_tiles(s, size);
+  CWA_TRY(upload_tile_order(s, t));
   Tile* d = nullptr;
   CWA_CUDA(cudaMalloc((void**)&d, std::max<size_t>(t.size(), 1) * sizeof(Tile)));
   if (!t.empty()) {
@@ -348,6 +375,8 @@ NbArgs nb_args(cwa_sim* s) {
   a.stage = s->opt.nb_stage >= 0 ? 1 : 0;
   a.scan_minb = s->opt.nb_scan_minb ? s->opt.nb_scan_minb : 4;
   a.force_minb = s->opt.nb_force_minb ? s->opt.nb_force_minb : 8;
+  a.order = s->d_porder;
+  a.queue = s->opt.nb_queue ? s->d_queue : nullptr;
   return a;
 }
 
@@ -709,6 +738,7 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   if (o.nb_threads != 0 && (o.nb_threads < 32 || o.nb_threads > 128 || (o.nb_threads & 31)))
     return arg_error("nb_threads must be 0 or a multiple of 32 in [32, 128]");
   if (o.wave_block < 0 || o.wave_block >= CWA_WAVE_BLOCK_COUNT) return arg_error("unknown wave_block variant");
+  if (o.nb_queue != 0 && o.nb_queue != 1) return arg_error("nb_queue must be 0 or 1");
   std::vector<int32_t> dims(3 * (size_t)n_scenes);
   int64_t np = 0, nc = 0, nw = 0;
   int32_t nmax = 0;
@@ -819,6 +849,10 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   ALLOC(s->D, (size_t)s->w_total);
   ALLOC(s->d_scenes, s->sd.size());
   ALLOC(s->d_ptiles, ptiles.size());
+  // tiles of 32 or more particles: at most N / 32 + one partial tile a scene
+  s->porder_cap = N / 32 + s->sd.size() + 1;
+  ALLOC(s->d_porder, s->porder_cap);
+  ALLOC(s->d_queue, 2);
   ALLOC(s->d_wtiles, wtiles.size());
   ALLOC(s->staging, (size_t)s->n_max);
   ALLOC(s->d_status, 1);
@@ -843,6 +877,7 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
                 cudaSuccess &&
             (ptiles.empty() || cudaMemcpy(s->d_ptiles, ptiles.data(), ptiles.size() * sizeof(Tile),
                                           cudaMemcpyHostToDevice) == cudaSuccess) &&
+            upload_tile_order(s, ptiles) == CWA_OK &&
             cudaMemcpy(s->d_wtiles, wtiles.data(), wtiles.size() * sizeof(Tile), cudaMemcpyHostToDevice) ==
                 cudaSuccess &&
             (N == 0 || (cudaMemcpy(s->ID[0], ids.data(), N * sizeof(int32_t), cudaMemcpyHostToDevice) ==

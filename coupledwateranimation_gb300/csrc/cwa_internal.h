@@ -175,6 +175,11 @@ struct NbArgs {
   int32_t stage;        // candidate scan may stage rows in shared memory
   int32_t scan_minb;    // launch-bound variant of the candidate scan (4, 6, 8)
   int32_t force_minb;   // launch-bound variant of force (6, 8, 10)
+  // Work-queue form of the per-step density pass and of force (null: one
+  // CTA a tile): resident CTAs take numbers t from queue[0] (density) or
+  // queue[1] (force), zeroed before each launch, and run tiles[order[t]].
+  const int32_t* order;
+  int32_t* queue;
 };
 // Candidate scan: the per-step density + row masks, or (list_mode) the
 // Verlet list, run only when *flag is set.

@@ -38,6 +38,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "cwa_device.cuh"
@@ -215,10 +216,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait on phase 0 of the staging barrier.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar) {
+// Bounded wait on one phase of the staging barrier (phase parity 0 for a
+// CTA's first stage, alternating in the work-queue form).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity = 0) {
   for (int k = 0; k < (1 << 20); ++k)
-    if (mbar_try_wait(bar, 0)) return true;
+    if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
 
@@ -360,49 +362,58 @@ __device__ __forceinline__ T scan_row_bits(Load load, int len, T px, T py, T pz,
 constexpr int MODE_DENSITY = 0;
 constexpr int MODE_LIST = 1;
 
-template <int P, int MODE, int MINB>
-__global__ void __launch_bounds__(kNbThreads, MINB)
-    k_scan_cands(const float4* __restrict__ pos, const int32_t* __restrict__ start,
-                 const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
-                 const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
-                 float2* __restrict__ rho_p, uint16_t* __restrict__ list, int32_t* __restrict__ list_cnt,
-                 RowMask* __restrict__ masks, float4* __restrict__ xref, int32_t n_total, int32_t* status,
-                 const int32_t* __restrict__ flag,
-                 int32_t allow_stage, const float4* __restrict__ vel, float4* __restrict__ xpair,
-                 float4* __restrict__ vpair) {
+// Shared memory of the candidate scan.
+template <int MODE>
+struct ScanShared {
+  static constexpr bool kCanStage = MODE == MODE_DENSITY;
+  __align__(128) float4 cand[kCanStage ? kStageCap : 1];
+  // the Verlet list build stages its codes (+ the overflow slot); the
+  // density pass keeps its hits in registers
+  uint16_t hit[MODE == MODE_LIST ? kMaxVerlet + 1 : 1][kNbThreads];
+  StagePlan sp;
+  __align__(8) uint64_t bar;
+};
+
+// One tile of the candidate scan.  Stages the tile's rows (bulk copies that
+// complete phase `parity` of the CTA's barrier) and scans them.  Returns 1
+// when the tile was staged (a barrier phase was used), plus 2 when the
+// staging wait timed out (then nothing was computed).  Contains CTA-wide
+// barriers: every thread of the CTA calls it.
+template <int P, int MODE>
+__device__ __forceinline__ int scan_tile(
+    ScanShared<MODE>& sh, const Tile tl, uint32_t parity, const float4* __restrict__ pos,
+    const int32_t* __restrict__ start, const int32_t* __restrict__ keys, const SceneDev* __restrict__ scenes,
+    const float* __restrict__ wave, float2* __restrict__ rho_p, uint16_t* __restrict__ list,
+    int32_t* __restrict__ list_cnt, RowMask* __restrict__ masks, float4* __restrict__ xref, int32_t n_total,
+    int32_t* status, int32_t allow_stage, const float4* __restrict__ vel, float4* __restrict__ xpair,
+    float4* __restrict__ vpair) {
   using T = Real<P>;
   constexpr int kCap = kMaxVerlet;  // the Verlet list build's codes per particle
   // The list build (rare: Verlet rebuilds only) reads candidates from global
   // memory, which keeps its static shared memory under 48 KB.
-  constexpr bool kCanStage = MODE == MODE_DENSITY;
-  __shared__ __align__(128) float4 s_cand[kCanStage ? kStageCap : 1];
-  // the Verlet list build stages its codes (+ the overflow slot); the
-  // density pass keeps its hits in registers
-  __shared__ uint16_t s_hit[MODE == MODE_LIST ? kCap + 1 : 1][kNbThreads];
-  __shared__ StagePlan sp;
-  __shared__ __align__(8) uint64_t s_bar;
-  if (MODE == MODE_LIST && flag && __ldg(flag) == 0) return;  // no rebuild this step
-  const Tile tl = tiles[blockIdx.x];
+  constexpr bool kCanStage = ScanShared<MODE>::kCanStage;
+  float4* const s_cand = sh.cand;
+  StagePlan& sp = sh.sp;
   const SceneDev* S = scenes + tl.scene;
   if (threadIdx.x < 32) plan_stage(S, start, keys, tl, sp);
-  if (threadIdx.x == 0) mbar_init(&s_bar, 1);
   __syncthreads();
   const bool staged = kCanStage && allow_stage && sp.ncols > 0;
   if (staged && threadIdx.x == 0) {
-    mbar_expect_tx(&s_bar, (uint32_t)sp.seg_off[kMaxSegs] * 16u);
+    mbar_expect_tx(&sh.bar, (uint32_t)sp.seg_off[kMaxSegs] * 16u);
     for (int s = 0; s < 9 * sp.ncols; ++s) {
       const int len = sp.seg_off[s + 1] - sp.seg_off[s];
-      if (len > 0) bulk_g2s(&s_cand[sp.seg_off[s]], pos + sp.seg_b[s], (uint32_t)len * 16u, &s_bar);
+      if (len > 0) bulk_g2s(&s_cand[sp.seg_off[s]], pos + sp.seg_b[s], (uint32_t)len * 16u, &sh.bar);
     }
   }
   bool ready = true;
-  if (staged && !mbar_wait_bounded(&s_bar)) {
+  if (staged && !mbar_wait_bounded(&sh.bar, parity)) {
     ready = false;
     if (threadIdx.x == 0) atomicOr(status, kStatusTimeout);
-    mbar_wait_bounded(&s_bar);  // let copies in flight land before the CTA exits
+    mbar_wait_bounded(&sh.bar, parity);  // let copies in flight land before the CTA moves on
   }
+  const int used = (staged ? 1 : 0) | (ready ? 0 : 2);
   const int i = tl.begin + threadIdx.x;
-  if (i >= tl.end || !ready) return;
+  if (i >= tl.end || !ready) return used;
 
   const float4 pi = __ldg(pos + i);
   const T hh = (T)S->h;
@@ -413,7 +424,7 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   row_ranges(S, start, pi, c, S->hl2, b, e);
   row_bases(S, start, c, base);
   const int g = staged ? c.x * S->dims[1] + c.y - sp.col0 : 0;
-  uint16_t* const hit_col = &s_hit[0][threadIdx.x];
+  uint16_t* const hit_col = &sh.hit[0][threadIdx.x];
   uint16_t* const hp_end = hit_col + kCap * kNbThreads;  // the overflow slot (list build)
   uint16_t* hp = hit_col;
   Sum<P> acc;
@@ -475,6 +486,45 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
     const float2 rp = eos(S, (float)rho_t, pi, wave);
     rho_p[i] = rp;
     write_pair_rec(xpair, vpair, vel, i, pi, rp);
+  }
+  return used;
+}
+
+// The candidate scan over the tile list, one CTA a tile; or (queue set,
+// density mode only) as the work-queue form: resident CTAs take tile
+// numbers from the counter *queue and scan tiles[order[t]] until the
+// n_tiles of the launch are taken.
+template <int P, int MODE, int MINB, bool WQ>
+__global__ void __launch_bounds__(kNbThreads, MINB)
+    k_scan_cands(const float4* __restrict__ pos, const int32_t* __restrict__ start,
+                 const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
+                 const SceneDev* __restrict__ scenes, const float* __restrict__ wave,
+                 float2* __restrict__ rho_p, uint16_t* __restrict__ list, int32_t* __restrict__ list_cnt,
+                 RowMask* __restrict__ masks, float4* __restrict__ xref, int32_t n_total, int32_t* status,
+                 const int32_t* __restrict__ flag,
+                 int32_t allow_stage, const float4* __restrict__ vel, float4* __restrict__ xpair,
+                 float4* __restrict__ vpair, const int32_t* __restrict__ order, int32_t* queue, int32_t n_tiles) {
+  __shared__ ScanShared<MODE> sh;
+  __shared__ int32_t s_next;
+  if (MODE == MODE_LIST && flag && __ldg(flag) == 0) return;  // no rebuild this step
+  if (threadIdx.x == 0) mbar_init(&sh.bar, 1);
+  if constexpr (!WQ || MODE != MODE_DENSITY) {
+    scan_tile<P, MODE>(sh, tiles[blockIdx.x], 0u, pos, start, keys, scenes, wave, rho_p, list, list_cnt, masks,
+                       xref, n_total, status, allow_stage, vel, xpair, vpair);
+    return;
+  }
+  uint32_t parity = 0u;
+  for (;;) {
+    if (threadIdx.x == 0) s_next = atomicAdd(queue, 1);
+    __syncthreads();  // also: every thread is done with the previous tile's stage and plan
+    const int t = s_next;
+    __syncthreads();  // s_next read by all before thread 0 may take the next number
+    if (t >= n_tiles) break;
+    const int used = scan_tile<P, MODE>(sh, tiles[__ldg(order + t)], parity, pos, start, keys, scenes, wave, rho_p,
+                                        list, list_cnt, masks, xref, n_total, status, allow_stage, vel, xpair,
+                                        vpair);
+    if (__syncthreads_or(used & 2)) break;  // a staging wait timed out (status set): stop taking tiles
+    if (used & 1) parity ^= 1u;
   }
 }
 
@@ -659,22 +709,15 @@ struct Acc3 {
 // records in shared memory, as the candidate scan does, measured slower
 // here: 48 KB of stage per CTA halves the resident warps this latency-bound
 // loop needs.
-template <int P, int MINB>
-__global__ void __launch_bounds__(kNbThreads, MINB)
-    k_force(const float4* __restrict__ pos, const float4* __restrict__ vel,
-            const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
-            const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
-            const SceneDev* __restrict__ scenes, const float* __restrict__ wave, float4* __restrict__ force,
-            const RowMask* __restrict__ nbm, const int32_t* __restrict__ nbr_cnt, int32_t n_total,
-            const float4* __restrict__ xpair, const float4* __restrict__ vpair, int32_t* status) {
+template <int P>
+__device__ __forceinline__ void force_tile(
+    RowMask (&s_w)[kNbRows][kNbThreads], int32_t (&s_jb)[kNbRows][kNbThreads], const Tile tl,
+    const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ rho_p,
+    const int32_t* __restrict__ start, const int32_t* __restrict__ keys, const SceneDev* __restrict__ scenes,
+    const float* __restrict__ wave, float4* __restrict__ force, const RowMask* __restrict__ nbm,
+    const int32_t* __restrict__ nbr_cnt, int32_t n_total, const float4* __restrict__ xpair,
+    const float4* __restrict__ vpair, int32_t* status) {
   using T = Real<P>;
-  // the particle's nonzero row masks and the index of each mask's bit 0
-  // (13.8 KB a CTA: eight CTAs fit the 132 KB shared carveout, which leaves
-  // the L1 more room for the gathers; 32-bit masks, 9.2 KB a CTA, measured
-  // slower: 209 against 143 us over the C1 run)
-  __shared__ RowMask s_w[kNbRows][kNbThreads];
-  __shared__ int32_t s_jb[kNbRows][kNbThreads];
-  const Tile tl = tiles[blockIdx.x];
   const SceneDev* S = scenes + tl.scene;
   const int i = tl.begin + threadIdx.x;
   if (i >= tl.end) return;
@@ -781,38 +824,101 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   force[i] = force_out(S, i, pi, vi, rpi.x, fpr, fvr, force, wave);
 }
 
+// The force pass over the tile list, one CTA a tile, or (queue set) in the
+// work-queue form.
+template <int P, int MINB, bool WQ>
+__global__ void __launch_bounds__(kNbThreads, MINB)
+    k_force(const float4* __restrict__ pos, const float4* __restrict__ vel,
+            const float2* __restrict__ rho_p, const int32_t* __restrict__ start,
+            const int32_t* __restrict__ keys, const Tile* __restrict__ tiles,
+            const SceneDev* __restrict__ scenes, const float* __restrict__ wave, float4* __restrict__ force,
+            const RowMask* __restrict__ nbm, const int32_t* __restrict__ nbr_cnt, int32_t n_total,
+            const float4* __restrict__ xpair, const float4* __restrict__ vpair, int32_t* status,
+            const int32_t* __restrict__ order, int32_t* queue, int32_t n_tiles) {
+  // the particle's nonzero row masks and the index of each mask's bit 0
+  // (13.8 KB a CTA: eight CTAs fit the 132 KB shared carveout, which leaves
+  // the L1 more room for the gathers; 32-bit masks, 9.2 KB a CTA, measured
+  // slower: 209 against 143 us over the C1 run)
+  __shared__ RowMask s_w[kNbRows][kNbThreads];
+  __shared__ int32_t s_jb[kNbRows][kNbThreads];
+  if constexpr (!WQ) {
+    force_tile<P>(s_w, s_jb, tiles[blockIdx.x], pos, vel, rho_p, start, keys, scenes, wave, force, nbm, nbr_cnt,
+                  n_total, xpair, vpair, status);
+    return;
+  }
+  // work-queue form: resident CTAs take tile numbers from *queue
+  __shared__ int32_t s_next[2];
+  for (int it = 0;; ++it) {
+    if (threadIdx.x == 0) s_next[it & 1] = atomicAdd(queue, 1);
+    __syncthreads();  // (two slots: thread 0 refills one while the other is still being read)
+    const int t = s_next[it & 1];
+    if (t >= n_tiles) break;
+    force_tile<P>(s_w, s_jb, tiles[__ldg(order + t)], pos, vel, rho_p, start, keys, scenes, wave, force, nbm,
+                  nbr_cnt, n_total, xpair, vpair, status);
+  }
+}
+
+// Grid of a work-queue launch: the CTAs of `kernel` that fit the device at
+// once (occupancy x SMs), at most n_tiles.
+template <typename K>
+int queue_grid(K kernel, int block, int n_tiles) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm < 1)
+    return n_tiles;
+  return std::min(n_tiles, per_sm * sms);
+}
+
 // Launch-bound variants (min CTAs per SM): the register budget trades
 // occupancy against loads in flight per warp; the autotuner picks one.
+// queue (density mode): the work-queue form, its counter zeroed first.
+template <int P, int MODE, int MB>
+void scan_launch_one(const NbArgs& a, uint16_t* list, int32_t* cnt, RowMask* masks, float4* xref,
+                     const int32_t* flag, int32_t* queue, cudaStream_t st) {
+  auto kern = queue ? k_scan_cands<P, MODE, MB, true> : k_scan_cands<P, MODE, MB, false>;
+  int grid = a.n_tiles;
+  if (queue) {
+    cudaMemsetAsync(queue, 0, sizeof(int32_t), st);
+    grid = queue_grid(kern, a.tile_size, a.n_tiles);
+  }
+  kern<<<grid, a.tile_size, 0, st>>>(a.pos, a.start, a.keys, a.tiles, a.scenes, a.wave, a.rho_p, list, cnt, masks,
+                                     xref, a.n_total, a.status, flag, a.stage, a.vel, a.xpair, a.vpair, a.order,
+                                     queue, a.n_tiles);
+}
+
 template <int P, int MODE>
 void scan_variant(int minb, const NbArgs& a, uint16_t* list, int32_t* cnt, RowMask* masks, float4* xref,
-                  const int32_t* flag, cudaStream_t st) {
-#define CWA_SCAN(MB)                                                                                          \
-  k_scan_cands<P, MODE, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.start, a.keys, a.tiles, a.scenes,    \
-                                                               a.wave, a.rho_p, list, cnt, masks, xref,       \
-                                                               a.n_total, a.status, flag, a.stage, a.vel,     \
-                                                               a.xpair, a.vpair)
+                  const int32_t* flag, int32_t* queue, cudaStream_t st) {
   if (minb >= 8)
-    CWA_SCAN(8);
+    scan_launch_one<P, MODE, 8>(a, list, cnt, masks, xref, flag, queue, st);
   else if (minb >= 6)
-    CWA_SCAN(6);
+    scan_launch_one<P, MODE, 6>(a, list, cnt, masks, xref, flag, queue, st);
   else
-    CWA_SCAN(4);
-#undef CWA_SCAN
+    scan_launch_one<P, MODE, 4>(a, list, cnt, masks, xref, flag, queue, st);
 }
 
 template <int P>
 void dispatch_scan(bool list_mode, const NbArgs& a, cudaStream_t st) {
   if (list_mode)
-    scan_variant<P, MODE_LIST>(a.scan_minb, a, a.vlist, a.vcnt, nullptr, a.xref, a.flag, st);
+    scan_variant<P, MODE_LIST>(a.scan_minb, a, a.vlist, a.vcnt, nullptr, a.xref, a.flag, nullptr, st);
   else
-    scan_variant<P, MODE_DENSITY>(a.scan_minb, a, nullptr, a.nbr_cnt, a.nbm, nullptr, nullptr, st);
+    scan_variant<P, MODE_DENSITY>(a.scan_minb, a, nullptr, a.nbr_cnt, a.nbm, nullptr, nullptr,
+                                  a.queue, st);
 }
 
 template <int P, int MB>
 void force_variant(const NbArgs& a, cudaStream_t st) {
-  k_force<P, MB><<<a.n_tiles, a.tile_size, 0, st>>>(a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles, a.scenes,
-                                                    a.wave, a.force, a.nbm, a.nbr_cnt, a.n_total, a.xpair,
-                                                    a.vpair, a.status);
+  int32_t* queue = a.queue ? a.queue + 1 : nullptr;
+  auto kern = queue ? k_force<P, MB, true> : k_force<P, MB, false>;
+  int grid = a.n_tiles;
+  if (queue) {
+    cudaMemsetAsync(queue, 0, sizeof(int32_t), st);
+    grid = queue_grid(kern, a.tile_size, a.n_tiles);
+  }
+  kern<<<grid, a.tile_size, 0, st>>>(a.pos, a.vel, a.rho_p, a.start, a.keys, a.tiles, a.scenes, a.wave, a.force,
+                                     a.nbm, a.nbr_cnt, a.n_total, a.xpair, a.vpair, a.status, a.order, queue,
+                                     a.n_tiles);
 }
 
 template <int P>

@@ -38,7 +38,7 @@ class Sim:
 
     def __init__(self, scenes, precision: int = PREC_COMPENSATED, use_graph: bool = True,
                  device: int = 0, nb_threads: int = 0, nb_stage: int = 0, verlet_skin: float = 0.0,
-                 nb_scan_minb: int = 0, nb_force_minb: int = 0, wave_block: int = 0):
+                 nb_scan_minb: int = 0, nb_force_minb: int = 0, wave_block: int = 0, nb_queue: int = 0):
         self._lib = _abi.load()
         if isinstance(scenes, SceneDesc):
             scenes = [scenes]
@@ -46,7 +46,8 @@ class Sim:
         arr = (SceneDesc * len(self.scenes))(*self.scenes)
         opt = SimOptions(device=device, precision=precision, use_graph=int(use_graph),
                          nb_threads=nb_threads, nb_stage=nb_stage, verlet_skin=verlet_skin,
-                         nb_scan_minb=nb_scan_minb, nb_force_minb=nb_force_minb, wave_block=wave_block)
+                         nb_scan_minb=nb_scan_minb, nb_force_minb=nb_force_minb, wave_block=wave_block,
+                         nb_queue=nb_queue)
         h = C.c_void_p()
         check(self._lib.cwa_create(C.byref(opt), arr, len(self.scenes), C.byref(h)), "cwa_create")
         self._h = h

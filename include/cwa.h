@@ -127,7 +127,12 @@ typedef struct cwa_sim_options {
                               (4, 6, 8; 0 = 4)                              */
   int32_t nb_force_minb;   /* force kernel variant (6, 8; 0 = 8)              */
   int32_t wave_block;      /* blocked wave advance variant (CWA_WAVE_BLOCK_*)  */
-  int32_t reserved[3];
+  int32_t nb_queue;        /* 1: the density and force passes run as
+                              persistent CTAs that take particle tiles from
+                              a work queue (scenes with the most particles
+                              first); 0: one CTA a tile (default).  Same
+                              results either way.                          */
+  int32_t reserved[2];
 } cwa_sim_options;
 
 /* Blocked wave advance variants: box of 128 x H cells (P: 256 x H) advanced

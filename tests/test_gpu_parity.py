@@ -378,6 +378,20 @@ def test_batched_equals_single(lib, zsub):
         assert np.array_equal(bits(together[k][1]), bits(alone[1])), f"scene {k} wave differs"
 
 
+def test_work_queue_batch_equals_single(lib):
+    """The work-queue form (persistent CTAs taking tiles, largest scenes
+    first) over a batch of uneven scenes equals each scene stepped alone."""
+    scs = [small_muller((6, 6, 6), 0.03, (32, 32), seed=5),
+           small_muller((18, 16, 20), 0.02, (64, 48), seed=6),
+           scenes.dam_break((9, 9, 9), 0.025, (40, 72), box_hi=(1.5, 1.0, 1.0), seed=7),
+           small_muller((3, 5, 7), 0.03, (21, 37), seed=8)]
+    together = _run(scs, 8, nb_queue=1)
+    for k, s in enumerate(scs):
+        alone = _run([s], 8)[0]
+        assert np.array_equal(bits(together[k][0]), bits(alone[0])), f"scene {k} particles differ"
+        assert np.array_equal(bits(together[k][1]), bits(alone[1])), f"scene {k} wave differs"
+
+
 def test_graph_equals_eager(lib):
     sc = small_muller((16, 16, 16), 0.02, (64, 64))
     a = _run([sc], 13, use_graph=True)[0]
@@ -530,9 +544,9 @@ def test_autotune_keeps_state_and_results(lib):
 @pytest.mark.parametrize("prec", [PREC_FP32, PREC_COMPENSATED])
 def test_neighbour_passes_invariant_to_staging_tiles_and_batching(lib, prec):
     """Every particle's neighbour sums run in an order fixed by the particle
-    alone, so staging on or off, 64- or 128-particle CTAs and the scene's
-    place in a batch (here behind a scene of odd size) leave every bit
-    unchanged."""
+    alone, so staging on or off, 64- or 128-particle CTAs, the work-queue
+    form of the passes and the scene's place in a batch (here behind a scene
+    of odd size) leave every bit unchanged."""
     sc = small_muller((14, 15, 13), 0.02, (48, 40), zsub=4, seed=31)
     odd = small_muller((5, 7, 9), 0.03, (32, 32), seed=32)  # 315 particles: the next scene starts at an odd index
     def run(scene_list, k, **kw):
@@ -543,6 +557,7 @@ def test_neighbour_passes_invariant_to_staging_tiles_and_batching(lib, prec):
             sim.synchronize()
             return records_f32(sim.download_particles(k))
     base = run([sc], 0)
-    for kw in ({"nb_stage": -1}, {"nb_threads": 64}, {"nb_threads": 96, "nb_stage": -1}):
+    for kw in ({"nb_stage": -1}, {"nb_threads": 64}, {"nb_threads": 96, "nb_stage": -1}, {"nb_queue": 1},
+               {"nb_queue": 1, "nb_threads": 64, "nb_force_minb": 6}):
         assert np.array_equal(bits(run([sc], 0, **kw)), bits(base)), kw
     assert np.array_equal(bits(run([odd, sc], 1)), bits(base)), "batched behind an odd-sized scene"
