@@ -13,9 +13,10 @@ untimed steps the run continues to the workload's last step, and exactly
 timed, so the figure covers the early dam-break, the collapse and the late
 sloshing state alike (config.timed_steps lists them).
 
-`e2e` runs the same step through the public C ABI with host buffers: each
-step uploads the particle records and both wave fields from pinned host
-memory, steps, and downloads the particle records and u^n.
+`e2e` runs the same step through the public C ABI with host buffers: the
+host owns the state, so each step uploads the particle records and both
+wave fields from pinned host memory, steps, and downloads the records and
+both wave fields, which the next step uploads.
 
 `--gpus N` without torchrun re-launches itself under torch.distributed.run
 with N ranks; every rank runs an independent replica (the single-scene step
@@ -519,7 +520,7 @@ def run_gpu(args) -> None:
         cwa._abi.check(lib.cwa_download_wave(sim.handle, k, C.c_void_p(hu.data_ptr()), C.c_void_p(hu2.data_ptr()),
                                              hu.shape[1], hu.shape[0]), "download_wave")
     h2d = sum(hp.numel() + hu.numel() * 8 for hp, hu, _ in pin)
-    d2h = sum(hp.numel() + hu.numel() * 4 for hp, hu, _ in pin)
+    d2h = sum(hp.numel() + hu.numel() * 8 for hp, hu, _ in pin)
     torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
@@ -533,11 +534,9 @@ def run_gpu(args) -> None:
                            "upload_wave")
         sim.step(1)
         for k, (hp, hu, hu2) in enumerate(pin):
-            # u^n becomes the next upload's u^(n-1): the old u^n moves first
-            hu2.copy_(hu)
             cwa._abi.check(lib.cwa_download_particles(sim.handle, k, C.c_void_p(hp.data_ptr()),
                                                       wl.scenes[k].desc.n_particles), "download")
-            cwa._abi.check(lib.cwa_download_wave(sim.handle, k, C.c_void_p(hu.data_ptr()), None,
+            cwa._abi.check(lib.cwa_download_wave(sim.handle, k, C.c_void_p(hu.data_ptr()), C.c_void_p(hu2.data_ptr()),
                                                  hu.shape[1], hu.shape[0]), "download_wave")
     e2e_s = time.perf_counter() - t0
     if ws > 1:
