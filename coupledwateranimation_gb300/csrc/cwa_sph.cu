@@ -455,8 +455,10 @@ __device__ __forceinline__ int scan_tile(
       }
       overflow |= off0 + len > kMaskBits;
       const RowMask m = off0 < kMaskBits ? bits << off0 : 0u;
-      masks[(size_t)r * n_total + i] = m;
-      if (m != 0u) hits |= 1 << r;
+      if (m != 0u) {  // the nonzero masks only, packed in row order (slot = rows with hits before r)
+        masks[(size_t)__popc(hits) * n_total + i] = m;
+        hits |= 1 << r;
+      }
       acc.add(part);
     } else {
       overflow |= off0 + len > kRowCodeMax;
@@ -616,8 +618,10 @@ __global__ void __launch_bounds__(kNbThreads, 8)
 #pragma unroll
   for (int r = 0; r < kNbRows; ++r) {
     const RowMask m = s_m[r][threadIdx.x];
-    nbm[(size_t)r * n_total + i] = m;
-    if (m != 0u) rows |= 1 << r;
+    if (m != 0u) {  // packed as the candidate scan packs them
+      nbm[(size_t)__popc(rows) * n_total + i] = m;
+      rows |= 1 << r;
+    }
   }
   nbr_cnt[i] = overflow ? -1 : rows;
   const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
@@ -721,8 +725,10 @@ __device__ __forceinline__ void force_tile(
   const SceneDev* S = scenes + tl.scene;
   const int i = tl.begin + threadIdx.x;
   if (i >= tl.end) return;
-  const float4 pi = __ldg(pos + i);
-  const float4 vi = __ldg(vel + i);
+  // FP32 modes read the particle's own position and velocity from its gather
+  // records (the same floats, and lines its neighbours' gathers share)
+  const float4 pi = P == CWA_PREC_FP64 ? __ldg(pos + i) : __ldg(xpair + i);
+  const float4 vi = P == CWA_PREC_FP64 ? __ldg(vel + i) : __ldg(vpair + i);
   const float2 rpi = __ldg(rho_p + i);
   const T hh = (T)S->h;
   const T h2 = hh * hh;
@@ -757,14 +763,17 @@ __device__ __forceinline__ void force_tile(
   row_bases(S, start, c, base);
   if (cnt >= 0) {
     // The row masks hold the particle itself: row 4 (its own column) at bit
-    // i - base[4], cleared here.  The nonzero masks are compacted in row
-    // order (all nine are loaded, back to back); hits are then popped in row
-    // then bit order, in groups of 8 whose neighbour indexes are found first
-    // so the gathers overlap.
-    int nw = 0, left = 0;
+    // i - base[4], cleared here.  The density pass stored only the nonzero
+    // masks, packed in row order; they are loaded back to back, and hits are
+    // then popped in row then bit order, in groups of 8 whose neighbour
+    // indexes are found first so the gathers overlap.
+    int nw = 0, left = 0, rest = cnt;  // cnt: the rows with hits, as bits
 #pragma unroll
-    for (int r = 0; r < kNbRows; ++r) {
-      RowMask m = __ldg(nbm + (size_t)r * n_total + i);
+    for (int k = 0; k < kNbRows; ++k) {
+      if (rest == 0) break;
+      const int r = __ffs(rest) - 1;  // the row of packed mask k
+      rest &= rest - 1;
+      RowMask m = __ldg(nbm + (size_t)k * n_total + i);
       if (r == 4 && i - base[4] < kMaskBits) m &= ~((RowMask)1u << (i - base[4]));
       if (m) {
         s_w[nw][threadIdx.x] = m;
