@@ -455,8 +455,8 @@ __device__ __forceinline__ int scan_tile(
       }
       overflow |= off0 + len > kMaskBits;
       const RowMask m = off0 < kMaskBits ? bits << off0 : 0u;
-      if (m != 0u) {  // the nonzero masks only, packed in row order (slot = rows with hits before r)
-        masks[(size_t)__popc(hits) * n_total + i] = m;
+      if (m != 0u) {  // the nonzero masks only; force reads the rows the bitmap names
+        masks[(size_t)r * n_total + i] = m;
         hits |= 1 << r;
       }
       acc.add(part);
@@ -618,8 +618,8 @@ __global__ void __launch_bounds__(kNbThreads, 8)
 #pragma unroll
   for (int r = 0; r < kNbRows; ++r) {
     const RowMask m = s_m[r][threadIdx.x];
-    if (m != 0u) {  // packed as the candidate scan packs them
-      nbm[(size_t)__popc(rows) * n_total + i] = m;
+    if (m != 0u) {  // stored as the candidate scan stores them
+      nbm[(size_t)r * n_total + i] = m;
       rows |= 1 << r;
     }
   }
@@ -764,16 +764,14 @@ __device__ __forceinline__ void force_tile(
   if (cnt >= 0) {
     // The row masks hold the particle itself: row 4 (its own column) at bit
     // i - base[4], cleared here.  The density pass stored only the nonzero
-    // masks, packed in row order; they are loaded back to back, and hits are
-    // then popped in row then bit order, in groups of 8 whose neighbour
-    // indexes are found first so the gathers overlap.
-    int nw = 0, left = 0, rest = cnt;  // cnt: the rows with hits, as bits
+    // masks; those are loaded back to back and compacted in row order, and
+    // hits are then popped in row then bit order, in groups of 8 whose
+    // neighbour indexes are found first so the gathers overlap.
+    int nw = 0, left = 0;
 #pragma unroll
-    for (int k = 0; k < kNbRows; ++k) {
-      if (rest == 0) break;
-      const int r = __ffs(rest) - 1;  // the row of packed mask k
-      rest &= rest - 1;
-      RowMask m = __ldg(nbm + (size_t)k * n_total + i);
+    for (int r = 0; r < kNbRows; ++r) {
+      // cnt: the rows with hits, as bits (the others were not stored this step)
+      RowMask m = (cnt >> r) & 1 ? __ldg(nbm + (size_t)r * n_total + i) : (RowMask)0u;
       if (r == 4 && i - base[4] < kMaskBits) m &= ~((RowMask)1u << (i - base[4]));
       if (m) {
         s_w[nw][threadIdx.x] = m;
