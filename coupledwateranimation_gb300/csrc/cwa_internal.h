@@ -138,10 +138,10 @@ cudaError_t launch_point_rank(const int32_t* key, const int32_t* slot, const int
 // This step's hits (r < h, the particle itself included), written by the
 // density pass and read by force: nine row masks per particle, word
 // r * n_total + i holding particle i's hits in candidate row r as bits
-// (bit b = the candidate at the row's cell-based start + b).  Only nonzero
-// masks are stored; nbr_cnt holds the rows with a nonzero mask (bit r),
-// which are the words force reads, or -1 when some row's window reaches past
-// bit 63 (force then rescans the particle's rows).
+// (bit b = the candidate at the row's cell-based start + b).  nbr_cnt holds
+// the rows with a nonzero mask (bit r), the only words force reads, or -1
+// when some row's window reaches past bit 63 (force then rescans the
+// particle's rows).
 // The Verlet list (pairs within h (1 + skin) at the last rebuild) holds
 // 16-bit codes (row << 12 | offset from the row's cell-based start), entry k
 // of particle i at list[k * n_total + i]; a count of kMaxVerlet + 1 marks an

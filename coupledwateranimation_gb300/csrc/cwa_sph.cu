@@ -455,10 +455,11 @@ __device__ __forceinline__ int scan_tile(
       }
       overflow |= off0 + len > kMaskBits;
       const RowMask m = off0 < kMaskBits ? bits << off0 : 0u;
-      if (m != 0u) {  // the nonzero masks only; force reads the rows the bitmap names
-        masks[(size_t)r * n_total + i] = m;
-        hits |= 1 << r;
-      }
+      // every row is stored (whole sectors: skipping the zero rows would make
+      // each store a partial-sector write that DRAM reads back to merge);
+      // force reads only the rows the bitmap names
+      masks[(size_t)r * n_total + i] = m;
+      if (m != 0u) hits |= 1 << r;
       acc.add(part);
     } else {
       overflow |= off0 + len > kRowCodeMax;
@@ -618,10 +619,8 @@ __global__ void __launch_bounds__(kNbThreads, 8)
 #pragma unroll
   for (int r = 0; r < kNbRows; ++r) {
     const RowMask m = s_m[r][threadIdx.x];
-    if (m != 0u) {  // stored as the candidate scan stores them
-      nbm[(size_t)r * n_total + i] = m;
-      rows |= 1 << r;
-    }
+    nbm[(size_t)r * n_total + i] = m;
+    if (m != 0u) rows |= 1 << r;
   }
   nbr_cnt[i] = overflow ? -1 : rows;
   const T rho_t = (P == CWA_PREC_FP64 ? (T)S->c_poly6_d : (T)S->c_poly6) * acc.get();
@@ -763,14 +762,14 @@ __device__ __forceinline__ void force_tile(
   row_bases(S, start, c, base);
   if (cnt >= 0) {
     // The row masks hold the particle itself: row 4 (its own column) at bit
-    // i - base[4], cleared here.  The density pass stored only the nonzero
-    // masks; those are loaded back to back and compacted in row order, and
+    // i - base[4], cleared here.  Only the nonzero masks are loaded, back to
+    // back, and compacted in row order, and
     // hits are then popped in row then bit order, in groups of 8 whose
     // neighbour indexes are found first so the gathers overlap.
     int nw = 0, left = 0;
 #pragma unroll
     for (int r = 0; r < kNbRows; ++r) {
-      // cnt: the rows with hits, as bits (the others were not stored this step)
+      // cnt: the rows with hits, as bits; the zero rows are not read
       RowMask m = (cnt >> r) & 1 ? __ldg(nbm + (size_t)r * n_total + i) : (RowMask)0u;
       if (r == 4 && i - base[4] < kMaskBits) m &= ~((RowMask)1u << (i - base[4]));
       if (m) {
