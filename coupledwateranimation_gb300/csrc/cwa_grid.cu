@@ -19,8 +19,8 @@
 namespace cwa {
 namespace {
 
-constexpr int kScanBlock = 256;
-constexpr int kScanItems = 16;  // 4096-item tiles: half the look-back chain of 2048
+constexpr int kScanBlock = 512;
+constexpr int kScanItems = 16;  // 8192-item tiles: 147 tiles for the 1.2M cells of the 1M-particle grid, one wave
 constexpr int kScanTile = kScanBlock * kScanItems;
 static_assert(kScanTile == kScanTileItems, "workspace sizes assume kScanTileItems items a tile");
 constexpr unsigned long long kFlagAgg = 1ull << 32;

@@ -97,7 +97,7 @@ cwa_status status_from_bits(int32_t bits);
 
 // ---- grid / sort kernels (cwa_grid.cu) ----
 // Items per scan tile: the workspace holds one 8-byte state per tile.
-constexpr int kScanTileItems = 4096;
+constexpr int kScanTileItems = 8192;
 int scan_tile_items();
 size_t scan_workspace_bytes(int32_t n_out);
 void scan_bind_workspace(void* ws, int32_t n_out, ScanWorkspace* out);

@@ -2,7 +2,7 @@
 // memory.
 //
 // cwa_exclusive_scan_i32 asks the caller for a workspace (the scan's
-// look-back needs one status word per tile of 4096 elements plus a ticket
+// look-back needs one status word per tile of 8192 elements plus a ticket
 // counter).  Some callers cannot provide one: code that runs inside a host
 // application which owns the whole device-memory budget and hands out no
 // allocations, and real-time loops that must not call cudaMalloc / cudaFree
@@ -39,7 +39,7 @@ namespace {
 
 constexpr int32_t kNoAllocMaxN = CWA_NOALLOC_SCAN_MAX_N;
 // ticket + tile states for kNoAllocMaxN elements (256 + 8 per tile; sized
-// for 2048-element tiles, twice what the 4096-element tiles use), then one
+// for 2048-element tiles, four times what the 8192-element tiles use), then one
 // status word in its own 256-byte line
 constexpr size_t kNoAllocScratchBytes = 256 + (size_t)(kNoAllocMaxN / 2048) * 8 + 256;
 constexpr size_t kNoAllocStatusOffset = kNoAllocScratchBytes - 256;
