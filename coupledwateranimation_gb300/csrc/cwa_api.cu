@@ -212,6 +212,8 @@ SceneDev make_scene_dev(const cwa_scene_desc& d, const int32_t dims[3], int32_t 
     s.hi[a] = d.box_hi[a];
     s.g[a] = d.gravity[a];
   }
+  div_magic(dims[2], &s.mz, &s.sz);
+  div_magic(dims[1], &s.my, &s.sy);
   s.cell = d.cell_size;
   s.cellz = d.cell_size_z > 0.0f ? d.cell_size_z : d.cell_size;
   s.inv_cell = 1.0f / s.cell;

@@ -51,6 +51,10 @@ struct SceneDev {
   // uniform grid (z fastest: id = (x*ny + y)*nz + z)
   int32_t coff, ncells;
   int32_t dims[3];
+  // division by dims[2] and dims[1] of a cell id below 2^31: q = (n * m) >> s
+  // (round-up reciprocal, exact for every such n; see div_magic)
+  uint32_t mz, my;
+  int32_t sz, sy;
   float lo[3], hi[3];
   float cell, cellz, inv_cell, inv_cellz;  // x/y and z cell edges
   float hs, hs2;  // h * (1 + 2^-10): float rounding never drops a pair
@@ -77,6 +81,19 @@ struct SceneDev {
   int32_t line_source;
   int32_t coupled;   // MULLER: deposits on
 };
+
+// Multiplier and shift for dividing numbers below 2^31 by d >= 1 with a
+// multiply-high: m = ceil(2^(31 + l) / d), l = ceil(log2 d), then
+// n / d = (n * m) >> (31 + l) for every 0 <= n < 2^31 (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", 1994,
+// with N = 31 so that m fits in 32 bits).
+inline void div_magic(int32_t d, uint32_t* m, int32_t* shift) {
+  int l = 0;
+  while ((1ll << l) < d) ++l;
+  const unsigned long long num = 1ull << (31 + l);
+  *m = (uint32_t)((num + (unsigned long long)d - 1) / (unsigned long long)d);
+  *shift = 31 + l;
+}
 
 // A contiguous run of particles (or wave cells) that belongs to one scene.
 struct Tile {

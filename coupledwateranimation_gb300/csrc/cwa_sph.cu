@@ -85,13 +85,14 @@ struct CellCoord {
   int x, y, z;
 };
 
-// Cell coordinates of a global cell id.
+// Cell coordinates of a global cell id (the two divisions by the scene's
+// grid dimensions as multiply-highs with the scene's exact magic numbers).
 __device__ __forceinline__ CellCoord cell_of_key(const SceneDev* S, int key) {
   const int local = key - S->coff, nz = S->dims[2], ny = S->dims[1];
-  const int xy = local / nz;
+  const int xy = (int)(((unsigned long long)(uint32_t)local * S->mz) >> S->sz);
   CellCoord c;
   c.z = local - xy * nz;
-  c.x = xy / ny;
+  c.x = (int)(((unsigned long long)(uint32_t)xy * S->my) >> S->sy);
   c.y = xy - c.x * ny;
   return c;
 }
