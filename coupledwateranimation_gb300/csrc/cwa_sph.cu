@@ -373,10 +373,6 @@ struct ScanShared {
   uint16_t hit[MODE == MODE_LIST ? kMaxVerlet + 1 : 1][kNbThreads];
   StagePlan sp;
   __align__(8) uint64_t bar;
-  // density pass: thread t scans the tile's particle perm[t]; wq[w][q] =
-  // particles of warp w's natural slots in quadrant q (see scan_tile)
-  uint8_t perm[kNbThreads];
-  int16_t wq[kNbThreads / 32][4];
 };
 
 // One tile of the candidate scan.  Stages the tile's rows (bulk copies that
@@ -400,42 +396,8 @@ __device__ __forceinline__ int scan_tile(
   float4* const s_cand = sh.cand;
   StagePlan& sp = sh.sp;
   const SceneDev* S = scenes + tl.scene;
-  // Density pass: the tile's particles go to threads grouped by the quadrant
-  // of their cell column's (x, y) cross-section they sit in (a stable
-  // counting sort by quadrant).  A warp's particles then lie near the same
-  // column faces, so their windows in each side row have similar lengths,
-  // and a warp's pass over a row, as long as its longest lane window, wastes
-  // less: 121 against 159 candidate steps a particle in the C1 start
-  // lattice.  Each particle's arithmetic is unchanged.
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int quad = 4, rank = 0;
-  if (MODE == MODE_DENSITY) {
-    const int i0 = tl.begin + threadIdx.x;
-    if (i0 < tl.end) {
-      const float4 p0 = __ldg(pos + i0);
-      const CellCoord c0 = cell_of_key(S, __ldg(keys + i0));
-      const float mx = S->lo[0] + ((float)c0.x + 0.5f) * S->cell;  // column centre
-      const float my = S->lo[1] + ((float)c0.y + 0.5f) * S->cell;
-      quad = (p0.x >= mx ? 2 : 0) + (p0.y >= my ? 1 : 0);
-    }
-    const unsigned below = (1u << lane) - 1u;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const unsigned m = __ballot_sync(0xffffffffu, quad == k);
-      if (lane == 0) sh.wq[warp][k] = (int16_t)__popc(m);
-      if (quad == k) rank = __popc(m & below);
-    }
-  }
   if (threadIdx.x < 32) plan_stage(S, start, keys, tl, sp);
   __syncthreads();
-  if (MODE == MODE_DENSITY && quad < 4) {
-    int dest = rank;
-    const int nw = (int)(blockDim.x >> 5);
-    for (int k = 0; k < quad; ++k)
-      for (int w = 0; w < nw; ++w) dest += sh.wq[w][k];
-    for (int w = 0; w < warp; ++w) dest += sh.wq[w][quad];
-    sh.perm[dest] = (uint8_t)threadIdx.x;
-  }
   const bool staged = kCanStage && allow_stage && sp.ncols > 0;
   if (staged && threadIdx.x == 0) {
     mbar_expect_tx(&sh.bar, (uint32_t)sp.seg_off[kMaxSegs] * 16u);
@@ -451,9 +413,8 @@ __device__ __forceinline__ int scan_tile(
     mbar_wait_bounded(&sh.bar, parity);  // let copies in flight land before the CTA moves on
   }
   const int used = (staged ? 1 : 0) | (ready ? 0 : 2);
-  if (MODE == MODE_DENSITY) __syncthreads();  // perm complete
-  if (tl.begin + (int)threadIdx.x >= tl.end || !ready) return used;
-  const int i = tl.begin + (MODE == MODE_DENSITY ? (int)sh.perm[threadIdx.x] : (int)threadIdx.x);
+  const int i = tl.begin + threadIdx.x;
+  if (i >= tl.end || !ready) return used;
 
   const float4 pi = __ldg(pos + i);
   const T hh = (T)S->h;
