@@ -411,8 +411,8 @@ cwa_status run_grid(cwa_sim* s) {
   const int32_t* flag = s->verlet ? s->d_flag : nullptr;
   if (!s->counts_pending) CWA_TRY(run_hash(s));
   s->counts_pending = false;  // the scan consumes (and clears) the counts
-  CWA_CUDA(scan_launch(s->count, s->start, s->c_total, s->c_total + 1, true, s->scan, s->d_status, st,
-                       &s->launches, flag));
+  CWA_CUDA(scan_launch_two_pass(s->count, s->start, s->c_total, s->c_total + 1, true, s->scan, st, &s->launches,
+                                flag));
   CWA_CUDA(launch_list_insert(s->key, s->slot, s->start, s->list, s->n_total, flag, st, s->d_status));
   CWA_CUDA(launch_rank_reorder(s->key, s->slot, s->start, s->list, s->P[cur], s->V[cur],
                                s->move_force ? s->F[cur] : nullptr, s->ID[cur], s->P[nxt], s->V[nxt],

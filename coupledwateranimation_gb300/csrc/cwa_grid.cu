@@ -203,6 +203,135 @@ __global__ void __launch_bounds__(kScanBlock)
   }
 }
 
+// Two-pass form of the same exclusive scan, for the sim's grid pass: first
+// every tile's total (k_tile_sum), then every tile adds the totals of the
+// tiles before it to its own local scan (k_tile_scan).  The input is read
+// twice (4.8 MB at the 1M-particle grid, from L2 the second time) but no
+// tile waits on another, where the look-back chain of k_scan kept each CTA
+// resident ~12 us for a ~5 us job.
+template <bool kVec>
+__device__ __forceinline__ void load_tile_items(const int32_t* in, int32_t n_in, long base, int (&v)[kScanItems]) {
+  if (kVec) {
+#pragma unroll
+    for (int q = 0; q < kScanItems / 4; ++q) {
+      const long idx = base + 4 * q;
+      if (idx + 3 < n_in) {
+        const int4 x = *reinterpret_cast<const int4*>(in + idx);
+        v[4 * q] = x.x;
+        v[4 * q + 1] = x.y;
+        v[4 * q + 2] = x.z;
+        v[4 * q + 3] = x.w;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[4 * q + k] = idx + k < n_in ? in[idx + k] : 0;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) v[k] = base + k < n_in ? in[base + k] : 0;
+  }
+}
+
+template <bool kVec>
+__global__ void __launch_bounds__(kScanBlock)
+    k_tile_sum(const int32_t* in, int32_t n_in, int32_t* __restrict__ sums, const int32_t* flag) {
+  chain_enter();
+  if (flag && __ldg(flag) == 0) return;  // grid kept this step (Verlet mode)
+  __shared__ int s_warp[kScanBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long base = (long)blockIdx.x * kScanTile + (long)threadIdx.x * kScanItems;
+  int v[kScanItems];
+  load_tile_items<kVec>(in, n_in, base, v);
+  int t = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) t += v[k];
+  t = warp_sum(t);
+  if (lane == 0) s_warp[warp] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int total = 0;
+#pragma unroll
+    for (int w = 0; w < kScanBlock / 32; ++w) total += s_warp[w];
+    sums[blockIdx.x] = total;
+  }
+}
+
+template <bool kZero, bool kVec>
+__global__ void __launch_bounds__(kScanBlock)
+    k_tile_scan(int32_t* in, int32_t* out, int32_t n_in, int32_t n_out, const int32_t* __restrict__ sums,
+                const int32_t* flag) {
+  chain_enter();
+  if (flag && __ldg(flag) == 0) return;
+  __shared__ int s_warp[kScanBlock / 32];
+  __shared__ int s_prefix;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int tile = blockIdx.x;
+  if (warp == 0) {  // the totals of the tiles before this one
+    int p = 0;
+    for (int t = lane; t < tile; t += 32) p += sums[t];
+    p = warp_sum(p);
+    if (lane == 0) s_prefix = p;
+  }
+  const long base = (long)tile * kScanTile + (long)threadIdx.x * kScanItems;
+  int v[kScanItems];
+  load_tile_items<kVec>(in, n_in, base, v);
+  if (kZero) {
+    if (kVec) {
+#pragma unroll
+      for (int q = 0; q < kScanItems / 4; ++q) {
+        const long idx = base + 4 * q;
+        if (idx + 3 < n_in)
+          *reinterpret_cast<int4*>(in + idx) = make_int4(0, 0, 0, 0);
+        else
+          for (int k = 0; k < 4; ++k)
+            if (idx + k < n_in) in[idx + k] = 0;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < kScanItems; ++k)
+        if (base + k < n_in) in[base + k] = 0;
+    }
+  }
+  int tsum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const int x = v[k];
+    v[k] = tsum;
+    tsum += x;
+  }
+  int incl = tsum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  int warp_excl = 0;
+#pragma unroll
+  for (int w = 0; w < kScanBlock / 32; ++w)
+    if (w < warp) warp_excl += s_warp[w];
+  const int prefix = s_prefix + warp_excl + incl - tsum;
+  if (kVec) {
+#pragma unroll
+    for (int q = 0; q < kScanItems / 4; ++q) {
+      const long idx = base + 4 * q;
+      if (idx + 3 < n_out) {
+        *reinterpret_cast<int4*>(out + idx) =
+            make_int4(prefix + v[4 * q], prefix + v[4 * q + 1], prefix + v[4 * q + 2], prefix + v[4 * q + 3]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (idx + k < n_out) out[idx + k] = prefix + v[4 * q + k];
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k)
+      if (base + k < n_out) out[base + k] = prefix + v[k];
+  }
+}
+
 __global__ void __launch_bounds__(256)
     k_hash_count(const float4* __restrict__ pos, const Tile* __restrict__ tiles,
                  const SceneDev* __restrict__ scenes, int32_t* __restrict__ key,
@@ -354,6 +483,34 @@ cudaError_t scan_launch(const int32_t* in, int32_t* out, int32_t n_in, int32_t n
 #undef CWA_SCAN_K
   if (launches) *launches += 1;
   return cudaGetLastError();
+}
+
+cudaError_t scan_launch_two_pass(int32_t* in, int32_t* out, int32_t n_in, int32_t n_out, bool zero_input,
+                                 const ScanWorkspace& ws, cudaStream_t stream, int64_t* launches,
+                                 const int32_t* flag) {
+  if (n_out <= 0) return cudaSuccess;
+  int32_t* sums = reinterpret_cast<int32_t*>(ws.state);  // n_tiles ints in the tile-state area
+  const bool vec = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+  const dim3 grid(ws.n_tiles), block(kScanBlock);
+  cudaError_t e;
+  if (vec)
+    e = launch_chained(k_tile_sum<true>, grid, block, 0, stream, in, n_in, sums, flag);
+  else
+    e = launch_chained(k_tile_sum<false>, grid, block, 0, stream, in, n_in, sums, flag);
+  if (e != cudaSuccess) return e;
+  if (zero_input) {
+    if (vec)
+      e = launch_chained(k_tile_scan<true, true>, grid, block, 0, stream, in, out, n_in, n_out, sums, flag);
+    else
+      e = launch_chained(k_tile_scan<true, false>, grid, block, 0, stream, in, out, n_in, n_out, sums, flag);
+  } else {
+    if (vec)
+      e = launch_chained(k_tile_scan<false, true>, grid, block, 0, stream, in, out, n_in, n_out, sums, flag);
+    else
+      e = launch_chained(k_tile_scan<false, false>, grid, block, 0, stream, in, out, n_in, n_out, sums, flag);
+  }
+  if (launches) *launches += 2;
+  return e;
 }
 
 cudaError_t launch_hash_count(const float4* pos, const Tile* tiles, int32_t n_tiles, int32_t tile_size,

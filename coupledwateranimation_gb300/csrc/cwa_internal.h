@@ -125,6 +125,13 @@ cudaError_t scan_launch(const int32_t* in, int32_t* out, int32_t n_in, int32_t n
                         const ScanWorkspace& ws, int32_t* status, cudaStream_t stream, int64_t* launches,
                         const int32_t* flag = nullptr);
 
+// The same scan as two chained kernels (tile totals, then every tile's
+// scan plus the totals before it); uses the workspace's tile-state area for
+// the totals, needs no zeroing and has no wait that can time out.
+cudaError_t scan_launch_two_pass(int32_t* in, int32_t* out, int32_t n_in, int32_t n_out, bool zero_input,
+                                 const ScanWorkspace& ws, cudaStream_t stream, int64_t* launches,
+                                 const int32_t* flag = nullptr);
+
 // The grid-build kernels take the Verlet rebuild flag (null = always run).
 cudaError_t launch_hash_count(const float4* pos, const Tile* tiles, int32_t n_tiles, int32_t tile_size,
                               const SceneDev* scenes, int32_t* key, int32_t* slot, int32_t* count,
