@@ -413,7 +413,7 @@ def run_gpu(args) -> None:
 
     tune = None
     if not args.no_tune:  # pick the kernel variants on this workload (state restored)
-        tune = sim.autotune(trial_steps=4)
+        tune = sim.autotune(trial_steps=8)
     clk = ClockSampler(local).__enter__()  # samples across warm-up, timed steps, profile and e2e
     # warm-up (graph capture happens here), then a checkpoint: the GPU is kept
     # loaded until the clock sampler is logging (at most ~5 s), and the timed

@@ -310,8 +310,9 @@ cwa_status cwa_get_launch_count(cwa_sim* sim, int64_t* launches);
  * Tries the neighbour-pass kernel variants on the sim's current state
  * (candidate staging on/off, launch-bound variants of the density scan and
  * force, 128- or 64-particle CTAs), each from the same snapshot for
- * trial_steps timed steps, keeps the fastest and restores the state.  It
- * allocates a snapshot of the state while it runs. */
+ * trial_steps timed steps, keeps the fastest (unless it beats the options at
+ * entry by less than 1.5%, which is within the trials' noise) and restores
+ * the state.  It allocates a snapshot of the state while it runs. */
 #define CWA_TUNE_MAX_TRIED 32
 typedef struct cwa_tune_report {
   cwa_sim_options best;
