@@ -285,6 +285,41 @@ cwa_status check_scene(cwa_sim* s, int32_t scene) {
 
 float4* cur_force(cwa_sim* s) { return s->move_force ? s->F[s->cur] : s->F[0]; }
 
+// Device address of a page-locked host buffer (cudaHostAlloc, or
+// cudaHostRegister'd), or nullptr for pageable memory or a buffer that is not
+// 16-byte aligned.  Kernels read and write such buffers directly over the
+// host link (NVLink-C2C on Grace), which moves contiguous data faster than
+// a copy-engine transfer does.
+void* host_alias(const void* host) {
+  if (!host || (reinterpret_cast<uintptr_t>(host) & 15u)) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();  // not a pointer CUDA knows: plain pageable memory
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer ||
+      (reinterpret_cast<uintptr_t>(a.devicePointer) & 15u))
+    return nullptr;
+  return a.devicePointer;
+}
+
+// One height field between the host and the device, on the sim's stream:
+// a kernel copy when the host side is page-locked and both sides are 16-byte
+// aligned, else cudaMemcpyAsync.
+cwa_status copy_field(cwa_sim* s, const float* src, float* dst, long cells, cudaMemcpyKind kind) {
+  const bool to_dev = kind == cudaMemcpyHostToDevice;
+  void* alias = host_alias(to_dev ? static_cast<const void*>(src) : static_cast<const void*>(dst));
+  const float* dev_side = to_dev ? dst : src;
+  if (alias && !(reinterpret_cast<uintptr_t>(dev_side) & 15u)) {
+    CWA_CUDA(launch_copy_f32(to_dev ? static_cast<const float*>(alias) : src,
+                             to_dev ? dst : static_cast<float*>(alias), cells, s->stream));
+    s->launches += 1;
+    return CWA_OK;
+  }
+  CWA_CUDA(cudaMemcpyAsync(dst, src, (size_t)cells * sizeof(float), kind, s->stream));
+  return CWA_OK;
+}
+
 // Particle work tiles of `size` particles, never straddling two scenes.
 std::vector<Tile> particle_tiles(const cwa_sim* s, int32_t size) {
   std::vector<Tile> t;
@@ -905,10 +940,16 @@ cwa_status cwa_upload_particles(cwa_sim* s, int32_t scene, const cwa_particle* h
   const SceneDev& d = s->sd[scene];
   if (n != d.n || (!host && n > 0)) return arg_error("upload size must equal the scene's n_particles");
   if (n == 0) return CWA_OK;
-  CWA_CUDA(cudaMemcpyAsync(s->staging, host, (size_t)n * sizeof(cwa_particle), cudaMemcpyHostToDevice,
-                           s->stream));
-  CWA_CUDA(launch_unpack(s->staging, n, d.poff, s->P[s->cur], s->V[s->cur], cur_force(s), s->RP, s->EX,
-                         s->ID[s->cur], s->stream));
+  // page-locked records are read by the unpack kernel itself, over the host
+  // link; pageable ones go through the staging buffer
+  const cwa_particle* src = static_cast<const cwa_particle*>(host_alias(host));
+  if (!src) {
+    CWA_CUDA(cudaMemcpyAsync(s->staging, host, (size_t)n * sizeof(cwa_particle), cudaMemcpyHostToDevice,
+                             s->stream));
+    src = s->staging;
+  }
+  CWA_CUDA(launch_unpack(src, n, d.poff, s->P[s->cur], s->V[s->cur], cur_force(s), s->RP, s->EX, s->ID[s->cur],
+                         s->stream));
   s->launches += 1;
   s->grid_fresh = false;
   CWA_TRY(drop_pending_counts(s));
@@ -928,8 +969,16 @@ cwa_status cwa_download_particles(cwa_sim* s, int32_t scene, cwa_particle* host,
   CWA_CUDA(launch_pack(s->staging, n, d.poff, s->P[s->cur], s->V[s->cur], cur_force(s), s->RP, s->EX,
                        s->ID[s->cur], s->stream));
   s->launches += 1;
-  CWA_CUDA(cudaMemcpyAsync(host, s->staging, (size_t)n * sizeof(cwa_particle), cudaMemcpyDeviceToHost,
-                           s->stream));
+  // the pack scatters the records back to upload order in device memory; a
+  // page-locked destination then takes them in one coalesced kernel copy
+  if (void* dst = host_alias(host)) {
+    CWA_CUDA(launch_copy_f32(reinterpret_cast<const float*>(s->staging), static_cast<float*>(dst),
+                             (long)n * (long)(sizeof(cwa_particle) / sizeof(float)), s->stream));
+    s->launches += 1;
+  } else {
+    CWA_CUDA(cudaMemcpyAsync(host, s->staging, (size_t)n * sizeof(cwa_particle), cudaMemcpyDeviceToHost,
+                             s->stream));
+  }
   CWA_CUDA(cudaStreamSynchronize(s->stream));
   return CWA_OK;
 }
@@ -939,11 +988,10 @@ cwa_status cwa_upload_wave(cwa_sim* s, int32_t scene, const float* u_n, const fl
   CWA_TRY(check_scene(s, scene));
   const SceneDev& d = s->sd[scene];
   if (nx != d.nx || nz != d.nz || !u_n) return arg_error("wave upload size must equal the scene's grid");
-  const size_t bytes = (size_t)nx * nz * sizeof(float);
+  const long cells = (long)nx * nz;
   const int w = s->wcur;
-  CWA_CUDA(cudaMemcpyAsync(s->U[w] + d.woff, u_n, bytes, cudaMemcpyHostToDevice, s->stream));
-  CWA_CUDA(cudaMemcpyAsync(s->U[(w + 2) % 3] + d.woff, u_nm1 ? u_nm1 : u_n, bytes, cudaMemcpyHostToDevice,
-                           s->stream));
+  CWA_TRY(copy_field(s, u_n, s->U[w] + d.woff, cells, cudaMemcpyHostToDevice));
+  CWA_TRY(copy_field(s, u_nm1 ? u_nm1 : u_n, s->U[(w + 2) % 3] + d.woff, cells, cudaMemcpyHostToDevice));
   CWA_CUDA(cudaStreamSynchronize(s->stream));
   return CWA_OK;
 }
@@ -952,11 +1000,10 @@ cwa_status cwa_download_wave(cwa_sim* s, int32_t scene, float* u_n, float* u_nm1
   CWA_TRY(check_scene(s, scene));
   const SceneDev& d = s->sd[scene];
   if (nx != d.nx || nz != d.nz) return arg_error("wave download size must equal the scene's grid");
-  const size_t bytes = (size_t)nx * nz * sizeof(float);
+  const long cells = (long)nx * nz;
   const int w = s->wcur;
-  if (u_n) CWA_CUDA(cudaMemcpyAsync(u_n, s->U[w] + d.woff, bytes, cudaMemcpyDeviceToHost, s->stream));
-  if (u_nm1)
-    CWA_CUDA(cudaMemcpyAsync(u_nm1, s->U[(w + 2) % 3] + d.woff, bytes, cudaMemcpyDeviceToHost, s->stream));
+  if (u_n) CWA_TRY(copy_field(s, s->U[w] + d.woff, u_n, cells, cudaMemcpyDeviceToHost));
+  if (u_nm1) CWA_TRY(copy_field(s, s->U[(w + 2) % 3] + d.woff, u_nm1, cells, cudaMemcpyDeviceToHost));
   CWA_CUDA(cudaStreamSynchronize(s->stream));
   return CWA_OK;
 }

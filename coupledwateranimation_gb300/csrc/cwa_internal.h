@@ -231,8 +231,13 @@ cudaError_t launch_wave_init(float* u, int32_t nx, int32_t nz, float mode, cudaS
 // u(x, y) = red(2x, y) / 255 of a w x h RGBA8 image (device memory), 0 past it.
 cudaError_t launch_wave_from_image(float* u, int32_t nx, int32_t nz, const uint8_t* rgba, int32_t w, int32_t h,
                                    cudaStream_t stream);
+// `aos` (16-byte aligned) may be device memory or the device address of
+// page-locked host memory.
 cudaError_t launch_unpack(const cwa_particle* aos, int32_t n, int32_t poff, float4* pos, float4* vel,
                           float4* force, float2* rho_p, float2* extra, int32_t* id, cudaStream_t stream);
+// n floats from src to dst, both 16-byte aligned (cudaErrorInvalidValue
+// otherwise); either may be the device address of page-locked host memory.
+cudaError_t launch_copy_f32(const float* src, float* dst, long n, cudaStream_t stream);
 cudaError_t launch_pack(cwa_particle* aos, int32_t n, int32_t poff, const float4* pos, const float4* vel,
                         const float4* force, const float2* rho_p, const float2* extra,
                         const int32_t* id, cudaStream_t stream);

@@ -269,19 +269,36 @@ __global__ void k_wave_init(float* __restrict__ u, int32_t nx, int32_t nz, float
   u[c] = fmul(peak, sm);
 }
 
-__global__ void k_unpack(const cwa_particle* __restrict__ aos, int32_t n, int32_t poff, float4* __restrict__ pos,
+// One thread a 16-byte quarter of a record: a warp reads 512 contiguous
+// bytes (8 records) of the source, which may be page-locked host memory
+// read over the host link, and writes each quarter's 8 words to its array as
+// 128 contiguous bytes.
+__global__ void k_unpack(const float4* __restrict__ aos, int32_t n, int32_t poff, float4* __restrict__ pos,
                          float4* __restrict__ vel, float4* __restrict__ force, float2* __restrict__ rho_p,
                          float2* __restrict__ extra, int32_t* __restrict__ id) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4* q = reinterpret_cast<const float4*>(aos + i);
-  const float4 e = q[3];
-  pos[poff + i] = q[0];
-  vel[poff + i] = q[1];
-  force[poff + i] = q[2];
-  rho_p[poff + i] = make_float2(e.x, e.y);
-  extra[poff + i] = make_float2(e.z, e.w);
-  id[poff + i] = i;
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= 4L * n) return;
+  const int i = (int)(t >> 2), q = (int)(t & 3);
+  const float4 v = aos[t];
+  if (q == 3) {
+    rho_p[poff + i] = make_float2(v.x, v.y);
+    extra[poff + i] = make_float2(v.z, v.w);
+    id[poff + i] = i;
+  } else {
+    (q == 0 ? pos : q == 1 ? vel : force)[poff + i] = v;
+  }
+}
+
+// Contiguous copy of n floats, both pointers 16-byte aligned, either side
+// device memory or page-locked host memory: one 16-byte word a thread, and
+// the thread past the last whole word copies the 0-3 floats left.
+__global__ void k_copy_f32(const float* __restrict__ src, float* __restrict__ dst, long n) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long n4 = n >> 2;
+  if (t < n4)
+    reinterpret_cast<float4*>(dst)[t] = reinterpret_cast<const float4*>(src)[t];
+  else if (t == n4)
+    for (long k = n4 * 4; k < n; ++k) dst[k] = src[k];
 }
 
 __global__ void k_pack(cwa_particle* __restrict__ aos, int32_t n, int32_t poff, const float4* __restrict__ pos,
@@ -408,7 +425,15 @@ cudaError_t launch_wave_init(float* u, int32_t nx, int32_t nz, float mode, cudaS
 cudaError_t launch_unpack(const cwa_particle* aos, int32_t n, int32_t poff, float4* pos, float4* vel,
                           float4* force, float2* rho_p, float2* extra, int32_t* id, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  k_unpack<<<blocks_for(n, 256), 256, 0, stream>>>(aos, n, poff, pos, vel, force, rho_p, extra, id);
+  k_unpack<<<blocks_for(4L * n, 256), 256, 0, stream>>>(reinterpret_cast<const float4*>(aos), n, poff, pos, vel,
+                                                         force, rho_p, extra, id);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_f32(const float* src, float* dst, long n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  if ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) return cudaErrorInvalidValue;
+  k_copy_f32<<<blocks_for((n >> 2) + 1, 256), 256, 0, stream>>>(src, dst, n);
   return cudaGetLastError();
 }
 

@@ -231,6 +231,11 @@ cwa_status cwa_make_bumps(const cwa_scene_desc* scene, int32_t n_bumps, uint64_t
 cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, int32_t n_scenes,
                       cwa_sim** out);
 cwa_status cwa_destroy(cwa_sim* sim);
+/* Host transfers return when the host buffer may be reused.  A page-locked
+ * host buffer (cudaHostAlloc / cudaHostRegister) that is 16-byte aligned is
+ * read or written by the library's kernels directly over the host link, in
+ * coalesced 16-byte words; other buffers go through cudaMemcpyAsync.  The
+ * bytes moved are the same either way. */
 cwa_status cwa_upload_particles(cwa_sim* sim, int32_t scene, const cwa_particle* host, int32_t n);
 cwa_status cwa_download_particles(cwa_sim* sim, int32_t scene, cwa_particle* host, int32_t n);
 cwa_status cwa_upload_wave(cwa_sim* sim, int32_t scene, const float* u_n, const float* u_nm1,
