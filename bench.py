@@ -23,10 +23,12 @@ with N ranks; every rank runs an independent replica (the single-scene step
 does not shard) and value = all ranks' updates / the slowest rank's time.
 
 `--impl reference` times the reference algorithm on the host cores instead:
-the reference's GLSL cannot run here (no graphics stack), so its CPU
-restatement (oracle/, FP64, OpenMP over all host threads), with inputs from
-the oracle's own generators, runs --warmup untimed and exactly --steps timed
-steps of the same workload.
+the reference's GLSL cannot run through OpenGL here (no graphics stack), and
+its shaders compiled for the CPU exist only beside the reference checkout and
+loop over a fixed 20,480 particles, so its CPU restatement (oracle/, FP64,
+OpenMP over all host threads; pinned to those shaders by
+tests/test_ref_shaders.py), with inputs from the oracle's own generators,
+runs --warmup untimed and exactly --steps timed steps of the same workload.
 """
 from __future__ import annotations
 
@@ -291,8 +293,9 @@ def run_reference(args) -> None:
                          "sample": f"the {steps} timed steps of the workload's run (the GPU arm's step numbers; "
                                    f"{secs:.1f} s timed; sort grid z cells of h/{CPU_ZSUB}, the oracle's "
                                    f"fastest) on the FP64 OpenMP restatement of the reference shaders, inputs "
-                                   f"from the oracle's own generators; the GLSL itself cannot run (no graphics "
-                                   f"stack)"},
+                                   f"from the oracle's own generators (the restatement is pinned to the "
+                                   f"reference's shaders compiled for the CPU; those run only beside the "
+                                   f"reference checkout, over a fixed 20,480 particles)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

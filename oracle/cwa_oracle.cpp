@@ -8,9 +8,13 @@
 // kernels' __f*_rn intrinsics.
 //
 // Parity: the exclusive scan is pinned to the reference's ParallelScanTest
-// vector (SphWave2D/ParallelScan.cpp:124-155).  SPH, integrate, coupling and
-// wave are parity unpinned (the GLSL cannot run here); they follow the
-// shader source.
+// vector (SphWave2D/ParallelScan.cpp:124-155).  The REFERENCE_3D density,
+// force, integrate and wave routines are pinned to the reference's own
+// compute shaders compiled for the CPU (oracle/ref_shaders/,
+// tests/test_ref_shaders.py): the FP64 routines equal the shaders run in
+// double to 1e-14, the float32 routines equal them run in float bit for bit
+// or within a few roundings where a sum is associated differently.  The
+// MULLER coupling terms have no reference counterpart.
 
 #include "cwa_oracle.h"
 
@@ -24,7 +28,13 @@
 
 namespace {
 
-const double kRefPi = 3.141592741;  // PI #define of the shaders (rho_pres_comp.glsl:8)
+// The shaders' float literals as the doubles they round to: the FP64 passes
+// compute the shaders' expressions on the shaders' own constant values.
+const double kRefPi = (double)3.141592741f;  // PI #define of the shaders (rho_pres_comp.glsl:8)
+const double kWaveStep = (double)0.01f;      // WaveVelocity's h (force_comp.glsl:119)
+const double kFoamScale = (double)0.1f;      // foam damping (integrate_comp.glsl:73,75)
+const double kCeilMargin = (double)0.1f;     // line-source ceiling (integrate_comp.glsl:172-174)
+const double kLineThreshold = (double)0.0001f, kLineLift = (double)0.001f;  // wave_comp.glsl:177,182
 
 // ---------------------------------------------------------------- RNG ----
 // splitmix64 seeding xoshiro256** (Blackman & Vigna), uniform doubles from
@@ -541,8 +551,8 @@ void orc_force(const cwa_scene_desc* sc, int32_t n, double* p16, const double* u
                           0.25 * (a[2] * fprev[0] - a[0] * fprev[2]),
                           0.25 * (a[0] * fprev[1] - a[1] * fprev[0])};
       // WaveVelocity (force_comp.glsl:117-128): step 0.01 in uv, shader dt.
-      double hx = sample64(u_n, W, Hh, s + 0.01, t), hy = sample64(u_n, W, Hh, s, t + 0.01);
-      double wv[3] = {(hx - H) / sc->dt, (hy - H) / sc->dt, (hx - hy) / 0.01};
+      double hx = sample64(u_n, W, Hh, s + kWaveStep, t), hy = sample64(u_n, W, Hh, s, t + kWaveStep);
+      double wv[3] = {(hx - H) / sc->dt, (hy - H) / sc->dt, (hx - hy) / kWaveStep};
       // WaveNormal (force_comp.glsl:130-139): cross((0,1,hT-h),(1,0,hR-h)).
       double hR = sample64(u_n, W, Hh, s + 1.0, t) - H;
       double hT = sample64(u_n, W, Hh, s, t + 1.0) - H;
@@ -595,9 +605,9 @@ void orc_integrate(const cwa_scene_desc* sc, int32_t n, double* p16, const doubl
     if (ref) {
       if (sc->foam_speed > 0.0f && sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) > sc->foam_speed) {
         for (int c = 0; c < 4; ++c) q[8 + c] *= 0.5;
-        q[12] *= 0.1;
+        q[12] *= kFoamScale;
         q[13] *= 0.25;
-        for (int c = 0; c < 3; ++c) v[c] *= 0.1;
+        for (int c = 0; c < 3; ++c) v[c] *= kFoamScale;
       }
       double H = sample64(u_n, W, Hh, s, t);
       if (x[1] < H) x[1] = H - sc->particle_radius;
@@ -634,7 +644,7 @@ void orc_integrate(const cwa_scene_desc* sc, int32_t n, double* p16, const doubl
       }
     }
     if (ref && sc->wave_mode > 0.0f && sc->wave_mode < 1.0f) {
-      double ceil_y = (double)sc->box_hi[1] + 0.1;
+      double ceil_y = (double)sc->box_hi[1] + kCeilMargin;
       if (x[1] > ceil_y) {
         x[1] = ceil_y;
         v[1] *= -e;
@@ -668,7 +678,7 @@ void orc_wave(const cwa_scene_desc* sc, const double* u_n, const double* u_nm1, 
       double ww = u_n[(size_t)j * W + std::max(i - 1, 0)];
       double w = (2.0 - 4.0 * lam - beta) * c0 + lam * (nn + ss + ee + ww) - (1.0 - beta) * c1;
       w *= att;
-      if (line && w > 0.0001 && i == W / 2) w += 0.001;
+      if (line && w > kLineThreshold && i == W / 2) w += kLineLift;
       if (deposits) w += (double)deposits[c] * dq;
       u_out[c] = w;
     }

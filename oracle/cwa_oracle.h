@@ -17,10 +17,11 @@
  *
  * Parity pinning: the reference's only known-answer test is the exclusive
  * scan (SphWave2D/ParallelScan.cpp:124-155); the scan restatement is pinned
- * to it.  The reference's shaders cannot be executed (GLSL through OpenGL, no
- * graphics stack), so the SPH, integrate, coupling and wave restatements are
- * parity unpinned: they follow the shader source line by line (cited per
- * function) but no reference output exists to check them against.
+ * to it.  The REFERENCE_3D SPH, integrate and wave restatements are pinned to
+ * the reference's compute shaders themselves, compiled for the CPU
+ * (oracle/ref_shaders/) and run on seeded inputs whose outputs are committed
+ * as tests/golden/ref_shader_outputs.npz.  The MULLER coupling terms are new
+ * physics with no reference output.
  *
  * Particle arrays are the 64-byte reference struct widened to double:
  * 16 doubles per particle = pos[4], vel[4], force[4], extras[4].

@@ -1,0 +1,221 @@
+"""The reference's compute shaders run on the CPU: ctypes access to
+oracle/_ref/libcwa_ref_shaders.so, plus the seeded inputs the golden
+fixtures of tests/golden/ref_shader_outputs.npz are computed on.
+
+TEST INFRASTRUCTURE ONLY.  The library is compiled from the reference
+checkout's own shader source (CoupledWaterAnimation/rho_pres_comp.glsl,
+force_comp.glsl, integrate_comp.glsl, wave_comp.glsl) by
+oracle/ref_shaders/Makefile; it exists only where that checkout does.  The
+fixtures it produced are committed, so the checks that use them run
+anywhere.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_ref" / "libcwa_ref_shaders.so"
+# the reference checkout of this container (absent elsewhere); CWA_REFERENCE overrides it
+DEFAULT_REFERENCE = Path("/root/reference")
+
+NUM_PARTICLES = 20480  # the shaders' NUM_PARTICLES (rho_pres_comp.glsl:4)
+F32, F64 = 0, 1
+
+
+class Uniforms(C.Structure):
+    """ref_uniforms (oracle/ref_shaders/ref_shaders.h): the uniform blocks of
+    Main.cpp:184-204 as the shaders declare them."""
+    _fields_ = [("mass", C.c_float), ("smoothing_coeff", C.c_float), ("visc", C.c_float),
+                ("resting_rho", C.c_float), ("upper", C.c_float * 4), ("lower", C.c_float * 4),
+                ("attributes", C.c_float * 4), ("mesh_ws_pos", C.c_float * 4), ("time", C.c_float),
+                ("mode", C.c_int32)]
+
+
+def reference_root() -> Path | None:
+    ref = Path(os.environ.get("CWA_REFERENCE", str(DEFAULT_REFERENCE)))
+    return ref if (ref / "CoupledWaterAnimation" / "rho_pres_comp.glsl").is_file() else None
+
+
+def build(verbose: bool = False) -> Path | None:
+    """Compile the shaders when the reference checkout is present; returns
+    the library path, or None without a checkout."""
+    ref = reference_root()
+    if ref is None:
+        return None
+    subprocess.run(["make", "-s" if not verbose else "-w", "-C", str(HERE / "ref_shaders"), f"REF={ref}"],
+                   check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def load():
+    """The compiled shaders, or None where they were not built."""
+    global _lib
+    if _lib is None and LIB_PATH.is_file():
+        lib = C.CDLL(str(LIB_PATH))
+        dp, fp = C.POINTER(C.c_double), C.POINTER(C.c_float)
+        for name in ("ref_rho_pres", "ref_force", "ref_integrate"):
+            f = getattr(lib, name)
+            f.argtypes = [C.c_int32, dp, C.c_int32, fp, C.c_int32, C.c_int32, C.POINTER(Uniforms)]
+            f.restype = C.c_int32
+        lib.ref_wave.argtypes = [C.c_int32, dp, dp, dp, C.c_int32, C.c_int32, fp, C.c_int32, C.c_int32,
+                                 C.POINTER(Uniforms)]
+        lib.ref_wave.restype = C.c_int32
+        _lib = lib
+    return _lib
+
+
+def uniforms(desc, mode: int = 0) -> Uniforms:
+    """The uniforms of a REFERENCE_3D scene description, with Main.cpp's
+    values for the fields the description does not carry (upper.w = 500,
+    lower.w = 50, Main.cpp:194-195)."""
+    u = Uniforms()
+    u.mass = desc.mass
+    u.smoothing_coeff = np.float32(desc.smoothing_length) / np.float32(desc.particle_radius)
+    u.visc = desc.visc
+    u.resting_rho = desc.rest_rho
+    u.upper[:] = [desc.box_hi[0], desc.box_hi[1], desc.box_hi[2], 500.0]
+    u.lower[:] = [desc.box_lo[0], desc.box_lo[1], desc.box_lo[2], 50.0]
+    u.attributes[:] = [desc.wave_lambda, desc.wave_atten, desc.wave_beta, desc.wave_mode]
+    u.time = 0.0
+    u.mode = mode
+    return u
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _fp(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _particle_pass(name: str, prec: int, p16: np.ndarray, wave: np.ndarray, u: Uniforms) -> np.ndarray:
+    lib = load()
+    out = np.ascontiguousarray(p16, dtype=np.float64).copy()
+    w = np.ascontiguousarray(wave, dtype=np.float32)
+    rc = getattr(lib, name)(prec, _dp(out), len(out), _fp(w), w.shape[1], w.shape[0], C.byref(u))
+    if rc != 0:
+        raise ValueError(f"{name}: {len(out)} particles (the shader loops over {NUM_PARTICLES})")
+    return out
+
+
+def rho_pres(prec, p16, wave, u):
+    return _particle_pass("ref_rho_pres", prec, p16, wave, u)
+
+
+def force(prec, p16, wave, u):
+    return _particle_pass("ref_force", prec, p16, wave, u)
+
+
+def integrate(prec, p16, wave, u):
+    return _particle_pass("ref_integrate", prec, p16, wave, u)
+
+
+def wave(prec, u_n, u_nm1, uni: Uniforms, init_rgba: np.ndarray | None = None) -> np.ndarray:
+    lib = load()
+    a = np.ascontiguousarray(u_n, dtype=np.float64)
+    b = np.ascontiguousarray(u_nm1, dtype=np.float64)
+    out = np.zeros_like(a)
+    img = None if init_rgba is None else np.ascontiguousarray(init_rgba, dtype=np.float32)
+    iw, ih = (0, 0) if img is None else (img.shape[1], img.shape[0])
+    rc = lib.ref_wave(prec, _dp(a), _dp(b), _dp(out), a.shape[1], a.shape[0], _fp(img), iw, ih, C.byref(uni))
+    if rc != 0:
+        raise ValueError("ref_wave failed")
+    return out
+
+
+# ----------------------------------------------------------- seeded inputs ----
+def uniform01(seed: int, n: int) -> np.ndarray:
+    """n doubles in [0, 1) from splitmix64 of (seed, index): integer
+    arithmetic only, so every host makes the same numbers."""
+    i = np.arange(n, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed) + (i + np.uint64(1)) * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def _u32(seed: int, n: int, lo: float, hi: float) -> np.ndarray:
+    return (lo + (hi - lo) * uniform01(seed, n)).astype(np.float32)
+
+
+def sph_state() -> np.ndarray:
+    """20480 particle records (float32 values): the reference's 64 x 5 x 64
+    cube (Main.cpp:735-778, spacing 2 * 0.85 * 0.005) with each position
+    jittered by up to 0.3 spacings, velocities in [-0.3, 0.3), a previous
+    step's force in [-500, 500) and the initial extras (1000, 0, 500, 50)."""
+    n = NUM_PARTICLES
+    sp = np.float32(2.0) * np.float32(0.85) * np.float32(0.005)
+    ii, jj, kk = np.meshgrid(np.arange(64), np.arange(5), np.arange(64), indexing="ij")
+    p = np.zeros((n, 16), np.float32)
+    p[:, 0] = ii.reshape(-1).astype(np.float32) * sp
+    p[:, 1] = jj.reshape(-1).astype(np.float32) * sp
+    p[:, 2] = kk.reshape(-1).astype(np.float32) * sp
+    for c in range(3):
+        p[:, c] += _u32(101 + c, n, -0.3, 0.3) * sp
+        p[:, 4 + c] = _u32(201 + c, n, -0.3, 0.3)
+        p[:, 8 + c] = _u32(301 + c, n, -500.0, 500.0)
+    p[:, 3] = 1.0
+    p[:, 11] = _u32(304, n, -10.0, 10.0)
+    p[:, 12:16] = [1000.0, 0.0, 500.0, 50.0]
+    return p
+
+
+def integrate_state(n: int = 1024) -> np.ndarray:
+    """n particle records spread over the reference box and a margin past its
+    walls (x, z in [-0.02, 0.5), y in [-0.04, 1.06)), velocities in [-5, 5)
+    with every 17th scaled past the foam speed 25, forces in [-3e4, 3e4),
+    rho in [900, 1100), p in [0, 4e5)."""
+    p = np.zeros((n, 16), np.float32)
+    p[:, 0] = _u32(401, n, -0.02, 0.5)
+    p[:, 1] = _u32(402, n, -0.04, 1.06)
+    p[:, 2] = _u32(403, n, -0.02, 0.5)
+    p[:, 3] = 1.0
+    for c in range(3):
+        p[:, 4 + c] = _u32(411 + c, n, -5.0, 5.0)
+        p[:, 8 + c] = _u32(421 + c, n, -3e4, 3e4)
+    p[::17, 4:7] *= np.float32(8.0)
+    p[:, 11] = _u32(424, n, -10.0, 10.0)
+    p[:, 12] = _u32(431, n, 900.0, 1100.0)
+    p[:, 13] = _u32(432, n, 0.0, 4e5)
+    p[:, 14:16] = [500.0, 50.0]
+    return p
+
+
+def height_field(seed: int, w: int, h: int, amp: float = 0.02) -> np.ndarray:
+    """A w x h field: two Gaussian bumps of height amp plus noise of amp/4."""
+    x = (np.arange(w, dtype=np.float64) + 0.5) / w
+    z = (np.arange(h, dtype=np.float64) + 0.5) / h
+    X, Z = np.meshgrid(x, z)
+    f = amp * (np.exp(-((X - 0.3) ** 2 + (Z - 0.4) ** 2) / 0.02) + 0.6 * np.exp(-((X - 0.75) ** 2 + (Z - 0.7) ** 2) / 0.01))
+    f += (amp / 4) * (uniform01(seed, w * h).reshape(h, w) - 0.5)
+    return f.astype(np.float32)
+
+
+def fixture_inputs(splash_rgba8: np.ndarray) -> dict[str, np.ndarray]:
+    """Every input of tests/golden/ref_shader_outputs.npz (its cases are
+    listed in tests/golden/make_ref_shader_golden.py).  splash_rgba8: the
+    reference's splash init texture, (64, 64, 4) uint8."""
+    un64 = height_field(11, 64, 64, amp=0.4)
+    un67 = height_field(13, 67, 45, amp=0.4)
+    return {
+        "sph": sph_state(),
+        "sph_wave": height_field(7, 64, 64),
+        "integ": integrate_state(512),
+        "evolve64_un": un64,
+        "evolve64_unm1": (un64 * np.float32(0.93)).astype(np.float32),
+        "evolve67_un": un67,
+        "evolve67_unm1": (un67 * np.float32(0.93)).astype(np.float32),
+        # GL's UNORM8 -> float: c / 255, rounded once
+        "image_rgba": (np.asarray(splash_rgba8).astype(np.float64) / 255.0).astype(np.float32),
+    }

@@ -1,0 +1,336 @@
+// glsl.h — the GLSL 4.50 types and built-in functions that the reference's
+// compute shaders use, so that their source compiles as C++.
+//
+// TEST INFRASTRUCTURE ONLY: it lets the oracle be checked against the
+// reference's own shader code run on the CPU (oracle/ref_shaders/).  The
+// product never includes it.
+//
+// Two arithmetic precisions share one set of types:
+//   glsl::f32 — the shaders' float arithmetic, one rounding per operation
+//               (built with -ffp-contract=off);
+//   glsl::f64 — the same source with float promoted to double.
+// Built-ins follow the GLSL 4.50 specification, section 8 (length = sqrt of
+// the dot product, normalize = v / length(v), smoothstep's Hermite formula,
+// distance = length(p0 - p1)).  Texture lookups follow the GL 4.5 core
+// specification, section 8.14: GL_LINEAR with GL_CLAMP_TO_EDGE, texel
+// centres at (i + 1/2) / size, weights in full precision (hardware filter
+// units quantise them; that difference is outside this check).
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+
+#include <utility>
+
+namespace glsl {
+
+// ---------------------------------------------------------- swizzles ----
+// A swizzle is a union member over the vector's storage: reading converts to
+// the vector type V it names, assigning writes the named components.
+template <class V, class S, int N, int... I>
+struct Swz {
+  S e[N];
+  operator V() const { return V(e[I]...); }
+  Swz& operator=(const V& v) {
+    assign(v, std::make_integer_sequence<int, (int)sizeof...(I)>());
+    return *this;
+  }
+  // a.xyz = b.xyz writes the named components only
+  Swz& operator=(const Swz& o) { return *this = V(o); }
+
+ private:
+  template <int... K>
+  void assign(const V& v, std::integer_sequence<int, K...>) {
+    const S t[] = {v[K]...};
+    ((e[I] = t[K]), ...);
+  }
+};
+
+template <class S> struct tvec2;
+template <class S> struct tvec3;
+template <class S> struct tvec4;
+
+#define GLSL_VEC_COMMON(T, N)                                                      \
+  S& operator[](int k) { return e[k]; }                                            \
+  const S& operator[](int k) const { return e[k]; }                                \
+  T& operator+=(const T& o) { for (int k = 0; k < N; ++k) e[k] = e[k] + o.e[k]; return *this; } \
+  T& operator-=(const T& o) { for (int k = 0; k < N; ++k) e[k] = e[k] - o.e[k]; return *this; } \
+  T& operator*=(const T& o) { for (int k = 0; k < N; ++k) e[k] = e[k] * o.e[k]; return *this; } \
+  T& operator/=(const T& o) { for (int k = 0; k < N; ++k) e[k] = e[k] / o.e[k]; return *this; } \
+  T& operator*=(S s) { for (int k = 0; k < N; ++k) e[k] = e[k] * s; return *this; }            \
+  T& operator/=(S s) { for (int k = 0; k < N; ++k) e[k] = e[k] / s; return *this; }            \
+  friend T operator+(const T& a, const T& b) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] + b.e[k]; return r; } \
+  friend T operator-(const T& a, const T& b) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] - b.e[k]; return r; } \
+  friend T operator*(const T& a, const T& b) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] * b.e[k]; return r; } \
+  friend T operator/(const T& a, const T& b) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] / b.e[k]; return r; } \
+  friend T operator*(const T& a, S s) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] * s; return r; }             \
+  friend T operator*(S s, const T& a) { T r; for (int k = 0; k < N; ++k) r.e[k] = s * a.e[k]; return r; }             \
+  friend T operator/(const T& a, S s) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] / s; return r; }             \
+  friend T operator-(const T& a) { T r; for (int k = 0; k < N; ++k) r.e[k] = -a.e[k]; return r; }
+
+template <class S>
+struct tvec2 {
+  union {
+    struct { S x, y; };
+    struct { S r, g; };
+    S e[2];
+  };
+  tvec2() { e[0] = e[1] = S(0); }
+  explicit tvec2(S s) { e[0] = e[1] = s; }
+  tvec2(S a, S b) { e[0] = a; e[1] = b; }
+  tvec2(const tvec2& o) { e[0] = o.e[0]; e[1] = o.e[1]; }
+  tvec2& operator=(const tvec2& o) { e[0] = o.e[0]; e[1] = o.e[1]; return *this; }
+  GLSL_VEC_COMMON(tvec2, 2)
+};
+
+template <class S>
+struct tvec3 {
+  union {
+    struct { S x, y, z; };
+    struct { S r, g, b; };
+    S e[3];
+    Swz<tvec2<S>, S, 3, 0, 2> xz;
+    Swz<tvec2<S>, S, 3, 0, 1> xy;
+  };
+  tvec3() { e[0] = e[1] = e[2] = S(0); }
+  explicit tvec3(S s) { e[0] = e[1] = e[2] = s; }
+  tvec3(S a, S b, S c) { e[0] = a; e[1] = b; e[2] = c; }
+  tvec3(const tvec3& o) { for (int k = 0; k < 3; ++k) e[k] = o.e[k]; }
+  tvec3& operator=(const tvec3& o) { for (int k = 0; k < 3; ++k) e[k] = o.e[k]; return *this; }
+  GLSL_VEC_COMMON(tvec3, 3)
+};
+
+template <class S>
+struct tvec4 {
+  union {
+    struct { S x, y, z, w; };
+    struct { S r, g, b, a; };
+    S e[4];
+    Swz<tvec3<S>, S, 4, 0, 1, 2> xyz;
+    Swz<tvec2<S>, S, 4, 0, 2> xz;
+    Swz<tvec2<S>, S, 4, 0, 1> xy;
+  };
+  tvec4() { e[0] = e[1] = e[2] = e[3] = S(0); }
+  explicit tvec4(S s) { e[0] = e[1] = e[2] = e[3] = s; }
+  tvec4(S a, S b, S c, S d) { e[0] = a; e[1] = b; e[2] = c; e[3] = d; }
+  tvec4(const tvec4& o) { for (int k = 0; k < 4; ++k) e[k] = o.e[k]; }
+  tvec4& operator=(const tvec4& o) { for (int k = 0; k < 4; ++k) e[k] = o.e[k]; return *this; }
+  GLSL_VEC_COMMON(tvec4, 4)
+};
+
+#undef GLSL_VEC_COMMON
+
+template <class S>
+struct tmat4 {
+  S m[16];
+  tmat4() { for (int k = 0; k < 16; ++k) m[k] = S(0); }
+};
+
+struct bvec2 {
+  bool x, y;
+};
+
+struct uvec2 {
+  unsigned x, y;
+  uvec2() : x(0), y(0) {}
+  uvec2(unsigned a, unsigned b) : x(a), y(b) {}
+  unsigned operator[](int k) const { return k == 0 ? x : y; }
+};
+
+struct uvec3 {
+  union {
+    struct { unsigned x, y, z; };
+    unsigned e[3];
+    Swz<uvec2, unsigned, 3, 0, 1> xy;
+  };
+  uvec3() { e[0] = e[1] = e[2] = 0u; }
+  uvec3(unsigned a, unsigned b, unsigned c) { e[0] = a; e[1] = b; e[2] = c; }
+  uvec3(const uvec3& o) { for (int k = 0; k < 3; ++k) e[k] = o.e[k]; }
+  uvec3& operator=(const uvec3& o) { for (int k = 0; k < 3; ++k) e[k] = o.e[k]; return *this; }
+};
+
+// ivec2 converts implicitly to the float vectors, as GLSL converts int
+// arguments of the float built-ins (distance(ivec2, ivec2)).
+struct ivec2 {
+  union {
+    struct { int x, y; };
+    int e[2];
+    Swz<ivec2, int, 2, 0, 1> xy;
+  };
+  ivec2() { e[0] = e[1] = 0; }
+  explicit ivec2(int s) { e[0] = e[1] = s; }
+  ivec2(int a, int b) { e[0] = a; e[1] = b; }
+  explicit ivec2(const uvec2& u) { e[0] = (int)u.x; e[1] = (int)u.y; }
+  explicit ivec2(const tvec2<float>& v) { e[0] = (int)v.e[0]; e[1] = (int)v.e[1]; }
+  explicit ivec2(const tvec2<double>& v) { e[0] = (int)v.e[0]; e[1] = (int)v.e[1]; }
+  ivec2(const ivec2& o) { e[0] = o.e[0]; e[1] = o.e[1]; }
+  ivec2& operator=(const ivec2& o) { e[0] = o.e[0]; e[1] = o.e[1]; return *this; }
+  int& operator[](int k) { return e[k]; }
+  int operator[](int k) const { return e[k]; }
+  operator tvec2<float>() const { return tvec2<float>((float)e[0], (float)e[1]); }
+  operator tvec2<double>() const { return tvec2<double>((double)e[0], (double)e[1]); }
+  friend ivec2 operator+(const ivec2& a, const ivec2& b) { return ivec2(a.e[0] + b.e[0], a.e[1] + b.e[1]); }
+  friend ivec2 operator-(const ivec2& a, const ivec2& b) { return ivec2(a.e[0] - b.e[0], a.e[1] - b.e[1]); }
+  friend ivec2 operator*(const ivec2& a, const ivec2& b) { return ivec2(a.e[0] * b.e[0], a.e[1] * b.e[1]); }
+  // float * ivec2: the int vector converts to a float vector first
+  friend tvec2<float> operator*(float s, const ivec2& a) { return tvec2<float>(s * (float)a.e[0], s * (float)a.e[1]); }
+  friend tvec2<double> operator*(double s, const ivec2& a) {
+    return tvec2<double>(s * (double)a.e[0], s * (double)a.e[1]);
+  }
+};
+
+inline ivec2 clamp(const ivec2& v, const ivec2& lo, const ivec2& hi) {
+  ivec2 r;
+  for (int k = 0; k < 2; ++k) r.e[k] = v.e[k] < lo.e[k] ? lo.e[k] : (v.e[k] > hi.e[k] ? hi.e[k] : v.e[k]);
+  return r;
+}
+inline bvec2 greaterThanEqual(const ivec2& a, const ivec2& b) { return bvec2{a.x >= b.x, a.y >= b.y}; }
+inline bool any(const bvec2& b) { return b.x || b.y; }
+
+// ---------------------------------------------------- textures, images ----
+// A bound texture: w x h texels of `comps` floats (1: the red channel only,
+// green, blue and alpha read 0, 1 reads 1 for alpha as GL does for a
+// one-channel format; 4: RGBA).
+struct sampler2D {
+  const float* texels = nullptr;
+  int w = 0, h = 0, comps = 1;
+  float at(int x, int y, int c) const {
+    if (c < comps) return texels[((size_t)y * w + x) * comps + c];
+    return c == 3 ? 1.0f : 0.0f;
+  }
+};
+
+inline ivec2 textureSize(const sampler2D& s, int) { return ivec2(s.w, s.h); }
+
+// A bound image2D, rgba32f: w x h texels of 4 scalars, float or double.
+struct image2D {
+  void* data = nullptr;
+  int w = 0, h = 0;
+  bool is_double = false;
+};
+
+inline ivec2 imageSize(const image2D& im) { return ivec2(im.w, im.h); }
+
+namespace detail {
+
+template <class S>
+tvec4<S> filter_linear(const sampler2D& t, S s, S u) {
+  // GL 4.5 core, 8.14.2: u' = s * w - 1/2, i0 = floor(u'), alpha = frac(u'),
+  // each index clamped to [0, w - 1] (GL_CLAMP_TO_EDGE)
+  const S us = s * (S)t.w - (S)0.5, vs = u * (S)t.h - (S)0.5;
+  const S fi = floor(us), fj = floor(vs);
+  const S a = us - fi, b = vs - fj;
+  auto cl = [](long v, int n) { return (int)(v < 0 ? 0 : (v > n - 1 ? n - 1 : v)); };
+  const long i0 = (long)fi, j0 = (long)fj;
+  const int x0 = cl(i0, t.w), x1 = cl(i0 + 1, t.w), y0 = cl(j0, t.h), y1 = cl(j0 + 1, t.h);
+  tvec4<S> r;
+  for (int c = 0; c < 4; ++c) {
+    const S t00 = t.at(x0, y0, c), t10 = t.at(x1, y0, c), t01 = t.at(x0, y1, c), t11 = t.at(x1, y1, c);
+    r.e[c] = ((S)1 - a) * ((S)1 - b) * t00 + a * ((S)1 - b) * t10 + ((S)1 - a) * b * t01 + a * b * t11;
+  }
+  return r;
+}
+
+template <class S>
+tvec4<S> image_load(const image2D& im, const ivec2& p) {
+  tvec4<S> r;  // out of range: zero (GLSL 4.50, 8.12)
+  if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return r;
+  const size_t o = ((size_t)p.y * im.w + p.x) * 4;
+  for (int c = 0; c < 4; ++c)
+    r.e[c] = im.is_double ? (S) static_cast<const double*>(im.data)[o + c] : (S) static_cast<const float*>(im.data)[o + c];
+  return r;
+}
+
+template <class S>
+void image_store(const image2D& im, const ivec2& p, const tvec4<S>& v) {
+  if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return;  // ignored out of range
+  const size_t o = ((size_t)p.y * im.w + p.x) * 4;
+  for (int c = 0; c < 4; ++c) {
+    if (im.is_double)
+      static_cast<double*>(im.data)[o + c] = (double)v.e[c];
+    else
+      static_cast<float*>(im.data)[o + c] = (float)v.e[c];
+  }
+}
+
+}  // namespace detail
+
+// ------------------------------------------------ per-precision built-ins ----
+#define GLSL_BUILTINS(S, NS)                                                                  \
+  namespace NS {                                                                              \
+  using vec2 = tvec2<S>;                                                                      \
+  using vec3 = tvec3<S>;                                                                      \
+  using vec4 = tvec4<S>;                                                                      \
+  using mat4 = tmat4<S>;                                                                      \
+  inline S pow(S a, S b) { return ::pow(a, b); }                                              \
+  inline S sqrt(S a) { return ::sqrt(a); }                                                    \
+  inline S abs(S a) { return ::fabs(a); }                                                     \
+  inline S max(S a, S b) { return b > a ? b : a; } /* GLSL: y if x < y, else x */             \
+  inline S min(S a, S b) { return b < a ? b : a; }                                            \
+  inline S clamp(S x, S lo, S hi) { return min(max(x, lo), hi); }                             \
+  inline S smoothstep(S e0, S e1, S x) {                                                      \
+    const S t = clamp((x - e0) / (e1 - e0), (S)0, (S)1);                                      \
+    return t * t * ((S)3 - (S)2 * t);                                                         \
+  }                                                                                           \
+  inline S dot(const vec2& a, const vec2& b) { return a.x * b.x + a.y * b.y; }                \
+  inline S dot(const vec3& a, const vec3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }    \
+  inline S length(const vec2& v) { return sqrt(dot(v, v)); }                                  \
+  inline S length(const vec3& v) { return sqrt(dot(v, v)); }                                  \
+  inline S distance(const vec2& a, const vec2& b) { return length(a - b); }                   \
+  inline vec3 normalize(const vec3& v) { return v / length(v); }                              \
+  inline vec3 cross(const vec3& a, const vec3& b) {                                           \
+    return vec3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);         \
+  }                                                                                           \
+  inline vec4 texture(const sampler2D& t, const vec2& uv) { return detail::filter_linear<S>(t, uv.x, uv.y); } \
+  inline vec4 texelFetch(const sampler2D& t, const ivec2& p, int) {                           \
+    vec4 r;                                                                                   \
+    if (p.x < 0 || p.y < 0 || p.x >= t.w || p.y >= t.h) return r;                             \
+    for (int c = 0; c < 4; ++c) r.e[c] = (S)t.at(p.x, p.y, c);                                \
+    return r;                                                                                 \
+  }                                                                                           \
+  inline vec4 imageLoad(const image2D& im, const ivec2& p) { return detail::image_load<S>(im, p); } \
+  inline void imageStore(const image2D& im, const ivec2& p, const vec4& v) { detail::image_store<S>(im, p, v); } \
+  }
+
+GLSL_BUILTINS(float, f32)
+GLSL_BUILTINS(double, f64)
+#undef GLSL_BUILTINS
+
+}  // namespace glsl
+
+// Opens a shader's namespace body: its types and built-ins at precision NS
+// (f32 or f64), found by ordinary lookup ahead of the C library's names, and
+// the invocation id that the dispatch loop sets.
+#define GLSL_PRELUDE(NS)                                                                  \
+  using glsl::bvec2;                                                                      \
+  using glsl::ivec2;                                                                      \
+  using glsl::uvec3;                                                                      \
+  using glsl::sampler2D;                                                                  \
+  using glsl::image2D;                                                                    \
+  using glsl::NS::vec2;                                                                   \
+  using glsl::NS::vec3;                                                                   \
+  using glsl::NS::vec4;                                                                   \
+  using glsl::NS::mat4;                                                                   \
+  using glsl::NS::pow;                                                                    \
+  using glsl::NS::sqrt;                                                                   \
+  using glsl::NS::abs;                                                                    \
+  using glsl::NS::max;                                                                    \
+  using glsl::NS::min;                                                                    \
+  using glsl::NS::clamp;                                                                  \
+  using glsl::clamp;                                                                      \
+  using glsl::NS::smoothstep;                                                             \
+  using glsl::NS::dot;                                                                    \
+  using glsl::NS::length;                                                                 \
+  using glsl::NS::distance;                                                               \
+  using glsl::NS::normalize;                                                              \
+  using glsl::NS::cross;                                                                  \
+  using glsl::NS::texture;                                                                \
+  using glsl::NS::texelFetch;                                                             \
+  using glsl::NS::imageLoad;                                                              \
+  using glsl::NS::imageStore;                                                             \
+  using glsl::textureSize;                                                                \
+  using glsl::imageSize;                                                                  \
+  using glsl::greaterThanEqual;                                                           \
+  using glsl::any;                                                                        \
+  typedef unsigned int uint;                                                              \
+  thread_local uvec3 gl_GlobalInvocationID;

@@ -1,0 +1,91 @@
+// ref_shaders.h — the reference's four compute shaders
+// (CoupledWaterAnimation/{rho_pres,force,integrate,wave}_comp.glsl) compiled
+// as C++ and dispatched on the CPU.  TEST INFRASTRUCTURE ONLY: the oracle's
+// check against the reference's own code.  Built from the reference's
+// sources into oracle/_ref/ (oracle/ref_shaders/Makefile); nothing under
+// oracle/_ref/ is committed.
+//
+// prec 0 runs the shaders' float arithmetic, prec 1 the same source with
+// float promoted to double.  Particles are n records of 16 doubles (pos,
+// vel, force, extras: the shaders' Particle, CoupledWaterAnimation/
+// rho_pres_comp.glsl:16-22); heights are the red channel of the wave image,
+// row-major w x h (row = texture t).  Every call returns 0, or -1 when n is
+// not what the shader's NUM_PARTICLES loop needs.
+#pragma once
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// The uniform blocks the shaders read (Main.cpp binds them; names as in the
+// shaders): ConstantsUniform, BoundaryUniform, WaveUniforms, and the loose
+// uniforms time and uMode.
+typedef struct ref_uniforms {
+  float mass, smoothing_coeff, visc, resting_rho;
+  float upper[4], lower[4];
+  float attributes[4], mesh_ws_pos[4];
+  float time;
+  int32_t mode;
+} ref_uniforms;
+
+// rho_pres_comp.glsl over all NUM_PARTICLES (20480) particles: writes extras.x, .y.
+int32_t ref_rho_pres(int32_t prec, double* p16, int32_t n, const float* wave, int32_t w, int32_t h,
+                     const ref_uniforms* u);
+// force_comp.glsl over all NUM_PARTICLES particles: writes force.
+int32_t ref_force(int32_t prec, double* p16, int32_t n, const float* wave, int32_t w, int32_t h,
+                  const ref_uniforms* u);
+// integrate_comp.glsl over the first n <= NUM_PARTICLES particles.
+int32_t ref_integrate(int32_t prec, double* p16, int32_t n, const float* wave, int32_t w, int32_t h,
+                      const ref_uniforms* u);
+// wave_comp.glsl in mode u->mode (0 InitWave, 1 InitFromImage, 2 EvolveWave)
+// over a w x h image: u_n is image 0 (t-1), u_nm1 image 1 (t-2), the result
+// the output image's red channel.  init_rgba: iw x ih RGBA texels (already
+// normalised to [0, 1]) for InitFromImage, else null.
+int32_t ref_wave(int32_t prec, const double* u_n, const double* u_nm1, double* out, int32_t w, int32_t h,
+                 const float* init_rgba, int32_t iw, int32_t ih, const ref_uniforms* u);
+
+#ifdef __cplusplus
+}
+
+#include <stddef.h>
+
+#include <vector>
+
+namespace ref_shaders {
+
+template <class P>
+void load_particles(std::vector<P>& v, const double* p16, int n) {
+  v.resize((size_t)n);
+  for (int i = 0; i < n; ++i) {
+    const double* q = p16 + 16 * (size_t)i;
+    for (int c = 0; c < 4; ++c) {
+      v[i].pos.e[c] = q[c];
+      v[i].vel.e[c] = q[4 + c];
+      v[i].force.e[c] = q[8 + c];
+      v[i].extras.e[c] = q[12 + c];
+    }
+  }
+}
+
+template <class P>
+void store_particles(const std::vector<P>& v, double* p16, int n) {
+  for (int i = 0; i < n; ++i) {
+    double* q = p16 + 16 * (size_t)i;
+    for (int c = 0; c < 4; ++c) {
+      q[c] = v[i].pos.e[c];
+      q[4 + c] = v[i].vel.e[c];
+      q[8 + c] = v[i].force.e[c];
+      q[12 + c] = v[i].extras.e[c];
+    }
+  }
+}
+
+template <class V>
+V vec4_of(const float* a) {
+  return V(a[0], a[1], a[2], a[3]);
+}
+
+}  // namespace ref_shaders
+#endif

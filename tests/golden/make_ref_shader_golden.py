@@ -1,0 +1,106 @@
+"""Regenerate tests/golden/ref_shader_outputs.npz: outputs of the reference's
+own compute shaders (CoupledWaterAnimation/rho_pres_comp.glsl,
+force_comp.glsl, integrate_comp.glsl, wave_comp.glsl) run on the CPU, on the
+seeded inputs of oracle/ref.py.
+
+The shaders are compiled as C++ (oracle/ref_shaders/: the GLSL source with
+its declarations rewritten, against a GLSL types-and-built-ins header) in
+two precisions: "f32", the shaders' float arithmetic with one rounding per
+operation, and "f64", the same source with float promoted to double.  The
+reference's constants stay float literals in both.
+
+Cases (every input regenerates from oracle/ref.py; its SHA-256 is stored):
+  sph      20,480 particles (the reference's 64 x 5 x 64 cube, jittered) on a
+           64 x 64 height field: rho_pres, then force on each precision's own
+           rho_pres output; stored for every 20th particle;
+  integ    512 particles spread over the box and past its walls (foam,
+           walls and surface branches): integrate, all outputs, in wave
+           mode 1 and in mode 0.5 (which adds the ceiling);
+  evolve   EvolveWave on 64 x 64 fields (wave modes 1 and 0.5) and on a
+           67 x 45 field (mode 0.5: the line source at x = 33);
+  init     InitWave for modes 1, 0 and 0.5 on 64 x 64 and mode 0.5 on 67 x 45;
+  image    InitFromImage of the reference's splash texture on a 32 x 64 field.
+
+Usage:  python tests/golden/make_ref_shader_golden.py
+        (needs the reference checkout; CWA_REFERENCE names it if it is not
+        at the default place oracle/ref.py looks)
+"""
+from __future__ import annotations
+
+import hashlib
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+OUT = HERE / "ref_shader_outputs.npz"
+SPH_SAMPLE = np.arange(0, 20480, 20)
+WAVE_MODES = {"m1": 1.0, "m0": 0.0, "m05": 0.5}
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def reference_desc():
+    import coupledwateranimation_gb300._abi as abi
+    from oracle import oracle as orc
+    return orc.scene_defaults(abi.PRESET_REFERENCE_3D, 0.0, abi.SceneDesc)
+
+
+def inputs() -> dict[str, np.ndarray]:
+    from oracle import ref
+    return ref.fixture_inputs(np.load(HERE / "init_textures.npz")["splash"])
+
+
+def main() -> None:
+    from oracle import ref
+    if ref.build() is None or ref.load() is None:
+        sys.exit("the reference checkout is needed (set CWA_REFERENCE)")
+    d = reference_desc()
+    x = inputs()
+    out: dict[str, np.ndarray] = {"sph_sample": SPH_SAMPLE}
+    for k, v in x.items():
+        out[f"sha_{k}"] = np.array(sha(v))
+    u = ref.uniforms(d)
+    sph64 = x["sph"].astype(np.float64)
+    for prec, tag, dt in ((ref.F32, "f32", np.float32), (ref.F64, "f64", np.float64)):
+        r = ref.rho_pres(prec, sph64, x["sph_wave"], u)
+        f = ref.force(prec, r, x["sph_wave"], u)
+        out[f"rho_{tag}"] = r[SPH_SAMPLE, 12:14].astype(dt)
+        out[f"force_{tag}"] = f[SPH_SAMPLE, 8:12].astype(dt)
+        out[f"integ_{tag}"] = ref.integrate(prec, x["integ"].astype(np.float64), x["sph_wave"], u).astype(dt)
+        d.wave_mode = 0.5  # the line-source mode adds the ceiling (integrate_comp.glsl:170-177)
+        out[f"integ_m05_{tag}"] = ref.integrate(prec, x["integ"].astype(np.float64), x["sph_wave"],
+                                                ref.uniforms(d)).astype(dt)
+        d.wave_mode = 1.0
+    for size in ("64", "67"):
+        un, unm1 = x[f"evolve{size}_un"], x[f"evolve{size}_unm1"]
+        for mk, mode in WAVE_MODES.items():
+            if mk == "m0" or (size == "67" and mk != "m05"):
+                continue
+            d.wave_mode = mode
+            uw = ref.uniforms(d, mode=2)
+            out[f"evolve{size}_{mk}_f32"] = ref.wave(ref.F32, un, unm1, uw).astype(np.float32)
+            if size == "64":
+                out[f"evolve{size}_{mk}_f64"] = ref.wave(ref.F64, un, unm1, uw)
+    for size, (w, h) in (("64", (64, 64)), ("67", (67, 45))):
+        z = np.zeros((h, w))
+        for mk, mode in WAVE_MODES.items():
+            if size == "67" and mk != "m05":
+                continue
+            d.wave_mode = mode
+            out[f"init{size}_{mk}_f32"] = ref.wave(ref.F32, z, z, ref.uniforms(d, mode=0)).astype(np.float32)
+    d.wave_mode = 1.0
+    z = np.zeros((64, 32))
+    out["image_f32"] = ref.wave(ref.F32, z, z, ref.uniforms(d, mode=1), init_rgba=x["image_rgba"]).astype(np.float32)
+    np.savez_compressed(OUT, **out)
+    print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
+
+
+if __name__ == "__main__":
+    main()

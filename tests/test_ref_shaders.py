@@ -1,0 +1,203 @@
+"""The oracle against the reference's own compute shaders.
+
+tests/golden/ref_shader_outputs.npz holds outputs of
+CoupledWaterAnimation/{rho_pres,force,integrate,wave}_comp.glsl compiled as
+C++ and run on the CPU (tests/golden/make_ref_shader_golden.py), in the
+shaders' float arithmetic ("f32") and with float promoted to double ("f64").
+These tests pin the oracle to them:
+  * the FP64 oracle (brute-force neighbour loops, integrate, EvolveWave)
+    computes the shaders' expressions on the shaders' constants: it equals
+    the f64 shader outputs to a few units of double rounding;
+  * the float32 restatements (integrate_f32, wave_f32, wave_init_f32,
+    wave_from_image_f32) equal the f32 shader outputs bit for bit, except
+    where the restatement associates a sum differently (the bilinear texture
+    weights, the stencil's neighbour sum), where they agree within a few
+    float32 roundings of the operands;
+  * where the reference checkout is present, the shaders are rebuilt and
+    rerun and reproduce the fixtures bit for bit.
+"""
+from __future__ import annotations
+
+import hashlib
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from coupledwateranimation_gb300 import _abi
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+G = np.load(GOLDEN / "ref_shader_outputs.npz")
+
+
+def _sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.fixture(scope="module")
+def x():
+    from oracle import ref
+    return ref.fixture_inputs(np.load(GOLDEN / "init_textures.npz")["splash"])
+
+
+@pytest.fixture(scope="module")
+def desc(orc):
+    return orc.scene_defaults(_abi.PRESET_REFERENCE_3D, 0.0, _abi.SceneDesc)
+
+
+def _normwise(got, want):
+    return float(np.max(np.abs(got - want)) / np.max(np.abs(want)))
+
+
+def _ulps(got32, want32):
+    """Distance in float32 ulps, element-wise."""
+    a = np.ascontiguousarray(got32, np.float32).view(np.int32).astype(np.int64)
+    b = np.ascontiguousarray(want32, np.float32).view(np.int32).astype(np.int64)
+    a = np.where(a < 0, -(a & 0x7FFFFFFF), a)  # two's-complement order of floats
+    b = np.where(b < 0, -(b & 0x7FFFFFFF), b)
+    return np.abs(a - b)
+
+
+def test_inputs_regenerate_bit_exactly(x):
+    for k, v in x.items():
+        assert _sha(v) == str(G[f"sha_{k}"]), f"input {k} differs from the one the fixtures were made on"
+
+
+def test_fp64_oracle_density_and_force_equal_the_shaders(orc, x, desc):
+    """rho_pres_comp.glsl:49-81 and force_comp.glsl:62-115 over all 20,480
+    particles (the shaders' all-pairs loops) against the oracle's brute-force
+    mode: per-particle relative 1e-14 for rho, normwise 1e-14 for p and force."""
+    s = G["sph_sample"]
+    p = x["sph"].astype(np.float64)
+    w = x["sph_wave"].astype(np.float64)
+    orc.rho_pres(desc, p, w, brute=True)
+    want = G["rho_f64"]
+    assert np.max(np.abs(p[s, 12] - want[:, 0]) / want[:, 0]) <= 1e-14
+    assert _normwise(p[s, 13], want[:, 1]) <= 1e-14
+    orc.force(desc, p, w, brute=True)
+    for c in range(3):
+        assert _normwise(p[s, 8 + c], G["force_f64"][:, c]) <= 1e-14, c
+    assert np.array_equal(p[s, 11], G["force_f64"][:, 3])  # w: the stored force's w, / 0.25 on crests
+    # the float32 shaders are within float rounding of it
+    assert np.max(np.abs(G["rho_f32"][:, 0] - want[:, 0]) / want[:, 0]) <= 1e-6
+    for c in range(3):
+        assert _normwise(G["force_f32"][:, c].astype(np.float64), G["force_f64"][:, c]) <= 1e-6
+
+
+@pytest.mark.parametrize("mode", [1.0, 0.5])
+def test_fp64_oracle_integrate_equals_the_shader(orc, x, desc, mode):
+    """integrate_comp.glsl:56-92 with CheckBoundary (:135-177)."""
+    desc.wave_mode = mode
+    try:
+        p = x["integ"].astype(np.float64)
+        orc.integrate(desc, p, x["sph_wave"].astype(np.float64))
+    finally:
+        desc.wave_mode = 1.0
+    want = G["integ_f64" if mode == 1.0 else "integ_m05_f64"]
+    scale = np.maximum(np.abs(want), 1.0)
+    assert np.max(np.abs(p - want) / scale) <= 1e-14
+
+
+@pytest.mark.parametrize("case,mode", [("evolve64_m1", 1.0), ("evolve64_m05", 0.5)])
+def test_fp64_oracle_wave_equals_the_shader(orc, x, desc, case, mode):
+    """EvolveWave with get_clamp and the line source (wave_comp.glsl:171-206)."""
+    desc.wave_mode = mode
+    try:
+        got = orc.wave(desc, x["evolve64_un"], x["evolve64_unm1"])
+    finally:
+        desc.wave_mode = 1.0
+    assert np.max(np.abs(got - G[f"{case}_f64"])) <= 1e-16
+
+
+@pytest.mark.parametrize("mode", [1.0, 0.5])
+def test_float32_integrate_equals_the_shader(orc, x, desc, mode):
+    """The float32 restatement (the CUDA kernel's arithmetic) against the f32
+    shader: bit-exact but for the bilinear surface sample, whose weights the
+    restatement applies as two nested lerps, not the GL formula's four
+    products (a few ulps of the height field on the rows projected to the
+    surface)."""
+    desc.wave_mode = mode
+    try:
+        got, _ = orc.integrate_f32(desc, x["integ"], x["sph_wave"], with_deposits=False)
+    finally:
+        desc.wave_mode = 1.0
+    want = G["integ_f32" if mode == 1.0 else "integ_m05_f32"]
+    # the sample only sets y = height - radius (integrate_comp.glsl:79-83)
+    other = [c for c in range(16) if c != 1]
+    assert np.array_equal(got[:, other].view(np.uint32), want[:, other].view(np.uint32))
+    dy = np.abs(got[:, 1].astype(np.float64) - want[:, 1])
+    assert np.count_nonzero(dy) <= len(got) // 20, f"{np.count_nonzero(dy)} heights differ"
+    assert dy.max() <= 4 * np.finfo(np.float32).eps * np.abs(x["sph_wave"]).max()
+
+
+@pytest.mark.parametrize("case,size,mode", [("evolve64_m1", "64", 1.0), ("evolve64_m05", "64", 0.5),
+                                            ("evolve67_m05", "67", 0.5)])
+def test_float32_wave_equals_the_shader(orc, x, desc, case, size, mode):
+    """The float32 stencil (the CUDA kernels' arithmetic) sums the four
+    neighbours as (n + s) + (e + w) and folds the constant coefficients in
+    double; the shader sums left to right in float: within two float32
+    roundings of the field's magnitude."""
+    un = x[f"evolve{size}_un"]
+    desc.wave_nx, desc.wave_nz = un.shape[1], un.shape[0]
+    desc.wave_mode = mode
+    try:
+        got = orc.wave_f32(desc, un, x[f"evolve{size}_unm1"])
+    finally:
+        desc.wave_nx = desc.wave_nz = 64
+        desc.wave_mode = 1.0
+    want = G[f"{case}_f32"]
+    scale = float(np.abs(un).max())
+    assert scale > 0.1
+    # a rounding of the neighbour sum, scaled by lambda and the attenuation
+    assert np.abs(got.astype(np.float64) - want).max() <= 2 * np.finfo(np.float32).eps * scale
+    assert np.mean(got == want) >= 0.9  # most cells round the same way
+    if mode == 0.5:  # the line source lifted the middle column in both
+        col = un.shape[1] // 2
+        lifted = want[:, col] > 0.0001 + 0.001
+        assert lifted.any() and np.array_equal(got[lifted, col] > 0.0011, lifted[lifted])
+
+
+@pytest.mark.parametrize("case,w,h,mode", [("init64_m1", 64, 64, 1.0), ("init64_m0", 64, 64, 0.0),
+                                           ("init64_m05", 64, 64, 0.5), ("init67_m05", 67, 45, 0.5)])
+def test_float32_wave_init_equals_the_shader_bit_exactly(orc, desc, case, w, h, mode):
+    """InitWave (wave_comp.glsl:82-140) for the splash, wave and wake modes."""
+    desc.wave_nx, desc.wave_nz, desc.wave_mode = w, h, mode
+    try:
+        got = orc.wave_init_f32(desc)
+    finally:
+        desc.wave_nx = desc.wave_nz = 64
+        desc.wave_mode = 1.0
+    assert np.array_equal(got.view(np.uint32), G[f"{case}_f32"].view(np.uint32))
+
+
+def test_float32_init_from_image_equals_the_shader_bit_exactly(orc):
+    """InitFromImage (wave_comp.glsl:76-80) of the reference's splash texture."""
+    tex = np.load(GOLDEN / "init_textures.npz")["splash"]
+    got = orc.wave_from_image_f32(32, 64, tex)
+    assert np.array_equal(got.view(np.uint32), G["image_f32"].view(np.uint32))
+
+
+def test_live_shaders_reproduce_the_fixtures(x, desc):
+    """With the reference checkout present: rebuild the shaders from its
+    source, rerun every case, and get the committed fixtures back bit for bit."""
+    from oracle import ref
+    if ref.build() is None or ref.load() is None:
+        pytest.skip("the reference checkout is not on this host")
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_ref_shader_golden", GOLDEN / "make_ref_shader_golden.py")
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    u = ref.uniforms(desc)
+    r = ref.rho_pres(ref.F64, x["sph"].astype(np.float64), x["sph_wave"], u)
+    assert np.array_equal(r[G["sph_sample"], 12:14], G["rho_f64"])
+    f = ref.force(ref.F32, ref.rho_pres(ref.F32, x["sph"].astype(np.float64), x["sph_wave"], u), x["sph_wave"], u)
+    assert np.array_equal(f[G["sph_sample"], 8:12].astype(np.float32), G["force_f32"])
+    i = ref.integrate(ref.F32, x["integ"].astype(np.float64), x["sph_wave"], u)
+    assert np.array_equal(i.astype(np.float32), G["integ_f32"])
+    desc.wave_mode = 0.5
+    try:
+        wv = ref.wave(ref.F64, x["evolve64_un"], x["evolve64_unm1"], ref.uniforms(desc, mode=2))
+    finally:
+        desc.wave_mode = 1.0
+    assert np.array_equal(wv, G["evolve64_m05_f64"])
+    assert mk.SPH_SAMPLE.tolist() == G["sph_sample"].tolist()
