@@ -68,6 +68,11 @@ def load():
         lib.ref_wave.argtypes = [C.c_int32, dp, dp, dp, C.c_int32, C.c_int32, fp, C.c_int32, C.c_int32,
                                  C.POINTER(Uniforms)]
         lib.ref_wave.restype = C.c_int32
+        ip = C.POINTER(C.c_int32)
+        lib.ref_exclusive_scan.argtypes = [ip, ip, C.c_int32]
+        lib.ref_exclusive_scan.restype = C.c_int32
+        lib.ref_grid_build.argtypes = [fp, C.c_int32, fp, fp, fp, ip, ip, ip, ip]
+        lib.ref_grid_build.restype = C.c_int32
         _lib = lib
     return _lib
 
@@ -130,6 +135,36 @@ def wave(prec, u_n, u_nm1, uni: Uniforms, init_rgba: np.ndarray | None = None) -
     if rc != 0:
         raise ValueError("ref_wave failed")
     return out
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def exclusive_scan(x: np.ndarray) -> np.ndarray:
+    """ParallelScan::Compute with prefix_sum_cs.glsl (n a power of two)."""
+    a = np.ascontiguousarray(x, np.int32)
+    out = np.zeros_like(a)
+    if load().ref_exclusive_scan(_ip(a), _ip(out), len(a)) != 0:
+        raise ValueError("the reference scan needs a power-of-two length")
+    return out
+
+
+def grid_build(pos4: np.ndarray, lo, hi, cell, dims):
+    """ugrid_particles_cs.glsl COMPUTE_COUNTS, the scan, INSERT_PARTICLES:
+    (counts, offsets, index list).  dims: (nx, ny, nz) with nx == nz and a
+    power-of-two product (what the reference's Index() and scan support)."""
+    p = np.ascontiguousarray(pos4, np.float32)
+    f = lambda v: np.ascontiguousarray(v, np.float32)  # noqa: E731
+    d = np.ascontiguousarray(dims, np.int32)
+    nc = int(np.prod(d))
+    counts, offsets, lst = np.zeros(nc, np.int32), np.zeros(nc, np.int32), np.zeros(len(p), np.int32)
+    lo_, hi_, cell_ = f(lo), f(hi), f(cell)
+    rc = load().ref_grid_build(_fp(p), len(p), _fp(lo_), _fp(hi_), _fp(cell_), _ip(d), _ip(counts), _ip(offsets),
+                               _ip(lst))
+    if rc != 0:
+        raise ValueError("the reference grid needs nx == nz and a power-of-two cell count")
+    return counts, offsets, lst
 
 
 # ----------------------------------------------------------- seeded inputs ----
@@ -202,6 +237,47 @@ def height_field(seed: int, w: int, h: int, amp: float = 0.02) -> np.ndarray:
     return f.astype(np.float32)
 
 
+def grid_points(seed: int, n: int, hi) -> np.ndarray:
+    """n float4 points over [-0.05, hi + 0.05) per axis (some outside the grid,
+    to be clamped), every 101st on a cell face (z = 0.25), w = 1."""
+    p = np.ones((n, 4), np.float32)
+    for c in range(3):
+        p[:, c] = _u32(seed + c, n, -0.05, float(hi[c]) + 0.05)
+    p[::101, 2] = np.float32(0.25)
+    return p
+
+
+def lattice_points(seed: int, dims, spacing: float, jitter: float) -> np.ndarray:
+    """A jittered lattice of float4 points (a dam-break block), w = 1."""
+    ii, jj, kk = np.meshgrid(*(np.arange(d) for d in dims), indexing="ij")
+    n = ii.size
+    p = np.ones((n, 4), np.float32)
+    for c, g in enumerate((ii, jj, kk)):
+        p[:, c] = (np.float32(spacing) * (g.reshape(-1).astype(np.float32) + np.float32(0.5))
+                   + _u32(seed + c, n, -jitter, jitter) * np.float32(spacing))
+    return p
+
+
+# grid cases of the fixtures: points, lo, hi, cubic cell edge, dims (nx == nz, 2^k cells)
+GRID_CASES = {
+    "grid_a": (lambda: grid_points(501, 20000, (1.0, 0.5, 1.0)), (0.0, 0.0, 0.0), (1.0, 0.5, 1.0), 1.0 / 16,
+               (16, 8, 16)),
+    "grid_b": (lambda: lattice_points(511, (24, 20, 24), 0.02, 0.3), (0.0, 0.0, 0.0), (0.64, 0.64, 0.64), 0.02,
+               (32, 32, 32)),
+}
+
+
+def scan_inputs() -> dict[str, np.ndarray]:
+    """The scan cases: the reference's ParallelScanTest vector
+    (SphWave2D/ParallelScan.cpp:129), counts in [0, 40) of length 2^10, and
+    values in [0, 10^4) of length 2^14."""
+    return {
+        "scan_kat": np.array([1, 0, 1, 0, 1, 2, 1, 2, 1, 2, 0, 1, 0, 2, 1, 0], np.int32),
+        "scan_1k": (uniform01(521, 1 << 10) * 40).astype(np.int32),
+        "scan_16k": (uniform01(522, 1 << 14) * 10000).astype(np.int32),
+    }
+
+
 def fixture_inputs(splash_rgba8: np.ndarray) -> dict[str, np.ndarray]:
     """Every input of tests/golden/ref_shader_outputs.npz (its cases are
     listed in tests/golden/make_ref_shader_golden.py).  splash_rgba8: the
@@ -218,4 +294,6 @@ def fixture_inputs(splash_rgba8: np.ndarray) -> dict[str, np.ndarray]:
         "evolve67_unm1": (un67 * np.float32(0.93)).astype(np.float32),
         # GL's UNORM8 -> float: c / 255, rounded once
         "image_rgba": (np.asarray(splash_rgba8).astype(np.float64) / 255.0).astype(np.float32),
+        **{name: case[0]() for name, case in GRID_CASES.items()},
+        **scan_inputs(),
     }

@@ -179,6 +179,54 @@ struct ivec2 {
   }
 };
 
+struct ivec3 {
+  union {
+    struct { int x, y, z; };
+    int e[3];
+  };
+  ivec3() { e[0] = e[1] = e[2] = 0; }
+  explicit ivec3(int s) { e[0] = e[1] = e[2] = s; }
+  ivec3(int a, int b, int c) { e[0] = a; e[1] = b; e[2] = c; }
+  explicit ivec3(const tvec3<float>& v) { for (int k = 0; k < 3; ++k) e[k] = (int)v.e[k]; }
+  explicit ivec3(const tvec3<double>& v) { for (int k = 0; k < 3; ++k) e[k] = (int)v.e[k]; }
+  ivec3(const ivec3& o) { for (int k = 0; k < 3; ++k) e[k] = o.e[k]; }
+  ivec3& operator=(const ivec3& o) { for (int k = 0; k < 3; ++k) e[k] = o.e[k]; return *this; }
+  int& operator[](int k) { return e[k]; }
+  int operator[](int k) const { return e[k]; }
+  friend ivec3 operator+(const ivec3& a, const ivec3& b) { return ivec3(a.x + b.x, a.y + b.y, a.z + b.z); }
+  friend ivec3 operator-(const ivec3& a, const ivec3& b) { return ivec3(a.x - b.x, a.y - b.y, a.z - b.z); }
+  friend ivec3 operator*(const ivec3& a, const ivec3& b) { return ivec3(a.x * b.x, a.y * b.y, a.z * b.z); }
+};
+
+struct ivec4 {
+  union {
+    struct { int x, y, z, w; };
+    int e[4];
+    Swz<ivec3, int, 4, 0, 1, 2> xyz;
+  };
+  ivec4() { e[0] = e[1] = e[2] = e[3] = 0; }
+  explicit ivec4(int s) { e[0] = e[1] = e[2] = e[3] = s; }
+  ivec4(int a, int b, int c, int d) { e[0] = a; e[1] = b; e[2] = c; e[3] = d; }
+  ivec4(const ivec4& o) { for (int k = 0; k < 4; ++k) e[k] = o.e[k]; }
+  ivec4& operator=(const ivec4& o) { for (int k = 0; k < 4; ++k) e[k] = o.e[k]; return *this; }
+  int& operator[](int k) { return e[k]; }
+  int operator[](int k) const { return e[k]; }
+};
+
+inline ivec3 clamp(const ivec3& v, const ivec3& lo, const ivec3& hi) {
+  ivec3 r;
+  for (int k = 0; k < 3; ++k) r.e[k] = v.e[k] < lo.e[k] ? lo.e[k] : (v.e[k] > hi.e[k] ? hi.e[k] : v.e[k]);
+  return r;
+}
+
+// atomicAdd on a buffer element: the invocations of a dispatch run one after
+// another, so the returned old values come in invocation order.
+inline int atomicAdd(int& mem, int v) {
+  const int old = mem;
+  mem = old + v;
+  return old;
+}
+
 inline ivec2 clamp(const ivec2& v, const ivec2& lo, const ivec2& hi) {
   ivec2 r;
   for (int k = 0; k < 2; ++k) r.e[k] = v.e[k] < lo.e[k] ? lo.e[k] : (v.e[k] > hi.e[k] ? hi.e[k] : v.e[k]);
@@ -268,6 +316,14 @@ void image_store(const image2D& im, const ivec2& p, const tvec4<S>& v) {
   inline S max(S a, S b) { return b > a ? b : a; } /* GLSL: y if x < y, else x */             \
   inline S min(S a, S b) { return b < a ? b : a; }                                            \
   inline S clamp(S x, S lo, S hi) { return min(max(x, lo), hi); }                             \
+  inline S floor(S a) { return ::floor(a); }                                                  \
+  inline vec3 floor(const vec3& v) { return vec3(floor(v.x), floor(v.y), floor(v.z)); }       \
+  inline vec4 max(const vec4& a, const vec4& b) {                                             \
+    return vec4(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z), max(a.w, b.w));                  \
+  }                                                                                           \
+  inline vec4 min(const vec4& a, const vec4& b) {                                             \
+    return vec4(min(a.x, b.x), min(a.y, b.y), min(a.z, b.z), min(a.w, b.w));                  \
+  }                                                                                           \
   inline S smoothstep(S e0, S e1, S x) {                                                      \
     const S t = clamp((x - e0) / (e1 - e0), (S)0, (S)1);                                      \
     return t * t * ((S)3 - (S)2 * t);                                                         \
@@ -304,6 +360,10 @@ GLSL_BUILTINS(double, f64)
 #define GLSL_PRELUDE(NS)                                                                  \
   using glsl::bvec2;                                                                      \
   using glsl::ivec2;                                                                      \
+  using glsl::ivec3;                                                                      \
+  using glsl::ivec4;                                                                      \
+  using glsl::atomicAdd;                                                                  \
+  using glsl::NS::floor;                                                                  \
   using glsl::uvec3;                                                                      \
   using glsl::sampler2D;                                                                  \
   using glsl::image2D;                                                                    \

@@ -11,14 +11,15 @@ Only declarations are rewritten; every function body compiles as written:
      become their members as globals; a runtime-sized array `T a[];` becomes
      a pointer `T* a;` that the dispatch binds;
   4. the remaining `layout(...)` qualifiers and the qualifiers `uniform`,
-     `readonly`, `writeonly`, `restrict`, `coherent` are dropped;
+     `readonly`, `writeonly`, `restrict`, `coherent` are dropped (a
+     uniform's initialiser, its default value, stays);
   5. a parameter `inout T x` becomes `T& x`;
   6. an unsuffixed floating literal gets the suffix `f` (a GLSL literal
      without `lf` is a float);
   7. a global whose initializer is not a constant (it reads a uniform or
      calls a function), and every global that is not `const` but has an
-     initializer (invocation-private storage in GLSL), is declared without
-     it; the initialisations move, in source order, into
+     initializer (invocation-private storage in GLSL; uniforms excepted), is
+     declared without it; the initialisations move, in source order, into
      `void glsl_init_globals()`, which the dispatch calls after binding the
      uniforms (once per dispatch, or before each invocation for shaders that
      write such globals).
@@ -31,8 +32,9 @@ import re
 import sys
 from pathlib import Path
 
-QUALIFIERS = ("uniform", "readonly", "writeonly", "restrict", "coherent")
-TYPE_NAMES = {"float", "int", "uint", "bool", "vec2", "vec3", "vec4", "ivec2", "uvec3", "mat4"}
+QUALIFIERS = ("readonly", "writeonly", "restrict", "coherent")
+UNIFORM_MARK = "GLSL_UNIFORM"
+TYPE_NAMES = {"float", "int", "uint", "bool", "vec2", "vec3", "vec4", "ivec2", "ivec3", "ivec4", "uvec3", "mat4"}
 
 
 def _drop_version(src: str) -> str:
@@ -58,6 +60,9 @@ def _blocks(src: str) -> str:
 
 def _qualifiers(src: str) -> str:
     src = re.sub(r"layout\s*\([^)]*\)", "", src)
+    # a uniform's initialiser is its default value, set once at link time:
+    # marked so that rule 7 leaves it in place
+    src = re.sub(r"\buniform\b", UNIFORM_MARK, src)
     for q in QUALIFIERS:
         src = re.sub(rf"\b{q}\b", "", src)
     return src
@@ -122,6 +127,7 @@ def transform(src: str) -> str:
     src = _inout(src)
     src = _float_literals(src)
     src, inits = _deferred_globals(src)
+    src = re.sub(rf"{UNIFORM_MARK}\s*", "", src)
     return src + "\nvoid glsl_init_globals() {\n" + "\n".join(inits) + "\n}\n"
 
 

@@ -1,7 +1,8 @@
 """Regenerate tests/golden/ref_shader_outputs.npz: outputs of the reference's
 own compute shaders (CoupledWaterAnimation/rho_pres_comp.glsl,
-force_comp.glsl, integrate_comp.glsl, wave_comp.glsl) run on the CPU, on the
-seeded inputs of oracle/ref.py.
+force_comp.glsl, integrate_comp.glsl, wave_comp.glsl;
+UniformGrid2D/ugrid_particles_cs.glsl and prefix_sum_cs.glsl) run on the
+CPU, on the seeded inputs of oracle/ref.py.
 
 The shaders are compiled as C++ (oracle/ref_shaders/: the GLSL source with
 its declarations rewritten, against a GLSL types-and-built-ins header) in
@@ -19,7 +20,15 @@ Cases (every input regenerates from oracle/ref.py; its SHA-256 is stored):
   evolve   EvolveWave on 64 x 64 fields (wave modes 1 and 0.5) and on a
            67 x 45 field (mode 0.5: the line source at x = 33);
   init     InitWave for modes 1, 0 and 0.5 on 64 x 64 and mode 0.5 on 67 x 45;
-  image    InitFromImage of the reference's splash texture on a 32 x 64 field.
+  image    InitFromImage of the reference's splash texture on a 32 x 64 field;
+  grid     UniformGrid2D/ugrid_particles_cs.glsl COMPUTE_COUNTS, the scan
+           (prefix_sum_cs.glsl dispatched as ParallelScan::Compute) and
+           INSERT_PARTICLES, as UniformGridGpu2D.cpp sequences them, on 20,000
+           scattered points (16 x 8 x 16 cells, points past every wall and on
+           cell faces) and a jittered 24 x 20 x 24 lattice (32^3 cells): counts,
+           offsets and index list;
+  scan     the scan alone on the reference's ParallelScanTest vector and on
+           2^10 and 2^14 values.
 
 Usage:  python tests/golden/make_ref_shader_golden.py
         (needs the reference checkout; CWA_REFERENCE names it if it is not
@@ -98,6 +107,11 @@ def main() -> None:
     d.wave_mode = 1.0
     z = np.zeros((64, 32))
     out["image_f32"] = ref.wave(ref.F32, z, z, ref.uniforms(d, mode=1), init_rgba=x["image_rgba"]).astype(np.float32)
+    for name, (_, lo, hi, cell, dims) in ref.GRID_CASES.items():
+        counts, offsets, lst = ref.grid_build(x[name], lo, hi, (cell, cell, cell), dims)
+        out[f"{name}_counts"], out[f"{name}_offsets"], out[f"{name}_list"] = counts, offsets, lst
+    for name in ref.scan_inputs():
+        out[f"{name}_out"] = ref.exclusive_scan(x[name])
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
 

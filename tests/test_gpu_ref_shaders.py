@@ -13,16 +13,21 @@ preset:
     float32 roundings of the field);
   * EvolveWave within two float32 roundings of the field's magnitude (the
     kernels sum the neighbours pairwise, the shader left to right);
-  * InitWave and InitFromImage bit-exact.
+  * InitWave and InitFromImage bit-exact;
+  * the stand-alone grid build (cwa_grid_build) and the exclusive scan
+    (cwa_exclusive_scan_i32) bit-exact against
+    UniformGrid2D/ugrid_particles_cs.glsl and prefix_sum_cs.glsl (the
+    no-allocation scan's check is in test_zz_no_alloc.py).
 """
 from __future__ import annotations
 
+import ctypes as C
 from pathlib import Path
 
 import numpy as np
 import pytest
 
-from coupledwateranimation_gb300 import PARTICLE_DTYPE, PREC_COMPENSATED, Sim, scenes
+from coupledwateranimation_gb300 import PARTICLE_DTYPE, PREC_COMPENSATED, Sim, _abi, scenes
 
 from _helpers import records_f32
 
@@ -118,3 +123,39 @@ def test_init_from_image_matches_the_shader_bit_exactly(lib):
         sim.wave_init_from_image(0, tex)
         got, _ = sim.download_wave(0)
     assert np.array_equal(got.view(np.uint32), G["image_f32"].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["grid_a", "grid_b"])
+def test_grid_build_matches_the_reference_grid_shader(lib, x, name):
+    import torch
+    from oracle import ref
+    _, lo, hi, cell, dims = ref.GRID_CASES[name]
+    pos = x[name]
+    n, nc = len(pos), int(np.prod(dims))
+    d_pos = torch.from_numpy(pos).cuda()
+    d_start = torch.empty(nc + 1, dtype=torch.int32, device="cuda")
+    d_idx = torch.empty(n, dtype=torch.int32, device="cuda")
+    ws = torch.empty(lib.cwa_grid_workspace_bytes(n, nc), dtype=torch.uint8, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    st = lib.cwa_grid_build(_abi.ptr(d_pos), n, (C.c_float * 3)(*lo), cell, (C.c_int32 * 3)(*dims),
+                            _abi.ptr(d_start), _abi.ptr(d_idx), None, _abi.ptr(ws), ws.numel(), stream)
+    assert st == 0, _abi.last_error()
+    assert lib.cwa_grid_status(n, nc, _abi.ptr(ws), stream) == 0, _abi.last_error()
+    start = d_start.cpu().numpy()
+    assert np.array_equal(np.diff(start), G[f"{name}_counts"])
+    assert np.array_equal(start[:-1], G[f"{name}_offsets"])
+    assert np.array_equal(d_idx.cpu().numpy(), G[f"{name}_list"])
+
+
+@pytest.mark.parametrize("name", ["scan_kat", "scan_1k", "scan_16k"])
+def test_exclusive_scan_matches_the_reference_scan_shader(lib, x, name):
+    import torch
+    xin = torch.from_numpy(x[name]).cuda()
+    out = torch.empty_like(xin)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    n = xin.numel()
+    ws = torch.empty(lib.cwa_scan_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    st = lib.cwa_exclusive_scan_i32(_abi.ptr(xin), _abi.ptr(out), n, _abi.ptr(ws), ws.numel(), stream)
+    assert st == 0, _abi.last_error()
+    assert lib.cwa_scan_status(n, _abi.ptr(ws), stream) == 0, _abi.last_error()
+    assert np.array_equal(out.cpu().numpy(), G[f"{name}_out"])

@@ -1,10 +1,13 @@
 """The oracle against the reference's own compute shaders.
 
 tests/golden/ref_shader_outputs.npz holds outputs of
-CoupledWaterAnimation/{rho_pres,force,integrate,wave}_comp.glsl compiled as
-C++ and run on the CPU (tests/golden/make_ref_shader_golden.py), in the
-shaders' float arithmetic ("f32") and with float promoted to double ("f64").
-These tests pin the oracle to them:
+CoupledWaterAnimation/{rho_pres,force,integrate,wave}_comp.glsl and of the
+grid and scan shaders UniformGrid2D/{ugrid_particles,prefix_sum}_cs.glsl
+compiled as C++ and run on the CPU (tests/golden/make_ref_shader_golden.py),
+in the shaders' float arithmetic ("f32") and with float promoted to double
+("f64").  These tests pin the oracle to them:
+  * the grid build (counts, offsets, index list) and the exclusive scan
+    equal the reference's shaders bit for bit;
   * the FP64 oracle (brute-force neighbour loops, integrate, EvolveWave)
     computes the shaders' expressions on the shaders' constants: it equals
     the f64 shader outputs to a few units of double rounding;
@@ -177,6 +180,28 @@ def test_float32_init_from_image_equals_the_shader_bit_exactly(orc):
     assert np.array_equal(got.view(np.uint32), G["image_f32"].view(np.uint32))
 
 
+@pytest.mark.parametrize("name", ["grid_a", "grid_b"])
+def test_grid_build_equals_the_reference_grid_shader(orc, x, name):
+    """UniformGrid2D/ugrid_particles_cs.glsl (cell = clamp(floor((p - min) /
+    cell size)), counts by atomicAdd, insert at offset + atomicAdd) with the
+    reference's scan between, invocations in index order: the oracle's
+    counts, cell starts and stable order equal it bit for bit."""
+    from oracle import ref
+    _, lo, hi, cell, dims = ref.GRID_CASES[name]
+    start, order, _ = orc.grid_build(x[name], list(lo), (cell, cell, cell), dims)
+    assert np.array_equal(np.diff(start), G[f"{name}_counts"])
+    assert np.array_equal(start[:-1], G[f"{name}_offsets"])
+    assert np.array_equal(order, G[f"{name}_list"])
+    assert G[f"{name}_counts"].sum() == len(x[name]) and start[-1] == len(x[name])
+
+
+@pytest.mark.parametrize("name", ["scan_kat", "scan_1k", "scan_16k"])
+def test_exclusive_scan_equals_the_reference_scan_shader(orc, x, name):
+    """prefix_sum_cs.glsl dispatched as ParallelScan::Compute (up-sweep, then
+    down-sweep, UniformGrid2D/ParallelScan.cpp:43-95)."""
+    assert np.array_equal(orc.exclusive_scan(x[name]), G[f"{name}_out"])
+
+
 def test_live_shaders_reproduce_the_fixtures(x, desc):
     """With the reference checkout present: rebuild the shaders from its
     source, rerun every case, and get the committed fixtures back bit for bit."""
@@ -201,3 +226,9 @@ def test_live_shaders_reproduce_the_fixtures(x, desc):
         desc.wave_mode = 1.0
     assert np.array_equal(wv, G["evolve64_m05_f64"])
     assert mk.SPH_SAMPLE.tolist() == G["sph_sample"].tolist()
+    for name, (_, lo, hi, cell, dims) in ref.GRID_CASES.items():
+        got = ref.grid_build(x[name], lo, hi, (cell, cell, cell), dims)
+        for part, a in zip(("counts", "offsets", "list"), got):
+            assert np.array_equal(a, G[f"{name}_{part}"])
+    for name in ref.scan_inputs():
+        assert np.array_equal(ref.exclusive_scan(x[name]), G[f"{name}_out"])

@@ -79,3 +79,18 @@ def test_no_alloc_scan_rejects_sizes_above_its_limit(lib):
     n = 16_777_216 + 1  # CWA_NOALLOC_SCAN_MAX_N + 1
     assert lib.cwa_exclusive_scan_i32_noalloc(None, None, n, None) == _abi.CWA_ERR_CAPACITY
     assert "CWA_NOALLOC_SCAN_MAX_N" in _abi.last_error()
+
+
+@pytest.mark.parametrize("name", ["scan_kat", "scan_1k", "scan_16k"])
+def test_no_alloc_scan_matches_the_reference_scan_shader(lib, name):
+    """The reference's prefix_sum_cs.glsl dispatched as ParallelScan::Compute
+    (UniformGrid2D/ParallelScan.cpp:43-95), compiled for the CPU: its
+    outputs are tests/golden/ref_shader_outputs.npz."""
+    import torch
+    from pathlib import Path
+
+    from oracle import ref
+    golden = np.load(Path(__file__).resolve().parent / "golden" / "ref_shader_outputs.npz")
+    x = torch.from_numpy(ref.scan_inputs()[name]).cuda()
+    got = _no_alloc(lib, torch, x, x.numel())
+    assert np.array_equal(got.cpu().numpy(), golden[f"{name}_out"])
