@@ -738,7 +738,7 @@ def run_sph2d(args) -> None:
         older = wave.copy()
         while cpu_frames < 3 or time.perf_counter() - t0 < 5.0:
             for _ in range(p.sph_substeps):
-                parts = orc.force_2d(p, orc.density_2d(p, parts, wave), wave)
+                parts = orc.force_2d(p, orc.density_2d(p, parts, wave), wave, grid_from=parts)
             for _ in range(p.wave_substeps):
                 if wave1d:
                     wave, older = orc.wave1d_iter_2d_f32(p, wave, older), wave

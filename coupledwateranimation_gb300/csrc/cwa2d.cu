@@ -110,13 +110,19 @@ __device__ __forceinline__ int cell_i(const Sph2dConst& c, float p, int axis) {
   return axis == 0 ? cell_axis(p, lo, c.cell_x, c.ncx) : cell_axis(p, lo, c.cell_y, c.ncy);
 }
 
+// A point enters the cell of its position only when it lies strictly inside
+// the grid's extents [0, view] (point_in_aabb, uniform_grid_sph_cs.glsl:19-23,
+// 101-105); the others go to bucket ncx * ncy past the last cell, which no
+// neighbour search visits, so they are invisible, to themselves too.
 __global__ void k2_hash(Sph2dConst c, const float4* __restrict__ pos, int32_t* __restrict__ key,
                         int32_t* __restrict__ slot, int32_t* __restrict__ count, int32_t* status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.n) return;
   const float4 p = pos[i];
   if (!finite3(make_float4(p.x, p.y, 0.0f, 0.0f))) atomicOr(status, kStatusNonFinite);
-  const int k = cell_i(c, p.x, 0) * c.ncy + cell_i(c, p.y, 1);  // Index(i, j) = i * ny + j
+  const bool inside = p.x > 0.0f && p.y > 0.0f && p.x < c.view_w && p.y < c.view_h;
+  const int k = inside ? cell_i(c, p.x, 0) * c.ncy + cell_i(c, p.y, 1)  // Index(i, j) = i * ny + j
+                       : c.ncx * c.ncy;
   key[i] = k;
   slot[i] = count_slot(count, k);
 }
@@ -474,10 +480,10 @@ void free2d(cwa2d_sim* s) {
 
 cwa_status pass_grid(cwa2d_sim* s) {
   const Sph2dConst& c = s->k;
-  const int nc = c.ncx * c.ncy;
+  const int nb = c.ncx * c.ncy + 1;  // the cells and the outside bucket
   k2_hash<<<blocks(c.n), kBlock, 0, s->stream>>>(c, s->P[s->cur], s->key, s->slot, s->count, s->d_status);
   CWA2_CUDA(cudaGetLastError());
-  CWA2_CUDA(scan_launch(s->count, s->start, nc, nc + 1, true, s->scan, s->d_status, s->stream, nullptr));
+  CWA2_CUDA(scan_launch(s->count, s->start, nb, nb + 1, true, s->scan, s->d_status, s->stream, nullptr));
   CWA2_CUDA(launch_list_insert(s->key, s->slot, s->start, s->list, c.n, nullptr, s->stream));
   CWA2_CUDA(launch_point_rank(s->key, s->slot, s->start, s->list, c.n, s->sorted, s->d_status, s->stream));
   s->grid_fresh = true;
@@ -644,7 +650,7 @@ cwa_status cwa2d_create(const cwa2d_params* p, int32_t device, cwa2d_sim** out) 
   k.w1_b = 1.0f - p->wave_beta;
   k.w1_atten = p->wave_atten;
   k.w1_half = 0.5f * p->wave_lambda;
-  const int nc = k.ncx * k.ncy;
+  const int nb = k.ncx * k.ncy + 1;  // grid cells + the bucket of points outside the grid
   auto fail = [&](cudaError_t e) {
     cwa::set_error(std::string("cwa2d_create: ") + cudaGetErrorString(e));
     free2d(s);
@@ -665,16 +671,16 @@ cwa_status cwa2d_create(const cwa2d_params* p, int32_t device, cwa2d_sim** out) 
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->slot, 4 * (size_t)k.n);
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->list, 4 * (size_t)k.n);
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->sorted, 4 * (size_t)k.n);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->count, 4 * (size_t)nc);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&s->start, 4 * ((size_t)nc + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&s->scan_ws, scan_workspace_bytes(nc + 1));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&s->count, 4 * (size_t)nb);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&s->start, 4 * ((size_t)nb + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&s->scan_ws, scan_workspace_bytes(nb + 1));
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_status, 4);
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->staging, sizeof(cwa2d_particle) * k.n);
-  if (e == cudaSuccess) e = cudaMemset(s->count, 0, 4 * (size_t)nc);
+  if (e == cudaSuccess) e = cudaMemset(s->count, 0, 4 * (size_t)nb);
   if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, 4);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return fail(e);
-  scan_bind_workspace(s->scan_ws, nc + 1, &s->scan);
+  scan_bind_workspace(s->scan_ws, nb + 1, &s->scan);
   const cwa_status st = cwa2d_reinit(s);
   if (st != CWA_OK) {
     free2d(s);

@@ -100,10 +100,27 @@ void wave_nh(const C2& c, const float* w4, double x, double* h, double* xvel) {
   *xvel = my / mx;
 }
 
-int cell_of(double p, float cell, int n) {
-  double t = floor((p - 0.0) / (double)cell);
-  t = t < 0.0 ? 0.0 : (t > n - 1 ? n - 1 : t);
+// ComputeCellIndex (uniform_grid_sph_cs.glsl:126-132) in float: the cell of
+// a float coordinate, clamped to the grid.
+int cell_of(float p, float cell, int n) {
+  float t = floorf((p - 0.0f) / cell);
+  t = t < 0.0f ? 0.0f : (t > (float)(n - 1) ? (float)(n - 1) : t);
   return (int)t;
+}
+
+// The cell lists of UniformGridSph2D::CollisionQuery (UniformGridGpu2D.cpp:
+// 220-265): a point enters the cell of its position only when it lies
+// strictly inside the grid's extents [0, view] (point_in_aabb,
+// uniform_grid_sph_cs.glsl:19-23, 101-105); a point outside is in no list,
+// so no neighbour search (its own included) sees it.  Members in index order.
+std::vector<std::vector<int>> cell_lists(const C2& c, const cwa2d_particle* src) {
+  std::vector<std::vector<int>> cells((size_t)c.ncx * c.ncy);
+  for (int j = 0; j < c.n; ++j) {
+    const float x = src[j].pos[0], y = src[j].pos[1];
+    if (!(x > 0.0f && y > 0.0f && x < c.view_w && y < c.view_h)) continue;
+    cells[(size_t)cell_of(x, c.cell_x, c.ncx) * c.ncy + cell_of(y, c.cell_y, c.ncy)].push_back(j);
+  }
+  return cells;
 }
 
 }  // namespace
@@ -253,9 +270,7 @@ void orc2d_wave1d_iter_f32(const cwa2d_params* prm, const float* cur4, const flo
 // the wall projection, enable flag, density, pressure).
 void orc2d_density(const cwa2d_params* prm, const cwa2d_particle* in, const float* wave4, cwa2d_particle* out) {
   const C2 c = consts(prm);
-  std::vector<std::vector<int>> cells((size_t)c.ncx * c.ncy);
-  for (int j = 0; j < c.n; ++j)
-    cells[(size_t)cell_of(in[j].pos[0], c.cell_x, c.ncx) * c.ncy + cell_of(in[j].pos[1], c.cell_y, c.ncy)].push_back(j);
+  const std::vector<std::vector<int>> cells = cell_lists(c, in);
 #pragma omp parallel for schedule(dynamic, 64)
   for (int ix = 0; ix < c.n; ++ix) {
     cwa2d_particle q = in[ix];
@@ -282,8 +297,9 @@ void orc2d_density(const cwa2d_params* prm, const cwa2d_particle* in, const floa
       continue;
     }
     double rho = 0.0;
-    const int x0 = cell_of(px - c.H, c.cell_x, c.ncx), x1 = cell_of(px + c.H, c.cell_x, c.ncx);
-    const int y0 = cell_of(py - c.H, c.cell_y, c.ncy), y1 = cell_of(py + c.H, c.cell_y, c.ncy);
+    // the query box around the stored (float) position, in float
+    const int x0 = cell_of(q.pos[0] - c.H, c.cell_x, c.ncx), x1 = cell_of(q.pos[0] + c.H, c.cell_x, c.ncx);
+    const int y0 = cell_of(q.pos[1] - c.H, c.cell_y, c.ncy), y1 = cell_of(q.pos[1] + c.H, c.cell_y, c.ncy);
     for (int ci = x0; ci <= x1; ++ci)
       for (int cj = y0; cj <= y1; ++cj)
         for (int j : cells[(size_t)ci * c.ncy + cj]) {
@@ -299,12 +315,15 @@ void orc2d_density(const cwa2d_params* prm, const cwa2d_particle* in, const floa
   }
 }
 
-// ComputeForces in FP64 (forward Euler at the end).
-void orc2d_force(const cwa2d_params* prm, const cwa2d_particle* in, const float* wave4, cwa2d_particle* out) {
+// ComputeForces in FP64 (forward Euler at the end).  The neighbour lists are
+// those of the grid built from `grid_src` (null: from `in`): SphUgrid::Compute
+// (SphWave2D/StencilBuffer.cpp:150-179) builds one grid per substep, before
+// the density pass, and the force pass searches that grid with the
+// positions the density pass left.
+void orc2d_force(const cwa2d_params* prm, const cwa2d_particle* in, const cwa2d_particle* grid_src,
+                 const float* wave4, cwa2d_particle* out) {
   const C2 c = consts(prm);
-  std::vector<std::vector<int>> cells((size_t)c.ncx * c.ncy);
-  for (int j = 0; j < c.n; ++j)
-    cells[(size_t)cell_of(in[j].pos[0], c.cell_x, c.ncx) * c.ncy + cell_of(in[j].pos[1], c.cell_y, c.ncy)].push_back(j);
+  const std::vector<std::vector<int>> cells = cell_lists(c, grid_src ? grid_src : in);
 #pragma omp parallel for schedule(dynamic, 64)
   for (int ix = 0; ix < c.n; ++ix) {
     cwa2d_particle q = in[ix];
@@ -315,8 +334,8 @@ void orc2d_force(const cwa2d_params* prm, const cwa2d_particle* in, const float*
     const double px = q.pos[0], py = q.pos[1], vxi = q.vel[0], vyi = q.vel[1];
     const double rho_i = q.acc[3], api = (double)q.vel[3] / (rho_i * rho_i);
     double apx = 0, apy = 0, avx = 0, avy = 0;
-    const int x0 = cell_of(px - c.H, c.cell_x, c.ncx), x1 = cell_of(px + c.H, c.cell_x, c.ncx);
-    const int y0 = cell_of(py - c.H, c.cell_y, c.ncy), y1 = cell_of(py + c.H, c.cell_y, c.ncy);
+    const int x0 = cell_of(q.pos[0] - c.H, c.cell_x, c.ncx), x1 = cell_of(q.pos[0] + c.H, c.cell_x, c.ncx);
+    const int y0 = cell_of(q.pos[1] - c.H, c.cell_y, c.ncy), y1 = cell_of(q.pos[1] + c.H, c.cell_y, c.ncy);
     for (int ci = x0; ci <= x1; ++ci)
       for (int cj = y0; cj <= y1; ++cj)
         for (int j : cells[(size_t)ci * c.ncy + cj]) {

@@ -109,7 +109,10 @@ void orc2d_wave_iter_f32(const cwa2d_params* prm, const float* in4, float* out4,
 void orc2d_wave1d_init_f32(const cwa2d_params* prm, const float* cur4, const float* prev4, float* out4, int32_t mode);
 void orc2d_wave1d_iter_f32(const cwa2d_params* prm, const float* cur4, const float* prev4, float* out4);
 void orc2d_density(const cwa2d_params* prm, const cwa2d_particle* in, const float* wave4, cwa2d_particle* out);
-void orc2d_force(const cwa2d_params* prm, const cwa2d_particle* in, const float* wave4, cwa2d_particle* out);
+/* grid_src: the particles the substep's grid was built from (before the
+ * density pass), or NULL for `in`. */
+void orc2d_force(const cwa2d_params* prm, const cwa2d_particle* in, const cwa2d_particle* grid_src,
+                 const float* wave4, cwa2d_particle* out);
 
 /* PBD box collisions (cwa_pbd_oracle.cpp): `steps` frames in place, float32
  * op by op with the library's accumulation order. */

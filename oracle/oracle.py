@@ -65,7 +65,7 @@ def load() -> C.CDLL:
             "orc2d_wave1d_init_f32": (None, [_P, _P, _P, _P, _I]),
             "orc2d_wave1d_iter_f32": (None, [_P, _P, _P, _P]),
             "orc2d_density": (None, [_P, _P, _P, _P]),
-            "orc2d_force": (None, [_P, _P, _P, _P]),
+            "orc2d_force": (None, [_P, _P, _P, _P, _P]),
             "orc_pbd_step": (None, [_P, _P, _I, _I]),
         }
         for name, (res, args) in protos.items():
@@ -309,10 +309,13 @@ def density_2d(params, particles, wave4) -> np.ndarray:
     return out
 
 
-def force_2d(params, particles, wave4) -> np.ndarray:
+def force_2d(params, particles, wave4, grid_from=None) -> np.ndarray:
+    """ComputeForces on `particles` over the grid of `grid_from` (the
+    substep's state before the density pass; default: `particles`)."""
     inp = np.ascontiguousarray(particles)
+    src = None if grid_from is None else np.ascontiguousarray(grid_from)
     out = np.zeros_like(inp)
-    load().orc2d_force(_pp(params), _p(inp), _p(np.ascontiguousarray(wave4, np.float32)), _p(out))
+    load().orc2d_force(_pp(params), _p(inp), _p(src), _p(np.ascontiguousarray(wave4, np.float32)), _p(out))
     return out
 
 

@@ -36,6 +36,28 @@ class Uniforms(C.Structure):
                 ("mode", C.c_int32)]
 
 
+class Uniforms2D(C.Structure):
+    """ref2d_uniforms (oracle/ref_shaders/ref_shaders.h)."""
+    _fields_ = [("time", C.c_float), ("bottom", C.c_float), ("grid_cells", C.c_int32 * 2),
+                ("extent_max", C.c_float * 2), ("wave_lambda", C.c_float), ("dx", C.c_float),
+                ("atten", C.c_float), ("beta", C.c_float), ("boundary", C.c_float * 2)]
+
+
+def uniforms_2d(params) -> Uniforms2D:
+    """The 2D family's uniforms from a cwa2d_params (its defaults are the
+    reference app's values)."""
+    u = Uniforms2D()
+    u.time = 0.0
+    u.bottom = params.bottom
+    u.grid_cells[:] = list(params.grid_cells)
+    u.extent_max[:] = list(params.view_size)
+    u.wave_lambda = params.wave_lambda
+    u.dx = params.wave_dx
+    u.atten = params.wave_atten
+    u.beta = params.wave_beta
+    return u
+
+
 def reference_root() -> Path | None:
     ref = Path(os.environ.get("CWA_REFERENCE", str(DEFAULT_REFERENCE)))
     return ref if (ref / "CoupledWaterAnimation" / "rho_pres_comp.glsl").is_file() else None
@@ -73,6 +95,13 @@ def load():
         lib.ref_exclusive_scan.restype = C.c_int32
         lib.ref_grid_build.argtypes = [fp, C.c_int32, fp, fp, fp, ip, ip, ip, ip]
         lib.ref_grid_build.restype = C.c_int32
+        u2 = C.POINTER(Uniforms2D)
+        lib.ref2d_sph.argtypes = [C.c_int32, C.c_int32, dp, dp, C.c_int32, fp, C.c_int32, u2]
+        lib.ref2d_sph.restype = C.c_int32
+        lib.ref2d_substep.argtypes = [C.c_int32, dp, dp, dp, C.c_int32, fp, C.c_int32, u2]
+        lib.ref2d_substep.restype = C.c_int32
+        lib.ref2d_field.argtypes = [C.c_int32, C.c_int32, fp, fp, fp, C.c_int32, fp, C.c_int32, u2]
+        lib.ref2d_field.restype = C.c_int32
         _lib = lib
     return _lib
 
@@ -165,6 +194,38 @@ def grid_build(pos4: np.ndarray, lo, hi, cell, dims):
     if rc != 0:
         raise ValueError("the reference grid needs nx == nz and a power-of-two cell count")
     return counts, offsets, lst
+
+
+def sph2d(prec: int, mode: int, p12: np.ndarray, wave4: np.ndarray, u: Uniforms2D) -> np.ndarray:
+    """The grid of p12, then one SphWaveKoschier2D mode over it."""
+    a = np.ascontiguousarray(p12, np.float64)
+    out = np.zeros_like(a)
+    w = np.ascontiguousarray(wave4, np.float32)
+    if load().ref2d_sph(prec, mode, _dp(a), _dp(out), len(a), _fp(w), len(w), C.byref(u)) != 0:
+        raise ValueError("ref2d_sph failed")
+    return out
+
+
+def substep2d(prec: int, p12: np.ndarray, wave4: np.ndarray, u: Uniforms2D):
+    """One SphUgrid::Compute substep: (after density, after forces)."""
+    a = np.ascontiguousarray(p12, np.float64)
+    dens, force = np.zeros_like(a), np.zeros_like(a)
+    w = np.ascontiguousarray(wave4, np.float32)
+    if load().ref2d_substep(prec, _dp(a), _dp(dens), _dp(force), len(a), _fp(w), len(w), C.byref(u)) != 0:
+        raise ValueError("ref2d_substep failed")
+    return dens, force
+
+
+def field2d(kind: int, mode: int, in0, in1, out_prev, u: Uniforms2D, init4=None) -> np.ndarray:
+    """One Shallow1D (kind 0) or Wave1D (kind 1) dispatch; out_prev: the
+    output image's contents before it."""
+    a = np.ascontiguousarray(in0, np.float32)
+    b = np.ascontiguousarray(a if in1 is None else in1, np.float32)
+    out = np.ascontiguousarray(out_prev, np.float32).copy()
+    img = None if init4 is None else np.ascontiguousarray(init4, np.float32)
+    load().ref2d_field(kind, mode, _fp(a), _fp(b), _fp(out), len(a), _fp(img), 0 if img is None else len(img),
+                       C.byref(u))
+    return out
 
 
 # ----------------------------------------------------------- seeded inputs ----
@@ -278,6 +339,48 @@ def scan_inputs() -> dict[str, np.ndarray]:
     }
 
 
+def sph2d_state(params) -> np.ndarray:
+    """params.n_particles records of 12 float32 (pos, vel, acc): the 2D app's
+    initial lattice (InitParticle, SphWaveKoschier2D_grid_cs.glsl:308-333)
+    jittered by up to 0.03, velocities in [-1, 1), every 7th particle
+    disabled (pos.w = 0), density 1000; then particles 0-7 moved past the
+    grid's extents (x <= 0, x >= 9.6, y >= 9.6: in no cell list) and
+    particles 8-15 below the floor plane (the unpenetrate branch)."""
+    n, cols = params.n_particles, params.init_columns
+    rows = n // cols
+    R = np.float32(params.particle_radius)
+    H = np.float32(4.0) * R
+    vw, vh = np.float32(params.view_size[0]), np.float32(params.view_size[1])
+    ix = np.arange(n)
+    p = np.zeros((n, 12), np.float32)
+    p[:, 0] = vw * ((ix % cols).astype(np.float32) / np.float32(cols)) + R
+    p[:, 1] = (np.float32(18.0) * H) * ((ix // cols).astype(np.float32) / np.float32(rows)) + (
+        (np.float32(0.5) * vh - np.float32(15.0) * R) + R)
+    p[:, 0] += _u32(601, n, -0.03, 0.03)
+    p[:, 1] += _u32(602, n, -0.03, 0.03)
+    p[:, 3] = 1.0
+    p[::7, 3] = 0.0
+    p[:, 4] = _u32(603, n, -1.0, 1.0)
+    p[:, 5] = _u32(604, n, -1.0, 1.0)
+    p[:, 11] = 1000.0
+    p[0:8, 0] = np.array([-0.01, -0.002, 0.0, 9.6, 9.61, 4.0, 5.0, 6.0], np.float32)
+    p[5:8, 1] = np.array([9.6, 9.7, 10.0], np.float32)
+    p[8:16, 1] = np.float32(0.5) * vh - np.float32(15.0) * R + _u32(605, 8, -0.2, 0.0)
+    return p
+
+
+def shallow_field(params) -> np.ndarray:
+    """A shallow-water state (h, uh, h_half, uh_half) for the SPH's wave
+    sampling: h = 4.8 plus a bump, uh up to 0.5 h so that |uh / h| crosses
+    the 0.05 enable threshold."""
+    n = params.wave_cells
+    x = (np.arange(n) + 0.5) / n
+    f = np.zeros((n, 4), np.float32)
+    f[:, 0] = (4.8 + 0.6 * np.exp(-((x - 0.4) ** 2) / 0.01)).astype(np.float32)
+    f[:, 1] = (f[:, 0] * (uniform01(611, n) - 0.5)).astype(np.float32)
+    return f
+
+
 def fixture_inputs(splash_rgba8: np.ndarray) -> dict[str, np.ndarray]:
     """Every input of tests/golden/ref_shader_outputs.npz (its cases are
     listed in tests/golden/make_ref_shader_golden.py).  splash_rgba8: the
@@ -296,4 +399,13 @@ def fixture_inputs(splash_rgba8: np.ndarray) -> dict[str, np.ndarray]:
         "image_rgba": (np.asarray(splash_rgba8).astype(np.float64) / 255.0).astype(np.float32),
         **{name: case[0]() for name, case in GRID_CASES.items()},
         **scan_inputs(),
+        **sph2d_inputs(),
     }
+
+
+def sph2d_inputs() -> dict[str, np.ndarray]:
+    """The 2D family's inputs, from the library's default parameters (the
+    reference app's values)."""
+    from coupledwateranimation_gb300.sim2d import defaults2d
+    p = defaults2d()
+    return {"s2d_state": sph2d_state(p), "s2d_wave": shallow_field(p)}

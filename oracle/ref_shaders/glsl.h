@@ -37,6 +37,9 @@ struct Swz {
   }
   // a.xyz = b.xyz writes the named components only
   Swz& operator=(const Swz& o) { return *this = V(o); }
+  Swz& operator+=(const V& v) { return *this = V(*this) + v; }
+  Swz& operator-=(const V& v) { return *this = V(*this) - v; }
+  Swz& operator*=(S s) { return *this = V(*this) * s; }
 
  private:
   template <int... K>
@@ -113,6 +116,7 @@ struct tvec4 {
   tvec4() { e[0] = e[1] = e[2] = e[3] = S(0); }
   explicit tvec4(S s) { e[0] = e[1] = e[2] = e[3] = s; }
   tvec4(S a, S b, S c, S d) { e[0] = a; e[1] = b; e[2] = c; e[3] = d; }
+  tvec4(const tvec2<S>& v, S c, S d) { e[0] = v.e[0]; e[1] = v.e[1]; e[2] = c; e[3] = d; }
   tvec4(const tvec4& o) { for (int k = 0; k < 4; ++k) e[k] = o.e[k]; }
   tvec4& operator=(const tvec4& o) { for (int k = 0; k < 4; ++k) e[k] = o.e[k]; return *this; }
   GLSL_VEC_COMMON(tvec4, 4)
@@ -172,6 +176,8 @@ struct ivec2 {
   friend ivec2 operator+(const ivec2& a, const ivec2& b) { return ivec2(a.e[0] + b.e[0], a.e[1] + b.e[1]); }
   friend ivec2 operator-(const ivec2& a, const ivec2& b) { return ivec2(a.e[0] - b.e[0], a.e[1] - b.e[1]); }
   friend ivec2 operator*(const ivec2& a, const ivec2& b) { return ivec2(a.e[0] * b.e[0], a.e[1] * b.e[1]); }
+  // GLSL == on vectors: every component equal
+  friend bool operator==(const ivec2& a, const ivec2& b) { return a.e[0] == b.e[0] && a.e[1] == b.e[1]; }
   // float * ivec2: the int vector converts to a float vector first
   friend tvec2<float> operator*(float s, const ivec2& a) { return tvec2<float>(s * (float)a.e[0], s * (float)a.e[1]); }
   friend tvec2<double> operator*(double s, const ivec2& a) {
@@ -232,8 +238,10 @@ inline ivec2 clamp(const ivec2& v, const ivec2& lo, const ivec2& hi) {
   for (int k = 0; k < 2; ++k) r.e[k] = v.e[k] < lo.e[k] ? lo.e[k] : (v.e[k] > hi.e[k] ? hi.e[k] : v.e[k]);
   return r;
 }
+inline ivec2 max(const ivec2& a, const ivec2& b) { return ivec2(b.x > a.x ? b.x : a.x, b.y > a.y ? b.y : a.y); }
 inline bvec2 greaterThanEqual(const ivec2& a, const ivec2& b) { return bvec2{a.x >= b.x, a.y >= b.y}; }
 inline bool any(const bvec2& b) { return b.x || b.y; }
+inline bool all(const bvec2& b) { return b.x && b.y; }
 
 // ---------------------------------------------------- textures, images ----
 // A bound texture: w x h texels of `comps` floats (1: the red channel only,
@@ -249,6 +257,27 @@ struct sampler2D {
 };
 
 inline ivec2 textureSize(const sampler2D& s, int) { return ivec2(s.w, s.h); }
+
+// A bound 1D texture: w texels of `comps` floats.
+struct sampler1D {
+  const float* texels = nullptr;
+  int w = 0, comps = 4;
+  float at(int x, int c) const {
+    if (c < comps) return texels[(size_t)x * comps + c];
+    return c == 3 ? 1.0f : 0.0f;
+  }
+};
+
+inline int textureSize(const sampler1D& s, int) { return s.w; }
+
+// A bound image1D, rgba32f: w texels of 4 scalars, float or double.
+struct image1D {
+  void* data = nullptr;
+  int w = 0;
+  bool is_double = false;
+};
+
+inline int imageSize(const image1D& im) { return im.w; }
 
 // A bound image2D, rgba32f: w x h texels of 4 scalars, float or double.
 struct image2D {
@@ -280,6 +309,40 @@ tvec4<S> filter_linear(const sampler2D& t, S s, S u) {
 }
 
 template <class S>
+tvec4<S> filter_linear_1d(const sampler1D& t, S s) {
+  const S us = s * (S)t.w - (S)0.5;
+  const S fi = floor(us);
+  const S a = us - fi;
+  auto cl = [](long v, int n) { return (int)(v < 0 ? 0 : (v > n - 1 ? n - 1 : v)); };
+  const long i0 = (long)fi;
+  const int x0 = cl(i0, t.w), x1 = cl(i0 + 1, t.w);
+  tvec4<S> r;
+  for (int c = 0; c < 4; ++c) r.e[c] = ((S)1 - a) * (S)t.at(x0, c) + a * (S)t.at(x1, c);
+  return r;
+}
+
+template <class S>
+tvec4<S> image_load_1d(const image1D& im, int x) {
+  tvec4<S> r;
+  if (x < 0 || x >= im.w) return r;
+  for (int c = 0; c < 4; ++c)
+    r.e[c] = im.is_double ? (S) static_cast<const double*>(im.data)[4 * (size_t)x + c]
+                          : (S) static_cast<const float*>(im.data)[4 * (size_t)x + c];
+  return r;
+}
+
+template <class S>
+void image_store_1d(const image1D& im, int x, const tvec4<S>& v) {
+  if (x < 0 || x >= im.w) return;
+  for (int c = 0; c < 4; ++c) {
+    if (im.is_double)
+      static_cast<double*>(im.data)[4 * (size_t)x + c] = (double)v.e[c];
+    else
+      static_cast<float*>(im.data)[4 * (size_t)x + c] = (float)v.e[c];
+  }
+}
+
+template <class S>
 tvec4<S> image_load(const image2D& im, const ivec2& p) {
   tvec4<S> r;  // out of range: zero (GLSL 4.50, 8.12)
   if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return r;
@@ -306,6 +369,7 @@ void image_store(const image2D& im, const ivec2& p, const tvec4<S>& v) {
 // ------------------------------------------------ per-precision built-ins ----
 #define GLSL_BUILTINS(S, NS)                                                                  \
   namespace NS {                                                                              \
+  using scalar = S;                                                                           \
   using vec2 = tvec2<S>;                                                                      \
   using vec3 = tvec3<S>;                                                                      \
   using vec4 = tvec4<S>;                                                                      \
@@ -317,7 +381,28 @@ void image_store(const image2D& im, const ivec2& p, const tvec4<S>& v) {
   inline S min(S a, S b) { return b < a ? b : a; }                                            \
   inline S clamp(S x, S lo, S hi) { return min(max(x, lo), hi); }                             \
   inline S floor(S a) { return ::floor(a); }                                                  \
+  inline S exp(S a) { return ::exp(a); }                                                      \
+  inline S sin(S a) { return ::sin(a); }                                                      \
+  inline S cos(S a) { return ::cos(a); }                                                      \
+  inline S acos(S a) { return ::acos(a); }                                                    \
+  inline S fract(S a) { return a - floor(a); }                                                \
+  inline S mix(S x, S y, S a) { return x * ((S)1 - a) + y * a; }                              \
+  inline S sign(S a) { return a > (S)0 ? (S)1 : (a < (S)0 ? (S)-1 : (S)0); }                  \
+  inline vec2 max(const vec2& a, const vec2& b) { return vec2(max(a.x, b.x), max(a.y, b.y)); } \
+  inline vec2 min(const vec2& a, const vec2& b) { return vec2(min(a.x, b.x), min(a.y, b.y)); } \
+  inline bvec2 greaterThan(const vec2& a, const vec2& b) { return bvec2{a.x > b.x, a.y > b.y}; } \
+  inline bvec2 lessThan(const vec2& a, const vec2& b) { return bvec2{a.x < b.x, a.y < b.y}; }   \
+  inline vec4 texture(const sampler1D& t, S s) { return detail::filter_linear_1d<S>(t, s); }  \
+  inline vec4 texelFetch(const sampler1D& t, int x, int) {                                    \
+    vec4 r;                                                                                   \
+    if (x < 0 || x >= t.w) return r;                                                          \
+    for (int c = 0; c < 4; ++c) r.e[c] = (S)t.at(x, c);                                       \
+    return r;                                                                                 \
+  }                                                                                           \
+  inline vec4 imageLoad(const image1D& im, int x) { return detail::image_load_1d<S>(im, x); } \
+  inline void imageStore(const image1D& im, int x, const vec4& v) { detail::image_store_1d<S>(im, x, v); } \
   inline vec3 floor(const vec3& v) { return vec3(floor(v.x), floor(v.y), floor(v.z)); }       \
+  inline vec2 floor(const vec2& v) { return vec2(floor(v.x), floor(v.y)); }                    \
   inline vec4 max(const vec4& a, const vec4& b) {                                             \
     return vec4(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z), max(a.w, b.w));                  \
   }                                                                                           \
@@ -334,6 +419,7 @@ void image_store(const image2D& im, const ivec2& p, const tvec4<S>& v) {
   inline S length(const vec3& v) { return sqrt(dot(v, v)); }                                  \
   inline S distance(const vec2& a, const vec2& b) { return length(a - b); }                   \
   inline vec3 normalize(const vec3& v) { return v / length(v); }                              \
+  inline vec2 normalize(const vec2& v) { return v / length(v); }                              \
   inline vec3 cross(const vec3& a, const vec3& b) {                                           \
     return vec3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);         \
   }                                                                                           \
@@ -356,7 +442,9 @@ GLSL_BUILTINS(double, f64)
 
 // Opens a shader's namespace body: its types and built-ins at precision NS
 // (f32 or f64), found by ordinary lookup ahead of the C library's names, and
-// the invocation id that the dispatch loop sets.
+// the invocation id that the dispatch loop sets.  Before the shader's text
+// the dispatch unit defines GLSL_CONST(name, init): `(init)` for the float
+// build, the float build's folded constant for the double build.
 #define GLSL_PRELUDE(NS)                                                                  \
   using glsl::bvec2;                                                                      \
   using glsl::ivec2;                                                                      \
@@ -392,5 +480,19 @@ GLSL_BUILTINS(double, f64)
   using glsl::imageSize;                                                                  \
   using glsl::greaterThanEqual;                                                           \
   using glsl::any;                                                                        \
+  using glsl::all;                                                                        \
+  using glsl::max;                                                                        \
+  using glsl::sampler1D;                                                                  \
+  using glsl::image1D;                                                                    \
+  using glsl::NS::exp;                                                                    \
+  using glsl::NS::sin;                                                                    \
+  using glsl::NS::cos;                                                                    \
+  using glsl::NS::acos;                                                                   \
+  using glsl::NS::fract;                                                                  \
+  using glsl::NS::mix;                                                                    \
+  using glsl::NS::sign;                                                                   \
+  using glsl::NS::greaterThan;                                                            \
+  using glsl::NS::lessThan;                                                               \
   typedef unsigned int uint;                                                              \
+  typedef glsl::NS::scalar glsl_cfloat;                                                   \
   thread_local uvec3 gl_GlobalInvocationID;

@@ -4,7 +4,7 @@ the reference's own shader code); the output goes to oracle/_ref/gen/ and is
 never committed.
 
 Only declarations are rewritten; every function body compiles as written:
-  1. the `#version` line is dropped;
+  1. the `#version` line and the comments are dropped;
   2. the work-group size declaration `layout(local_size_x = ...) in;` is
      dropped (the dispatch loop supplies gl_GlobalInvocationID);
   3. interface blocks `uniform NAME { ... };` and `buffer NAME { ... };`
@@ -13,16 +13,26 @@ Only declarations are rewritten; every function body compiles as written:
   4. the remaining `layout(...)` qualifiers and the qualifiers `uniform`,
      `readonly`, `writeonly`, `restrict`, `coherent` are dropped (a
      uniform's initialiser, its default value, stays);
-  5. a parameter `inout T x` becomes `T& x`;
+  5. a parameter `inout T x` or `out T x` becomes `T& x`, `in T x` becomes
+     `T x`;
   6. an unsuffixed floating literal gets the suffix `f` (a GLSL literal
      without `lf` is a float);
   7. a global whose initializer is not a constant (it reads a uniform or
-     calls a function), and every global that is not `const` but has an
-     initializer (invocation-private storage in GLSL; uniforms excepted), is
-     declared without it; the initialisations move, in source order, into
+     calls a function other than a constructor or a pure math built-in; a
+     constant reads only literals, macros and earlier constants), and every
+     global that is not `const` but has an initializer (invocation-private
+     storage in GLSL; uniforms excepted), is declared without it; the
+     initialisations move, in source order, into
      `void glsl_init_globals()`, which the dispatch calls after binding the
      uniforms (once per dispatch, or before each invocation for shaders that
-     write such globals).
+     write such globals);
+  8. a global `const float` with a constant initializer, and a `float`
+     uniform's default value, become `glsl_cfloat NAME = GLSL_CONST(NAME,
+     init)`: the compiler folds a shader's constants, and the GL sets a
+     uniform's default, in float.  The float build evaluates the
+     initializer; the double build (glsl_cfloat = double) takes the value the
+     float build folded, so its constants are the shader's float values and
+     only its run-time arithmetic is in double.
 
 Usage: python glsl_to_cpp.py SHADER.glsl OUT.inc
 """
@@ -34,7 +44,9 @@ from pathlib import Path
 
 QUALIFIERS = ("readonly", "writeonly", "restrict", "coherent")
 UNIFORM_MARK = "GLSL_UNIFORM"
+CONST_FLOAT = "glsl_cfloat"
 TYPE_NAMES = {"float", "int", "uint", "bool", "vec2", "vec3", "vec4", "ivec2", "ivec3", "ivec4", "uvec3", "mat4"}
+PURE_BUILTINS = {"sqrt", "pow", "exp", "sin", "cos", "abs", "min", "max", "floor"}
 
 
 def _drop_version(src: str) -> str:
@@ -68,17 +80,20 @@ def _qualifiers(src: str) -> str:
     return src
 
 
-def _inout(src: str) -> str:
-    return re.sub(r"\binout\s+(\w+)\s+(\w+)", r"\1& \2", src)
+def _strip_comments(src: str) -> str:
+    # one left-to-right pass, so a line comment that holds "/*" or "*/"
+    # (the "//*" block toggles) stays a line comment
+    return re.sub(r"//[^\n]*|/\*.*?\*/", lambda m: "" if m.group(0).startswith("//") else " ", src, flags=re.S)
+
+
+def _param_qualifiers(src: str) -> str:
+    # in a parameter list: `inout T x` / `out T x` -> `T& x`, `in T x` -> `T x`
+    src = re.sub(r"(?<=[(,])(\s*)(?:inout|out)\s+(\w+)\s+(\w+)", r"\1\2& \3", src)
+    return re.sub(r"(?<=[(,])(\s*)in\s+(\w+)\s+(\w+)", r"\1\2 \3", src)
 
 
 def _float_literals(src: str) -> str:
-    out = []
-    for line in src.split("\n"):
-        code, sep, comment = line.partition("//")
-        code = re.sub(r"(?<![\w.])(\d+\.\d*|\.\d+)([eE][+-]?\d+)?(?![\w.])", r"\1\2f", code)
-        out.append(code + sep + comment)
-    return "\n".join(out)
+    return re.sub(r"(?<![\w.])(\d+\.\d*|\.\d+)([eE][+-]?\d+)?(?![\w.])", r"\1\2f", src)
 
 
 def _macro_names(src: str) -> set[str]:
@@ -88,7 +103,7 @@ def _macro_names(src: str) -> set[str]:
 def _deferred_globals(src: str) -> tuple[str, list[str]]:
     """Top-level `[const] T name = init;` statements: keep constant ones,
     defer the rest (rule 7)."""
-    macros = _macro_names(src)
+    constant = _macro_names(src) | TYPE_NAMES | PURE_BUILTINS
     inits: list[str] = []
     out: list[str] = []
     depth = 0
@@ -101,10 +116,13 @@ def _deferred_globals(src: str) -> tuple[str, list[str]]:
             line_start = src.rfind("\n", 0, i) + 1
             if m and src[line_start:i].strip() == "" and m.group(2) not in ("return", "else"):
                 is_const, typ, name, init = m.group(1), m.group(2), m.group(3), m.group(4)
-                idents = set(re.findall(r"\b[A-Za-z_]\w*\b", init)) - TYPE_NAMES - macros
-                idents = {w for w in idents if not re.fullmatch(r"\d+\w*", w)}
+                idents = set(re.findall(r"\b[A-Za-z_]\w*\b", init)) - constant
                 if is_const and not idents:
-                    out.append(m.group(0))
+                    if typ == "float":  # rule 8
+                        out.append(f"const {CONST_FLOAT} {name} = GLSL_CONST({name}, {init.strip()});")
+                    else:
+                        out.append(f"const {typ} {name} = {init.strip()};")
+                    constant.add(name)
                 else:
                     out.append(f"{typ} {name};")
                     inits.append(f"  {name} = {init.strip()};")
@@ -121,12 +139,16 @@ def _deferred_globals(src: str) -> tuple[str, list[str]]:
 
 def transform(src: str) -> str:
     src = _drop_version(src)
+    src = _strip_comments(src)
     src = _drop_local_size(src)
     src = _blocks(src)
     src = _qualifiers(src)
-    src = _inout(src)
+    src = _param_qualifiers(src)
     src = _float_literals(src)
     src, inits = _deferred_globals(src)
+    # rule 8 for a float uniform's default value
+    src = re.sub(rf"{UNIFORM_MARK}\s+float\s+(\w+)\s*=\s*([^;]+);",
+                 lambda m: f"{CONST_FLOAT} {m.group(1)} = GLSL_CONST({m.group(1)}, {m.group(2).strip()});", src)
     src = re.sub(rf"{UNIFORM_MARK}\s*", "", src)
     return src + "\nvoid glsl_init_globals() {\n" + "\n".join(inits) + "\n}\n"
 

@@ -31,12 +31,15 @@
     return 0;                                                                            \
   }
 
+#define GLSL_CONST(name, init) (init)
 namespace ref_force_f32 {
 GLSL_PRELUDE(f32)
 #include "force_comp.inc"
 REF_FORCE_RUN
 }  // namespace ref_force_f32
 
+#undef GLSL_CONST
+#define GLSL_CONST(name, init) (ref_force_f32::name)
 namespace ref_force_f64 {
 GLSL_PRELUDE(f64)
 #define float double

@@ -11,6 +11,8 @@
 #include "glsl.h"
 #include "ref_shaders.h"
 
+#define GLSL_CONST(name, init) (init)
+
 namespace ref_ugrid {
 GLSL_PRELUDE(f32)
 #include "ugrid_particles_cs.inc"

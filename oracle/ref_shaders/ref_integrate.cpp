@@ -25,12 +25,15 @@
     return 0;                                                                            \
   }
 
+#define GLSL_CONST(name, init) (init)
 namespace ref_integrate_f32 {
 GLSL_PRELUDE(f32)
 #include "integrate_comp.inc"
 REF_INTEGRATE_RUN
 }  // namespace ref_integrate_f32
 
+#undef GLSL_CONST
+#define GLSL_CONST(name, init) (ref_integrate_f32::name)
 namespace ref_integrate_f64 {
 GLSL_PRELUDE(f64)
 #define float double

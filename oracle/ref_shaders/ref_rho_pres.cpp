@@ -32,12 +32,15 @@
     return 0;                                                                            \
   }
 
+#define GLSL_CONST(name, init) (init)
 namespace ref_rho_pres_f32 {
 GLSL_PRELUDE(f32)
 #include "rho_pres_comp.inc"
 REF_RHO_PRES_RUN
 }  // namespace ref_rho_pres_f32
 
+#undef GLSL_CONST
+#define GLSL_CONST(name, init) (ref_rho_pres_f32::name)
 namespace ref_rho_pres_f64 {
 GLSL_PRELUDE(f64)
 #define float double

@@ -46,6 +46,31 @@ int32_t ref_integrate(int32_t prec, double* p16, int32_t n, const float* wave, i
 int32_t ref_wave(int32_t prec, const double* u_n, const double* u_nm1, double* out, int32_t w, int32_t h,
                  const float* init_rgba, int32_t iw, int32_t ih, const ref_uniforms* u);
 
+// The 2D family (SphWave2D).  Particles are n records of 12 doubles (pos,
+// vel, acc: SphWaveKoschier2D_grid_cs.glsl:39-44); fields are n cells of 4
+// floats (rgba32f image1D).
+typedef struct ref2d_uniforms {
+  float time, bottom;                  // SphWaveKoschier2D_grid_cs.glsl uniforms
+  int32_t grid_cells[2];               // UniformGridSph2D: 32 x 32
+  float extent_max[2];                 // over [0, extent_max]: 9.6 x 9.6
+  float lambda, dx, atten, beta;       // Shallow1D / Wave1D uniforms
+  float boundary[2];
+} ref2d_uniforms;
+
+// The grid of `in`, then one mode (0 init, 1 density/pressure, 2 forces)
+// reading `in`, writing `out`.  -1 unless the cell count is a power of two.
+int32_t ref2d_sph(int32_t prec, int32_t mode, const double* in12, double* out12, int32_t n, const float* wave4,
+                  int32_t wave_n, const ref2d_uniforms* u);
+// One substep as SphUgrid::Compute runs it: the grid of `in`, density
+// (in -> dens), forces (dens -> force) on that same grid.
+int32_t ref2d_substep(int32_t prec, const double* in12, double* dens12, double* force12, int32_t n,
+                      const float* wave4, int32_t wave_n, const ref2d_uniforms* u);
+// One dispatch of Shallow1D_cs.glsl (kind 0; image in0) or Wave1D_cs.glsl
+// (kind 1; images in0 = t-1, in1 = t-2) in `mode`; out4 holds the output
+// image (cells the dispatch does not write keep their values).
+int32_t ref2d_field(int32_t kind, int32_t mode, const float* in0, const float* in1, float* out4, int32_t n,
+                    const float* init4, int32_t init_n, const ref2d_uniforms* u);
+
 #ifdef __cplusplus
 }
 

@@ -34,12 +34,15 @@
     return 0;                                                                                 \
   }
 
+#define GLSL_CONST(name, init) (init)
 namespace ref_wave_f32 {
 GLSL_PRELUDE(f32)
 #include "wave_comp.inc"
 REF_WAVE_RUN
 }  // namespace ref_wave_f32
 
+#undef GLSL_CONST
+#define GLSL_CONST(name, init) (ref_wave_f32::name)
 namespace ref_wave_f64 {
 GLSL_PRELUDE(f64)
 #define float double

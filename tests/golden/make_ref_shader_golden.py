@@ -1,8 +1,8 @@
 """Regenerate tests/golden/ref_shader_outputs.npz: outputs of the reference's
 own compute shaders (CoupledWaterAnimation/rho_pres_comp.glsl,
 force_comp.glsl, integrate_comp.glsl, wave_comp.glsl;
-UniformGrid2D/ugrid_particles_cs.glsl and prefix_sum_cs.glsl) run on the
-CPU, on the seeded inputs of oracle/ref.py.
+UniformGrid2D/ugrid_particles_cs.glsl and prefix_sum_cs.glsl; the SphWave2D
+family) run on the CPU, on the seeded inputs of oracle/ref.py.
 
 The shaders are compiled as C++ (oracle/ref_shaders/: the GLSL source with
 its declarations rewritten, against a GLSL types-and-built-ins header) in
@@ -28,7 +28,14 @@ Cases (every input regenerates from oracle/ref.py; its SHA-256 is stored):
            cell faces) and a jittered 24 x 20 x 24 lattice (32^3 cells): counts,
            offsets and index list;
   scan     the scan alone on the reference's ParallelScanTest vector and on
-           2^10 and 2^14 values.
+           2^10 and 2^14 values;
+  s2d      the 2D family (SphWave2D): InitParticle; one SphUgrid substep
+           (the grid of uniform_grid_sph_cs.glsl, then the density and force
+           modes of SphWaveKoschier2D_grid_cs.glsl on that grid) of a jittered
+           lattice with particles past the grid and below the floor, stored
+           for every 4th particle; Shallow1D InitWave, Splash, predictor and
+           corrector; Wave1D InitWave (modes 0 and 1) and one iteration.  The
+           bit-exact ones are stored as SHA-256 of their float32 bytes.
 
 Usage:  python tests/golden/make_ref_shader_golden.py
         (needs the reference checkout; CWA_REFERENCE names it if it is not
@@ -52,7 +59,12 @@ WAVE_MODES = {"m1": 1.0, "m0": 0.0, "m05": 0.5}
 
 
 def sha(a: np.ndarray) -> str:
-    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    """SHA-256 of an array's bytes, every NaN as the positive quiet NaN
+    (a NaN's sign and payload differ between x86, Arm and the GPU)."""
+    a = np.ascontiguousarray(a).copy()
+    if a.dtype.kind == "f":
+        a[np.isnan(a)] = np.nan
+    return hashlib.sha256(a.tobytes()).hexdigest()
 
 
 def reference_desc():
@@ -64,6 +76,48 @@ def reference_desc():
 def inputs() -> dict[str, np.ndarray]:
     from oracle import ref
     return ref.fixture_inputs(np.load(HERE / "init_textures.npz")["splash"])
+
+
+S2D_SAMPLE = np.arange(0, 4096, 4)
+
+
+def sph2d_cases(ref, x, out) -> None:
+    """The 2D family (SphWave2D): bit-exact cases as SHA-256 of their float32
+    bytes, the SPH passes on a sample of particles."""
+    from coupledwateranimation_gb300._abi import WAVE2D_1D
+    from coupledwateranimation_gb300.sim2d import defaults2d
+    p = defaults2d()
+    u = ref.uniforms_2d(p)
+    n = p.n_particles
+    z = np.zeros((p.wave_cells, 4), np.float32)
+    init = ref.sph2d(ref.F32, 0, np.zeros((n, 12)), z, u).astype(np.float32)
+    out["s2d_init_sha"] = np.array(sha(init))
+    out["s2d_sample"] = S2D_SAMPLE
+    st = x["s2d_state"].astype(np.float64)
+    for prec, tag, dt in ((ref.F32, "f32", np.float32), (ref.F64, "f64", np.float64)):
+        dens, force = ref.substep2d(prec, st, x["s2d_wave"], u)
+        out[f"s2d_density_{tag}"] = dens[S2D_SAMPLE].astype(dt)
+        out[f"s2d_force_{tag}"] = force[S2D_SAMPLE].astype(dt)
+    # Shallow1D: InitWave, Splash on it, the predictor (into the buffer that
+    # held the splash), the corrector (into the buffer that held the splash)
+    init0 = ref.field2d(0, 0, z, None, z, u)
+    splash = ref.field2d(0, 1, init0, None, init0, u)
+    pred = ref.field2d(0, 2, splash, None, splash, u)
+    corr = ref.field2d(0, 3, pred, None, splash, u)
+    for name, a in (("init", init0), ("splash", splash), ("corr", corr)):
+        out[f"s2d_shallow_{name}_sha"] = np.array(sha(a))
+    out["s2d_shallow_init"], out["s2d_shallow_splash"] = init0, splash  # the GPU's inputs (expf-free steps)
+    out["s2d_shallow_pred_sha"] = np.array(sha(pred[1:]))  # cell 0: see the test
+    # Wave1D on the app's 1024 cells
+    p1 = defaults2d(WAVE2D_1D)
+    u1 = ref.uniforms_2d(p1)
+    z1 = np.zeros((p1.wave_cells, 4), np.float32)
+    w0 = ref.field2d(1, 0, z1, z1, z1, u1)
+    w1 = ref.field2d(1, 1, w0, z1, w0, u1)
+    it = ref.field2d(1, 2, w1, w0, z1, u1)
+    for name, a in (("init0", w0), ("init1", w1), ("iter", it)):
+        out[f"s2d_wave1d_{name}_sha"] = np.array(sha(a))
+    out["s2d_wave1d_init0"], out["s2d_wave1d_init1"] = w0, w1
 
 
 def main() -> None:
@@ -112,6 +166,7 @@ def main() -> None:
         out[f"{name}_counts"], out[f"{name}_offsets"], out[f"{name}_list"] = counts, offsets, lst
     for name in ref.scan_inputs():
         out[f"{name}_out"] = ref.exclusive_scan(x[name])
+    sph2d_cases(ref, x, out)
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
 

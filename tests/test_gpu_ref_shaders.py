@@ -17,7 +17,11 @@ preset:
   * the stand-alone grid build (cwa_grid_build) and the exclusive scan
     (cwa_exclusive_scan_i32) bit-exact against
     UniformGrid2D/ugrid_particles_cs.glsl and prefix_sum_cs.glsl (the
-    no-allocation scan's check is in test_zz_no_alloc.py).
+    no-allocation scan's check is in test_zz_no_alloc.py);
+  * the 2D family (cwa2d_*): initial particles bit-exact and initial fields
+    within 1e-6 (expf), one substep's grid, density and forces within the
+    oracle's bars of the double shaders, the shallow-water and Wave1D steps
+    bit-exact.
 """
 from __future__ import annotations
 
@@ -159,3 +163,78 @@ def test_exclusive_scan_matches_the_reference_scan_shader(lib, x, name):
     assert st == 0, _abi.last_error()
     assert lib.cwa_scan_status(n, _abi.ptr(ws), stream) == 0, _abi.last_error()
     assert np.array_equal(out.cpu().numpy(), G[f"{name}_out"])
+
+
+# ---- the 2D family (SphWave2D) ---------------------------------------------
+def _sha(a) -> str:
+    """SHA-256 of the bytes, NaNs as the positive quiet NaN (the GPU's NaN
+    differs from the host's in sign and payload)."""
+    import hashlib
+    a = np.ascontiguousarray(a).copy()
+    if a.dtype.kind == "f":
+        a[np.isnan(a)] = np.nan
+    return hashlib.sha256(a.tobytes()).hexdigest()
+
+
+def _f12(rec):
+    return np.ascontiguousarray(rec).view(np.float32).reshape(-1, 12)
+
+
+def test_2d_init_matches_the_shaders(lib):
+    """InitParticle (bit-exact) and Shallow1D InitWave and Splash from
+    cwa2d_create: the fields go through expf, which the GPU and the host
+    library round differently in the last bit, so they are held to 1e-6 of
+    the shaders' fields."""
+    from coupledwateranimation_gb300.sim2d import Sim2D
+    init0, splash = G["s2d_shallow_init"], G["s2d_shallow_splash"]
+    with Sim2D() as sim:
+        assert _sha(_f12(sim.download_particles())) == str(G["s2d_init_sha"])
+        assert np.allclose(sim.download_wave(), init0, rtol=1e-6, atol=1e-6)
+        sim.splash()
+        assert np.allclose(sim.download_wave(), splash, rtol=1e-6, atol=1e-6)
+
+
+def test_2d_substep_matches_the_shaders(lib, x):
+    """Grid, density, forces on a state with particles past the grid's
+    extents and below the floor, against the double shaders: the bars of
+    the oracle's own check (rho 1e-5, forces 5e-5 normwise)."""
+    from coupledwateranimation_gb300._abi import PARTICLE2D_DTYPE
+    from coupledwateranimation_gb300.sim2d import Sim2D
+    s = G["s2d_sample"]
+    with Sim2D() as sim:
+        sim.upload_particles(np.ascontiguousarray(x["s2d_state"]).view(PARTICLE2D_DTYPE).reshape(-1))
+        sim.upload_wave(x["s2d_wave"])
+        sim.run_pass("grid")
+        sim.run_pass("density")
+        d = _f12(sim.download_particles()).astype(np.float64)
+        sim.run_pass("force")
+        f = _f12(sim.download_particles()).astype(np.float64)
+    want = G["s2d_density_f64"]
+    assert np.array_equal(d[s][:, 3], want[:, 3])
+    assert np.max(np.abs(d[s][:, 11] - want[:, 11]) / want[:, 11]) <= 1e-5
+    assert np.max(np.abs(d[s][:, 7] - want[:, 7])) / np.max(np.abs(want[:, 7])) <= 2e-5
+    assert np.max(np.abs(d[s][:, :2] - want[:, :2])) <= 1e-6
+    wf = G["s2d_force_f64"]
+    for k in (8, 9):
+        assert np.max(np.abs(f[s][:, k] - wf[:, k])) / np.max(np.abs(wf[:, k])) <= 5e-5, k
+    for k in (0, 1, 4, 5):
+        assert np.max(np.abs(f[s][:, k] - wf[:, k])) / np.max(np.abs(wf[:, k])) <= 1e-5, k
+
+
+def test_2d_fields_match_the_shaders_bit_exactly(lib):
+    """The Lax-Wendroff predictor and corrector on the splash field (the
+    predictor's cell 0 aside: two invocations write it, see
+    tests/test_ref_shaders.py), and one Wave1D iteration."""
+    from coupledwateranimation_gb300._abi import WAVE2D_1D
+    from coupledwateranimation_gb300.sim2d import Sim2D, defaults2d
+    with Sim2D() as sim:
+        sim.upload_wave(G["s2d_shallow_splash"])
+        sim.run_pass("wave_predict")
+        assert _sha(sim.download_wave()[1:]) == str(G["s2d_shallow_pred_sha"])
+        sim.run_pass("wave_correct")
+        assert _sha(sim.download_wave()) == str(G["s2d_shallow_corr_sha"])
+    with Sim2D(defaults2d(WAVE2D_1D)) as sim:
+        sim.upload_wave(G["s2d_wave1d_init1"])
+        sim.upload_wave_prev(G["s2d_wave1d_init0"])
+        sim.run_pass("wave_iterate")
+        assert _sha(sim.download_wave()) == str(G["s2d_wave1d_iter_sha"])

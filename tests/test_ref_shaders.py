@@ -34,7 +34,11 @@ G = np.load(GOLDEN / "ref_shader_outputs.npz")
 
 
 def _sha(a: np.ndarray) -> str:
-    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    """SHA-256 of the bytes, NaNs as the positive quiet NaN (as the fixtures)."""
+    a = np.ascontiguousarray(a).copy()
+    if a.dtype.kind == "f":
+        a[np.isnan(a)] = np.nan
+    return hashlib.sha256(a.tobytes()).hexdigest()
 
 
 @pytest.fixture(scope="module")
@@ -232,3 +236,87 @@ def test_live_shaders_reproduce_the_fixtures(x, desc):
             assert np.array_equal(a, G[f"{name}_{part}"])
     for name in ref.scan_inputs():
         assert np.array_equal(ref.exclusive_scan(x[name]), G[f"{name}_out"])
+
+
+# ---- the 2D family (SphWave2D) ---------------------------------------------
+@pytest.fixture(scope="module")
+def p2d():
+    from coupledwateranimation_gb300.sim2d import defaults2d
+    return defaults2d()
+
+
+def _records2d(a):
+    from coupledwateranimation_gb300._abi import PARTICLE2D_DTYPE
+    return np.ascontiguousarray(a, np.float32).view(PARTICLE2D_DTYPE).reshape(-1)
+
+
+def _f12(rec):
+    return np.ascontiguousarray(rec).view(np.float32).reshape(-1, 12)
+
+
+def test_2d_init_particles_equal_the_shader_bit_exactly(orc, p2d):
+    """InitParticle (SphWaveKoschier2D_grid_cs.glsl:308-333)."""
+    from coupledwateranimation_gb300._abi import PARTICLE2D_DTYPE
+    got = _f12(orc.init_particles_2d(p2d, PARTICLE2D_DTYPE))
+    assert _sha(got) == str(G["s2d_init_sha"])
+
+
+def test_2d_substep_equals_the_shaders(orc, x, p2d):
+    """One SphUgrid::Compute substep (SphWave2D/StencilBuffer.cpp:150-179):
+    the grid of uniform_grid_sph_cs.glsl, then ComputeDensityPressure and
+    ComputeForces on that grid.  The state holds particles outside the grid
+    (in no cell list, so they see no neighbour, not even themselves) and
+    below the floor (moved by the density pass, after the grid was built).
+    FP64 oracle against the double shaders, within 1e-5 (rho, per particle)
+    and 5e-5 (forces, normwise): the oracle forms the wall planes' offsets
+    in float and stores float32 records, the double shaders compute the
+    offsets in double, and the forces' pressure and viscous differences
+    amplify both.  (A particle wrongly in or out of a cell list moves rho by
+    10-30%.)"""
+    s = G["s2d_sample"]
+    st = _records2d(x["s2d_state"])
+    dens = orc.density_2d(p2d, st, x["s2d_wave"])
+    d = _f12(dens).astype(np.float64)
+    want = G["s2d_density_f64"]
+    assert np.array_equal(d[s][:, 3], want[:, 3])  # enable flags
+    assert np.max(np.abs(d[s][:, 11] - want[:, 11]) / want[:, 11]) <= 1e-5  # rho
+    assert np.max(np.abs(d[s][:, 7] - want[:, 7])) / np.max(np.abs(want[:, 7])) <= 2e-5  # pressure
+    assert np.max(np.abs(d[s][:, :2] - want[:, :2])) <= 1e-6  # positions after the wall projection
+    forc = _f12(orc.force_2d(p2d, dens, x["s2d_wave"], grid_from=st)).astype(np.float64)
+    wf = G["s2d_force_f64"]
+    for k in (8, 9):  # acceleration
+        assert np.max(np.abs(forc[s][:, k] - wf[:, k])) / np.max(np.abs(wf[:, k])) <= 5e-5, k
+    for k in (0, 1, 4, 5):  # the Euler update's positions and velocities
+        assert np.max(np.abs(forc[s][:, k] - wf[:, k])) / np.max(np.abs(wf[:, k])) <= 1e-5, k
+    # the particles outside the grid: density from the wall term alone
+    assert np.all(want[:2, 11] >= 1000.0)
+
+
+def test_2d_fields_equal_the_shaders_bit_exactly(orc):
+    """Shallow1D (InitWave, Splash, the Lax-Wendroff predictor and corrector,
+    Shallow1D_cs.glsl:88-174) and Wave1D (InitWave in modes 0 and 1, one
+    iteration, Wave1D_cs.glsl:92-207) in float32.  The predictor's cell 0 is
+    written by two invocations (its own final store and cell 1's FreeBC copy,
+    Shallow1D_cs.glsl:146-152, 195-201), an order GLSL leaves open: the
+    restatement keeps the own store, as a warp executing both in lockstep
+    does; the CPU dispatch runs cell 1 last.  It is left out."""
+    from coupledwateranimation_gb300._abi import WAVE2D_1D
+    from coupledwateranimation_gb300.sim2d import defaults2d
+    p = defaults2d()
+    z = np.zeros((p.wave_cells, 4), np.float32)
+    init0 = orc.wave_init_2d_f32(p, z, splash=False)
+    splash = orc.wave_init_2d_f32(p, init0, splash=True)
+    pred = orc.wave_iter_2d_f32(p, splash, 0, out_prev=splash)
+    corr = orc.wave_iter_2d_f32(p, pred, 1, out_prev=splash)
+    assert _sha(init0) == str(G["s2d_shallow_init_sha"])
+    assert _sha(splash) == str(G["s2d_shallow_splash_sha"])
+    assert _sha(pred[1:]) == str(G["s2d_shallow_pred_sha"])
+    assert _sha(corr) == str(G["s2d_shallow_corr_sha"])
+    p1 = defaults2d(WAVE2D_1D)
+    z1 = np.zeros((p1.wave_cells, 4), np.float32)
+    w0 = orc.wave1d_init_2d_f32(p1, 0, z1, z1)
+    w1 = orc.wave1d_init_2d_f32(p1, 1, w0, z1)
+    it = orc.wave1d_iter_2d_f32(p1, w1, w0)
+    assert _sha(w0) == str(G["s2d_wave1d_init0_sha"])
+    assert _sha(w1) == str(G["s2d_wave1d_init1_sha"])
+    assert _sha(it) == str(G["s2d_wave1d_iter_sha"])
