@@ -58,6 +58,34 @@ def uniforms_2d(params) -> Uniforms2D:
     return u
 
 
+class PbdParams(C.Structure):
+    """ref_pbd_params (oracle/ref_shaders/ref_shaders.h)."""
+    _fields_ = [("grid_cells", C.c_int32 * 3), ("lo", C.c_float * 3), ("hi", C.c_float * 3), ("g", C.c_float * 3),
+                ("dt", C.c_float), ("damping", C.c_float), ("k", C.c_float), ("k_static", C.c_float),
+                ("sleep_thresh", C.c_float), ("mu_k", C.c_float), ("mu_s", C.c_float), ("e", C.c_float),
+                ("substeps", C.c_int32)]
+
+
+def pbd_params(params) -> PbdParams:
+    """The shader's Params block and grid from a cwa_pbd_params."""
+    q = PbdParams()
+    q.grid_cells[:] = list(params.grid_cells)
+    q.lo[:] = list(params.extents_lo)
+    q.hi[:] = list(params.extents_hi)
+    q.g[:] = list(params.g)
+    for f in ("dt", "damping", "k", "k_static", "sleep_thresh", "mu_k", "mu_s", "e", "substeps"):
+        setattr(q, f, getattr(params, f))
+    return q
+
+
+def pbd(prec: int, boxes32: np.ndarray, frames: int, q: PbdParams) -> np.ndarray:
+    """`frames` frames of the PBD shader on (n, 32) box records."""
+    a = np.ascontiguousarray(boxes32, np.float64).copy()
+    if load().ref_pbd(prec, _dp(a), len(a), frames, C.byref(q)) != 0:
+        raise ValueError("ref_pbd needs nx == nz and a power-of-two cell count")
+    return a
+
+
 def reference_root() -> Path | None:
     ref = Path(os.environ.get("CWA_REFERENCE", str(DEFAULT_REFERENCE)))
     return ref if (ref / "CoupledWaterAnimation" / "rho_pres_comp.glsl").is_file() else None
@@ -102,6 +130,8 @@ def load():
         lib.ref2d_substep.restype = C.c_int32
         lib.ref2d_field.argtypes = [C.c_int32, C.c_int32, fp, fp, fp, C.c_int32, fp, C.c_int32, u2]
         lib.ref2d_field.restype = C.c_int32
+        lib.ref_pbd.argtypes = [C.c_int32, dp, C.c_int32, C.c_int32, C.POINTER(PbdParams)]
+        lib.ref_pbd.restype = C.c_int32
         _lib = lib
     return _lib
 
@@ -381,6 +411,23 @@ def shallow_field(params) -> np.ndarray:
     return f
 
 
+def pbd_boxes(params, n: int | None = None) -> np.ndarray:
+    """(n, 32) float32 box records (PbdObj) as GridTestPbdGpu3D::Init lays
+    them out: positions 0.5 U(-1, 1)^3, velocities 0.1 U(-1, 1)^3, half widths
+    U(0.15, 0.45) cell edges per axis, 1 / mass = 1 / (hw.x hw.y hw.z), white."""
+    n = params.n_boxes if n is None else n
+    b = np.zeros((n, 32), np.float32)
+    b[:, 0:4] = 1.0
+    edge = [(params.extents_hi[a] - params.extents_lo[a]) / params.grid_cells[a] for a in range(3)]
+    for a in range(3):
+        b[:, 4 + a] = _u32(701 + a, n, -0.5, 0.5)
+        b[:, 8 + a] = _u32(711 + a, n, -0.1, 0.1)
+        b[:, 24 + a] = _u32(721 + a, n, 0.15, 0.45) * np.float32(edge[a])
+    b[:, 7] = 1.0
+    b[:, 28] = np.float32(1.0) / (b[:, 24] * b[:, 25] * b[:, 26])
+    return b
+
+
 def fixture_inputs(splash_rgba8: np.ndarray) -> dict[str, np.ndarray]:
     """Every input of tests/golden/ref_shader_outputs.npz (its cases are
     listed in tests/golden/make_ref_shader_golden.py).  splash_rgba8: the
@@ -400,7 +447,14 @@ def fixture_inputs(splash_rgba8: np.ndarray) -> dict[str, np.ndarray]:
         **{name: case[0]() for name, case in GRID_CASES.items()},
         **scan_inputs(),
         **sph2d_inputs(),
+        **pbd_inputs(),
     }
+
+
+def pbd_inputs() -> dict[str, np.ndarray]:
+    """The PBD demo's boxes, from the library's default parameters."""
+    from coupledwateranimation_gb300.pbd import pbd_defaults
+    return {"pbd_boxes": pbd_boxes(pbd_defaults())}
 
 
 def sph2d_inputs() -> dict[str, np.ndarray]:

@@ -202,7 +202,12 @@ struct ivec3 {
   friend ivec3 operator+(const ivec3& a, const ivec3& b) { return ivec3(a.x + b.x, a.y + b.y, a.z + b.z); }
   friend ivec3 operator-(const ivec3& a, const ivec3& b) { return ivec3(a.x - b.x, a.y - b.y, a.z - b.z); }
   friend ivec3 operator*(const ivec3& a, const ivec3& b) { return ivec3(a.x * b.x, a.y * b.y, a.z * b.z); }
+  friend bool operator==(const ivec3& a, const ivec3& b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
 };
+
+inline ivec3 max(const ivec3& a, const ivec3& b) {
+  return ivec3(b.x > a.x ? b.x : a.x, b.y > a.y ? b.y : a.y, b.z > a.z ? b.z : a.z);
+}
 
 struct ivec4 {
   union {
@@ -229,6 +234,17 @@ inline ivec3 clamp(const ivec3& v, const ivec3& lo, const ivec3& hi) {
 // another, so the returned old values come in invocation order.
 inline int atomicAdd(int& mem, int v) {
   const int old = mem;
+  mem = old + v;
+  return old;
+}
+// float atomics (GL_NV_shader_atomic_float), and their double-build form
+inline float atomicAdd(float& mem, float v) {
+  const float old = mem;
+  mem = old + v;
+  return old;
+}
+inline double atomicAdd(double& mem, double v) {
+  const double old = mem;
   mem = old + v;
   return old;
 }

@@ -4,12 +4,13 @@ the reference's own shader code); the output goes to oracle/_ref/gen/ and is
 never committed.
 
 Only declarations are rewritten; every function body compiles as written:
-  1. the `#version` line and the comments are dropped;
+  1. the `#version` and `#extension` lines and the comments are dropped;
   2. the work-group size declaration `layout(local_size_x = ...) in;` is
      dropped (the dispatch loop supplies gl_GlobalInvocationID);
   3. interface blocks `uniform NAME { ... };` and `buffer NAME { ... };`
-     become their members as globals; a runtime-sized array `T a[];` becomes
-     a pointer `T* a;` that the dispatch binds;
+     become their members as globals (an instance-named block
+     `... } inst;` a struct NAME and its instance); a runtime-sized array
+     `T a[];` becomes a pointer `T* a;` that the dispatch binds;
   4. the remaining `layout(...)` qualifiers and the qualifiers `uniform`,
      `readonly`, `writeonly`, `restrict`, `coherent` are dropped (a
      uniform's initialiser, its default value, stays);
@@ -50,7 +51,8 @@ PURE_BUILTINS = {"sqrt", "pow", "exp", "sin", "cos", "abs", "min", "max", "floor
 
 
 def _drop_version(src: str) -> str:
-    return re.sub(r"^\s*#version[^\n]*\n", "", src, count=1, flags=re.M)
+    src = re.sub(r"^\s*#version[^\n]*\n", "", src, count=1, flags=re.M)
+    return re.sub(r"^\s*#extension[^\n]*\n", "", src, flags=re.M)
 
 
 def _drop_local_size(src: str) -> str:
@@ -61,10 +63,9 @@ def _blocks(src: str) -> str:
     pat = re.compile(r"(?:layout\s*\([^)]*\)\s*)?\b(uniform|buffer)\s+(\w+)\s*\{(.*?)\}\s*(\w*)\s*;", re.S)
 
     def repl(m: re.Match) -> str:
-        if m.group(4):
-            raise SystemExit(f"instance-named interface block {m.group(2)} is not handled")
-        body = m.group(3)
-        body = re.sub(r"(\w+)\s+(\w+)\s*\[\s*\]\s*;", r"\1* \2 = nullptr;", body)
+        body = re.sub(r"(\w+)\s+(\w+)\s*\[\s*\]\s*;", r"\1* \2 = nullptr;", m.group(3))
+        if m.group(4):  # an instance-named block: a struct and its instance
+            return f"struct {m.group(2)} {{{body}}};\n{m.group(2)} {m.group(4)};"
         return body
 
     return pat.sub(repl, src)

@@ -71,6 +71,19 @@ int32_t ref2d_substep(int32_t prec, const double* in12, double* dens12, double* 
 int32_t ref2d_field(int32_t kind, int32_t mode, const float* in0, const float* in1, float* out4, int32_t n,
                     const float* init4, int32_t init_n, const ref2d_uniforms* u);
 
+// PBD boxes (UniformGrid2D/uniform_grid_pbd_3D_cs.glsl): records of 32
+// doubles (PbdObj: color, x, v, p, dp_t, dp_n, hw, then rm, n, e, padding).
+typedef struct ref_pbd_params {
+  int32_t grid_cells[3];
+  float lo[3], hi[3];
+  float g[3], dt, damping, k, k_static, sleep_thresh, mu_k, mu_s, e;
+  int32_t substeps;
+} ref_pbd_params;
+
+// `frames` frames of GridTestPbdGpu3D::Animate.  -1 unless the grid has
+// nx == nz and a power-of-two cell count.
+int32_t ref_pbd(int32_t prec, double* b32, int32_t n, int32_t frames, const ref_pbd_params* q);
+
 #ifdef __cplusplus
 }
 

@@ -1,8 +1,9 @@
 """Regenerate tests/golden/ref_shader_outputs.npz: outputs of the reference's
 own compute shaders (CoupledWaterAnimation/rho_pres_comp.glsl,
 force_comp.glsl, integrate_comp.glsl, wave_comp.glsl;
-UniformGrid2D/ugrid_particles_cs.glsl and prefix_sum_cs.glsl; the SphWave2D
-family) run on the CPU, on the seeded inputs of oracle/ref.py.
+UniformGrid2D/ugrid_particles_cs.glsl, prefix_sum_cs.glsl and
+uniform_grid_pbd_3D_cs.glsl; the SphWave2D family) run on the CPU, on the
+seeded inputs of oracle/ref.py.
 
 The shaders are compiled as C++ (oracle/ref_shaders/: the GLSL source with
 its declarations rewritten, against a GLSL types-and-built-ins header) in
@@ -35,7 +36,12 @@ Cases (every input regenerates from oracle/ref.py; its SHA-256 is stored):
            lattice with particles past the grid and below the floor, stored
            for every 4th particle; Shallow1D InitWave, Splash, predictor and
            corrector; Wave1D InitWave (modes 0 and 1) and one iteration.  The
-           bit-exact ones are stored as SHA-256 of their float32 bytes.
+           bit-exact ones are stored as SHA-256 of their float32 bytes;
+  pbd      one frame of UniformGrid2D/uniform_grid_pbd_3D_cs.glsl (the box
+           grid, PreAnimate, the collision query, PostAnimate, as
+           GridTestPbdGpu3D::Animate sequences them) on the demo's 4096
+           boxes: the constraint counts and colours as SHA-256, every 8th
+           box's record.
 
 Usage:  python tests/golden/make_ref_shader_golden.py
         (needs the reference checkout; CWA_REFERENCE names it if it is not
@@ -120,6 +126,21 @@ def sph2d_cases(ref, x, out) -> None:
     out["s2d_wave1d_init0"], out["s2d_wave1d_init1"] = w0, w1
 
 
+PBD_SAMPLE = np.arange(0, 4096, 8)
+
+
+def pbd_cases(ref, x, out) -> None:
+    """One frame of the PBD demo in float: the constraint counts and colours
+    (the contact set) as SHA-256, every 8th box's record in full."""
+    from coupledwateranimation_gb300.pbd import pbd_defaults
+    q = ref.pbd_params(pbd_defaults())
+    r = ref.pbd(ref.F32, x["pbd_boxes"].astype(np.float64), 1, q).astype(np.float32)
+    out["pbd_counts_sha"] = np.array(sha(r[:, 29]))
+    out["pbd_colors_sha"] = np.array(sha(r[:, 0:4]))
+    out["pbd_sample"] = PBD_SAMPLE
+    out["pbd_frame1_f32"] = r[PBD_SAMPLE]
+
+
 def main() -> None:
     from oracle import ref
     if ref.build() is None or ref.load() is None:
@@ -167,6 +188,7 @@ def main() -> None:
     for name in ref.scan_inputs():
         out[f"{name}_out"] = ref.exclusive_scan(x[name])
     sph2d_cases(ref, x, out)
+    pbd_cases(ref, x, out)
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
 

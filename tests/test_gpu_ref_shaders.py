@@ -238,3 +238,23 @@ def test_2d_fields_match_the_shaders_bit_exactly(lib):
         sim.upload_wave_prev(G["s2d_wave1d_init0"])
         sim.run_pass("wave_iterate")
         assert _sha(sim.download_wave()) == str(G["s2d_wave1d_iter_sha"])
+
+
+# ---- PBD boxes ---------------------------------------------------------------
+def test_pbd_frame_matches_the_shader(lib, x):
+    """One frame on the GPU (cwa_pbd_step) against uniform_grid_pbd_3D_cs.glsl
+    run on the CPU: the same contacts (every box's constraint count, the
+    colours), the continuous fields within the rounding of the shader's
+    float atomics (the GPU gathers the contacts in a fixed order)."""
+    from coupledwateranimation_gb300._abi import PBD_BOX_DTYPE
+    from coupledwateranimation_gb300.pbd import PbdSim, pbd_defaults
+    with PbdSim(pbd_defaults()) as sim:
+        sim.upload(np.ascontiguousarray(x["pbd_boxes"]).view(PBD_BOX_DTYPE).reshape(-1))
+        sim.step(1)
+        got = np.ascontiguousarray(sim.download()).view(np.float32).reshape(-1, 32)
+    assert _sha(got[:, 29]) == str(G["pbd_counts_sha"]) and _sha(got[:, 0:4]) == str(G["pbd_colors_sha"])
+    s = G["pbd_sample"]
+    g, w = got[s].astype(np.float64), G["pbd_frame1_f32"].astype(np.float64)
+    for sl, tol in ((slice(4, 7), 1e-6), (slice(12, 15), 1e-6), (slice(8, 11), 1e-5),
+                    (slice(16, 19), 1e-5), (slice(20, 23), 1e-5)):
+        assert np.max(np.abs(g[:, sl] - w[:, sl])) <= tol * np.max(np.abs(w[:, sl])), sl

@@ -320,3 +320,32 @@ def test_2d_fields_equal_the_shaders_bit_exactly(orc):
     assert _sha(w0) == str(G["s2d_wave1d_init0_sha"])
     assert _sha(w1) == str(G["s2d_wave1d_init1_sha"])
     assert _sha(it) == str(G["s2d_wave1d_iter_sha"])
+
+
+# ---- PBD boxes ---------------------------------------------------------------
+def _pbd_close(got32, want32):
+    """One frame: the contact set exact (constraint counts, colours); the
+    continuous fields within the float rounding of the shader's atomic adds,
+    which the restatement makes in another (fixed) order."""
+    g = np.asarray(got32, np.float64)
+    w = np.asarray(want32, np.float64)
+    assert np.array_equal(g[:, 29], w[:, 29]) and np.array_equal(g[:, 0:4], w[:, 0:4])
+    for sl, tol in ((slice(4, 7), 1e-6), (slice(12, 15), 1e-6), (slice(8, 11), 1e-5),
+                    (slice(16, 19), 1e-5), (slice(20, 23), 1e-5)):
+        assert np.max(np.abs(g[:, sl] - w[:, sl])) <= tol * np.max(np.abs(w[:, sl])), sl
+    assert np.array_equal(g[:, 24:29], w[:, 24:29])  # half widths and 1 / mass
+
+
+def test_pbd_frame_equals_the_shader(orc, x):
+    """One frame of uniform_grid_pbd_3D_cs.glsl as GridTestPbdGpu3D::Animate
+    runs it (UniformGridGpu3D.cpp:120-183, 338-346) on the demo's 4096
+    boxes: the float32 restatement finds the same contacts (the constraint
+    count of every box, the colours) and lands within the rounding of the
+    shader's float atomics."""
+    from coupledwateranimation_gb300._abi import PBD_BOX_DTYPE
+    from coupledwateranimation_gb300.pbd import pbd_defaults
+    got = orc.pbd_step(pbd_defaults(), np.ascontiguousarray(x["pbd_boxes"]).view(PBD_BOX_DTYPE).reshape(-1), 1)
+    got = np.ascontiguousarray(got).view(np.float32).reshape(-1, 32)
+    assert _sha(got[:, 29]) == str(G["pbd_counts_sha"]) and _sha(got[:, 0:4]) == str(G["pbd_colors_sha"])
+    assert got[:, 29].sum() > 20000  # a dense pile: tens of thousands of contacts
+    _pbd_close(got[G["pbd_sample"]], G["pbd_frame1_f32"])
