@@ -96,6 +96,16 @@ float orc_sample_f32(const float* u, int32_t w, int32_t h, float s, float t);
  * map (6 faces of sky_size^2 RGBA8, or NULL), out = width*height RGBA8. */
 void orc_render(const float* pos4, int32_t n, const float* wave, int32_t nx, int32_t nz, const cwa_camera* cam,
                 const cwa_render_params* prm, const uint8_t* sky, int32_t sky_size, uint8_t* out);
+/* One fragment of each fragment shader, with the inputs the shader reads:
+ * particle_fs.glsl pass 0 at pixel (px, py), r sprite widths from the
+ * centre, particle at world position pp (inv_p, inv_v: the row-major
+ * inverses of P and V; D: the w x h pass-2 depth image); wave_fs.glsl at
+ * world position p with wave sample v.  out: r, g, b, a before blending. */
+void orc_shade_particle(const float inv_p[16], const float inv_v[16], const float eye[3], const uint8_t* sky,
+                        int32_t sky_size, const float* D, int32_t w, int32_t h, int32_t px, int32_t py, float r,
+                        const float pp[3], float out[4]);
+void orc_shade_wave(const float eye[3], const uint8_t* sky, int32_t sky_size, const float p[3], float v,
+                    float out[4]);
 
 /* The 2D solver family (cwa2d_oracle.cpp): SphWave2D's initialisers, one
  * phase of the shallow-water step (float32 op by op), and the two SPH passes

@@ -311,6 +311,69 @@ V3 m3x(const float* m, V3 v, float w) {
             m[8] * v.x + m[9] * v.y + m[10] * v.z + m[11] * w);
 }
 
+// wave_fs.glsl main (:36-50) for a fragment at world position p whose wave
+// sample is v; the mesh normal is (0, 1, 0) (Surf.cpp:49-61 gives (0, -1, 0),
+// wave_vs.glsl:40 negates it).  Colour before blending.
+void shade_wave(const Frame& f, V3 p, float v, V3* rgb, float* a) {
+  const V3 light_col = v3(1.0f, 0.85f, 0.7f), eye = f.eye;
+  const V3 nrm = v3(0.0f, 1.0f, 0.0f);
+  const V3 I = normalize(sub(p, eye));
+  const V3 refl = cube(f, reflect(I, nrm)), refr = cube(f, refract(I, nrm, 1.0f / 1.33f));
+  const V3 ld = normalize(sub(v3(0.0f, 1.0f, 0.0f), p));
+  const float diff = fmaxf(dot(nrm, ld), 0.0f);
+  const V3 vd = normalize(sub(eye, p));
+  const float spec = powf(fmaxf(dot(vd, reflect(v3(-ld.x, -ld.y, -ld.z), nrm)), 0.0f), 32.0f);
+  const V3 lit = hmul(add(add(mul(0.8f, light_col), mul(diff, light_col)), mul(10.0f * spec, light_col)),
+                      v3(0.6f, 0.8f, 1.0f));
+  const V3 comb = add(mul(0.75f, add(refl, refr)), mul(0.1f, lit));
+  *rgb = v3(mixf(comb.x, 0.7f, v), mixf(comb.y, 0.9f, v), mixf(comb.z, 1.0f, v));
+  *a = mixf(0.2f, 0.0f, v);
+}
+
+// particle_fs.glsl pass 0 (:47-68) for the fragment at pixel (px, py), r
+// sprite widths from the sprite's centre, of the particle at world position
+// pp; depth_at reads the pass-2 depth image (0 off the image).  Colour
+// before blending.
+template <class DepthAt>
+void shade_particle(const Frame& f, int px, int py, float r, V3 pp, DepthAt depth_at, V3* rgb, float* a) {
+  const V3 light_col = v3(1.0f, 0.85f, 0.7f), eye = f.eye;
+  const float spec = powf(fmaxf(dot(normalize(pp), normalize(v3(1.0f, 1.0f, 0.0f))), 0.0f), 16.0f);
+  const float aa = expf(-12.0f * r) + 0.1f * expf(-2.0f * r);
+  const float dzdx = 0.5f * (depth_at(px + 1, py) - depth_at(px - 1, py));
+  const float dzdy = 0.5f * (depth_at(px, py + 1) - depth_at(px, py - 1));
+  const V3 nrm = normalize(v3(-dzdx, -dzdy, 1.0f));
+  const V3 I = normalize(sub(eye, pp));
+  const V3 refl = cube(f, reflect(I, nrm)), refr = cube(f, refract(I, nrm, 1.0f / 1.33f));
+  const float dz = depth_at(px, py);
+  const float cx = (px + 0.5f) * 2.0f - 1.0f, cy = (py + 0.5f) * 2.0f - 1.0f, cz = dz * 2.0f - 1.0f;
+  const float vw = f.inv_p[12] * cx + f.inv_p[13] * cy + f.inv_p[14] * cz + f.inv_p[15];
+  const V3 view = mul(1.0f / vw, m3x(f.inv_p, v3(cx, cy, cz), 1.0f));
+  const V3 pos = m3x(f.inv_v, view, 1.0f);
+  const V3 ld = normalize(sub(v3(1.0f, 1.0f, 0.0f), pos));
+  const float diff = fmaxf(dot(nrm, ld), 0.0f);
+  const V3 vd = normalize(sub(eye, pos));
+  const float spec2 = powf(fmaxf(dot(vd, reflect(v3(-ld.x, -ld.y, -ld.z), nrm)), 0.0f), 32.0f);
+  const V3 lit = hmul(add(add(mul(0.8f, light_col), mul(diff, light_col)), mul(0.9f * spec2, light_col)),
+                      v3(0.4f, 0.7f, 1.0f));
+  const V3 comb = add(mul(0.75f, add(refl, refr)), mul(0.1f, lit));
+  const float t = 2.0f * pp.y;
+  *rgb = v3(mixf(comb.x, 1.0f, t) + spec, mixf(comb.y, 1.0f, t) + spec, mixf(comb.z, 1.0f, t) + spec);
+  *a = mixf(0.1f, aa, t);
+}
+
+Frame shade_frame(const float inv_p[16], const float inv_v[16], const float eye[3], const uint8_t* sky,
+                  int32_t sky_size) {
+  Frame f{};
+  for (int k = 0; k < 16; ++k) {
+    f.inv_p[k] = inv_p[k];
+    f.inv_v[k] = inv_v[k];
+  }
+  f.eye = v3(eye[0], eye[1], eye[2]);
+  f.sky = sky;
+  f.sky_size = sky ? sky_size : 0;
+  return f;
+}
+
 }  // namespace
 
 void orc_render(const float* pos4, int32_t n, const float* wave, int32_t nx, int32_t nz, const cwa_camera* cam,
@@ -397,7 +460,6 @@ void orc_render(const float* pos4, int32_t n, const float* wave, int32_t nx, int
     if (win >= 0) D[p] = pw[win].cz;
   }
   auto depth_at = [&](int x, int y) { return (x < 0 || y < 0 || x >= W || y >= H) ? 0.0f : D[(size_t)y * W + x]; };
-  const V3 light_col = v3(1.0f, 0.85f, 0.7f);
   for (int py = 0; py < H; ++py)
     for (int px = 0; px < W; ++px) {
       float c[3] = {0.0f, 0.0f, 0.0f};
@@ -437,19 +499,7 @@ void orc_render(const float* pos4, int32_t n, const float* wave, int32_t nx, int
             tt += wgt * mv[s.o[k]].t;
             p = add(p, mul(wgt, mv[s.o[k]].pw));
           }
-          const float v = orc_sample_f32(wave, nx, nz, ts, tt);
-          const V3 nrm = v3(0.0f, 1.0f, 0.0f);
-          const V3 I = normalize(sub(p, eye));
-          const V3 refl = cube(f, reflect(I, nrm)), refr = cube(f, refract(I, nrm, 1.0f / 1.33f));
-          const V3 ld = normalize(sub(v3(0.0f, 1.0f, 0.0f), p));
-          const float diff = fmaxf(dot(nrm, ld), 0.0f);
-          const V3 vd = normalize(sub(eye, p));
-          const float spec = powf(fmaxf(dot(vd, reflect(v3(-ld.x, -ld.y, -ld.z), nrm)), 0.0f), 32.0f);
-          const V3 lit = hmul(add(add(mul(0.8f, light_col), mul(diff, light_col)), mul(10.0f * spec, light_col)),
-                              v3(0.6f, 0.8f, 1.0f));
-          const V3 comb = add(mul(0.75f, add(refl, refr)), mul(0.1f, lit));
-          rgb = v3(mixf(comb.x, 0.7f, v), mixf(comb.y, 0.9f, v), mixf(comb.z, 1.0f, v));
-          a = mixf(0.2f, 0.0f, v);
+          shade_wave(f, p, orc_sample_f32(wave, nx, nz, ts, tt), &rgb, &a);
         } else {  // particle_fs.glsl pass 0
           const int i = fr.prim - first_particle;
           const Win& w = pw[i];
@@ -458,28 +508,7 @@ void orc_render(const float* pos4, int32_t n, const float* wave, int32_t nx, int
           const float* q = pos4 + 4 * i;
           const V3 pp = v3(row4(f.m_p, q[0], q[1], q[2]), row4(f.m_p + 4, q[0], q[1], q[2]),
                            row4(f.m_p + 8, q[0], q[1], q[2]));
-          const float spec = powf(fmaxf(dot(normalize(pp), normalize(v3(1.0f, 1.0f, 0.0f))), 0.0f), 16.0f);
-          const float aa = expf(-12.0f * r) + 0.1f * expf(-2.0f * r);
-          const float dzdx = 0.5f * (depth_at(px + 1, py) - depth_at(px - 1, py));
-          const float dzdy = 0.5f * (depth_at(px, py + 1) - depth_at(px, py - 1));
-          const V3 nrm = normalize(v3(-dzdx, -dzdy, 1.0f));
-          const V3 I = normalize(sub(eye, pp));
-          const V3 refl = cube(f, reflect(I, nrm)), refr = cube(f, refract(I, nrm, 1.0f / 1.33f));
-          const float dz = depth_at(px, py);
-          const float cx = (px + 0.5f) * 2.0f - 1.0f, cy = (py + 0.5f) * 2.0f - 1.0f, cz = dz * 2.0f - 1.0f;
-          const float vw = f.inv_p[12] * cx + f.inv_p[13] * cy + f.inv_p[14] * cz + f.inv_p[15];
-          const V3 view = mul(1.0f / vw, m3x(f.inv_p, v3(cx, cy, cz), 1.0f));
-          const V3 pos = m3x(f.inv_v, view, 1.0f);
-          const V3 ld = normalize(sub(v3(1.0f, 1.0f, 0.0f), pos));
-          const float diff = fmaxf(dot(nrm, ld), 0.0f);
-          const V3 vd = normalize(sub(eye, pos));
-          const float spec2 = powf(fmaxf(dot(vd, reflect(v3(-ld.x, -ld.y, -ld.z), nrm)), 0.0f), 32.0f);
-          const V3 lit = hmul(add(add(mul(0.8f, light_col), mul(diff, light_col)), mul(0.9f * spec2, light_col)),
-                              v3(0.4f, 0.7f, 1.0f));
-          const V3 comb = add(mul(0.75f, add(refl, refr)), mul(0.1f, lit));
-          const float t = 2.0f * pp.y;
-          rgb = v3(mixf(comb.x, 1.0f, t) + spec, mixf(comb.y, 1.0f, t) + spec, mixf(comb.z, 1.0f, t) + spec);
-          a = mixf(0.1f, aa, t);
+          shade_particle(f, px, py, r, pp, depth_at, &rgb, &a);
         }
         a = a < 0.0f ? 0.0f : (a > 1.0f ? 1.0f : a);
         const float src[3] = {rgb.x, rgb.y, rgb.z};
@@ -494,4 +523,27 @@ void orc_render(const float* pos4, int32_t n, const float* wave, int32_t nx, int
       o[2] = (uint8_t)c[2];
       o[3] = 255;
     }
+}
+
+void orc_shade_particle(const float inv_p[16], const float inv_v[16], const float eye[3], const uint8_t* sky,
+                        int32_t sky_size, const float* D, int32_t w, int32_t h, int32_t px, int32_t py, float r,
+                        const float pp[3], float out[4]) {
+  const Frame f = shade_frame(inv_p, inv_v, eye, sky, sky_size);
+  auto depth_at = [&](int x, int y) { return (x < 0 || y < 0 || x >= w || y >= h) ? 0.0f : D[(size_t)y * w + x]; };
+  V3 rgb;
+  shade_particle(f, px, py, r, v3(pp[0], pp[1], pp[2]), depth_at, &rgb, &out[3]);
+  out[0] = rgb.x;
+  out[1] = rgb.y;
+  out[2] = rgb.z;
+}
+
+void orc_shade_wave(const float eye[3], const uint8_t* sky, int32_t sky_size, const float p[3], float v,
+                    float out[4]) {
+  const float id[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  const Frame f = shade_frame(id, id, eye, sky, sky_size);
+  V3 rgb;
+  shade_wave(f, v3(p[0], p[1], p[2]), v, &rgb, &out[3]);
+  out[0] = rgb.x;
+  out[1] = rgb.y;
+  out[2] = rgb.z;
 }

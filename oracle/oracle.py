@@ -59,6 +59,8 @@ def load() -> C.CDLL:
             "orc_wave_from_image_f32": (None, [C.c_int32, C.c_int32, _P, C.c_int32, C.c_int32, _P]),
             "orc_sample_f32": (C.c_float, [_P, _I, _I, C.c_float, C.c_float]),
             "orc_render": (None, [_P, _I, _P, _I, _I, _P, _P, _P, _I, _P]),
+            "orc_shade_particle": (None, [_P, _P, _P, _P, _I, _P, _I, _I, _I, _I, C.c_float, _P, _P]),
+            "orc_shade_wave": (None, [_P, _P, _I, _P, C.c_float, _P]),
             "orc2d_init_particles": (None, [_P, _P]),
             "orc2d_wave_init_f32": (None, [_P, _P, _P, _I]),
             "orc2d_wave_iter_f32": (None, [_P, _P, _P, _I]),
@@ -254,6 +256,26 @@ def render(pos4: np.ndarray, wave: np.ndarray, camera, params, sky: np.ndarray |
     sk = None if sky is None else np.ascontiguousarray(sky, np.uint8)
     load().orc_render(_p(p), p.shape[0], _p(u), u.shape[1], u.shape[0], C.cast(C.pointer(camera), C.c_void_p),
                       C.cast(C.pointer(params), C.c_void_p), _p(sk), 0 if sk is None else sk.shape[1], _p(out))
+    return out
+
+
+def shade_particle(inv_p, inv_v, eye, sky, sky_size, depth, px: int, py: int, r: float, pp) -> np.ndarray:
+    """particle_fs.glsl pass 0 for one fragment (rgba before blending)."""
+    f = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+    out = np.zeros(4, np.float32)
+    d = f(depth)
+    skyb = None if sky is None else np.ascontiguousarray(sky, np.uint8)
+    load().orc_shade_particle(_p(f(inv_p)), _p(f(inv_v)), _p(f(eye)), _p(skyb), sky_size, _p(d), d.shape[1],
+                              d.shape[0], px, py, r, _p(f(pp)), _p(out))
+    return out
+
+
+def shade_wave(eye, sky, sky_size, p, v: float) -> np.ndarray:
+    """wave_fs.glsl for one fragment (rgba before blending)."""
+    f = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+    out = np.zeros(4, np.float32)
+    skyb = None if sky is None else np.ascontiguousarray(sky, np.uint8)
+    load().orc_shade_wave(_p(f(eye)), _p(skyb), sky_size, _p(f(p)), v, _p(out))
     return out
 
 

@@ -86,6 +86,30 @@ def pbd(prec: int, boxes32: np.ndarray, frames: int, q: PbdParams) -> np.ndarray
     return a
 
 
+class RenderInputs(C.Structure):
+    """ref_render_inputs (oracle/ref_shaders/ref_shaders.h)."""
+    _fields_ = [("P", C.c_float * 16), ("V", C.c_float * 16), ("PV", C.c_float * 16), ("eye", C.c_float * 3),
+                ("sky", C.c_void_p), ("sky_size", C.c_int32), ("depth_image", C.c_void_p), ("w", C.c_int32),
+                ("h", C.c_int32)]
+
+
+def particle_fragment(inp: RenderInputs, pp, depth: float, px: float, py: float, point_coord):
+    """particle_fs.glsl pass 0 for one fragment: (rgba, discarded)."""
+    out = np.zeros(4, np.float32)
+    a = np.ascontiguousarray(pp, np.float32)
+    pc = np.ascontiguousarray(point_coord, np.float32)
+    d = load().ref_particle_fragment(C.byref(inp), _fp(a), depth, px, py, _fp(pc), _fp(out))
+    return out, bool(d)
+
+
+def wave_fragment(inp: RenderInputs, pw, nw, v: float) -> np.ndarray:
+    """wave_fs.glsl for one fragment."""
+    out = np.zeros(4, np.float32)
+    load().ref_wave_fragment(C.byref(inp), _fp(np.ascontiguousarray(pw, np.float32)),
+                             _fp(np.ascontiguousarray(nw, np.float32)), v, _fp(out))
+    return out
+
+
 def reference_root() -> Path | None:
     ref = Path(os.environ.get("CWA_REFERENCE", str(DEFAULT_REFERENCE)))
     return ref if (ref / "CoupledWaterAnimation" / "rho_pres_comp.glsl").is_file() else None
@@ -132,6 +156,11 @@ def load():
         lib.ref2d_field.restype = C.c_int32
         lib.ref_pbd.argtypes = [C.c_int32, dp, C.c_int32, C.c_int32, C.POINTER(PbdParams)]
         lib.ref_pbd.restype = C.c_int32
+        ri = C.POINTER(RenderInputs)
+        lib.ref_particle_fragment.argtypes = [ri, fp, C.c_float, C.c_float, C.c_float, fp, fp]
+        lib.ref_particle_fragment.restype = C.c_int32
+        lib.ref_wave_fragment.argtypes = [ri, fp, fp, C.c_float, fp]
+        lib.ref_wave_fragment.restype = C.c_int32
         _lib = lib
     return _lib
 
@@ -448,7 +477,74 @@ def fixture_inputs(splash_rgba8: np.ndarray) -> dict[str, np.ndarray]:
         **scan_inputs(),
         **sph2d_inputs(),
         **pbd_inputs(),
+        **render_inputs(),
     }
+
+
+def _persp(fovy: float, aspect: float, zn: float, zf: float) -> np.ndarray:
+    f = 1.0 / np.tan(fovy / 2)
+    return np.array([[f / aspect, 0, 0, 0], [0, f, 0, 0], [0, 0, (zf + zn) / (zn - zf), 2 * zf * zn / (zn - zf)],
+                     [0, 0, -1, 0]], np.float64)
+
+
+def _look_at(eye, center, up) -> np.ndarray:
+    fwd = center - eye
+    fwd = fwd / np.linalg.norm(fwd)
+    s = np.cross(fwd, up)
+    s = s / np.linalg.norm(s)
+    u = np.cross(s, fwd)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = s, u, -fwd
+    m[0, 3], m[1, 3], m[2, 3] = -s @ eye, -u @ eye, fwd @ eye
+    return m
+
+
+def render_inputs(n: int = 2000) -> dict[str, np.ndarray]:
+    """Fragment-shader inputs: a camera (P, V and their inverses, float32,
+    row-major), an 8^2 cube map of seeded RGBA8 texels, a 64 x 48 pass-2
+    depth image, and n fragments of each shader: window pixel, point
+    coordinate (about a fifth land outside the sprite and are discarded) and
+    particle position for particle_fs; world position and wave sample for
+    wave_fs."""
+    w, h = 64, 48
+    eye = np.array([0.3, 0.8, 1.6])
+    P = _persp(0.8, w / h, 0.1, 100.0).astype(np.float32)
+    V = _look_at(eye, np.array([0.25, 0.0, 0.25]), np.array([0.0, 1.0, 0.0])).astype(np.float32)
+    u = lambda seed, k, lo, hi: _u32(seed, k, lo, hi)  # noqa: E731
+    return {
+        "rfs_P": P, "rfs_V": V,
+        "rfs_PV": (P.astype(np.float64) @ V.astype(np.float64)).astype(np.float32),
+        "rfs_inv_p": np.linalg.inv(P.astype(np.float64)).astype(np.float32),
+        "rfs_inv_v": np.linalg.inv(V.astype(np.float64)).astype(np.float32),
+        "rfs_eye": eye.astype(np.float32),
+        "rfs_sky": (uniform01(801, 6 * 8 * 8 * 4) * 256).astype(np.uint8).reshape(6, 8, 8, 4),
+        "rfs_depth": u(802, w * h, 0.2, 0.9).reshape(h, w),
+        "rfs_px": (uniform01(803, n) * w).astype(np.int32),
+        "rfs_py": (uniform01(804, n) * h).astype(np.int32),
+        "rfs_pc": np.stack([u(805, n, 0.0, 1.0), u(806, n, 0.0, 1.0)], axis=1),
+        "rfs_pp": np.stack([u(807 + c, n, 0.0, 0.5) for c in range(3)], axis=1),
+        "rfs_pw": np.stack([u(811 + c, n, -0.5, 1.0) for c in range(3)], axis=1),
+        "rfs_v": u(814, n, -0.2, 1.0),
+    }
+
+
+def render_inputs_struct(x: dict[str, np.ndarray]) -> RenderInputs:
+    """The RenderInputs of render_inputs() (the arrays must stay alive)."""
+    inp = RenderInputs()
+    inp.P[:] = x["rfs_P"].T.ravel().tolist()  # GLSL matrices are column-major
+    inp.V[:] = x["rfs_V"].T.ravel().tolist()
+    inp.PV[:] = x["rfs_PV"].T.ravel().tolist()
+    inp.eye[:] = x["rfs_eye"].tolist()
+    inp.sky, inp.sky_size = x["rfs_sky"].ctypes.data, x["rfs_sky"].shape[1]
+    inp.depth_image = x["rfs_depth"].ctypes.data
+    inp.h, inp.w = x["rfs_depth"].shape
+    return inp
+
+
+def point_radius(pc: np.ndarray) -> np.ndarray:
+    """length(gl_PointCoord - vec2(0.5)) in float32, per fragment."""
+    d = pc.astype(np.float32) - np.float32(0.5)
+    return np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]).astype(np.float32)
 
 
 def pbd_inputs() -> dict[str, np.ndarray]:

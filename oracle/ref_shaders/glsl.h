@@ -40,6 +40,11 @@ struct Swz {
   Swz& operator+=(const V& v) { return *this = V(*this) + v; }
   Swz& operator-=(const V& v) { return *this = V(*this) - v; }
   Swz& operator*=(S s) { return *this = V(*this) * s; }
+  Swz& operator+=(S s) {
+    V v = V(*this);
+    v += s;
+    return *this = v;
+  }
 
  private:
   template <int... K>
@@ -61,6 +66,8 @@ template <class S> struct tvec4;
   T& operator*=(const T& o) { for (int k = 0; k < N; ++k) e[k] = e[k] * o.e[k]; return *this; } \
   T& operator/=(const T& o) { for (int k = 0; k < N; ++k) e[k] = e[k] / o.e[k]; return *this; } \
   T& operator*=(S s) { for (int k = 0; k < N; ++k) e[k] = e[k] * s; return *this; }            \
+  T& operator+=(S s) { for (int k = 0; k < N; ++k) e[k] = e[k] + s; return *this; }            \
+  T& operator-=(S s) { for (int k = 0; k < N; ++k) e[k] = e[k] - s; return *this; }            \
   T& operator/=(S s) { for (int k = 0; k < N; ++k) e[k] = e[k] / s; return *this; }            \
   friend T operator+(const T& a, const T& b) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] + b.e[k]; return r; } \
   friend T operator-(const T& a, const T& b) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] - b.e[k]; return r; } \
@@ -69,6 +76,10 @@ template <class S> struct tvec4;
   friend T operator*(const T& a, S s) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] * s; return r; }             \
   friend T operator*(S s, const T& a) { T r; for (int k = 0; k < N; ++k) r.e[k] = s * a.e[k]; return r; }             \
   friend T operator/(const T& a, S s) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] / s; return r; }             \
+  friend T operator+(const T& a, S s) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] + s; return r; }             \
+  friend T operator-(const T& a, S s) { T r; for (int k = 0; k < N; ++k) r.e[k] = a.e[k] - s; return r; }             \
+  friend T operator+(S s, const T& a) { T r; for (int k = 0; k < N; ++k) r.e[k] = s + a.e[k]; return r; }             \
+  friend T operator-(S s, const T& a) { T r; for (int k = 0; k < N; ++k) r.e[k] = s - a.e[k]; return r; }             \
   friend T operator-(const T& a) { T r; for (int k = 0; k < N; ++k) r.e[k] = -a.e[k]; return r; }
 
 template <class S>
@@ -82,6 +93,7 @@ struct tvec2 {
   explicit tvec2(S s) { e[0] = e[1] = s; }
   tvec2(S a, S b) { e[0] = a; e[1] = b; }
   tvec2(const tvec2& o) { e[0] = o.e[0]; e[1] = o.e[1]; }
+  explicit tvec2(const tvec4<S>& v);  // the first two components
   tvec2& operator=(const tvec2& o) { e[0] = o.e[0]; e[1] = o.e[1]; return *this; }
   GLSL_VEC_COMMON(tvec2, 2)
 };
@@ -99,6 +111,7 @@ struct tvec3 {
   explicit tvec3(S s) { e[0] = e[1] = e[2] = s; }
   tvec3(S a, S b, S c) { e[0] = a; e[1] = b; e[2] = c; }
   tvec3(const tvec3& o) { for (int k = 0; k < 3; ++k) e[k] = o.e[k]; }
+  explicit tvec3(const tvec4<S>& v);  // the first three components
   tvec3& operator=(const tvec3& o) { for (int k = 0; k < 3; ++k) e[k] = o.e[k]; return *this; }
   GLSL_VEC_COMMON(tvec3, 3)
 };
@@ -110,10 +123,12 @@ struct tvec4 {
     struct { S r, g, b, a; };
     S e[4];
     Swz<tvec3<S>, S, 4, 0, 1, 2> xyz;
+    Swz<tvec3<S>, S, 4, 0, 1, 2> rgb;
     Swz<tvec2<S>, S, 4, 0, 2> xz;
     Swz<tvec2<S>, S, 4, 0, 1> xy;
   };
   tvec4() { e[0] = e[1] = e[2] = e[3] = S(0); }
+  tvec4(const tvec3<S>& v, S d) { e[0] = v.e[0]; e[1] = v.e[1]; e[2] = v.e[2]; e[3] = d; }
   explicit tvec4(S s) { e[0] = e[1] = e[2] = e[3] = s; }
   tvec4(S a, S b, S c, S d) { e[0] = a; e[1] = b; e[2] = c; e[3] = d; }
   tvec4(const tvec2<S>& v, S c, S d) { e[0] = v.e[0]; e[1] = v.e[1]; e[2] = c; e[3] = d; }
@@ -125,10 +140,76 @@ struct tvec4 {
 #undef GLSL_VEC_COMMON
 
 template <class S>
+tvec2<S>::tvec2(const tvec4<S>& v) { e[0] = v.e[0]; e[1] = v.e[1]; }
+template <class S>
+tvec3<S>::tvec3(const tvec4<S>& v) { e[0] = v.e[0]; e[1] = v.e[1]; e[2] = v.e[2]; }
+
+// Column-major 4x4: m[c * 4 + r] is column c, row r (GLSL's layout).
+template <class S>
 struct tmat4 {
   S m[16];
   tmat4() { for (int k = 0; k < 16; ++k) m[k] = S(0); }
+  friend tvec4<S> operator*(const tmat4& a, const tvec4<S>& v) {
+    tvec4<S> r;
+    for (int row = 0; row < 4; ++row)
+      r.e[row] = a.m[row] * v.e[0] + a.m[4 + row] * v.e[1] + a.m[8 + row] * v.e[2] + a.m[12 + row] * v.e[3];
+    return r;
+  }
+  friend tmat4 operator*(const tmat4& a, const tmat4& b) {
+    tmat4 r;
+    for (int c = 0; c < 4; ++c)
+      for (int row = 0; row < 4; ++row) {
+        S acc = S(0);
+        for (int k = 0; k < 4; ++k) acc = acc + a.m[k * 4 + row] * b.m[c * 4 + k];
+        r.m[c * 4 + row] = acc;
+      }
+    return r;
+  }
 };
+
+// inverse (GLSL 4.50, 8.6): the adjugate over the determinant, by cofactor
+// expansion.
+template <class S>
+tmat4<S> inverse_of(const tmat4<S>& a) {
+  const S* m = a.m;
+  S inv[16];
+  inv[0] = m[5] * m[10] * m[15] - m[5] * m[11] * m[14] - m[9] * m[6] * m[15] + m[9] * m[7] * m[14] +
+           m[13] * m[6] * m[11] - m[13] * m[7] * m[10];
+  inv[4] = -m[4] * m[10] * m[15] + m[4] * m[11] * m[14] + m[8] * m[6] * m[15] - m[8] * m[7] * m[14] -
+           m[12] * m[6] * m[11] + m[12] * m[7] * m[10];
+  inv[8] = m[4] * m[9] * m[15] - m[4] * m[11] * m[13] - m[8] * m[5] * m[15] + m[8] * m[7] * m[13] +
+           m[12] * m[5] * m[11] - m[12] * m[7] * m[9];
+  inv[12] = -m[4] * m[9] * m[14] + m[4] * m[10] * m[13] + m[8] * m[5] * m[14] - m[8] * m[6] * m[13] -
+            m[12] * m[5] * m[10] + m[12] * m[6] * m[9];
+  inv[1] = -m[1] * m[10] * m[15] + m[1] * m[11] * m[14] + m[9] * m[2] * m[15] - m[9] * m[3] * m[14] -
+           m[13] * m[2] * m[11] + m[13] * m[3] * m[10];
+  inv[5] = m[0] * m[10] * m[15] - m[0] * m[11] * m[14] - m[8] * m[2] * m[15] + m[8] * m[3] * m[14] +
+           m[12] * m[2] * m[11] - m[12] * m[3] * m[10];
+  inv[9] = -m[0] * m[9] * m[15] + m[0] * m[11] * m[13] + m[8] * m[1] * m[15] - m[8] * m[3] * m[13] -
+           m[12] * m[1] * m[11] + m[12] * m[3] * m[9];
+  inv[13] = m[0] * m[9] * m[14] - m[0] * m[10] * m[13] - m[8] * m[1] * m[14] + m[8] * m[2] * m[13] +
+            m[12] * m[1] * m[10] - m[12] * m[2] * m[9];
+  inv[2] = m[1] * m[6] * m[15] - m[1] * m[7] * m[14] - m[5] * m[2] * m[15] + m[5] * m[3] * m[14] +
+           m[13] * m[2] * m[7] - m[13] * m[3] * m[6];
+  inv[6] = -m[0] * m[6] * m[15] + m[0] * m[7] * m[14] + m[4] * m[2] * m[15] - m[4] * m[3] * m[14] -
+           m[12] * m[2] * m[7] + m[12] * m[3] * m[6];
+  inv[10] = m[0] * m[5] * m[15] - m[0] * m[7] * m[13] - m[4] * m[1] * m[15] + m[4] * m[3] * m[13] +
+            m[12] * m[1] * m[7] - m[12] * m[3] * m[5];
+  inv[14] = -m[0] * m[5] * m[14] + m[0] * m[6] * m[13] + m[4] * m[1] * m[14] - m[4] * m[2] * m[13] -
+            m[12] * m[1] * m[6] + m[12] * m[2] * m[5];
+  inv[3] = -m[1] * m[6] * m[11] + m[1] * m[7] * m[10] + m[5] * m[2] * m[11] - m[5] * m[3] * m[10] -
+           m[9] * m[2] * m[7] + m[9] * m[3] * m[6];
+  inv[7] = m[0] * m[6] * m[11] - m[0] * m[7] * m[10] - m[4] * m[2] * m[11] + m[4] * m[3] * m[10] +
+           m[8] * m[2] * m[7] - m[8] * m[3] * m[6];
+  inv[11] = -m[0] * m[5] * m[11] + m[0] * m[7] * m[9] + m[4] * m[1] * m[11] - m[4] * m[3] * m[9] -
+            m[8] * m[1] * m[7] + m[8] * m[3] * m[5];
+  inv[15] = m[0] * m[5] * m[10] - m[0] * m[6] * m[9] - m[4] * m[1] * m[10] + m[4] * m[2] * m[9] +
+            m[8] * m[1] * m[6] - m[8] * m[2] * m[5];
+  const S det = m[0] * inv[0] + m[1] * inv[4] + m[2] * inv[8] + m[3] * inv[12];
+  tmat4<S> r;
+  for (int k = 0; k < 16; ++k) r.m[k] = inv[k] / det;
+  return r;
+}
 
 struct bvec2 {
   bool x, y;
@@ -167,6 +248,8 @@ struct ivec2 {
   explicit ivec2(const uvec2& u) { e[0] = (int)u.x; e[1] = (int)u.y; }
   explicit ivec2(const tvec2<float>& v) { e[0] = (int)v.e[0]; e[1] = (int)v.e[1]; }
   explicit ivec2(const tvec2<double>& v) { e[0] = (int)v.e[0]; e[1] = (int)v.e[1]; }
+  explicit ivec2(const tvec4<float>& v) { e[0] = (int)v.e[0]; e[1] = (int)v.e[1]; }
+  explicit ivec2(const tvec4<double>& v) { e[0] = (int)v.e[0]; e[1] = (int)v.e[1]; }
   ivec2(const ivec2& o) { e[0] = o.e[0]; e[1] = o.e[1]; }
   ivec2& operator=(const ivec2& o) { e[0] = o.e[0]; e[1] = o.e[1]; return *this; }
   int& operator[](int k) { return e[k]; }
@@ -286,6 +369,16 @@ struct sampler1D {
 
 inline int textureSize(const sampler1D& s, int) { return s.w; }
 
+// A bound cube map: 6 faces (+x, -x, +y, -y, +z, -z) of size x size RGBA8
+// texels, read as c / 255.
+struct samplerCube {
+  const uint8_t* faces = nullptr;
+  int size = 0;
+  float at(int face, int x, int y, int c) const {
+    return faces[(((size_t)face * size + y) * size + x) * 4 + c] / 255.0f;
+  }
+};
+
 // A bound image1D, rgba32f: w texels of 4 scalars, float or double.
 struct image1D {
   void* data = nullptr;
@@ -334,6 +427,35 @@ tvec4<S> filter_linear_1d(const sampler1D& t, S s) {
   const int x0 = cl(i0, t.w), x1 = cl(i0 + 1, t.w);
   tvec4<S> r;
   for (int c = 0; c < 4; ++c) r.e[c] = ((S)1 - a) * (S)t.at(x0, c) + a * (S)t.at(x1, c);
+  return r;
+}
+
+// GL 4.5 core, 8.13: the face of the major axis, (s, t) = ((sc / |ma|) + 1) / 2,
+// ((tc / |ma|) + 1) / 2 from table 8.19, then GL_LINEAR with the coordinates
+// clamped within the face (GL_TEXTURE_CUBE_MAP_SEAMLESS off).
+template <class S>
+tvec4<S> filter_cube(const samplerCube& t, S rx, S ry, S rz) {
+  tvec4<S> r;
+  if (!t.faces) return r;
+  const S ax = rx < 0 ? -rx : rx, ay = ry < 0 ? -ry : ry, az = rz < 0 ? -rz : rz;
+  int face;
+  S sc, tc, ma;
+  if (ax >= ay && ax >= az) {
+    face = rx >= 0 ? 0 : 1, sc = rx >= 0 ? -rz : rz, tc = -ry, ma = ax;
+  } else if (ay >= az) {
+    face = ry >= 0 ? 2 : 3, sc = rx, tc = ry >= 0 ? rz : -rz, ma = ay;
+  } else {
+    face = rz >= 0 ? 4 : 5, sc = rz >= 0 ? rx : -rx, tc = -ry, ma = az;
+  }
+  if (ma == 0) return r;
+  const S s = (S)0.5 * (sc / ma + (S)1), tt = (S)0.5 * (tc / ma + (S)1);
+  const S u = s * (S)t.size - (S)0.5, v = tt * (S)t.size - (S)0.5;
+  const S u0 = floor(u), v0 = floor(v), a = u - u0, b = v - v0;
+  auto cl = [&](long i) { return (int)(i < 0 ? 0 : (i > t.size - 1 ? t.size - 1 : i)); };
+  const int x0 = cl((long)u0), x1 = cl((long)u0 + 1), y0 = cl((long)v0), y1 = cl((long)v0 + 1);
+  for (int c = 0; c < 4; ++c)
+    r.e[c] = ((S)1 - a) * ((S)1 - b) * (S)t.at(face, x0, y0, c) + a * ((S)1 - b) * (S)t.at(face, x1, y0, c) +
+             ((S)1 - a) * b * (S)t.at(face, x0, y1, c) + a * b * (S)t.at(face, x1, y1, c);
   return r;
 }
 
@@ -436,6 +558,15 @@ void image_store(const image2D& im, const ivec2& p, const tvec4<S>& v) {
   inline S distance(const vec2& a, const vec2& b) { return length(a - b); }                   \
   inline vec3 normalize(const vec3& v) { return v / length(v); }                              \
   inline vec2 normalize(const vec2& v) { return v / length(v); }                              \
+  inline vec3 reflect(const vec3& i, const vec3& n) { return i - (S)2 * dot(n, i) * n; }      \
+  inline vec3 refract(const vec3& i, const vec3& n, S eta) {                                  \
+    const S d = dot(n, i), k = (S)1 - eta * eta * ((S)1 - d * d);                             \
+    if (k < (S)0) return vec3((S)0);                                                          \
+    return eta * i - (eta * d + sqrt(k)) * n;                                                 \
+  }                                                                                           \
+  inline vec4 mix(const vec4& x, const vec4& y, S a) { return x * ((S)1 - a) + y * a; }       \
+  inline vec4 texture(const samplerCube& t, const vec3& r) { return detail::filter_cube<S>(t, r.x, r.y, r.z); } \
+  inline mat4 inverse(const mat4& m) { return inverse_of(m); }                                \
   inline vec3 cross(const vec3& a, const vec3& b) {                                           \
     return vec3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);         \
   }                                                                                           \
@@ -506,6 +637,10 @@ GLSL_BUILTINS(double, f64)
   using glsl::NS::acos;                                                                   \
   using glsl::NS::fract;                                                                  \
   using glsl::NS::mix;                                                                    \
+  using glsl::NS::reflect;                                                                \
+  using glsl::NS::refract;                                                                \
+  using glsl::NS::inverse;                                                                \
+  using glsl::samplerCube;                                                                \
   using glsl::NS::sign;                                                                   \
   using glsl::NS::greaterThan;                                                            \
   using glsl::NS::lessThan;                                                               \

@@ -8,9 +8,11 @@ Only declarations are rewritten; every function body compiles as written:
   2. the work-group size declaration `layout(local_size_x = ...) in;` is
      dropped (the dispatch loop supplies gl_GlobalInvocationID);
   3. interface blocks `uniform NAME { ... };` and `buffer NAME { ... };`
-     become their members as globals (an instance-named block
-     `... } inst;` a struct NAME and its instance); a runtime-sized array
-     `T a[];` becomes a pointer `T* a;` that the dispatch binds;
+     become their members as globals (an instance-named block, also a
+     stage's `in` / `out` block, `... } inst;` becomes a struct NAME and its
+     instance); a runtime-sized array `T a[];` becomes a pointer `T* a;` that
+     the dispatch binds; a global stage input or output `in T x;` /
+     `out T x;` loses its qualifier;
   4. the remaining `layout(...)` qualifiers and the qualifiers `uniform`,
      `readonly`, `writeonly`, `restrict`, `coherent` are dropped (a
      uniform's initialiser, its default value, stays);
@@ -60,7 +62,7 @@ def _drop_local_size(src: str) -> str:
 
 
 def _blocks(src: str) -> str:
-    pat = re.compile(r"(?:layout\s*\([^)]*\)\s*)?\b(uniform|buffer)\s+(\w+)\s*\{(.*?)\}\s*(\w*)\s*;", re.S)
+    pat = re.compile(r"(?:layout\s*\([^)]*\)\s*)?\b(uniform|buffer|in|out)\s+(\w+)\s*\{(.*?)\}\s*(\w*)\s*;", re.S)
 
     def repl(m: re.Match) -> str:
         body = re.sub(r"(\w+)\s+(\w+)\s*\[\s*\]\s*;", r"\1* \2 = nullptr;", m.group(3))
@@ -85,6 +87,11 @@ def _strip_comments(src: str) -> str:
     # one left-to-right pass, so a line comment that holds "/*" or "*/"
     # (the "//*" block toggles) stays a line comment
     return re.sub(r"//[^\n]*|/\*.*?\*/", lambda m: "" if m.group(0).startswith("//") else " ", src, flags=re.S)
+
+
+def _io_qualifiers(src: str) -> str:
+    # a global `in T x;` / `out T x;` (stage inputs and outputs) loses the qualifier
+    return re.sub(r"(?m)^(\s*)(?:in|out)\s+(?=\w+\s+\w+\s*;)", r"\1", src)
 
 
 def _param_qualifiers(src: str) -> str:
@@ -144,6 +151,7 @@ def transform(src: str) -> str:
     src = _drop_local_size(src)
     src = _blocks(src)
     src = _qualifiers(src)
+    src = _io_qualifiers(src)
     src = _param_qualifiers(src)
     src = _float_literals(src)
     src, inits = _deferred_globals(src)

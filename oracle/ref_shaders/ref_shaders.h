@@ -84,6 +84,27 @@ typedef struct ref_pbd_params {
 // nx == nz and a power-of-two cell count.
 int32_t ref_pbd(int32_t prec, double* b32, int32_t n, int32_t frames, const ref_pbd_params* q);
 
+// The fragment shaders, one fragment at a time.  Matrices column-major (as
+// GLSL stores them); sky: 6 faces of sky_size^2 RGBA8 (+x, -x, +y, -y, +z,
+// -z); depth_image: the w x h pass-2 depth texture (its red channel).
+typedef struct ref_render_inputs {
+  float P[16], V[16], PV[16];
+  float eye[3];
+  const uint8_t* sky;
+  int32_t sky_size;
+  const float* depth_image;
+  int32_t w, h;
+} ref_render_inputs;
+
+// particle_fs.glsl pass 0 at window position (px, py) (gl_FragCoord.xy)
+// with gl_PointCoord point_coord: out = frag_color; returns 1 when the
+// fragment was discarded.
+int32_t ref_particle_fragment(const ref_render_inputs* in, const float pp[3], float depth, float px, float py,
+                              const float point_coord[2], float out[4]);
+// wave_fs.glsl with the interpolated world position pw, normal nw and wave
+// sample v: out = fragcolor.
+int32_t ref_wave_fragment(const ref_render_inputs* in, const float pw[3], const float nw[3], float v, float out[4]);
+
 #ifdef __cplusplus
 }
 

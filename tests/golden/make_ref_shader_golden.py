@@ -41,7 +41,10 @@ Cases (every input regenerates from oracle/ref.py; its SHA-256 is stored):
            grid, PreAnimate, the collision query, PostAnimate, as
            GridTestPbdGpu3D::Animate sequences them) on the demo's 4096
            boxes: the constraint counts and colours as SHA-256, every 8th
-           box's record.
+           box's record;
+  frag     particle_fs.glsl (pass 0) and wave_fs.glsl for 2000 fragments
+           each: a camera, a seeded cube map and depth image, fragments over
+           the window (about a fifth outside the sprite: discarded).
 
 Usage:  python tests/golden/make_ref_shader_golden.py
         (needs the reference checkout; CWA_REFERENCE names it if it is not
@@ -141,6 +144,21 @@ def pbd_cases(ref, x, out) -> None:
     out["pbd_frame1_f32"] = r[PBD_SAMPLE]
 
 
+def fragment_cases(ref, x, out) -> None:
+    """particle_fs.glsl pass 0 and wave_fs.glsl, one fragment at a time."""
+    inp = ref.render_inputs_struct(x)
+    n = len(x["rfs_px"])
+    part = np.zeros((n, 4), np.float32)
+    disc = np.zeros(n, bool)
+    for k in range(n):
+        part[k], disc[k] = ref.particle_fragment(inp, x["rfs_pp"][k], 0.5, x["rfs_px"][k] + 0.5,
+                                                 x["rfs_py"][k] + 0.5, x["rfs_pc"][k])
+    part[disc] = 0.0
+    up = np.array([0.0, 1.0, 0.0], np.float32)  # -normal_attrib: Surf.cpp's normals are (0, -1, 0)
+    wave = np.stack([ref.wave_fragment(inp, x["rfs_pw"][k], up, float(x["rfs_v"][k])) for k in range(n)])
+    out["rfs_particle"], out["rfs_discard"], out["rfs_wave"] = part, disc, wave
+
+
 def main() -> None:
     from oracle import ref
     if ref.build() is None or ref.load() is None:
@@ -189,6 +207,7 @@ def main() -> None:
         out[f"{name}_out"] = ref.exclusive_scan(x[name])
     sph2d_cases(ref, x, out)
     pbd_cases(ref, x, out)
+    fragment_cases(ref, x, out)
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
 

@@ -349,3 +349,25 @@ def test_pbd_frame_equals_the_shader(orc, x):
     assert _sha(got[:, 29]) == str(G["pbd_counts_sha"]) and _sha(got[:, 0:4]) == str(G["pbd_colors_sha"])
     assert got[:, 29].sum() > 20000  # a dense pile: tens of thousands of contacts
     _pbd_close(got[G["pbd_sample"]], G["pbd_frame1_f32"])
+
+
+# ---- the renderer's fragment shaders -----------------------------------------
+def test_fragment_shading_equals_the_shaders(orc, x):
+    """particle_fs.glsl pass 0 (:47-68 and its reflection / refraction /
+    lighting helpers) and wave_fs.glsl (:36-88) for 2000 fragments each,
+    against the render oracle's per-fragment shading (the arithmetic the
+    CUDA renderer follows): the same discards (gl_PointCoord outside the
+    sprite), colours and alpha within 1e-5 (float rounding; colours reach
+    ~2 before blending)."""
+    from oracle import ref
+    r = ref.point_radius(x["rfs_pc"])
+    assert np.array_equal(r >= 0.5, G["rfs_discard"])
+    assert 0.1 < G["rfs_discard"].mean() < 0.4
+    sky, size = x["rfs_sky"], x["rfs_sky"].shape[1]
+    for k in np.nonzero(~G["rfs_discard"])[0]:
+        got = orc.shade_particle(x["rfs_inv_p"], x["rfs_inv_v"], x["rfs_eye"], sky, size, x["rfs_depth"],
+                                 int(x["rfs_px"][k]), int(x["rfs_py"][k]), float(r[k]), x["rfs_pp"][k])
+        assert np.max(np.abs(got - G["rfs_particle"][k])) <= 1e-5, k
+    for k in range(len(x["rfs_v"])):
+        got = orc.shade_wave(x["rfs_eye"], sky, size, x["rfs_pw"][k], float(x["rfs_v"][k]))
+        assert np.max(np.abs(got - G["rfs_wave"][k])) <= 1e-5, k
