@@ -14,8 +14,9 @@ them without the reference checkout.
 
 oracle_regression.json — outputs of the CPU oracle on small fixed scenes
 (hashes of float32 bit patterns and int arrays).  These pin the oracle
-against accidental change; they are not reference outputs (the reference's
-GLSL cannot be executed anywhere here).
+against accidental change; they are not reference outputs (those are in
+ref_shader_outputs.npz, made by make_ref_shader_golden.py from the
+reference's shaders compiled for the CPU).
 
 Usage:  python tests/golden/make_golden.py [/path/to/reference]
 The reference checkout is needed only for the KAT file.
