@@ -623,7 +623,8 @@ def run_dry(args) -> None:
 def run_profile(args) -> None:
     """Plain eager steps of the workload for ncu captures: no timing, no L2
     flush, each kernel a separate launch (the launch order of one step is
-    hash, scan, list insert, reorder, rho_pres, force, integrate, wave)."""
+    the count scan's tile totals and tile scans, list insert, reorder,
+    rho_pres, force, integrate with the next step's hash and count, wave)."""
     from coupledwateranimation_gb300 import Sim, scenes
     wl = scenes.with_zsub(scenes.CONFIGS[args.config](), args.zsub)
     with Sim([s.desc for s in wl.scenes], precision=args.precision, use_graph=False) as sim:
