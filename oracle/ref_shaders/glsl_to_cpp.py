@@ -18,8 +18,9 @@ Only declarations are rewritten; every function body compiles as written:
      uniform's initialiser, its default value, stays);
   5. a parameter `inout T x` or `out T x` becomes `T& x`, `in T x` becomes
      `T x`;
-  6. an unsuffixed floating literal gets the suffix `f` (a GLSL literal
-     without `lf` is a float);
+  6. an unsuffixed floating literal (`1.5`, `.5`, `2.`, `1e5`, `2.5e-3`)
+     gets the suffix `f` (a GLSL literal without `lf` is a float); one with
+     `lf` loses the suffix (a C++ double);
   7. a global whose initializer is not a constant (it reads a uniform or
      calls a function other than a constructor or a pure math built-in; a
      constant reads only literals, macros and earlier constants), and every
@@ -100,8 +101,14 @@ def _param_qualifiers(src: str) -> str:
     return re.sub(r"(?<=[(,])(\s*)in\s+(\w+)\s+(\w+)", r"\1\2 \3", src)
 
 
+_FLOAT_LITERAL = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(lf|LF)?(?![\w.])")
+
+
 def _float_literals(src: str) -> str:
-    return re.sub(r"(?<![\w.])(\d+\.\d*|\.\d+)([eE][+-]?\d+)?(?![\w.])", r"\1\2f", src)
+    # GLSL's floating literals: digits with a point, an exponent, or both.
+    # Unsuffixed ones are float (suffix f); `lf` ones are double (no suffix
+    # in C++).  Suffixed float literals, integers and hex are left alone.
+    return _FLOAT_LITERAL.sub(lambda m: m.group(1) if m.group(2) else m.group(1) + "f", src)
 
 
 def _macro_names(src: str) -> set[str]:
