@@ -411,7 +411,7 @@ NbArgs nb_args(cwa_sim* s) {
   a.flag = s->verlet ? s->d_flag : nullptr;
   a.stage = s->opt.nb_stage >= 0 ? 1 : 0;
   a.scan_minb = s->opt.nb_scan_minb ? s->opt.nb_scan_minb : 4;
-  a.force_minb = s->opt.nb_force_minb ? s->opt.nb_force_minb : 8;
+  a.force_minb = s->opt.nb_force_minb ? s->opt.nb_force_minb : 9;
   a.order = s->d_porder;
   a.queue = s->opt.nb_queue ? s->d_queue : nullptr;
   return a;
@@ -770,8 +770,8 @@ cwa_status cwa_create(const cwa_sim_options* opt, const cwa_scene_desc* scenes, 
   if (o.precision < CWA_PREC_FP32 || o.precision > CWA_PREC_FP64) return arg_error("unknown precision");
   if (o.nb_stage < -1 || o.nb_stage > 1) return arg_error("nb_stage must be -1, 0 or 1");
   if (!(o.verlet_skin >= 0.0f && o.verlet_skin <= 1.0f)) return arg_error("verlet_skin must be in [0, 1]");
-  if (o.nb_scan_minb < 0 || o.nb_scan_minb > 8 || o.nb_force_minb < 0 || o.nb_force_minb > 8)
-    return arg_error("nb_scan_minb and nb_force_minb must be 0..8");
+  if (o.nb_scan_minb < 0 || o.nb_scan_minb > 8) return arg_error("nb_scan_minb must be 0..8");
+  if (o.nb_force_minb < 0 || o.nb_force_minb > 9) return arg_error("nb_force_minb must be 0..9");
   if (o.nb_threads != 0 && (o.nb_threads < 32 || o.nb_threads > 128 || (o.nb_threads & 31)))
     return arg_error("nb_threads must be 0 or a multiple of 32 in [32, 128]");
   if (o.wave_block < 0 || o.wave_block >= CWA_WAVE_BLOCK_COUNT) return arg_error("unknown wave_block variant");
@@ -1419,7 +1419,7 @@ cwa_status cwa_autotune(cwa_sim* s, int32_t trial_steps, cwa_tune_report* out) {
   cudaError_t err = copy_state(true);
   if (err == cudaSuccess) err = cudaEventCreate(&e0);
   if (err == cudaSuccess) err = cudaEventCreate(&e1);
-  const int stages[2] = {0, -1}, scans[3] = {4, 6, 8}, forces[2] = {6, 8}, ctas[2] = {128, 64};
+  const int stages[2] = {0, -1}, scans[3] = {4, 6, 8}, forces[2] = {8, 9}, ctas[2] = {128, 64};
   constexpr int kCombos = 2 * 3 * 2 * 2;
   // Two rounds, the second in reverse order; each combination keeps its
   // faster round, which damps clock and neighbour-load noise.
@@ -1471,7 +1471,7 @@ cwa_status cwa_autotune(cwa_sim* s, int32_t trial_steps, cwa_tune_report* out) {
         // the entry options, with 0 read as each knob's default
         if ((o.nb_stage < 0) == (entry.nb_stage < 0) &&
             o.nb_scan_minb == (entry.nb_scan_minb ? entry.nb_scan_minb : 4) &&
-            o.nb_force_minb == (entry.nb_force_minb ? entry.nb_force_minb : 8) &&
+            o.nb_force_minb == (entry.nb_force_minb ? entry.nb_force_minb : 9) &&
             o.nb_threads == (entry.nb_threads ? entry.nb_threads : 128))
           rep.entry_ms = ms;
         if (ms < rep.best_ms) {

@@ -858,9 +858,10 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
             const float4* __restrict__ xpair, const float4* __restrict__ vpair, int32_t* status,
             const int32_t* __restrict__ order, int32_t* queue, int32_t n_tiles) {
   // the particle's nonzero row masks and the index of each mask's bit 0
-  // (13.8 KB a CTA: eight CTAs fit the 132 KB shared carveout, which leaves
-  // the L1 more room for the gathers; 32-bit masks, 9.2 KB a CTA, measured
-  // slower: 209 against 143 us over the C1 run)
+  // (13.8 KB a CTA; 32-bit masks, 9.2 KB a CTA, measured slower: 209 against
+  // 143 us over the C1 run).  The default variant runs nine CTAs a SM at 56
+  // registers: 135.9 against 139.2 us at eight (64 registers), though nine
+  // stages leave the L1 a smaller share of the SM's 256 KB.
   __shared__ RowMask s_w[kNbRows][kNbThreads];
   __shared__ int32_t s_jb[kNbRows][kNbThreads];
   if constexpr (!WQ) {
@@ -945,6 +946,13 @@ void force_variant(const NbArgs& a, cudaStream_t st) {
 
 template <int P>
 void dispatch_force(const NbArgs& a, cudaStream_t st) {
+  // FP64 keeps eight CTAs a SM for nine: its 56-register form spills more
+  if constexpr (P != CWA_PREC_FP64) {
+    if (a.force_minb >= 9) {
+      force_variant<P, 9>(a, st);
+      return;
+    }
+  }
   if (a.force_minb >= 8)
     force_variant<P, 8>(a, st);
   else

@@ -125,7 +125,8 @@ typedef struct cwa_sim_options {
                               skin h / 2 (needs cell_size >= h (1 + skin)) */
   int32_t nb_scan_minb;    /* density-scan kernel variant: min CTAs per SM
                               (4, 6, 8; 0 = 4)                              */
-  int32_t nb_force_minb;   /* force kernel variant (6, 8; 0 = 8)              */
+  int32_t nb_force_minb;   /* force kernel variant: min CTAs per SM (6, 8, 9;
+                              0 = 9; FP64 runs 9 as 8)                      */
   int32_t wave_block;      /* blocked wave advance variant (CWA_WAVE_BLOCK_*)  */
   int32_t nb_queue;        /* 1: the density and force passes run as
                               persistent CTAs that take particle tiles from

@@ -544,8 +544,8 @@ def test_autotune_keeps_state_and_results(lib):
 @pytest.mark.parametrize("prec", [PREC_FP32, PREC_COMPENSATED])
 def test_neighbour_passes_invariant_to_staging_tiles_and_batching(lib, prec):
     """Every particle's neighbour sums run in an order fixed by the particle
-    alone, so staging on or off, 64- or 128-particle CTAs, the work-queue
-    form of the passes and the scene's place in a batch (here behind a scene
+    alone, so staging on or off, 64- or 128-particle CTAs, the launch-bound
+    variants, the work-queue form of the passes and the scene's place in a batch (here behind a scene
     of odd size) leave every bit unchanged."""
     sc = small_muller((14, 15, 13), 0.02, (48, 40), zsub=4, seed=31)
     odd = small_muller((5, 7, 9), 0.03, (32, 32), seed=32)  # 315 particles: the next scene starts at an odd index
@@ -558,6 +558,6 @@ def test_neighbour_passes_invariant_to_staging_tiles_and_batching(lib, prec):
             return records_f32(sim.download_particles(k))
     base = run([sc], 0)
     for kw in ({"nb_stage": -1}, {"nb_threads": 64}, {"nb_threads": 96, "nb_stage": -1}, {"nb_queue": 1},
-               {"nb_queue": 1, "nb_threads": 64, "nb_force_minb": 6}):
+               {"nb_queue": 1, "nb_threads": 64, "nb_force_minb": 6}, {"nb_force_minb": 8, "nb_scan_minb": 6}):
         assert np.array_equal(bits(run([sc], 0, **kw)), bits(base)), kw
     assert np.array_equal(bits(run([odd, sc], 1)), bits(base)), "batched behind an odd-sized scene"
