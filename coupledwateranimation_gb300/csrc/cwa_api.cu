@@ -119,6 +119,7 @@ namespace {
     cudaError_t e_ = (expr);                                                  \
     if (e_ != cudaSuccess) {                                                  \
       set_error(std::string(#expr) + ": " + cudaGetErrorString(e_));          \
+      cudaGetLastError(); /* a non-sticky error must not fail the next call */ \
       return e_ == cudaErrorMemoryAllocation ? CWA_ERR_OOM : CWA_ERR_CUDA;    \
     }                                                                         \
   } while (0)
@@ -285,22 +286,30 @@ cwa_status check_scene(cwa_sim* s, int32_t scene) {
 
 float4* cur_force(cwa_sim* s) { return s->move_force ? s->F[s->cur] : s->F[0]; }
 
-// Device address of a page-locked host buffer (cudaHostAlloc, or
-// cudaHostRegister'd), or nullptr for pageable memory or a buffer that is not
-// 16-byte aligned.  Kernels read and write such buffers directly over the
-// host link (NVLink-C2C on Grace), which moves contiguous data faster than
-// a copy-engine transfer does.
-void* host_alias(const void* host) {
-  if (!host || (reinterpret_cast<uintptr_t>(host) & 15u)) return nullptr;
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
-    cudaGetLastError();  // not a pointer CUDA knows: plain pageable memory
+// Device address of a page-locked host buffer of `bytes` bytes (cudaHostAlloc,
+// or cudaHostRegister'd), or nullptr for pageable memory, a buffer that is not
+// 16-byte aligned, or one whose last byte is not page-locked at the matching
+// device address (a buffer that runs past its registration).  Kernels read and
+// write such buffers directly over the host link (NVLink-C2C on Grace), which
+// moves contiguous data faster than a copy-engine transfer does.
+void* host_alias(const void* host, size_t bytes) {
+  if (!host || bytes == 0 || (reinterpret_cast<uintptr_t>(host) & 15u)) return nullptr;
+  auto mapped = [](const void* p, void** dev) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+      cudaGetLastError();  // not a pointer CUDA knows: plain pageable memory
+      return false;
+    }
+    *dev = a.devicePointer;
+    return a.type == cudaMemoryTypeHost && a.devicePointer != nullptr;
+  };
+  void* first = nullptr;
+  void* last = nullptr;
+  if (!mapped(host, &first) || (reinterpret_cast<uintptr_t>(first) & 15u)) return nullptr;
+  if (!mapped(static_cast<const char*>(host) + bytes - 1, &last) ||
+      static_cast<char*>(last) != static_cast<char*>(first) + bytes - 1)
     return nullptr;
-  }
-  if (a.type != cudaMemoryTypeHost || !a.devicePointer ||
-      (reinterpret_cast<uintptr_t>(a.devicePointer) & 15u))
-    return nullptr;
-  return a.devicePointer;
+  return first;
 }
 
 // One height field between the host and the device, on the sim's stream:
@@ -308,7 +317,8 @@ void* host_alias(const void* host) {
 // aligned, else cudaMemcpyAsync.
 cwa_status copy_field(cwa_sim* s, const float* src, float* dst, long cells, cudaMemcpyKind kind) {
   const bool to_dev = kind == cudaMemcpyHostToDevice;
-  void* alias = host_alias(to_dev ? static_cast<const void*>(src) : static_cast<const void*>(dst));
+  void* alias = host_alias(to_dev ? static_cast<const void*>(src) : static_cast<const void*>(dst),
+                           (size_t)cells * sizeof(float));
   const float* dev_side = to_dev ? dst : src;
   if (alias && !(reinterpret_cast<uintptr_t>(dev_side) & 15u)) {
     CWA_CUDA(launch_copy_f32(to_dev ? static_cast<const float*>(alias) : src,
@@ -942,7 +952,7 @@ cwa_status cwa_upload_particles(cwa_sim* s, int32_t scene, const cwa_particle* h
   if (n == 0) return CWA_OK;
   // page-locked records are read by the unpack kernel itself, over the host
   // link; pageable ones go through the staging buffer
-  const cwa_particle* src = static_cast<const cwa_particle*>(host_alias(host));
+  const cwa_particle* src = static_cast<const cwa_particle*>(host_alias(host, (size_t)n * sizeof(cwa_particle)));
   if (!src) {
     CWA_CUDA(cudaMemcpyAsync(s->staging, host, (size_t)n * sizeof(cwa_particle), cudaMemcpyHostToDevice,
                              s->stream));
@@ -971,7 +981,7 @@ cwa_status cwa_download_particles(cwa_sim* s, int32_t scene, cwa_particle* host,
   s->launches += 1;
   // the pack scatters the records back to upload order in device memory; a
   // page-locked destination then takes them in one coalesced kernel copy
-  if (void* dst = host_alias(host)) {
+  if (void* dst = host_alias(host, (size_t)n * sizeof(cwa_particle))) {
     CWA_CUDA(launch_copy_f32(reinterpret_cast<const float*>(s->staging), static_cast<float*>(dst),
                              (long)n * (long)(sizeof(cwa_particle) / sizeof(float)), s->stream));
     s->launches += 1;

@@ -62,6 +62,7 @@ cwa_status scratch_on_current_device(cudaStream_t stream, void** out) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) {
     set_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    cudaGetLastError();  // clear a non-sticky error for the next call
     return CWA_ERR_CUDA;
   }
   if (dev < 0 || dev >= kMaxDevices) {
@@ -72,6 +73,7 @@ cwa_status scratch_on_current_device(cudaStream_t stream, void** out) {
   e = cudaStreamIsCapturing(stream, &cap);
   if (e != cudaSuccess) {
     set_error(std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e));
+    cudaGetLastError();  // clear a non-sticky error for the next call
     return CWA_ERR_CUDA;
   }
   std::lock_guard<std::mutex> lock(g_scratch_mu);
@@ -80,6 +82,7 @@ cwa_status scratch_on_current_device(cudaStream_t stream, void** out) {
     e = cudaGetSymbolAddress(&p, g_scan_scratch);
     if (e != cudaSuccess || !p) {
       set_error(std::string("cudaGetSymbolAddress(scan scratch): ") + cudaGetErrorString(e));
+      cudaGetLastError();  // clear a non-sticky error for the next call
       return CWA_ERR_CUDA;
     }
     g_scratch_addr[dev] = p;
@@ -125,6 +128,7 @@ extern "C" cwa_status cwa_exclusive_scan_i32_noalloc(const int32_t* d_in, int32_
   if (e == cudaSuccess) e = scan_launch(d_in, d_out, n, n, false, ws, status, s, nullptr);
   if (e != cudaSuccess) {
     set_error(std::string("no-allocation scan: ") + cudaGetErrorString(e));
+    cudaGetLastError();  // clear a non-sticky error for the next call
     return CWA_ERR_CUDA;
   }
   return CWA_OK;
@@ -142,6 +146,7 @@ extern "C" cwa_status cwa_scan_noalloc_status(void* stream) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     set_error(std::string("no-allocation scan status: ") + cudaGetErrorString(e));
+    cudaGetLastError();  // clear a non-sticky error for the next call
     return CWA_ERR_CUDA;
   }
   return status_from_bits(v);

@@ -364,6 +364,7 @@ cwa_status perr(const std::string& m, cwa_status s = CWA_ERR_INVALID_ARG) {
     cudaError_t e_ = (expr);                                             \
     if (e_ != cudaSuccess) {                                             \
       cwa::set_error(std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+      cudaGetLastError(); /* clear a non-sticky error for the next call */ \
       return e_ == cudaErrorMemoryAllocation ? CWA_ERR_OOM : CWA_ERR_CUDA; \
     }                                                                    \
   } while (0)

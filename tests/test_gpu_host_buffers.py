@@ -150,3 +150,49 @@ def test_pinned_buffers_of_a_later_scene(lib):
     finally:
         for s in sims:
             s.close()
+
+
+def test_buffer_running_past_its_registration(lib):
+    """A host buffer whose first pages are page-locked (cudaHostRegister) and
+    whose tail is not.  The library checks both ends of the range before its
+    kernels touch host memory, so no kernel reads or writes past the
+    registration; the copy engine then refuses the mixed range (invalid
+    argument), which comes back as CWA_ERR_CUDA, and the sim stays usable:
+    the same records through pageable memory step exactly as in a sim that
+    never saw the error."""
+    torch = pytest.importorskip("torch")
+    import os
+    cudart = torch.cuda.cudart()
+    page = os.sysconf("SC_PAGE_SIZE")
+    sc = small_muller((24, 20, 24), 0.02, (64, 64), seed=41)
+    n = sc.desc.n_particles
+    rec = np.ascontiguousarray(sc.particles).view(np.uint8).reshape(-1)
+    raw = np.zeros(rec.size + 2 * page, np.uint8)
+    off = (-raw.ctypes.data) % page
+    view = raw[off:off + rec.size]
+    view[:] = rec
+    reg = (rec.size // 2) // page * page  # the first whole pages of the first half
+    assert reg > 0
+    assert int(cudart.cudaHostRegister(view.ctypes.data, reg, 0)) == 0
+    lib_ = _abi.load()
+    sims = [Sim(sc.desc), Sim(sc.desc)]
+    try:
+        for s in sims:
+            s.upload_particles(0, sc.particles)
+            s.upload_wave(0, sc.wave, sc.wave)
+        st = lib_.cwa_upload_particles(sims[1].handle, 0, C.c_void_p(view.ctypes.data), n)
+        assert st in (_abi.CWA_OK, _abi.CWA_ERR_CUDA)
+        if st != _abi.CWA_OK:
+            sims[1].upload_particles(0, sc.particles)  # the next call is not failed by the last error
+        st = lib_.cwa_download_particles(sims[1].handle, 0, C.c_void_p(view.ctypes.data), n)
+        assert st in (_abi.CWA_OK, _abi.CWA_ERR_CUDA)
+        if st == _abi.CWA_OK:
+            assert np.array_equal(view, rec)
+        for s in sims:
+            s.step(3)
+        assert np.array_equal(sims[1].download_particles(0).view(np.uint8),
+                              sims[0].download_particles(0).view(np.uint8))
+    finally:
+        for s in sims:
+            s.close()
+        assert int(cudart.cudaHostUnregister(view.ctypes.data)) == 0
