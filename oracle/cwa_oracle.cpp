@@ -1,6 +1,7 @@
 // cwa_oracle.cpp — CPU oracle of the coupled SPH + wave step.
 //
-// TEST INFRASTRUCTURE ONLY: the checker and the timed CPU baseline.  The
+// TEST INFRASTRUCTURE ONLY: what the tests compare against, and the timed
+// CPU baseline.  The
 // product never links or calls this file.  Every function cites the
 // reference shader or host code it restates (paths relative to the
 // reference project root).  Built with -ffp-contract=off so each float

@@ -1,6 +1,6 @@
 // cwa_render_oracle.cpp — CPU restatement of one headless frame of the
 // reference's display() (CoupledWaterAnimation/Main.cpp:326-474).  Test
-// infrastructure only: it is the checker for the renderer.
+// infrastructure only: the tests compare the renderer against it.
 //
 // It follows GL's pipeline directly.  Primitives (the strip mesh of
 // Surf.cpp:68-190 displaced by wave_vs.glsl:30-42, then the particle

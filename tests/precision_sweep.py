@@ -13,7 +13,7 @@ lattice at s = 0.004 with a 2048^2 wave) this measures, per precision mode:
   energy, their relative difference to the FP64 run, and the L1 distance of
   the density histogram to the FP64 run's.
 
-The oracle is the checker only.  Usage (GPU required):
+The oracle only provides the comparisons; it is not timed.  Usage (GPU required):
     python tests/precision_sweep.py [--config 2] [--steps 100] [--warm 20] [--zsub 4]
 Prints one JSON line per mode and a summary line.
 """
