@@ -1,9 +1,8 @@
 // cwa_oracle.cpp — CPU oracle of the coupled SPH + wave step.
 //
 // TEST INFRASTRUCTURE ONLY: what the tests compare against, and the timed
-// CPU baseline.  The
-// product never links or calls this file.  Every function cites the
-// reference shader or host code it restates (paths relative to the
+// CPU baseline.  The product never links or calls this file.  Every function
+// cites the reference shader or host code it restates (paths relative to the
 // reference project root).  Built with -ffp-contract=off so each float
 // operation of the *_f32 routines is rounded on its own, like the CUDA
 // kernels' __f*_rn intrinsics.
