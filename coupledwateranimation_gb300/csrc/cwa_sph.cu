@@ -861,23 +861,23 @@ __global__ void __launch_bounds__(kNbThreads, MINB)
   // (13.8 KB a CTA; 32-bit masks, 9.2 KB a CTA, measured slower: 209 against
   // 143 us over the C1 run).  The default variant runs nine CTAs a SM at 56
   // registers: 135.9 against 139.2 us at eight (64 registers), though nine
-  // stages leave the L1 a smaller share of the SM's 256 KB.
+  // CTAs' arrays leave the L1 a smaller share of the SM's 256 KB.
   __shared__ RowMask s_w[kNbRows][kNbThreads];
   __shared__ int32_t s_jb[kNbRows][kNbThreads];
   if constexpr (!WQ) {
     force_tile<P>(s_w, s_jb, tiles[blockIdx.x], pos, vel, rho_p, start, keys, scenes, wave, force, nbm, nbr_cnt,
                   n_total, xpair, vpair, status);
-    return;
-  }
-  // work-queue form: resident CTAs take tile numbers from *queue
-  __shared__ int32_t s_next[2];
-  for (int it = 0;; ++it) {
-    if (threadIdx.x == 0) s_next[it & 1] = atomicAdd(queue, 1);
-    __syncthreads();  // (two slots: thread 0 refills one while the other is still being read)
-    const int t = s_next[it & 1];
-    if (t >= n_tiles) break;
-    force_tile<P>(s_w, s_jb, tiles[__ldg(order + t)], pos, vel, rho_p, start, keys, scenes, wave, force, nbm,
-                  nbr_cnt, n_total, xpair, vpair, status);
+  } else {
+    // work-queue form: resident CTAs take tile numbers from *queue
+    __shared__ int32_t s_next[2];
+    for (int it = 0;; ++it) {
+      if (threadIdx.x == 0) s_next[it & 1] = atomicAdd(queue, 1);
+      __syncthreads();  // (two slots: thread 0 refills one while the other is still being read)
+      const int t = s_next[it & 1];
+      if (t >= n_tiles) break;
+      force_tile<P>(s_w, s_jb, tiles[__ldg(order + t)], pos, vel, rho_p, start, keys, scenes, wave, force, nbm,
+                    nbr_cnt, n_total, xpair, vpair, status);
+    }
   }
 }
 
