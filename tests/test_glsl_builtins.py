@@ -5,7 +5,8 @@ order the definitions write, in float for the float build and in double
 for the double build.  A wrong built-in would move every pin built on it,
 so each one the shaders use is compared bit for bit on seeded inputs,
 edges included (clamped texture coordinates, NaN operands of max/min,
-total internal reflection).  Needs g++, not the reference or a GPU."""
+total internal reflection, every cube-map face, out-of-range texelFetch and
+imageLoad).  Needs g++, not the reference or a GPU."""
 from __future__ import annotations
 
 import shutil
@@ -18,7 +19,7 @@ import pytest
 ROOT = Path(__file__).resolve().parents[1]
 SHADERS = ROOT / "oracle" / "ref_shaders"
 N = 2000
-TW, TH, T1 = 7, 5, 9  # 2D texture w x h, 1D texture w
+TW, TH, T1, CS = 7, 5, 9, 4  # 2D texture w x h, 1D texture w, cube face size
 
 HARNESS = r"""
 #include "glsl.h"
@@ -26,7 +27,7 @@ HARNESS = r"""
 #include <cstdlib>
 #include <vector>
 
-constexpr int kN = @N@, kTW = @TW@, kTH = @TH@, kT1 = @T1@;
+constexpr int kN = @N@, kTW = @TW@, kTH = @TH@, kT1 = @T1@, kCS = @CS@;
 
 template <class T> std::vector<T> slurp(const char* path, size_t n) {
   std::vector<T> v(n);
@@ -45,6 +46,11 @@ template <class T> std::vector<T> slurp(const char* path, size_t n) {
     auto tex1 = slurp<float>("tex1d.bin", (size_t)kT1 * 4);                                \
     glsl::sampler2D t2{tex.data(), kTW, kTH, 4};                                              \
     glsl::sampler1D t1{tex1.data(), kT1, 4};                                               \
+    auto cube = slurp<uint8_t>("cube.bin", (size_t)6 * kCS * kCS * 4);                      \
+    glsl::samplerCube tc{cube.data(), kCS};                                                 \
+    std::vector<S> img((size_t)kTW * kTH * 4);                                              \
+    for (size_t e = 0; e < img.size(); ++e) img[e] = (S)tex[e];                             \
+    glsl::image2D im{img.data(), kTW, kTH, sizeof(S) == sizeof(double)};                    \
     FILE* o = std::fopen(TAG ".bin", "wb");                                                 \
     auto put = [&](S v) { double d = (double)v; std::fwrite(&d, sizeof d, 1, o); };        \
     for (int k = 0; k < kN; ++k) {                                                         \
@@ -69,7 +75,11 @@ template <class T> std::vector<T> slurp(const char* path, size_t n) {
       const vec4 s2 = texture(t2, vec2((S)q[9], (S)q[10]));                                 \
       const vec4 s1 = texture(t1, (S)q[11]);                                                \
       const vec4 f2 = texelFetch(t2, glsl::ivec2((int)q[12] - 2, (int)q[13] - 2), 0);       \
-      for (int e = 0; e < 4; ++e) { put(s2.e[e]); put(s1.e[e]); put(f2.e[e]); }             \
+      const vec4 sc = texture(tc, u);                                                       \
+      const vec4 il = imageLoad(im, glsl::ivec2((int)q[12] - 2, (int)q[13] - 2));           \
+      for (int e = 0; e < 4; ++e) {                                                         \
+        put(s2.e[e]); put(s1.e[e]); put(f2.e[e]); put(sc.e[e]); put(il.e[e]);               \
+      }                                                                                     \
     }                                                                                       \
     std::fclose(o);                                                                         \
   }
@@ -83,7 +93,7 @@ int main() {
 
 OUTS = ["smoothstep", "mix", "fract", "sign", "clamp", "max", "min", "length",
         "nx", "ny", "nz", "rfx", "rfy", "rfz", "rrx", "rry", "rrz", "crx", "cry", "crz", "dot"] + \
-       [f"{kind}{e}" for e in range(4) for kind in ("tex2d", "tex1d", "fetch")]
+       [f"{kind}{e}" for e in range(4) for kind in ("tex2d", "tex1d", "fetch", "cube", "iload")]
 
 
 def _inputs():
@@ -103,10 +113,13 @@ def _inputs():
     q[:, 13] = np.floor(rng.uniform(0, TH + 4, N))
     tex2 = rng.uniform(0, 1, (TH, TW, 4)).astype(np.float32)
     tex1 = rng.uniform(0, 1, (T1, 4)).astype(np.float32)
-    return q, tex2, tex1
+    cube = rng.integers(0, 256, (6, CS, CS, 4), dtype=np.uint8)
+    q[20:26, 3:6] = [[1, 0.5, -0.25], [-1, 0.25, 0.5], [0.5, 1, 0.25], [0.25, -1, -0.5], [0.5, 0.25, 1],
+                     [-0.25, 0.5, -1]]  # one direction into each cube face
+    return q, tex2, tex1, cube
 
 
-def _spec(q, tex2, tex1, T):
+def _spec(q, tex2, tex1, cube, T):
     """The GLSL / GL definitions in numpy at scalar type T, one rounding per
     operation in the definitions' order."""
     one, zero, two, half = T(1), T(0), T(2), T(0.5)
@@ -170,8 +183,30 @@ def _spec(q, tex2, tex1, T):
         inside = (fx >= 0) & (fy >= 0) & (fx < TW) & (fy < TH)
         f2 = np.zeros((N, 4), T)
         f2[inside] = t2[fy[inside], fx[inside]]
+        # GL 4.5 core 8.13, table 8.19: the major axis picks the face, (s, t) = ((sc / |ma|) + 1) / 2,
+        # ((tc / |ma|) + 1) / 2, then GL_LINEAR inside the face, coordinates clamped to its edge
+        rx, ry, rz = u[:, 0], u[:, 1], u[:, 2]
+        ax, ay, az = np.abs(rx), np.abs(ry), np.abs(rz)
+        xm = (ax >= ay) & (ax >= az)
+        ym = ~xm & (ay >= az)
+        zm = ~xm & ~ym
+        face = np.where(xm, np.where(rx >= 0, 0, 1), np.where(ym, np.where(ry >= 0, 2, 3), np.where(rz >= 0, 4, 5)))
+        sc = np.where(xm, np.where(rx >= 0, -rz, rz), np.where(ym, rx, np.where(rz >= 0, rx, -rx)))
+        tc = np.where(xm, -ry, np.where(ym, np.where(ry >= 0, rz, -rz), -ry))
+        ma = np.where(xm, ax, np.where(ym, ay, az))
+        cs = half * (sc / ma + one)
+        ct = half * (tc / ma + one)
+        cx0, cx1, ca = axis(cs, CS)
+        cy0, cy1, cb = axis(ct, CS)
+        texel = (cube.astype(np.float32) / np.float32(255)).astype(T)
+        fsel = lambda yy, xx: texel[face, yy, xx]
+        sc4 = (((((one - ca) * (one - cb))[:, None] * fsel(cy0, cx0) + (ca * (one - cb))[:, None] * fsel(cy0, cx1))
+                + ((one - ca) * cb)[:, None] * fsel(cy1, cx0)) + (ca * cb)[:, None] * fsel(cy1, cx1))
+        il = np.zeros((N, 4), T)  # imageLoad: zero out of range (GLSL 4.50, 8.12)
+        il[inside] = t2[fy[inside], fx[inside]]
         for e in range(4):
             out[f"tex2d{e}"], out[f"tex1d{e}"], out[f"fetch{e}"] = s2[:, e], s1[:, e], f2[:, e]
+            out[f"cube{e}"], out[f"iload{e}"] = sc4[:, e], il[:, e]
     return out
 
 
@@ -180,11 +215,13 @@ def results(tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("needs g++")
     d = tmp_path_factory.mktemp("glsl_builtins")
-    q, tex2, tex1 = _inputs()
+    q, tex2, tex1, cube = _inputs()
     q.tofile(d / "in.bin")
+    cube.tofile(d / "cube.bin")
     tex2.tofile(d / "tex2d.bin")
     tex1.tofile(d / "tex1d.bin")
-    src = HARNESS.replace("@N@", str(N)).replace("@TW@", str(TW)).replace("@TH@", str(TH)).replace("@T1@", str(T1))
+    src = (HARNESS.replace("@N@", str(N)).replace("@TW@", str(TW)).replace("@TH@", str(TH))
+           .replace("@T1@", str(T1)).replace("@CS@", str(CS)))
     (d / "h.cpp").write_text(src)
     subprocess.run(["g++", "-std=c++20", "-O1", "-ffp-contract=off", "-fno-fast-math", f"-I{SHADERS}",
                     "-o", str(d / "h"), str(d / "h.cpp")],
@@ -194,19 +231,19 @@ def results(tmp_path_factory):
     for tag in ("f32", "f64"):
         raw = np.fromfile(d / f"{tag}.bin", np.float64).reshape(N, len(OUTS))
         got[tag] = {name: raw[:, i] for i, name in enumerate(OUTS)}
-    return q, tex2, tex1, got
+    return q, tex2, tex1, cube, got
 
 
 @pytest.mark.parametrize("tag,T", [("f32", np.float32), ("f64", np.float64)])
 @pytest.mark.parametrize("name", OUTS)
 def test_builtin_equals_its_definition(results, tag, T, name):
-    q, tex2, tex1, got = results
-    want = _spec(q, tex2, tex1, T)[name].astype(np.float64)
+    q, tex2, tex1, cube, got = results
+    want = _spec(q, tex2, tex1, cube, T)[name].astype(np.float64)
     np.testing.assert_array_equal(got[tag][name], want, err_msg=f"{name} ({tag})")
 
 
 def test_edge_cases_are_exercised(results):
-    q, tex2, tex1, got = results
+    q, tex2, tex1, cube, got = results
     g = got["f32"]
     assert np.isnan(g["max"][8]) and g["max"][9] == np.float32(q[9, 0])  # max(NaN, y) = NaN; max(x, NaN) = x
     assert np.isnan(g["min"][8]) and g["min"][9] == np.float32(q[9, 0])
